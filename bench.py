@@ -1,0 +1,433 @@
+#!/usr/bin/env python
+"""Benchmark of the DOLFINx assembly + CG hot path on GB300.
+
+Workload (one "step"): FP64 Poisson, Lagrange P2 on the unit cube split
+into 64^3 hexahedra x 6 tetrahedra (1,572,864 cells, 2,146,689 dofs),
+per-cell kappa ~ lognormal(0, 1) and f ~ U[-1, 1] per P1 node from one
+seed, u = 0 on x = 0 and x = 1. A step assembles the CSR matrix (values
+zeroed, cell loop, diagonal of constrained rows), the right-hand side
+(assemble_vector + apply_lifting + set_bc) and solves with
+Jacobi-preconditioned CG to rtol 1e-10. Mesh, sparsity pattern and
+cell->slot map are built once, outside the timed region, as a serving
+loop keeps them resident.
+
+Metric: GDoF/s of assembly + solve = dofs / step time. The matrix (487 MB
+of values) is larger than L2, so no flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "GDoF/s assembly+CG (P2 Poisson, Jacobi-PCG rtol 1e-10)"
+UNIT = "GDoF/s"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    p.add_argument("--n", type=int, default=64, help="hexahedra per direction")
+    p.add_argument("--mode", default="atomic", choices=["atomic", "coloured"])
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--cpu-sample-cells", type=int, default=120000)
+    return p.parse_args()
+
+
+def workload_config(args, n_dofs=None, nnz=None):
+    n = args.n
+    cfg = {"workload": f"P2 Poisson unit cube {n}^3x6 tets, lognormal kappa, Jacobi-PCG rtol 1e-10",
+           "cells": 6 * n ** 3, "degree": 2, "rtol": 1e-10, "seed": 0,
+           "l2": "matrix values (nnz*8 B) exceed the 129 MB L2; no flush between steps",
+           "assembly_mode": args.mode, "parallelism": "replicas" if args.gpus > 1 else "single"}
+    if n_dofs is not None:
+        cfg["dofs"] = int(n_dofs)
+    if nnz is not None:
+        cfg["nnz"] = int(nnz)
+    return cfg
+
+
+# --------------------------------------------------------------------------- problem
+def make_inputs(n, seed=0):
+    import numpy as np
+
+    from dolfinx_gb300 import mesh
+
+    m = mesh.create_unit_cube(n, n, n)
+    rng = np.random.default_rng(seed)
+    kappa = np.exp(rng.normal(0.0, 1.0, m.num_cells))
+    f = rng.uniform(-1.0, 1.0, m.num_nodes)
+    return m, kappa, f
+
+
+class Problem:
+    """Device-resident c2 problem with reusable assemblers and solver."""
+
+    def __init__(self, m, kappa, f, mode="atomic"):
+        import numpy as np
+        import torch
+
+        from dolfinx_gb300 import fem, la
+
+        self.m = m
+        self.V = fem.functionspace(m, ("Lagrange", 2))
+        X = self.V.tabulate_dof_coordinates()
+        bnd = np.flatnonzero(np.isclose(X[:, 0], 0.0) | np.isclose(X[:, 0], 1.0)).astype(np.int32)
+        self.bc = fem.dirichletbc(0.0, bnd, self.V)
+        self.kappa = torch.from_numpy(kappa).cuda()
+        self.f = torch.from_numpy(f).cuda()
+        self.a = fem.poisson_form(self.V, self.kappa)
+        self.L = fem.source_form(self.V, self.f)
+        self.masm = fem.MatrixAssembler(self.a, [self.bc], mode=mode)
+        self.rhs = fem.RhsAssembler(self.L, self.a, [self.bc], mode=mode)
+        self.A = self.masm.A
+        self.b = torch.zeros(self.V.num_dofs, dtype=torch.float64, device="cuda")
+        self.x = torch.zeros_like(self.b)
+        self.masm.assemble()
+        self.solver = la.CGSolver(self.A, jacobi=True)
+        self.last = None
+
+    def step(self):
+        self.masm.assemble(zero=True)
+        self.rhs.assemble(self.b)
+        self.solver.refresh_preconditioner()
+        self.x.zero_()
+        self.last = self.solver.solve(self.b, self.x, rtol=1e-10)
+        return self.last
+
+
+# --------------------------------------------------------------------------- timing helpers
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}",
+                                          f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.fh,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self):
+        import statistics
+
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax),
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profile_traffic(name):
+    """Per-launch DRAM bytes of a kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return d.get(name)
+    return None
+
+
+# --------------------------------------------------------------------------- CPU baseline
+def cpu_baseline(m, kappa, f, P, iters, sample_cells):
+    """Oracle (CPU restatement of the reference loops) timed on a bounded
+    sample: the matrix cell loop over `sample_cells` cells, the vector cell
+    loop over the same cells, and 3 CSR SpMV passes, extrapolated to one
+    full step with the GPU run's CG iteration count."""
+    import numpy as np
+
+    from oracle import oracle as O
+
+    O.build(with_ref=False)
+    V = P.V
+    rp = P.A.row_ptr.cpu().numpy()
+    cols = P.A.cols.cpu().numpy()
+    vals = np.zeros(cols.size)
+    nc = m.num_cells
+    s = min(sample_cells, nc)
+    cells = np.ascontiguousarray(m.cells[:s])
+    dm = np.ascontiguousarray(V.dofmap[:s])
+    t0 = time.perf_counter()
+    O.assemble_matrix(0, 2, cells, m.x, dm, rp, cols, kappa=kappa[:s], vals=vals)
+    t_mat = (time.perf_counter() - t0) * nc / s
+    t0 = time.perf_counter()
+    O.assemble_vector(0, 2, cells, m.x, dm, V.num_nodes, f=f)
+    t_vec = (time.perf_counter() - t0) * nc / s
+    A = P.A.vals.cpu().numpy()
+    xv = np.random.default_rng(0).standard_normal(V.num_nodes)
+    t0 = time.perf_counter()
+    for _ in range(3):
+        O.spmv(rp, cols, A, xv)
+    t_spmv = (time.perf_counter() - t0) / 3
+    n = V.num_nodes
+    t0 = time.perf_counter()
+    for _ in range(3):  # the 5 BLAS-1 passes of a PCG iteration
+        y = xv * 1.0001 + xv
+        float(np.dot(y, xv))
+        float(np.dot(xv, xv))
+        y *= 0.5
+    t_blas = (time.perf_counter() - t0) / 3
+    t_step = t_mat + t_vec + iters * (t_spmv + t_blas)
+    return {"value": n / t_step / 1e9, "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": f"oracle matrix+vector cell loops over {s} of {nc} cells and 3 CSR SpMV "
+                      f"passes of {rp[-1]} nnz, extrapolated to a full step with {iters} CG "
+                      f"iterations",
+            "seconds_per_step": t_step}
+
+
+# --------------------------------------------------------------------------- reference arm
+def _ref_worker(args_tuple):
+    n, sample_cells, iters_hint = args_tuple
+    import numpy as np
+
+    sys.path.insert(0, ROOT)
+    from oracle import oracle as O
+
+    O.build(with_ref=False)
+    cells, x = O.create_box_tet(n, n, n)
+    dm, nn = O.dofmap_tet(cells, 2)
+    nc = cells.shape[0]
+    rng = np.random.default_rng(0)
+    kappa = np.exp(rng.normal(0.0, 1.0, nc))
+    f = rng.uniform(-1.0, 1.0, x.shape[0])
+    s = min(sample_cells, nc)
+    # Sparsity of the sample cells only (bounded CPU work).
+    rp, cols = O.sparsity(nn, np.ascontiguousarray(dm[:s]))
+    vals = np.zeros(cols.size)
+    t0 = time.perf_counter()
+    O.assemble_matrix(0, 2, np.ascontiguousarray(cells[:s]), x, np.ascontiguousarray(dm[:s]), rp,
+                      cols, kappa=kappa[:s], vals=vals)
+    O.assemble_vector(0, 2, np.ascontiguousarray(cells[:s]), x, np.ascontiguousarray(dm[:s]), nn,
+                      f=f)
+    t_cells = (time.perf_counter() - t0) * nc / s
+    # SpMV cost per nnz from the sample matrix, scaled to the full nnz
+    # (28.35 nnz per row for P2 tets).
+    xv = rng.standard_normal(nn)
+    t0 = time.perf_counter()
+    for _ in range(3):
+        O.spmv(rp, cols, vals, xv)
+    t_spmv = (time.perf_counter() - t0) / 3 * (28.35 * nn) / max(cols.size, 1)
+    return nn, t_cells, t_spmv
+
+
+def run_reference(args):
+    """The reference's CPU path (the oracle restatement of its loops; the
+    reference itself needs MPI/Basix/FFCx and does not build here), as N
+    single-thread replicas, one per host core, on bounded samples."""
+    import multiprocessing as mp
+
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    cores = os.cpu_count() or 1
+    iters = 1500  # CG iterations of this system at rtol 1e-10 (measured on the GPU arm)
+    ctx = mp.get_context("spawn")
+    sample = max(2000, args.cpu_sample_cells // 8)
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        res = pool.map(_ref_worker, [(args.n, sample, iters)] * cores)
+    wall = time.perf_counter() - t0
+    nn = res[0][0]
+    per = [nn / (tc + iters * ts * 1.15) for _, tc, ts in res]
+    value = sum(per) / 1e9
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded)", "config": workload_config(args, nn),
+            "ms_per_step": 1e3 * nn / (value * 1e9) if value else None,
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": f"{cores} single-thread replicas; each times the oracle's "
+                                       f"matrix+vector cell loops over {sample} cells and 3 "
+                                       f"SpMV passes, extrapolated to a full step with {iters} "
+                                       f"CG iterations (BLAS-1 as 15% of SpMV)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+            "wall_s": wall}
+    print(json.dumps(line))
+
+
+# --------------------------------------------------------------------------- our arm
+def run_ours(args):
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    m, kappa, f = make_inputs(args.n, seed=rank)
+    P = Problem(m, kappa, f, mode=args.mode)
+    n_dofs = P.V.num_dofs
+    stream = torch.cuda.current_stream()
+
+    for _ in range(args.warmup):
+        P.step()
+    torch.cuda.synchronize()
+
+    # ---- device-resident timed region
+    launches = 0
+    iters = []
+    with Clocks(local) as clk:
+        barrier()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            r = P.step()
+            iters.append(r.iterations)
+            k = P.solver.graph_iters
+            launches += 5 + 2 + 3 * k * ((r.iterations + k - 1) // k)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier()
+    ms = e0.elapsed_time(e1) / args.steps
+    clocks = clk.summary()
+    t = torch.tensor([ms], device="cuda")
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    ms_max = float(t.item())
+    value = world * n_dofs / (ms_max * 1e-3) / 1e9
+
+    # ---- end to end through the public API with host buffers
+    kap_h = torch.from_numpy(kappa).pin_memory()
+    f_h = torch.from_numpy(f).pin_memory()
+    x_h = torch.empty(n_dofs, dtype=torch.float64).pin_memory()
+    barrier()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        P.kappa.copy_(kap_h, non_blocking=True)
+        P.f.copy_(f_h, non_blocking=True)
+        P.step()
+        x_h.copy_(P.x, non_blocking=True)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    ms_e2e = e0.elapsed_time(e1) / args.steps
+    t = torch.tensor([ms_e2e], device="cuda")
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    e2e_value = world * n_dofs / (float(t.item()) * 1e-3) / 1e9
+
+    # ---- roofline of the dominant kernel: the CG SpMV (CSR FP64)
+    A = P.A
+    y = torch.empty_like(P.x)
+    xin = P.x.clone()
+    for _ in range(3):
+        A.matvec(xin, y)
+    reps = 20
+    e0.record(stream)
+    for _ in range(reps):
+        A.matvec(xin, y)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    spmv_ms = e0.elapsed_time(e1) / reps
+    nnz, nrows = A.nnz, A.nrows
+    alg_bytes = nnz * (8 + 4) + (nrows + 1) * 8 + 2 * nrows * 8
+    peak, peak_kind = measured_peaks()
+    achieved = alg_bytes / (spmv_ms * 1e-3) / 1e9
+    traffic = profile_traffic("spmv_csr_f64_c2")
+
+    # ---- CPU baseline (rank 0, N = 1 only)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(m, kappa, f, P, int(np.median(iters)), args.cpu_sample_cells)
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded lognormal kappa, uniform f)",
+                "config": workload_config(args, n_dofs, A.nnz),
+                "cg_iterations": iters,
+                "e2e": {"value": e2e_value, "unit": UNIT,
+                        "h2d_bytes_per_step": int(kappa.nbytes + f.nbytes),
+                        "d2h_bytes_per_step": int(n_dofs * 8)},
+                "roofline": {"bound": "hbm", "kernel": "k_spmv_csr<16,f64> (CG operator)",
+                             "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "peak_source": peak_kind,
+                             "alg_bytes_per_launch": alg_bytes, "launch_ms": spmv_ms,
+                             "traffic": traffic},
+                "gpu_launches": launches,
+                "clocks": clocks,
+                "cpu_baseline": cpu}
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

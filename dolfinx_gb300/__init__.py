@@ -1,0 +1,20 @@
+"""dolfinx_gb300: DOLFINx's assembly + CG hot path on one GB300 (sm_103a).
+
+Host set-up (mesh, dofmaps, sparsity) and every device kernel live in the
+in-tree shared library ``_lib/libdfxgpu.so`` behind the C ABI of
+``include/dfx_gpu.h``; this package is the Python mirror of the
+reference's ``dolfinx.mesh`` / ``dolfinx.fem`` / ``dolfinx.la`` calls.
+Torch supplies device memory and streams only.
+"""
+
+from . import _capi  # noqa: F401
+
+__all__ = ["mesh", "fem", "la"]
+
+
+def __getattr__(name):
+    if name in __all__:
+        import importlib
+
+        return importlib.import_module(f"{__name__}.{name}")
+    raise AttributeError(name)

@@ -1,0 +1,716 @@
+// Cell assembly kernels: fem::assemble_matrix / assemble_vector /
+// apply_lifting / DirichletBC::set / set_diagonal on sm_103a.
+//
+// Design (per block of CPB cells, RCM cell order keeps neighbouring
+// cells' rows close together in L2):
+//   stage 0  dofs, row starts and BC markers of the cells -> shared memory
+//   stage 1  element tensor in FP64 (geometry + exact reference tensors,
+//            minimal FP64 operation count) -> shared memory (upper
+//            triangle, the tensors are symmetric)
+//   stage 2  one thread per element entry: BC zeroing, CSR slot from the
+//            cell->slot map, scatter. Consecutive threads write
+//            consecutive columns of one row, so atomics and map reads
+//            coalesce by sector.
+// Modes: FP64 atomics (one launch), or colour classes with plain
+// read-modify-write (deterministic summation order).
+#include "common.cuh"
+#include "element_tables.h"
+
+#include <vector>
+
+namespace
+{
+constexpr int kThreads = 128;
+
+__device__ __forceinline__ void load_cell_coords(const dfx_form& a, int64_t c, double* xc)
+{
+  const int4 xd = __ldg(reinterpret_cast<const int4*>(a.x_dofmap) + c);
+  const int nodes[4] = {xd.x, xd.y, xd.z, xd.w};
+#pragma unroll
+  for (int v = 0; v < 4; ++v)
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+      xc[3 * v + k] = __ldg(a.x + 3 * (int64_t)nodes[v] + k);
+}
+
+// adj(J) (= det J * J^{-1}) and det J of the affine map of a tetrahedron,
+// J_ij = dx_i/dX_j with columns x1-x0, x2-x0, x3-x0.
+__device__ __forceinline__ double tet_adjugate(const double* xc, double adj[3][3])
+{
+  double J[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      J[i][j] = xc[3 * (j + 1) + i] - xc[i];
+  adj[0][0] = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+  adj[0][1] = J[0][2] * J[2][1] - J[0][1] * J[2][2];
+  adj[0][2] = J[0][1] * J[1][2] - J[0][2] * J[1][1];
+  adj[1][0] = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+  adj[1][1] = J[0][0] * J[2][2] - J[0][2] * J[2][0];
+  adj[1][2] = J[0][2] * J[1][0] - J[0][0] * J[1][2];
+  adj[2][0] = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+  adj[2][1] = J[0][1] * J[2][0] - J[0][0] * J[2][1];
+  adj[2][2] = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+  return J[0][0] * adj[0][0] + J[0][1] * adj[1][0] + J[0][2] * adj[2][0];
+}
+
+// G_ab = kappa |det J| (K K^T)_ab = kappa (adj adj^T)_ab / |det J|, in the
+// order 00, 11, 22, 01, 02, 12. Returns |det J|.
+__device__ __forceinline__ double tet_metric(const double* xc, double kappa, double* G)
+{
+  double adj[3][3];
+  const double adet = fabs(tet_adjugate(xc, adj));
+  const double s = kappa / adet;
+  auto dot = [&](int a, int b)
+  { return adj[a][0] * adj[b][0] + adj[a][1] * adj[b][1] + adj[a][2] * adj[b][2]; };
+  G[0] = s * dot(0, 0);
+  G[1] = s * dot(1, 1);
+  G[2] = s * dot(2, 2);
+  G[3] = s * dot(0, 1);
+  G[4] = s * dot(0, 2);
+  G[5] = s * dot(1, 2);
+  return adet;
+}
+
+__device__ __forceinline__ double tet_absdet(const double* xc)
+{
+  double J[3][3];
+#pragma unroll
+  for (int i = 0; i < 3; ++i)
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+      J[i][j] = xc[3 * (j + 1) + i] - xc[i];
+  return fabs(J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1])
+              - J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0])
+              + J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]));
+}
+
+__host__ __device__ constexpr int packed(int i, int j, int n)
+{
+  return i * n - i * (i - 1) / 2 + (j - i);
+}
+
+// Position of `col` in the sorted row [b, e) of cols, or -1.
+__device__ __forceinline__ int64_t row_search(const int32_t* __restrict__ cols, int64_t b,
+                                              int64_t e, int32_t col)
+{
+  while (b < e)
+  {
+    const int64_t m = (b + e) >> 1;
+    const int32_t v = __ldg(cols + m);
+    if (v < col)
+      b = m + 1;
+    else
+      e = m;
+  }
+  return (e < 0) ? -1 : e;
+}
+
+template <bool COLOURED>
+__device__ __forceinline__ void scatter_add(double* p, double v)
+{
+  if constexpr (COLOURED)
+    *p += v;
+  else
+    atomicAdd(p, v);
+}
+
+// Form traits: scalar P1/P2 Poisson(+mass) or vector P2 elasticity.
+template <int DEG, bool ELAST>
+struct Traits
+{
+  static constexpr int ND = DEG == 1 ? 4 : 10; // nodes per cell
+  static constexpr int BS = ELAST ? 3 : 1;
+  static constexpr int N = ND * BS; // element tensor dimension
+  static constexpr int NU = N * (N + 1) / 2;
+  static constexpr int CPB = ELAST ? 4 : 32; // cells per block
+};
+
+// Stage-1 element tensors for the CPB cells of a block into sA.
+template <int DEG, bool ELAST, bool MASS>
+__device__ __forceinline__ void element_tensors(const dfx_form& a, const int32_t* sCell,
+                                                const int8_t* sActive, int nloc, double* sA,
+                                                double* sScratch)
+{
+  using T = Traits<DEG, ELAST>;
+  if constexpr (!ELAST)
+  {
+    const int cl = threadIdx.x;
+    if (cl < nloc && sActive[cl])
+    {
+      const int64_t c = sCell[cl];
+      double xc[12];
+      load_cell_coords(a, c, xc);
+      const double kap = a.kappa ? __ldg(a.kappa + c) : a.kappa_const;
+      double G[6];
+      const double adet = tet_metric(xc, kap, G);
+      double A[T::NU];
+      if constexpr (DEG == 1)
+        tet_p1_poisson_upper<MASS>(G, a.k2 * adet, A);
+      else
+        tet_p2_poisson_upper<MASS>(G, a.k2 * adet, A);
+#pragma unroll
+      for (int k = 0; k < T::NU; ++k)
+        sA[cl * T::NU + k] = A[k];
+    }
+    __syncthreads();
+  }
+  else
+  {
+    // sScratch layout per cell: K (9), w*|det| (1), mu (1), lambda (1),
+    // then physical gradients g[q][i][3] (120).
+    constexpr int SS = 132;
+    const int cl = threadIdx.x;
+    if (cl < nloc && sActive[cl])
+    {
+      const int64_t c = sCell[cl];
+      double xc[12], adj[3][3];
+      load_cell_coords(a, c, xc);
+      const double det = tet_adjugate(xc, adj);
+      const double inv = 1.0 / det;
+      double* s = sScratch + cl * SS;
+#pragma unroll
+      for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j)
+          s[3 * i + j] = adj[i][j] * inv; // K = J^{-1}
+      const double E = a.kappa ? __ldg(a.kappa + c) : a.kappa_const;
+      const double nu = a.nu;
+      s[9] = fabs(det) * (1.0 / 24.0);
+      s[10] = E / (2.0 * (1.0 + nu));
+      s[11] = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu));
+    }
+    __syncthreads();
+    // g_i(q) = K^T dphi_i(q): thread per (cell, q, i).
+    for (int t = threadIdx.x; t < nloc * 40; t += blockDim.x)
+    {
+      const int c = t / 40, qi = t % 40, q = qi / 10, i = qi % 10;
+      if (!sActive[c])
+        continue;
+      double* s = sScratch + c * SS;
+      const double d0 = kP2GradQ4[q][i][0], d1 = kP2GradQ4[q][i][1], d2 = kP2GradQ4[q][i][2];
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+        s[12 + 3 * qi + k] = s[k] * d0 + s[3 + k] * d1 + s[6 + k] * d2;
+    }
+    __syncthreads();
+    // 3x3 block (i <= j): thread per (cell, block pair).
+    for (int t = threadIdx.x; t < nloc * 55; t += blockDim.x)
+    {
+      const int c = t / 55;
+      if (!sActive[c])
+        continue;
+      int p = t % 55, i = 0;
+      while (p >= 10 - i)
+      {
+        p -= 10 - i;
+        ++i;
+      }
+      const int j = i + p;
+      const double* s = sScratch + c * SS;
+      const double w = s[9], mu = s[10], lm = s[11];
+      double B[3][3] = {};
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+      {
+        const double* gi = s + 12 + 3 * (10 * q + i);
+        const double* gj = s + 12 + 3 * (10 * q + j);
+        const double gg = gi[0] * gj[0] + gi[1] * gj[1] + gi[2] * gj[2];
+#pragma unroll
+        for (int k = 0; k < 3; ++k)
+#pragma unroll
+          for (int l = 0; l < 3; ++l)
+            B[k][l] += w * (mu * ((k == l ? gg : 0.0) + gi[l] * gj[k]) + lm * gi[k] * gj[l]);
+      }
+      double* A = sA + c * T::NU;
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+#pragma unroll
+        for (int l = 0; l < 3; ++l)
+          if (i < j || k <= l)
+            A[packed(3 * i + k, 3 * j + l, 30)] = B[k][l];
+    }
+    __syncthreads();
+  }
+}
+
+// Matrix assembly (LIFT = false) or lifting (LIFT = true) over a list of
+// cells (list == nullptr: cells [0, count)).
+template <int DEG, bool ELAST, bool MASS, bool COLOURED, bool LIFT>
+__global__ void __launch_bounds__(kThreads)
+    k_cells_matrix(const dfx_form a, const int64_t* __restrict__ row_ptr,
+                   const int32_t* __restrict__ cols, double* __restrict__ vals,
+                   const uint8_t* __restrict__ map, const int8_t* __restrict__ bc,
+                   const double* __restrict__ g, const double* __restrict__ x0, double alpha,
+                   double* __restrict__ b, const int32_t* __restrict__ list, int32_t count,
+                   int* __restrict__ status)
+{
+  using T = Traits<DEG, ELAST>;
+  constexpr int ND = T::ND, BS = T::BS, N = T::N, NU = T::NU, CPB = T::CPB;
+  __shared__ double sA[CPB * NU];
+  __shared__ double sScratch[ELAST ? CPB * 132 : 1];
+  __shared__ int32_t sCell[CPB];
+  __shared__ int32_t sDof[CPB * ND];
+  __shared__ int64_t sRow[CPB * ND];
+  __shared__ int8_t sBc[CPB * N];
+  __shared__ int8_t sActive[CPB];
+
+  const int64_t base = (int64_t)blockIdx.x * CPB;
+  const int nloc = (int)(((int64_t)count - base) < CPB ? ((int64_t)count - base) : CPB);
+  if (nloc <= 0)
+    return;
+  if (threadIdx.x < nloc)
+  {
+    sCell[threadIdx.x] = list ? __ldg(list + base + threadIdx.x) : (int32_t)(base + threadIdx.x);
+    sActive[threadIdx.x] = LIFT ? 0 : 1;
+  }
+  __syncthreads();
+  for (int t = threadIdx.x; t < nloc * ND; t += blockDim.x)
+  {
+    const int cl = t / ND, i = t % ND;
+    const int32_t d = __ldg(a.dofmap + (int64_t)sCell[cl] * ND + i);
+    sDof[t] = d;
+    if (!LIFT)
+      sRow[t] = __ldg(row_ptr + d);
+    bool any = false;
+#pragma unroll
+    for (int k = 0; k < BS; ++k)
+    {
+      const int8_t m = bc ? __ldg(bc + (int64_t)BS * d + k) : 0;
+      sBc[cl * N + BS * i + k] = m;
+      any |= (m != 0);
+    }
+    if (LIFT && any)
+      sActive[cl] = 1; // benign race: every writer stores 1
+  }
+  __syncthreads();
+  element_tensors<DEG, ELAST, MASS>(a, sCell, sActive, nloc, sA, sScratch);
+
+  if constexpr (!LIFT)
+  {
+    // Stage 2: scatter Ae into the CSR values, BC rows/columns zeroed
+    // (fem/assemble_matrix_impl.h:161-196).
+    constexpr int NN = ND * ND;
+    for (int e = threadIdx.x; e < nloc * N * N; e += blockDim.x)
+    {
+      const int cl = e / (N * N), IJ = e % (N * N), I = IJ / N, J = IJ % N;
+      if (sBc[cl * N + I] | sBc[cl * N + J])
+        continue;
+      const int i = I / BS, j = J / BS, k = I % BS, l = J % BS;
+      const double v = sA[cl * NU + (I <= J ? packed(I, J, N) : packed(J, I, N))];
+      int64_t pos;
+      if (map)
+        pos = sRow[cl * ND + i] + map[(int64_t)sCell[cl] * NN + i * ND + j];
+      else
+      {
+        const int32_t di = sDof[cl * ND + i];
+        const int64_t rb = sRow[cl * ND + i], re = __ldg(row_ptr + di + 1);
+        pos = row_search(cols, rb, re, sDof[cl * ND + j]);
+        if (pos >= re || __ldg(cols + pos) != sDof[cl * ND + j])
+        {
+          atomicExch(status, (int)DFX_ERR_NOT_IN_SPARSITY);
+          continue;
+        }
+      }
+      scatter_add<COLOURED>(vals + pos * (BS * BS) + k * BS + l, v);
+    }
+  }
+  else
+  {
+    // Lifting (fem/assemble_vector_impl.h:377-402): thread per element row.
+    for (int e = threadIdx.x; e < nloc * N; e += blockDim.x)
+    {
+      const int cl = e / N, I = e % N;
+      if (!sActive[cl])
+        continue;
+      double acc = 0.0;
+      for (int J = 0; J < N; ++J)
+      {
+        if (!sBc[cl * N + J])
+          continue;
+        const int64_t jj = (int64_t)BS * sDof[cl * ND + J / BS] + J % BS;
+        const double gv = g[jj] - (x0 ? x0[jj] : 0.0);
+        acc += sA[cl * NU + (I <= J ? packed(I, J, N) : packed(J, I, N))] * gv;
+      }
+      if (acc != 0.0)
+        scatter_add<COLOURED>(b + (int64_t)BS * sDof[cl * ND + I / BS] + I % BS, -alpha * acc);
+    }
+  }
+}
+
+// Vector assembly: source (scalar, P1 coefficient f) or body force.
+template <int DEG, bool BODY, bool COLOURED>
+__global__ void __launch_bounds__(kThreads)
+    k_cells_vector(const dfx_form a, double* __restrict__ b, const int32_t* __restrict__ list,
+                   int32_t count)
+{
+  constexpr int ND = DEG == 1 ? 4 : 10;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count)
+    return;
+  const int64_t c = list ? __ldg(list + t) : t;
+  double xc[12];
+  load_cell_coords(a, c, xc);
+  const double adet = tet_absdet(xc);
+  const int32_t* dofs = a.dofmap + c * ND;
+  if constexpr (!BODY)
+  {
+    double f[4];
+    const int4 xd = __ldg(reinterpret_cast<const int4*>(a.x_dofmap) + c);
+    if (a.f)
+    {
+      f[0] = __ldg(a.f + xd.x);
+      f[1] = __ldg(a.f + xd.y);
+      f[2] = __ldg(a.f + xd.z);
+      f[3] = __ldg(a.f + xd.w);
+    }
+    else
+      f[0] = f[1] = f[2] = f[3] = a.f_const[0];
+    double be[ND];
+    if constexpr (DEG == 1)
+      tet_p1_source(f, adet, be);
+    else
+      tet_p2_source(f, adet, be);
+#pragma unroll
+    for (int i = 0; i < ND; ++i)
+      scatter_add<COLOURED>(b + __ldg(dofs + i), be[i]);
+  }
+  else
+  {
+#pragma unroll
+    for (int i = 0; i < ND; ++i)
+    {
+      const int64_t d = __ldg(dofs + i);
+      const double w = adet * kTetP2Integral[i];
+#pragma unroll
+      for (int k = 0; k < 3; ++k)
+        scatter_add<COLOURED>(b + 3 * d + k, w * a.f_const[k]);
+    }
+  }
+}
+
+// Cell -> CSR slot map (byte offset of each entry within its row).
+template <int ND>
+__global__ void k_slot_map(const int32_t* __restrict__ dofmap, int32_t num_cells,
+                           const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ cols,
+                           uint8_t* __restrict__ map, int* __restrict__ status)
+{
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)num_cells * ND * ND)
+    return;
+  const int64_t c = t / (ND * ND);
+  const int ij = (int)(t % (ND * ND)), i = ij / ND, j = ij % ND;
+  const int32_t di = __ldg(dofmap + c * ND + i), dj = __ldg(dofmap + c * ND + j);
+  const int64_t rb = __ldg(row_ptr + di), re = __ldg(row_ptr + di + 1);
+  const int64_t p = row_search(cols, rb, re, dj);
+  if (p >= re || __ldg(cols + p) != dj)
+  {
+    atomicExch(status, (int)DFX_ERR_NOT_IN_SPARSITY);
+    map[t] = 0;
+    return;
+  }
+  if (p - rb > 255)
+  {
+    atomicExch(status, (int)DFX_ERR_UNSUPPORTED);
+    map[t] = 0;
+    return;
+  }
+  map[t] = (uint8_t)(p - rb);
+}
+
+__global__ void k_set_bc(double* __restrict__ x, int64_t n, const int32_t* __restrict__ dofs,
+                         int32_t ndofs, const double* __restrict__ g, double g_const,
+                         const double* __restrict__ x0, double alpha)
+{
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ndofs)
+    return;
+  const int32_t d = dofs[i];
+  if (d < 0 || d >= n)
+    return;
+  if (alpha == 0.0)
+  {
+    x[d] = 0.0;
+    return;
+  }
+  const double gv = g ? g[d] : g_const;
+  x[d] = alpha * (gv - (x0 ? x0[d] : 0.0));
+}
+
+__global__ void k_set_diagonal(const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ cols,
+                               double* __restrict__ vals, int bs, int32_t nrows,
+                               const int32_t* __restrict__ dofs, int32_t ndofs, double diag,
+                               int* __restrict__ status)
+{
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ndofs)
+    return;
+  const int32_t d = dofs[i], r = d / bs, k = d % bs;
+  if (r < 0 || r >= nrows)
+    return;
+  const int64_t rb = row_ptr[r], re = row_ptr[r + 1];
+  const int64_t p = row_search(cols, rb, re, r);
+  if (p >= re || cols[p] != r)
+  {
+    atomicExch(status, (int)DFX_ERR_NOT_IN_SPARSITY);
+    return;
+  }
+  vals[p * bs * bs + k * bs + k] = diag;
+}
+
+int check_form(const dfx_form* a, bool bilinear)
+{
+  DFX_REQUIRE(a, "form is NULL");
+  DFX_REQUIRE(a->num_cells >= 0, "negative cell count");
+  if (a->num_cells == 0)
+    return DFX_OK;
+  DFX_REQUIRE(a->x_dofmap && a->x && a->dofmap, "form arrays must be non-NULL");
+  DFX_REQUIRE(((uintptr_t)a->x_dofmap & 15) == 0, "x_dofmap must be 16-byte aligned");
+  if (bilinear)
+  {
+    DFX_REQUIRE(a->kind == DFX_FORM_POISSON || a->kind == DFX_FORM_ELASTICITY,
+                "form kind %d is not a bilinear form", a->kind);
+  }
+  else
+  {
+    DFX_REQUIRE(a->kind == DFX_FORM_SOURCE || a->kind == DFX_FORM_BODYFORCE,
+                "form kind %d is not a linear form", a->kind);
+  }
+  DFX_REQUIRE(a->degree == 1 || a->degree == 2, "degree %d not supported", a->degree);
+  DFX_REQUIRE(!((a->kind == DFX_FORM_ELASTICITY || a->kind == DFX_FORM_BODYFORCE)
+                && a->degree != 2),
+              "vector forms are P2 only");
+  return DFX_OK;
+}
+
+int form_nd(const dfx_form* a) { return a->degree == 1 ? 4 : 10; }
+int form_bs(const dfx_form* a)
+{
+  return (a->kind == DFX_FORM_ELASTICITY || a->kind == DFX_FORM_BODYFORCE) ? 3 : 1;
+}
+
+int read_status(int* status, cudaStream_t s)
+{
+  int h = 0;
+  DFX_CUDA(cudaMemcpyAsync(&h, status, sizeof(int), cudaMemcpyDeviceToHost, s));
+  DFX_CUDA(cudaStreamSynchronize(s));
+  if (h == DFX_ERR_NOT_IN_SPARSITY)
+    return dfx::fail(DFX_ERR_NOT_IN_SPARSITY, "Entry not in sparsity");
+  if (h == DFX_ERR_UNSUPPORTED)
+    return dfx::fail(DFX_ERR_UNSUPPORTED, "CSR row longer than 255 entries");
+  return h;
+}
+
+// Launch the matrix/lifting kernel for one cell list.
+template <int DEG, bool ELAST, bool MASS, bool COLOURED, bool LIFT>
+void launch_cells(const dfx_form& a, const dfx_csr* A, const uint8_t* map, const int8_t* bc,
+                  const double* g, const double* x0, double alpha, double* b,
+                  const int32_t* list, int32_t count, int* status, cudaStream_t s)
+{
+  constexpr int CPB = Traits<DEG, ELAST>::CPB;
+  if (count <= 0)
+    return;
+  const unsigned grid = (unsigned)((count + CPB - 1) / CPB);
+  k_cells_matrix<DEG, ELAST, MASS, COLOURED, LIFT><<<grid, kThreads, 0, s>>>(
+      a, A ? A->row_ptr : nullptr, A ? A->cols : nullptr, A ? (double*)A->vals : nullptr, map, bc,
+      g, x0, alpha, b, list, count, status);
+}
+
+template <bool COLOURED, bool LIFT>
+void dispatch_cells(const dfx_form& a, const dfx_csr* A, const uint8_t* map, const int8_t* bc,
+                    const double* g, const double* x0, double alpha, double* b,
+                    const int32_t* list, int32_t count, int* status, cudaStream_t s)
+{
+  const bool mass = a.kind == DFX_FORM_POISSON && a.k2 != 0.0;
+  if (a.kind == DFX_FORM_ELASTICITY)
+    launch_cells<2, true, false, COLOURED, LIFT>(a, A, map, bc, g, x0, alpha, b, list, count,
+                                                 status, s);
+  else if (a.degree == 1)
+  {
+    if (mass)
+      launch_cells<1, false, true, COLOURED, LIFT>(a, A, map, bc, g, x0, alpha, b, list, count,
+                                                   status, s);
+    else
+      launch_cells<1, false, false, COLOURED, LIFT>(a, A, map, bc, g, x0, alpha, b, list, count,
+                                                    status, s);
+  }
+  else
+  {
+    if (mass)
+      launch_cells<2, false, true, COLOURED, LIFT>(a, A, map, bc, g, x0, alpha, b, list, count,
+                                                   status, s);
+    else
+      launch_cells<2, false, false, COLOURED, LIFT>(a, A, map, bc, g, x0, alpha, b, list, count,
+                                                    status, s);
+  }
+}
+
+} // namespace
+
+extern "C" size_t dfx_slot_map_bytes(const dfx_form* a)
+{
+  if (!a)
+    return 0;
+  const int nd = form_nd(a);
+  return (size_t)a->num_cells * nd * nd;
+}
+
+extern "C" int dfx_slot_map_create(const dfx_form* a, const dfx_csr* A, uint8_t* d_map,
+                                   void* stream)
+{
+  if (int st = check_form(a, true))
+    return st;
+  DFX_REQUIRE(A && A->row_ptr && A->cols && d_map, "matrix/map must be non-NULL");
+  if (a->num_cells == 0)
+    return DFX_OK;
+  cudaStream_t s = dfx::as_stream(stream);
+  int* status = dfx::device_status_page();
+  DFX_REQUIRE(status, "could not allocate the status page");
+  DFX_CUDA(cudaMemsetAsync(status, 0, sizeof(int), s));
+  const int nd = form_nd(a);
+  const int64_t n = (int64_t)a->num_cells * nd * nd;
+  const unsigned grid = (unsigned)((n + 255) / 256);
+  if (nd == 4)
+    k_slot_map<4><<<grid, 256, 0, s>>>(a->dofmap, a->num_cells, A->row_ptr, A->cols, d_map, status);
+  else
+    k_slot_map<10><<<grid, 256, 0, s>>>(a->dofmap, a->num_cells, A->row_ptr, A->cols, d_map,
+                                        status);
+  DFX_CHECK_LAUNCH();
+  return read_status(status, s);
+}
+
+extern "C" int dfx_assemble_matrix(const dfx_form* a, const dfx_csr* A, const uint8_t* d_map,
+                                   const int8_t* d_bc, int32_t mode, const int32_t* d_order,
+                                   const int32_t* colour_offsets, int32_t num_colours,
+                                   void* stream)
+{
+  if (int st = check_form(a, true))
+    return st;
+  DFX_REQUIRE(A && A->row_ptr && A->cols && A->vals, "matrix must be non-NULL");
+  DFX_REQUIRE(A->dtype == DFX_F64, "assembly writes FP64 values");
+  DFX_REQUIRE(A->bs == form_bs(a), "matrix block size %d does not match the form (%d)", A->bs,
+              form_bs(a));
+  if (a->num_cells == 0)
+    return DFX_OK;
+  cudaStream_t s = dfx::as_stream(stream);
+  int* status = dfx::device_status_page();
+  DFX_REQUIRE(status, "could not allocate the status page");
+  if (!d_map)
+    DFX_CUDA(cudaMemsetAsync(status, 0, sizeof(int), s));
+  if (mode == DFX_MODE_ATOMIC)
+    dispatch_cells<false, false>(*a, A, d_map, d_bc, nullptr, nullptr, 0.0, nullptr, nullptr,
+                                 a->num_cells, status, s);
+  else if (mode == DFX_MODE_COLOURED)
+  {
+    DFX_REQUIRE(d_order && colour_offsets && num_colours > 0, "coloured mode needs a colouring");
+    for (int k = 0; k < num_colours; ++k)
+      dispatch_cells<true, false>(*a, A, d_map, d_bc, nullptr, nullptr, 0.0, nullptr,
+                                  d_order + colour_offsets[k],
+                                  colour_offsets[k + 1] - colour_offsets[k], status, s);
+  }
+  else
+    return dfx::fail(DFX_ERR_INVALID, "unknown assembly mode %d", mode);
+  DFX_CHECK_LAUNCH();
+  if (!d_map)
+    return read_status(status, s);
+  return DFX_OK;
+}
+
+extern "C" int dfx_apply_lifting(const dfx_form* a, double* d_b, const int8_t* d_bc,
+                                 const double* d_g, const double* d_x0, double alpha, int32_t mode,
+                                 const int32_t* d_order, const int32_t* colour_offsets,
+                                 int32_t num_colours, void* stream)
+{
+  if (int st = check_form(a, true))
+    return st;
+  DFX_REQUIRE(d_b && d_bc && d_g, "b, bc markers and g must be non-NULL");
+  if (a->num_cells == 0)
+    return DFX_OK;
+  cudaStream_t s = dfx::as_stream(stream);
+  if (mode == DFX_MODE_ATOMIC)
+    dispatch_cells<false, true>(*a, nullptr, nullptr, d_bc, d_g, d_x0, alpha, d_b, nullptr,
+                                a->num_cells, nullptr, s);
+  else if (mode == DFX_MODE_COLOURED)
+  {
+    DFX_REQUIRE(d_order && colour_offsets && num_colours > 0, "coloured mode needs a colouring");
+    for (int k = 0; k < num_colours; ++k)
+      dispatch_cells<true, true>(*a, nullptr, nullptr, d_bc, d_g, d_x0, alpha, d_b,
+                                 d_order + colour_offsets[k],
+                                 colour_offsets[k + 1] - colour_offsets[k], nullptr, s);
+  }
+  else
+    return dfx::fail(DFX_ERR_INVALID, "unknown assembly mode %d", mode);
+  DFX_CHECK_LAUNCH();
+  return DFX_OK;
+}
+
+extern "C" int dfx_assemble_vector(const dfx_form* L, double* d_b, int32_t mode,
+                                   const int32_t* d_order, const int32_t* colour_offsets,
+                                   int32_t num_colours, void* stream)
+{
+  if (int st = check_form(L, false))
+    return st;
+  DFX_REQUIRE(d_b, "b must be non-NULL");
+  if (L->num_cells == 0)
+    return DFX_OK;
+  cudaStream_t s = dfx::as_stream(stream);
+  auto launch = [&](auto coloured, const int32_t* list, int32_t count)
+  {
+    constexpr bool C = decltype(coloured)::value;
+    if (count <= 0)
+      return;
+    const unsigned grid = (unsigned)((count + kThreads - 1) / kThreads);
+    if (L->kind == DFX_FORM_BODYFORCE)
+      k_cells_vector<2, true, C><<<grid, kThreads, 0, s>>>(*L, d_b, list, count);
+    else if (L->degree == 1)
+      k_cells_vector<1, false, C><<<grid, kThreads, 0, s>>>(*L, d_b, list, count);
+    else
+      k_cells_vector<2, false, C><<<grid, kThreads, 0, s>>>(*L, d_b, list, count);
+  };
+  if (mode == DFX_MODE_ATOMIC)
+    launch(std::false_type{}, nullptr, L->num_cells);
+  else if (mode == DFX_MODE_COLOURED)
+  {
+    DFX_REQUIRE(d_order && colour_offsets && num_colours > 0, "coloured mode needs a colouring");
+    for (int k = 0; k < num_colours; ++k)
+      launch(std::true_type{}, d_order + colour_offsets[k],
+             colour_offsets[k + 1] - colour_offsets[k]);
+  }
+  else
+    return dfx::fail(DFX_ERR_INVALID, "unknown assembly mode %d", mode);
+  DFX_CHECK_LAUNCH();
+  return DFX_OK;
+}
+
+extern "C" int dfx_set_bc(double* d_x, int64_t n, const int32_t* d_dofs, int32_t ndofs,
+                          const double* d_g, double g_const, const double* d_x0, double alpha,
+                          void* stream)
+{
+  DFX_REQUIRE(ndofs >= 0, "negative dof count");
+  if (ndofs == 0)
+    return DFX_OK;
+  DFX_REQUIRE(d_x && d_dofs, "x and dofs must be non-NULL");
+  k_set_bc<<<(ndofs + 255) / 256, 256, 0, dfx::as_stream(stream)>>>(d_x, n, d_dofs, ndofs, d_g,
+                                                                    g_const, d_x0, alpha);
+  DFX_CHECK_LAUNCH();
+  return DFX_OK;
+}
+
+extern "C" int dfx_set_diagonal(const dfx_csr* A, const int32_t* d_dofs, int32_t ndofs,
+                                double diagonal, void* stream)
+{
+  DFX_REQUIRE(A && A->row_ptr && A->cols && A->vals, "matrix must be non-NULL");
+  DFX_REQUIRE(A->dtype == DFX_F64, "set_diagonal writes FP64 values");
+  if (ndofs == 0)
+    return DFX_OK;
+  DFX_REQUIRE(d_dofs && ndofs > 0, "dofs must be non-NULL");
+  cudaStream_t s = dfx::as_stream(stream);
+  int* status = dfx::device_status_page();
+  DFX_REQUIRE(status, "could not allocate the status page");
+  DFX_CUDA(cudaMemsetAsync(status, 0, sizeof(int), s));
+  k_set_diagonal<<<(ndofs + 255) / 256, 256, 0, s>>>(A->row_ptr, A->cols, (double*)A->vals, A->bs,
+                                                     A->nrows, d_dofs, ndofs, diagonal, status);
+  DFX_CHECK_LAUNCH();
+  return read_status(status, s);
+}

@@ -1,0 +1,219 @@
+// Linear algebra on la::MatrixCSR / la::Vector storage: CSR SpMV (FP64,
+// FP32 values, 3x3 blocks), the float cast of the values, the Jacobi
+// diagonal and a deterministic inner product.
+#include "la_kernels.cuh"
+
+namespace
+{
+__global__ void k_to_f32(const double* __restrict__ v, float* __restrict__ o, int64_t n)
+{
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    o[i] = (float)v[i];
+}
+
+__global__ void k_jacobi(const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ cols,
+                         const double* __restrict__ vals, int bs, int32_t nrows,
+                         double* __restrict__ dinv)
+{
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (int64_t)nrows * bs)
+    return;
+  const int32_t r = (int32_t)(t / bs), k = (int32_t)(t % bs);
+  int64_t b = row_ptr[r], e = row_ptr[r + 1];
+  while (b < e)
+  {
+    const int64_t m = (b + e) >> 1;
+    if (cols[m] < r)
+      b = m + 1;
+    else
+      e = m;
+  }
+  const double d = (b < row_ptr[r + 1] && cols[b] == r) ? vals[b * bs * bs + k * bs + k] : 0.0;
+  dinv[t] = d != 0.0 ? 1.0 / d : 0.0;
+}
+
+__global__ void k_dot_partial(const double* __restrict__ a, const double* __restrict__ b, int64_t n,
+                              double* __restrict__ partial)
+{
+  __shared__ double sh[32];
+  double s = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    s += a[i] * b[i];
+  s = dfx::block_sum(s, sh);
+  if (threadIdx.x == 0)
+    partial[blockIdx.x] = s;
+}
+
+__global__ void k_sum_partials(const double* __restrict__ partial, int n, double* __restrict__ out)
+{
+  __shared__ double sh[32];
+  double s = 0.0;
+  for (int i = threadIdx.x; i < n; i += blockDim.x)
+    s += partial[i];
+  s = dfx::block_sum(s, sh);
+  if (threadIdx.x == 0)
+    *out = s;
+}
+} // namespace
+
+namespace dfx
+{
+int launch_spmv(const dfx_csr* A, const void* x, void* y, double beta, cudaStream_t s)
+{
+  const bool acc = beta != 0.0;
+  if (A->nrows == 0)
+    return DFX_OK;
+  if (A->bs == 1)
+  {
+    const int lanes = spmv_lanes(A);
+    const int rows_per_block = kSpmvThreads / lanes;
+    const unsigned grid = (unsigned)((A->nrows + rows_per_block - 1) / rows_per_block);
+    if (A->dtype == DFX_F64)
+    {
+#define DFX_SPMV_CASE(L)                                                                           \
+  case L:                                                                                          \
+    if (acc)                                                                                       \
+      k_spmv_csr<L, double, double, double, true><<<grid, kSpmvThreads, 0, s>>>(                   \
+          A->nrows, A->row_ptr, A->cols, (const double*)A->vals, (const double*)x, (double*)y);    \
+    else                                                                                           \
+      k_spmv_csr<L, double, double, double, false><<<grid, kSpmvThreads, 0, s>>>(                  \
+          A->nrows, A->row_ptr, A->cols, (const double*)A->vals, (const double*)x, (double*)y);    \
+    break;
+      switch (lanes)
+      {
+        DFX_SPMV_CASE(4)
+        DFX_SPMV_CASE(8)
+        DFX_SPMV_CASE(16)
+        DFX_SPMV_CASE(32)
+      }
+#undef DFX_SPMV_CASE
+    }
+    else
+    {
+#define DFX_SPMV_CASE(L)                                                                           \
+  case L:                                                                                          \
+    if (acc)                                                                                       \
+      k_spmv_csr<L, float, float, float, true><<<grid, kSpmvThreads, 0, s>>>(                      \
+          A->nrows, A->row_ptr, A->cols, (const float*)A->vals, (const float*)x, (float*)y);       \
+    else                                                                                           \
+      k_spmv_csr<L, float, float, float, false><<<grid, kSpmvThreads, 0, s>>>(                     \
+          A->nrows, A->row_ptr, A->cols, (const float*)A->vals, (const float*)x, (float*)y);       \
+    break;
+      switch (lanes)
+      {
+        DFX_SPMV_CASE(4)
+        DFX_SPMV_CASE(8)
+        DFX_SPMV_CASE(16)
+        DFX_SPMV_CASE(32)
+      }
+#undef DFX_SPMV_CASE
+    }
+  }
+  else if (A->bs == 3)
+  {
+    const int rows_per_block = kSpmvThreads / 8;
+    const unsigned grid = (unsigned)((A->nrows + rows_per_block - 1) / rows_per_block);
+    if (A->dtype == DFX_F64)
+    {
+      if (acc)
+        k_spmv_bsr3<double, double, double, true><<<grid, kSpmvThreads, 0, s>>>(
+            A->nrows, A->row_ptr, A->cols, (const double*)A->vals, (const double*)x, (double*)y);
+      else
+        k_spmv_bsr3<double, double, double, false><<<grid, kSpmvThreads, 0, s>>>(
+            A->nrows, A->row_ptr, A->cols, (const double*)A->vals, (const double*)x, (double*)y);
+    }
+    else
+    {
+      if (acc)
+        k_spmv_bsr3<float, float, float, true><<<grid, kSpmvThreads, 0, s>>>(
+            A->nrows, A->row_ptr, A->cols, (const float*)A->vals, (const float*)x, (float*)y);
+      else
+        k_spmv_bsr3<float, float, float, false><<<grid, kSpmvThreads, 0, s>>>(
+            A->nrows, A->row_ptr, A->cols, (const float*)A->vals, (const float*)x, (float*)y);
+    }
+  }
+  else
+    return fail(DFX_ERR_UNSUPPORTED, "block size %d not supported", A->bs);
+  DFX_CHECK_LAUNCH();
+  return DFX_OK;
+}
+
+int check_csr(const dfx_csr* A)
+{
+  DFX_REQUIRE(A, "matrix is NULL");
+  DFX_REQUIRE(A->nrows >= 0 && A->ncols >= 0 && A->nnz >= 0, "negative matrix sizes");
+  DFX_REQUIRE(A->bs == 1 || A->bs == 3, "block size %d not supported", A->bs);
+  DFX_REQUIRE(A->dtype == DFX_F64 || A->dtype == DFX_F32, "unknown dtype %d", A->dtype);
+  if (A->nrows > 0)
+    DFX_REQUIRE(A->row_ptr && A->cols && A->vals, "matrix arrays must be non-NULL");
+  return DFX_OK;
+}
+} // namespace dfx
+
+extern "C" int dfx_spmv(const dfx_csr* A, const void* d_x, void* d_y, double beta, void* stream)
+{
+  if (int st = dfx::check_csr(A))
+    return st;
+  DFX_REQUIRE(beta == 0.0 || beta == 1.0, "beta must be 0 or 1");
+  DFX_REQUIRE(d_x && d_y, "x and y must be non-NULL");
+  return dfx::launch_spmv(A, d_x, d_y, beta, dfx::as_stream(stream));
+}
+
+extern "C" int dfx_csr_values_to_f32(const dfx_csr* A, float* d_vals32, void* stream)
+{
+  if (int st = dfx::check_csr(A))
+    return st;
+  DFX_REQUIRE(A->dtype == DFX_F64, "source values must be FP64");
+  const int64_t n = A->nnz * A->bs * A->bs;
+  if (n == 0)
+    return DFX_OK;
+  const unsigned grid = (unsigned)std::min<int64_t>((n + 255) / 256, 16 * dfx::num_sms());
+  k_to_f32<<<grid, 256, 0, dfx::as_stream(stream)>>>((const double*)A->vals, d_vals32, n);
+  DFX_CHECK_LAUNCH();
+  return DFX_OK;
+}
+
+extern "C" int dfx_jacobi_inverse_diagonal(const dfx_csr* A, double* d_dinv, void* stream)
+{
+  if (int st = dfx::check_csr(A))
+    return st;
+  DFX_REQUIRE(A->dtype == DFX_F64, "values must be FP64");
+  const int64_t n = (int64_t)A->nrows * A->bs;
+  if (n == 0)
+    return DFX_OK;
+  k_jacobi<<<(unsigned)((n + 255) / 256), 256, 0, dfx::as_stream(stream)>>>(
+      A->row_ptr, A->cols, (const double*)A->vals, A->bs, A->nrows, d_dinv);
+  DFX_CHECK_LAUNCH();
+  return DFX_OK;
+}
+
+extern "C" size_t dfx_inner_product_workspace_bytes(int64_t n)
+{
+  (void)n;
+  return sizeof(double) * (size_t)(8 * 152 + 8);
+}
+
+extern "C" int dfx_inner_product(const double* d_a, const double* d_b, int64_t n, void* d_work,
+                                 size_t work_bytes, double* result, void* stream)
+{
+  DFX_REQUIRE(result, "result must be non-NULL");
+  DFX_REQUIRE(n >= 0, "negative size");
+  if (n == 0)
+  {
+    *result = 0.0;
+    return DFX_OK;
+  }
+  DFX_REQUIRE(d_a && d_b && d_work, "arrays must be non-NULL");
+  const int blocks = (int)std::min<int64_t>((n + 255) / 256, 4 * dfx::num_sms());
+  DFX_REQUIRE(work_bytes >= sizeof(double) * (size_t)(blocks + 1), "workspace too small");
+  cudaStream_t s = dfx::as_stream(stream);
+  double* partial = (double*)d_work;
+  k_dot_partial<<<blocks, 256, 0, s>>>(d_a, d_b, n, partial);
+  k_sum_partials<<<1, 256, 0, s>>>(partial, blocks, partial + blocks);
+  DFX_CHECK_LAUNCH();
+  DFX_CUDA(cudaMemcpyAsync(result, partial + blocks, sizeof(double), cudaMemcpyDeviceToHost, s));
+  DFX_CUDA(cudaStreamSynchronize(s));
+  return DFX_OK;
+}

@@ -1,0 +1,464 @@
+// Host-side one-time structure of the hot path: box mesh with RCM cell
+// order, Lagrange dofmaps, CSR sparsity and cell colouring. These are the
+// inputs the reference hands to its assemblers; the numbering reproduces
+// DOLFINx on one rank bit for bit (checked against the oracle, whose
+// mesh ordering is itself pinned to the reference's compiled
+// graph/ordering.cpp and common/sort.h).
+#include "dfx_gpu.h"
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdint>
+#include <cstring>
+#include <numeric>
+#include <thread>
+#include <vector>
+
+namespace dfx
+{
+int fail(int code, const char* fmt, ...);
+}
+
+namespace
+{
+// Basix reference tetrahedron sub-entities.
+constexpr int kEdges[6][2] = {{2, 3}, {1, 3}, {1, 2}, {0, 3}, {0, 2}, {0, 1}};
+constexpr int kFacets[4][3] = {{1, 2, 3}, {0, 2, 3}, {0, 1, 3}, {0, 1, 2}};
+
+int num_threads()
+{
+  unsigned n = std::thread::hardware_concurrency();
+  return n == 0 ? 1 : (int)std::min(n, 64u);
+}
+
+template <typename F>
+void parallel_for(int64_t n, F&& f)
+{
+  const int nt = (int)std::min<int64_t>(num_threads(), std::max<int64_t>(1, n / 4096));
+  if (nt <= 1)
+  {
+    f(0, n);
+    return;
+  }
+  std::vector<std::thread> th;
+  for (int t = 0; t < nt; ++t)
+  {
+    const int64_t a = n * t / nt, b = n * (t + 1) / nt;
+    th.emplace_back([&f, a, b] { f(a, b); });
+  }
+  for (auto& t : th)
+    t.join();
+}
+
+// Facet-connected dual graph in the order of build_local_dual_graph
+// (mesh/graphbuild.cpp:566-905, serial path): facets keyed by their
+// sorted vertex triple, stably sorted, matched pairs become edges,
+// adjacency filled in edge order.
+void dual_graph(int64_t nc, const int64_t* cells, int64_t nverts, std::vector<int32_t>& off,
+                std::vector<int32_t>& adj)
+{
+  const int64_t nf = 4 * nc;
+  const bool pack = nverts < (int64_t(1) << 21);
+  std::vector<std::pair<uint64_t, uint64_t>> keys(nf); // (key hi, key lo | index)
+  for (int64_t c = 0; c < nc; ++c)
+    for (int f = 0; f < 4; ++f)
+    {
+      uint64_t v[3];
+      for (int k = 0; k < 3; ++k)
+        v[k] = (uint64_t)cells[4 * c + kFacets[f][k]];
+      if (v[0] > v[1])
+        std::swap(v[0], v[1]);
+      if (v[1] > v[2])
+        std::swap(v[1], v[2]);
+      if (v[0] > v[1])
+        std::swap(v[0], v[1]);
+      const uint64_t idx = (uint64_t)(4 * c + f);
+      if (pack)
+        keys[4 * c + f] = {(v[0] << 42) | (v[1] << 21) | v[2], idx};
+      else
+        keys[4 * c + f] = {(v[0] << 32) | v[1], (v[2] << 32) | idx};
+    }
+  // (key, facet index) is a strict order, so an unstable sort gives the
+  // stable-sort permutation of the reference.
+  std::sort(keys.begin(), keys.end());
+  auto same = [&](int64_t a, int64_t b)
+  {
+    if (pack)
+      return keys[a].first == keys[b].first;
+    return keys[a].first == keys[b].first && (keys[a].second >> 32) == (keys[b].second >> 32);
+  };
+  auto index = [&](int64_t a) -> int64_t
+  { return pack ? (int64_t)keys[a].second : (int64_t)(keys[a].second & 0xffffffffu); };
+  std::vector<std::pair<int32_t, int32_t>> edges;
+  edges.reserve(2 * nc);
+  for (int64_t i = 0; i < nf;)
+  {
+    int64_t j = i + 1;
+    while (j < nf && same(i, j))
+      ++j;
+    for (int64_t a = i; a < j; ++a)
+      for (int64_t b = a + 1; b < j; ++b)
+        edges.push_back({(int32_t)(index(a) / 4), (int32_t)(index(b) / 4)});
+    i = j;
+  }
+  off.assign(nc + 1, 0);
+  for (auto& e : edges)
+  {
+    ++off[e.first + 1];
+    ++off[e.second + 1];
+  }
+  for (int64_t c = 0; c < nc; ++c)
+    off[c + 1] += off[c];
+  adj.resize(off[nc]);
+  std::vector<int32_t> pos(off.begin(), off.end() - 1);
+  for (auto& e : edges)
+  {
+    adj[pos[e.first]++] = e.second;
+    adj[pos[e.second]++] = e.first;
+  }
+}
+
+// Rooted level structure; returns the number of levels, fills `ls` with
+// the nodes in level order and `lend` with level end offsets.
+int levels(const std::vector<int32_t>& off, const std::vector<int32_t>& adj, int s,
+           std::vector<int8_t>& mark, std::vector<int>& ls, std::vector<int>& lend)
+{
+  std::fill(mark.begin(), mark.end(), 0);
+  ls.clear();
+  lend.clear();
+  ls.push_back(s);
+  mark[s] = 1;
+  size_t begin = 0;
+  while (begin < ls.size())
+  {
+    const size_t end = ls.size();
+    lend.push_back((int)end);
+    for (size_t i = begin; i < end; ++i)
+      for (int k = off[ls[i]]; k < off[ls[i] + 1]; ++k)
+        if (!mark[adj[k]])
+        {
+          mark[adj[k]] = 1;
+          ls.push_back(adj[k]);
+        }
+    begin = end;
+  }
+  return (int)lend.size();
+}
+
+// Reverse Cuthill-McKee with a George-Liu pseudo-peripheral root
+// (graph/ordering.cpp:66-170). Ties in the degree sort follow
+// std::ranges::sort exactly as the reference does. r[old] = new.
+void rcm(const std::vector<int32_t>& off, const std::vector<int32_t>& adj,
+         std::vector<int32_t>& r)
+{
+  const int n = (int)off.size() - 1;
+  r.assign(n, -1);
+  auto deg = [&](int a) { return off[a + 1] - off[a]; };
+  auto cmp = [&](int a, int b) { return deg(a) < deg(b); };
+  std::vector<int8_t> mark(n);
+  std::vector<int> ls, lend, ls2, lend2, rv, nbr;
+  int count = 0;
+  while (count < n)
+  {
+    int v = 0, dmin = INT32_MAX;
+    for (int i = 0; i < n; ++i)
+      if (r[i] == -1 && deg(i) < dmin)
+      {
+        v = i;
+        dmin = deg(i);
+      }
+    int nl = levels(off, adj, v, mark, ls, lend);
+    for (;;)
+    {
+      const int b = nl > 1 ? lend[nl - 2] : 0;
+      const int s = *std::ranges::min_element(
+          std::ranges::subrange(ls.begin() + b, ls.begin() + lend[nl - 1]), cmp);
+      const int nl2 = levels(off, adj, s, mark, ls2, lend2);
+      if (nl2 > nl)
+      {
+        v = s;
+        nl = nl2;
+        ls.swap(ls2);
+        lend.swap(lend2);
+      }
+      else
+        break;
+    }
+    std::fill(mark.begin(), mark.end(), 0);
+    rv.clear();
+    rv.push_back(v);
+    mark[v] = 1;
+    for (size_t cur = 0; cur < rv.size(); ++cur)
+    {
+      nbr.clear();
+      for (int k = off[rv[cur]]; k < off[rv[cur] + 1]; ++k)
+        if (!mark[adj[k]])
+        {
+          nbr.push_back(adj[k]);
+          mark[adj[k]] = 1;
+        }
+      std::ranges::sort(nbr, cmp);
+      rv.insert(rv.end(), nbr.begin(), nbr.end());
+    }
+    for (auto it = rv.rbegin(); it != rv.rend(); ++it)
+      r[*it] = count++;
+  }
+}
+
+// Open-addressing map from 64-bit keys to int32 ids.
+struct KeyMap
+{
+  std::vector<uint64_t> k;
+  std::vector<int32_t> v;
+  uint64_t mask;
+  explicit KeyMap(int64_t n)
+  {
+    uint64_t cap = 16;
+    while (cap < (uint64_t)(2 * n))
+      cap <<= 1;
+    k.assign(cap, ~uint64_t(0));
+    v.assign(cap, -1);
+    mask = cap - 1;
+  }
+  // Returns the id of `key`, inserting `next` if absent (flag set).
+  int32_t get(uint64_t key, int32_t next, bool& inserted)
+  {
+    uint64_t h = (key * 0x9E3779B97F4A7C15ull) >> 17;
+    for (;; ++h)
+    {
+      const uint64_t i = h & mask;
+      if (k[i] == key)
+      {
+        inserted = false;
+        return v[i];
+      }
+      if (k[i] == ~uint64_t(0))
+      {
+        k[i] = key;
+        v[i] = next;
+        inserted = true;
+        return next;
+      }
+    }
+  }
+};
+
+} // namespace
+
+extern "C" int dfx_mesh_create_box_tet(int32_t nx, int32_t ny, int32_t nz, const double* p0,
+                                       const double* p1, int32_t reorder, int32_t* cells_out,
+                                       double* x_out)
+{
+  if (nx < 1 || ny < 1 || nz < 1)
+    return dfx::fail(DFX_ERR_INVALID, "At least one cell is required.");
+  for (int i = 0; i < 3; ++i)
+    if (!(p0[i] < p1[i]))
+      return dfx::fail(DFX_ERR_INVALID, "It must hold p[0] < p[1].");
+  const int64_t sqxy = (int64_t)(nx + 1) * (ny + 1);
+  const int64_t nv = sqxy * (nz + 1);
+  const int64_t nhex = (int64_t)nx * ny * nz;
+  const int64_t nc = 6 * nhex;
+  if (nc > INT32_MAX / 4)
+    return dfx::fail(DFX_ERR_INVALID, "mesh too large for int32 cell indices");
+  // Lexicographic vertices (generation.h:332-377) and the 6-tet split of
+  // each hexahedron sharing the v0-v7 diagonal (generation.h:404-420).
+  const double ext[3] = {(p1[0] - p0[0]) / nx, (p1[1] - p0[1]) / ny, (p1[2] - p0[2]) / nz};
+  std::vector<int64_t> cells(4 * nc);
+  for (int64_t i = 0; i < nhex; ++i)
+  {
+    const int64_t iz = i / ((int64_t)nx * ny), j = i % ((int64_t)nx * ny);
+    const int64_t iy = j / nx, ix = j % nx;
+    const int64_t v0 = iz * sqxy + iy * (nx + 1) + ix, v1 = v0 + 1;
+    const int64_t v2 = v0 + (nx + 1), v3 = v1 + (nx + 1);
+    const int64_t v4 = v0 + sqxy, v5 = v1 + sqxy, v6 = v2 + sqxy, v7 = v3 + sqxy;
+    const int64_t t[24] = {v0, v1, v3, v7, v0, v1, v7, v5, v0, v5, v7, v4,
+                           v0, v3, v2, v7, v0, v6, v4, v7, v0, v2, v6, v7};
+    std::memcpy(&cells[24 * i], t, sizeof(t));
+  }
+  std::vector<int32_t> perm; // new -> old cell
+  if (reorder)
+  {
+    std::vector<int32_t> off, adj, r;
+    dual_graph(nc, cells.data(), nv, off, adj);
+    rcm(off, adj, r);
+    perm.resize(nc);
+    for (int64_t c = 0; c < nc; ++c)
+      perm[r[c]] = (int32_t)c;
+  }
+  // Geometry nodes numbered by first appearance over the (reordered)
+  // cells (fem/dofmapbuilder.cpp:440-474, no graph reordering).
+  std::vector<int32_t> node(nv, -1);
+  int32_t cnt = 0;
+  for (int64_t c = 0; c < nc; ++c)
+  {
+    const int64_t co = reorder ? perm[c] : c;
+    for (int k = 0; k < 4; ++k)
+    {
+      const int64_t v = cells[4 * co + k];
+      if (node[v] < 0)
+        node[v] = cnt++;
+      cells_out[4 * c + k] = node[v];
+    }
+  }
+  for (int64_t v = 0; v < nv; ++v)
+  {
+    const int64_t p = v % sqxy;
+    const int64_t idx[3] = {p % (nx + 1), p / (nx + 1), v / sqxy};
+    for (int i = 0; i < 3; ++i)
+      x_out[3 * (int64_t)node[v] + i] = p0[i] + (double)idx[i] * ext[i];
+  }
+  return DFX_OK;
+}
+
+extern "C" int dfx_dofmap_create_tet(int32_t num_cells, const int32_t* cells, int32_t degree,
+                                     int32_t* dofmap, int32_t* num_nodes)
+{
+  if (degree != 1 && degree != 2)
+    return dfx::fail(DFX_ERR_UNSUPPORTED, "Lagrange degree %d not supported", degree);
+  int32_t vmax = -1;
+  for (int64_t i = 0; i < 4 * (int64_t)num_cells; ++i)
+    vmax = std::max(vmax, cells[i]);
+  // Vertex dofs keyed by vertex, edge dofs by their sorted vertex pair;
+  // ids handed out in order of first appearance over the cell dofmap.
+  std::vector<int32_t> vid(vmax + 1, -1);
+  KeyMap emap(degree == 2 ? 7 * (int64_t)num_cells / 5 + 16 : 16);
+  int32_t cnt = 0;
+  const int nd = degree == 1 ? 4 : 10;
+  for (int64_t c = 0; c < num_cells; ++c)
+  {
+    const int32_t* v = cells + 4 * c;
+    for (int i = 0; i < 4; ++i)
+    {
+      if (vid[v[i]] < 0)
+        vid[v[i]] = cnt++;
+      dofmap[nd * c + i] = vid[v[i]];
+    }
+    if (degree == 2)
+      for (int e = 0; e < 6; ++e)
+      {
+        uint64_t a = (uint32_t)v[kEdges[e][0]], b = (uint32_t)v[kEdges[e][1]];
+        if (a > b)
+          std::swap(a, b);
+        bool ins;
+        const int32_t id = emap.get((a << 32) | b, cnt, ins);
+        if (ins)
+          ++cnt;
+        dofmap[nd * c + 4 + e] = id;
+      }
+  }
+  // Ids were handed out in one pass over the local dofs of the cells in
+  // order, which is the reference's first-appearance numbering.
+  *num_nodes = cnt;
+  return DFX_OK;
+}
+
+extern "C" int dfx_sparsity_create(int32_t nrows, int32_t num_cells, int32_t nd,
+                                   const int32_t* dofmap, int64_t* row_ptr, int32_t* cols,
+                                   int64_t* nnz_out)
+{
+  if (nrows < 0 || num_cells < 0 || nd <= 0 || !row_ptr)
+    return dfx::fail(DFX_ERR_INVALID, "invalid sparsity arguments");
+  // Transpose dofmap: node -> cells.
+  std::vector<int32_t> coff(nrows + 1, 0);
+  for (int64_t i = 0; i < (int64_t)num_cells * nd; ++i)
+  {
+    if (dofmap[i] < 0 || dofmap[i] >= nrows)
+      return dfx::fail(DFX_ERR_INVALID, "dofmap entry %d out of range", dofmap[i]);
+    ++coff[dofmap[i] + 1];
+  }
+  for (int r = 0; r < nrows; ++r)
+    coff[r + 1] += coff[r];
+  std::vector<int32_t> ccell(coff[nrows]);
+  {
+    std::vector<int32_t> pos(coff.begin(), coff.end() - 1);
+    for (int64_t c = 0; c < num_cells; ++c)
+      for (int i = 0; i < nd; ++i)
+        ccell[pos[dofmap[c * nd + i]]++] = (int32_t)c;
+  }
+  auto row_cols = [&](int32_t r, std::vector<int32_t>& buf)
+  {
+    buf.clear();
+    for (int k = coff[r]; k < coff[r + 1]; ++k)
+    {
+      const int32_t* d = dofmap + (int64_t)ccell[k] * nd;
+      buf.insert(buf.end(), d, d + nd);
+    }
+    std::sort(buf.begin(), buf.end());
+    buf.erase(std::unique(buf.begin(), buf.end()), buf.end());
+  };
+  if (!cols)
+  {
+    std::vector<int64_t> len(nrows);
+    parallel_for(nrows,
+                 [&](int64_t a, int64_t b)
+                 {
+                   std::vector<int32_t> buf;
+                   for (int64_t r = a; r < b; ++r)
+                   {
+                     row_cols((int32_t)r, buf);
+                     len[r] = (int64_t)buf.size();
+                   }
+                 });
+    row_ptr[0] = 0;
+    for (int r = 0; r < nrows; ++r)
+      row_ptr[r + 1] = row_ptr[r] + len[r];
+    if (nnz_out)
+      *nnz_out = row_ptr[nrows];
+    return DFX_OK;
+  }
+  parallel_for(nrows,
+               [&](int64_t a, int64_t b)
+               {
+                 std::vector<int32_t> buf;
+                 for (int64_t r = a; r < b; ++r)
+                 {
+                   row_cols((int32_t)r, buf);
+                   std::copy(buf.begin(), buf.end(), cols + row_ptr[r]);
+                 }
+               });
+  if (nnz_out)
+    *nnz_out = row_ptr[nrows];
+  return DFX_OK;
+}
+
+extern "C" int dfx_colour_cells(int32_t num_cells, int32_t nd, const int32_t* dofmap,
+                                int32_t num_nodes, int32_t* order, int32_t* offsets,
+                                int32_t max_colours, int32_t* num_colours)
+{
+  // Greedy first-fit in cell order; per-node bitmasks of used colours.
+  constexpr int W = 4; // 256 colours max
+  if (max_colours < 1)
+    return dfx::fail(DFX_ERR_INVALID, "max_colours must be >= 1");
+  std::vector<uint64_t> used((size_t)num_nodes * W, 0);
+  std::vector<int32_t> colour(num_cells);
+  int ncol = 0;
+  for (int64_t c = 0; c < num_cells; ++c)
+  {
+    uint64_t m[W] = {0, 0, 0, 0};
+    const int32_t* d = dofmap + c * nd;
+    for (int i = 0; i < nd; ++i)
+      for (int w = 0; w < W; ++w)
+        m[w] |= used[(size_t)d[i] * W + w];
+    int col = -1;
+    for (int w = 0; w < W && col < 0; ++w)
+      if (~m[w])
+        col = 64 * w + __builtin_ctzll(~m[w]);
+    if (col < 0 || col >= max_colours)
+      return dfx::fail(DFX_ERR_UNSUPPORTED, "cell colouring needs more than %d colours",
+                       std::min(max_colours, 64 * W));
+    colour[c] = col;
+    ncol = std::max(ncol, col + 1);
+    for (int i = 0; i < nd; ++i)
+      used[(size_t)d[i] * W + col / 64] |= uint64_t(1) << (col % 64);
+  }
+  std::fill(offsets, offsets + ncol + 1, 0);
+  for (int64_t c = 0; c < num_cells; ++c)
+    ++offsets[colour[c] + 1];
+  for (int k = 0; k < ncol; ++k)
+    offsets[k + 1] += offsets[k];
+  std::vector<int32_t> pos(offsets, offsets + ncol);
+  for (int64_t c = 0; c < num_cells; ++c)
+    order[pos[colour[c]]++] = (int32_t)c;
+  *num_colours = ncol;
+  return DFX_OK;
+}

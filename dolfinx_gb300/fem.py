@@ -1,0 +1,367 @@
+"""Finite-element front end mirroring ``dolfinx.fem`` for the GPU hot path.
+
+Names, argument meaning and accumulate semantics follow the reference's
+Python layer (python/dolfinx/fem/assemble.py:111-493,
+python/dolfinx/fem/bcs.py) and C++ assemblers (cpp/dolfinx/fem/assembler.h).
+The bilinear/linear forms are the built-in element kernels of libdfxgpu
+(Poisson/Helmholtz, linear elasticity, sources) in place of UFL + FFCx.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _capi
+from .la import MatrixCSR, _ptr, _stream
+from .mesh import Mesh
+
+_EDGES = np.array([[2, 3], [1, 3], [1, 2], [0, 3], [0, 2], [0, 1]])
+
+
+class FunctionSpace:
+    """Lagrange P1/P2 space (scalar or vector, bs 3) on a tetrahedral mesh."""
+
+    def __init__(self, mesh: Mesh, degree: int, bs: int = 1, device="cuda"):
+        self.mesh, self.degree, self.bs = mesh, int(degree), int(bs)
+        nd = 4 if degree == 1 else 10
+        self.dofmap = np.empty((mesh.num_cells, nd), np.int32)
+        n = C.c_int32(0)
+        _capi.check(_capi.lib().dfx_dofmap_create_tet(mesh.num_cells, mesh.cells.ctypes.data,
+                                                      self.degree, self.dofmap.ctypes.data,
+                                                      C.byref(n)))
+        self.num_nodes = int(n.value)
+        self.device = device
+        self._dofmap_dev = None
+        self._sparsity = None
+        self._colouring = None
+
+    @property
+    def num_dofs(self) -> int:
+        """Scalar dofs (nodes x bs)."""
+        return self.num_nodes * self.bs
+
+    @property
+    def ndofs_cell(self) -> int:
+        return self.dofmap.shape[1]
+
+    def dofmap_device(self) -> torch.Tensor:
+        if self._dofmap_dev is None:
+            self._dofmap_dev = torch.from_numpy(self.dofmap).to(self.device)
+        return self._dofmap_dev
+
+    def tabulate_dof_coordinates(self) -> np.ndarray:
+        """Coordinates of the dof nodes (vertices, then edge midpoints)."""
+        X = np.empty((self.num_nodes, 3))
+        xc = self.mesh.x[self.mesh.cells]  # (nc, 4, 3)
+        X[self.dofmap[:, :4].ravel()] = xc.reshape(-1, 3)
+        if self.degree == 2:
+            mid = 0.5 * (xc[:, _EDGES[:, 0]] + xc[:, _EDGES[:, 1]])
+            X[self.dofmap[:, 4:].ravel()] = mid.reshape(-1, 3)
+        return X
+
+    def sparsity(self):
+        """(row_ptr, cols) of the cell sparsity pattern on the host (cached)."""
+        if self._sparsity is None:
+            nd = self.ndofs_cell
+            rp = np.empty(self.num_nodes + 1, np.int64)
+            nnz = C.c_int64(0)
+            L = _capi.lib()
+            _capi.check(L.dfx_sparsity_create(self.num_nodes, self.mesh.num_cells, nd,
+                                              self.dofmap.ctypes.data, rp.ctypes.data, None,
+                                              C.byref(nnz)))
+            cols = np.empty(nnz.value, np.int32)
+            _capi.check(L.dfx_sparsity_create(self.num_nodes, self.mesh.num_cells, nd,
+                                              self.dofmap.ctypes.data, rp.ctypes.data,
+                                              cols.ctypes.data, C.byref(nnz)))
+            self._sparsity = (rp, cols)
+        return self._sparsity
+
+    def colouring(self, max_colours: int = 256):
+        """Cell colouring for deterministic assembly: (order on device, offsets)."""
+        if self._colouring is None:
+            nc = self.mesh.num_cells
+            order = np.empty(nc, np.int32)
+            offsets = np.zeros(max_colours + 1, np.int32)
+            ncol = C.c_int32(0)
+            _capi.check(_capi.lib().dfx_colour_cells(nc, self.ndofs_cell, self.dofmap.ctypes.data,
+                                                     self.num_nodes, order.ctypes.data,
+                                                     offsets.ctypes.data, max_colours,
+                                                     C.byref(ncol)))
+            off = offsets[: ncol.value + 1].copy()
+            self._colouring = (torch.from_numpy(order).to(self.device), off)
+        return self._colouring
+
+
+def functionspace(mesh: Mesh, element, device="cuda") -> FunctionSpace:
+    """``functionspace(mesh, ("Lagrange", k))`` or ``("Lagrange", k, (3,))``."""
+    family, degree = element[0], int(element[1])
+    if family not in ("Lagrange", "P", "CG"):
+        raise ValueError(f"element family {family} is not on the GPU hot path")
+    bs = 1
+    if len(element) > 2 and element[2]:
+        bs = int(np.prod(element[2]))
+    return FunctionSpace(mesh, degree, bs, device)
+
+
+def locate_dofs_geometrical(V: FunctionSpace, marker) -> np.ndarray:
+    """Node (block) indices whose coordinates satisfy ``marker(x)`` (x: (3, n))."""
+    X = V.tabulate_dof_coordinates()
+    return np.flatnonzero(marker(X.T)).astype(np.int32)
+
+
+class DirichletBC:
+    """Dirichlet condition u = g on the given dof nodes (fem/DirichletBC.h)."""
+
+    def __init__(self, value, dofs, V: FunctionSpace):
+        self.V = V
+        dofs = np.unique(np.asarray(dofs, np.int32))
+        bs = V.bs
+        # _dofs0 unrolled by block size (fem/DirichletBC.h:357-359).
+        self.dofs = (dofs[:, None] * bs + np.arange(bs, dtype=np.int32)[None, :]).ravel()
+        self.dofs = self.dofs.astype(np.int32)
+        n = V.num_dofs
+        dev = V.device
+        if np.isscalar(value):
+            self.g_const = float(value)
+            self.g = None
+        else:
+            val = np.asarray(value, np.float64)
+            if val.size == bs:  # constant per component
+                g = np.zeros(n)
+                g[self.dofs] = val[self.dofs % bs]
+                self.g = torch.from_numpy(g).to(dev)
+            else:
+                assert val.size == n, "BC value must be a constant or a full dof vector"
+                self.g = torch.from_numpy(val.copy()).to(dev)
+            self.g_const = 0.0
+        self.dofs_dev = torch.from_numpy(self.dofs).to(dev)
+
+    def g_full(self) -> torch.Tensor:
+        if self.g is None:
+            self.g = torch.full((self.V.num_dofs,), self.g_const, dtype=torch.float64,
+                                device=self.V.device)
+        return self.g
+
+    def mark_dofs(self, markers: torch.Tensor) -> None:
+        markers[self.dofs_dev.long()] = 1
+
+    def set(self, x: torch.Tensor, x0: torch.Tensor | None = None, alpha: float = 1.0) -> None:
+        _capi.check(_capi.lib().dfx_set_bc(_ptr(x), x.numel(), _ptr(self.dofs_dev),
+                                           int(self.dofs.size), _ptr(self.g), self.g_const,
+                                           _ptr(x0), float(alpha), _stream()))
+
+
+def dirichletbc(value, dofs, V: FunctionSpace) -> DirichletBC:
+    return DirichletBC(value, dofs, V)
+
+
+@dataclass
+class Form:
+    """A built-in form on a function space (cell integral only)."""
+
+    kind: int
+    V: FunctionSpace
+    kappa: torch.Tensor | None = None  # per-cell coefficient (kappa or E)
+    kappa_const: float = 1.0
+    k2: float = 0.0
+    nu: float = 0.3
+    f: torch.Tensor | None = None  # P1 source values on the geometry nodes
+    f_const: tuple = (0.0, 0.0, 0.0)
+    _cache: dict = field(default_factory=dict, repr=False)
+
+    @property
+    def rank(self) -> int:
+        return 2 if self.kind in (_capi.FORM_POISSON, _capi.FORM_ELASTICITY) else 1
+
+    def cstruct(self) -> _capi.Form:
+        V = self.V
+        xd, x = V.mesh.device(V.device)
+        fc = (C.c_double * 3)(*[float(v) for v in self.f_const])
+        return _capi.Form(self.kind, V.degree, V.mesh.num_cells, V.mesh.num_nodes,
+                          xd.data_ptr(), x.data_ptr(), V.dofmap_device().data_ptr(),
+                          None if self.kappa is None else self.kappa.data_ptr(),
+                          float(self.kappa_const), float(self.k2), float(self.nu),
+                          None if self.f is None else self.f.data_ptr(), fc)
+
+
+def _dev(v, V):
+    if v is None or np.isscalar(v):
+        return None
+    t = torch.as_tensor(np.asarray(v, np.float64)) if not torch.is_tensor(v) else v
+    return t.to(device=V.device, dtype=torch.float64).contiguous()
+
+
+def poisson_form(V: FunctionSpace, kappa=1.0, k2: float = 0.0) -> Form:
+    """a(u,v) = int kappa grad u.grad v + k2 u v dx; kappa constant or per cell."""
+    return Form(_capi.FORM_POISSON, V, kappa=_dev(kappa, V),
+                kappa_const=float(kappa) if np.isscalar(kappa) else 1.0, k2=float(k2))
+
+
+def elasticity_form(V: FunctionSpace, E=1.0, nu: float = 0.3) -> Form:
+    """a(u,v) = int sigma(u):eps(v) dx, E constant or per cell."""
+    assert V.bs == 3 and V.degree == 2
+    return Form(_capi.FORM_ELASTICITY, V, kappa=_dev(E, V),
+                kappa_const=float(E) if np.isscalar(E) else 1.0, nu=float(nu))
+
+
+def source_form(V: FunctionSpace, f=1.0) -> Form:
+    """L(v) = int f v dx, f constant or P1 values on the geometry nodes."""
+    return Form(_capi.FORM_SOURCE, V, f=_dev(f, V),
+                f_const=(float(f) if np.isscalar(f) else 0.0, 0.0, 0.0))
+
+
+def body_force_form(V: FunctionSpace, f=(0.0, 0.0, -1.0)) -> Form:
+    assert V.bs == 3 and V.degree == 2
+    return Form(_capi.FORM_BODYFORCE, V, f_const=tuple(float(v) for v in f))
+
+
+def _mode(mode: str) -> int:
+    return {"atomic": _capi.MODE_ATOMIC, "coloured": _capi.MODE_COLOURED,
+            "colored": _capi.MODE_COLOURED}[mode]
+
+
+def _colour_args(V: FunctionSpace, mode: int):
+    if mode != _capi.MODE_COLOURED:
+        return None, None, 0
+    order, off = V.colouring()
+    return C.c_void_p(order.data_ptr()), off.ctypes.data_as(C.c_void_p), int(off.size - 1)
+
+
+def create_matrix(a: Form) -> MatrixCSR:
+    """Matrix with the form's sparsity pattern, values zero (create_matrix)."""
+    rp, cols = a.V.sparsity()
+    dev = a.V.device
+    bs = a.V.bs
+    vals = torch.zeros(cols.size * bs * bs, dtype=torch.float64, device=dev)
+    return MatrixCSR(torch.from_numpy(rp).to(dev), torch.from_numpy(cols).to(dev), vals, bs)
+
+
+def bc_markers(V: FunctionSpace, bcs) -> torch.Tensor | None:
+    if not bcs:
+        return None
+    m = torch.zeros(V.num_dofs, dtype=torch.int8, device=V.device)
+    for bc in bcs:
+        bc.mark_dofs(m)
+    return m
+
+
+class MatrixAssembler:
+    """Reusable matrix assembly for one form: the cell->slot map, BC markers
+    and colouring are computed once (serving-style reuse)."""
+
+    def __init__(self, a: Form, bcs=(), diagonal: float = 1.0, mode: str = "atomic",
+                 A: MatrixCSR | None = None, use_slot_map: bool = True):
+        self.a, self.bcs, self.diagonal, self.mode = a, list(bcs), float(diagonal), _mode(mode)
+        self.A = create_matrix(a) if A is None else A
+        self.form = a.cstruct()
+        self.markers = bc_markers(a.V, self.bcs)
+        self.map = None
+        if use_slot_map:
+            nb = int(_capi.lib().dfx_slot_map_bytes(C.byref(self.form)))
+            self.map = torch.empty(nb, dtype=torch.uint8, device=a.V.device)
+            _capi.check(_capi.lib().dfx_slot_map_create(C.byref(self.form), C.byref(self.A.csr()),
+                                                        _ptr(self.map), _stream()))
+        self.colour = _colour_args(a.V, self.mode)
+        bc_dofs = [bc.dofs for bc in self.bcs if bc.V is a.V]
+        self.diag_dofs = (torch.from_numpy(np.unique(np.concatenate(bc_dofs))).to(a.V.device)
+                          if bc_dofs else None)
+
+    def assemble(self, zero: bool = True) -> MatrixCSR:
+        if zero:
+            self.A.vals.zero_()
+        order, off, ncol = self.colour
+        _capi.check(_capi.lib().dfx_assemble_matrix(C.byref(self.form), C.byref(self.A.csr()),
+                                                    _ptr(self.map), _ptr(self.markers), self.mode,
+                                                    order, off, ncol, _stream()))
+        if self.diag_dofs is not None:
+            _capi.check(_capi.lib().dfx_set_diagonal(C.byref(self.A.csr()), _ptr(self.diag_dofs),
+                                                     int(self.diag_dofs.numel()), self.diagonal,
+                                                     _stream()))
+        return self.A
+
+
+def assemble_matrix(a: Form, bcs=(), diagonal: float = 1.0, mode: str = "atomic",
+                    use_slot_map: bool = True) -> MatrixCSR:
+    """Assemble a bilinear form into a new MatrixCSR; constrained rows and
+    columns are zeroed and `diagonal` placed on constrained diagonal entries
+    (python/dolfinx/fem/assemble.py:282-372)."""
+    return MatrixAssembler(a, bcs, diagonal, mode, use_slot_map=use_slot_map).assemble(zero=True)
+
+
+def assemble_vector(L: Form, b: torch.Tensor | None = None, mode: str = "atomic") -> torch.Tensor:
+    """b += assembled linear form (a new zero vector when b is None)."""
+    V = L.V
+    if b is None:
+        b = torch.zeros(V.num_dofs, dtype=torch.float64, device=V.device)
+    m = _mode(mode)
+    order, off, ncol = _colour_args(V, m)
+    cf = L.cstruct()
+    _capi.check(_capi.lib().dfx_assemble_vector(C.byref(cf), _ptr(b), m, order, off, ncol,
+                                                _stream()))
+    return b
+
+
+def apply_lifting(b: torch.Tensor, a, bcs, x0=None, alpha: float = 1.0,
+                  mode: str = "atomic") -> None:
+    """b -= alpha * A (g - x0) restricted to constrained columns, for each
+    form a[j] with boundary conditions bcs[j]."""
+    m = _mode(mode)
+    x0 = x0 or [None] * len(a)
+    for aj, bcj, x0j in zip(a, bcs, x0):
+        if aj is None or not bcj:
+            continue
+        V = aj.V
+        markers = bc_markers(V, bcj)
+        g = torch.zeros(V.num_dofs, dtype=torch.float64, device=V.device)
+        for bc in bcj:
+            bc.set(g)
+        order, off, ncol = _colour_args(V, m)
+        cf = aj.cstruct()
+        _capi.check(_capi.lib().dfx_apply_lifting(C.byref(cf), _ptr(b), _ptr(markers), _ptr(g),
+                                                  _ptr(x0j), float(alpha), m, order, off, ncol,
+                                                  _stream()))
+
+
+def set_bc(b: torch.Tensor, bcs, x0: torch.Tensor | None = None, alpha: float = 1.0) -> None:
+    for bc in bcs:
+        bc.set(b, x0, alpha)
+
+
+class RhsAssembler:
+    """Reusable right-hand side: b = assemble_vector(L); apply_lifting(b, [a],
+    [bcs]); set_bc(b, bcs) -- the canonical sequence of
+    python/test/unit/fem/test_fem_pipeline.py:91-98 -- with the BC markers,
+    BC values and colouring prepared once."""
+
+    def __init__(self, L: Form, a: Form | None, bcs=(), mode: str = "atomic"):
+        self.L, self.a, self.bcs, self.mode = L, a, list(bcs), _mode(mode)
+        V = L.V
+        self.Lc = L.cstruct()
+        self.ac = a.cstruct() if a is not None else None
+        self.markers = bc_markers(V, self.bcs)
+        self.g = torch.zeros(V.num_dofs, dtype=torch.float64, device=V.device)
+        for bc in self.bcs:
+            bc.set(self.g)
+        self.colour = _colour_args(V, self.mode)
+
+    def assemble(self, b: torch.Tensor | None = None) -> torch.Tensor:
+        V = self.L.V
+        if b is None:
+            b = torch.zeros(V.num_dofs, dtype=torch.float64, device=V.device)
+        else:
+            b.zero_()
+        order, off, ncol = self.colour
+        L = _capi.lib()
+        _capi.check(L.dfx_assemble_vector(C.byref(self.Lc), _ptr(b), self.mode, order, off, ncol,
+                                          _stream()))
+        if self.ac is not None and self.bcs:
+            _capi.check(L.dfx_apply_lifting(C.byref(self.ac), _ptr(b), _ptr(self.markers),
+                                            _ptr(self.g), None, 1.0, self.mode, order, off, ncol,
+                                            _stream()))
+        for bc in self.bcs:
+            bc.set(b)
+        return b

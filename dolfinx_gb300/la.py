@@ -1,0 +1,175 @@
+"""Device-resident linear algebra mirroring ``dolfinx.la`` (MatrixCSR, Vector,
+inner_product, norm) plus the Jacobi-preconditioned CG of the matrix-free
+demo. Storage is la::MatrixCSR's (int64 row pointers, int32 columns,
+row-major bs x bs blocks) in device memory owned by torch tensors; every
+operation runs in libdfxgpu.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from . import _capi
+
+
+def _stream():
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _ptr(t):
+    return None if t is None else C.c_void_p(t.data_ptr())
+
+
+class MatrixCSR:
+    """CSR matrix with square bs x bs blocks (cpp/dolfinx/la/MatrixCSR.h:67-1017)."""
+
+    def __init__(self, row_ptr: torch.Tensor, cols: torch.Tensor, vals: torch.Tensor, bs: int = 1,
+                 ncols: int | None = None):
+        assert row_ptr.dtype == torch.int64 and cols.dtype == torch.int32
+        assert vals.dtype in (torch.float64, torch.float32)
+        self.row_ptr, self.cols, self.vals, self.bs = row_ptr, cols, vals, int(bs)
+        self.nrows = int(row_ptr.numel() - 1)
+        self.ncols = self.nrows if ncols is None else int(ncols)
+        self.nnz = int(cols.numel())
+        self._slot_map = None
+        self._csr = None
+
+    @property
+    def dtype(self):
+        return self.vals.dtype
+
+    @property
+    def block_size(self):
+        return (self.bs, self.bs)
+
+    def csr(self) -> _capi.Csr:
+        c = self._csr
+        if c is None or c.vals != self.vals.data_ptr():
+            c = _capi.Csr(self.nrows, self.ncols, self.bs,
+                          _capi.F64 if self.vals.dtype == torch.float64 else _capi.F32, self.nnz,
+                          self.row_ptr.data_ptr(), self.cols.data_ptr(), self.vals.data_ptr())
+            self._csr = c
+        return c
+
+    def set_value(self, v: float = 0.0) -> None:
+        self.vals.fill_(v)
+
+    def mult(self, x: torch.Tensor, y: torch.Tensor) -> None:
+        """y += A x (MatrixCSR::mult)."""
+        _capi.check(_capi.lib().dfx_spmv(C.byref(self.csr()), _ptr(x), _ptr(y), 1.0, _stream()))
+
+    def matvec(self, x: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        """Return A x (overwrites `out`)."""
+        if out is None:
+            out = torch.empty(self.nrows * self.bs, dtype=x.dtype, device=x.device)
+        _capi.check(_capi.lib().dfx_spmv(C.byref(self.csr()), _ptr(x), _ptr(out), 0.0, _stream()))
+        return out
+
+    def astype_float32(self) -> "MatrixCSR":
+        """The float copy of the values (MatrixCSR converting constructor)."""
+        v32 = torch.empty(self.vals.numel(), dtype=torch.float32, device=self.vals.device)
+        _capi.check(_capi.lib().dfx_csr_values_to_f32(C.byref(self.csr()), _ptr(v32), _stream()))
+        return MatrixCSR(self.row_ptr, self.cols, v32, self.bs, self.ncols)
+
+    def inverse_diagonal(self) -> torch.Tensor:
+        d = torch.empty(self.nrows * self.bs, dtype=torch.float64, device=self.vals.device)
+        _capi.check(_capi.lib().dfx_jacobi_inverse_diagonal(C.byref(self.csr()), _ptr(d),
+                                                            _stream()))
+        return d
+
+    def squared_norm(self) -> float:
+        return float((self.vals.double() ** 2).sum())
+
+    def to_scipy(self):
+        import scipy.sparse as sp
+
+        rp = self.row_ptr.cpu().numpy()
+        cols = self.cols.cpu().numpy()
+        vals = self.vals.cpu().numpy()
+        if self.bs == 1:
+            return sp.csr_matrix((vals, cols, rp), shape=(self.nrows, self.ncols))
+        return sp.bsr_matrix((vals.reshape(-1, self.bs, self.bs), cols, rp),
+                             shape=(self.nrows * self.bs, self.ncols * self.bs))
+
+
+class Vector:
+    """la::Vector on the device: ``array`` is a torch tensor."""
+
+    def __init__(self, array: torch.Tensor, bs: int = 1):
+        self.array = array
+        self.bs = bs
+
+    def scatter_forward(self):  # one rank: no ghosts
+        pass
+
+    def scatter_reverse(self, *args):  # one rank: no ghosts
+        pass
+
+
+def inner_product(a: torch.Tensor, b: torch.Tensor) -> float:
+    """la::inner_product (deterministic two-stage device reduction)."""
+    n = a.numel()
+    wb = _capi.lib().dfx_inner_product_workspace_bytes(n)
+    work = torch.empty(int(wb) // 8 + 1, dtype=torch.float64, device=a.device)
+    out = C.c_double(0.0)
+    _capi.check(_capi.lib().dfx_inner_product(_ptr(a), _ptr(b), n, _ptr(work), wb, C.byref(out),
+                                              _stream()))
+    return out.value
+
+
+def squared_norm(a: torch.Tensor) -> float:
+    return inner_product(a, a)
+
+
+def norm(a: torch.Tensor) -> float:
+    return float(np.sqrt(squared_norm(a)))
+
+
+@dataclass
+class CGResult:
+    iterations: int
+    status: int
+    rnorm0_sq: float
+    rnorm_sq: float
+
+
+class CGSolver:
+    """Jacobi-preconditioned CG on a device CSR matrix, FP64 (graph-captured
+    iterations; workspace allocated once and reused)."""
+
+    def __init__(self, A: MatrixCSR, jacobi: bool = True, graph_iters: int = 20):
+        assert A.dtype == torch.float64
+        self.A = A
+        self.n = A.nrows * A.bs
+        self.dinv = A.inverse_diagonal() if jacobi else None
+        wb = int(_capi.lib().dfx_cg_workspace_bytes(self.n))
+        self.work = torch.empty(wb, dtype=torch.uint8, device=A.vals.device)
+        self.graph_iters = graph_iters
+
+    def refresh_preconditioner(self):
+        if self.dinv is not None:
+            _capi.check(_capi.lib().dfx_jacobi_inverse_diagonal(C.byref(self.A.csr()),
+                                                                _ptr(self.dinv), _stream()))
+
+    def solve(self, b: torch.Tensor, x: torch.Tensor, rtol: float = 1e-10,
+              max_iters: int = 100000, raise_on_fail: bool = True) -> CGResult:
+        info = _capi.CgInfo()
+        rc = _capi.lib().dfx_cg_solve(C.byref(self.A.csr()), _ptr(b), _ptr(x), _ptr(self.dinv),
+                                      float(rtol), int(max_iters), int(self.graph_iters),
+                                      _ptr(self.work), self.work.numel(), C.byref(info), _stream())
+        if raise_on_fail:
+            _capi.check(rc)
+        return CGResult(info.iterations, info.status, info.rnorm0_sq, info.rnorm_sq)
+
+
+def cg(A: MatrixCSR, b: torch.Tensor, x: torch.Tensor | None = None, rtol: float = 1e-10,
+       max_iters: int = 100000, jacobi: bool = True):
+    """Solve A x = b; returns (x, CGResult)."""
+    if x is None:
+        x = torch.zeros_like(b)
+    res = CGSolver(A, jacobi=jacobi).solve(b, x, rtol, max_iters)
+    return x, res

@@ -1,0 +1,64 @@
+"""Mesh creation, mirroring ``dolfinx.mesh.create_box`` / ``create_unit_cube``
+for tetrahedral boxes (cpp/dolfinx/mesh/generation.h:104-134, 380-426).
+
+The cells are RCM-reordered and the geometry nodes numbered exactly as
+DOLFINx does on one rank; the work runs in the host part of libdfxgpu.
+"""
+
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _capi
+
+
+class CellType:
+    tetrahedron = "tetrahedron"
+
+
+@dataclass
+class Mesh:
+    """Tetrahedral mesh: ``cells`` (nc, 4) geometry node indices, ``x`` (nv, 3)."""
+
+    cells: np.ndarray
+    x: np.ndarray
+    _dev: dict = field(default_factory=dict, repr=False)
+
+    @property
+    def num_cells(self) -> int:
+        return int(self.cells.shape[0])
+
+    @property
+    def num_nodes(self) -> int:
+        return int(self.x.shape[0])
+
+    def device(self, device="cuda"):
+        """(x_dofmap, x) as device tensors (cached)."""
+        import torch
+
+        key = str(device)
+        if key not in self._dev:
+            self._dev[key] = (torch.from_numpy(self.cells).to(device),
+                              torch.from_numpy(self.x).to(device))
+        return self._dev[key]
+
+
+def create_box(points, n, cell_type=CellType.tetrahedron, reorder: bool = True) -> Mesh:
+    if cell_type != CellType.tetrahedron:
+        raise ValueError("only tetrahedral boxes are on the GPU hot path")
+    nx, ny, nz = (int(v) for v in n)
+    p0 = np.ascontiguousarray(points[0], np.float64)
+    p1 = np.ascontiguousarray(points[1], np.float64)
+    nc = 6 * nx * ny * nz
+    nv = (nx + 1) * (ny + 1) * (nz + 1)
+    cells = np.empty((nc, 4), np.int32)
+    x = np.empty((nv, 3), np.float64)
+    _capi.check(_capi.lib().dfx_mesh_create_box_tet(nx, ny, nz, p0.ctypes.data, p1.ctypes.data,
+                                                    int(reorder), cells.ctypes.data, x.ctypes.data))
+    return Mesh(cells, x)
+
+
+def create_unit_cube(nx, ny, nz, cell_type=CellType.tetrahedron, reorder: bool = True) -> Mesh:
+    return create_box(((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)), (nx, ny, nz), cell_type, reorder)

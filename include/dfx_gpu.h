@@ -1,0 +1,237 @@
+/* dfx_gpu.h -- C ABI of the GB300 (sm_103a) FEM assembly + CG hot path.
+ *
+ * libdfxgpu.so replaces, behind DOLFINx's own C++ API, the cell loops of
+ * fem::assemble_matrix / fem::assemble_vector, fem::apply_lifting,
+ * DirichletBC::set, set_diagonal, MatrixCSR::mult and the CG iteration of
+ * the matrix-free Poisson demo. Every entry point takes plain pointers and
+ * sizes and returns an int status (DFX_OK == 0); dfx_last_error() gives the
+ * message of the last failure on the calling thread. Pointers named d_*
+ * are device pointers; `stream` is a cudaStream_t (NULL = default stream).
+ * Arrays are caller-owned; nothing is freed by the library.
+ *
+ * Paths cited below are relative to the DOLFINx source tree.
+ */
+#ifndef DFX_GPU_H
+#define DFX_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+enum dfx_status
+{
+  DFX_OK = 0,
+  DFX_ERR_INVALID = 1,           /* bad argument or size mismatch */
+  DFX_ERR_CUDA = 2,              /* CUDA runtime error */
+  DFX_ERR_NOT_IN_SPARSITY = 3,   /* "Entry not in sparsity" (la/matrix_csr_impl.h:93-94) */
+  DFX_ERR_NOT_CONVERGED = 4,     /* CG hit its iteration cap */
+  DFX_ERR_TIMEOUT = 5,           /* a bounded device wait gave up */
+  DFX_ERR_NO_MEMORY = 6,         /* workspace too small / HBM budget exceeded */
+  DFX_ERR_BREAKDOWN = 7,         /* CG breakdown (p.Ap <= 0 or NaN) */
+  DFX_ERR_UNSUPPORTED = 8
+};
+
+/* Message of the last failing call on this thread ("" if none). */
+const char* dfx_last_error(void);
+int dfx_abi_version(void);
+
+/* ---------------------------------------------------------------- types */
+enum dfx_form_kind
+{
+  /* a(u,v) = \int kappa grad u . grad v + k2 u v dx, Lagrange P1/P2 tets */
+  DFX_FORM_POISSON = 0,
+  /* a(u,v) = \int 2 mu eps(u):eps(v) + lambda div u div v, vector P2, bs 3,
+     mu, lambda from a per-cell Young's modulus E (kappa) and nu */
+  DFX_FORM_ELASTICITY = 1,
+  /* L(v) = \int f v dx, f a P1 coefficient on the geometry nodes (f == NULL:
+     f = f_const[0]) */
+  DFX_FORM_SOURCE = 2,
+  /* L(v) = \int f . v dx, f = f_const (vector P2, bs 3) */
+  DFX_FORM_BODYFORCE = 3
+};
+
+enum dfx_assembly_mode
+{
+  DFX_MODE_ATOMIC = 0,   /* FP64 atomic scatter, one launch */
+  DFX_MODE_COLOURED = 1  /* cells grouped by colour, plain adds: deterministic */
+};
+
+enum dfx_dtype
+{
+  DFX_F64 = 0,
+  DFX_F32 = 1
+};
+
+/* A form on a tetrahedral mesh, all arrays on the device.
+ * Replaces fem::Form + the FFCx kernel of its cell integral
+ * (fem/Form.h:116-668, fem/kernel.h:18-27): the element kernel is chosen
+ * by `kind`, the coefficients are packed per cell (fem/pack.h:77-176). */
+typedef struct dfx_form
+{
+  int32_t kind;            /* dfx_form_kind */
+  int32_t degree;          /* 1 or 2 (elasticity/body force: 2) */
+  int32_t num_cells;
+  int32_t num_nodes;       /* rows of x */
+  const int32_t* x_dofmap; /* (num_cells, 4) geometry dofmap */
+  const double* x;         /* (num_nodes, 3) coordinates */
+  const int32_t* dofmap;   /* (num_cells, ndofs) node (block) indices */
+  const double* kappa;     /* per-cell kappa / E, or NULL -> kappa_const */
+  double kappa_const;
+  double k2;               /* Helmholtz mass coefficient (scalar bilinear) */
+  double nu;               /* Poisson ratio (elasticity) */
+  const double* f;         /* P1 source values per geometry node, or NULL */
+  double f_const[3];
+} dfx_form;
+
+/* A CSR matrix with square bs x bs blocks on the device, the storage of
+ * la::MatrixCSR (la/MatrixCSR.h:67-70): row_ptr int64 (nrows+1), cols
+ * int32 (nnz, sorted per row), vals nnz*bs*bs, blocks row-major. */
+typedef struct dfx_csr
+{
+  int32_t nrows;  /* block rows */
+  int32_t ncols;  /* block columns */
+  int32_t bs;     /* 1 or 3 */
+  int32_t dtype;  /* dfx_dtype of vals */
+  int64_t nnz;    /* blocks */
+  const int64_t* row_ptr;
+  const int32_t* cols;
+  void* vals;
+} dfx_csr;
+
+/* ---------------------------------------------------------- host set-up
+ * One-time structure built on the host CPU. Results are bit-identical to
+ * DOLFINx on one rank. */
+
+/* mesh::create_box(tetrahedron) with the default RCM cell reordering
+ * (mesh/generation.h:104-134, 380-426; mesh/utils.h:232-310;
+ * graph/ordering.cpp:148-170). cells: (6 nx ny nz, 4) geometry node
+ * indices; x: ((nx+1)(ny+1)(nz+1), 3). reorder = 0 keeps build order. */
+int dfx_mesh_create_box_tet(int32_t nx, int32_t ny, int32_t nz, const double* p0,
+                            const double* p1, int32_t reorder, int32_t* cells,
+                            double* x);
+
+/* fem::create_dofmap for Lagrange P1/P2 on tetrahedra
+ * (fem/utils.cpp:32-76, fem/dofmapbuilder.cpp:153-710). dofmap:
+ * (num_cells, 4 or 10). Returns the number of dof nodes in *num_nodes. */
+int dfx_dofmap_create_tet(int32_t num_cells, const int32_t* cells, int32_t degree,
+                          int32_t* dofmap, int32_t* num_nodes);
+
+/* fem::create_sparsity_pattern + SparsityPattern::finalize
+ * (fem/utils.h:197-314, la/SparsityPattern.cpp:264-491) for a cell integral
+ * with the same dofmap on both sides. Two-phase: call with cols == NULL to
+ * get *nnz and row_ptr (nrows+1), then again with cols (nnz). */
+int dfx_sparsity_create(int32_t nrows, int32_t num_cells, int32_t ndofs,
+                        const int32_t* dofmap, int64_t* row_ptr, int32_t* cols,
+                        int64_t* nnz);
+
+/* Greedy cell colouring for DFX_MODE_COLOURED: no two cells of one colour
+ * share a dof. order: (num_cells) cells grouped by colour, offsets:
+ * (max_colours+1). Returns the colour count in *num_colours. */
+int dfx_colour_cells(int32_t num_cells, int32_t ndofs, const int32_t* dofmap,
+                     int32_t num_nodes, int32_t* order, int32_t* offsets,
+                     int32_t max_colours, int32_t* num_colours);
+
+/* ------------------------------------------------------------- assembly */
+
+/* Bytes of the cell -> CSR slot map (one byte per element entry). */
+size_t dfx_slot_map_bytes(const dfx_form* a);
+
+/* Cell -> CSR slot map, built once from the sparsity pattern: for cell c
+ * and local dofs (i, j), d_map[(c*nd + i)*nd + j] is the position of
+ * dofmap[c,j] within row dofmap[c,i]. Fails with DFX_ERR_NOT_IN_SPARSITY
+ * when an entry is missing, DFX_ERR_UNSUPPORTED when a row is longer
+ * than 255. Replaces the per-entry std::lower_bound of insert_csr
+ * (la/matrix_csr_impl.h:86-94). */
+int dfx_slot_map_create(const dfx_form* a, const dfx_csr* A, uint8_t* d_map,
+                        void* stream);
+
+/* fem::assemble_matrix (fem/assembler.h:513-602;
+ * fem/assemble_matrix_impl.h:92-200): A += sum_cells Ae, rows and
+ * columns of constrained dofs (d_bc[bs*node+k] != 0) zeroed in Ae.
+ * d_map from dfx_slot_map_create, or NULL to search the row.
+ * DFX_MODE_COLOURED needs d_order/colour_offsets (host array) from
+ * dfx_colour_cells (uploaded order). A is accumulated, not zeroed. */
+int dfx_assemble_matrix(const dfx_form* a, const dfx_csr* A, const uint8_t* d_map,
+                        const int8_t* d_bc, int32_t mode, const int32_t* d_order,
+                        const int32_t* colour_offsets, int32_t num_colours,
+                        void* stream);
+
+/* fem::assemble_vector (fem/assembler.h:229-257;
+ * fem/assemble_vector_impl.h:75-116): b += sum_cells be. */
+int dfx_assemble_vector(const dfx_form* L, double* d_b, int32_t mode,
+                        const int32_t* d_order, const int32_t* colour_offsets,
+                        int32_t num_colours, void* stream);
+
+/* fem::apply_lifting for one bilinear form (fem/assembler.h:341-421;
+ * fem/assemble_vector_impl.h:361-414): for cells with a constrained
+ * column, b[r] -= Ae[r,c] * alpha * (g[c] - x0[c]). d_x0 may be NULL. */
+int dfx_apply_lifting(const dfx_form* a, double* d_b, const int8_t* d_bc,
+                      const double* d_g, const double* d_x0, double alpha,
+                      int32_t mode, const int32_t* d_order,
+                      const int32_t* colour_offsets, int32_t num_colours,
+                      void* stream);
+
+/* DirichletBC::set (fem/DirichletBC.h:495-578): x[dofs[i]] =
+ * alpha * (g - x0) with g = d_g[dofs[i]] (or g_const when d_g is NULL);
+ * dofs >= n are skipped. */
+int dfx_set_bc(double* d_x, int64_t n, const int32_t* d_dofs, int32_t ndofs,
+               const double* d_g, double g_const, const double* d_x0,
+               double alpha, void* stream);
+
+/* set_diagonal (fem/assembler.h:644-686) through MatrixCSR::set:
+ * A[d, d] = diagonal for each constrained scalar dof d. */
+int dfx_set_diagonal(const dfx_csr* A, const int32_t* d_dofs, int32_t ndofs,
+                     double diagonal, void* stream);
+
+/* --------------------------------------------------------- linear algebra */
+
+/* MatrixCSR::mult (la/MatrixCSR.h:877-946; la/matrix_csr_impl.h:259-286):
+ * y = beta*y + A x, beta in {0, 1} (1 = the reference's y += A x).
+ * dtype of x/y equals A->dtype. */
+int dfx_spmv(const dfx_csr* A, const void* d_x, void* d_y, double beta,
+             void* stream);
+
+/* Cast of MatrixCSR values to float (la/MatrixCSR.h:223-237). */
+int dfx_csr_values_to_f32(const dfx_csr* A, float* d_vals32, void* stream);
+
+/* d_dinv[i] = 1 / A_ii (Jacobi), scalar rows of a bs-blocked matrix. */
+int dfx_jacobi_inverse_diagonal(const dfx_csr* A, double* d_dinv, void* stream);
+
+/* la::inner_product (la/Vector.h:434-460), deterministic two-stage
+ * reduction; the result is written to *result (host). */
+size_t dfx_inner_product_workspace_bytes(int64_t n);
+int dfx_inner_product(const double* d_a, const double* d_b, int64_t n,
+                      void* d_work, size_t work_bytes, double* result,
+                      void* stream);
+
+/* ------------------------------------------------------------------ CG */
+typedef struct dfx_cg_info
+{
+  int32_t iterations;
+  int32_t status;       /* DFX_OK, DFX_ERR_NOT_CONVERGED, DFX_ERR_BREAKDOWN */
+  double rnorm0_sq;     /* |r0|^2 */
+  double rnorm_sq;      /* |r_k|^2 */
+} dfx_cg_info;
+
+/* Workspace of dfx_cg_solve for n scalar unknowns. */
+size_t dfx_cg_workspace_bytes(int64_t n);
+
+/* Jacobi-preconditioned CG (the demo's CG, cpp/demo/poisson_matrix_free/
+ * main.cpp:84-132, with z = D^{-1} r; d_dinv == NULL gives plain CG).
+ * Stops when |r|^2 / |r0|^2 < rtol^2. d_x holds the initial guess. FP64
+ * throughout. The iteration runs as a CUDA graph of `graph_iters`
+ * iterations (0: default) with device-side convergence tests. */
+int dfx_cg_solve(const dfx_csr* A, const double* d_b, double* d_x,
+                 const double* d_dinv, double rtol, int32_t max_iters,
+                 int32_t graph_iters, void* d_work, size_t work_bytes,
+                 dfx_cg_info* info, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DFX_GPU_H */

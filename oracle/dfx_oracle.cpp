@@ -1,0 +1,898 @@
+// CPU oracle for the DOLFINx assembly + CG hot path.
+//
+// TEST INFRASTRUCTURE ONLY. This file is the checker for the GPU path:
+// only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg
+// load it. The product library (libdfxgpu.so) never links or calls it.
+//
+// It is a plain, sequential restatement of the reference algorithms,
+// each function citing the reference file:line it follows (paths are
+// relative to the DOLFINx source tree). Element kernels, which DOLFINx
+// takes from FFCx-generated code that is not part of the reference tree,
+// are restated from the finite-element mathematics: Lagrange P1/P2 on the
+// Basix reference tetrahedron, integrated with a collapsed (Duffy) Gauss
+// product rule that is exact for every integrand used here.
+//
+// Pinned against: the reference's own graph/ordering.cpp (RCM),
+// common/sort.h (facet sort), la/matrix_csr_impl.h (insert_csr, spmv),
+// compiled from the reference sources into oracle/_ref/ and frozen as
+// golden vectors under tests/golden/.
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <numeric>
+#include <unordered_map>
+#include <vector>
+
+namespace
+{
+
+enum
+{
+  ORC_OK = 0,
+  ORC_ERR_INVALID = 1,
+  ORC_ERR_NOT_IN_SPARSITY = 3,
+  ORC_ERR_NOT_CONVERGED = 4,
+};
+
+// Basix reference tetrahedron sub-entities (vertex indices).
+// Edges: basix cell topology of tetrahedron, dim 1; facets: dim 2.
+const int kTetEdges[6][2] = {{2, 3}, {1, 3}, {1, 2}, {0, 3}, {0, 2}, {0, 1}};
+const int kTetFacets[4][3] = {{1, 2, 3}, {0, 2, 3}, {0, 1, 3}, {0, 1, 2}};
+
+//---------------------------------------------------------------------------
+// Quadrature
+//---------------------------------------------------------------------------
+
+// Gauss-Legendre rule with m points on [0, 1] (Newton on P_m).
+void gauss_legendre01(int m, std::vector<double>& x, std::vector<double>& w)
+{
+  x.resize(m);
+  w.resize(m);
+  for (int i = 0; i < m; ++i)
+  {
+    double z = std::cos(M_PI * (i + 0.75) / (m + 0.5));
+    for (int it = 0; it < 100; ++it)
+    {
+      double p0 = 1.0, p1 = z;
+      for (int k = 2; k <= m; ++k)
+      {
+        double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+        p0 = p1;
+        p1 = p2;
+      }
+      double dp = m * (z * p1 - p0) / (z * z - 1.0);
+      double dz = p1 / dp;
+      z -= dz;
+      if (std::abs(dz) < 1e-16)
+        break;
+    }
+    double p0 = 1.0, p1 = z;
+    for (int k = 2; k <= m; ++k)
+    {
+      double p2 = ((2.0 * k - 1.0) * z * p1 - (k - 1.0) * p0) / k;
+      p0 = p1;
+      p1 = p2;
+    }
+    double dp = m * (z * p1 - p0) / (z * z - 1.0);
+    x[i] = 0.5 * (1.0 - z);
+    w[i] = 1.0 / ((1.0 - z * z) * dp * dp);
+  }
+}
+
+// Collapsed product rule on the reference tetrahedron
+// {X,Y,Z >= 0, X+Y+Z <= 1}: X = u, Y = v(1-u), Z = w(1-u)(1-v).
+// With m points per direction it integrates polynomials of total
+// degree <= 2m-3 exactly.
+struct TetQuad
+{
+  std::vector<double> X; // (nq, 3)
+  std::vector<double> w;
+};
+
+TetQuad tet_quadrature(int m)
+{
+  std::vector<double> g, gw;
+  gauss_legendre01(m, g, gw);
+  TetQuad q;
+  for (int a = 0; a < m; ++a)
+    for (int b = 0; b < m; ++b)
+      for (int c = 0; c < m; ++c)
+      {
+        double u = g[a], v = g[b], s = g[c];
+        q.X.push_back(u);
+        q.X.push_back(v * (1.0 - u));
+        q.X.push_back(s * (1.0 - u) * (1.0 - v));
+        q.w.push_back(gw[a] * gw[b] * gw[c] * (1.0 - u) * (1.0 - u) * (1.0 - v));
+      }
+  return q;
+}
+
+//---------------------------------------------------------------------------
+// Lagrange basis on the reference tetrahedron (Basix dof ordering:
+// vertices 0..3, then one dof per edge in kTetEdges order).
+//---------------------------------------------------------------------------
+void tabulate_tet(int degree, const double* X, double* phi, double (*dphi)[3])
+{
+  const double l[4] = {1.0 - X[0] - X[1] - X[2], X[0], X[1], X[2]};
+  const double dl[4][3]
+      = {{-1.0, -1.0, -1.0}, {1.0, 0.0, 0.0}, {0.0, 1.0, 0.0}, {0.0, 0.0, 1.0}};
+  if (degree == 1)
+  {
+    for (int i = 0; i < 4; ++i)
+    {
+      phi[i] = l[i];
+      for (int k = 0; k < 3; ++k)
+        dphi[i][k] = dl[i][k];
+    }
+    return;
+  }
+  for (int i = 0; i < 4; ++i)
+  {
+    phi[i] = l[i] * (2.0 * l[i] - 1.0);
+    for (int k = 0; k < 3; ++k)
+      dphi[i][k] = (4.0 * l[i] - 1.0) * dl[i][k];
+  }
+  for (int e = 0; e < 6; ++e)
+  {
+    const int a = kTetEdges[e][0], b = kTetEdges[e][1];
+    phi[4 + e] = 4.0 * l[a] * l[b];
+    for (int k = 0; k < 3; ++k)
+      dphi[4 + e][k] = 4.0 * (l[a] * dl[b][k] + l[b] * dl[a][k]);
+  }
+}
+
+int tet_ndofs(int degree) { return degree == 1 ? 4 : 10; }
+
+// Affine P1 coordinate map: J_ij = dx_i/dX_j, K = J^{-1}.
+double tet_geometry(const double* c, double J[3][3], double K[3][3])
+{
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j)
+      J[i][j] = c[3 * (j + 1) + i] - c[i];
+  const double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1])
+                     - J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0])
+                     + J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+  K[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) / det;
+  K[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / det;
+  K[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / det;
+  K[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) / det;
+  K[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / det;
+  K[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / det;
+  K[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) / det;
+  K[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / det;
+  K[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
+  return det;
+}
+
+const TetQuad& quad_for_tets()
+{
+  static const TetQuad q = tet_quadrature(4); // exact to degree 5
+  return q;
+}
+
+// Symmetric 4-point rule, exact to degree 2 (barycentric (a,b,b,b) and
+// permutations, a = (5+3 sqrt 5)/20, b = (5-sqrt 5)/20, weights 1/24):
+// the rule a degree-2 integrand (stiffness, elasticity, P2 load) gets.
+const TetQuad& quad_degree2()
+{
+  static const TetQuad q = []
+  {
+    TetQuad r;
+    const double a = (5.0 + 3.0 * std::sqrt(5.0)) / 20.0, b = (5.0 - std::sqrt(5.0)) / 20.0;
+    for (int p = 0; p < 4; ++p)
+    {
+      double l[4] = {b, b, b, b};
+      l[p] = a;
+      r.X.insert(r.X.end(), {l[1], l[2], l[3]});
+      r.w.push_back(1.0 / 24.0);
+    }
+    return r;
+  }();
+  return q;
+}
+
+// Physical gradients g_i = K^T dphi_i.
+void push_forward(int nd, const double K[3][3], const double (*dphi)[3],
+                  double (*g)[3])
+{
+  for (int i = 0; i < nd; ++i)
+    for (int k = 0; k < 3; ++k)
+      g[i][k] = K[0][k] * dphi[i][0] + K[1][k] * dphi[i][1] + K[2][k] * dphi[i][2];
+}
+
+//---------------------------------------------------------------------------
+// Element kernels (stand-ins for the FFCx tabulate_tensor ABI of
+// cpp/dolfinx/fem/kernel.h:18-27: Ae row-major, coords 3 per node).
+//---------------------------------------------------------------------------
+
+// a(u, v) = \int kappa grad u . grad v + k2 u v dx on a P1/P2 tetrahedron.
+void kernel_poisson(int degree, double* Ae, double kappa, double k2,
+                    const double* coords)
+{
+  const int nd = tet_ndofs(degree);
+  double J[3][3], K[3][3];
+  const double adet = std::abs(tet_geometry(coords, J, K));
+  // Stiffness alone has degree 2(p-1) <= 2; the mass term needs degree 2p.
+  const TetQuad& q = k2 == 0.0 ? quad_degree2() : quad_for_tets();
+  double phi[10], dphi[10][3], g[10][3];
+  for (std::size_t p = 0; p < q.w.size(); ++p)
+  {
+    tabulate_tet(degree, &q.X[3 * p], phi, dphi);
+    push_forward(nd, K, dphi, g);
+    const double wq = q.w[p] * adet;
+    for (int i = 0; i < nd; ++i)
+      for (int j = 0; j < nd; ++j)
+        Ae[i * nd + j] += wq
+                          * (kappa * (g[i][0] * g[j][0] + g[i][1] * g[j][1]
+                                      + g[i][2] * g[j][2])
+                             + k2 * phi[i] * phi[j]);
+  }
+}
+
+// L(v) = \int f v dx, f a P1 coefficient given by its 4 vertex values.
+void kernel_source(int degree, double* be, const double* f,
+                   const double* coords)
+{
+  const int nd = tet_ndofs(degree);
+  double J[3][3], K[3][3];
+  const double adet = std::abs(tet_geometry(coords, J, K));
+  // integrand degree p + 1 <= 3: collapsed rule with 3 points per direction
+  static const TetQuad q3 = tet_quadrature(3);
+  const TetQuad& q = q3;
+  double phi[10], dphi[10][3], l[4], dl[4][3];
+  for (std::size_t p = 0; p < q.w.size(); ++p)
+  {
+    tabulate_tet(degree, &q.X[3 * p], phi, dphi);
+    tabulate_tet(1, &q.X[3 * p], l, dl);
+    const double fq = f[0] * l[0] + f[1] * l[1] + f[2] * l[2] + f[3] * l[3];
+    for (int i = 0; i < nd; ++i)
+      be[i] += q.w[p] * adet * fq * phi[i];
+  }
+}
+
+// Linear elasticity, vector P2 (bs = 3, interleaved dofs 3*i + k):
+// a(u, v) = \int 2 mu eps(u):eps(v) + lambda div u div v dx.
+void kernel_elasticity(double* Ae, double E, double nu, const double* coords)
+{
+  const double mu = E / (2.0 * (1.0 + nu));
+  const double lmbda = E * nu / ((1.0 + nu) * (1.0 - 2.0 * nu));
+  double J[3][3], K[3][3];
+  const double adet = std::abs(tet_geometry(coords, J, K));
+  const TetQuad& q = quad_degree2();
+  double phi[10], dphi[10][3], g[10][3];
+  const int n = 30;
+  for (std::size_t p = 0; p < q.w.size(); ++p)
+  {
+    tabulate_tet(2, &q.X[3 * p], phi, dphi);
+    push_forward(10, K, dphi, g);
+    const double wq = q.w[p] * adet;
+    for (int i = 0; i < 10; ++i)
+      for (int j = 0; j < 10; ++j)
+      {
+        const double gg = g[i][0] * g[j][0] + g[i][1] * g[j][1] + g[i][2] * g[j][2];
+        for (int k = 0; k < 3; ++k)
+          for (int l = 0; l < 3; ++l)
+            Ae[(3 * i + k) * n + 3 * j + l]
+                += wq * (mu * ((k == l ? gg : 0.0) + g[i][l] * g[j][k])
+                         + lmbda * g[i][k] * g[j][l]);
+      }
+  }
+}
+
+// L(v) = \int f . v dx with a constant vector f, vector P2.
+void kernel_bodyforce(double* be, const double* f, const double* coords)
+{
+  double J[3][3], K[3][3];
+  const double adet = std::abs(tet_geometry(coords, J, K));
+  const TetQuad& q = quad_degree2();
+  double phi[10], dphi[10][3];
+  for (std::size_t p = 0; p < q.w.size(); ++p)
+  {
+    tabulate_tet(2, &q.X[3 * p], phi, dphi);
+    for (int i = 0; i < 10; ++i)
+      for (int k = 0; k < 3; ++k)
+        be[3 * i + k] += q.w[p] * adet * f[k] * phi[i];
+  }
+}
+
+//---------------------------------------------------------------------------
+// Mesh ordering helpers
+//---------------------------------------------------------------------------
+
+// Level structure rooted at s (cpp/dolfinx/graph/ordering.cpp:23-60).
+void level_structure(const int32_t* off, const int32_t* adj, int n, int s,
+                     std::vector<int>& ls, std::vector<int>& loff)
+{
+  std::vector<char> seen(n, 0);
+  seen[s] = 1;
+  ls.assign(1, s);
+  loff.assign(1, 0);
+  int l = 0;
+  while ((int)ls.size() > loff.back())
+  {
+    loff.push_back(ls.size());
+    for (int i = loff[l]; i < loff[l + 1]; ++i)
+    {
+      const int node = ls[i];
+      for (int k = off[node]; k < off[node + 1]; ++k)
+      {
+        const int w = adj[k];
+        if (!seen[w])
+        {
+          ls.push_back(w);
+          seen[w] = 1;
+        }
+      }
+    }
+    ++l;
+  }
+}
+
+} // namespace
+
+extern "C"
+{
+
+//---------------------------------------------------------------------------
+// Mesh: box of tetrahedra (cpp/dolfinx/mesh/generation.h:332-426)
+//---------------------------------------------------------------------------
+
+// Original (unordered) cells and vertex coordinates of the Kuhn split:
+// create_geom (generation.h:332-377) and build_tet (generation.h:380-426).
+int orc_box_tet_raw(int nx, int ny, int nz, const double* p0, const double* p1,
+                    int64_t* cells, double* x)
+{
+  if (nx < 1 || ny < 1 || nz < 1)
+    return ORC_ERR_INVALID;
+  const double ext[3] = {(p1[0] - p0[0]) / nx, (p1[1] - p0[1]) / ny,
+                         (p1[2] - p0[2]) / nz};
+  const int64_t sqxy = (int64_t)(nx + 1) * (ny + 1);
+  const int64_t npts = sqxy * (nz + 1);
+  for (int64_t v = 0; v < npts; ++v)
+  {
+    const int64_t p = v % sqxy;
+    const int64_t idx[3] = {p % (nx + 1), p / (nx + 1), v / sqxy};
+    for (int i = 0; i < 3; ++i)
+      x[3 * v + i] = p0[i] + (double)idx[i] * ext[i];
+  }
+  const int64_t nhex = (int64_t)nx * ny * nz;
+  for (int64_t i = 0; i < nhex; ++i)
+  {
+    const int64_t iz = i / ((int64_t)nx * ny);
+    const int64_t j = i % ((int64_t)nx * ny);
+    const int64_t iy = j / nx, ix = j % nx;
+    const int64_t v0 = iz * sqxy + iy * (nx + 1) + ix;
+    const int64_t v1 = v0 + 1, v2 = v0 + (nx + 1), v3 = v1 + (nx + 1);
+    const int64_t v4 = v0 + sqxy, v5 = v1 + sqxy, v6 = v2 + sqxy, v7 = v3 + sqxy;
+    const int64_t t[24] = {v0, v1, v3, v7, v0, v1, v7, v5, v0, v5, v7, v4,
+                           v0, v3, v2, v7, v0, v6, v4, v7, v0, v2, v6, v7};
+    std::memcpy(cells + 24 * i, t, sizeof(t));
+  }
+  return ORC_OK;
+}
+
+// Facet-connected dual graph of a tetrahedral mesh, serial path of
+// build_local_dual_graph (cpp/dolfinx/mesh/graphbuild.cpp:566-905):
+// facets as sorted vertex triples, a stable lexicographic sort, one
+// edge per matched pair, both directions filled in edge order.
+// offsets has nc+1 entries; adj must hold 4*nc entries.
+int orc_dual_graph_tet(int nc, const int64_t* cells, int32_t* offsets,
+                       int32_t* adj)
+{
+  const int64_t nf = 4 * (int64_t)nc;
+  std::vector<int64_t> key(3 * nf);
+  for (int c = 0; c < nc; ++c)
+    for (int f = 0; f < 4; ++f)
+    {
+      int64_t v[3];
+      for (int k = 0; k < 3; ++k)
+        v[k] = cells[4 * (int64_t)c + kTetFacets[f][k]];
+      std::sort(v, v + 3);
+      for (int k = 0; k < 3; ++k)
+        key[3 * (4 * (int64_t)c + f) + k] = v[k];
+    }
+  std::vector<int32_t> perm(nf);
+  std::iota(perm.begin(), perm.end(), 0);
+  std::stable_sort(perm.begin(), perm.end(),
+                   [&](int32_t a, int32_t b)
+                   {
+                     for (int k = 0; k < 3; ++k)
+                       if (key[3 * a + k] != key[3 * b + k])
+                         return key[3 * a + k] < key[3 * b + k];
+                     return false;
+                   });
+  std::vector<std::pair<int32_t, int32_t>> edges;
+  for (int64_t i = 0; i < nf;)
+  {
+    int64_t j = i + 1;
+    while (j < nf && key[3 * perm[j]] == key[3 * perm[i]]
+           && key[3 * perm[j] + 1] == key[3 * perm[i] + 1]
+           && key[3 * perm[j] + 2] == key[3 * perm[i] + 2])
+      ++j;
+    for (int64_t a = i; a < j; ++a)
+      for (int64_t b = a + 1; b < j; ++b)
+        edges.push_back({perm[a] / 4, perm[b] / 4});
+    i = j;
+  }
+  std::vector<int32_t> cnt(nc, 0);
+  for (auto& e : edges)
+  {
+    ++cnt[e.first];
+    ++cnt[e.second];
+  }
+  offsets[0] = 0;
+  for (int c = 0; c < nc; ++c)
+    offsets[c + 1] = offsets[c] + cnt[c];
+  std::vector<int32_t> pos(offsets, offsets + nc);
+  for (auto& e : edges)
+  {
+    adj[pos[e.first]++] = e.second;
+    adj[pos[e.second]++] = e.first;
+  }
+  return ORC_OK;
+}
+
+// Reverse Cuthill-McKee (cpp/dolfinx/graph/ordering.cpp:66-170).
+// r[old] = new position.
+int orc_reorder_rcm(int n, const int32_t* off, const int32_t* adj, int32_t* r)
+{
+  std::fill(r, r + n, -1);
+  auto deg = [&](int a) { return off[a + 1] - off[a]; };
+  auto cmp = [&](int a, int b) { return deg(a) < deg(b); };
+  int count = 0;
+  std::vector<int> ls, loff, ls2, loff2;
+  while (count < n)
+  {
+    int v = 0, dmin = INT32_MAX;
+    for (int i = 0; i < n; ++i)
+      if (r[i] == -1 && deg(i) < dmin)
+      {
+        v = i;
+        dmin = deg(i);
+      }
+    level_structure(off, adj, n, v, ls, loff);
+    for (;;)
+    {
+      const int nl = (int)loff.size() - 1;
+      auto b = ls.begin() + loff[nl - 1], e = ls.begin() + loff[nl];
+      const int s = *std::ranges::min_element(std::ranges::subrange(b, e), cmp);
+      level_structure(off, adj, n, s, ls2, loff2);
+      if (loff2.size() > loff.size())
+      {
+        v = s;
+        ls.swap(ls2);
+        loff.swap(loff2);
+      }
+      else
+        break;
+    }
+    std::vector<char> lab(n, 0);
+    std::vector<int> rv{v};
+    lab[v] = 1;
+    std::vector<int> nbr;
+    for (std::size_t cur = 0; cur < rv.size(); ++cur)
+    {
+      nbr.clear();
+      for (int k = off[rv[cur]]; k < off[rv[cur] + 1]; ++k)
+        if (!lab[adj[k]])
+        {
+          nbr.push_back(adj[k]);
+          lab[adj[k]] = 1;
+        }
+      std::ranges::sort(nbr, cmp);
+      rv.insert(rv.end(), nbr.begin(), nbr.end());
+    }
+    std::reverse(rv.begin(), rv.end());
+    for (int q : rv)
+      r[q] = count++;
+  }
+  return ORC_OK;
+}
+
+// Full mesh pipeline for create_box(tetrahedron) on one rank:
+// build_tet -> dual graph -> reorder_rcm -> cells permuted
+// (cpp/dolfinx/mesh/utils.h:280-308; reorder_list utils.h:57-71) ->
+// geometry nodes numbered by first appearance in the cell loop
+// (cpp/dolfinx/fem/dofmapbuilder.cpp:440-474 with no graph reordering,
+// create_geometry mesh/Geometry.h:235-311).
+// Outputs: cells (nc, 4) geometry node indices, x (nv, 3).
+int orc_create_box_tet(int nx, int ny, int nz, const double* p0,
+                       const double* p1, int reorder, int32_t* cells_out,
+                       double* x_out)
+{
+  const int64_t nc = 6 * (int64_t)nx * ny * nz;
+  const int64_t nv = (int64_t)(nx + 1) * (ny + 1) * (nz + 1);
+  std::vector<int64_t> cells(4 * nc);
+  std::vector<double> x(3 * nv);
+  int st = orc_box_tet_raw(nx, ny, nz, p0, p1, cells.data(), x.data());
+  if (st)
+    return st;
+  std::vector<int64_t> cells_new(cells);
+  if (reorder)
+  {
+    std::vector<int32_t> off(nc + 1), adj(4 * nc), r(nc);
+    orc_dual_graph_tet((int)nc, cells.data(), off.data(), adj.data());
+    orc_reorder_rcm((int)nc, off.data(), adj.data(), r.data());
+    for (int64_t c = 0; c < nc; ++c)
+      for (int k = 0; k < 4; ++k)
+        cells_new[4 * (int64_t)r[c] + k] = cells[4 * c + k];
+  }
+  std::vector<int32_t> node(nv, -1);
+  int32_t cnt = 0;
+  for (int64_t i = 0; i < 4 * nc; ++i)
+  {
+    int64_t v = cells_new[i];
+    if (node[v] < 0)
+      node[v] = cnt++;
+    cells_out[i] = node[v];
+  }
+  for (int64_t v = 0; v < nv; ++v)
+    for (int k = 0; k < 3; ++k)
+      x_out[3 * (int64_t)node[v] + k] = x[3 * v + k];
+  return ORC_OK;
+}
+
+//---------------------------------------------------------------------------
+// Dofmap: Lagrange P1/P2 on tetrahedra. Basic dofmap from the element
+// dof layout (cpp/dolfinx/fem/dofmapbuilder.cpp:153-397), then owned
+// dofs numbered by first appearance while iterating the cell dofmap
+// (dofmapbuilder.cpp:440-474). create_functionspace passes no reorder
+// function (cpp/dolfinx/fem/utils.h:925-950), so this is the final
+// numbering. Returns the number of dof nodes (blocks).
+//---------------------------------------------------------------------------
+int orc_dofmap_tet(int nc, const int32_t* cells, int degree, int32_t* dofmap)
+{
+  if (degree == 1)
+  {
+    std::unordered_map<int32_t, int32_t> id;
+    int32_t cnt = 0;
+    for (int64_t i = 0; i < 4 * (int64_t)nc; ++i)
+    {
+      auto [it, ins] = id.try_emplace(cells[i], cnt);
+      if (ins)
+        ++cnt;
+      dofmap[i] = it->second;
+    }
+    return cnt;
+  }
+  if (degree != 2)
+    return -1;
+  std::unordered_map<int64_t, int32_t> id;
+  int32_t cnt = 0;
+  for (int64_t c = 0; c < nc; ++c)
+  {
+    const int32_t* v = cells + 4 * c;
+    for (int i = 0; i < 10; ++i)
+    {
+      int64_t k;
+      if (i < 4)
+        k = v[i];
+      else
+      {
+        int64_t a = v[kTetEdges[i - 4][0]], b = v[kTetEdges[i - 4][1]];
+        if (a > b)
+          std::swap(a, b);
+        k = ((a + 1) << 32) | b; // distinct from vertex keys
+      }
+      auto [it, ins] = id.try_emplace(k, cnt);
+      if (ins)
+        ++cnt;
+      dofmap[10 * c + i] = it->second;
+    }
+  }
+  return cnt;
+}
+
+//---------------------------------------------------------------------------
+// Sparsity pattern: cell outer products (cpp/dolfinx/fem/sparsitybuild.cpp
+// :16-54), rows deduplicated and sorted (cpp/dolfinx/la/SparsityPattern.cpp
+// :264-491); one rank, so all columns are owned and in ascending order.
+// Call with cols == nullptr to get nnz; then again to fill.
+//---------------------------------------------------------------------------
+int64_t orc_sparsity(int nrows, int nc, int nd, const int32_t* dofmap,
+                     int64_t* row_ptr, int32_t* cols)
+{
+  std::vector<std::vector<int32_t>> rows(nrows);
+  for (int64_t c = 0; c < nc; ++c)
+    for (int i = 0; i < nd; ++i)
+      for (int j = 0; j < nd; ++j)
+        rows[dofmap[nd * c + i]].push_back(dofmap[nd * c + j]);
+  int64_t nnz = 0;
+  if (row_ptr)
+    row_ptr[0] = 0;
+  for (int r = 0; r < nrows; ++r)
+  {
+    auto& v = rows[r];
+    std::sort(v.begin(), v.end());
+    v.erase(std::unique(v.begin(), v.end()), v.end());
+    if (cols)
+      std::copy(v.begin(), v.end(), cols + nnz);
+    nnz += v.size();
+    if (row_ptr)
+      row_ptr[r + 1] = nnz;
+  }
+  return nnz;
+}
+
+//---------------------------------------------------------------------------
+// Element kernels, exposed for tests.
+//---------------------------------------------------------------------------
+void orc_kernel_poisson(int degree, double* Ae, double kappa, double k2,
+                        const double* coords)
+{
+  kernel_poisson(degree, Ae, kappa, k2, coords);
+}
+void orc_kernel_source(int degree, double* be, const double* f,
+                       const double* coords)
+{
+  kernel_source(degree, be, f, coords);
+}
+void orc_kernel_elasticity(double* Ae, double E, double nu, const double* coords)
+{
+  kernel_elasticity(Ae, E, nu, coords);
+}
+
+//---------------------------------------------------------------------------
+// Forms used on the hot path. kind: 0 = Poisson/Helmholtz (scalar P1/P2),
+// 1 = linear elasticity (vector P2, bs 3).
+//---------------------------------------------------------------------------
+struct orc_form
+{
+  int kind;
+  int degree;
+  const double* kappa; // per-cell coefficient (kappa or E); null -> 1
+  double k2;           // mass coefficient (Helmholtz), scalar forms
+  double nu;           // Poisson ratio, elasticity
+};
+
+// Matrix cell loop (cpp/dolfinx/fem/assemble_matrix_impl.h:92-200) with
+// insertion by binary search (cpp/dolfinx/la/matrix_csr_impl.h:67-109).
+// dofmap holds node (block) indices; bc is indexed by bs*node + k.
+int orc_assemble_matrix(const orc_form* form, int nc, const int32_t* x_dofmap,
+                        const double* x, const int32_t* dofmap,
+                        const int8_t* bc, const int64_t* row_ptr,
+                        const int32_t* cols, double* vals)
+{
+  const int nd = tet_ndofs(form->degree);
+  const int bs = form->kind == 1 ? 3 : 1;
+  const int n = nd * bs;
+  std::vector<double> Ae(n * n);
+  double coords[12];
+  for (int c = 0; c < nc; ++c)
+  {
+    for (int v = 0; v < 4; ++v)
+      for (int k = 0; k < 3; ++k)
+        coords[3 * v + k] = x[3 * (int64_t)x_dofmap[4 * c + v] + k];
+    std::fill(Ae.begin(), Ae.end(), 0.0);
+    const double kap = form->kappa ? form->kappa[c] : 1.0;
+    if (form->kind == 0)
+      kernel_poisson(form->degree, Ae.data(), kap, form->k2, coords);
+    else
+      kernel_elasticity(Ae.data(), kap, form->nu, coords);
+    const int32_t* dofs = dofmap + (int64_t)nd * c;
+    if (bc)
+    {
+      for (int i = 0; i < nd; ++i)
+        for (int k = 0; k < bs; ++k)
+          if (bc[bs * dofs[i] + k])
+          {
+            std::fill_n(Ae.begin() + n * (bs * i + k), n, 0.0);
+            for (int r = 0; r < n; ++r)
+              Ae[r * n + bs * i + k] = 0.0;
+          }
+    }
+    for (int i = 0; i < nd; ++i)
+    {
+      const int32_t row = dofs[i];
+      const int32_t* c0 = cols + row_ptr[row];
+      const int32_t* c1 = cols + row_ptr[row + 1];
+      for (int j = 0; j < nd; ++j)
+      {
+        const int32_t* it = std::lower_bound(c0, c1, dofs[j]);
+        if (it == c1 || *it != dofs[j])
+          return ORC_ERR_NOT_IN_SPARSITY;
+        const int64_t d = (it - cols) * bs * bs;
+        for (int a = 0; a < bs; ++a)
+          for (int b = 0; b < bs; ++b)
+            vals[d + a * bs + b] += Ae[(bs * i + a) * n + bs * j + b];
+      }
+    }
+  }
+  return ORC_OK;
+}
+
+// Vector cell loop (cpp/dolfinx/fem/assemble_vector_impl.h:75-116).
+// kind 0: L = \int f v, f a P1 coefficient (values per geometry node,
+// f == nullptr -> f = 1). kind 1: L = \int fvec . v (vector P2).
+int orc_assemble_vector(int kind, int degree, int nc, const int32_t* x_dofmap,
+                        const double* x, const int32_t* dofmap, const double* f,
+                        const double* fvec, double* b)
+{
+  const int nd = tet_ndofs(degree);
+  const int bs = kind == 1 ? 3 : 1;
+  double be[30], coords[12], fc[4];
+  for (int c = 0; c < nc; ++c)
+  {
+    for (int v = 0; v < 4; ++v)
+    {
+      for (int k = 0; k < 3; ++k)
+        coords[3 * v + k] = x[3 * (int64_t)x_dofmap[4 * c + v] + k];
+      fc[v] = f ? f[x_dofmap[4 * c + v]] : 1.0;
+    }
+    std::fill_n(be, 30, 0.0);
+    if (kind == 0)
+      kernel_source(degree, be, fc, coords);
+    else
+      kernel_bodyforce(be, fvec, coords);
+    const int32_t* dofs = dofmap + (int64_t)nd * c;
+    for (int i = 0; i < nd; ++i)
+      for (int k = 0; k < bs; ++k)
+        b[bs * dofs[i] + k] += be[bs * i + k];
+  }
+  return ORC_OK;
+}
+
+// apply_lifting for one form (cpp/dolfinx/fem/assembler.h:341-421,
+// lift_bc cpp/dolfinx/fem/assemble_vector_impl.h:361-414): cells with a
+// constrained column only, b[r] -= Ae[r, c] * alpha * (g_c - x0_c).
+int orc_apply_lifting(const orc_form* form, int nc, const int32_t* x_dofmap,
+                      const double* x, const int32_t* dofmap,
+                      const int8_t* bc, const double* g, const double* x0,
+                      double alpha, double* b)
+{
+  const int nd = tet_ndofs(form->degree);
+  const int bs = form->kind == 1 ? 3 : 1;
+  const int n = nd * bs;
+  std::vector<double> Ae(n * n);
+  double coords[12];
+  for (int c = 0; c < nc; ++c)
+  {
+    const int32_t* dofs = dofmap + (int64_t)nd * c;
+    bool has = false;
+    for (int i = 0; i < nd && !has; ++i)
+      for (int k = 0; k < bs; ++k)
+        has = has || bc[bs * dofs[i] + k];
+    if (!has)
+      continue;
+    for (int v = 0; v < 4; ++v)
+      for (int k = 0; k < 3; ++k)
+        coords[3 * v + k] = x[3 * (int64_t)x_dofmap[4 * c + v] + k];
+    std::fill(Ae.begin(), Ae.end(), 0.0);
+    const double kap = form->kappa ? form->kappa[c] : 1.0;
+    if (form->kind == 0)
+      kernel_poisson(form->degree, Ae.data(), kap, form->k2, coords);
+    else
+      kernel_elasticity(Ae.data(), kap, form->nu, coords);
+    for (int j = 0; j < nd; ++j)
+      for (int k = 0; k < bs; ++k)
+      {
+        const int32_t jj = bs * dofs[j] + k;
+        if (!bc[jj])
+          continue;
+        const double xb = g[jj], xz = x0 ? x0[jj] : 0.0;
+        for (int i = 0; i < nd; ++i)
+          for (int m = 0; m < bs; ++m)
+            b[bs * dofs[i] + m] -= Ae[(bs * i + m) * n + bs * j + k] * alpha * (xb - xz);
+      }
+  }
+  return ORC_OK;
+}
+
+// DirichletBC::set (cpp/dolfinx/fem/DirichletBC.h:495-578):
+// x[dofs[i]] = alpha * (g[dofs[i]] - x0[dofs[i]]), skipping dofs >= n.
+void orc_set_bc(int n, double* xv, int ndofs, const int32_t* dofs,
+                const double* g, const double* x0, double alpha)
+{
+  for (int i = 0; i < ndofs; ++i)
+    if (dofs[i] < n)
+      xv[dofs[i]] = alpha == 0.0 ? 0.0 : alpha * (g[dofs[i]] - (x0 ? x0[dofs[i]] : 0.0));
+}
+
+// set_diagonal (cpp/dolfinx/fem/assembler.h:644-686) via MatrixCSR::set:
+// A[d, d] = diag for each constrained scalar dof d (block row d / bs).
+int orc_set_diagonal(int bs, const int64_t* row_ptr, const int32_t* cols,
+                     double* vals, int ndofs, const int32_t* dofs, double diag)
+{
+  for (int i = 0; i < ndofs; ++i)
+  {
+    const int32_t r = dofs[i] / bs, k = dofs[i] % bs;
+    const int32_t* c0 = cols + row_ptr[r];
+    const int32_t* c1 = cols + row_ptr[r + 1];
+    const int32_t* it = std::lower_bound(c0, c1, r);
+    if (it == c1 || *it != r)
+      return ORC_ERR_NOT_IN_SPARSITY;
+    vals[(it - cols) * bs * bs + k * bs + k] = diag;
+  }
+  return ORC_OK;
+}
+
+// y += A x (cpp/dolfinx/la/matrix_csr_impl.h:259-286).
+void orc_spmv(int nrows, int bs, const int64_t* row_ptr, const int32_t* cols,
+              const double* vals, const double* xv, double* y)
+{
+  for (int k0 = 0; k0 < bs; ++k0)
+    for (int i = 0; i < nrows; ++i)
+    {
+      double vi = 0.0;
+      for (int64_t j = row_ptr[i]; j < row_ptr[i + 1]; ++j)
+        for (int k1 = 0; k1 < bs; ++k1)
+          vi += vals[j * bs * bs + k0 * bs + k1] * xv[cols[j] * bs + k1];
+      y[i * bs + k0] += vi;
+    }
+}
+
+// Same product, with float matrix values (MatrixCSR<float> obtained via
+// the converting constructor cpp/dolfinx/la/MatrixCSR.h:223-237).
+void orc_spmv_f32(int nrows, int bs, const int64_t* row_ptr,
+                  const int32_t* cols, const float* vals, const float* xv,
+                  float* y)
+{
+  for (int k0 = 0; k0 < bs; ++k0)
+    for (int i = 0; i < nrows; ++i)
+    {
+      float vi = 0.0f;
+      for (int64_t j = row_ptr[i]; j < row_ptr[i + 1]; ++j)
+        for (int k1 = 0; k1 < bs; ++k1)
+          vi += vals[j * bs * bs + k0 * bs + k1] * xv[cols[j] * bs + k1];
+      y[i * bs + k0] += vi;
+    }
+}
+
+// Conjugate gradients (cpp/demo/poisson_matrix_free/main.cpp:84-132),
+// with optional Jacobi preconditioning (dinv != nullptr): z = D^{-1} r,
+// rho = r.z drives alpha/beta; convergence is tested on the unpreconditioned
+// residual, |r|^2 / |r0|^2 < rtol^2, as in the demo. x holds the initial
+// guess. Returns iterations (negative on non-convergence).
+int orc_cg(int nrows, int bs, const int64_t* row_ptr, const int32_t* cols,
+           const double* vals, const double* b, double* xv, const double* dinv,
+           double rtol, int kmax)
+{
+  const int64_t n = (int64_t)nrows * bs;
+  std::vector<double> r(n), y(n, 0.0), p(n), z(n);
+  orc_spmv(nrows, bs, row_ptr, cols, vals, xv, y.data());
+  for (int64_t i = 0; i < n; ++i)
+    r[i] = b[i] - y[i];
+  for (int64_t i = 0; i < n; ++i)
+    z[i] = dinv ? dinv[i] * r[i] : r[i];
+  p = z;
+  double rr0 = 0, rz = 0;
+  for (int64_t i = 0; i < n; ++i)
+  {
+    rr0 += r[i] * r[i];
+    rz += r[i] * z[i];
+  }
+  if (rr0 == 0.0)
+    return 0;
+  const double rtol2 = rtol * rtol;
+  int k = 0;
+  while (k < kmax)
+  {
+    ++k;
+    std::fill(y.begin(), y.end(), 0.0);
+    orc_spmv(nrows, bs, row_ptr, cols, vals, p.data(), y.data());
+    double py = 0;
+    for (int64_t i = 0; i < n; ++i)
+      py += p[i] * y[i];
+    const double alpha = rz / py;
+    double rr = 0, rzn = 0;
+    for (int64_t i = 0; i < n; ++i)
+    {
+      xv[i] += alpha * p[i];
+      r[i] -= alpha * y[i];
+      rr += r[i] * r[i];
+      z[i] = dinv ? dinv[i] * r[i] : r[i];
+      rzn += r[i] * z[i];
+    }
+    if (rr / rr0 < rtol2)
+      return k;
+    const double beta = rzn / rz;
+    rz = rzn;
+    for (int64_t i = 0; i < n; ++i)
+      p[i] = z[i] + beta * p[i];
+  }
+  return -k;
+}
+
+} // extern "C"

@@ -1,0 +1,246 @@
+"""ctypes front end of the CPU oracle (test infrastructure only).
+
+Loads ``oracle/_build/liboracle.so`` (the CPU restatement of the DOLFINx
+hot path, ``oracle/dfx_oracle.cpp``) and, when it was built,
+``oracle/_ref/libdfxref.so`` (the reference's own ordering / sort / CSR
+code). Only the test-suite, ``__graft_entry__.smoke()`` and the CPU
+baseline leg of ``bench.py`` use this module; the product package never
+imports it.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "liboracle.so")
+REFLIB = os.path.join(HERE, "_ref", "libdfxref.so")
+REF_SRC = "/root/reference"
+
+_i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
+_i64p = np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")
+_f64p = np.ctypeslib.ndpointer(np.float64, flags="C_CONTIGUOUS")
+_f32p = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
+_i8p = np.ctypeslib.ndpointer(np.int8, flags="C_CONTIGUOUS")
+
+
+def build(with_ref: bool | None = None) -> None:
+    """Compile the oracle (and the reference pieces when the tree exists)."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    if with_ref is None:
+        with_ref = os.path.isdir(os.path.join(REF_SRC, "cpp", "dolfinx"))
+    if with_ref:
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={REF_SRC}"], check=True)
+
+
+class _Form(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int),
+        ("degree", C.c_int),
+        ("kappa", C.c_void_p),
+        ("k2", C.c_double),
+        ("nu", C.c_double),
+    ]
+
+
+_lib = None
+_ref = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build(with_ref=False)
+        L = C.CDLL(LIB)
+        L.orc_create_box_tet.argtypes = [C.c_int] * 3 + [_f64p, _f64p, C.c_int, _i32p, _f64p]
+        L.orc_box_tet_raw.argtypes = [C.c_int] * 3 + [_f64p, _f64p, _i64p, _f64p]
+        L.orc_dual_graph_tet.argtypes = [C.c_int, _i64p, _i32p, _i32p]
+        L.orc_reorder_rcm.argtypes = [C.c_int, _i32p, _i32p, _i32p]
+        L.orc_dofmap_tet.argtypes = [C.c_int, _i32p, C.c_int, _i32p]
+        L.orc_sparsity.argtypes = [C.c_int, C.c_int, C.c_int, _i32p, C.c_void_p, C.c_void_p]
+        L.orc_sparsity.restype = C.c_int64
+        L.orc_kernel_poisson.argtypes = [C.c_int, _f64p, C.c_double, C.c_double, _f64p]
+        L.orc_kernel_source.argtypes = [C.c_int, _f64p, _f64p, _f64p]
+        L.orc_kernel_elasticity.argtypes = [_f64p, C.c_double, C.c_double, _f64p]
+        L.orc_assemble_matrix.argtypes = [C.POINTER(_Form), C.c_int, _i32p, _f64p, _i32p,
+                                          C.c_void_p, _i64p, _i32p, _f64p]
+        L.orc_assemble_vector.argtypes = [C.c_int, C.c_int, C.c_int, _i32p, _f64p, _i32p,
+                                          C.c_void_p, C.c_void_p, _f64p]
+        L.orc_apply_lifting.argtypes = [C.POINTER(_Form), C.c_int, _i32p, _f64p, _i32p, _i8p,
+                                        _f64p, C.c_void_p, C.c_double, _f64p]
+        L.orc_set_bc.argtypes = [C.c_int, _f64p, C.c_int, _i32p, _f64p, C.c_void_p, C.c_double]
+        L.orc_set_diagonal.argtypes = [C.c_int, _i64p, _i32p, _f64p, C.c_int, _i32p, C.c_double]
+        L.orc_spmv.argtypes = [C.c_int, C.c_int, _i64p, _i32p, _f64p, _f64p, _f64p]
+        L.orc_spmv_f32.argtypes = [C.c_int, C.c_int, _i64p, _i32p, _f32p, _f32p, _f32p]
+        L.orc_cg.argtypes = [C.c_int, C.c_int, _i64p, _i32p, _f64p, _f64p, _f64p, C.c_void_p,
+                             C.c_double, C.c_int]
+        _lib = L
+    return _lib
+
+
+def ref():
+    """The reference's own compiled code, or None when it was not built."""
+    global _ref
+    if _ref is None and os.path.exists(REFLIB):
+        R = C.CDLL(REFLIB)
+        R.ref_reorder_rcm.argtypes = [C.c_int, _i32p, _i32p, _i32p]
+        R.ref_sort_by_perm3.argtypes = [C.c_int64, _i64p, _i64p, _i64p, _i32p]
+        R.ref_insert_csr_add.argtypes = [C.c_int, _f64p, C.c_int64, _i32p, _i64p, C.c_int64,
+                                         _f64p, C.c_int, _i32p, C.c_int, _i32p]
+        R.ref_spmv.argtypes = [C.c_int64, C.c_int, _i64p, _i32p, _f64p, C.c_int64, _f64p, _f64p]
+        _ref = R
+    return _ref
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+# ---------------------------------------------------------------- mesh
+def create_box_tet(nx, ny, nz, p0=(0.0, 0.0, 0.0), p1=(1.0, 1.0, 1.0), reorder=True):
+    nc = 6 * nx * ny * nz
+    nv = (nx + 1) * (ny + 1) * (nz + 1)
+    cells = np.empty((nc, 4), np.int32)
+    x = np.empty((nv, 3), np.float64)
+    rc = lib().orc_create_box_tet(nx, ny, nz, np.asarray(p0, np.float64),
+                                  np.asarray(p1, np.float64), int(reorder), cells, x)
+    assert rc == 0
+    return cells, x
+
+
+def box_tet_raw(nx, ny, nz, p0=(0.0, 0.0, 0.0), p1=(1.0, 1.0, 1.0)):
+    nc = 6 * nx * ny * nz
+    nv = (nx + 1) * (ny + 1) * (nz + 1)
+    cells = np.empty((nc, 4), np.int64)
+    x = np.empty((nv, 3), np.float64)
+    lib().orc_box_tet_raw(nx, ny, nz, np.asarray(p0, np.float64), np.asarray(p1, np.float64),
+                          cells, x)
+    return cells, x
+
+
+def dual_graph_tet(cells64):
+    nc = cells64.shape[0]
+    off = np.empty(nc + 1, np.int32)
+    adj = np.empty(4 * nc, np.int32)
+    lib().orc_dual_graph_tet(nc, np.ascontiguousarray(cells64, np.int64), off, adj)
+    return off, adj[: off[-1]].copy()
+
+
+def reorder_rcm(off, adj):
+    n = off.size - 1
+    r = np.empty(n, np.int32)
+    lib().orc_reorder_rcm(n, off, np.ascontiguousarray(adj, np.int32), r)
+    return r
+
+
+def dofmap_tet(cells, degree):
+    nc = cells.shape[0]
+    nd = 4 if degree == 1 else 10
+    dm = np.empty((nc, nd), np.int32)
+    n = lib().orc_dofmap_tet(nc, np.ascontiguousarray(cells, np.int32), degree, dm)
+    return dm, int(n)
+
+
+def sparsity(nrows, dofmap):
+    nc, nd = dofmap.shape
+    dm = np.ascontiguousarray(dofmap, np.int32)
+    rp = np.empty(nrows + 1, np.int64)
+    nnz = lib().orc_sparsity(nrows, nc, nd, dm, rp.ctypes.data, None)
+    cols = np.empty(nnz, np.int32)
+    lib().orc_sparsity(nrows, nc, nd, dm, rp.ctypes.data, cols.ctypes.data)
+    return rp, cols
+
+
+# ---------------------------------------------------------------- assembly
+def _form(kind, degree, kappa, k2, nu):
+    f = _Form(kind, degree, None, float(k2), float(nu))
+    if kappa is not None:
+        f.kappa = kappa.ctypes.data
+    return f
+
+
+def assemble_matrix(kind, degree, cells, x, dofmap, row_ptr, cols, kappa=None, k2=0.0, nu=0.3,
+                    bc_markers=None, vals=None):
+    bs = 3 if kind == 1 else 1
+    if vals is None:
+        vals = np.zeros(cols.size * bs * bs, np.float64)
+    kap = None if kappa is None else np.ascontiguousarray(kappa, np.float64)
+    f = _form(kind, degree, kap, k2, nu)
+    bcm = None if bc_markers is None else np.ascontiguousarray(bc_markers, np.int8)
+    rc = lib().orc_assemble_matrix(C.byref(f), cells.shape[0], np.ascontiguousarray(cells), x,
+                                   np.ascontiguousarray(dofmap), _ptr(bcm), row_ptr, cols, vals)
+    if rc == 3:
+        raise RuntimeError("Entry not in sparsity")
+    return vals
+
+
+def assemble_vector(kind, degree, cells, x, dofmap, n, f=None, fvec=None, b=None):
+    bs = 3 if kind == 1 else 1
+    if b is None:
+        b = np.zeros(n * bs, np.float64)
+    fa = None if f is None else np.ascontiguousarray(f, np.float64)
+    fv = None if fvec is None else np.ascontiguousarray(fvec, np.float64)
+    lib().orc_assemble_vector(kind, degree, cells.shape[0], np.ascontiguousarray(cells), x,
+                              np.ascontiguousarray(dofmap), _ptr(fa), _ptr(fv), b)
+    return b
+
+
+def apply_lifting(b, kind, degree, cells, x, dofmap, bc_markers, g, kappa=None, k2=0.0, nu=0.3,
+                  x0=None, alpha=1.0):
+    kap = None if kappa is None else np.ascontiguousarray(kappa, np.float64)
+    f = _form(kind, degree, kap, k2, nu)
+    x0a = None if x0 is None else np.ascontiguousarray(x0, np.float64)
+    lib().orc_apply_lifting(C.byref(f), cells.shape[0], np.ascontiguousarray(cells), x,
+                            np.ascontiguousarray(dofmap), np.ascontiguousarray(bc_markers, np.int8),
+                            np.ascontiguousarray(g, np.float64), _ptr(x0a), float(alpha), b)
+    return b
+
+
+def set_bc(b, dofs, g, x0=None, alpha=1.0):
+    x0a = None if x0 is None else np.ascontiguousarray(x0, np.float64)
+    lib().orc_set_bc(b.size, b, dofs.size, np.ascontiguousarray(dofs, np.int32),
+                     np.ascontiguousarray(g, np.float64), _ptr(x0a), float(alpha))
+    return b
+
+
+def set_diagonal(bs, row_ptr, cols, vals, dofs, diag=1.0):
+    rc = lib().orc_set_diagonal(bs, row_ptr, cols, vals, dofs.size,
+                                np.ascontiguousarray(dofs, np.int32), float(diag))
+    if rc:
+        raise RuntimeError("Entry not in sparsity")
+    return vals
+
+
+def spmv(row_ptr, cols, vals, x, bs=1, y=None):
+    nrows = row_ptr.size - 1
+    if y is None:
+        y = np.zeros(nrows * bs, np.float64)
+    lib().orc_spmv(nrows, bs, row_ptr, cols, vals, np.ascontiguousarray(x, np.float64), y)
+    return y
+
+
+def cg(row_ptr, cols, vals, b, bs=1, x=None, dinv=None, rtol=1e-10, kmax=100000):
+    nrows = row_ptr.size - 1
+    x = np.zeros(nrows * bs) if x is None else np.ascontiguousarray(x, np.float64).copy()
+    d = None if dinv is None else np.ascontiguousarray(dinv, np.float64)
+    it = lib().orc_cg(nrows, bs, row_ptr, cols, vals, np.ascontiguousarray(b, np.float64), x,
+                      _ptr(d), float(rtol), int(kmax))
+    return x, int(it)
+
+
+def kernel_poisson(degree, coords, kappa=1.0, k2=0.0):
+    nd = 4 if degree == 1 else 10
+    Ae = np.zeros(nd * nd)
+    lib().orc_kernel_poisson(degree, Ae, kappa, k2, np.ascontiguousarray(coords, np.float64).ravel())
+    return Ae.reshape(nd, nd)
+
+
+def kernel_elasticity(coords, E=1.0, nu=0.3):
+    Ae = np.zeros(900)
+    lib().orc_kernel_elasticity(Ae, E, nu, np.ascontiguousarray(coords, np.float64).ravel())
+    return Ae.reshape(30, 30)

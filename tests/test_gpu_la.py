@@ -1,0 +1,129 @@
+"""GPU parity: SpMV (FP64, FP32 values, 3x3 blocks), Jacobi diagonal,
+inner product and CG against the oracle."""
+
+import numpy as np
+import pytest
+import torch
+
+from gpu_util import assert_close, problem
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("deg,bs", [(1, 1), (2, 1), (2, 3)])
+@pytest.mark.parametrize("beta", [0.0, 1.0])
+def test_spmv_f64(cuda, oracle, capi, deg, bs, beta):
+    from dolfinx_gb300 import fem
+
+    m, V, kappa, f, rp, cols = problem(oracle, (5, 6, 4), deg, bs=bs)
+    a = fem.poisson_form(V, kappa) if bs == 1 else fem.elasticity_form(V, kappa)
+    A = fem.assemble_matrix(a)
+    vals = A.vals.cpu().numpy()
+    rng = np.random.default_rng(11)
+    x = rng.standard_normal(V.num_dofs)
+    y0 = rng.standard_normal(V.num_dofs)
+    xd = torch.from_numpy(x).cuda()
+    yd = torch.from_numpy(y0.copy()).cuda()
+    if beta == 1.0:
+        A.mult(xd, yd)
+        ref = oracle.spmv(rp, cols, vals, x, bs=bs, y=y0.copy())
+    else:
+        A.matvec(xd, yd)
+        ref = oracle.spmv(rp, cols, vals, x, bs=bs)
+    assert_close(yd.cpu().numpy(), ref, rtol=1e-13)
+
+
+@pytest.mark.parametrize("bs", [1, 3])
+def test_spmv_f32(cuda, oracle, capi, bs):
+    from dolfinx_gb300 import fem
+
+    m, V, kappa, f, rp, cols = problem(oracle, (4, 4, 4), 2, bs=bs)
+    a = fem.poisson_form(V, kappa) if bs == 1 else fem.elasticity_form(V, kappa)
+    A32 = fem.assemble_matrix(a).astype_float32()
+    x = np.random.default_rng(3).standard_normal(V.num_dofs).astype(np.float32)
+    y = A32.matvec(torch.from_numpy(x).cuda()).cpu().numpy()
+    ref = oracle.spmv(rp, cols, A32.vals.cpu().numpy().astype(np.float64), x.astype(np.float64),
+                      bs=bs)
+    assert_close(y, ref, rtol=2e-6)
+
+
+def test_inner_product(cuda, capi):
+    from dolfinx_gb300 import la
+
+    rng = np.random.default_rng(5)
+    for n in [1, 1000, 1234567]:
+        a = rng.standard_normal(n)
+        b = rng.standard_normal(n)
+        v = la.inner_product(torch.from_numpy(a).cuda(), torch.from_numpy(b).cuda())
+        assert abs(v - np.dot(a, b)) <= 1e-12 * np.abs(a * b).sum()
+
+
+@pytest.mark.parametrize("deg", [1, 2])
+def test_cg_c1_pipeline(cuda, oracle, capi, deg):
+    """Full c1-style pipeline: assemble, lift, set_bc, Jacobi-CG; solution
+    vs the oracle's CG on the oracle's system (rtol 1e-10)."""
+    from dolfinx_gb300 import fem, la
+
+    n = (8, 8, 8) if deg == 2 else (16, 16, 16)
+    m, V, kappa, f, rp, cols = problem(oracle, n, deg, seed=12)
+    X = V.tabulate_dof_coordinates()
+    bnd = np.flatnonzero(np.isclose(X, 0).any(1) | np.isclose(X, 1).any(1)).astype(np.int32)
+    bc = fem.dirichletbc(0.0, bnd, V)
+    a = fem.poisson_form(V, kappa)
+    A = fem.assemble_matrix(a, bcs=[bc])
+    b = fem.assemble_vector(fem.source_form(V, f))
+    fem.apply_lifting(b, [a], [[bc]])
+    fem.set_bc(b, [bc])
+    x, res = la.cg(A, b, rtol=1e-10)
+    assert res.status == 0 and res.iterations > 0
+    mk = np.zeros(V.num_nodes, np.int8)
+    mk[bnd] = 1
+    Ar = oracle.assemble_matrix(0, deg, m.cells, m.x, V.dofmap, rp, cols, kappa=kappa,
+                                bc_markers=mk)
+    oracle.set_diagonal(1, rp, cols, Ar, bnd)
+    br = oracle.assemble_vector(0, deg, m.cells, m.x, V.dofmap, V.num_nodes, f=f)
+    oracle.set_bc(br, bnd, np.zeros(V.num_nodes))
+    assert_close(b.cpu().numpy(), br)
+    diag = np.array([Ar[rp[i] + np.searchsorted(cols[rp[i]:rp[i + 1]], i)]
+                     for i in range(V.num_nodes)])
+    xr, it = oracle.cg(rp, cols, Ar, br, dinv=1.0 / diag, rtol=1e-10)
+    assert it > 0
+    assert abs(res.iterations - it) <= 2
+    xs = x.cpu().numpy()
+    rel = np.linalg.norm(xs - xr) / np.linalg.norm(xr)
+    assert rel < 1e-8, rel
+    # residual of the GPU solution in the oracle's system
+    r = br - oracle.spmv(rp, cols, Ar, xs)
+    assert np.linalg.norm(r) / np.linalg.norm(br) < 1e-9
+
+
+def test_cg_elasticity_small(cuda, oracle, capi):
+    from dolfinx_gb300 import fem, la
+
+    m, V, E, f, rp, cols = problem(oracle, (4, 2, 2), 2, bs=3, seed=2)
+    X = V.tabulate_dof_coordinates()
+    clamp = np.flatnonzero(np.isclose(X[:, 0], 0)).astype(np.int32)
+    bc = fem.dirichletbc(np.zeros(3), clamp, V)
+    a = fem.elasticity_form(V, 1e3 * E, 0.3)
+    A = fem.assemble_matrix(a, bcs=[bc])
+    b = fem.assemble_vector(fem.body_force_form(V, (0, 0, -1)))
+    fem.apply_lifting(b, [a], [[bc]])
+    fem.set_bc(b, [bc])
+    x, res = la.cg(A, b, rtol=1e-10)
+    vals = A.vals.cpu().numpy()
+    bh = b.cpu().numpy()
+    r = bh - oracle.spmv(rp, cols, vals, x.cpu().numpy(), bs=3)
+    assert np.linalg.norm(r) / np.linalg.norm(bh) < 1e-9
+
+
+def test_cg_not_converged_reports(cuda, oracle, capi):
+    from dolfinx_gb300 import fem, la
+
+    m, V, kappa, f, rp, cols = problem(oracle, (6, 6, 6), 1)
+    X = V.tabulate_dof_coordinates()
+    bnd = np.flatnonzero(np.isclose(X, 0).any(1)).astype(np.int32)
+    bc = fem.dirichletbc(0.0, bnd, V)
+    A = fem.assemble_matrix(fem.poisson_form(V, kappa), bcs=[bc])
+    b = fem.assemble_vector(fem.source_form(V, f))
+    with pytest.raises(capi.DfxError, match="exceeded max iterations"):
+        la.cg(A, b, rtol=1e-14, max_iters=3)

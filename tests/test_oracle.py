@@ -1,0 +1,140 @@
+"""The CPU oracle against the reference's own code (golden vectors written
+by tests/golden/make_golden.py from oracle/_ref) and against the
+properties the reference's tests pin (cpp/test/matrix.cpp,
+python/test/unit/fem/test_fem_pipeline.py, test_symmetry.py,
+test_custom_assembler.py)."""
+
+import os
+
+import numpy as np
+import pytest
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "reference_golden.npz")
+
+
+@pytest.fixture(scope="module")
+def golden():
+    return np.load(GOLDEN)
+
+
+@pytest.mark.parametrize("n", [(1, 1, 1), (2, 2, 2), (3, 2, 4), (5, 4, 3)])
+def test_dual_graph_and_rcm_match_reference(oracle, golden, n):
+    tag = "%dx%dx%d" % n
+    raw, _ = oracle.box_tet_raw(*n)
+    off, adj = oracle.dual_graph_tet(raw)
+    np.testing.assert_array_equal(off, golden[f"dual_off_{tag}"])
+    np.testing.assert_array_equal(adj, golden[f"dual_adj_{tag}"])
+    r = oracle.reorder_rcm(off, adj)
+    np.testing.assert_array_equal(r, golden[f"rcm_{tag}"])
+
+
+@pytest.mark.parametrize("tag,n,kind", [("p2", (2, 2, 2), 0), ("el", (2, 1, 1), 1)])
+def test_insert_and_spmv_match_reference(oracle, golden, tag, n, kind):
+    cells, x = oracle.create_box_tet(*n)
+    dm, nn = oracle.dofmap_tet(cells, 2)
+    rp, cols = oracle.sparsity(nn, dm)
+    np.testing.assert_array_equal(rp, golden[f"csr_rowptr_{tag}"])
+    np.testing.assert_array_equal(cols, golden[f"csr_cols_{tag}"])
+    bs = 3 if kind == 1 else 1
+    # Replay the reference's insertion with the oracle's CSR search: the
+    # oracle's assembly inserts with the same lower_bound semantics.
+    rng = np.random.default_rng(7)
+    vals = np.zeros(cols.size * bs * bs)
+    for c in range(cells.shape[0]):
+        Ae = rng.standard_normal((10 * bs) ** 2).reshape(10 * bs, 10 * bs)
+        for i in range(10):
+            row = dm[c, i]
+            for j in range(10):
+                p = rp[row] + np.searchsorted(cols[rp[row]:rp[row + 1]], dm[c, j])
+                vals[p * bs * bs:(p + 1) * bs * bs] += Ae[bs * i:bs * i + bs,
+                                                          bs * j:bs * j + bs].ravel()
+    np.testing.assert_array_equal(vals, golden[f"csr_vals_{tag}"])
+    y = golden[f"spmv_y0_{tag}"].copy()
+    oracle.spmv(rp, cols, vals, golden[f"spmv_x_{tag}"], bs=bs, y=y)
+    np.testing.assert_array_equal(y, golden[f"spmv_y_{tag}"])
+
+
+def test_c1_counts(oracle):
+    cells, x = oracle.create_box_tet(16, 16, 16)
+    dm, n = oracle.dofmap_tet(cells, 1)
+    rp, cols = oracle.sparsity(n, dm)
+    assert cells.shape[0] == 24576 and n == 4913 and cols.size == 66961
+    # P1 dofmap == geometry dofmap (both first-appearance numbered)
+    np.testing.assert_array_equal(dm, cells)
+
+
+def test_p2_laplacian_kills_constants(oracle):
+    # cpp/test/matrix.cpp:66-120: P2 Laplacian on a 12^3 x 6 box, A 1 = 0
+    cells, x = oracle.create_box_tet(12, 12, 12)
+    dm, n = oracle.dofmap_tet(cells, 2)
+    rp, cols = oracle.sparsity(n, dm)
+    A = oracle.assemble_matrix(0, 2, cells, x, dm, rp, cols)
+    y = oracle.spmv(rp, cols, A, np.ones(n))
+    assert np.abs(y).max() < 1e-13
+
+
+@pytest.mark.parametrize("deg", [1, 2])
+def test_element_symmetry_and_row_sums(oracle, deg):
+    rng = np.random.default_rng(1)
+    coords = rng.standard_normal((4, 3))
+    Ae = oracle.kernel_poisson(deg, coords, kappa=2.5, k2=0.0)
+    np.testing.assert_allclose(Ae, Ae.T, rtol=0, atol=1e-13 * np.abs(Ae).max())
+    np.testing.assert_allclose(Ae.sum(axis=1), 0.0, atol=1e-13 * np.abs(Ae).max())
+    # mass part: sum of all entries = k2 * |T|
+    M = oracle.kernel_poisson(deg, coords, kappa=0.0, k2=1.0)
+    vol = abs(np.linalg.det((coords[1:] - coords[0]).T)) / 6
+    assert abs(M.sum() - vol) < 1e-13 * vol
+
+
+def test_elasticity_rigid_motions(oracle):
+    rng = np.random.default_rng(2)
+    coords = rng.standard_normal((4, 3))
+    Ae = oracle.kernel_elasticity(coords, E=3.0, nu=0.3)
+    np.testing.assert_allclose(Ae, Ae.T, atol=1e-12 * np.abs(Ae).max())
+    # P2 nodes
+    e = [(2, 3), (1, 3), (1, 2), (0, 3), (0, 2), (0, 1)]
+    X = np.vstack([coords, [(coords[a] + coords[b]) / 2 for a, b in e]])
+    for rig in [np.tile([1.0, 0, 0], 10), np.cross([0, 0, 1.0], X).ravel()]:
+        assert np.abs(Ae @ rig).max() < 1e-11 * np.abs(Ae).max()
+
+
+def test_rhs_total_is_volume(oracle):
+    # python/test/unit/fem/test_custom_assembler.py:162: sum(b) = |Omega| for f = 1
+    for deg in (1, 2):
+        cells, x = oracle.create_box_tet(3, 2, 2)
+        dm, n = oracle.dofmap_tet(cells, deg)
+        b = oracle.assemble_vector(0, deg, cells, x, dm, n)
+        assert abs(b.sum() - 1.0) < 1e-13
+
+
+@pytest.mark.parametrize("deg", [1, 2])
+def test_pipeline_reproduces_polynomial(oracle, deg):
+    # python/test/unit/fem/test_fem_pipeline.py:55-108: u = y^p is exact in P_p
+    cells, x = oracle.create_box_tet(4, 3, 5)
+    dm, n = oracle.dofmap_tet(cells, deg)
+    rp, cols = oracle.sparsity(n, dm)
+    # dof coordinates
+    X = np.empty((n, 3))
+    e = np.array([[2, 3], [1, 3], [1, 2], [0, 3], [0, 2], [0, 1]])
+    xc = x[cells]
+    X[dm[:, :4].ravel()] = xc.reshape(-1, 3)
+    if deg == 2:
+        X[dm[:, 4:].ravel()] = (0.5 * (xc[:, e[:, 0]] + xc[:, e[:, 1]])).reshape(-1, 3)
+    u = X[:, 1] ** deg
+    f_p1 = np.full(x.shape[0], -2.0 if deg == 2 else 0.0)  # -div grad y^2 = -2
+    bnd = np.flatnonzero(np.isclose(X, 0).any(1) | np.isclose(X, 1).any(1))
+    mk = np.zeros(n, np.int8)
+    mk[bnd] = 1
+    g = np.zeros(n)
+    g[bnd] = u[bnd]
+    A = oracle.assemble_matrix(0, deg, cells, x, dm, rp, cols, bc_markers=mk)
+    oracle.set_diagonal(1, rp, cols, A, bnd.astype(np.int32))
+    b = oracle.assemble_vector(0, deg, cells, x, dm, n, f=f_p1)
+    oracle.apply_lifting(b, 0, deg, cells, x, dm, mk, g)
+    oracle.set_bc(b, bnd.astype(np.int32), g)
+    d = np.zeros(n)
+    d = oracle.spmv(rp, cols, A, np.ones(n))  # just exercise; compute diagonal below
+    diag = np.array([A[rp[i] + np.searchsorted(cols[rp[i]:rp[i + 1]], i)] for i in range(n)])
+    uh, it = oracle.cg(rp, cols, A, b, dinv=1.0 / diag, rtol=1e-12)
+    assert it > 0
+    assert np.abs(uh - u).max() < 1e-9
