@@ -43,6 +43,9 @@ def parse():
     p.add_argument("--mode", default="atomic", choices=["atomic", "coloured"])
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-sample-cells", type=int, default=120000)
+    p.add_argument("--inner-rtol", type=float, default=None,
+                   help="reliable: residual drop between replacements (0.1); restart: inner rtol")
+    p.add_argument("--ir-variant", default="reliable", choices=["reliable", "restart"])
     return p.parse_args()
 
 
@@ -51,7 +54,8 @@ def workload_config(args, n_dofs=None, nnz=None):
     cfg = {"workload": f"P2 Poisson unit cube {n}^3x6 tets, lognormal kappa, Jacobi-PCG rtol 1e-10",
            "cells": 6 * n ** 3, "degree": 2, "rtol": 1e-10, "seed": 0,
            "l2": "matrix values (nnz*8 B) exceed the 129 MB L2; no flush between steps",
-           "assembly_mode": args.mode, "parallelism": "replicas" if args.gpus > 1 else "single"}
+           "assembly_mode": args.mode, "ir_variant": args.ir_variant,
+           "parallelism": "replicas" if args.gpus > 1 else "single"}
     if n_dofs is not None:
         cfg["dofs"] = int(n_dofs)
     if nnz is not None:
@@ -73,9 +77,11 @@ def make_inputs(n, seed=0):
 
 
 class Problem:
-    """Device-resident c2 problem with reusable assemblers and solver."""
+    """Device-resident c2 problem with reusable assemblers and both solvers:
+    the plain FP64 path (sliced-ELL FP64 operator, Jacobi-PCG) and the
+    mixed-precision path (FP32 inner PCG inside FP64 refinement)."""
 
-    def __init__(self, m, kappa, f, mode="atomic"):
+    def __init__(self, m, kappa, f, mode="atomic", inner_rtol=None, variant="reliable"):
         import numpy as np
         import torch
 
@@ -96,15 +102,26 @@ class Problem:
         self.b = torch.zeros(self.V.num_dofs, dtype=torch.float64, device="cuda")
         self.x = torch.zeros_like(self.b)
         self.masm.assemble()
-        self.solver = la.CGSolver(self.A, jacobi=True)
+        self.fp64 = la.OperatorCGSolver(self.A, jacobi=True)
+        self.ir = la.IRSolver(self.A, jacobi=True, inner_rtol=inner_rtol, variant=variant)
         self.last = None
 
-    def step(self):
+    def assemble(self):
         self.masm.assemble(zero=True)
         self.rhs.assemble(self.b)
-        self.solver.refresh_preconditioner()
+
+    def step_fp64(self):
+        self.assemble()
+        self.fp64.refresh()
         self.x.zero_()
-        self.last = self.solver.solve(self.b, self.x, rtol=1e-10)
+        self.last = self.fp64.solve(self.b, self.x, rtol=1e-10)
+        return self.last
+
+    def step_ir(self):
+        self.assemble()
+        self.ir.refresh()
+        self.x.zero_()
+        self.last = self.ir.solve(self.b, self.x, rtol=1e-10)
         return self.last
 
 
@@ -303,6 +320,37 @@ def run_reference(args):
 
 
 # --------------------------------------------------------------------------- our arm
+def _timed(fn, steps, stream):
+    import torch
+
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    res = []
+    e0.record(stream)
+    for _ in range(steps):
+        res.append(fn())
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps, res
+
+
+def _kernel_ms(fn, reps, stream):
+    import torch
+
+    for _ in range(3):
+        fn()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -319,100 +367,111 @@ def run_ours(args):
         if world > 1:
             dist.barrier()
 
+    def max_over_ranks(v):
+        t = torch.tensor([v], device="cuda")
+        if world > 1:
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
     m, kappa, f = make_inputs(args.n, seed=rank)
-    P = Problem(m, kappa, f, mode=args.mode)
+    P = Problem(m, kappa, f, mode=args.mode, inner_rtol=args.inner_rtol, variant=args.ir_variant)
     n_dofs = P.V.num_dofs
     stream = torch.cuda.current_stream()
 
     for _ in range(args.warmup):
-        P.step()
+        P.step_fp64()
+        P.step_ir()
     torch.cuda.synchronize()
 
-    # ---- device-resident timed region
-    launches = 0
-    iters = []
+    # ---- plain FP64 GPU path (the reference point of the mixed path)
+    barrier()
+    ms64, res64 = _timed(P.step_fp64, args.steps, stream)
+    barrier()
+    x64 = P.x.clone()
+    ms64 = max_over_ranks(ms64)
+
+    # ---- headline path: FP32-inner / FP64-outer refinement (device resident)
     with Clocks(local) as clk:
         barrier()
-        torch.cuda.synchronize()
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
-        for _ in range(args.steps):
-            r = P.step()
-            iters.append(r.iterations)
-            k = P.solver.graph_iters
-            launches += 5 + 2 + 3 * k * ((r.iterations + k - 1) // k)
-        e1.record(stream)
-        torch.cuda.synchronize()
+        ms, res = _timed(P.step_ir, args.steps, stream)
         barrier()
-    ms = e0.elapsed_time(e1) / args.steps
     clocks = clk.summary()
-    t = torch.tensor([ms], device="cuda")
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    ms_max = float(t.item())
+    ms_max = max_over_ranks(ms)
     value = world * n_dofs / (ms_max * 1e-3) / 1e9
+    rel_err = float((P.x - x64).norm() / x64.norm())
+    launches = int(np.mean([7 + r.kernel_launches for r in res]))
 
     # ---- end to end through the public API with host buffers
     kap_h = torch.from_numpy(kappa).pin_memory()
     f_h = torch.from_numpy(f).pin_memory()
     x_h = torch.empty(n_dofs, dtype=torch.float64).pin_memory()
-    barrier()
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for _ in range(args.steps):
+
+    def e2e_step():
         P.kappa.copy_(kap_h, non_blocking=True)
         P.f.copy_(f_h, non_blocking=True)
-        P.step()
+        r = P.step_ir()
         x_h.copy_(P.x, non_blocking=True)
-    e1.record(stream)
-    torch.cuda.synchronize()
+        return r
+
     barrier()
-    ms_e2e = e0.elapsed_time(e1) / args.steps
-    t = torch.tensor([ms_e2e], device="cuda")
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    e2e_value = world * n_dofs / (float(t.item()) * 1e-3) / 1e9
+    ms_e2e, _ = _timed(e2e_step, args.steps, stream)
+    barrier()
+    e2e_value = world * n_dofs / (max_over_ranks(ms_e2e) * 1e-3) / 1e9
 
-    # ---- roofline of the dominant kernel: the CG SpMV (CSR FP64)
-    A = P.A
-    y = torch.empty_like(P.x)
-    xin = P.x.clone()
-    for _ in range(3):
-        A.matvec(xin, y)
-    reps = 20
-    e0.record(stream)
-    for _ in range(reps):
-        A.matvec(xin, y)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    spmv_ms = e0.elapsed_time(e1) / reps
-    nnz, nrows = A.nnz, A.nrows
-    alg_bytes = nnz * (8 + 4) + (nrows + 1) * 8 + 2 * nrows * 8
+    # ---- roofline: the inner operator (FP32 sliced-ELL, 16-bit columns)
+    # and the FP64 operator, each timed alone on its own numbering
     peak, peak_kind = measured_peaks()
-    achieved = alg_bytes / (spmv_ms * 1e-3) / 1e9
-    traffic = profile_traffic("spmv_csr_f64_c2")
+    op32, op64 = P.ir.op32, P.ir.op64
+    n = P.A.nrows
+    nnz = P.A.nnz
+    info32 = op32.info()
+    xp32 = torch.rand(n, dtype=torch.float32, device="cuda")
+    yp32 = torch.empty_like(xp32)
+    xp64 = torch.rand(n, dtype=torch.float64, device="cuda")
+    yp64 = torch.empty_like(xp64)
+    ms32 = _kernel_ms(lambda: op32.apply_renumbered(xp32, yp32), 30, stream)
+    ms64k = _kernel_ms(lambda: op64.apply_renumbered(xp64, yp64), 30, stream)
+    slices = info32["slices"]
+    alg32 = nnz * (4 + 2) + 32 * slices * 4 + n * (4 + 4) + (slices + 1) * 8
+    alg64 = nnz * (8 + 4) + n * (8 + 8) + (slices + 1) * 8
+    ach32 = alg32 / (ms32 * 1e-3) / 1e9
+    ach64 = alg64 / (ms64k * 1e-3) / 1e9
 
-    # ---- CPU baseline (rank 0, N = 1 only)
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(m, kappa, f, P, int(np.median(iters)), args.cpu_sample_cells)
+        cpu = cpu_baseline(m, kappa, f, P, int(np.median([r.iterations for r in res64])),
+                           args.cpu_sample_cells)
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max,
-                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64 (FP32 inner solve, FP64 residual/update)",
                 "data": "synthetic (seeded lognormal kappa, uniform f)",
-                "config": workload_config(args, n_dofs, A.nnz),
-                "cg_iterations": iters,
+                "config": workload_config(args, n_dofs, nnz),
+                "solver": {"path": "FP32-inner / FP64-outer iterative refinement",
+                           "variant": args.ir_variant, "inner_rtol": P.ir.inner_rtol,
+                           "outer_iterations": [r.outer_iterations for r in res],
+                           "inner_iterations": [r.inner_iterations for r in res],
+                           "rel_err_vs_fp64_solution": rel_err,
+                           "final_rel_residual_fp64": float(np.sqrt(res[-1].rnorm_sq
+                                                                    / res[-1].rnorm0_sq))},
+                "fp64_plain": {"value": world * n_dofs / (ms64 * 1e-3) / 1e9, "unit": UNIT,
+                               "ms_per_step": ms64,
+                               "cg_iterations": [r.iterations for r in res64],
+                               "speedup_of_mixed": ms64 / ms_max},
                 "e2e": {"value": e2e_value, "unit": UNIT,
                         "h2d_bytes_per_step": int(kappa.nbytes + f.nbytes),
                         "d2h_bytes_per_step": int(n_dofs * 8)},
-                "roofline": {"bound": "hbm", "kernel": "k_spmv_csr<16,f64> (CG operator)",
-                             "achieved": achieved, "peak": peak, "unit": "GB/s",
-                             "frac": achieved / peak, "peak_source": peak_kind,
-                             "alg_bytes_per_launch": alg_bytes, "launch_ms": spmv_ms,
-                             "traffic": traffic},
+                "roofline": {"bound": "hbm", "kernel": "k_sell_spmv<float,16-bit cols> (inner CG)",
+                             "achieved": ach32, "peak": peak, "unit": "GB/s",
+                             "frac": ach32 / peak, "peak_source": peak_kind,
+                             "alg_bytes_per_launch": alg32, "launch_ms": ms32,
+                             "padding": info32["padding"],
+                             "traffic": profile_traffic("sell_f32_c2")},
+                "roofline_fp64_operator": {"achieved": ach64, "frac": ach64 / peak,
+                                           "alg_bytes_per_launch": alg64, "launch_ms": ms64k,
+                                           "traffic": profile_traffic("sell_f64_c2")},
                 "gpu_launches": launches,
                 "clocks": clocks,
                 "cpu_baseline": cpu}

@@ -33,6 +33,9 @@ MODE_COLOURED = 1
 F64 = 0
 F32 = 1
 
+IR_RESTART = 0
+IR_RELIABLE = 1
+
 
 class DfxError(RuntimeError):
     def __init__(self, code: int, msg: str):
@@ -77,6 +80,19 @@ class CgInfo(C.Structure):
         ("status", C.c_int32),
         ("rnorm0_sq", C.c_double),
         ("rnorm_sq", C.c_double),
+        ("kernel_launches", C.c_int64),
+    ]
+
+
+class IrInfo(C.Structure):
+    _fields_ = [
+        ("outer_iterations", C.c_int32),
+        ("inner_iterations", C.c_int32),
+        ("status", C.c_int32),
+        ("reserved", C.c_int32),
+        ("rnorm0_sq", C.c_double),
+        ("rnorm_sq", C.c_double),
+        ("kernel_launches", C.c_int64),
     ]
 
 
@@ -105,6 +121,20 @@ _SIGS = {
     "dfx_cg_workspace_bytes": (C.c_size_t, [C.c_int64]),
     "dfx_cg_solve": (C.c_int, [C.POINTER(Csr), _P, _P, _P, C.c_double, C.c_int32, C.c_int32, _P,
                                C.c_size_t, C.POINTER(CgInfo), _P]),
+    "dfx_operator_create": (C.c_int, [C.POINTER(Csr), C.c_int32, C.c_int32, C.c_int32,
+                                      C.POINTER(C.c_void_p), _P]),
+    "dfx_operator_update_values": (C.c_int, [_P, C.POINTER(Csr), _P]),
+    "dfx_operator_apply": (C.c_int, [_P, _P, _P, _P]),
+    "dfx_operator_apply_renumbered": (C.c_int, [_P, _P, _P, _P]),
+    "dfx_operator_info": (C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int32),
+                                    C.POINTER(C.c_void_p)]),
+    "dfx_operator_destroy": (C.c_int, [_P]),
+    "dfx_cg_op_workspace_bytes": (C.c_size_t, [C.c_int64]),
+    "dfx_cg_solve_op": (C.c_int, [_P, _P, _P, _P, C.c_double, C.c_int32, C.c_int32, _P,
+                                  C.c_size_t, C.POINTER(CgInfo), _P]),
+    "dfx_ir_workspace_bytes": (C.c_size_t, [C.c_int64]),
+    "dfx_ir_solve": (C.c_int, [_P, _P, _P, _P, _P, C.c_double, C.c_double, C.c_int32, C.c_int32,
+                               C.c_int32, C.c_int32, _P, C.c_size_t, C.POINTER(IrInfo), _P]),
 }
 
 _lib = None

@@ -1,18 +1,25 @@
-// Jacobi-preconditioned conjugate gradients on the device.
+// Conjugate gradients on the device: FP64 Jacobi-PCG (CSR or sliced-ELL
+// operator) and FP32-inner / FP64-outer iterative refinement.
 //
-// The iteration of the reference demo (cpp/demo/poisson_matrix_free/
-// main.cpp:84-132) as three fused kernels per iteration:
-//   1. y = A p and p.y           (SpMV with a fused dot product)
-//   2. x += a p, r -= a y, z = D^{-1} r, r.r and r.z, convergence test
+// One PCG iteration (the demo's loop, cpp/demo/poisson_matrix_free/
+// main.cpp:84-132, with z = D^{-1} r) is three kernels:
+//   1. y = A p and p.y          (SpMV with a fused dot product)
+//   2. x += a p, r -= a y, r.r and r.z with z = D^{-1} r; convergence test
 //   3. p = z + b p
-// Every reduction is two-stage and deterministic: per-block partial sums,
-// then the last block to finish (atomic ticket) sums the partials in index
-// order and updates the scalar state in device memory. Scalars never leave
-// the device; kernels return immediately once the state says "done", so a
-// CUDA graph of K iterations is replayed until the host sees done.
+// Reductions are two-stage and deterministic: per-block partial sums in
+// FP64, then the last block to finish (atomic ticket) sums the partials in
+// index order and updates the scalar state in device memory. Scalars never
+// leave the device; every kernel returns at once when the state says done,
+// so a CUDA graph of K iterations is replayed until the host reads done.
+//
+// Mixed precision: the refinement loop keeps the residual r = b - A x, its
+// norm and the update x += d in FP64 with the FP64 operator; the inner
+// solve A d = r runs the same PCG with FP32 values, FP32 vectors and the
+// 16-bit-column operator. Its dot products sum FP32 products per thread
+// (a thread owns ~16 entries) and reduce the per-thread sums in FP64.
 #include "la_kernels.cuh"
+#include "sell.cuh"
 
-#include <cstring>
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -30,109 +37,210 @@ struct CgState
   double alpha;
   double beta;
   double rtol2;
+  double rmax2;  // reliable updates: largest |r|^2 since the last update
+  double delta2; // reliable updates: update when |r|^2 < delta2 * rmax2
   int32_t iter;
   int32_t max_iter;
   int32_t done;
   int32_t status;
+  int32_t updates; // reliable updates performed
+  int32_t pad;
   unsigned int ticket[4];
 };
 
-struct Work
-{
-  CgState* st;
-  double* part0;
-  double* part1;
-  double* r;
-  double* p;
-  double* y;
-  int blocks;
-};
+// Internal pause codes of the reliable-update solve (never returned).
+constexpr int32_t kPauseUpdate = 100;    // residual dropped by delta: replace it
+constexpr int32_t kPauseConverged = 101; // iterated residual converged: verify in FP64
 
 size_t align256(size_t b) { return (b + 255) & ~size_t(255); }
 
-int grid_blocks() { return 4 * dfx::num_sms(); }
+// Sliced-ELL kernels: 128 threads, one slice (32 rows) per warp; the
+// hardware block scheduler balances slices of different lengths.
+constexpr int kSellThreads = 128;
+int sell_blocks(int64_t n) { return (int)std::max<int64_t>(1, (((n + 31) / 32) + 3) / 4); }
 
-size_t work_bytes(int64_t n, int blocks)
+// Grid of the grid-stride kernels without SpMV (init, correction, CSR).
+int stride_grid() { return 8 * dfx::num_sms(); }
+
+// Elementwise kernels: 256 threads x 8 entries per block and round, all
+// loads of a round issued before any use.
+constexpr int kElemThreads = 256;
+constexpr int kElemPerThread = 8;
+int elem_grid(int64_t n)
 {
-  return align256(sizeof(CgState)) + 2 * align256(sizeof(double) * blocks)
-         + 3 * align256(sizeof(double) * (size_t)n);
+  const int64_t per = (int64_t)kElemThreads * kElemPerThread;
+  return (int)std::max<int64_t>(1, (n + per - 1) / per);
 }
 
-Work carve(void* w, int64_t n, int blocks)
+// Largest grid of any CG kernel for n unknowns (sizes the partial sums).
+int max_blocks(int64_t n)
 {
-  char* p = (char*)w;
-  Work k;
-  k.st = (CgState*)p;
-  p += align256(sizeof(CgState));
-  k.part0 = (double*)p;
-  p += align256(sizeof(double) * blocks);
-  k.part1 = (double*)p;
-  p += align256(sizeof(double) * blocks);
-  k.r = (double*)p;
-  p += align256(sizeof(double) * n);
-  k.p = (double*)p;
-  p += align256(sizeof(double) * n);
-  k.y = (double*)p;
-  k.blocks = blocks;
-  return k;
+  return std::max({sell_blocks(n), elem_grid(n), stride_grid()});
 }
 
-// Publish this block's partial sums; returns true in the last block.
-__device__ __forceinline__ bool publish(double v0, double v1, double* p0, double* p1,
+// Blocks per reduction group of the two-level reduction.
+constexpr int kGroup = 64;
+int groups_of(int blocks) { return (blocks + kGroup - 1) / kGroup; }
+
+// Carves typed arrays out of a workspace (p == nullptr: only counts).
+struct Carver
+{
+  char* p;
+  size_t used = 0;
+  template <typename T>
+  T* take(size_t count)
+  {
+    T* r = p ? (T*)(p + used) : nullptr;
+    used += align256(sizeof(T) * count);
+    return r;
+  }
+};
+
+// Buffers of the deterministic two-level reduction: per-block partial sums,
+// per-group sums, per-group tickets.
+struct Red
+{
+  double* part0;
+  double* part1;
+  double* gpart0;
+  double* gpart1;
+  unsigned int* gticket;
+};
+
+Red carve_red(Carver& c, int blocks)
+{
+  Red r;
+  r.part0 = c.take<double>(blocks);
+  r.part1 = c.take<double>(blocks);
+  r.gpart0 = c.take<double>(groups_of(blocks));
+  r.gpart1 = c.take<double>(groups_of(blocks));
+  r.gticket = c.take<unsigned int>(groups_of(blocks));
+  return r;
+}
+
+template <typename T>
+struct Work
+{
+  CgState* st;
+  Red red;
+  T* r;
+  T* p;
+  T* y;
+  int blocks;
+};
+
+template <typename T>
+Work<T> carve_work(Carver& c, int64_t n)
+{
+  Work<T> w;
+  w.blocks = max_blocks(n);
+  w.st = c.take<CgState>(1);
+  w.red = carve_red(c, w.blocks);
+  w.r = c.take<T>(n);
+  w.p = c.take<T>(n);
+  w.y = c.take<T>(n);
+  return w;
+}
+
+// Zero the state and the group tickets of a work area.
+int reset_work(CgState* st, const Red& red, int blocks, cudaStream_t s)
+{
+  DFX_CUDA(cudaMemsetAsync(st, 0, sizeof(CgState), s));
+  DFX_CUDA(cudaMemsetAsync(red.gticket, 0, sizeof(unsigned int) * groups_of(blocks), s));
+  return DFX_OK;
+}
+
+// Publish this block's partial sums. The last block of each group of
+// kGroup blocks sums its group in index order; the last group to finish
+// returns true (in every thread of its block), with the group sums ready in
+// red.gpart0/1. Both levels use fixed summation orders, so the result does
+// not depend on block scheduling.
+__device__ __forceinline__ bool publish(double v0, double v1, const Red& red,
                                         unsigned int* ticket, bool two)
 {
   __shared__ double sh[32];
-  __shared__ bool last;
+  __shared__ int in_group_last, last;
   v0 = dfx::block_sum(v0, sh);
   if (two)
     v1 = dfx::block_sum(v1, sh);
+  const unsigned g = blockIdx.x / kGroup;
+  const unsigned ng = (gridDim.x + kGroup - 1) / kGroup;
+  const unsigned gsize = min((unsigned)kGroup, gridDim.x - g * kGroup);
   if (threadIdx.x == 0)
   {
-    p0[blockIdx.x] = v0;
+    red.part0[blockIdx.x] = v0;
     if (two)
-      p1[blockIdx.x] = v1;
+      red.part1[blockIdx.x] = v1;
     __threadfence();
-    last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+    in_group_last = atomicAdd(&red.gticket[g], 1u) == gsize - 1;
+  }
+  __syncthreads();
+  if (!in_group_last)
+    return false;
+  if (threadIdx.x < 32)
+  {
+    double s0 = 0.0, s1 = 0.0;
+    for (unsigned i = threadIdx.x; i < gsize; i += 32)
+    {
+      s0 += __ldcg(red.part0 + g * kGroup + i);
+      if (two)
+        s1 += __ldcg(red.part1 + g * kGroup + i);
+    }
+    s0 = dfx::warp_sum(s0);
+    if (two)
+      s1 = dfx::warp_sum(s1);
+    if (threadIdx.x == 0)
+    {
+      red.gpart0[g] = s0;
+      if (two)
+        red.gpart1[g] = s1;
+      red.gticket[g] = 0;
+      __threadfence();
+      last = atomicAdd(ticket, 1u) == ng - 1;
+    }
   }
   __syncthreads();
   return last;
 }
 
-// Deterministic sum of gridDim.x partials (called by the last block).
-__device__ __forceinline__ double final_sum(const double* p)
+// Deterministic sum of the group sums; all threads of the final block call
+// it, thread 0 gets the result.
+__device__ __forceinline__ double final_sum(const double* gpart)
 {
   __shared__ double sh[32];
+  const int ng = (gridDim.x + kGroup - 1) / kGroup;
   double s = 0.0;
-  for (int i = threadIdx.x; i < (int)gridDim.x; i += blockDim.x)
-    s += __ldcg(p + i);
+  for (int i = threadIdx.x; i < ng; i += blockDim.x)
+    s += __ldcg(gpart + i);
   return dfx::block_sum(s, sh);
 }
 
-__device__ __forceinline__ bool is_done(const CgState* st)
-{
-  return __ldcg(&st->done) != 0;
-}
+__device__ __forceinline__ bool is_done(const CgState* st) { return __ldcg(&st->done) != 0; }
 
-template <bool PRE>
+// r = rhs - Ax (Ax == nullptr: x0 = 0 and x is zeroed), z = D^{-1} r,
+// p = z; state initialised. rhs may alias w.r.
+template <typename T, bool PRE>
 __global__ void __launch_bounds__(kThreads)
-    k_cg_init(const double* __restrict__ b, const double* __restrict__ dinv, int64_t n,
-              Work w, double rtol2, int max_iter)
+    k_init(const T* rhs, const T* __restrict__ Ax, T* __restrict__ x, const T* __restrict__ dinv,
+           int64_t n, Work<T> w, double rtol2, int max_iter)
 {
-  double rr = 0.0, rz = 0.0;
+  T rr = 0, rz = 0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
   {
-    const double r = b[i] - w.y[i];
-    const double z = PRE ? dinv[i] * r : r;
+    const T r = Ax ? rhs[i] - Ax[i] : rhs[i];
+    const T z = PRE ? dinv[i] * r : r;
+    if (!Ax)
+      x[i] = T(0);
     w.r[i] = r;
     w.p[i] = z;
     rr += r * r;
     rz += r * z;
   }
-  if (publish(rr, rz, w.part0, w.part1, &w.st->ticket[0], true))
+  if (publish((double)rr, (double)rz, w.red, &w.st->ticket[0], true))
   {
-    const double srr = final_sum(w.part0);
-    const double srz = final_sum(w.part1);
+    const double srr = final_sum(w.red.gpart0);
+    const double srz = final_sum(w.red.gpart1);
     if (threadIdx.x == 0)
     {
       CgState* st = w.st;
@@ -150,11 +258,30 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
-// y = A p and p.y; alpha = rz / p.y.
+// Last block of an SpMV-dot kernel: alpha = rz / p.Ap.
+__device__ __forceinline__ void finish_pap(const double* part, CgState* st)
+{
+  const double pAp = final_sum(part);
+  if (threadIdx.x == 0)
+  {
+    st->pAp = pAp;
+    if (!(pAp > 0.0) || !isfinite(pAp))
+    {
+      st->status = DFX_ERR_BREAKDOWN;
+      st->done = 1;
+    }
+    else
+      st->alpha = st->rz / pAp;
+    st->ticket[1] = 0;
+    __threadfence();
+  }
+}
+
+// y = A p, p.y -- CSR operator (L lanes per row, or 8 lanes per 3x3 block row).
 template <int L, int BS>
 __global__ void __launch_bounds__(kThreads)
-    k_cg_spmv_dot(int32_t nrows, const int64_t* __restrict__ rp, const int32_t* __restrict__ cols,
-                  const double* __restrict__ vals, Work w)
+    k_spmv_dot_csr(int32_t nrows, const int64_t* __restrict__ rp, const int32_t* __restrict__ cols,
+                   const double* __restrict__ vals, Work<double> w)
 {
   if (is_done(w.st))
     return;
@@ -199,57 +326,91 @@ __global__ void __launch_bounds__(kThreads)
       }
     }
   }
-  if (publish(dot, 0.0, w.part0, nullptr, &w.st->ticket[1], false))
-  {
-    const double pAp = final_sum(w.part0);
-    if (threadIdx.x == 0)
-    {
-      CgState* st = w.st;
-      st->pAp = pAp;
-      if (!(pAp > 0.0) || !isfinite(pAp))
-      {
-        st->status = DFX_ERR_BREAKDOWN;
-        st->done = 1;
-      }
-      else
-        st->alpha = st->rz / pAp;
-      st->ticket[1] = 0;
-      __threadfence();
-    }
-  }
+  if (publish(dot, 0.0, w.red, &w.st->ticket[1], false))
+    finish_pap(w.red.gpart0, w.st);
 }
 
-template <bool PRE>
-__global__ void __launch_bounds__(kThreads)
-    k_cg_update(double* __restrict__ x, const double* __restrict__ dinv, int64_t n, Work w)
+// y = A p, p.y -- sliced-ELL operator, one row per lane, warp per slice.
+template <typename V, typename T, bool COMP>
+__global__ void __launch_bounds__(kSellThreads)
+    k_spmv_dot_sell(const dfx_operator_s op, Work<T> w)
 {
   if (is_done(w.st))
     return;
-  const double alpha = __ldcg(&w.st->alpha);
-  double rr = 0.0, rz = 0.0;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * blockDim.x)
+  const int lane = threadIdx.x & 31;
+  const dfx::SliceRange sr = dfx::block_slices(op.nslices);
+  T dot = 0;
+  for (int32_t s = sr.begin; s < sr.end; s += sr.step)
   {
-    x[i] += alpha * w.p[i];
-    const double r = w.r[i] - alpha * w.y[i];
-    w.r[i] = r;
-    const double z = PRE ? dinv[i] * r : r;
-    rr += r * r;
-    rz += r * z;
+    const T acc = dfx::sell_row<V, T, T, COMP>(op, (const V*)op.vals, w.p, s, lane);
+    const int32_t row = 32 * s + lane;
+    if (row < op.n)
+    {
+      w.y[row] = acc;
+      dot += acc * w.p[row];
+    }
   }
-  if (publish(rr, rz, w.part0, w.part1, &w.st->ticket[2], true))
+  if (publish((double)dot, 0.0, w.red, &w.st->ticket[1], false))
+    finish_pap(w.red.gpart0, w.st);
+}
+
+template <typename T, bool PRE, bool RELIABLE>
+__global__ void __launch_bounds__(kElemThreads)
+    k_update(T* __restrict__ x, const T* __restrict__ dinv, int64_t n, Work<T> w)
+{
+  if (is_done(w.st))
+    return;
+  const T alpha = (T)__ldcg(&w.st->alpha);
+  T rr = 0, rz = 0;
+  constexpr int E = kElemPerThread;
+  const int64_t stride = (int64_t)gridDim.x * kElemThreads * E;
+  for (int64_t base = (int64_t)blockIdx.x * kElemThreads * E + threadIdx.x; base < n;
+       base += stride)
   {
-    const double srr = final_sum(w.part0);
-    const double srz = final_sum(w.part1);
+    T p[E], y[E], r[E], xv[E], d[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e)
+    {
+      const int64_t i = base + (int64_t)e * kElemThreads;
+      const bool ok = i < n;
+      p[e] = ok ? w.p[i] : T(0);
+      y[e] = ok ? w.y[i] : T(0);
+      r[e] = ok ? w.r[i] : T(0);
+      xv[e] = ok ? x[i] : T(0);
+      d[e] = (ok && PRE) ? dinv[i] : T(1);
+    }
+#pragma unroll
+    for (int e = 0; e < E; ++e)
+    {
+      const int64_t i = base + (int64_t)e * kElemThreads;
+      if (i >= n)
+        continue;
+      x[i] = xv[e] + alpha * p[e];
+      const T rn = r[e] - alpha * y[e];
+      w.r[i] = rn;
+      rr += rn * rn;
+      rz += rn * (PRE ? d[e] * rn : rn);
+    }
+  }
+  if (publish((double)rr, (double)rz, w.red, &w.st->ticket[2], true))
+  {
+    const double srr = final_sum(w.red.gpart0);
+    const double srz = final_sum(w.red.gpart1);
     if (threadIdx.x == 0)
     {
       CgState* st = w.st;
       st->rr = srr;
       st->iter += 1;
-      st->beta = srz / st->rz;
-      st->rz = srz;
+      bool pause = false;
       if (srr / st->rr0 < st->rtol2)
+      {
         st->done = 1;
+        if (RELIABLE)
+        {
+          st->status = kPauseConverged;
+          pause = true;
+        }
+      }
       else if (!isfinite(srr))
       {
         st->status = DFX_ERR_BREAKDOWN;
@@ -260,69 +421,361 @@ __global__ void __launch_bounds__(kThreads)
         st->status = DFX_ERR_NOT_CONVERGED;
         st->done = 1;
       }
+      else if (RELIABLE && srr < st->delta2 * st->rmax2)
+      {
+        st->status = kPauseUpdate;
+        st->done = 1;
+        pause = true;
+      }
+      // A pause keeps rz = r_old.z_old: beta is formed after the residual
+      // has been replaced.
+      if (!pause)
+      {
+        st->beta = srz / st->rz;
+        st->rz = srz;
+        if (RELIABLE)
+          st->rmax2 = fmax(st->rmax2, srr);
+      }
       st->ticket[2] = 0;
       __threadfence();
     }
   }
 }
 
-template <bool PRE>
-__global__ void __launch_bounds__(kThreads)
-    k_cg_pupdate(const double* __restrict__ dinv, int64_t n, Work w)
+template <typename T, bool PRE>
+__global__ void __launch_bounds__(kElemThreads)
+    k_pupdate(const T* __restrict__ dinv, int64_t n, Work<T> w)
 {
   if (is_done(w.st))
     return;
-  const double beta = __ldcg(&w.st->beta);
+  const T beta = (T)__ldcg(&w.st->beta);
+  constexpr int E = kElemPerThread;
+  const int64_t stride = (int64_t)gridDim.x * kElemThreads * E;
+  for (int64_t base = (int64_t)blockIdx.x * kElemThreads * E + threadIdx.x; base < n;
+       base += stride)
+  {
+    T p[E], r[E], d[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e)
+    {
+      const int64_t i = base + (int64_t)e * kElemThreads;
+      const bool ok = i < n;
+      p[e] = ok ? w.p[i] : T(0);
+      r[e] = ok ? w.r[i] : T(0);
+      d[e] = (ok && PRE) ? dinv[i] : T(1);
+    }
+#pragma unroll
+    for (int e = 0; e < E; ++e)
+    {
+      const int64_t i = base + (int64_t)e * kElemThreads;
+      if (i < n)
+        w.p[i] = (PRE ? d[e] * r[e] : r[e]) + beta * p[e];
+    }
+  }
+}
+
+// Outer residual of the refinement: r = b - A x in FP64 with the FP64
+// operator, |r|^2 in FP64, r handed to the inner solve in FP32. The outer
+// state counts residual evaluations; the first one sets |r0|^2.
+__global__ void __launch_bounds__(kSellThreads)
+    k_ir_residual(const dfx_operator_s op, const double* __restrict__ b,
+                  const double* __restrict__ x, float* __restrict__ r32, CgState* st,
+                  Red red, double rtol2, int max_outer)
+{
+  const int lane = threadIdx.x & 31;
+  const dfx::SliceRange sr = dfx::block_slices(op.nslices);
+  double rr = 0.0;
+  for (int32_t s = sr.begin; s < sr.end; s += sr.step)
+  {
+    const double ax = dfx::sell_row<double, double, double, false>(op, (const double*)op.vals, x,
+                                                                   s, lane);
+    const int32_t row = 32 * s + lane;
+    if (row < op.n)
+    {
+      const double r = b[row] - ax;
+      r32[row] = (float)r;
+      rr += r * r;
+    }
+  }
+  if (publish(rr, 0.0, red, &st->ticket[3], false))
+  {
+    const double srr = final_sum(red.gpart0);
+    if (threadIdx.x == 0)
+    {
+      if (st->iter == 0)
+      {
+        st->rr0 = srr;
+        st->status = DFX_OK;
+      }
+      st->rr = srr;
+      st->iter += 1;
+      if (srr == 0.0 || srr / st->rr0 < rtol2)
+        st->done = 1;
+      else if (!isfinite(srr))
+      {
+        st->status = DFX_ERR_BREAKDOWN;
+        st->done = 1;
+      }
+      else if (st->iter > max_outer)
+      {
+        st->status = DFX_ERR_NOT_CONVERGED;
+        st->done = 1;
+      }
+      st->ticket[3] = 0;
+      __threadfence();
+    }
+  }
+}
+
+// x += d in FP64; d is reset to zero for the next correction.
+__global__ void k_ir_correct(double* __restrict__ x, float* __restrict__ d, int64_t n)
+{
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
   {
-    const double z = PRE ? dinv[i] * w.r[i] : w.r[i];
-    w.p[i] = z + beta * w.p[i];
+    x[i] += (double)d[i];
+    d[i] = 0.0f;
   }
 }
 
-// Enqueue one CG iteration.
-void enqueue_iteration(const dfx_csr* A, double* x, const double* dinv, int64_t n, const Work& w,
-                       cudaStream_t s)
+// Reliable update (residual replacement): r = b - A x in FP64 with the FP64
+// operator; the FP32 iterated residual is replaced by it, |r|^2 and r.z are
+// formed in FP64, and beta = (r.z)_new / (r.z)_old keeps the search
+// direction. The first call (iter == 0) initialises |r0|^2 and sets beta = 0
+// (p is zero then, so the following p = z + beta p gives p = z).
+template <bool PRE>
+__global__ void __launch_bounds__(kSellThreads)
+    k_rel_residual(const dfx_operator_s op, const double* __restrict__ b,
+                   const double* __restrict__ x, const float* __restrict__ dinv32, Work<float> w)
 {
-  const int blocks = w.blocks;
-  const double* vals = (const double*)A->vals;
-  if (A->bs == 1)
+  const int lane = threadIdx.x & 31;
+  const dfx::SliceRange sr = dfx::block_slices(op.nslices);
+  double rr = 0.0, rz = 0.0;
+  for (int32_t s = sr.begin; s < sr.end; s += sr.step)
   {
-    switch (dfx::spmv_lanes(A))
+    const double ax = dfx::sell_row<double, double, double, false>(op, (const double*)op.vals, x,
+                                                                   s, lane);
+    const int32_t row = 32 * s + lane;
+    if (row < op.n)
     {
-    case 4:
-      k_cg_spmv_dot<4, 1><<<blocks, kThreads, 0, s>>>(A->nrows, A->row_ptr, A->cols, vals, w);
-      break;
-    case 8:
-      k_cg_spmv_dot<8, 1><<<blocks, kThreads, 0, s>>>(A->nrows, A->row_ptr, A->cols, vals, w);
-      break;
-    case 16:
-      k_cg_spmv_dot<16, 1><<<blocks, kThreads, 0, s>>>(A->nrows, A->row_ptr, A->cols, vals, w);
-      break;
-    default:
-      k_cg_spmv_dot<32, 1><<<blocks, kThreads, 0, s>>>(A->nrows, A->row_ptr, A->cols, vals, w);
+      const double r = b[row] - ax;
+      const float r32 = (float)r;
+      w.r[row] = r32;
+      rr += r * r;
+      const double z = PRE ? (double)(dinv32[row] * r32) : (double)r32;
+      rz += (double)r32 * z;
     }
   }
-  else
-    k_cg_spmv_dot<8, 3><<<blocks, kThreads, 0, s>>>(A->nrows, A->row_ptr, A->cols, vals, w);
-  if (dinv)
+  if (publish(rr, rz, w.red, &w.st->ticket[3], true))
   {
-    k_cg_update<true><<<blocks, kThreads, 0, s>>>(x, dinv, n, w);
-    k_cg_pupdate<true><<<blocks, kThreads, 0, s>>>(dinv, n, w);
-  }
-  else
-  {
-    k_cg_update<false><<<blocks, kThreads, 0, s>>>(x, dinv, n, w);
-    k_cg_pupdate<false><<<blocks, kThreads, 0, s>>>(dinv, n, w);
+    const double srr = final_sum(w.red.gpart0);
+    const double srz = final_sum(w.red.gpart1);
+    if (threadIdx.x == 0)
+    {
+      CgState* st = w.st;
+      const bool first = st->iter == 0 && st->updates == 0;
+      if (first)
+        st->rr0 = srr;
+      st->rr = srr;
+      st->rmax2 = srr;
+      st->updates += first ? 0 : 1;
+      if (srr == 0.0 || srr / st->rr0 < st->rtol2)
+      {
+        st->status = DFX_OK;
+        st->done = 1;
+      }
+      else if (!isfinite(srr))
+      {
+        st->status = DFX_ERR_BREAKDOWN;
+        st->done = 1;
+      }
+      else
+      {
+        st->beta = first ? 0.0 : srz / st->rz;
+        st->rz = srz;
+        st->status = DFX_OK;
+        st->done = 0;
+      }
+      st->ticket[3] = 0;
+      __threadfence();
+    }
   }
 }
 
-// Graphs of K iterations, cached by the pointers and sizes they bake in.
-using GraphKey = std::tuple<const void*, const void*, const void*, const void*, int64_t, int64_t,
-                            int, const void*, const void*, const void*, int, int, int>;
+template <typename TI, typename TO>
+__global__ void k_gather(const TI* __restrict__ in, TO* __restrict__ out,
+                         const int32_t* __restrict__ perm, int32_t n)
+{
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n)
+    out[i] = (TO)in[perm[i]];
+}
+
+__global__ void k_scatter(const double* __restrict__ in, double* __restrict__ out,
+                          const int32_t* __restrict__ perm, int32_t n)
+{
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n)
+    out[perm[i]] = in[i];
+}
+
+// ------------------------------------------------------------ enqueueing
+enum OpKind
+{
+  kCsr = 0,
+  kSell = 1
+};
+
+struct OpRef
+{
+  OpKind kind;
+  const dfx_csr* A;          // kCsr
+  const dfx_operator_s* op;  // kSell
+};
+
+template <typename T>
+void enqueue_spmv_dot(const OpRef& o, const Work<T>& w, cudaStream_t s);
+
+template <>
+void enqueue_spmv_dot<double>(const OpRef& o, const Work<double>& w, cudaStream_t s)
+{
+  const int blocks = stride_grid();
+  if (o.kind == kSell)
+  {
+    k_spmv_dot_sell<double, double, false><<<sell_blocks(o.op->n), kSellThreads, 0, s>>>(*o.op,
+                                                                                       w);
+    return;
+  }
+  const dfx_csr* A = o.A;
+  const double* vals = (const double*)A->vals;
+  if (A->bs == 3)
+  {
+    k_spmv_dot_csr<8, 3><<<blocks, kThreads, 0, s>>>(A->nrows, A->row_ptr, A->cols, vals, w);
+    return;
+  }
+  switch (dfx::spmv_lanes(A))
+  {
+  case 4:
+    k_spmv_dot_csr<4, 1><<<blocks, kThreads, 0, s>>>(A->nrows, A->row_ptr, A->cols, vals, w);
+    break;
+  case 8:
+    k_spmv_dot_csr<8, 1><<<blocks, kThreads, 0, s>>>(A->nrows, A->row_ptr, A->cols, vals, w);
+    break;
+  case 16:
+    k_spmv_dot_csr<16, 1><<<blocks, kThreads, 0, s>>>(A->nrows, A->row_ptr, A->cols, vals, w);
+    break;
+  default:
+    k_spmv_dot_csr<32, 1><<<blocks, kThreads, 0, s>>>(A->nrows, A->row_ptr, A->cols, vals, w);
+  }
+}
+
+template <>
+void enqueue_spmv_dot<float>(const OpRef& o, const Work<float>& w, cudaStream_t s)
+{
+  if (o.op->compressed)
+    k_spmv_dot_sell<float, float, true><<<sell_blocks(o.op->n), kSellThreads, 0, s>>>(*o.op, w);
+  else
+    k_spmv_dot_sell<float, float, false><<<sell_blocks(o.op->n), kSellThreads, 0, s>>>(*o.op, w);
+}
+
+template <typename T>
+void enqueue_pupdate(const T* dinv, int64_t n, const Work<T>& w, cudaStream_t s)
+{
+  const int g = elem_grid(n);
+  if (dinv)
+    k_pupdate<T, true><<<g, kElemThreads, 0, s>>>(dinv, n, w);
+  else
+    k_pupdate<T, false><<<g, kElemThreads, 0, s>>>(dinv, n, w);
+}
+
+template <typename T>
+void enqueue_iteration(const OpRef& o, T* x, const T* dinv, int64_t n, const Work<T>& w,
+                       bool reliable, cudaStream_t s)
+{
+  enqueue_spmv_dot<T>(o, w, s);
+  const int g = elem_grid(n);
+  if (dinv)
+  {
+    if (reliable)
+      k_update<T, true, true><<<g, kElemThreads, 0, s>>>(x, dinv, n, w);
+    else
+      k_update<T, true, false><<<g, kElemThreads, 0, s>>>(x, dinv, n, w);
+  }
+  else
+  {
+    if (reliable)
+      k_update<T, false, true><<<g, kElemThreads, 0, s>>>(x, dinv, n, w);
+    else
+      k_update<T, false, false><<<g, kElemThreads, 0, s>>>(x, dinv, n, w);
+  }
+  enqueue_pupdate<T>(dinv, n, w, s);
+}
+
+template <typename T>
+void enqueue_init(const T* rhs, const T* Ax, T* x, const T* dinv, int64_t n, const Work<T>& w,
+                  double rtol, int max_iters, cudaStream_t s)
+{
+  if (dinv)
+    k_init<T, true><<<stride_grid(), kThreads, 0, s>>>(rhs, Ax, x, dinv, n, w, rtol * rtol,
+                                                       max_iters);
+  else
+    k_init<T, false><<<stride_grid(), kThreads, 0, s>>>(rhs, Ax, x, dinv, n, w, rtol * rtol,
+                                                        max_iters);
+}
+
+// Graphs of K iterations, cached by everything they bake in.
+using GraphKey = std::tuple<int, const void*, const void*, const void*, const void*, const void*,
+                            const void*, int64_t, int, int, int>;
 std::mutex g_graph_mutex;
 std::map<GraphKey, cudaGraphExec_t> g_graphs;
+
+template <typename T>
+int iteration_graph(const OpRef& o, T* x, const T* dinv, int64_t n, const Work<T>& w, int K,
+                    bool reliable, cudaGraphExec_t* out)
+{
+  GraphKey key{(int)o.kind * 4 + (sizeof(T) == 4) * 2 + (reliable ? 1 : 0),
+               o.kind == kSell ? (const void*)o.op : (const void*)o.A->row_ptr,
+               o.kind == kSell ? (const void*)o.op->vals : (const void*)o.A->vals,
+               o.kind == kSell ? nullptr : (const void*)o.A->cols,
+               (const void*)x,
+               (const void*)dinv,
+               (const void*)w.st,
+               n,
+               K,
+               w.blocks,
+               o.kind == kCsr ? o.A->bs : 1};
+  std::lock_guard<std::mutex> lk(g_graph_mutex);
+  auto it = g_graphs.find(key);
+  if (it != g_graphs.end())
+  {
+    *out = it->second;
+    return DFX_OK;
+  }
+  cudaStream_t cs;
+  DFX_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+  cudaGraph_t graph;
+  cudaError_t ce = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+  if (ce == cudaSuccess)
+  {
+    for (int k = 0; k < K; ++k)
+      enqueue_iteration<T>(o, x, dinv, n, w, reliable, cs);
+    ce = cudaStreamEndCapture(cs, &graph);
+  }
+  cudaStreamDestroy(cs);
+  DFX_CUDA(ce);
+  cudaGraphExec_t exec;
+  ce = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  DFX_CUDA(ce);
+  if (g_graphs.size() >= 32)
+  {
+    cudaGraphExecDestroy(g_graphs.begin()->second);
+    g_graphs.erase(g_graphs.begin());
+  }
+  g_graphs[key] = exec;
+  *out = exec;
+  return DFX_OK;
+}
 
 struct PinnedState
 {
@@ -335,9 +788,98 @@ struct PinnedState
 };
 thread_local PinnedState t_pinned;
 
+int read_state(const CgState* d, CgState** h, cudaStream_t s)
+{
+  if (!t_pinned.h)
+    DFX_CUDA(cudaMallocHost(&t_pinned.h, 2 * sizeof(CgState)));
+  *h = t_pinned.h;
+  DFX_CUDA(cudaMemcpyAsync(*h, d, sizeof(CgState), cudaMemcpyDeviceToHost, s));
+  DFX_CUDA(cudaStreamSynchronize(s));
+  return DFX_OK;
+}
+
+// Replay the iteration graph until the state is done. Each replay runs K
+// iterations and the state is done at max_iter at the latest, so the loop
+// bound only guards against a corrupted state.
+int run_to_done(cudaGraphExec_t exec, const CgState* dst, int max_iters, int K, CgState** h,
+                cudaStream_t s, int64_t* kernels)
+{
+  const int64_t max_launches = (int64_t)max_iters / K + 2;
+  for (int64_t launch = 0;; ++launch)
+  {
+    if (int st = read_state(dst, h, s))
+      return st;
+    if ((*h)->done)
+      return DFX_OK;
+    if (launch > max_launches)
+      return dfx::fail(DFX_ERR_TIMEOUT, "CG state never reported completion");
+    DFX_CUDA(cudaGraphLaunch(exec, s));
+    *kernels += 3 * (int64_t)K;
+  }
+}
+
+int report(const CgState* h, dfx_cg_info* info, int64_t kernels)
+{
+  if (info)
+  {
+    info->iterations = h->iter;
+    info->status = h->status;
+    info->rnorm0_sq = h->rr0;
+    info->rnorm_sq = h->rr;
+    info->kernel_launches = kernels;
+  }
+  if (h->status == DFX_ERR_NOT_CONVERGED)
+    return dfx::fail(DFX_ERR_NOT_CONVERGED,
+                     "Solver exceeded max iterations (%d). Relative residual=%g.", h->iter,
+                     h->rr0 > 0 ? h->rr / h->rr0 : 0.0);
+  if (h->status == DFX_ERR_BREAKDOWN)
+    return dfx::fail(DFX_ERR_BREAKDOWN, "CG breakdown at iteration %d (p.Ap=%g)", h->iter, h->pAp);
+  return DFX_OK;
+}
+
+size_t csr_work_bytes(int64_t n)
+{
+  Carver c{nullptr};
+  carve_work<double>(c, n);
+  return c.used;
+}
+
+size_t op_work_bytes(int64_t n)
+{
+  Carver c{nullptr};
+  carve_work<double>(c, n);
+  c.take<double>(n); // x
+  c.take<double>(n); // b
+  c.take<double>(n); // dinv
+  return c.used;
+}
+
+size_t ir_work_bytes(int64_t n)
+{
+  Carver c{nullptr};
+  carve_work<float>(c, n);
+  c.take<CgState>(1);           // outer state
+  carve_red(c, max_blocks(n));  // outer reduction
+  c.take<double>(n); // x
+  c.take<double>(n); // b
+  c.take<double>(n); // dinv (unused FP64 copy kept for symmetry with op solve)
+  c.take<float>(n);  // d
+  c.take<float>(n);  // dinv32
+  return c.used;
+}
+
+int check_solve_args(const double* b, const double* x, const void* work, double rtol,
+                     int max_iters)
+{
+  DFX_REQUIRE(b && x && work, "b, x and workspace must be non-NULL");
+  DFX_REQUIRE(rtol > 0.0 && max_iters > 0, "rtol and max_iters must be positive");
+  DFX_REQUIRE(((uintptr_t)work & 255) == 0, "workspace must be 256-byte aligned");
+  return DFX_OK;
+}
+
 } // namespace
 
-extern "C" size_t dfx_cg_workspace_bytes(int64_t n) { return work_bytes(n, grid_blocks()); }
+extern "C" size_t dfx_cg_workspace_bytes(int64_t n) { return csr_work_bytes(n); }
 
 extern "C" int dfx_cg_solve(const dfx_csr* A, const double* d_b, double* d_x,
                             const double* d_dinv, double rtol, int32_t max_iters,
@@ -348,88 +890,245 @@ extern "C" int dfx_cg_solve(const dfx_csr* A, const double* d_b, double* d_x,
     return st;
   DFX_REQUIRE(A->dtype == DFX_F64, "dfx_cg_solve runs in FP64");
   DFX_REQUIRE(A->nrows == A->ncols, "matrix must be square");
-  DFX_REQUIRE(d_b && d_x && d_work, "b, x and workspace must be non-NULL");
-  DFX_REQUIRE(rtol > 0.0 && max_iters > 0, "rtol and max_iters must be positive");
+  if (int st = check_solve_args(d_b, d_x, d_work, rtol, max_iters))
+    return st;
   const int64_t n = (int64_t)A->nrows * A->bs;
-  const int blocks = grid_blocks();
-  DFX_REQUIRE(wbytes >= work_bytes(n, blocks), "workspace too small (%zu < %zu)", wbytes,
-              work_bytes(n, blocks));
-  DFX_REQUIRE(((uintptr_t)d_work & 255) == 0, "workspace must be 256-byte aligned");
+  DFX_REQUIRE(wbytes >= csr_work_bytes(n), "workspace too small (%zu < %zu)", wbytes,
+              csr_work_bytes(n));
   cudaStream_t s = dfx::as_stream(stream);
   const int K = graph_iters > 0 ? graph_iters : 20;
-  Work w = carve(d_work, n, blocks);
-  DFX_CUDA(cudaMemsetAsync(w.st, 0, sizeof(CgState), s));
-
-  // r0 = b - A x0, z0 = D^{-1} r0, p0 = z0.
-  dfx_csr Ay = *A;
-  if (int st = dfx::launch_spmv(&Ay, d_x, w.y, 0.0, s))
+  Carver c{(char*)d_work};
+  Work<double> w = carve_work<double>(c, n);
+  if (int st = reset_work(w.st, w.red, w.blocks, s))
     return st;
-  if (d_dinv)
-    k_cg_init<true><<<blocks, kThreads, 0, s>>>(d_b, d_dinv, n, w, rtol * rtol, max_iters);
-  else
-    k_cg_init<false><<<blocks, kThreads, 0, s>>>(d_b, d_dinv, n, w, rtol * rtol, max_iters);
+  if (int st = dfx::launch_spmv(A, d_x, w.y, 0.0, s))
+    return st;
+  enqueue_init<double>(d_b, w.y, d_x, d_dinv, n, w, rtol, max_iters, s);
   DFX_CHECK_LAUNCH();
+  OpRef o{kCsr, A, nullptr};
+  cudaGraphExec_t exec;
+  if (int st = iteration_graph<double>(o, d_x, d_dinv, n, w, K, false, &exec))
+    return st;
+  CgState* h;
+  int64_t kernels = 2;
+  if (int st = run_to_done(exec, w.st, max_iters, K, &h, s, &kernels))
+    return st;
+  return report(h, info, kernels);
+}
 
-  cudaGraphExec_t exec = nullptr;
+extern "C" size_t dfx_cg_op_workspace_bytes(int64_t n) { return op_work_bytes(n); }
+
+extern "C" int dfx_cg_solve_op(dfx_operator op, const double* d_b, double* d_x,
+                               const double* d_dinv, double rtol, int32_t max_iters,
+                               int32_t graph_iters, void* d_work, size_t wbytes, dfx_cg_info* info,
+                               void* stream)
+{
+  DFX_REQUIRE(op, "operator is NULL");
+  DFX_REQUIRE(op->dtype == DFX_F64, "dfx_cg_solve_op needs an FP64 operator");
+  if (int st = check_solve_args(d_b, d_x, d_work, rtol, max_iters))
+    return st;
+  const int64_t n = op->n;
+  DFX_REQUIRE(wbytes >= op_work_bytes(n), "workspace too small (%zu < %zu)", wbytes,
+              op_work_bytes(n));
+  if (n == 0)
+    return DFX_OK;
+  cudaStream_t s = dfx::as_stream(stream);
+  const int K = graph_iters > 0 ? graph_iters : 20;
+  Carver c{(char*)d_work};
+  Work<double> w = carve_work<double>(c, n);
+  double* xp = c.take<double>(n);
+  double* bp = c.take<double>(n);
+  double* dp = d_dinv ? c.take<double>(n) : nullptr;
+  const unsigned g = (unsigned)((n + 255) / 256);
+  if (int st = reset_work(w.st, w.red, w.blocks, s))
+    return st;
+  k_gather<double, double><<<g, 256, 0, s>>>(d_x, xp, op->perm, (int32_t)n);
+  k_gather<double, double><<<g, 256, 0, s>>>(d_b, bp, op->perm, (int32_t)n);
+  if (dp)
+    k_gather<double, double><<<g, 256, 0, s>>>(d_dinv, dp, op->perm, (int32_t)n);
+  if (int st = dfx::sell_spmv(*op, xp, w.y, s))
+    return st;
+  enqueue_init<double>(bp, w.y, xp, dp, n, w, rtol, max_iters, s);
+  DFX_CHECK_LAUNCH();
+  OpRef o{kSell, nullptr, op};
+  cudaGraphExec_t exec;
+  if (int st = iteration_graph<double>(o, xp, dp, n, w, K, false, &exec))
+    return st;
+  CgState* h;
+  int64_t kernels = 5 + (dp ? 1 : 0);
+  int st = run_to_done(exec, w.st, max_iters, K, &h, s, &kernels);
+  CgState hs = *h;
+  k_scatter<<<g, 256, 0, s>>>(xp, d_x, op->perm, (int32_t)n);
+  DFX_CHECK_LAUNCH();
+  if (st)
+    return st;
+  return report(&hs, info, kernels);
+}
+
+extern "C" size_t dfx_ir_workspace_bytes(int64_t n) { return ir_work_bytes(n); }
+
+__global__ void k_state_init(CgState* st, double rtol2, double delta2, int max_iter)
+{
+  *st = CgState{};
+  st->rtol2 = rtol2;
+  st->delta2 = delta2;
+  st->max_iter = max_iter;
+}
+
+extern "C" int dfx_ir_solve(dfx_operator op64, dfx_operator op32, const double* d_b, double* d_x,
+                            const double* d_dinv, double rtol, double inner_rtol,
+                            int32_t max_outer, int32_t max_inner, int32_t graph_iters,
+                            int32_t variant, void* d_work, size_t wbytes, dfx_ir_info* info,
+                            void* stream)
+{
+  DFX_REQUIRE(op64 && op32, "operators must be non-NULL");
+  DFX_REQUIRE(op64->dtype == DFX_F64 && op32->dtype == DFX_F32,
+              "refinement needs an FP64 outer and an FP32 inner operator");
+  DFX_REQUIRE(op64->n == op32->n && op64->sigma == op32->sigma && op64->nslices == op32->nslices
+                  && op64->csr_nnz == op32->csr_nnz,
+              "inner and outer operators must come from the same matrix and sigma");
+  if (int st = check_solve_args(d_b, d_x, d_work, rtol, max_outer))
+    return st;
+  DFX_REQUIRE(inner_rtol > 0.0 && inner_rtol < 1.0 && max_inner > 0,
+              "inner_rtol must be in (0, 1) and max_inner positive");
+  DFX_REQUIRE(variant == DFX_IR_RESTART || variant == DFX_IR_RELIABLE, "unknown variant %d",
+              variant);
+  const int64_t n = op64->n;
+  DFX_REQUIRE(wbytes >= ir_work_bytes(n), "workspace too small (%zu < %zu)", wbytes,
+              ir_work_bytes(n));
+  if (info)
+    *info = dfx_ir_info{};
+  if (n == 0)
+    return DFX_OK;
+  cudaStream_t s = dfx::as_stream(stream);
+  const int K = graph_iters > 0 ? graph_iters : 20;
+  Carver c{(char*)d_work};
+  Work<float> w = carve_work<float>(c, n);
+  CgState* outer = c.take<CgState>(1);
+  Red ored = carve_red(c, max_blocks(n));
+  double* xp = c.take<double>(n);
+  double* bp = c.take<double>(n);
+  c.take<double>(n);
+  float* d32 = c.take<float>(n);
+  float* dinv32 = d_dinv ? c.take<float>(n) : nullptr;
+  const unsigned g = (unsigned)((n + 255) / 256);
+  k_gather<double, double><<<g, 256, 0, s>>>(d_x, xp, op64->perm, (int32_t)n);
+  k_gather<double, double><<<g, 256, 0, s>>>(d_b, bp, op64->perm, (int32_t)n);
+  if (dinv32)
+    k_gather<double, float><<<g, 256, 0, s>>>(d_dinv, dinv32, op64->perm, (int32_t)n);
+  DFX_CHECK_LAUNCH();
+  const bool reliable = variant == DFX_IR_RELIABLE;
+  OpRef o{kSell, nullptr, op32};
+  cudaGraphExec_t exec;
+  if (int st = iteration_graph<float>(o, d32, dinv32, n, w, K, reliable, &exec))
+    return st;
+  const int blocks = stride_grid();
+  int inner_total = 0, outer_count = 0, st = DFX_OK;
+  int64_t kernels = 2 + (dinv32 ? 1 : 0);
+  CgState* h = nullptr;
+  CgState ho{};
+  if (!reliable)
   {
-    GraphKey key{A->row_ptr, A->cols, A->vals, d_b, n, A->nnz, A->bs, d_x, d_dinv, d_work, K,
-                 blocks, A->dtype};
-    std::lock_guard<std::mutex> lk(g_graph_mutex);
-    auto it = g_graphs.find(key);
-    if (it != g_graphs.end())
-      exec = it->second;
-    else
+    // Restarted refinement: each correction is a fresh FP32 PCG solve.
+    if (int e = reset_work(outer, ored, w.blocks, s))
+      return e;
+    if (int e = reset_work(w.st, w.red, w.blocks, s))
+      return e;
+    for (;;)
     {
-      cudaStream_t cs;
-      DFX_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
-      cudaGraph_t graph;
-      DFX_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
-      for (int k = 0; k < K; ++k)
-        enqueue_iteration(A, d_x, d_dinv, n, w, cs);
-      cudaError_t ce = cudaStreamEndCapture(cs, &graph);
-      cudaStreamDestroy(cs);
-      DFX_CUDA(ce);
-      ce = cudaGraphInstantiate(&exec, graph, 0);
-      cudaGraphDestroy(graph);
-      DFX_CUDA(ce);
-      if (g_graphs.size() >= 16)
+      k_ir_residual<<<sell_blocks(n), kSellThreads, 0, s>>>(*op64, bp, xp, w.r, outer, ored,
+                                                            rtol * rtol, max_outer);
+      DFX_CHECK_LAUNCH();
+      kernels += 1;
+      if ((st = read_state(outer, &h, s)))
+        break;
+      ho = *h;
+      if (ho.done)
+        break;
+      enqueue_init<float>(w.r, nullptr, d32, dinv32, n, w, inner_rtol, max_inner, s);
+      DFX_CHECK_LAUNCH();
+      if ((st = run_to_done(exec, w.st, max_inner, K, &h, s, &kernels)))
+        break;
+      inner_total += h->iter;
+      // A stalled or broken-down inner solve still yields a usable correction.
+      k_ir_correct<<<blocks, kThreads, 0, s>>>(xp, d32, n);
+      DFX_CHECK_LAUNCH();
+      kernels += 2;
+    }
+    outer_count = ho.iter - 1;
+  }
+  else
+  {
+    // One FP32 PCG whose residual is replaced by the FP64 residual each time
+    // it has dropped by inner_rtol (reliable updates); the FP32 correction
+    // is folded into x in FP64 at every replacement.
+    if (int e = reset_work(w.st, w.red, w.blocks, s))
+      return e;
+    k_state_init<<<1, 1, 0, s>>>(w.st, rtol * rtol, inner_rtol * inner_rtol, max_inner);
+    DFX_CUDA(cudaMemsetAsync(d32, 0, sizeof(float) * n, s));
+    DFX_CUDA(cudaMemsetAsync(w.p, 0, sizeof(float) * n, s));
+    auto replace = [&]() -> int
+    {
+      if (dinv32)
+        k_rel_residual<true><<<sell_blocks(n), kSellThreads, 0, s>>>(*op64, bp, xp, dinv32, w);
+      else
+        k_rel_residual<false><<<sell_blocks(n), kSellThreads, 0, s>>>(*op64, bp, xp, dinv32, w);
+      DFX_CHECK_LAUNCH();
+      kernels += 1;
+      return read_state(w.st, &h, s);
+    };
+    kernels += 1;
+    if (!(st = replace()) && !h->done)
+    {
+      for (;;)
       {
-        cudaGraphExecDestroy(g_graphs.begin()->second);
-        g_graphs.erase(g_graphs.begin());
+        enqueue_pupdate<float>(dinv32, n, w, s);
+        DFX_CHECK_LAUNCH();
+        kernels += 1;
+        if ((st = run_to_done(exec, w.st, max_inner, K, &h, s, &kernels)))
+          break;
+        const int32_t why = h->status;
+        k_ir_correct<<<blocks, kThreads, 0, s>>>(xp, d32, n);
+        DFX_CHECK_LAUNCH();
+        kernels += 1;
+        if (why != kPauseUpdate && why != kPauseConverged)
+          break; // not converged within max_inner, or breakdown
+        if ((st = replace()) || h->done)
+          break;
+        if (h->updates > max_outer)
+        {
+          st = dfx::fail(DFX_ERR_NOT_CONVERGED,
+                         "Refinement exceeded max residual replacements (%d).", max_outer);
+          break;
+        }
       }
-      g_graphs[key] = exec;
+    }
+    if (h)
+    {
+      ho = *h;
+      inner_total = ho.iter;
+      outer_count = ho.updates;
     }
   }
-  if (!t_pinned.h)
-    DFX_CUDA(cudaMallocHost(&t_pinned.h, sizeof(CgState)));
-  CgState* h = t_pinned.h;
-  // Every graph replay advances K iterations until the state is done, and
-  // the state is done at max_iters at the latest; the bound below only
-  // guards against a corrupted state.
-  const int64_t max_launches = (int64_t)max_iters / K + 2;
-  for (int64_t launch = 0;; ++launch)
-  {
-    DFX_CUDA(cudaMemcpyAsync(h, w.st, sizeof(CgState), cudaMemcpyDeviceToHost, s));
-    DFX_CUDA(cudaStreamSynchronize(s));
-    if (h->done)
-      break;
-    if (launch > max_launches)
-      return dfx::fail(DFX_ERR_TIMEOUT, "CG state never reported completion");
-    DFX_CUDA(cudaGraphLaunch(exec, s));
-  }
+  k_scatter<<<g, 256, 0, s>>>(xp, d_x, op64->perm, (int32_t)n);
+  DFX_CHECK_LAUNCH();
+  if (st)
+    return st;
+  DFX_CUDA(cudaStreamSynchronize(s));
   if (info)
   {
-    info->iterations = h->iter;
-    info->status = h->status;
-    info->rnorm0_sq = h->rr0;
-    info->rnorm_sq = h->rr;
+    info->outer_iterations = outer_count;
+    info->inner_iterations = inner_total;
+    info->status = ho.status;
+    info->rnorm0_sq = ho.rr0;
+    info->rnorm_sq = ho.rr;
+    info->kernel_launches = kernels + 1;
   }
-  if (h->status == DFX_ERR_NOT_CONVERGED)
+  if (ho.status == DFX_ERR_NOT_CONVERGED)
     return dfx::fail(DFX_ERR_NOT_CONVERGED,
-                     "Solver exceeded max iterations (%d). Relative residual=%g.", h->iter,
-                     h->rr0 > 0 ? h->rr / h->rr0 : 0.0);
-  if (h->status == DFX_ERR_BREAKDOWN)
-    return dfx::fail(DFX_ERR_BREAKDOWN, "CG breakdown at iteration %d (p.Ap=%g)", h->iter,
-                     h->pAp);
+                     "Refinement did not converge. Relative residual=%g.",
+                     ho.rr0 > 0 ? ho.rr / ho.rr0 : 0.0);
+  if (ho.status == DFX_ERR_BREAKDOWN)
+    return dfx::fail(DFX_ERR_BREAKDOWN, "refinement breakdown (non-finite residual or p.Ap <= 0)");
   return DFX_OK;
 }

@@ -1,0 +1,107 @@
+// Sliced-ELL (SELL-32-sigma) operator: the solver-side layout of a
+// la::MatrixCSR.
+//
+// GB300 executes FP64 at ~1/58 of its FP32 rate, so an FP64 SpMV is bound
+// by FP64 warp instructions as much as by HBM: a CSR kernel with several
+// lanes per row spends more FP64 instructions on shuffle reductions and
+// idle lanes than on products. SELL-32 gives every lane one row and no
+// reduction: each FP64 instruction does 32 useful FMAs.
+//   - rows are sorted by length (descending, stable) inside windows of
+//     sigma rows, which keeps the RCM locality and cuts padding to a few
+//     percent; the system is renumbered symmetrically with that
+//     permutation, so vectors stay coalesced;
+//   - slices of 32 consecutive (renumbered) rows are stored column-major:
+//     entry k of row 32*s + lane sits at slice_ptr[s] + 32*k + lane;
+//   - columns are int32, or (FP32 operator) a per-row first column plus
+//     16-bit deltas between the row's sorted columns (2 bytes per entry);
+//   - padding entries have value 0 and repeat a valid column.
+// Values are refilled from the CSR values after every assembly through a
+// precomputed slot map (SELL entry -> CSR entry, -1 for padding).
+#pragma once
+
+#include "common.cuh"
+
+struct dfx_operator_s
+{
+  int32_t n = 0;        // rows (scalar rows; block size 1)
+  int32_t nslices = 0;
+  int32_t sigma = 0;
+  int32_t dtype = DFX_F64;
+  int32_t compressed = 0;
+  int64_t nslots = 0;   // SELL entries incl. padding (multiple of 32)
+  int64_t csr_nnz = 0;
+  int32_t* perm = nullptr;      // new -> old row (n)
+  int32_t* iperm = nullptr;     // old -> new row (n)
+  int64_t* slice_ptr = nullptr; // (nslices + 1), in entries
+  int32_t* cols = nullptr;      // (nslots), uncompressed operators
+  uint16_t* delta = nullptr;    // (nslots), compressed operators
+  int32_t* first = nullptr;     // (32 * nslices), compressed operators
+  int32_t* map = nullptr;       // (nslots) CSR entry or -1
+  void* vals = nullptr;         // (nslots) f64 or f32
+  void* tmp = nullptr;          // 2 n scratch values for dfx_operator_apply
+  int device = 0;
+};
+
+namespace dfx
+{
+#ifdef __CUDACC__
+// Row sum of lane `lane` of slice `s` (row 32 s + lane, padded slices).
+template <typename V, typename X, typename ACC, bool COMP>
+__device__ __forceinline__ ACC sell_row(const dfx_operator_s& op, const V* __restrict__ vals,
+                                        const X* __restrict__ x, int32_t s, int lane)
+{
+  const int64_t b = __ldg(op.slice_ptr + s);
+  const int len = (int)((__ldg(op.slice_ptr + s + 1) - b) >> 5);
+  const V* v = vals + b + lane;
+  ACC acc = ACC(0);
+  if constexpr (COMP)
+  {
+    const uint16_t* d = op.delta + b + lane;
+    int32_t col = __ldg(op.first + 32 * (int64_t)s + lane);
+#pragma unroll 8
+    for (int k = 0; k < len; ++k)
+    {
+      if (k)
+        col += __ldcs(d + 32 * k);
+      acc = fma((ACC)__ldcs(v + 32 * k), (ACC)__ldg(x + col), acc);
+    }
+  }
+  else
+  {
+    const int32_t* c = op.cols + b + lane;
+#pragma unroll 4
+    for (int k = 0; k < len; ++k)
+      acc = fma((ACC)__ldcs(v + 32 * k), (ACC)__ldg(x + __ldcs(c + 32 * k)), acc);
+  }
+  return acc;
+}
+#endif
+
+#ifdef __CUDACC__
+// Slices of this block: a contiguous run, so that the rows one SM works on
+// are neighbours and their x gathers hit the same L1 lines. Warps of the
+// block interleave inside the run.
+struct SliceRange
+{
+  int32_t begin, end, step;
+};
+__device__ __forceinline__ SliceRange block_slices(int32_t nslices)
+{
+  const int32_t per = (nslices + (int32_t)gridDim.x - 1) / (int32_t)gridDim.x;
+  const int32_t b = (int32_t)blockIdx.x * per;
+  SliceRange r;
+  r.begin = b + (int32_t)(threadIdx.x >> 5);
+  r.end = min(nslices, b + per);
+  r.step = (int32_t)(blockDim.x >> 5);
+  return r;
+}
+#endif
+
+// Grid of the sliced-ELL kernels (blocks of 256 threads), and the largest
+// grid any kernel with per-block partial sums uses.
+int sell_grid(int32_t nslices);
+int max_grid_blocks();
+
+// Launch y = A x on renumbered vectors (both of length op.n).
+int sell_spmv(const dfx_operator_s& op, const void* x, void* y, cudaStream_t s);
+} // namespace dfx

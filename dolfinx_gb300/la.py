@@ -135,6 +135,7 @@ class CGResult:
     status: int
     rnorm0_sq: float
     rnorm_sq: float
+    kernel_launches: int = 0
 
 
 class CGSolver:
@@ -163,7 +164,149 @@ class CGSolver:
                                       _ptr(self.work), self.work.numel(), C.byref(info), _stream())
         if raise_on_fail:
             _capi.check(rc)
-        return CGResult(info.iterations, info.status, info.rnorm0_sq, info.rnorm_sq)
+        return CGResult(info.iterations, info.status, info.rnorm0_sq, info.rnorm_sq,
+                        info.kernel_launches)
+
+
+class SellOperator:
+    """Sliced-ELL (SELL-32-sigma) solver copy of a scalar MatrixCSR: FP64, or
+    FP32 with 16-bit column deltas. Values are refreshed from the CSR values
+    with update_values() after re-assembly."""
+
+    def __init__(self, A: MatrixCSR, dtype=torch.float64, sigma: int = 256,
+                 compress_cols: bool | None = None):
+        if compress_cols is None:
+            compress_cols = dtype == torch.float32
+        self.A, self.dtype, self.sigma = A, dtype, sigma
+        h = C.c_void_p()
+        dt = _capi.F64 if dtype == torch.float64 else _capi.F32
+        _capi.check(_capi.lib().dfx_operator_create(C.byref(A.csr()), sigma, dt,
+                                                    int(bool(compress_cols)), C.byref(h),
+                                                    _stream()))
+        self.handle = h
+        self.compressed = bool(compress_cols)
+
+    def update_values(self):
+        _capi.check(_capi.lib().dfx_operator_update_values(self.handle, C.byref(self.A.csr()),
+                                                           _stream()))
+
+    def apply(self, x: torch.Tensor, y: torch.Tensor | None = None) -> torch.Tensor:
+        if y is None:
+            y = torch.empty_like(x)
+        _capi.check(_capi.lib().dfx_operator_apply(self.handle, _ptr(x), _ptr(y), _stream()))
+        return y
+
+    def apply_renumbered(self, xp: torch.Tensor, yp: torch.Tensor) -> torch.Tensor:
+        """The bare SpMV in the operator's numbering."""
+        _capi.check(_capi.lib().dfx_operator_apply_renumbered(self.handle, _ptr(xp), _ptr(yp),
+                                                              _stream()))
+        return yp
+
+    def info(self):
+        ns = C.c_int64()
+        nsl = C.c_int32()
+        perm = C.c_void_p()
+        _capi.check(_capi.lib().dfx_operator_info(self.handle, C.byref(ns), C.byref(nsl),
+                                                   C.byref(perm)))
+        return {"slots": ns.value, "slices": nsl.value, "padding": ns.value / self.A.nnz - 1}
+
+    def __del__(self):
+        h = getattr(self, "handle", None)
+        if h is not None and h.value and _capi is not None:
+            try:
+                _capi.lib().dfx_operator_destroy(h)
+            except Exception:
+                pass
+            self.handle = None
+
+
+class OperatorCGSolver:
+    """FP64 Jacobi-PCG on the sliced-ELL operator (same iteration and
+    stopping test as CGSolver)."""
+
+    def __init__(self, A: MatrixCSR, jacobi: bool = True, graph_iters: int = 20,
+                 sigma: int = 256):
+        self.A = A
+        self.op = SellOperator(A, torch.float64, sigma)
+        self.n = A.nrows
+        self.dinv = A.inverse_diagonal() if jacobi else None
+        wb = int(_capi.lib().dfx_cg_op_workspace_bytes(self.n))
+        self.work = torch.empty(wb, dtype=torch.uint8, device=A.vals.device)
+        self.graph_iters = graph_iters
+
+    def refresh(self):
+        """Re-read the CSR values (after re-assembly)."""
+        self.op.update_values()
+        if self.dinv is not None:
+            _capi.check(_capi.lib().dfx_jacobi_inverse_diagonal(C.byref(self.A.csr()),
+                                                                _ptr(self.dinv), _stream()))
+
+    def solve(self, b, x, rtol=1e-10, max_iters=100000, raise_on_fail=True) -> CGResult:
+        info = _capi.CgInfo()
+        rc = _capi.lib().dfx_cg_solve_op(self.op.handle, _ptr(b), _ptr(x), _ptr(self.dinv),
+                                         float(rtol), int(max_iters), int(self.graph_iters),
+                                         _ptr(self.work), self.work.numel(), C.byref(info),
+                                         _stream())
+        if raise_on_fail:
+            _capi.check(rc)
+        return CGResult(info.iterations, info.status, info.rnorm0_sq, info.rnorm_sq,
+                        info.kernel_launches)
+
+
+@dataclass
+class IRResult:
+    outer_iterations: int
+    inner_iterations: int
+    status: int
+    rnorm0_sq: float
+    rnorm_sq: float
+    kernel_launches: int = 0
+
+    @property
+    def iterations(self):
+        return self.inner_iterations
+
+
+class IRSolver:
+    """Mixed-precision iterative refinement: FP64 residual, norm and update
+    with the FP64 operator; FP32 Jacobi-PCG corrections on the FP32
+    16-bit-column operator."""
+
+    def __init__(self, A: MatrixCSR, jacobi: bool = True, graph_iters: int = 20,
+                 sigma: int = 256, inner_rtol: float | None = None, compress_cols: bool = True,
+                 variant: str = "reliable"):
+        self.variant = {"restart": _capi.IR_RESTART, "reliable": _capi.IR_RELIABLE}[variant]
+        if inner_rtol is None:
+            inner_rtol = 0.1 if self.variant == _capi.IR_RELIABLE else 1e-4
+        self.A = A
+        self.op64 = SellOperator(A, torch.float64, sigma)
+        self.op32 = SellOperator(A, torch.float32, sigma, compress_cols=compress_cols)
+        self.n = A.nrows
+        self.dinv = A.inverse_diagonal() if jacobi else None
+        wb = int(_capi.lib().dfx_ir_workspace_bytes(self.n))
+        self.work = torch.empty(wb, dtype=torch.uint8, device=A.vals.device)
+        self.graph_iters = graph_iters
+        self.inner_rtol = inner_rtol
+
+    def refresh(self):
+        self.op64.update_values()
+        self.op32.update_values()
+        if self.dinv is not None:
+            _capi.check(_capi.lib().dfx_jacobi_inverse_diagonal(C.byref(self.A.csr()),
+                                                                _ptr(self.dinv), _stream()))
+
+    def solve(self, b, x, rtol=1e-10, max_outer=200, max_inner=100000,
+              raise_on_fail=True) -> IRResult:
+        info = _capi.IrInfo()
+        rc = _capi.lib().dfx_ir_solve(self.op64.handle, self.op32.handle, _ptr(b), _ptr(x),
+                                      _ptr(self.dinv), float(rtol), float(self.inner_rtol),
+                                      int(max_outer), int(max_inner), int(self.graph_iters),
+                                      int(self.variant), _ptr(self.work), self.work.numel(),
+                                      C.byref(info), _stream())
+        if raise_on_fail:
+            _capi.check(rc)
+        return IRResult(info.outer_iterations, info.inner_iterations, info.status,
+                        info.rnorm0_sq, info.rnorm_sq, info.kernel_launches)
 
 
 def cg(A: MatrixCSR, b: torch.Tensor, x: torch.Tensor | None = None, rtol: float = 1e-10,

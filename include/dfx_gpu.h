@@ -212,9 +212,10 @@ int dfx_inner_product(const double* d_a, const double* d_b, int64_t n,
 typedef struct dfx_cg_info
 {
   int32_t iterations;
-  int32_t status;       /* DFX_OK, DFX_ERR_NOT_CONVERGED, DFX_ERR_BREAKDOWN */
-  double rnorm0_sq;     /* |r0|^2 */
-  double rnorm_sq;      /* |r_k|^2 */
+  int32_t status;          /* DFX_OK, DFX_ERR_NOT_CONVERGED, DFX_ERR_BREAKDOWN */
+  double rnorm0_sq;        /* |r0|^2 */
+  double rnorm_sq;         /* |r_k|^2 */
+  int64_t kernel_launches; /* kernels this solve launched (graph nodes included) */
 } dfx_cg_info;
 
 /* Workspace of dfx_cg_solve for n scalar unknowns. */
@@ -229,6 +230,73 @@ int dfx_cg_solve(const dfx_csr* A, const double* d_b, double* d_x,
                  const double* d_dinv, double rtol, int32_t max_iters,
                  int32_t graph_iters, void* d_work, size_t work_bytes,
                  dfx_cg_info* info, void* stream);
+
+/* ------------------------------------------------- sliced-ELL operator
+ * The solver-side copy of a scalar MatrixCSR: rows sorted by length
+ * within windows of `sigma` rows (a multiple of 32), the system renumbered
+ * symmetrically with that permutation, 32-row slices stored column-major
+ * so that every lane of a warp owns one row. No reference counterpart: it
+ * is the GB300 layout behind MatrixCSR::mult inside the solvers
+ * (la/MatrixCSR.h:877-946). FP32 operators may store columns as a first
+ * column per row plus 16-bit deltas (DFX_ERR_UNSUPPORTED if a row has a
+ * gap above 65535). The library owns the operator's device memory. */
+typedef struct dfx_operator_s* dfx_operator;
+
+int dfx_operator_create(const dfx_csr* A, int32_t sigma, int32_t value_dtype,
+                        int32_t compress_cols, dfx_operator* op, void* stream);
+/* Refill the operator's values from A's FP64 values (after re-assembly). */
+int dfx_operator_update_values(dfx_operator op, const dfx_csr* A, void* stream);
+/* y = A x in the original numbering (x, y of the operator's dtype). */
+int dfx_operator_apply(dfx_operator op, const void* d_x, void* d_y, void* stream);
+/* y' = A' x' in the operator's own (renumbered) numbering: the bare SpMV
+ * kernel the solvers run. */
+int dfx_operator_apply_renumbered(dfx_operator op, const void* d_x, void* d_y, void* stream);
+int dfx_operator_info(dfx_operator op, int64_t* nslots, int32_t* nslices,
+                      const int32_t** d_perm);
+int dfx_operator_destroy(dfx_operator op);
+
+/* dfx_cg_solve on an FP64 operator (same iteration and stopping test). */
+size_t dfx_cg_op_workspace_bytes(int64_t n);
+int dfx_cg_solve_op(dfx_operator op, const double* d_b, double* d_x,
+                    const double* d_dinv, double rtol, int32_t max_iters,
+                    int32_t graph_iters, void* d_work, size_t work_bytes,
+                    dfx_cg_info* info, void* stream);
+
+/* Mixed-precision iterative refinement (no reference counterpart; it
+ * wraps the demo's CG): r = b - A x, |r| and x += d in FP64 with op64;
+ * corrections d come from Jacobi-PCG in FP32 (op32, FP32 vectors).
+ *   DFX_IR_RESTART:  each correction is a fresh FP32 PCG solve of A d = r
+ *                    to inner_rtol; max_outer caps the corrections.
+ *   DFX_IR_RELIABLE: one FP32 PCG whose residual is replaced by the FP64
+ *                    residual b - A x whenever it has dropped by inner_rtol
+ *                    (reliable updates); x += d in FP64 at each replacement,
+ *                    the search direction is kept; max_outer caps the
+ *                    replacements, max_inner the FP32 iterations.
+ * Stops when |b - A x|^2 / |b - A x0|^2 < rtol^2 evaluated in FP64 -- the
+ * stopping test of dfx_cg_solve. op64 and op32 must be built from the same
+ * matrix with the same sigma. */
+enum dfx_ir_variant
+{
+  DFX_IR_RESTART = 0,
+  DFX_IR_RELIABLE = 1
+};
+typedef struct dfx_ir_info
+{
+  int32_t outer_iterations;
+  int32_t inner_iterations;   /* total FP32 PCG iterations */
+  int32_t status;
+  int32_t reserved;
+  double rnorm0_sq;
+  double rnorm_sq;
+  int64_t kernel_launches;    /* kernels this solve launched (graph nodes included) */
+} dfx_ir_info;
+
+size_t dfx_ir_workspace_bytes(int64_t n);
+int dfx_ir_solve(dfx_operator op64, dfx_operator op32, const double* d_b, double* d_x,
+                 const double* d_dinv, double rtol, double inner_rtol,
+                 int32_t max_outer, int32_t max_inner, int32_t graph_iters,
+                 int32_t variant, void* d_work, size_t work_bytes, dfx_ir_info* info,
+                 void* stream);
 
 #ifdef __cplusplus
 }

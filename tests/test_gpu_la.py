@@ -127,3 +127,90 @@ def test_cg_not_converged_reports(cuda, oracle, capi):
     b = fem.assemble_vector(fem.source_form(V, f))
     with pytest.raises(capi.DfxError, match="exceeded max iterations"):
         la.cg(A, b, rtol=1e-14, max_iters=3)
+
+
+@pytest.mark.parametrize("sigma", [32, 256])
+def test_sell_operator_f64(cuda, oracle, capi, sigma):
+    from dolfinx_gb300 import fem, la
+
+    m, V, kappa, f, rp, cols = problem(oracle, (6, 5, 7), 2, seed=21)
+    A = fem.assemble_matrix(fem.poisson_form(V, kappa))
+    op = la.SellOperator(A, torch.float64, sigma)
+    inf = op.info()
+    assert inf["slots"] % 32 == 0 and inf["padding"] >= 0
+    x = np.random.default_rng(1).standard_normal(V.num_dofs)
+    y = op.apply(torch.from_numpy(x).cuda()).cpu().numpy()
+    ref = oracle.spmv(rp, cols, A.vals.cpu().numpy(), x)
+    assert_close(y, ref, rtol=1e-13)
+    # values refresh after re-assembly
+    A.vals.mul_(2.0)
+    op.update_values()
+    y = op.apply(torch.from_numpy(x).cuda()).cpu().numpy()
+    assert_close(y, 2 * ref, rtol=1e-13)
+
+
+@pytest.mark.parametrize("compress", [False, True])
+def test_sell_operator_f32(cuda, oracle, capi, compress):
+    from dolfinx_gb300 import fem, la
+
+    m, V, kappa, f, rp, cols = problem(oracle, (6, 5, 7), 2, seed=22)
+    A = fem.assemble_matrix(fem.poisson_form(V, kappa))
+    op = la.SellOperator(A, torch.float32, 256, compress_cols=compress)
+    x = np.random.default_rng(2).standard_normal(V.num_dofs).astype(np.float32)
+    y = op.apply(torch.from_numpy(x).cuda()).cpu().numpy()
+    v32 = A.vals.cpu().numpy().astype(np.float32).astype(np.float64)
+    ref = oracle.spmv(rp, cols, v32, x.astype(np.float64))
+    assert_close(y, ref, rtol=2e-6)
+
+
+def _c1_system(oracle, n, deg, seed):
+    from dolfinx_gb300 import fem
+
+    m, V, kappa, f, rp, cols = problem(oracle, n, deg, seed=seed)
+    X = V.tabulate_dof_coordinates()
+    bnd = np.flatnonzero(np.isclose(X[:, 0], 0) | np.isclose(X[:, 0], 1)).astype(np.int32)
+    bc = fem.dirichletbc(0.0, bnd, V)
+    a = fem.poisson_form(V, kappa)
+    A = fem.assemble_matrix(a, bcs=[bc])
+    b = fem.RhsAssembler(fem.source_form(V, f), a, [bc]).assemble()
+    return A, b, rp, cols
+
+
+def test_operator_cg_matches_csr_cg(cuda, oracle, capi):
+    from dolfinx_gb300 import la
+
+    A, b, rp, cols = _c1_system(oracle, (10, 9, 8), 2, 31)
+    x1, r1 = la.cg(A, b, rtol=1e-10)
+    s = la.OperatorCGSolver(A)
+    x2 = torch.zeros_like(b)
+    r2 = s.solve(b, x2, rtol=1e-10)
+    assert r2.status == 0 and abs(r2.iterations - r1.iterations) <= 3
+    bh = b.cpu().numpy()
+    res = bh - oracle.spmv(rp, cols, A.vals.cpu().numpy(), x2.cpu().numpy())
+    assert np.linalg.norm(res) / np.linalg.norm(bh) < 1e-10 * 1.0001
+    rel = (x1 - x2).norm() / x1.norm()
+    assert rel < 1e-7
+
+
+@pytest.mark.parametrize("variant,inner_rtol", [("restart", 1e-3), ("restart", 1e-5),
+                                                 ("reliable", 0.1), ("reliable", 0.01)])
+def test_iterative_refinement_reaches_fp64(cuda, oracle, capi, variant, inner_rtol):
+    """FP32-inner refinement meets the FP64 stopping test (|r|/|r0| < 1e-10
+    in FP64) and agrees with the plain FP64 CG solution to the accuracy
+    both solves carry."""
+    from dolfinx_gb300 import la
+
+    A, b, rp, cols = _c1_system(oracle, (12, 12, 12), 2, 32)
+    s64 = la.OperatorCGSolver(A)
+    x64 = torch.zeros_like(b)
+    s64.solve(b, x64, rtol=1e-12)
+    ir = la.IRSolver(A, inner_rtol=inner_rtol, variant=variant)
+    x = torch.zeros_like(b)
+    r = ir.solve(b, x, rtol=1e-12)
+    assert r.status == 0 and r.outer_iterations >= 2
+    bh = b.cpu().numpy()
+    xs = x.cpu().numpy()
+    res = bh - oracle.spmv(rp, cols, A.vals.cpu().numpy(), xs)
+    assert np.linalg.norm(res) / np.linalg.norm(bh) < 1e-12 * 1.0001
+    rel = (x - x64).norm().item() / x64.norm().item()
+    assert rel < 1e-10, rel
