@@ -72,15 +72,13 @@ int elem_grid(int64_t n)
   return (int)std::max<int64_t>(1, (n + per - 1) / per);
 }
 
-// Largest grid of any CG kernel for n unknowns (sizes the partial sums).
-int max_blocks(int64_t n)
-{
-  return std::max({sell_blocks(n), elem_grid(n), stride_grid()});
-}
+// Largest grid of any CG kernel for n unknowns (each block publishes one
+// partial sum).
+int max_blocks(int64_t n) { return std::max({sell_blocks(n), elem_grid(n), stride_grid()}); }
 
-// Blocks per reduction group of the two-level reduction.
+// Warps per reduction group of the two-level reduction.
 constexpr int kGroup = 64;
-int groups_of(int blocks) { return (blocks + kGroup - 1) / kGroup; }
+int groups_of(int units) { return (units + kGroup - 1) / kGroup; }
 
 // Carves typed arrays out of a workspace (p == nullptr: only counts).
 struct Carver
@@ -150,72 +148,122 @@ int reset_work(CgState* st, const Red& red, int blocks, cudaStream_t s)
   return DFX_OK;
 }
 
-// Publish this block's partial sums. The last block of each group of
-// kGroup blocks sums its group in index order; the last group to finish
-// returns true (in every thread of its block), with the group sums ready in
-// red.gpart0/1. Both levels use fixed summation orders, so the result does
-// not depend on block scheduling.
-__device__ __forceinline__ bool publish(double v0, double v1, const Red& red,
-                                        unsigned int* ticket, bool two)
+// Deterministic reduction without block barriers. Each warp reduces its
+// lanes and drops the result in shared memory; the last warp of the block
+// to arrive (shared-memory ticket) sums the block's warps in index order and
+// publishes one partial per block, in slot blockIdx.x. The last block of
+// each group of kGroup blocks sums the group in index order; the last group
+// to finish sums the group totals in index order and returns true in all
+// lanes of that one warp. Kernels call block_reduce_init() once at entry.
+struct WarpFinal
 {
-  __shared__ double sh[32];
-  __shared__ int in_group_last, last;
-  v0 = dfx::block_sum(v0, sh);
-  if (two)
-    v1 = dfx::block_sum(v1, sh);
-  const unsigned g = blockIdx.x / kGroup;
-  const unsigned ng = (gridDim.x + kGroup - 1) / kGroup;
-  const unsigned gsize = min((unsigned)kGroup, gridDim.x - g * kGroup);
+  bool last;
+  double s0, s1; // valid in the last warp (all lanes)
+};
+
+struct BlockScratch
+{
+  double p0[32];
+  double p1[32];
+  unsigned int count;
+};
+
+__device__ __forceinline__ BlockScratch& block_scratch()
+{
+  __shared__ BlockScratch b;
+  return b;
+}
+
+__device__ __forceinline__ void block_reduce_init()
+{
   if (threadIdx.x == 0)
-  {
-    red.part0[blockIdx.x] = v0;
-    if (two)
-      red.part1[blockIdx.x] = v1;
-    __threadfence();
-    in_group_last = atomicAdd(&red.gticket[g], 1u) == gsize - 1;
-  }
+    block_scratch().count = 0;
   __syncthreads();
-  if (!in_group_last)
-    return false;
-  if (threadIdx.x < 32)
-  {
-    double s0 = 0.0, s1 = 0.0;
-    for (unsigned i = threadIdx.x; i < gsize; i += 32)
-    {
-      s0 += __ldcg(red.part0 + g * kGroup + i);
-      if (two)
-        s1 += __ldcg(red.part1 + g * kGroup + i);
-    }
-    s0 = dfx::warp_sum(s0);
-    if (two)
-      s1 = dfx::warp_sum(s1);
-    if (threadIdx.x == 0)
-    {
-      red.gpart0[g] = s0;
-      if (two)
-        red.gpart1[g] = s1;
-      red.gticket[g] = 0;
-      __threadfence();
-      last = atomicAdd(ticket, 1u) == ng - 1;
-    }
-  }
-  __syncthreads();
-  return last;
 }
 
-// Deterministic sum of the group sums; all threads of the final block call
-// it, thread 0 gets the result.
-__device__ __forceinline__ double final_sum(const double* gpart)
+__device__ __forceinline__ WarpFinal publish(double v0, double v1, const Red& red,
+                                             unsigned int* ticket, bool two)
 {
-  __shared__ double sh[32];
-  const int ng = (gridDim.x + kGroup - 1) / kGroup;
-  double s = 0.0;
-  for (int i = threadIdx.x; i < ng; i += blockDim.x)
-    s += __ldcg(gpart + i);
-  return dfx::block_sum(s, sh);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned nw = blockDim.x >> 5;
+  BlockScratch& bs = block_scratch();
+  WarpFinal out{false, 0.0, 0.0};
+  v0 = dfx::warp_sum(v0);
+  if (two)
+    v1 = dfx::warp_sum(v1);
+  int flag = 0;
+  if (lane == 0)
+  {
+    bs.p0[warp] = v0;
+    if (two)
+      bs.p1[warp] = v1;
+    __threadfence_block();
+    flag = atomicAdd(&bs.count, 1u) == nw - 1;
+  }
+  if (!__shfl_sync(0xffffffffu, flag, 0))
+    return out;
+  // Last warp of the block: block partial in warp-index order.
+  __threadfence_block();
+  double b0 = lane < (int)nw ? ((volatile double*)bs.p0)[lane] : 0.0;
+  double b1 = (two && lane < (int)nw) ? ((volatile double*)bs.p1)[lane] : 0.0;
+  b0 = dfx::warp_sum(b0);
+  if (two)
+    b1 = dfx::warp_sum(b1);
+  const unsigned unit = blockIdx.x, nunits = gridDim.x;
+  const unsigned g = unit / kGroup;
+  const unsigned ng = (nunits + kGroup - 1) / kGroup;
+  const unsigned gsize = min((unsigned)kGroup, nunits - g * kGroup);
+  if (lane == 0)
+  {
+    red.part0[unit] = b0;
+    if (two)
+      red.part1[unit] = b1;
+    __threadfence();
+    flag = atomicAdd(&red.gticket[g], 1u) == gsize - 1;
+  }
+  if (!__shfl_sync(0xffffffffu, flag, 0))
+    return out;
+  double s0 = 0.0, s1 = 0.0;
+  for (unsigned i = lane; i < gsize; i += 32)
+  {
+    s0 += __ldcg(red.part0 + g * kGroup + i);
+    if (two)
+      s1 += __ldcg(red.part1 + g * kGroup + i);
+  }
+  s0 = dfx::warp_sum(s0);
+  if (two)
+    s1 = dfx::warp_sum(s1);
+  if (lane == 0)
+  {
+    red.gpart0[g] = s0;
+    if (two)
+      red.gpart1[g] = s1;
+    red.gticket[g] = 0;
+    __threadfence();
+    flag = atomicAdd(ticket, 1u) == ng - 1;
+  }
+  if (!__shfl_sync(0xffffffffu, flag, 0))
+    return out;
+  s0 = 0.0;
+  s1 = 0.0;
+  for (unsigned i = lane; i < ng; i += 32)
+  {
+    s0 += __ldcg(red.gpart0 + i);
+    if (two)
+      s1 += __ldcg(red.gpart1 + i);
+  }
+  out.last = true;
+  out.s0 = dfx::warp_sum(s0);
+  out.s1 = two ? dfx::warp_sum(s1) : 0.0;
+  return out;
 }
 
-__device__ __forceinline__ bool is_done(const CgState* st) { return __ldcg(&st->done) != 0; }
+
+// Scalars of the state are produced by earlier kernels of the stream and
+// only read by this one (the one warp that updates them does so after its
+// last read), so they go through the read-only path: one L2 fetch per SM
+// instead of one request per warp to a single L2 line.
+__device__ __forceinline__ bool is_done(const CgState* st) { return __ldg(&st->done) != 0; }
 
 // r = rhs - Ax (Ax == nullptr: x0 = 0 and x is zeroed), z = D^{-1} r,
 // p = z; state initialised. rhs may alias w.r.
@@ -224,6 +272,8 @@ __global__ void __launch_bounds__(kThreads)
     k_init(const T* rhs, const T* __restrict__ Ax, T* __restrict__ x, const T* __restrict__ dinv,
            int64_t n, Work<T> w, double rtol2, int max_iter)
 {
+  block_reduce_init();
+
   T rr = 0, rz = 0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x)
@@ -237,11 +287,11 @@ __global__ void __launch_bounds__(kThreads)
     rr += r * r;
     rz += r * z;
   }
-  if (publish((double)rr, (double)rz, w.red, &w.st->ticket[0], true))
+  const WarpFinal f = publish((double)rr, (double)rz, w.red, &w.st->ticket[0], true);
+  if (f.last)
   {
-    const double srr = final_sum(w.red.gpart0);
-    const double srz = final_sum(w.red.gpart1);
-    if (threadIdx.x == 0)
+    const double srr = f.s0, srz = f.s1;
+    if ((threadIdx.x & 31) == 0)
     {
       CgState* st = w.st;
       st->rr0 = srr;
@@ -258,11 +308,13 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
-// Last block of an SpMV-dot kernel: alpha = rz / p.Ap.
-__device__ __forceinline__ void finish_pap(const double* part, CgState* st)
+// Last warp of an SpMV-dot kernel: alpha = rz / p.Ap.
+__device__ __forceinline__ void finish_pap(const WarpFinal& f, CgState* st)
 {
-  const double pAp = final_sum(part);
-  if (threadIdx.x == 0)
+  if (!f.last)
+    return;
+  const double pAp = f.s0;
+  if ((threadIdx.x & 31) == 0)
   {
     st->pAp = pAp;
     if (!(pAp > 0.0) || !isfinite(pAp))
@@ -283,6 +335,8 @@ __global__ void __launch_bounds__(kThreads)
     k_spmv_dot_csr(int32_t nrows, const int64_t* __restrict__ rp, const int32_t* __restrict__ cols,
                    const double* __restrict__ vals, Work<double> w)
 {
+  block_reduce_init();
+
   if (is_done(w.st))
     return;
   constexpr int G = BS == 1 ? L : 8; // lanes per row
@@ -326,8 +380,7 @@ __global__ void __launch_bounds__(kThreads)
       }
     }
   }
-  if (publish(dot, 0.0, w.red, &w.st->ticket[1], false))
-    finish_pap(w.red.gpart0, w.st);
+  finish_pap(publish(dot, 0.0, w.red, &w.st->ticket[1], false), w.st);
 }
 
 // y = A p, p.y -- sliced-ELL operator, one row per lane, warp per slice.
@@ -335,6 +388,8 @@ template <typename V, typename T, bool COMP>
 __global__ void __launch_bounds__(kSellThreads)
     k_spmv_dot_sell(const dfx_operator_s op, Work<T> w)
 {
+  block_reduce_init();
+
   if (is_done(w.st))
     return;
   const int lane = threadIdx.x & 31;
@@ -350,17 +405,18 @@ __global__ void __launch_bounds__(kSellThreads)
       dot += acc * w.p[row];
     }
   }
-  if (publish((double)dot, 0.0, w.red, &w.st->ticket[1], false))
-    finish_pap(w.red.gpart0, w.st);
+  finish_pap(publish((double)dot, 0.0, w.red, &w.st->ticket[1], false), w.st);
 }
 
 template <typename T, bool PRE, bool RELIABLE>
 __global__ void __launch_bounds__(kElemThreads)
     k_update(T* __restrict__ x, const T* __restrict__ dinv, int64_t n, Work<T> w)
 {
+  block_reduce_init();
+
   if (is_done(w.st))
     return;
-  const T alpha = (T)__ldcg(&w.st->alpha);
+  const T alpha = (T)__ldg(&w.st->alpha);
   T rr = 0, rz = 0;
   constexpr int E = kElemPerThread;
   const int64_t stride = (int64_t)gridDim.x * kElemThreads * E;
@@ -392,11 +448,11 @@ __global__ void __launch_bounds__(kElemThreads)
       rz += rn * (PRE ? d[e] * rn : rn);
     }
   }
-  if (publish((double)rr, (double)rz, w.red, &w.st->ticket[2], true))
+  const WarpFinal f = publish((double)rr, (double)rz, w.red, &w.st->ticket[2], true);
+  if (f.last)
   {
-    const double srr = final_sum(w.red.gpart0);
-    const double srz = final_sum(w.red.gpart1);
-    if (threadIdx.x == 0)
+    const double srr = f.s0, srz = f.s1;
+    if ((threadIdx.x & 31) == 0)
     {
       CgState* st = w.st;
       st->rr = srr;
@@ -448,7 +504,7 @@ __global__ void __launch_bounds__(kElemThreads)
 {
   if (is_done(w.st))
     return;
-  const T beta = (T)__ldcg(&w.st->beta);
+  const T beta = (T)__ldg(&w.st->beta);
   constexpr int E = kElemPerThread;
   const int64_t stride = (int64_t)gridDim.x * kElemThreads * E;
   for (int64_t base = (int64_t)blockIdx.x * kElemThreads * E + threadIdx.x; base < n;
@@ -482,6 +538,8 @@ __global__ void __launch_bounds__(kSellThreads)
                   const double* __restrict__ x, float* __restrict__ r32, CgState* st,
                   Red red, double rtol2, int max_outer)
 {
+  block_reduce_init();
+
   const int lane = threadIdx.x & 31;
   const dfx::SliceRange sr = dfx::block_slices(op.nslices);
   double rr = 0.0;
@@ -497,10 +555,11 @@ __global__ void __launch_bounds__(kSellThreads)
       rr += r * r;
     }
   }
-  if (publish(rr, 0.0, red, &st->ticket[3], false))
+  const WarpFinal f = publish(rr, 0.0, red, &st->ticket[3], false);
+  if (f.last)
   {
-    const double srr = final_sum(red.gpart0);
-    if (threadIdx.x == 0)
+    const double srr = f.s0;
+    if ((threadIdx.x & 31) == 0)
     {
       if (st->iter == 0)
       {
@@ -548,6 +607,8 @@ __global__ void __launch_bounds__(kSellThreads)
     k_rel_residual(const dfx_operator_s op, const double* __restrict__ b,
                    const double* __restrict__ x, const float* __restrict__ dinv32, Work<float> w)
 {
+  block_reduce_init();
+
   const int lane = threadIdx.x & 31;
   const dfx::SliceRange sr = dfx::block_slices(op.nslices);
   double rr = 0.0, rz = 0.0;
@@ -566,11 +627,11 @@ __global__ void __launch_bounds__(kSellThreads)
       rz += (double)r32 * z;
     }
   }
-  if (publish(rr, rz, w.red, &w.st->ticket[3], true))
+  const WarpFinal f = publish(rr, rz, w.red, &w.st->ticket[3], true);
+  if (f.last)
   {
-    const double srr = final_sum(w.red.gpart0);
-    const double srz = final_sum(w.red.gpart1);
-    if (threadIdx.x == 0)
+    const double srr = f.s0, srz = f.s1;
+    if ((threadIdx.x & 31) == 0)
     {
       CgState* st = w.st;
       const bool first = st->iter == 0 && st->updates == 0;
@@ -1132,3 +1193,4 @@ extern "C" int dfx_ir_solve(dfx_operator op64, dfx_operator op32, const double* 
     return dfx::fail(DFX_ERR_BREAKDOWN, "refinement breakdown (non-finite residual or p.Ap <= 0)");
   return DFX_OK;
 }
+

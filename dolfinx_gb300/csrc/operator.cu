@@ -163,6 +163,9 @@ extern "C" int dfx_operator_create(const dfx_csr* A, int32_t sigma, int32_t dtyp
   for (int32_t i = 0; i < n; ++i)
     iperm[perm[i]] = i;
   const int32_t ns = (n + 31) / 32;
+  // FP32 operators store entries in k-pairs per lane (8-byte loads), so
+  // their slices have an even length.
+  const bool pairs = dtype == DFX_F32;
   std::vector<int64_t> sp(ns + 1, 0);
   for (int32_t sl = 0; sl < ns; ++sl)
   {
@@ -173,8 +176,12 @@ extern "C" int dfx_operator_create(const dfx_csr* A, int32_t sigma, int32_t dtyp
       if (i < n)
         len = std::max(len, rp[perm[i] + 1] - rp[perm[i]]);
     }
+    if (pairs)
+      len += len & 1;
     sp[sl + 1] = sp[sl] + 32 * len;
   }
+  auto slot_of = [&](int64_t sl, int64_t k, int l) -> int64_t
+  { return pairs ? sp[sl] + 64 * (k >> 1) + 2 * l + (k & 1) : sp[sl] + 32 * k + l; };
   const int64_t nslots = sp[ns];
   DFX_REQUIRE(nslots < INT32_MAX, "operator too large");
   std::vector<int32_t> scols(compress_cols ? 0 : nslots), smap(nslots);
@@ -204,7 +211,7 @@ extern "C" int dfx_operator_create(const dfx_csr* A, int32_t sigma, int32_t dtyp
                        sfirst[32 * sl + l] = prev;
                      for (int64_t k = 0; k < len; ++k)
                      {
-                       const int64_t slot = sp[sl] + 32 * k + l;
+                       const int64_t slot = slot_of(sl, k, l);
                        const bool real = k < (int64_t)row.size();
                        const int32_t c = real ? row[k].first : prev;
                        smap[slot] = real ? row[k].second : -1;

@@ -14,6 +14,8 @@
 //     entry k of row 32*s + lane sits at slice_ptr[s] + 32*k + lane;
 //   - columns are int32, or (FP32 operator) a per-row first column plus
 //     16-bit deltas between the row's sorted columns (2 bytes per entry);
+//   - FP32 operators keep each lane's entries in consecutive pairs, so a
+//     lane moves 8 bytes of values per load like the FP64 operator does;
 //   - padding entries have value 0 and repeat a valid column.
 // Values are refilled from the CSR values after every assembly through a
 // precomputed slot map (SELL entry -> CSR entry, -1 for padding).
@@ -46,28 +48,52 @@ namespace dfx
 {
 #ifdef __CUDACC__
 // Row sum of lane `lane` of slice `s` (row 32 s + lane, padded slices).
+// FP64 operators: entry k of the lane at slice_ptr[s] + 32 k + lane.
+// FP32 operators: entries in k-pairs, pair j of the lane at
+// slice_ptr[s] + 64 j + 2 lane (+0, +1), read as one 8-byte load of values
+// and one 4- or 8-byte load of column data.
 template <typename V, typename X, typename ACC, bool COMP>
 __device__ __forceinline__ ACC sell_row(const dfx_operator_s& op, const V* __restrict__ vals,
                                         const X* __restrict__ x, int32_t s, int lane)
 {
   const int64_t b = __ldg(op.slice_ptr + s);
   const int len = (int)((__ldg(op.slice_ptr + s + 1) - b) >> 5);
-  const V* v = vals + b + lane;
   ACC acc = ACC(0);
-  if constexpr (COMP)
+  if constexpr (sizeof(V) == 4)
   {
-    const uint16_t* d = op.delta + b + lane;
-    int32_t col = __ldg(op.first + 32 * (int64_t)s + lane);
-#pragma unroll 8
-    for (int k = 0; k < len; ++k)
+    const float2* v = reinterpret_cast<const float2*>(vals + b) + lane;
+    const int np = len >> 1;
+    if constexpr (COMP)
     {
-      if (k)
-        col += __ldcs(d + 32 * k);
-      acc = fma((ACC)__ldcs(v + 32 * k), (ACC)__ldg(x + col), acc);
+      const ushort2* d = reinterpret_cast<const ushort2*>(op.delta + b) + lane;
+      int32_t col = __ldg(op.first + 32 * (int64_t)s + lane);
+#pragma unroll 4
+      for (int j = 0; j < np; ++j)
+      {
+        const float2 vv = __ldcs(v + 32 * j);
+        const ushort2 dd = __ldcs(d + 32 * j);
+        col += dd.x; // delta of entry 0 is stored as 0
+        acc = fma((ACC)vv.x, (ACC)__ldg(x + col), acc);
+        col += dd.y;
+        acc = fma((ACC)vv.y, (ACC)__ldg(x + col), acc);
+      }
+    }
+    else
+    {
+      const int2* c = reinterpret_cast<const int2*>(op.cols + b) + lane;
+#pragma unroll 4
+      for (int j = 0; j < np; ++j)
+      {
+        const float2 vv = __ldcs(v + 32 * j);
+        const int2 cc = __ldcs(c + 32 * j);
+        acc = fma((ACC)vv.x, (ACC)__ldg(x + cc.x), acc);
+        acc = fma((ACC)vv.y, (ACC)__ldg(x + cc.y), acc);
+      }
     }
   }
   else
   {
+    const V* v = vals + b + lane;
     const int32_t* c = op.cols + b + lane;
 #pragma unroll 4
     for (int k = 0; k < len; ++k)
