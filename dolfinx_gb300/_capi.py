@@ -121,6 +121,8 @@ _SIGS = {
     "dfx_cg_workspace_bytes": (C.c_size_t, [C.c_int64]),
     "dfx_cg_solve": (C.c_int, [C.POINTER(Csr), _P, _P, _P, C.c_double, C.c_int32, C.c_int32, _P,
                                C.c_size_t, C.POINTER(CgInfo), _P]),
+    "dfx_cg_solve_noalloc": (C.c_int, [C.POINTER(Csr), _P, _P, _P, C.c_double, C.c_int32,
+                                       C.c_int32, C.POINTER(CgInfo), _P]),
     "dfx_operator_create": (C.c_int, [C.POINTER(Csr), C.c_int32, C.c_int32, C.c_int32,
                                       C.POINTER(C.c_void_p), _P]),
     "dfx_operator_update_values": (C.c_int, [_P, C.POINTER(Csr), _P]),

@@ -1194,3 +1194,97 @@ extern "C" int dfx_ir_solve(dfx_operator op64, dfx_operator op32, const double* 
   return DFX_OK;
 }
 
+// ---------------------------------------------------------------------------
+// CG without any allocation.
+//
+// For callers that may not allocate device or pinned host memory themselves
+// or have the library do it: code running between a host application's own
+// memory-pool set-up and its capture of a CUDA graph, plugins whose host
+// owns every allocation, and real-time loops that forbid allocation after
+// start-up. The solve uses a fixed scratch array that lives in the library's
+// device image (loaded on every GPU that loads the library and kept until
+// the process exits), launches its kernels directly (no graph is built) and
+// reads the solver state back into pageable host memory.
+namespace
+{
+// Largest problem of the no-allocation solve, in scalar unknowns.
+constexpr int64_t kNoAllocMaxN = 524288;
+// State, reduction buffers and the three CG vectors r, p, y for
+// kNoAllocMaxN unknowns (13 MiB).
+constexpr size_t kNoAllocBytes = (size_t)13 << 20;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+std::mutex g_noalloc_mutex;
+void* g_noalloc_ptr[64] = {};
+
+// Device address of the scratch array on the current device (set up once
+// per device, with that device current).
+int noalloc_scratch(void** out)
+{
+  int dev = 0;
+  DFX_CUDA(cudaGetDevice(&dev));
+  DFX_REQUIRE(dev >= 0 && dev < 64, "device index %d out of range", dev);
+  std::lock_guard<std::mutex> lk(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev])
+  {
+    void* p = nullptr;
+    DFX_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return DFX_OK;
+}
+} // namespace
+
+extern "C" int dfx_cg_solve_noalloc(const dfx_csr* A, const double* d_b, double* d_x,
+                                    const double* d_dinv, double rtol, int32_t max_iters,
+                                    int32_t check_every, dfx_cg_info* info, void* stream)
+{
+  if (int st = dfx::check_csr(A))
+    return st;
+  DFX_REQUIRE(A->dtype == DFX_F64, "dfx_cg_solve_noalloc runs in FP64");
+  DFX_REQUIRE(A->nrows == A->ncols, "matrix must be square");
+  DFX_REQUIRE(d_b && d_x, "b and x must be non-NULL");
+  DFX_REQUIRE(rtol > 0.0 && max_iters > 0, "rtol and max_iters must be positive");
+  const int64_t n = (int64_t)A->nrows * A->bs;
+  DFX_REQUIRE(n <= kNoAllocMaxN,
+              "dfx_cg_solve_noalloc takes at most %lld unknowns (got %lld); use dfx_cg_solve",
+              (long long)kNoAllocMaxN, (long long)n);
+  DFX_REQUIRE(csr_work_bytes(n) <= kNoAllocBytes,
+              "scratch of %zu bytes exceeds the fixed %zu bytes; use dfx_cg_solve",
+              csr_work_bytes(n), kNoAllocBytes);
+  void* scratch = nullptr;
+  if (int st = noalloc_scratch(&scratch))
+    return st;
+  cudaStream_t s = dfx::as_stream(stream);
+  const int K = check_every > 0 ? check_every : 20;
+  Carver c{(char*)scratch};
+  Work<double> w = carve_work<double>(c, n);
+  // The array keeps the previous call's contents: the state and the group
+  // tickets must start from zero.
+  if (int st = reset_work(w.st, w.red, w.blocks, s))
+    return st;
+  if (int st = dfx::launch_spmv(A, d_x, w.y, 0.0, s))
+    return st;
+  enqueue_init<double>(d_b, w.y, d_x, d_dinv, n, w, rtol, max_iters, s);
+  DFX_CHECK_LAUNCH();
+  OpRef o{kCsr, A, nullptr};
+  CgState h{};
+  int64_t kernels = 2;
+  const int64_t max_rounds = (int64_t)max_iters / K + 2;
+  for (int64_t round = 0;; ++round)
+  {
+    DFX_CUDA(cudaMemcpyAsync(&h, w.st, sizeof(CgState), cudaMemcpyDeviceToHost, s));
+    DFX_CUDA(cudaStreamSynchronize(s));
+    if (h.done)
+      break;
+    if (round > max_rounds)
+      return dfx::fail(DFX_ERR_TIMEOUT, "CG state never reported completion");
+    for (int k = 0; k < K; ++k)
+      enqueue_iteration<double>(o, d_x, d_dinv, n, w, false, s);
+    DFX_CHECK_LAUNCH();
+    kernels += 3 * (int64_t)K;
+  }
+  return report(&h, info, kernels);
+}
