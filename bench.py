@@ -46,6 +46,8 @@ def parse():
     p.add_argument("--inner-rtol", type=float, default=None,
                    help="reliable: residual drop between replacements (0.1); restart: inner rtol")
     p.add_argument("--ir-variant", default="reliable", choices=["reliable", "restart"])
+    p.add_argument("--profile", action="store_true",
+                   help="profiling target: a few launches of every hot kernel, no timing")
     return p.parse_args()
 
 
@@ -480,9 +482,34 @@ def run_ours(args):
         dist.destroy_process_group()
 
 
+def run_profile(args):
+    """A short run for ncu: one assembly, two launches of each operator's
+    SpMV, and a mixed-precision solve stopped at rtol 1e-3 (a few dozen
+    iterations of the fused CG kernels)."""
+    import torch
+
+    torch.cuda.set_device(0)
+    m, kappa, f = make_inputs(args.n, seed=0)
+    P = Problem(m, kappa, f, mode=args.mode, inner_rtol=args.inner_rtol, variant=args.ir_variant)
+    P.assemble()
+    P.ir.refresh()
+    n = P.A.nrows
+    x32 = torch.rand(n, dtype=torch.float32, device="cuda")
+    x64 = torch.rand(n, dtype=torch.float64, device="cuda")
+    for _ in range(2):
+        P.ir.op32.apply_renumbered(x32, torch.empty_like(x32))
+        P.ir.op64.apply_renumbered(x64, torch.empty_like(x64))
+    P.x.zero_()
+    r = P.ir.solve(P.b, P.x, rtol=1e-3)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile": "ok", "inner_iterations": r.inner_iterations}))
+
+
 def main():
     args = parse()
-    if args.impl == "reference":
+    if args.profile:
+        run_profile(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

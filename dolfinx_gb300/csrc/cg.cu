@@ -62,10 +62,10 @@ int sell_blocks(int64_t n) { return (int)std::max<int64_t>(1, (((n + 31) / 32) +
 // Grid of the grid-stride kernels without SpMV (init, correction, CSR).
 int stride_grid() { return 8 * dfx::num_sms(); }
 
-// Elementwise kernels: 256 threads x 8 entries per block and round, all
+// Elementwise kernels: 256 threads x 4 entries per block and round, all
 // loads of a round issued before any use.
 constexpr int kElemThreads = 256;
-constexpr int kElemPerThread = 8;
+constexpr int kElemPerThread = 4;
 int elem_grid(int64_t n)
 {
   const int64_t per = (int64_t)kElemThreads * kElemPerThread;
@@ -161,10 +161,12 @@ struct WarpFinal
   double s0, s1; // valid in the last warp (all lanes)
 };
 
+// Per-block staging of partial sums: one value per lane (FP64 kernels) or
+// per warp (FP32 kernels), for up to 8 warps.
 struct BlockScratch
 {
-  double p0[32];
-  double p1[32];
+  double p0[256];
+  double p1[256];
   unsigned int count;
 };
 
@@ -181,34 +183,74 @@ __device__ __forceinline__ void block_reduce_init()
   __syncthreads();
 }
 
-__device__ __forceinline__ WarpFinal publish(double v0, double v1, const Red& red,
-                                             unsigned int* ticket, bool two)
+// T = float: each warp sums its lanes in FP32 (its lanes hold FP32 partials
+// of at most a few entries each) and lane 0 stages the warp sum; the last
+// warp adds the block's warp sums in FP64 in one lane. T = double: every lane
+// stages its FP64 partial; the last warp adds them in lane-then-warp order.
+// Both keep FP64 instructions -- 1/58 of the FP32 rate here -- off the
+// per-warp path.
+template <typename T>
+__device__ __forceinline__ WarpFinal publish(T v0, T v1, const Red& red, unsigned int* ticket,
+                                             bool two)
 {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const unsigned nw = blockDim.x >> 5;
   BlockScratch& bs = block_scratch();
   WarpFinal out{false, 0.0, 0.0};
-  v0 = dfx::warp_sum(v0);
-  if (two)
-    v1 = dfx::warp_sum(v1);
+  if constexpr (sizeof(T) == 4)
+  {
+    v0 = dfx::warp_sum(v0);
+    if (two)
+      v1 = dfx::warp_sum(v1);
+    if (lane == 0)
+    {
+      bs.p0[warp] = (double)v0;
+      if (two)
+        bs.p1[warp] = (double)v1;
+    }
+  }
+  else
+  {
+    bs.p0[threadIdx.x] = (double)v0;
+    if (two)
+      bs.p1[threadIdx.x] = (double)v1;
+  }
+  __syncwarp();
   int flag = 0;
   if (lane == 0)
   {
-    bs.p0[warp] = v0;
-    if (two)
-      bs.p1[warp] = v1;
     __threadfence_block();
     flag = atomicAdd(&bs.count, 1u) == nw - 1;
   }
   if (!__shfl_sync(0xffffffffu, flag, 0))
     return out;
-  // Last warp of the block: block partial in warp-index order.
+  // Last warp of the block: the block partial, in a fixed order.
   __threadfence_block();
-  double b0 = lane < (int)nw ? ((volatile double*)bs.p0)[lane] : 0.0;
-  double b1 = (two && lane < (int)nw) ? ((volatile double*)bs.p1)[lane] : 0.0;
-  b0 = dfx::warp_sum(b0);
-  if (two)
-    b1 = dfx::warp_sum(b1);
+  volatile double* q0 = bs.p0;
+  volatile double* q1 = bs.p1;
+  double b0 = 0.0, b1 = 0.0;
+  if constexpr (sizeof(T) == 4)
+  {
+    if (lane == 0)
+      for (unsigned w = 0; w < nw; ++w)
+      {
+        b0 += q0[w];
+        if (two)
+          b1 += q1[w];
+      }
+  }
+  else
+  {
+    for (unsigned w = 0; w < nw; ++w)
+    {
+      b0 += q0[32 * w + lane];
+      if (two)
+        b1 += q1[32 * w + lane];
+    }
+    b0 = dfx::warp_sum(b0);
+    if (two)
+      b1 = dfx::warp_sum(b1);
+  }
   const unsigned unit = blockIdx.x, nunits = gridDim.x;
   const unsigned g = unit / kGroup;
   const unsigned ng = (nunits + kGroup - 1) / kGroup;
@@ -287,7 +329,7 @@ __global__ void __launch_bounds__(kThreads)
     rr += r * r;
     rz += r * z;
   }
-  const WarpFinal f = publish((double)rr, (double)rz, w.red, &w.st->ticket[0], true);
+  const WarpFinal f = publish<T>(rr, rz, w.red, &w.st->ticket[0], true);
   if (f.last)
   {
     const double srr = f.s0, srz = f.s1;
@@ -380,7 +422,7 @@ __global__ void __launch_bounds__(kThreads)
       }
     }
   }
-  finish_pap(publish(dot, 0.0, w.red, &w.st->ticket[1], false), w.st);
+  finish_pap(publish<double>(dot, 0.0, w.red, &w.st->ticket[1], false), w.st);
 }
 
 // y = A p, p.y -- sliced-ELL operator, one row per lane, warp per slice.
@@ -405,7 +447,7 @@ __global__ void __launch_bounds__(kSellThreads)
       dot += acc * w.p[row];
     }
   }
-  finish_pap(publish((double)dot, 0.0, w.red, &w.st->ticket[1], false), w.st);
+  finish_pap(publish<T>(dot, T(0), w.red, &w.st->ticket[1], false), w.st);
 }
 
 template <typename T, bool PRE, bool RELIABLE>
@@ -448,7 +490,7 @@ __global__ void __launch_bounds__(kElemThreads)
       rz += rn * (PRE ? d[e] * rn : rn);
     }
   }
-  const WarpFinal f = publish((double)rr, (double)rz, w.red, &w.st->ticket[2], true);
+  const WarpFinal f = publish<T>(rr, rz, w.red, &w.st->ticket[2], true);
   if (f.last)
   {
     const double srr = f.s0, srz = f.s1;
@@ -555,7 +597,7 @@ __global__ void __launch_bounds__(kSellThreads)
       rr += r * r;
     }
   }
-  const WarpFinal f = publish(rr, 0.0, red, &st->ticket[3], false);
+  const WarpFinal f = publish<double>(rr, 0.0, red, &st->ticket[3], false);
   if (f.last)
   {
     const double srr = f.s0;
@@ -627,7 +669,7 @@ __global__ void __launch_bounds__(kSellThreads)
       rz += (double)r32 * z;
     }
   }
-  const WarpFinal f = publish(rr, rz, w.red, &w.st->ticket[3], true);
+  const WarpFinal f = publish<double>(rr, rz, w.red, &w.st->ticket[3], true);
   if (f.last)
   {
     const double srr = f.s0, srz = f.s1;
