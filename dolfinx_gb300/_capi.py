@@ -96,6 +96,21 @@ class IrInfo(C.Structure):
     ]
 
 
+class BatchSystem(C.Structure):
+    _fields_ = [
+        ("op32", C.c_void_p),
+        ("op64", C.c_void_p),
+        ("b", C.c_void_p),
+        ("x", C.c_void_p),
+        ("dinv", C.c_void_p),
+        ("work", C.c_void_p),
+        ("rtol", C.c_double),
+        ("delta", C.c_double),
+        ("max_iters", C.c_int32),
+        ("mode", C.c_int32),
+    ]
+
+
 _P = C.c_void_p
 _SIGS = {
     "dfx_last_error": (C.c_char_p, []),
@@ -131,6 +146,16 @@ _SIGS = {
     "dfx_operator_info": (C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int32),
                                     C.POINTER(C.c_void_p)]),
     "dfx_operator_destroy": (C.c_int, [_P]),
+    "dfx_operator_share": (C.c_int, [_P, C.POINTER(C.c_void_p)]),
+    "dfx_operator_permute": (C.c_int, [_P, _P, _P, C.c_int32, _P]),
+    "dfx_batch_workspace_bytes": (C.c_size_t, [C.c_int64, C.c_int32]),
+    "dfx_batch_create": (C.c_int, [C.c_int32, C.POINTER(C.c_void_p)]),
+    "dfx_batch_destroy": (C.c_int, [_P]),
+    "dfx_batch_set": (C.c_int, [_P, C.c_int32, C.POINTER(BatchSystem), _P]),
+    "dfx_batch_clear": (C.c_int, [_P, C.c_int32]),
+    "dfx_batch_step": (C.c_int, [_P, C.c_int32, C.POINTER(C.c_int32), _P]),
+    "dfx_batch_info": (C.c_int, [_P, C.c_int32, C.POINTER(CgInfo), C.POINTER(C.c_int32),
+                                 C.POINTER(C.c_int32)]),
     "dfx_cg_op_workspace_bytes": (C.c_size_t, [C.c_int64]),
     "dfx_cg_solve_op": (C.c_int, [_P, _P, _P, _P, C.c_double, C.c_int32, C.c_int32, _P,
                                   C.c_size_t, C.POINTER(CgInfo), _P]),

@@ -76,8 +76,14 @@ void free_op(dfx_operator_s* op)
   int cur = 0;
   cudaGetDevice(&cur);
   cudaSetDevice(op->device);
-  for (void* p : {(void*)op->perm, (void*)op->iperm, (void*)op->slice_ptr, (void*)op->cols,
-                  (void*)op->delta, (void*)op->first, (void*)op->map, op->vals, op->tmp})
+  if (op->owns_structure)
+    for (void* p : {(void*)op->perm, (void*)op->iperm, (void*)op->slice_ptr, (void*)op->cols,
+                    (void*)op->delta, (void*)op->first, (void*)op->map})
+      if (p)
+        cudaFree(p);
+  else if (op->source)
+    op->source->shares -= 1;
+  for (void* p : {op->vals, op->tmp})
     if (p)
       cudaFree(p);
   cudaSetDevice(cur);
@@ -298,7 +304,35 @@ extern "C" int dfx_operator_update_values(dfx_operator op, const dfx_csr* A, voi
 
 extern "C" int dfx_operator_destroy(dfx_operator op)
 {
+  if (op && op->shares > 0)
+    return dfx::fail(DFX_ERR_INVALID, "operator structure is still shared by %d operators",
+                     op->shares);
   free_op(op);
+  return DFX_OK;
+}
+
+extern "C" int dfx_operator_share(dfx_operator src, dfx_operator* out)
+{
+  DFX_REQUIRE(src && out, "arguments must be non-NULL");
+  DFX_REQUIRE(src->owns_structure, "share the source operator, not a share");
+  *out = nullptr;
+  auto* op = new dfx_operator_s(*src);
+  op->owns_structure = 0;
+  op->shares = 0;
+  op->source = src;
+  op->vals = nullptr;
+  op->tmp = nullptr;
+  const size_t vb = op->dtype == DFX_F64 ? 8 : 4;
+  if (cudaMalloc(&op->vals, vb * std::max<int64_t>(op->nslots, 1)) != cudaSuccess
+      || cudaMalloc(&op->tmp, vb * 2 * std::max<int64_t>(op->n, 1)) != cudaSuccess)
+  {
+    if (op->vals)
+      cudaFree(op->vals);
+    delete op;
+    return dfx::fail(DFX_ERR_NO_MEMORY, "operator values: out of device memory");
+  }
+  src->shares += 1;
+  *out = op;
   return DFX_OK;
 }
 

@@ -42,6 +42,12 @@ struct dfx_operator_s
   void* vals = nullptr;         // (nslots) f64 or f32
   void* tmp = nullptr;          // 2 n scratch values for dfx_operator_apply
   int device = 0;
+  // Structure sharing (dfx_operator_share): a share points at its source's
+  // structure arrays and owns only its values; the source counts its shares
+  // and may not be destroyed while any is alive.
+  int32_t owns_structure = 1;
+  int32_t shares = 0;
+  dfx_operator_s* source = nullptr;
 };
 
 namespace dfx

@@ -174,17 +174,43 @@ class SellOperator:
     with update_values() after re-assembly."""
 
     def __init__(self, A: MatrixCSR, dtype=torch.float64, sigma: int = 256,
-                 compress_cols: bool | None = None):
-        if compress_cols is None:
-            compress_cols = dtype == torch.float32
+                 compress_cols: bool | None = None, share_of: "SellOperator | None" = None):
         self.A, self.dtype, self.sigma = A, dtype, sigma
         h = C.c_void_p()
+        if share_of is not None:
+            # same structure as share_of, own values (one set per request)
+            self.dtype, self.sigma, self.compressed = share_of.dtype, share_of.sigma, share_of.compressed
+            _capi.check(_capi.lib().dfx_operator_share(share_of.handle, C.byref(h)))
+            self.source = share_of
+            self.handle = h
+            if A is not None:
+                self.update_values()
+            return
+        if compress_cols is None:
+            compress_cols = dtype == torch.float32
         dt = _capi.F64 if dtype == torch.float64 else _capi.F32
         _capi.check(_capi.lib().dfx_operator_create(C.byref(A.csr()), sigma, dt,
                                                     int(bool(compress_cols)), C.byref(h),
                                                     _stream()))
         self.handle = h
         self.compressed = bool(compress_cols)
+
+    def share(self, A: MatrixCSR) -> "SellOperator":
+        """An operator with this structure and the values of A."""
+        return SellOperator(A, share_of=self)
+
+    def to_operator(self, v: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        """v in the operator's (renumbered) numbering."""
+        if out is None:
+            out = torch.empty_like(v)
+        _capi.check(_capi.lib().dfx_operator_permute(self.handle, _ptr(v), _ptr(out), 1, _stream()))
+        return out
+
+    def from_operator(self, v: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        if out is None:
+            out = torch.empty_like(v)
+        _capi.check(_capi.lib().dfx_operator_permute(self.handle, _ptr(v), _ptr(out), 0, _stream()))
+        return out
 
     def update_values(self):
         _capi.check(_capi.lib().dfx_operator_update_values(self.handle, C.byref(self.A.csr()),

@@ -1,0 +1,384 @@
+"""Device-resident serving loop for assemble-and-solve requests.
+
+Each request is a Poisson/Helmholtz problem
+``a(u, v) = int kappa grad u.grad v + k2 u v``, ``L(v) = int f v`` on a unit
+cube of n^3 x 6 tetrahedra, Lagrange P1 or P2, with u = 0 on the whole
+boundary. kappa is lognormal(0, 1) per cell and f ~ U[-1, 1] per P1 node, both
+from the request's seed. The ``+ k2`` sign keeps the operator SPD for every
+kappa field, so CG applies. The reference defines this Helmholtz problem in
+python/demo/demo_helmholtz.py; the sign is this loop's stated choice.
+
+Design (GB300, one GPU):
+
+- **Resident structure.** Meshes, dofmaps, CSR structure, the cell->slot
+  maps and the sliced-ELL operator structures are built once per
+  (n, degree) and kept on the device in an LRU cache. A request only adds
+  its own values: the CSR values, operator values and vectors.
+- **Admission by HBM budget.** A request enters when its bytes fit under
+  the budget, next to the cached structures and the requests in flight.
+- **Small systems** (at most ``batch_max_dofs`` dofs) share one persistent
+  batched CG launch (``dfx_batch_step``), one CTA per system. The launch
+  advances every active system by ``quantum`` iterations; between launches
+  finished systems retire and new requests join. This is continuous
+  batching: requests that arrive while others run are admitted as slots and
+  memory free up, and their work overlaps on the device.
+- **Larger systems** go to a whole-GPU solver on worker threads, each with
+  its own CUDA stream, so they overlap with the batch.
+
+``mode = "mixed"``: FP32 operator and inner PCG with FP64 reliable updates.
+``mode = "fp64"``: plain FP64 PCG. Both stop at ``|b - A x| / |b| < rtol``,
+evaluated in FP64.
+"""
+
+from __future__ import annotations
+
+import collections
+import ctypes as C
+import math
+import queue
+import threading
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _capi, fem, la, mesh
+
+
+@dataclass
+class Request:
+    rid: int
+    n: int
+    degree: int
+    k2: float
+    seed: int
+    arrival: float = 0.0  # seconds from the start of the stream
+
+
+def make_requests(count: int, rate: float, seed: int = 0, n_range=(8, 96)) -> list[Request]:
+    """Synthetic request stream: Poisson arrivals at `rate`/s, n log-uniform
+    in n_range, P1/P2 with equal probability, k2 ~ U[0, 10]."""
+    rng = np.random.default_rng(seed)
+    t = np.cumsum(rng.exponential(1.0 / rate, count))
+    lo, hi = math.log(n_range[0]), math.log(n_range[1])
+    out = []
+    for i in range(count):
+        n = int(round(math.exp(rng.uniform(lo, hi))))
+        deg = 1 if rng.uniform() < 0.5 else 2
+        out.append(Request(i, n, deg, float(rng.uniform(0.0, 10.0)), int(rng.integers(2 ** 31)),
+                           float(t[i])))
+    return out
+
+
+def request_inputs(msh: mesh.Mesh, seed: int):
+    rng = np.random.default_rng(seed)
+    kappa = np.exp(rng.normal(0.0, 1.0, msh.num_cells))
+    f = rng.uniform(-1.0, 1.0, msh.num_nodes)
+    return kappa, f
+
+
+def _stream_ptr(s):
+    return C.c_void_p(s.cuda_stream)
+
+
+class Structure:
+    """Everything of one (n, degree) that requests share."""
+
+    def __init__(self, n: int, degree: int, device="cuda"):
+        self.n, self.degree = n, degree
+        self.mesh = mesh.create_unit_cube(n, n, n)
+        self.V = fem.functionspace(self.mesh, ("Lagrange", degree), device=device)
+        X = self.V.tabulate_dof_coordinates()
+        bnd = np.flatnonzero(np.isclose(X, 0.0).any(1) | np.isclose(X, 1.0).any(1))
+        self.bc = fem.dirichletbc(0.0, bnd.astype(np.int32), self.V)
+        a = fem.poisson_form(self.V, 1.0, k2=1.0)
+        self.asm = fem.MatrixAssembler(a, [self.bc])  # slot map, markers, structure
+        self.A0 = self.asm.A
+        self.A0.vals.fill_(1.0)  # any values: the operators copy only the structure here
+        self.op64 = la.SellOperator(self.A0, torch.float64)
+        self.op32 = la.SellOperator(self.A0, torch.float32, compress_cols=True)
+        self.ndofs = self.V.num_dofs
+        self.nnz = self.A0.nnz
+        self.mesh.device(device)
+        self.bytes = (self.A0.row_ptr.numel() * 8 + self.A0.cols.numel() * 4 + self.nnz * 8
+                      + self.asm.map.numel() + 3 * self.ops_slots() * 4 + self.ops_slots() * 6
+                      + self.V.dofmap.nbytes + self.mesh.cells.nbytes + self.mesh.x.nbytes)
+        self.users = 0
+
+    def ops_slots(self):
+        return self.op64.info()["slots"]
+
+    def request_bytes(self) -> int:
+        n = self.ndofs
+        slots = self.ops_slots()
+        return (self.nnz * 8 + slots * 12 + n * 8 * 8 + self.mesh.num_cells * 8
+                + self.mesh.num_nodes * 8 + int(_capi.lib().dfx_ir_workspace_bytes(n)))
+
+
+class Job:
+    """One admitted request: its values and vectors on the device."""
+
+    def __init__(self, req: Request, st: Structure, mode: str, stream, assembly: str = "atomic"):
+        self.req, self.st, self.mode = req, st, mode
+        V = st.V
+        kappa, f = request_inputs(st.mesh, req.seed)
+        with torch.cuda.stream(stream):
+            self.kappa = torch.from_numpy(kappa).to("cuda", non_blocking=True)
+            self.f = torch.from_numpy(f).to("cuda", non_blocking=True)
+            a = fem.poisson_form(V, self.kappa, k2=req.k2)
+            L = fem.source_form(V, self.f)
+            self.A = la.MatrixCSR(st.A0.row_ptr, st.A0.cols,
+                                  torch.zeros_like(st.A0.vals), 1)
+            asm = st.asm
+            amode = fem._mode(assembly)
+            order, off, ncol = fem._colour_args(V, amode)
+            _capi.check(_capi.lib().dfx_assemble_matrix(
+                C.byref(a.cstruct()), C.byref(self.A.csr()), la._ptr(asm.map),
+                la._ptr(asm.markers), amode, order, off, ncol, _stream_ptr(stream)))
+            _capi.check(_capi.lib().dfx_set_diagonal(
+                C.byref(self.A.csr()), la._ptr(asm.diag_dofs), int(asm.diag_dofs.numel()), 1.0,
+                _stream_ptr(stream)))
+            self.b = fem.RhsAssembler(L, a, [st.bc], mode=assembly).assemble()
+            self.dinv = self.A.inverse_diagonal()
+            self.op64 = st.op64.share(self.A)
+            self.op32 = st.op32.share(self.A) if mode == "mixed" else None
+            self.bp = self.op64.to_operator(self.b)
+            self.dp = self.op64.to_operator(self.dinv)
+            self.xp = torch.zeros_like(self.bp)
+        self.slot = None
+        self.info = None
+        self.t_done = None
+
+    def solution(self) -> torch.Tensor:
+        return self.op64.from_operator(self.xp)
+
+
+class Server:
+    """Continuous-batching server (one GPU)."""
+
+    def __init__(self, mode: str = "mixed", hbm_budget: float = 64e9, capacity: int = 512,
+                 quantum: int = 25, batch_max_dofs: int = 65536, rtol: float = 1e-10,
+                 workers: int = 2, delta: float = 0.01, assembly: str = "atomic"):
+        """assembly: "atomic" (FP64 atomics) or "coloured" (deterministic
+        summation order, so a request's matrix is bitwise reproducible)."""
+        assert mode in ("mixed", "fp64")
+        self.assembly = assembly
+        self.mode, self.budget, self.capacity = mode, hbm_budget, capacity
+        self.quantum, self.batch_max_dofs, self.rtol = quantum, batch_max_dofs, rtol
+        self.delta = delta
+        self.structures: collections.OrderedDict = collections.OrderedDict()
+        self.used = 0
+        h = C.c_void_p()
+        _capi.check(_capi.lib().dfx_batch_create(capacity, C.byref(h)))
+        self.batch = h
+        self.free_slots = list(range(capacity))
+        self.active: dict[int, Job] = {}
+        self.stream_setup = torch.cuda.Stream()
+        self.stream_batch = torch.cuda.Stream()
+        self.lock = threading.Lock()
+        self.large_q: queue.Queue = queue.Queue()
+        self.workers = [threading.Thread(target=self._worker, daemon=True) for _ in range(workers)]
+        self.finished: list[Job] = []
+        self._stop = False
+        for w in self.workers:
+            w.start()
+
+    # ------------------------------------------------------------ structures
+    def structure(self, n: int, degree: int) -> Structure:
+        key = (n, degree)
+        st = self.structures.get(key)
+        if st is None:
+            st = Structure(n, degree)
+            self.structures[key] = st
+            self.used += st.bytes
+            self._evict()
+        self.structures.move_to_end(key)
+        return st
+
+    def _evict(self):
+        for key in list(self.structures):
+            if self.used <= self.budget:
+                break
+            st = self.structures[key]
+            if st.users == 0:
+                self.used -= st.bytes
+                del self.structures[key]
+
+    def prewarm(self, requests):
+        for key in sorted({(r.n, r.degree) for r in requests}):
+            self.structure(*key)
+        torch.cuda.synchronize()
+
+    # ------------------------------------------------------------ admission
+    def admit(self, req: Request) -> Job | None:
+        st = self.structure(req.n, req.degree)
+        need = st.request_bytes()
+        small = st.ndofs <= self.batch_max_dofs
+        with self.lock:
+            if self.used + need > self.budget:
+                return None
+            if small and not self.free_slots:
+                return None
+            self.used += need
+            st.users += 1
+        job = Job(req, st, self.mode, self.stream_setup, self.assembly)
+        job.bytes = need
+        if small:
+            self.stream_setup.synchronize()
+            slot = self.free_slots.pop()
+            wb = int(_capi.lib().dfx_batch_workspace_bytes(st.ndofs, 1 if self.mode == "mixed" else 0))
+            job.work = torch.empty(wb, dtype=torch.uint8, device="cuda")
+            sysd = _capi.BatchSystem(
+                None if job.op32 is None else job.op32.handle.value, job.op64.handle.value,
+                job.bp.data_ptr(), job.xp.data_ptr(), job.dp.data_ptr(), job.work.data_ptr(),
+                self.rtol, self.delta, 100000, 1 if self.mode == "mixed" else 0)
+            _capi.check(_capi.lib().dfx_batch_set(self.batch, slot, C.byref(sysd),
+                                                  _stream_ptr(self.stream_setup)))
+            job.slot = slot
+            self.active[slot] = job
+        else:
+            self.stream_setup.synchronize()
+            self.large_q.put(job)
+        return job
+
+    def _release(self, job: Job):
+        with self.lock:
+            self.used -= job.bytes
+            job.st.users -= 1
+            if job.slot is not None:
+                self.free_slots.append(job.slot)
+            self.finished.append(job)
+
+    # ------------------------------------------------------------ solving
+    def _worker(self):
+        stream = torch.cuda.Stream()
+        while True:
+            job = self.large_q.get()
+            if job is None:
+                return
+            n = job.st.ndofs
+            with torch.cuda.stream(stream):
+                if self.mode == "mixed":
+                    wb = int(_capi.lib().dfx_ir_workspace_bytes(n))
+                    work = torch.empty(wb, dtype=torch.uint8, device="cuda")
+                    info = _capi.IrInfo()
+                    x = torch.zeros_like(job.b)
+                    _capi.check(_capi.lib().dfx_ir_solve(
+                        job.op64.handle, job.op32.handle, la._ptr(job.b), la._ptr(x),
+                        la._ptr(job.dinv), self.rtol, self.delta, 200, 100000, 20,
+                        _capi.IR_RELIABLE, la._ptr(work), wb, C.byref(info), _stream_ptr(stream)))
+                    job.iterations = info.inner_iterations
+                else:
+                    wb = int(_capi.lib().dfx_cg_op_workspace_bytes(n))
+                    work = torch.empty(wb, dtype=torch.uint8, device="cuda")
+                    info = _capi.CgInfo()
+                    x = torch.zeros_like(job.b)
+                    _capi.check(_capi.lib().dfx_cg_solve_op(
+                        job.op64.handle, la._ptr(job.b), la._ptr(x), la._ptr(job.dinv),
+                        self.rtol, 100000, 20, la._ptr(work), wb, C.byref(info),
+                        _stream_ptr(stream)))
+                    job.iterations = info.iterations
+                job.x = x.cpu()
+                stream.synchronize()
+            job.t_done = time.perf_counter()
+            job.status = info.status
+            self._release(job)
+
+    def step(self) -> int:
+        """One batched launch; retires finished systems. Returns #active."""
+        if not self.active:
+            return 0
+        cnt = C.c_int32(0)
+        _capi.check(_capi.lib().dfx_batch_step(self.batch, self.quantum, C.byref(cnt),
+                                               _stream_ptr(self.stream_batch)))
+        now = time.perf_counter()
+        for slot in list(self.active):
+            done = C.c_int32(0)
+            rep = C.c_int32(0)
+            info = _capi.CgInfo()
+            _capi.lib().dfx_batch_info(self.batch, slot, C.byref(info), C.byref(done),
+                                       C.byref(rep))
+            if done.value:
+                job = self.active.pop(slot)
+                _capi.lib().dfx_batch_clear(self.batch, slot)
+                with torch.cuda.stream(self.stream_batch):
+                    job.x = job.solution().cpu()
+                job.t_done = now
+                job.status = info.status
+                job.iterations = info.iterations
+                self._release(job)
+        return len(self.active)
+
+    def run(self, requests: list[Request]) -> dict:
+        """Serve a timed stream (arrival times relative to the start)."""
+        pending = collections.deque(sorted(requests, key=lambda r: r.arrival))
+        total = len(pending)
+        self.finished = []
+        t0 = time.perf_counter()
+        waiting: collections.deque = collections.deque()
+        arrivals = {}
+        while len(self.finished) < total:
+            now = time.perf_counter() - t0
+            while pending and pending[0].arrival <= now:
+                r = pending.popleft()
+                waiting.append(r)
+                arrivals[r.rid] = t0 + r.arrival
+            while waiting:
+                job = self.admit(waiting[0])
+                if job is None:
+                    break
+                waiting.popleft()
+            if self.active:
+                self.step()
+            elif pending and not waiting:
+                time.sleep(max(0.0, min(0.002, pending[0].arrival - (time.perf_counter() - t0))))
+            else:
+                time.sleep(0.0005)
+        wall = time.perf_counter() - t0
+        lat = np.array([j.t_done - arrivals[j.req.rid] for j in self.finished])
+        bad = [j.req.rid for j in self.finished if j.status != 0]
+        return {"mode": self.mode, "requests": total, "wall_s": wall,
+                "solves_per_s": total / wall,
+                "p50_ms": float(np.percentile(lat, 50) * 1e3),
+                "p99_ms": float(np.percentile(lat, 99) * 1e3),
+                "mean_ms": float(lat.mean() * 1e3),
+                "dofs_per_s": float(sum(j.st.ndofs for j in self.finished) / wall),
+                "failed": bad}
+
+    def close(self):
+        for _ in self.workers:
+            self.large_q.put(None)
+        for w in self.workers:
+            w.join(timeout=30)
+        _capi.lib().dfx_batch_destroy(self.batch)
+        self.batch = None
+
+
+def serve(requests, mode="mixed", **kw) -> tuple[dict, list[Job]]:
+    srv = Server(mode=mode, **kw)
+    try:
+        srv.prewarm(requests)
+        stats = srv.run(requests)
+        return stats, list(srv.finished)
+    finally:
+        srv.close()
+
+
+if __name__ == "__main__":
+    import argparse
+    import json
+
+    p = argparse.ArgumentParser(description="serving-loop measurement (one GPU)")
+    p.add_argument("--requests", type=int, default=200)
+    p.add_argument("--rates", type=float, nargs="+", default=[100.0, 1000.0])
+    p.add_argument("--nmin", type=int, default=8)
+    p.add_argument("--nmax", type=int, default=96)
+    p.add_argument("--budget-gb", type=float, default=64.0)
+    args = p.parse_args()
+    for rate in args.rates:
+        reqs = make_requests(args.requests, rate, seed=1, n_range=(args.nmin, args.nmax))
+        for mode in ("fp64", "mixed"):
+            stats, _ = serve(reqs, mode=mode, hbm_budget=args.budget_gb * 1e9)
+            stats["rate"] = rate
+            print(json.dumps(stats), flush=True)

@@ -319,6 +319,52 @@ int dfx_ir_solve(dfx_operator op64, dfx_operator op32, const double* d_b, double
                  int32_t variant, void* d_work, size_t work_bytes, dfx_ir_info* info,
                  void* stream);
 
+/* dfx_operator whose structure (permutation, slices, columns, slot map) is
+ * src's and whose values are its own: one structure per mesh, one set of
+ * values per request. src must outlive its shares. */
+int dfx_operator_share(dfx_operator src, dfx_operator* out);
+/* to_operator != 0: out[i] = in[perm[i]] (into the operator's numbering);
+ * otherwise out[perm[i]] = in[i] (back to the original numbering). */
+int dfx_operator_permute(dfx_operator op, const double* d_in, double* d_out,
+                         int32_t to_operator, void* stream);
+
+/* --------------------------------------------------------- batched CG
+ * Serving path (no reference counterpart; it runs the demo's CG,
+ * cpp/demo/poisson_matrix_free/main.cpp:84-132, for many systems at once).
+ * One persistent launch advances every active system by up to `iterations`
+ * PCG iterations, one CTA of 1024 threads per system, block reductions only;
+ * the host retires finished systems and admits new ones between steps
+ * (continuous batching). Vectors are in the operators' numbering
+ * (dfx_operator_permute). mode 0: FP64 PCG on op64; mode 1: FP32 PCG on
+ * op32 with FP64 reliable updates on op64 every time |r| drops by `delta`
+ * (<= 0: 0.01). Stopping test |b - A x|^2 / |b - A x0|^2 < rtol^2, evaluated
+ * in FP64. A system's result does not depend on the other systems. */
+typedef struct dfx_batch_s* dfx_batch;
+typedef struct dfx_batch_system
+{
+  dfx_operator op32;   /* FP32 operator (mode 1), or NULL */
+  dfx_operator op64;   /* FP64 operator */
+  const double* b;     /* right-hand side, operator numbering */
+  double* x;           /* initial guess in, solution out, operator numbering */
+  const double* dinv;  /* Jacobi inverse diagonal (operator numbering) or NULL */
+  void* work;          /* dfx_batch_workspace_bytes(n, mode) bytes, 256-aligned */
+  double rtol;
+  double delta;
+  int32_t max_iters;
+  int32_t mode;
+} dfx_batch_system;
+
+size_t dfx_batch_workspace_bytes(int64_t n, int32_t mode);
+int dfx_batch_create(int32_t capacity, dfx_batch* out);
+int dfx_batch_destroy(dfx_batch b);
+/* Put a system in a slot (its state restarts). */
+int dfx_batch_set(dfx_batch b, int32_t slot, const dfx_batch_system* sys, void* stream);
+int dfx_batch_clear(dfx_batch b, int32_t slot);
+/* One launch over the set, unfinished slots; returns when it is done. */
+int dfx_batch_step(dfx_batch b, int32_t iterations, int32_t* num_active, void* stream);
+int dfx_batch_info(dfx_batch b, int32_t slot, dfx_cg_info* info, int32_t* done,
+                   int32_t* replacements);
+
 #ifdef __cplusplus
 }
 #endif
