@@ -46,6 +46,10 @@ def parse():
     p.add_argument("--inner-rtol", type=float, default=None,
                    help="reliable: residual drop between replacements (0.1); restart: inner rtol")
     p.add_argument("--ir-variant", default="reliable", choices=["reliable", "restart"])
+    p.add_argument("--serving-requests", type=int, default=100,
+                   help="requests of the bounded serving sample (0: skip)")
+    p.add_argument("--serving-nmax", type=int, default=48)
+    p.add_argument("--no-c3", action="store_true", help="skip the elasticity (c3) sample")
     p.add_argument("--profile", action="store_true",
                    help="profiling target: a few launches of every hot kernel, no timing")
     return p.parse_args()
@@ -322,6 +326,84 @@ def run_reference(args):
 
 
 # --------------------------------------------------------------------------- our arm
+def c3_sample(steps=1, warmup=1):
+    """Linear elasticity, vector P2 on [0,4]x[0,1]^2 split into 96x24x24
+    hexahedra x 6 tetrahedra (331,776 cells, 1,390,179 dofs), E lognormal
+    (log 1e3, 0.5) per cell, nu = 0.3, body force (0,0,-1), clamped at x = 0.
+    Block (3x3) CSR assembly, expansion to the scalar CSR, then plain FP64
+    Jacobi-PCG and FP32-inner / FP64-outer refinement, both to rtol 1e-10
+    evaluated in FP64."""
+    import numpy as np
+    import torch
+
+    from dolfinx_gb300 import fem, la, mesh
+
+    m = mesh.create_box(((0.0, 0.0, 0.0), (4.0, 1.0, 1.0)), (96, 24, 24))
+    V = fem.functionspace(m, ("Lagrange", 2, (3,)))
+    rng = np.random.default_rng(3)
+    E = np.exp(rng.normal(np.log(1e3), 0.5, m.num_cells))
+    X = V.tabulate_dof_coordinates()
+    bc = fem.dirichletbc(np.zeros(3), np.flatnonzero(np.isclose(X[:, 0], 0.0)).astype(np.int32), V)
+    a = fem.elasticity_form(V, torch.from_numpy(E).cuda(), 0.3)
+    masm = fem.MatrixAssembler(a, [bc])
+    rhs = fem.RhsAssembler(fem.body_force_form(V, (0.0, 0.0, -1.0)), a, [bc])
+    A = masm.assemble()
+    S = A.expand_blocks()
+    b = rhs.assemble()
+    fp64 = la.OperatorCGSolver(S)
+    ir = la.IRSolver(S, inner_rtol=0.01)
+    x = torch.zeros_like(b)
+    stream = torch.cuda.current_stream()
+
+    def step_raw(solver):
+        masm.assemble(zero=True)
+        A.expand_blocks(out=S)
+        rhs.assemble(b)
+        solver.refresh()
+        x.zero_()
+        return solver.solve(b, x, rtol=1e-10, raise_on_fail=False)
+
+    out = {"workload": "vector P2 elasticity, box 4x1x1, 96x24x24x6 tets", "cells": m.num_cells,
+           "dofs": V.num_dofs, "blocks": A.nnz, "scalar_nnz": S.nnz}
+    for name, solver in (("fp64_plain", fp64), ("mixed", ir)):
+        for _ in range(warmup):
+            step_raw(solver)
+        ms, res = _timed(lambda: step_raw(solver), steps, stream)
+        r = res[-1]
+        out[name] = {"ms_per_step": ms, "gdof_per_s": V.num_dofs / (ms * 1e-3) / 1e9,
+                     "iterations": [q.iterations for q in res], "status": r.status,
+                     "final_rel_residual": float(np.sqrt(r.rnorm_sq / r.rnorm0_sq))}
+        if name == "fp64_plain":
+            x64 = x.clone()
+    out["rel_err_vs_fp64_solution"] = float((x - x64).norm() / x64.norm())
+    out["speedup_of_mixed"] = out["fp64_plain"]["ms_per_step"] / out["mixed"]["ms_per_step"]
+    out["note"] = ("status 4 = the FP32-valued inner solve stagnated before rtol 1e-10: its "
+                   "entry rounding exceeds the smallest eigenvalue of this system")
+    return out
+
+
+def serving_sample(args):
+    """Serving loop on a bounded stream drawn like the serving config (unit
+    cubes, n log-uniform, P1/P2, Helmholtz k2 in [0, 10], lognormal kappa),
+    with n capped at --serving-nmax so that the sample ends in seconds. Two
+    arrival rates: 200/s (latency) and 5000/s (saturation: solves/s is the
+    capacity), each in FP64 and mixed precision."""
+    from dolfinx_gb300 import serving
+
+    out = {"requests": args.serving_requests, "n_range": [8, args.serving_nmax], "runs": []}
+    for rate in (200.0, 5000.0):
+        reqs = serving.make_requests(args.serving_requests, rate, seed=1,
+                                     n_range=(8, args.serving_nmax))
+        res = {}
+        for mode in ("fp64", "mixed"):
+            stats, _ = serving.serve(reqs, mode=mode, hbm_budget=64e9, max_wall_s=120.0)
+            res[mode] = {k: stats[k] for k in ("solves_per_s", "p50_ms", "p99_ms", "failed")}
+        res["rate"] = rate
+        res["mixed_over_fp64_solves"] = res["mixed"]["solves_per_s"] / res["fp64"]["solves_per_s"]
+        out["runs"].append(res)
+    return out
+
+
 def _timed(fn, steps, stream):
     import torch
 
@@ -439,6 +521,16 @@ def run_ours(args):
     ach32 = alg32 / (ms32 * 1e-3) / 1e9
     ach64 = alg64 / (ms64k * 1e-3) / 1e9
 
+    # ---- c3: elasticity through the same solvers (block CSR expanded)
+    c3 = None
+    if not args.no_c3:
+        c3 = c3_sample()
+
+    # ---- serving loop: bounded sample of the request stream (both modes)
+    serving_out = None
+    if args.serving_requests > 0:
+        serving_out = serving_sample(args)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(m, kappa, f, P, int(np.median([r.iterations for r in res64])),
@@ -474,6 +566,8 @@ def run_ours(args):
                 "roofline_fp64_operator": {"achieved": ach64, "frac": ach64 / peak,
                                            "alg_bytes_per_launch": alg64, "launch_ms": ms64k,
                                            "traffic": profile_traffic("sell_f64_c2")},
+                "c3_elasticity": c3,
+                "serving": serving_out,
                 "gpu_launches": launches,
                 "clocks": clocks,
                 "cpu_baseline": cpu}

@@ -130,6 +130,7 @@ _SIGS = {
     "dfx_set_diagonal": (C.c_int, [C.POINTER(Csr), _P, C.c_int32, C.c_double, _P]),
     "dfx_spmv": (C.c_int, [C.POINTER(Csr), _P, _P, C.c_double, _P]),
     "dfx_csr_values_to_f32": (C.c_int, [C.POINTER(Csr), _P, _P]),
+    "dfx_csr_expand_blocks": (C.c_int, [C.POINTER(Csr), _P, _P, _P, _P]),
     "dfx_jacobi_inverse_diagonal": (C.c_int, [C.POINTER(Csr), _P, _P]),
     "dfx_inner_product_workspace_bytes": (C.c_size_t, [C.c_int64]),
     "dfx_inner_product": (C.c_int, [_P, _P, C.c_int64, _P, C.c_size_t, C.POINTER(C.c_double), _P]),

@@ -829,8 +829,19 @@ void enqueue_init(const T* rhs, const T* Ax, T* x, const T* dinv, int64_t n, con
 // Graphs of K iterations, cached by everything they bake in.
 using GraphKey = std::tuple<int, const void*, const void*, const void*, const void*, const void*,
                             const void*, int64_t, int, int, int>;
-std::mutex g_graph_mutex;
-std::map<GraphKey, cudaGraphExec_t> g_graphs;
+// Per host thread: a solve returns only after its graph launches have
+// finished, so a thread can evict its own graphs safely; a process-wide
+// cache let one thread destroy a graph another thread was launching.
+struct GraphCache
+{
+  std::map<GraphKey, cudaGraphExec_t> graphs;
+  ~GraphCache()
+  {
+    for (auto& kv : graphs)
+      cudaGraphExecDestroy(kv.second);
+  }
+};
+thread_local GraphCache t_graphs;
 
 template <typename T>
 int iteration_graph(const OpRef& o, T* x, const T* dinv, int64_t n, const Work<T>& w, int K,
@@ -847,7 +858,7 @@ int iteration_graph(const OpRef& o, T* x, const T* dinv, int64_t n, const Work<T
                K,
                w.blocks,
                o.kind == kCsr ? o.A->bs : 1};
-  std::lock_guard<std::mutex> lk(g_graph_mutex);
+  auto& g_graphs = t_graphs.graphs;
   auto it = g_graphs.find(key);
   if (it != g_graphs.end())
   {
@@ -1181,8 +1192,15 @@ extern "C" int dfx_ir_solve(dfx_operator op64, dfx_operator op32, const double* 
       return read_state(w.st, &h, s);
     };
     kernels += 1;
+    // Stagnation: when the FP32 operator's rounding (about 6e-8 |A| per
+    // entry) exceeds the smallest eigenvalue, replacements stop reducing the
+    // FP64 residual; stop after kStall replacements without a 2x gain.
+    constexpr int kStall = 4;
+    double best = 0.0;
+    int stall = 0;
     if (!(st = replace()) && !h->done)
     {
+      best = h->rr;
       for (;;)
       {
         enqueue_pupdate<float>(dinv32, n, w, s);
@@ -1198,6 +1216,16 @@ extern "C" int dfx_ir_solve(dfx_operator op64, dfx_operator op32, const double* 
           break; // not converged within max_inner, or breakdown
         if ((st = replace()) || h->done)
           break;
+        if (h->rr < 0.25 * best)
+        {
+          best = h->rr;
+          stall = 0;
+        }
+        else if (++stall >= kStall)
+        {
+          h->status = DFX_ERR_NOT_CONVERGED;
+          break;
+        }
         if (h->updates > max_outer)
         {
           st = dfx::fail(DFX_ERR_NOT_CONVERGED,

@@ -217,3 +217,73 @@ extern "C" int dfx_inner_product(const double* d_a, const double* d_b, int64_t n
   DFX_CUDA(cudaStreamSynchronize(s));
   return DFX_OK;
 }
+
+namespace
+{
+// Scalar row 3 I + k0 of a 3x3-block CSR: row_ptr = 9 rp[I] + 3 k0 len(I).
+__global__ void k_expand_rowptr(const int64_t* __restrict__ rp, int32_t nrows, int bs,
+                                int64_t* __restrict__ out)
+{
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nr = (int64_t)nrows * bs;
+  if (t > nr)
+    return;
+  if (t == nr)
+  {
+    out[t] = (int64_t)bs * bs * rp[nrows];
+    return;
+  }
+  const int64_t I = t / bs, k0 = t % bs;
+  const int64_t len = rp[I + 1] - rp[I];
+  out[t] = (int64_t)bs * bs * rp[I] + (int64_t)bs * k0 * len;
+}
+
+// One thread per scalar entry of the expanded matrix, in block order.
+__global__ void k_expand_entries(const int64_t* __restrict__ rp, const int32_t* __restrict__ cols,
+                                 const double* __restrict__ vals, int32_t nrows, int bs,
+                                 const int64_t* __restrict__ orp, int32_t* __restrict__ ocols,
+                                 double* __restrict__ ovals, int64_t nnz)
+{
+  const int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= nnz * bs * bs)
+    return;
+  const int64_t j = e / (bs * bs);
+  const int r = (int)(e % (bs * bs)), k0 = r / bs, k1 = r % bs;
+  // block row of entry j: binary search in rp
+  int32_t lo = 0, hi = nrows;
+  while (hi - lo > 1)
+  {
+    const int32_t m = (lo + hi) >> 1;
+    if (rp[m] <= j)
+      lo = m;
+    else
+      hi = m;
+  }
+  const int64_t I = lo;
+  const int64_t pos = orp[bs * I + k0] + (int64_t)bs * (j - rp[I]) + k1;
+  if (ocols)
+    ocols[pos] = bs * cols[j] + k1;
+  ovals[pos] = vals[e];
+}
+} // namespace
+
+extern "C" int dfx_csr_expand_blocks(const dfx_csr* A, int64_t* d_row_ptr, int32_t* d_cols,
+                                     double* d_vals, void* stream)
+{
+  if (int st = dfx::check_csr(A))
+    return st;
+  DFX_REQUIRE(A->dtype == DFX_F64, "values must be FP64");
+  DFX_REQUIRE(d_row_ptr && d_vals, "row_ptr and vals must be non-NULL");
+  const int bs = A->bs;
+  const int64_t nr = (int64_t)A->nrows * bs;
+  DFX_REQUIRE(nr < INT32_MAX && (int64_t)A->ncols * bs < INT32_MAX, "matrix too large");
+  cudaStream_t s = dfx::as_stream(stream);
+  k_expand_rowptr<<<(unsigned)((nr + 256) / 256), 256, 0, s>>>(A->row_ptr, A->nrows, bs, d_row_ptr);
+  const int64_t ne = A->nnz * bs * bs;
+  if (ne > 0)
+    k_expand_entries<<<(unsigned)((ne + 255) / 256), 256, 0, s>>>(
+        A->row_ptr, A->cols, (const double*)A->vals, A->nrows, bs, d_row_ptr, d_cols,
+        (double*)d_vals, A->nnz);
+  DFX_CHECK_LAUNCH();
+  return DFX_OK;
+}

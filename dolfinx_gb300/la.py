@@ -75,6 +75,21 @@ class MatrixCSR:
         _capi.check(_capi.lib().dfx_csr_values_to_f32(C.byref(self.csr()), _ptr(v32), _stream()))
         return MatrixCSR(self.row_ptr, self.cols, v32, self.bs, self.ncols)
 
+    def expand_blocks(self, out: "MatrixCSR | None" = None) -> "MatrixCSR":
+        """Scalar CSR of a block matrix (out: refresh its values only)."""
+        assert self.vals.dtype == torch.float64
+        if out is None:
+            dev = self.vals.device
+            rp = torch.empty(self.nrows * self.bs + 1, dtype=torch.int64, device=dev)
+            cols = torch.empty(self.nnz * self.bs * self.bs, dtype=torch.int32, device=dev)
+            vals = torch.empty(self.nnz * self.bs * self.bs, dtype=torch.float64, device=dev)
+            _capi.check(_capi.lib().dfx_csr_expand_blocks(C.byref(self.csr()), _ptr(rp),
+                                                          _ptr(cols), _ptr(vals), _stream()))
+            return MatrixCSR(rp, cols, vals, 1, self.ncols * self.bs)
+        _capi.check(_capi.lib().dfx_csr_expand_blocks(C.byref(self.csr()), _ptr(out.row_ptr),
+                                                      None, _ptr(out.vals), _stream()))
+        return out
+
     def inverse_diagonal(self) -> torch.Tensor:
         d = torch.empty(self.nrows * self.bs, dtype=torch.float64, device=self.vals.device)
         _capi.check(_capi.lib().dfx_jacobi_inverse_diagonal(C.byref(self.csr()), _ptr(d),

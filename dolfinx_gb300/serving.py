@@ -257,33 +257,42 @@ class Server:
             job = self.large_q.get()
             if job is None:
                 return
-            n = job.st.ndofs
-            with torch.cuda.stream(stream):
-                if self.mode == "mixed":
-                    wb = int(_capi.lib().dfx_ir_workspace_bytes(n))
-                    work = torch.empty(wb, dtype=torch.uint8, device="cuda")
-                    info = _capi.IrInfo()
-                    x = torch.zeros_like(job.b)
-                    _capi.check(_capi.lib().dfx_ir_solve(
-                        job.op64.handle, job.op32.handle, la._ptr(job.b), la._ptr(x),
-                        la._ptr(job.dinv), self.rtol, self.delta, 200, 100000, 20,
-                        _capi.IR_RELIABLE, la._ptr(work), wb, C.byref(info), _stream_ptr(stream)))
-                    job.iterations = info.inner_iterations
-                else:
-                    wb = int(_capi.lib().dfx_cg_op_workspace_bytes(n))
-                    work = torch.empty(wb, dtype=torch.uint8, device="cuda")
-                    info = _capi.CgInfo()
-                    x = torch.zeros_like(job.b)
-                    _capi.check(_capi.lib().dfx_cg_solve_op(
-                        job.op64.handle, la._ptr(job.b), la._ptr(x), la._ptr(job.dinv),
-                        self.rtol, 100000, 20, la._ptr(work), wb, C.byref(info),
-                        _stream_ptr(stream)))
-                    job.iterations = info.iterations
-                job.x = x.cpu()
-                stream.synchronize()
-            job.t_done = time.perf_counter()
-            job.status = info.status
-            self._release(job)
+            try:
+                self._solve_large(job, stream)
+            except Exception as exc:  # a failed request must still leave the loop
+                job.t_done = time.perf_counter()
+                job.status = getattr(exc, "code", -1)
+                job.error = str(exc)
+                self._release(job)
+
+    def _solve_large(self, job, stream):
+        n = job.st.ndofs
+        with torch.cuda.stream(stream):
+            if self.mode == "mixed":
+                wb = int(_capi.lib().dfx_ir_workspace_bytes(n))
+                work = torch.empty(wb, dtype=torch.uint8, device="cuda")
+                info = _capi.IrInfo()
+                x = torch.zeros_like(job.b)
+                _capi.check(_capi.lib().dfx_ir_solve(
+                    job.op64.handle, job.op32.handle, la._ptr(job.b), la._ptr(x),
+                    la._ptr(job.dinv), self.rtol, self.delta, 200, 100000, 20,
+                    _capi.IR_RELIABLE, la._ptr(work), wb, C.byref(info), _stream_ptr(stream)))
+                job.iterations = info.inner_iterations
+            else:
+                wb = int(_capi.lib().dfx_cg_op_workspace_bytes(n))
+                work = torch.empty(wb, dtype=torch.uint8, device="cuda")
+                info = _capi.CgInfo()
+                x = torch.zeros_like(job.b)
+                _capi.check(_capi.lib().dfx_cg_solve_op(
+                    job.op64.handle, la._ptr(job.b), la._ptr(x), la._ptr(job.dinv),
+                    self.rtol, 100000, 20, la._ptr(work), wb, C.byref(info),
+                    _stream_ptr(stream)))
+                job.iterations = info.iterations
+            job.x = x.cpu()
+            stream.synchronize()
+        job.t_done = time.perf_counter()
+        job.status = info.status
+        self._release(job)
 
     def step(self) -> int:
         """One batched launch; retires finished systems. Returns #active."""
@@ -310,8 +319,9 @@ class Server:
                 self._release(job)
         return len(self.active)
 
-    def run(self, requests: list[Request]) -> dict:
-        """Serve a timed stream (arrival times relative to the start)."""
+    def run(self, requests: list[Request], max_wall_s: float = 600.0) -> dict:
+        """Serve a timed stream (arrival times relative to the start). Stops
+        with an error after max_wall_s seconds."""
         pending = collections.deque(sorted(requests, key=lambda r: r.arrival))
         total = len(pending)
         self.finished = []
@@ -320,6 +330,9 @@ class Server:
         arrivals = {}
         while len(self.finished) < total:
             now = time.perf_counter() - t0
+            if now > max_wall_s:
+                raise RuntimeError(f"serving stream not finished after {max_wall_s} s "
+                                   f"({len(self.finished)} of {total} done)")
             while pending and pending[0].arrival <= now:
                 r = pending.popleft()
                 waiting.append(r)
@@ -355,11 +368,11 @@ class Server:
         self.batch = None
 
 
-def serve(requests, mode="mixed", **kw) -> tuple[dict, list[Job]]:
+def serve(requests, mode="mixed", max_wall_s: float = 600.0, **kw) -> tuple[dict, list[Job]]:
     srv = Server(mode=mode, **kw)
     try:
         srv.prewarm(requests)
-        stats = srv.run(requests)
+        stats = srv.run(requests, max_wall_s=max_wall_s)
         return stats, list(srv.finished)
     finally:
         srv.close()

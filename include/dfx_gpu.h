@@ -198,6 +198,15 @@ int dfx_spmv(const dfx_csr* A, const void* d_x, void* d_y, double beta,
 /* Cast of MatrixCSR values to float (la/MatrixCSR.h:223-237). */
 int dfx_csr_values_to_f32(const dfx_csr* A, float* d_vals32, void* stream);
 
+/* The scalar CSR of a bs x bs block CSR: row bs*I + k0 holds the entries
+ * (bs*J + k1) of every block J of block row I, in ascending column order
+ * (la/MatrixCSR.h:56-66 block layout). row_ptr: nrows*bs + 1 entries;
+ * cols, vals: nnz*bs*bs. d_cols == NULL refreshes the values only. Lets
+ * the scalar solvers (sliced-ELL operators, refinement) take vector-valued
+ * problems such as elasticity. */
+int dfx_csr_expand_blocks(const dfx_csr* A, int64_t* d_row_ptr, int32_t* d_cols,
+                          double* d_vals, void* stream);
+
 /* d_dinv[i] = 1 / A_ii (Jacobi), scalar rows of a bs-blocked matrix. */
 int dfx_jacobi_inverse_diagonal(const dfx_csr* A, double* d_dinv, void* stream);
 

@@ -214,3 +214,27 @@ def test_iterative_refinement_reaches_fp64(cuda, oracle, capi, variant, inner_rt
     assert np.linalg.norm(res) / np.linalg.norm(bh) < 1e-12 * 1.0001
     rel = (x - x64).norm().item() / x64.norm().item()
     assert rel < 1e-10, rel
+
+
+def test_block_expansion_and_elasticity_refinement(cuda, oracle, capi):
+    """bs-3 CSR -> scalar CSR: same product; FP64 PCG and mixed refinement
+    on the expanded elasticity system meet the FP64 stopping test."""
+    from dolfinx_gb300 import fem, la
+
+    m, V, E, f, rp, cols = problem(oracle, (6, 3, 3), 2, bs=3, seed=13)
+    X = V.tabulate_dof_coordinates()
+    clamp = np.flatnonzero(np.isclose(X[:, 0], 0)).astype(np.int32)
+    bc = fem.dirichletbc(np.zeros(3), clamp, V)
+    a = fem.elasticity_form(V, 1e3 * E, 0.3)
+    A = fem.assemble_matrix(a, bcs=[bc])
+    b = fem.RhsAssembler(fem.body_force_form(V, (0, 0, -1)), a, [bc]).assemble()
+    S = A.expand_blocks()
+    x = torch.from_numpy(np.random.default_rng(0).standard_normal(V.num_dofs)).cuda()
+    assert_close(S.matvec(x).cpu().numpy(), A.matvec(x).cpu().numpy(), rtol=1e-14)
+    vals = A.vals.cpu().numpy()
+    for solver in (la.OperatorCGSolver(S), la.IRSolver(S)):
+        xs = torch.zeros_like(b)
+        solver.solve(b, xs, rtol=1e-10)
+        bh = b.cpu().numpy()
+        r = bh - oracle.spmv(rp, cols, vals, xs.cpu().numpy(), bs=3)
+        assert np.linalg.norm(r) / np.linalg.norm(bh) < 1e-10 * 1.001

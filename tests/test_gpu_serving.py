@@ -83,3 +83,18 @@ def test_admission_respects_the_hbm_budget(cuda, capi):
         assert srv.admit(serving.Request(1, 6, 1, 0.0, 1)) is not None
     finally:
         srv.close()
+
+
+def test_concurrent_whole_gpu_workers(cuda, oracle, capi):
+    """Several large requests on two worker threads at once (each thread
+    captures and replays its own CG graphs)."""
+    from dolfinx_gb300 import serving
+
+    reqs = [serving.Request(i, 9 + i % 3, 1 + i % 2, 0.5 * i, 40 + i, 0.0) for i in range(6)]
+    for mode in ("mixed", "fp64"):
+        stats, jobs = serving.serve(reqs, mode=mode, hbm_budget=8e9, batch_max_dofs=100,
+                                    workers=2)
+        assert stats["failed"] == []
+        assert all(j.slot is None for j in jobs)
+        for job in jobs:
+            assert _residual(oracle, job) < 1e-10 * 1.001
