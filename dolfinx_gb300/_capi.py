@@ -111,6 +111,16 @@ class BatchSystem(C.Structure):
     ]
 
 
+class Q4Mesh(C.Structure):
+    _fields_ = [
+        ("nx", C.c_int32),
+        ("ny", C.c_int32),
+        ("nz", C.c_int32),
+        ("verts", C.c_void_p),
+        ("kappa", C.c_double),
+    ]
+
+
 _P = C.c_void_p
 _SIGS = {
     "dfx_last_error": (C.c_char_p, []),
@@ -160,6 +170,11 @@ _SIGS = {
     "dfx_cg_op_workspace_bytes": (C.c_size_t, [C.c_int64]),
     "dfx_cg_solve_op": (C.c_int, [_P, _P, _P, _P, C.c_double, C.c_int32, C.c_int32, _P,
                                   C.c_size_t, C.POINTER(CgInfo), _P]),
+    "dfx_q4_num_dofs": (C.c_int64, [C.POINTER(Q4Mesh)]),
+    "dfx_q4_action": (C.c_int, [C.POINTER(Q4Mesh), C.c_int32, _P, _P, _P]),
+    "dfx_q4_cg_workspace_bytes": (C.c_size_t, [C.c_int64, C.c_int32]),
+    "dfx_q4_cg_solve": (C.c_int, [C.POINTER(Q4Mesh), _P, _P, C.c_double, C.c_int32, C.c_int32,
+                                  C.c_double, C.c_int32, _P, C.c_size_t, C.POINTER(CgInfo), _P]),
     "dfx_ir_workspace_bytes": (C.c_size_t, [C.c_int64]),
     "dfx_ir_solve": (C.c_int, [_P, _P, _P, _P, _P, C.c_double, C.c_double, C.c_int32, C.c_int32,
                                C.c_int32, C.c_int32, _P, C.c_size_t, C.POINTER(IrInfo), _P]),

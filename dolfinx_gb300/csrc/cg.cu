@@ -18,6 +18,7 @@
 // 16-bit-column operator. Its dot products sum FP32 products per thread
 // (a thread owns ~16 entries) and reduce the per-thread sums in FP64.
 #include "la_kernels.cuh"
+#include "q4.cuh"
 #include "sell.cuh"
 
 #include <map>
@@ -44,9 +45,17 @@ struct CgState
   int32_t done;
   int32_t status;
   int32_t updates; // reliable updates performed
-  int32_t pad;
+  int32_t since;   // iterations since the last reliable update
+  int32_t forced;  // reliable updates: replace at least every `forced` iterations (0: never)
   unsigned int ticket[4];
 };
+
+// Reliable updates with an assembled FP64 operator: a residual replacement
+// at least this often, so that a stalled FP32 recurrence is caught by the
+// stagnation test. A matrix-free FP64 action costs far more than an FP32
+// iteration, so the Q4 solve replaces less often.
+constexpr int32_t kForcedUpdate = 200;
+constexpr int32_t kForcedUpdateQ4 = 1000;
 
 // Internal pause codes of the reliable-update solve (never returned).
 constexpr int32_t kPauseUpdate = 100;    // residual dropped by delta: replace it
@@ -519,12 +528,15 @@ __global__ void __launch_bounds__(kElemThreads)
         st->status = DFX_ERR_NOT_CONVERGED;
         st->done = 1;
       }
-      else if (RELIABLE && srr < st->delta2 * st->rmax2)
+      else if (RELIABLE
+               && (srr < st->delta2 * st->rmax2 || (st->forced > 0 && st->since + 1 >= st->forced)))
       {
         st->status = kPauseUpdate;
         st->done = 1;
         pause = true;
       }
+      if (RELIABLE)
+        st->since = pause ? 0 : st->since + 1;
       // A pause keeps rz = r_old.z_old: beta is formed after the residual
       // has been replaced.
       if (!pause)
@@ -639,6 +651,44 @@ __global__ void k_ir_correct(double* __restrict__ x, float* __restrict__ d, int6
   }
 }
 
+// Last warp of a residual replacement: the replaced |r|^2 and r.z decide
+// whether the solve has converged, and give beta.
+__device__ __forceinline__ void rel_finish(const WarpFinal& f, CgState* st)
+{
+  if (f.last)
+  {
+    const double srr = f.s0, srz = f.s1;
+    if ((threadIdx.x & 31) == 0)
+    {
+      const bool first = st->iter == 0 && st->updates == 0;
+      if (first)
+        st->rr0 = srr;
+      st->rr = srr;
+      st->rmax2 = srr;
+      st->updates += first ? 0 : 1;
+      if (srr == 0.0 || srr / st->rr0 < st->rtol2)
+      {
+        st->status = DFX_OK;
+        st->done = 1;
+      }
+      else if (!isfinite(srr))
+      {
+        st->status = DFX_ERR_BREAKDOWN;
+        st->done = 1;
+      }
+      else
+      {
+        st->beta = first ? 0.0 : srz / st->rz;
+        st->rz = srz;
+        st->status = DFX_OK;
+        st->done = 0;
+      }
+      st->ticket[3] = 0;
+      __threadfence();
+    }
+  }
+}
+
 // Reliable update (residual replacement): r = b - A x in FP64 with the FP64
 // operator; the FP32 iterated residual is replaced by it, |r|^2 and r.z are
 // formed in FP64, and beta = (r.z)_new / (r.z)_old keeps the search
@@ -669,40 +719,59 @@ __global__ void __launch_bounds__(kSellThreads)
       rz += (double)r32 * z;
     }
   }
-  const WarpFinal f = publish<double>(rr, rz, w.red, &w.st->ticket[3], true);
-  if (f.last)
+  rel_finish(publish<double>(rr, rz, w.red, &w.st->ticket[3], true), w.st);
+}
+
+// Residual replacement of the matrix-free solve: r = b - ax with ax = A x
+// from the FP64 action, otherwise as k_rel_residual.
+template <bool PRE>
+__global__ void __launch_bounds__(kElemThreads)
+    k_rel_residual_vec(const double* __restrict__ b, const double* __restrict__ ax,
+                       const float* __restrict__ dinv32, int64_t n, Work<float> w)
+{
+  block_reduce_init();
+
+  double rr = 0.0, rz = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
   {
-    const double srr = f.s0, srz = f.s1;
-    if ((threadIdx.x & 31) == 0)
-    {
-      CgState* st = w.st;
-      const bool first = st->iter == 0 && st->updates == 0;
-      if (first)
-        st->rr0 = srr;
-      st->rr = srr;
-      st->rmax2 = srr;
-      st->updates += first ? 0 : 1;
-      if (srr == 0.0 || srr / st->rr0 < st->rtol2)
-      {
-        st->status = DFX_OK;
-        st->done = 1;
-      }
-      else if (!isfinite(srr))
-      {
-        st->status = DFX_ERR_BREAKDOWN;
-        st->done = 1;
-      }
-      else
-      {
-        st->beta = first ? 0.0 : srz / st->rz;
-        st->rz = srz;
-        st->status = DFX_OK;
-        st->done = 0;
-      }
-      st->ticket[3] = 0;
-      __threadfence();
-    }
+    const double r = b[i] - ax[i];
+    const float r32 = (float)r;
+    w.r[i] = r32;
+    rr += r * r;
+    const double z = PRE ? (double)(dinv32[i] * r32) : (double)r32;
+    rz += (double)r32 * z;
   }
+  rel_finish(publish<double>(rr, rz, w.red, &w.st->ticket[3], true), w.st);
+}
+
+// p.y and alpha, for an operator applied by a separate kernel (matrix-free).
+template <typename T>
+__global__ void __launch_bounds__(kElemThreads) k_dot_pap(int64_t n, Work<T> w)
+{
+  block_reduce_init();
+
+  if (is_done(w.st))
+    return;
+  constexpr int E = kElemPerThread;
+  const int64_t stride = (int64_t)gridDim.x * kElemThreads * E;
+  T dot = 0;
+  for (int64_t base = (int64_t)blockIdx.x * kElemThreads * E + threadIdx.x; base < n;
+       base += stride)
+  {
+    T p[E], y[E];
+#pragma unroll
+    for (int e = 0; e < E; ++e)
+    {
+      const int64_t i = base + (int64_t)e * kElemThreads;
+      p[e] = i < n ? w.p[i] : T(0);
+      y[e] = i < n ? w.y[i] : T(0);
+    }
+#pragma unroll
+    for (int e = 0; e < E; ++e)
+      dot += p[e] * y[e];
+  }
+  finish_pap(publish<T>(dot, T(0), w.red, &w.st->ticket[1], false), w.st);
 }
 
 template <typename TI, typename TO>
@@ -726,7 +795,8 @@ __global__ void k_scatter(const double* __restrict__ in, double* __restrict__ ou
 enum OpKind
 {
   kCsr = 0,
-  kSell = 1
+  kSell = 1,
+  kQ4 = 2
 };
 
 struct OpRef
@@ -734,6 +804,7 @@ struct OpRef
   OpKind kind;
   const dfx_csr* A;          // kCsr
   const dfx_operator_s* op;  // kSell
+  const dfx_q4_mesh* q4;     // kQ4 (matrix-free action)
 };
 
 template <typename T>
@@ -795,7 +866,14 @@ template <typename T>
 void enqueue_iteration(const OpRef& o, T* x, const T* dinv, int64_t n, const Work<T>& w,
                        bool reliable, cudaStream_t s)
 {
-  enqueue_spmv_dot<T>(o, w, s);
+  if (o.kind == kQ4)
+  {
+    // The colour kernels return at once when the state is done.
+    dfx::q4_apply<T>(*o.q4, w.p, w.y, s, &w.st->done);
+    k_dot_pap<T><<<elem_grid(n), kElemThreads, 0, s>>>(n, w);
+  }
+  else
+    enqueue_spmv_dot<T>(o, w, s);
   const int g = elem_grid(n);
   if (dinv)
   {
@@ -828,7 +906,7 @@ void enqueue_init(const T* rhs, const T* Ax, T* x, const T* dinv, int64_t n, con
 
 // Graphs of K iterations, cached by everything they bake in.
 using GraphKey = std::tuple<int, const void*, const void*, const void*, const void*, const void*,
-                            const void*, int64_t, int, int, int>;
+                            const void*, int64_t, int, int, int, int64_t, double>;
 // Per host thread: a solve returns only after its graph launches have
 // finished, so a thread can evict its own graphs safely; a process-wide
 // cache let one thread destroy a graph another thread was launching.
@@ -847,17 +925,21 @@ template <typename T>
 int iteration_graph(const OpRef& o, T* x, const T* dinv, int64_t n, const Work<T>& w, int K,
                     bool reliable, cudaGraphExec_t* out)
 {
+  const bool q4 = o.kind == kQ4;
   GraphKey key{(int)o.kind * 4 + (sizeof(T) == 4) * 2 + (reliable ? 1 : 0),
-               o.kind == kSell ? (const void*)o.op : (const void*)o.A->row_ptr,
-               o.kind == kSell ? (const void*)o.op->vals : (const void*)o.A->vals,
-               o.kind == kSell ? nullptr : (const void*)o.A->cols,
+               q4 ? (const void*)o.q4->verts
+                  : (o.kind == kSell ? (const void*)o.op : (const void*)o.A->row_ptr),
+               q4 ? nullptr : (o.kind == kSell ? (const void*)o.op->vals : (const void*)o.A->vals),
+               o.kind == kCsr ? (const void*)o.A->cols : nullptr,
                (const void*)x,
                (const void*)dinv,
                (const void*)w.st,
                n,
                K,
                w.blocks,
-               o.kind == kCsr ? o.A->bs : 1};
+               o.kind == kCsr ? o.A->bs : 1,
+               q4 ? (int64_t)o.q4->nx | ((int64_t)o.q4->ny << 21) | ((int64_t)o.q4->nz << 42) : 0,
+               q4 ? o.q4->kappa : 0.0};
   auto& g_graphs = t_graphs.graphs;
   auto it = g_graphs.find(key);
   if (it != g_graphs.end())
@@ -873,6 +955,8 @@ int iteration_graph(const OpRef& o, T* x, const T* dinv, int64_t n, const Work<T
   {
     for (int k = 0; k < K; ++k)
       enqueue_iteration<T>(o, x, dinv, n, w, reliable, cs);
+    // A launch error inside capture invalidates the capture; EndCapture
+    // reports it.
     ce = cudaStreamEndCapture(cs, &graph);
   }
   cudaStreamDestroy(cs);
@@ -916,7 +1000,7 @@ int read_state(const CgState* d, CgState** h, cudaStream_t s)
 // iterations and the state is done at max_iter at the latest, so the loop
 // bound only guards against a corrupted state.
 int run_to_done(cudaGraphExec_t exec, const CgState* dst, int max_iters, int K, CgState** h,
-                cudaStream_t s, int64_t* kernels)
+                cudaStream_t s, int64_t* kernels, int per_iter = 3)
 {
   const int64_t max_launches = (int64_t)max_iters / K + 2;
   for (int64_t launch = 0;; ++launch)
@@ -928,7 +1012,7 @@ int run_to_done(cudaGraphExec_t exec, const CgState* dst, int max_iters, int K, 
     if (launch > max_launches)
       return dfx::fail(DFX_ERR_TIMEOUT, "CG state never reported completion");
     DFX_CUDA(cudaGraphLaunch(exec, s));
-    *kernels += 3 * (int64_t)K;
+    *kernels += per_iter * (int64_t)K;
   }
 }
 
@@ -1081,12 +1165,13 @@ extern "C" int dfx_cg_solve_op(dfx_operator op, const double* d_b, double* d_x,
 
 extern "C" size_t dfx_ir_workspace_bytes(int64_t n) { return ir_work_bytes(n); }
 
-__global__ void k_state_init(CgState* st, double rtol2, double delta2, int max_iter)
+__global__ void k_state_init(CgState* st, double rtol2, double delta2, int max_iter, int forced)
 {
   *st = CgState{};
   st->rtol2 = rtol2;
   st->delta2 = delta2;
   st->max_iter = max_iter;
+  st->forced = forced;
 }
 
 extern "C" int dfx_ir_solve(dfx_operator op64, dfx_operator op32, const double* d_b, double* d_x,
@@ -1178,7 +1263,8 @@ extern "C" int dfx_ir_solve(dfx_operator op64, dfx_operator op32, const double* 
     // is folded into x in FP64 at every replacement.
     if (int e = reset_work(w.st, w.red, w.blocks, s))
       return e;
-    k_state_init<<<1, 1, 0, s>>>(w.st, rtol * rtol, inner_rtol * inner_rtol, max_inner);
+    k_state_init<<<1, 1, 0, s>>>(w.st, rtol * rtol, inner_rtol * inner_rtol, max_inner,
+                                 kForcedUpdate);
     DFX_CUDA(cudaMemsetAsync(d32, 0, sizeof(float) * n, s));
     DFX_CUDA(cudaMemsetAsync(w.p, 0, sizeof(float) * n, s));
     auto replace = [&]() -> int
@@ -1262,6 +1348,144 @@ extern "C" int dfx_ir_solve(dfx_operator op64, dfx_operator op32, const double* 
   if (ho.status == DFX_ERR_BREAKDOWN)
     return dfx::fail(DFX_ERR_BREAKDOWN, "refinement breakdown (non-finite residual or p.Ap <= 0)");
   return DFX_OK;
+}
+
+// ---------------------------------------------------------------------------
+// CG on the matrix-free Q4 action.
+namespace
+{
+// Kernels of one matrix-free iteration: 8 colour kernels, p.Ap, update,
+// p update (the y memset is a graph memset node, not a kernel).
+constexpr int kQ4IterKernels = 11;
+
+size_t q4_work_bytes(int64_t n, int mode)
+{
+  Carver c{nullptr};
+  if (mode == 0)
+    carve_work<double>(c, n);
+  else
+  {
+    carve_work<float>(c, n);
+    c.take<double>(n); // A x in FP64
+    c.take<float>(n);  // FP32 correction d
+  }
+  return c.used;
+}
+} // namespace
+
+extern "C" size_t dfx_q4_cg_workspace_bytes(int64_t n, int32_t mode)
+{
+  return (mode == 0 || mode == 1) ? q4_work_bytes(n, mode) : 0;
+}
+
+extern "C" int dfx_q4_cg_solve(const dfx_q4_mesh* mesh, const double* d_b, double* d_x,
+                               double rtol, int32_t max_iters, int32_t mode, double delta,
+                               int32_t graph_iters, void* d_work, size_t wbytes, dfx_cg_info* info,
+                               void* stream)
+{
+  DFX_REQUIRE(mesh && mesh->nx > 0 && mesh->ny > 0 && mesh->nz > 0 && mesh->verts,
+              "invalid Q4 mesh");
+  if (int st = check_solve_args(d_b, d_x, d_work, rtol, max_iters))
+    return st;
+  DFX_REQUIRE(mode == 0 || mode == 1, "mode must be 0 (FP64) or 1 (mixed), got %d", mode);
+  DFX_REQUIRE(mode == 0 || (delta > 0.0 && delta < 1.0), "delta must be in (0, 1)");
+  const int64_t n = dfx::q4_ndofs(*mesh);
+  DFX_REQUIRE(wbytes >= q4_work_bytes(n, mode), "workspace too small (%zu < %zu)", wbytes,
+              q4_work_bytes(n, mode));
+  if (info)
+    *info = dfx_cg_info{};
+  if (int st = dfx::q4_prepare())
+    return st;
+  cudaStream_t s = dfx::as_stream(stream);
+  const int K = graph_iters > 0 ? graph_iters : 20;
+  const OpRef o{kQ4, nullptr, nullptr, mesh};
+  Carver c{(char*)d_work};
+  CgState* h = nullptr;
+  int64_t kernels = 0;
+  if (mode == 0)
+  {
+    Work<double> w = carve_work<double>(c, n);
+    if (int st = reset_work(w.st, w.red, w.blocks, s))
+      return st;
+    if (int st = dfx::q4_apply<double>(*mesh, d_x, w.y, s))
+      return st;
+    enqueue_init<double>(d_b, w.y, d_x, nullptr, n, w, rtol, max_iters, s);
+    DFX_CHECK_LAUNCH();
+    cudaGraphExec_t exec;
+    if (int st = iteration_graph<double>(o, d_x, nullptr, n, w, K, false, &exec))
+      return st;
+    kernels = 9;
+    if (int st = run_to_done(exec, w.st, max_iters, K, &h, s, &kernels, kQ4IterKernels))
+      return st;
+    return report(h, info, kernels);
+  }
+  // Mixed: FP32 CG on the FP32 action, its residual replaced by b - A x from
+  // the FP64 action whenever |r| has dropped by delta (reliable updates); the
+  // FP32 correction is folded into x in FP64 at each replacement.
+  Work<float> w = carve_work<float>(c, n);
+  double* ax = c.take<double>(n);
+  float* d32 = c.take<float>(n);
+  if (int st = reset_work(w.st, w.red, w.blocks, s))
+    return st;
+  k_state_init<<<1, 1, 0, s>>>(w.st, rtol * rtol, delta * delta, max_iters, kForcedUpdateQ4);
+  DFX_CUDA(cudaMemsetAsync(d32, 0, sizeof(float) * n, s));
+  DFX_CUDA(cudaMemsetAsync(w.p, 0, sizeof(float) * n, s));
+  DFX_CHECK_LAUNCH();
+  cudaGraphExec_t exec;
+  if (int st = iteration_graph<float>(o, d32, nullptr, n, w, K, true, &exec))
+    return st;
+  kernels = 1;
+  auto replace = [&]() -> int
+  {
+    if (int st = dfx::q4_apply<double>(*mesh, d_x, ax, s))
+      return st;
+    k_rel_residual_vec<false><<<elem_grid(n), kElemThreads, 0, s>>>(d_b, ax, nullptr, n, w);
+    DFX_CHECK_LAUNCH();
+    kernels += 9;
+    return read_state(w.st, &h, s);
+  };
+  constexpr int kStall = 4;
+  const int max_updates = max_iters / 10 + 100;
+  int st = replace();
+  if (!st && !h->done)
+  {
+    double best = h->rr;
+    int stall = 0;
+    for (;;)
+    {
+      enqueue_pupdate<float>(nullptr, n, w, s);
+      DFX_CHECK_LAUNCH();
+      kernels += 1;
+      if ((st = run_to_done(exec, w.st, max_iters, K, &h, s, &kernels, kQ4IterKernels)))
+        break;
+      const int32_t why = h->status;
+      k_ir_correct<<<stride_grid(), kThreads, 0, s>>>(d_x, d32, n);
+      DFX_CHECK_LAUNCH();
+      kernels += 1;
+      if (why != kPauseUpdate && why != kPauseConverged)
+        break; // iteration cap or breakdown
+      if ((st = replace()) || h->done)
+        break;
+      if (h->rr < 0.25 * best)
+      {
+        best = h->rr;
+        stall = 0;
+      }
+      else if (++stall >= kStall)
+      {
+        h->status = DFX_ERR_NOT_CONVERGED;
+        break;
+      }
+      if (h->updates > max_updates)
+      {
+        h->status = DFX_ERR_NOT_CONVERGED;
+        break;
+      }
+    }
+  }
+  if (st)
+    return st;
+  return report(h, info, kernels);
 }
 
 // ---------------------------------------------------------------------------

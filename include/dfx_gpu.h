@@ -374,6 +374,37 @@ int dfx_batch_step(dfx_batch b, int32_t iterations, int32_t* num_active, void* s
 int dfx_batch_info(dfx_batch b, int32_t slot, dfx_cg_info* info, int32_t* done,
                    int32_t* replacements);
 
+/* ------------------------------------------------ matrix-free Q4 action
+ * The operator of the matrix-free Poisson demo (cpp/demo/poisson_matrix_free/
+ * main.cpp:201-222; its form M = action(a, u), poisson.py:33-46) for
+ * a(u,v) = \int kappa grad u . grad v on Lagrange Q4 hexahedra, applied by
+ * sum factorisation: a structured nx x ny x nz hexahedral mesh with
+ * trilinear geometry (vertices lexicographic, x fastest), Gauss-Lobatto-
+ * Legendre nodes, Gauss-Legendre 5^3 quadrature, nodes lexicographic on the
+ * (4nx+1)(4ny+1)(4nz+1) lattice. y = A u on interior nodes (boundary
+ * entries of u read as 0), y = u on boundary nodes: homogeneous Dirichlet
+ * rows set to the identity. */
+typedef struct dfx_q4_mesh
+{
+  int32_t nx, ny, nz;
+  const double* verts;  /* ((nx+1)(ny+1)(nz+1), 3) vertex coordinates */
+  double kappa;
+} dfx_q4_mesh;
+
+int64_t dfx_q4_num_dofs(const dfx_q4_mesh* mesh);
+/* y = A u; u, y of `dtype` (DFX_F64 or DFX_F32; FP32 forms the geometry
+ * and contractions in FP32 from FP64 vertex differences). */
+int dfx_q4_action(const dfx_q4_mesh* mesh, int32_t dtype, const void* d_u, void* d_y,
+                  void* stream);
+/* CG on the Q4 action (the demo's unpreconditioned CG, main.cpp:84-132).
+ * mode 0: FP64 throughout; mode 1: FP32 action and vectors with FP64
+ * reliable updates (FP64 action for the residual, x += d in FP64) when |r|
+ * has dropped by `delta`. Stops at |b - A x|^2/|b - A x0|^2 < rtol^2 in FP64. */
+size_t dfx_q4_cg_workspace_bytes(int64_t n, int32_t mode);
+int dfx_q4_cg_solve(const dfx_q4_mesh* mesh, const double* d_b, double* d_x, double rtol,
+                    int32_t max_iters, int32_t mode, double delta, int32_t graph_iters,
+                    void* d_work, size_t work_bytes, dfx_cg_info* info, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

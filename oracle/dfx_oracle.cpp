@@ -896,3 +896,174 @@ int orc_cg(int nrows, int bs, const int64_t* row_ptr, const int32_t* cols,
 }
 
 } // extern "C"
+
+//---------------------------------------------------------------------------
+// Q4 hexahedral Laplacian action (matrix-free demo action,
+// cpp/demo/poisson_matrix_free/main.cpp:201-222, on the Q4 configuration).
+// Structured n_x x n_y x n_z mesh of the box with vertices `verts`
+// ((nx+1)(ny+1)(nz+1) x 3, lexicographic, x fastest), trilinear geometry,
+// Lagrange Q4 on Gauss-Lobatto-Legendre points (Basix's GLL variant, which
+// on tensor-product cells is the GLL lattice), Gauss-Legendre 5^3
+// quadrature. Global nodes: lexicographic on the (4n+1)^3 lattice.
+// y = A u on interior nodes with boundary entries of u taken as 0, y = u on
+// boundary nodes (homogeneous Dirichlet rows set to the identity). Plain
+// quadrature loops with the full 125 x 125 element matrix (no sum
+// factorisation): an independent check of the GPU kernels.
+//---------------------------------------------------------------------------
+namespace
+{
+void q4_tables(double B[5][5], double D[5][5], double* wq)
+{
+  const double s = std::sqrt(3.0 / 7.0);
+  const double xn[5] = {0.0, 0.5 * (1.0 - s), 0.5, 0.5 * (1.0 + s), 1.0};
+  std::vector<double> g, w;
+  gauss_legendre01(5, g, w);
+  for (int q = 0; q < 5; ++q)
+  {
+    wq[q] = w[q];
+    for (int a = 0; a < 5; ++a)
+    {
+      double l = 1.0, dl = 0.0;
+      for (int m = 0; m < 5; ++m)
+      {
+        if (m == a)
+          continue;
+        l *= (g[q] - xn[m]) / (xn[a] - xn[m]);
+      }
+      for (int k = 0; k < 5; ++k)
+      {
+        if (k == a)
+          continue;
+        double t = 1.0 / (xn[a] - xn[k]);
+        for (int m = 0; m < 5; ++m)
+          if (m != a && m != k)
+            t *= (g[q] - xn[m]) / (xn[a] - xn[m]);
+        dl += t;
+      }
+      B[q][a] = l;
+      D[q][a] = dl;
+    }
+  }
+}
+} // namespace
+
+extern "C" void orc_q4_tables(double* B, double* D, double* w)
+{
+  double b[5][5], d[5][5];
+  q4_tables(b, d, w);
+  std::memcpy(B, b, sizeof(b));
+  std::memcpy(D, d, sizeof(d));
+}
+
+extern "C" int orc_q4_action(int nx, int ny, int nz, const double* verts, double kappa,
+                             const double* u, double* y, int apply_bc)
+{
+  double B[5][5], D[5][5], w[5];
+  q4_tables(B, D, w);
+  std::vector<double> g, gw;
+  gauss_legendre01(5, g, gw);
+  const int64_t NX = 4 * (int64_t)nx + 1, NY = 4 * (int64_t)ny + 1, NZ = 4 * (int64_t)nz + 1;
+  const int64_t ndofs = NX * NY * NZ;
+  auto on_bnd = [&](int64_t I, int64_t J, int64_t K)
+  {
+    return apply_bc
+           && (I == 0 || J == 0 || K == 0 || I == NX - 1 || J == NY - 1 || K == NZ - 1);
+  };
+  std::fill(y, y + ndofs, 0.0);
+  std::vector<double> grad(125 * 125 * 3);
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i)
+      {
+        double xv[8][3];
+        for (int v = 0; v < 8; ++v)
+        {
+          const int64_t vi = i + (v & 1), vj = j + ((v >> 1) & 1), vk = k + ((v >> 2) & 1);
+          const int64_t id = (vk * (ny + 1) + vj) * (nx + 1) + vi;
+          for (int c = 0; c < 3; ++c)
+            xv[v][c] = verts[3 * id + c];
+        }
+        int64_t dof[125];
+        double ue[125];
+        for (int c = 0; c < 5; ++c)
+          for (int b = 0; b < 5; ++b)
+            for (int a = 0; a < 5; ++a)
+            {
+              const int64_t I = 4 * i + a, J = 4 * j + b, K = 4 * k + c;
+              const int e = a + 5 * b + 25 * c;
+              dof[e] = (K * NY + J) * NX + I;
+              ue[e] = on_bnd(I, J, K) ? 0.0 : u[dof[e]];
+            }
+        double ye[125] = {0.0};
+        for (int q3 = 0; q3 < 5; ++q3)
+          for (int q2 = 0; q2 < 5; ++q2)
+            for (int q1 = 0; q1 < 5; ++q1)
+            {
+              const double px = g[q1], py = g[q2], pz = g[q3];
+              double J[3][3];
+              for (int c = 0; c < 3; ++c)
+              {
+                double dX = 0, dY = 0, dZ = 0;
+                for (int v = 0; v < 8; ++v)
+                {
+                  const int bx = v & 1, by = (v >> 1) & 1, bz = (v >> 2) & 1;
+                  const double Nx = bx ? px : 1 - px, Ny = by ? py : 1 - py, Nz = bz ? pz : 1 - pz;
+                  const double sx = bx ? 1.0 : -1.0, sy = by ? 1.0 : -1.0, sz = bz ? 1.0 : -1.0;
+                  dX += xv[v][c] * sx * Ny * Nz;
+                  dY += xv[v][c] * Nx * sy * Nz;
+                  dZ += xv[v][c] * Nx * Ny * sz;
+                }
+                J[c][0] = dX;
+                J[c][1] = dY;
+                J[c][2] = dZ;
+              }
+              double Jt[3][3], K[3][3];
+              for (int a = 0; a < 3; ++a)
+                for (int b = 0; b < 3; ++b)
+                  Jt[a][b] = J[a][b];
+              const double det = Jt[0][0] * (Jt[1][1] * Jt[2][2] - Jt[1][2] * Jt[2][1])
+                                 - Jt[0][1] * (Jt[1][0] * Jt[2][2] - Jt[1][2] * Jt[2][0])
+                                 + Jt[0][2] * (Jt[1][0] * Jt[2][1] - Jt[1][1] * Jt[2][0]);
+              K[0][0] = (Jt[1][1] * Jt[2][2] - Jt[1][2] * Jt[2][1]) / det;
+              K[0][1] = (Jt[0][2] * Jt[2][1] - Jt[0][1] * Jt[2][2]) / det;
+              K[0][2] = (Jt[0][1] * Jt[1][2] - Jt[0][2] * Jt[1][1]) / det;
+              K[1][0] = (Jt[1][2] * Jt[2][0] - Jt[1][0] * Jt[2][2]) / det;
+              K[1][1] = (Jt[0][0] * Jt[2][2] - Jt[0][2] * Jt[2][0]) / det;
+              K[1][2] = (Jt[0][2] * Jt[1][0] - Jt[0][0] * Jt[1][2]) / det;
+              K[2][0] = (Jt[1][0] * Jt[2][1] - Jt[1][1] * Jt[2][0]) / det;
+              K[2][1] = (Jt[0][1] * Jt[2][0] - Jt[0][0] * Jt[2][1]) / det;
+              K[2][2] = (Jt[0][0] * Jt[1][1] - Jt[0][1] * Jt[1][0]) / det;
+              const double wq = w[q1] * w[q2] * w[q3] * std::abs(det) * kappa;
+              // physical gradients of all 125 basis functions at this point
+              double gr[125][3];
+              for (int c = 0; c < 5; ++c)
+                for (int b = 0; b < 5; ++b)
+                  for (int a = 0; a < 5; ++a)
+                  {
+                    const double dref[3] = {D[q1][a] * B[q2][b] * B[q3][c],
+                                            B[q1][a] * D[q2][b] * B[q3][c],
+                                            B[q1][a] * B[q2][b] * D[q3][c]};
+                    const int e = a + 5 * b + 25 * c;
+                    for (int m = 0; m < 3; ++m)
+                      gr[e][m] = K[0][m] * dref[0] + K[1][m] * dref[1] + K[2][m] * dref[2];
+                  }
+              double gu[3] = {0, 0, 0};
+              for (int e = 0; e < 125; ++e)
+                for (int m = 0; m < 3; ++m)
+                  gu[m] += gr[e][m] * ue[e];
+              for (int e = 0; e < 125; ++e)
+                ye[e] += wq * (gr[e][0] * gu[0] + gr[e][1] * gu[1] + gr[e][2] * gu[2]);
+            }
+        for (int e = 0; e < 125; ++e)
+          y[dof[e]] += ye[e];
+      }
+  for (int64_t K = 0; K < NZ; ++K)
+    for (int64_t J = 0; J < NY; ++J)
+      for (int64_t I = 0; I < NX; ++I)
+        if (on_bnd(I, J, K))
+        {
+          const int64_t d = (K * NY + J) * NX + I;
+          y[d] = u[d];
+        }
+  return 0;
+}

@@ -77,6 +77,8 @@ def lib():
         L.orc_set_diagonal.argtypes = [C.c_int, _i64p, _i32p, _f64p, C.c_int, _i32p, C.c_double]
         L.orc_spmv.argtypes = [C.c_int, C.c_int, _i64p, _i32p, _f64p, _f64p, _f64p]
         L.orc_spmv_f32.argtypes = [C.c_int, C.c_int, _i64p, _i32p, _f32p, _f32p, _f32p]
+        L.orc_q4_action.argtypes = [C.c_int] * 3 + [_f64p, C.c_double, _f64p, _f64p, C.c_int]
+        L.orc_q4_tables.argtypes = [_f64p, _f64p, _f64p]
         L.orc_cg.argtypes = [C.c_int, C.c_int, _i64p, _i32p, _f64p, _f64p, _f64p, C.c_void_p,
                              C.c_double, C.c_int]
         _lib = L
@@ -244,3 +246,14 @@ def kernel_elasticity(coords, E=1.0, nu=0.3):
     Ae = np.zeros(900)
     lib().orc_kernel_elasticity(Ae, E, nu, np.ascontiguousarray(coords, np.float64).ravel())
     return Ae.reshape(30, 30)
+
+
+def q4_action(n, verts, u, kappa=1.0, apply_bc=True):
+    """y = A u for the Q4 hex Laplacian on a structured mesh of n^3 cells
+    (n an int) or nx x ny x nz cells (n a tuple); see orc_q4_action."""
+    nx, ny, nz = (n, n, n) if np.isscalar(n) else n
+    u = np.ascontiguousarray(u, np.float64)
+    y = np.zeros_like(u)
+    lib().orc_q4_action(nx, ny, nz, np.ascontiguousarray(verts, np.float64), float(kappa), u, y,
+                        int(apply_bc))
+    return y

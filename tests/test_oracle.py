@@ -138,3 +138,32 @@ def test_pipeline_reproduces_polynomial(oracle, deg):
     uh, it = oracle.cg(rp, cols, A, b, dinv=1.0 / diag, rtol=1e-12)
     assert it > 0
     assert np.abs(uh - u).max() < 1e-9
+
+
+def test_q4_action_exact_on_linears(oracle):
+    """Q4 on perturbed trilinear hexahedra: the space holds the physical
+    linear functions and 5^3 Gauss-Legendre integrates their stiffness rows
+    exactly, so A u vanishes at interior nodes for linear u, A 1 = 0, and
+    u^T A u = kappa |grad u|^2 vol(cube) = kappa."""
+    from dolfinx_gb300 import matrix_free as mf
+
+    dims = (2, 3, 2)
+    v = mf.hex_box_vertices(*dims, perturb=0.05, seed=3)
+    xyz = mf.node_coordinates(v, *dims)
+    bnd = mf.boundary_mask(*dims)
+    n = xyz.shape[0]
+    assert n == 9 * 13 * 9
+    one = np.ones(n)
+    assert np.abs(oracle.q4_action(dims, v, one, apply_bc=False)).max() < 1e-12
+    u = 0.3 + 1.0 * xyz[:, 0] - 2.0 * xyz[:, 1] + 0.5 * xyz[:, 2]
+    y = oracle.q4_action(dims, v, u, kappa=1.7, apply_bc=False)
+    assert np.abs(y[~bnd]).max() < 1e-11
+    x = xyz[:, 0]
+    e = x @ oracle.q4_action(dims, v, x, kappa=1.7, apply_bc=False)
+    assert abs(e - 1.7) < 1e-12
+    # With the boundary rows set to the identity the operator stays symmetric.
+    rng = np.random.default_rng(0)
+    a, b = rng.standard_normal(n), rng.standard_normal(n)
+    a[bnd] = 0.0
+    b[bnd] = 0.0
+    assert abs(a @ oracle.q4_action(dims, v, b) - b @ oracle.q4_action(dims, v, a)) < 1e-11
