@@ -1,13 +1,12 @@
 // Q4 hexahedral Laplacian action by sum factorisation.
 //
-// One CTA per cell, one thread per quadrature point / node of the 5x5x5
-// tensor lattice. The gradient at the 125 quadrature points costs 8
-// one-dimensional contractions (5 FMAs each per thread) instead of the
+// The gradient at the 125 quadrature points of a cell costs 8
+// one-dimensional contractions of 5 terms per point instead of the
 // 125 x 125 x 3 products of the full element matrix; the transpose costs 8
 // more. The Jacobian of the trilinear map is formed at each quadrature
-// point in the kernel's precision from the cell's 8 vertices (differences
-// taken in FP64). Cells are processed in 8 colours (parity of i, j, k):
-// cells of one colour share no node, so the scatter is a plain
+// point in the kernel's precision from the cell's edge vectors (vertex
+// differences taken in FP64). Cells are processed in 8 colours (parity of
+// i, j, k): cells of one colour share no node, so the scatter is a plain
 // read-modify-write, deterministic and free of atomics.
 #include "q4.cuh"
 
@@ -111,69 +110,11 @@ int upload_tables()
   return DFX_OK;
 }
 
-// Per-thread rows of the 1D tables. The forward phases need B(q, a) and
-// D(q, a) for the thread's quadrature index q in each direction; the
-// transpose phases need B(q, a) and D(q, a) for the thread's node index a.
-// FP32: held in registers for the whole kernel (each CTA processes many
-// cells). FP64: read from shared memory (the FP64 pipe bounds that kernel).
-template <typename T, bool REG>
-struct Rows;
+// Cells per CTA batch: 5 cells x 25 lines of 5 nodes = 125 threads.
+constexpr int kBatch = 5;
+constexpr int kLattice = 125;
 
-template <typename T>
-struct Rows<T, true>
-{
-  T f[3][2][5]; // f[d][0][a] = B(t_d, a), f[d][1][a] = D(t_d, a)
-  T c[3][2][5]; // c[d][0][q] = B(q, t_d), c[d][1][q] = D(q, t_d)
-  __device__ void init(const T* sB, const T* sD, const int (&td)[3])
-  {
-#pragma unroll
-    for (int d = 0; d < 3; ++d)
-#pragma unroll
-      for (int a = 0; a < 5; ++a)
-      {
-        f[d][0][a] = sB[5 * td[d] + a];
-        f[d][1][a] = sD[5 * td[d] + a];
-        c[d][0][a] = sB[5 * a + td[d]];
-        c[d][1][a] = sD[5 * a + td[d]];
-      }
-  }
-  __device__ T fB(int d, int a) const { return f[d][0][a]; }
-  __device__ T fD(int d, int a) const { return f[d][1][a]; }
-  __device__ T cB(int d, int q) const { return c[d][0][q]; }
-  __device__ T cD(int d, int q) const { return c[d][1][q]; }
-};
-
-template <typename T>
-struct Rows<T, false>
-{
-  const T* B;
-  const T* D;
-  int td[3];
-  __device__ void init(const T* sB, const T* sD, const int (&t)[3])
-  {
-    B = sB;
-    D = sD;
-    td[0] = t[0];
-    td[1] = t[1];
-    td[2] = t[2];
-  }
-  __device__ T fB(int d, int a) const { return B[5 * td[d] + a]; }
-  __device__ T fD(int d, int a) const { return D[5 * td[d] + a]; }
-  __device__ T cB(int d, int q) const { return B[5 * q + td[d]]; }
-  __device__ T cD(int d, int q) const { return D[5 * q + td[d]]; }
-};
-
-// Edge e of a hexahedron (vertex v = bx + 2 by + 4 bz): e / 4 is its
-// direction, e % 4 its position; returns the lower vertex (the upper is
-// lower + 1, + 2 or + 4).
-__device__ __forceinline__ int edge_lo(int e)
-{
-  const int d = e >> 2, m = e & 3;
-  return d == 0 ? 2 * m : (d == 1 ? (m & 1) + 4 * (m >> 1) : m);
-}
-
-// The 12 edge components of one coordinate, read with 16-byte loads (the
-// same address in every lane: one broadcast per load).
+// The 12 edge components of one coordinate, read with 16-byte loads.
 __device__ __forceinline__ void load_edges(const float* p, float (&e)[12])
 {
   const float4* q = reinterpret_cast<const float4*>(p);
@@ -199,223 +140,322 @@ __device__ __forceinline__ void load_edges(const double* p, double (&e)[12])
   }
 }
 
-// One CTA processes the cells of one colour in turn; thread t < 125 owns
-// quadrature point / node (t1, t2, t3) of the 5^3 lattice.
+// Edge e of a hexahedron (vertex v = bx + 2 by + 4 bz): e / 4 is its
+// direction, e % 4 its position; returns the lower vertex (the upper is
+// lower + 1, + 2 or + 4).
+__device__ __forceinline__ int edge_lo(int e)
+{
+  const int d = e >> 2, m = e & 3;
+  return d == 0 ? 2 * m : (d == 1 ? (m & 1) + 4 * (m >> 1) : m);
+}
+
+// A CTA takes batches of 5 cells of one colour. Thread t < 125 owns cell
+// t / 25 of the batch and line l = t % 25 of its 5^3 lattice; in each
+// phase the line runs along the direction being contracted, so a thread
+// holds 5 values and produces 5, every table entry is a compile-time index
+// (an immediate constant-bank operand of the FMA) and the 125 values of a
+// cell pass between phases through shared memory:
+//   1. x: u on the line (registers, from global)   -> A, Ad   (B, D in x)
+//   2. y: A, Ad                                      -> C, Cy, Cx
+//   3. z: C, Cy, Cx -> grad at 5 points -> G grad -> transpose in z
+//   4. y transpose;  5. x transpose -> y += on the line (global).
+// Lines of phases 1/5 are (y, z) node rows, of 2/4 (x, z), of 3 (x, y).
 template <typename T>
-__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 3 : 2)
+__global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2)
     k_q4_cells(const dfx_q4_mesh_s m, const T* __restrict__ u, T* __restrict__ y, int ci, int cj,
                int ck, const int32_t* __restrict__ skip)
 {
   if (skip && __ldg(skip))
     return;
-  constexpr bool REG = sizeof(T) == 4;
-  __shared__ T su[128], sA[128], sAd[128], sC[128], sCx[128], sCy[128];
-  __shared__ T sB[25], sD[25];
-  __shared__ __align__(16) T se[3][12]; // edge vectors of the cell, by component
-  __shared__ double sv[8][3];
+  using Tb = Tab<T>;
+  __shared__ T S[6][kBatch * kLattice];
+  __shared__ __align__(16) T se[kBatch][3][12]; // edge vectors by cell and component
+  __shared__ double sv[kBatch][24];
   const int t = threadIdx.x;
-  const bool act = t < 125;
-  const int tt = act ? t : 0;
-  const int td[3] = {tt % 5, (tt / 5) % 5, tt / 25};
-  const int t1 = td[0], t2 = td[1], t3 = td[2];
-  if (t < 25)
-  {
-    sB[t] = Tab<T>::B(t / 5, t % 5);
-    sD[t] = Tab<T>::D(t / 5, t % 5);
-  }
-  // Trilinear-map weights of the Jacobian columns at this quadrature point.
-  T wx[4], wy[4], wz[4];
-  {
-    const T X = Tab<T>::G(t1), Y = Tab<T>::G(t2), Z = Tab<T>::G(t3);
-    wx[0] = (1 - Y) * (1 - Z), wx[1] = Y * (1 - Z), wx[2] = (1 - Y) * Z, wx[3] = Y * Z;
-    wy[0] = (1 - X) * (1 - Z), wy[1] = X * (1 - Z), wy[2] = (1 - X) * Z, wy[3] = X * Z;
-    wz[0] = (1 - X) * (1 - Y), wz[1] = X * (1 - Y), wz[2] = (1 - X) * Y, wz[3] = X * Y;
-  }
-  const T qw = Tab<T>::W(t1) * Tab<T>::W(t2) * Tab<T>::W(t3) * (T)m.kappa;
-  __syncthreads();
-  Rows<T, REG> R;
-  R.init(sB, sD, td);
+  const bool act = t < kBatch * kLattice / 5;
+  const int c = act ? t / 25 : 0, l = t % 25;
+  const int la = l % 5, lb = l / 5;
+  T* const S0 = S[0] + c * kLattice;
+  T* const S1 = S[1] + c * kLattice;
+  T* const S2 = S[2] + c * kLattice;
+  T* const S3 = S[3] + c * kLattice;
+  T* const S4 = S[4] + c * kLattice;
+  T* const S5 = S[5] + c * kLattice;
 
   const int hx = (m.nx - ci + 1) / 2, hy = (m.ny - cj + 1) / 2, hz = (m.nz - ck + 1) / 2;
-  const int64_t cells = (int64_t)hx * hy * hz;
-  const int64_t NX = 4 * (int64_t)m.nx + 1, NY = 4 * (int64_t)m.ny + 1, NZ = 4 * (int64_t)m.nz + 1;
-  // This thread's node of cell b, and whether it lies on the boundary.
-  auto node = [&](int64_t b, int64_t& gid, bool& bnd)
+  const int cells = hx * hy * hz; // < 2^31, checked on the host
+  const int batches = (cells + kBatch - 1) / kBatch;
+  const int NX = 4 * m.nx + 1, NY = 4 * m.ny + 1, NZ = 4 * m.nz + 1;
+  // Lattice (y, z) coordinates of this thread's phase-1/5 line in cell
+  // (i, j, k), and the line's first node.
+  struct Line
   {
-    const int64_t i = ci + 2 * (b % hx), j = cj + 2 * ((b / hx) % hy);
-    const int64_t k = ck + 2 * (b / ((int64_t)hx * hy));
-    const int64_t I = 4 * i + t1, J = 4 * j + t2, K = 4 * k + t3;
-    gid = (K * NY + J) * NX + I;
-    bnd = I == 0 || J == 0 || K == 0 || I == NX - 1 || J == NY - 1 || K == NZ - 1;
+    int64_t base;
+    bool row_bnd; // the whole line lies on a y or z boundary face
+    bool x_lo, x_hi;
+    bool valid;
   };
-  // Loads of cell b's inputs (node value; one vertex coordinate for t < 24),
-  // issued one cell ahead so that their latency overlaps a cell's work.
-  auto fetch = [&](int64_t b, T& un, double& vn)
+  auto line_of = [&](int bt) -> Line
   {
-    if (b >= cells)
-      return;
-    if (act)
-    {
-      int64_t g;
-      bool bd;
-      node(b, g, bd);
-      un = u[g];
-    }
-    if (t < 24)
-    {
-      const int64_t i = ci + 2 * (b % hx), j = cj + 2 * ((b / hx) % hy);
-      const int64_t k = ck + 2 * (b / ((int64_t)hx * hy));
-      const int v = t / 3, c = t % 3;
-      const int64_t vi = i + (v & 1), vj = j + ((v >> 1) & 1), vk = k + ((v >> 2) & 1);
-      vn = m.verts[3 * ((vk * (m.ny + 1) + vj) * (m.nx + 1) + vi) + c];
-    }
+    Line L{0, false, false, false, false};
+    const int b = kBatch * bt + c;
+    if (!act || b >= cells)
+      return L;
+    const int i = ci + 2 * (b % hx), j = cj + 2 * ((b / hx) % hy), k = ck + 2 * (b / (hx * hy));
+    const int J = 4 * j + la, K = 4 * k + lb;
+    L.base = ((int64_t)K * NY + J) * NX + 4 * (int64_t)i;
+    L.row_bnd = J == 0 || K == 0 || J == NY - 1 || K == NZ - 1;
+    L.x_lo = i == 0;
+    L.x_hi = i == m.nx - 1;
+    L.valid = true;
+    return L;
   };
-  T un = 0;
+  // One vertex coordinate of the batch (threads t < 120).
+  auto vert_of = [&](int bt) -> double
+  {
+    const int cc = t / 24, r = t % 24, v = r / 3, comp = r % 3;
+    const int b = kBatch * bt + cc;
+    if (t >= kBatch * 24 || b >= cells)
+      return 0.0;
+    const int i = ci + 2 * (b % hx), j = cj + 2 * ((b / hx) % hy), k = ck + 2 * (b / (hx * hy));
+    const int64_t vi = i + (v & 1), vj = j + ((v >> 1) & 1), vk = k + ((v >> 2) & 1);
+    return m.verts[3 * ((vk * (m.ny + 1) + vj) * (m.nx + 1) + vi) + comp];
+  };
+
+  // Per-thread quadrature data of the phase-3 line (x = la, y = lb).
+  const T X = Tb::G(la), Y = Tb::G(lb);
+  const T qwl = Tb::W(la) * Tb::W(lb) * (T)m.kappa;
+
+  T un[5];
   double vn = 0.0;
-  fetch(blockIdx.x, un, vn);
-  for (int64_t b = blockIdx.x; b < cells; b += gridDim.x)
   {
-    int64_t gid = 0;
-    bool bnd = false;
-    const T ucur = un;
-    T yold = 0;
-    if (t < 24)
-      sv[t / 3][t % 3] = vn;
-    if (act)
+    const Line L = line_of(blockIdx.x);
+#pragma unroll
+    for (int a = 0; a < 5; ++a)
+      un[a] = L.valid ? u[L.base + a] : T(0);
+    vn = vert_of(blockIdx.x);
+  }
+  for (int bt = blockIdx.x; bt < batches; bt += gridDim.x)
+  {
+    const Line L = line_of(bt);
+    T ucur[5], yold[5];
+    bool bnd[5];
+#pragma unroll
+    for (int a = 0; a < 5; ++a)
     {
-      node(b, gid, bnd);
-      su[t] = bnd ? T(0) : ucur;
+      ucur[a] = un[a];
+      bnd[a] = L.row_bnd || (a == 0 && L.x_lo) || (a == 4 && L.x_hi);
       // No other CTA of this colour touches this cell's nodes.
-      if (!bnd)
-        yold = y[gid];
+      yold[a] = (L.valid && !bnd[a]) ? y[L.base + a] : T(0);
     }
-    fetch(b + gridDim.x, un, vn);
+    if (t < kBatch * 24)
+      sv[t / 24][t % 24] = vn;
+    // Inputs of the next batch, in flight while this one is processed.
+    {
+      const int nb = bt + gridDim.x;
+      if (nb < batches)
+      {
+        const Line N = line_of(nb);
+#pragma unroll
+        for (int a = 0; a < 5; ++a)
+          un[a] = N.valid ? u[N.base + a] : T(0);
+        vn = vert_of(nb);
+      }
+    }
     __syncthreads();
     // Edge vectors: differences of the FP64 vertices, rounded once to T.
-    if (t < 36)
+    for (int e = t; e < kBatch * 36; e += blockDim.x)
     {
-      const int c = t / 12, e = t % 12;
-      const int lo = edge_lo(e), hi = lo + (1 << (e >> 2));
-      se[c][e] = (T)(sv[hi][c] - sv[lo][c]);
+      const int cc = e / 36, r = e % 36, comp = r / 12, ed = r % 12;
+      const int lo = edge_lo(ed), hi = lo + (1 << (ed >> 2));
+      se[cc][comp][ed] = (T)(sv[cc][3 * hi + comp] - sv[cc][3 * lo + comp]);
     }
-    // Gradient in reference coordinates: contract x, then y, then z.
-    if (act)
+    // Phase 1: contract x on the (y, z) = (la, lb) line.
+    if (L.valid)
     {
-      T a0 = 0, a1 = 0;
+      T v[5];
+#pragma unroll
+      for (int a = 0; a < 5; ++a)
+        v[a] = bnd[a] ? T(0) : ucur[a];
+#pragma unroll
+      for (int q = 0; q < 5; ++q)
+      {
+        T a0 = 0, a1 = 0;
+#pragma unroll
+        for (int a = 0; a < 5; ++a)
+        {
+          a0 += Tb::B(q, a) * v[a];
+          a1 += Tb::D(q, a) * v[a];
+        }
+        S0[25 * lb + 5 * la + q] = a0;
+        S1[25 * lb + 5 * la + q] = a1;
+      }
+    }
+    __syncthreads();
+    const bool cv = act && kBatch * bt + c < cells;
+    // Phase 2: contract y on the (x, z) = (la, lb) line.
+    if (cv)
+    {
+      T va[5], vd[5];
+#pragma unroll
+      for (int b = 0; b < 5; ++b)
+      {
+        va[b] = S0[25 * lb + 5 * b + la];
+        vd[b] = S1[25 * lb + 5 * b + la];
+      }
+#pragma unroll
+      for (int q = 0; q < 5; ++q)
+      {
+        T c0 = 0, cy = 0, cx = 0;
+#pragma unroll
+        for (int b = 0; b < 5; ++b)
+        {
+          c0 += Tb::B(q, b) * va[b];
+          cy += Tb::D(q, b) * va[b];
+          cx += Tb::B(q, b) * vd[b];
+        }
+        S2[25 * lb + 5 * q + la] = c0;
+        S3[25 * lb + 5 * q + la] = cy;
+        S4[25 * lb + 5 * q + la] = cx;
+      }
+    }
+    __syncthreads();
+    // Phase 3: contract z on the (x, y) = (la, lb) line, apply the
+    // geometry at its 5 quadrature points, transpose z.
+    if (cv)
+    {
+      T c0[5], cy[5], cx[5];
+#pragma unroll
+      for (int r = 0; r < 5; ++r)
+      {
+        c0[r] = S2[25 * r + 5 * lb + la];
+        cy[r] = S3[25 * r + 5 * lb + la];
+        cx[r] = S4[25 * r + 5 * lb + la];
+      }
+      // Jacobian columns along the line: d/dX and d/dY are linear in Z,
+      // d/dZ does not depend on Z.
+      T P0[3], dP[3], Q0[3], dQ[3], R[3];
+#pragma unroll
+      for (int comp = 0; comp < 3; ++comp)
+      {
+        T e[12];
+        load_edges(se[c][comp], e);
+        const T p0 = (1 - Y) * e[0] + Y * e[1], p1 = (1 - Y) * e[2] + Y * e[3];
+        const T q0 = (1 - X) * e[4] + X * e[5], q1 = (1 - X) * e[6] + X * e[7];
+        P0[comp] = p0;
+        dP[comp] = p1 - p0;
+        Q0[comp] = q0;
+        dQ[comp] = q1 - q0;
+        R[comp] = (1 - X) * (1 - Y) * e[8] + X * (1 - Y) * e[9] + (1 - X) * Y * e[10]
+                  + X * Y * e[11];
+      }
+      T vx[5], vy[5], vz[5];
+#pragma unroll
+      for (int q = 0; q < 5; ++q)
+      {
+        T ux = 0, uy = 0, uz = 0;
+#pragma unroll
+        for (int r = 0; r < 5; ++r)
+        {
+          ux += Tb::B(q, r) * cx[r];
+          uy += Tb::B(q, r) * cy[r];
+          uz += Tb::D(q, r) * c0[r];
+        }
+        const T Z = Tb::G(q);
+        T J[3][3];
+#pragma unroll
+        for (int comp = 0; comp < 3; ++comp)
+        {
+          J[comp][0] = P0[comp] + Z * dP[comp];
+          J[comp][1] = Q0[comp] + Z * dQ[comp];
+          J[comp][2] = R[comp];
+        }
+        T adj[3][3];
+        adj[0][0] = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+        adj[0][1] = J[0][2] * J[2][1] - J[0][1] * J[2][2];
+        adj[0][2] = J[0][1] * J[1][2] - J[0][2] * J[1][1];
+        adj[1][0] = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+        adj[1][1] = J[0][0] * J[2][2] - J[0][2] * J[2][0];
+        adj[1][2] = J[0][2] * J[1][0] - J[0][0] * J[1][2];
+        adj[2][0] = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+        adj[2][1] = J[0][1] * J[2][0] - J[0][0] * J[2][1];
+        adj[2][2] = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+        const T det = J[0][0] * adj[0][0] + J[0][1] * adj[1][0] + J[0][2] * adj[2][0];
+        // G = w kappa |det| K K^T = w kappa adj adj^T / |det|, K = J^{-1}
+        const T sc = qwl * Tb::W(q) / fabs(det);
+        T G[3][3];
+#pragma unroll
+        for (int p = 0; p < 3; ++p)
+#pragma unroll
+          for (int pp = p; pp < 3; ++pp)
+            G[p][pp] = sc * (adj[p][0] * adj[pp][0] + adj[p][1] * adj[pp][1]
+                             + adj[p][2] * adj[pp][2]);
+        vx[q] = G[0][0] * ux + G[0][1] * uy + G[0][2] * uz;
+        vy[q] = G[0][1] * ux + G[1][1] * uy + G[1][2] * uz;
+        vz[q] = G[0][2] * ux + G[1][2] * uy + G[2][2] * uz;
+      }
 #pragma unroll
       for (int a = 0; a < 5; ++a)
       {
-        const T v = su[25 * t3 + 5 * t2 + a];
-        a0 += R.fB(0, a) * v;
-        a1 += R.fD(0, a) * v;
+        T ex = 0, ey = 0, ez = 0;
+#pragma unroll
+        for (int q = 0; q < 5; ++q)
+        {
+          ex += Tb::B(q, a) * vx[q];
+          ey += Tb::B(q, a) * vy[q];
+          ez += Tb::D(q, a) * vz[q];
+        }
+        S0[25 * a + 5 * lb + la] = ex;
+        S1[25 * a + 5 * lb + la] = ey;
+        S5[25 * a + 5 * lb + la] = ez;
       }
-      sA[t] = a0;
-      sAd[t] = a1;
     }
     __syncthreads();
-    if (act)
+    // Phase 4: transpose y on the (x, z) = (la, lb) line.
+    if (cv)
     {
-      T c0 = 0, cy = 0, cx = 0;
-#pragma unroll
-      for (int bb = 0; bb < 5; ++bb)
-      {
-        const T va = sA[25 * t3 + 5 * bb + t1], vd = sAd[25 * t3 + 5 * bb + t1];
-        c0 += R.fB(1, bb) * va;
-        cy += R.fD(1, bb) * va;
-        cx += R.fB(1, bb) * vd;
-      }
-      sC[t] = c0;
-      sCy[t] = cy;
-      sCx[t] = cx;
-    }
-    __syncthreads();
-    if (act)
-    {
-      T ux = 0, uy = 0, uz = 0;
-#pragma unroll
-      for (int c = 0; c < 5; ++c)
-      {
-        const int o = 25 * c + 5 * t2 + t1;
-        ux += R.fB(2, c) * sCx[o];
-        uy += R.fB(2, c) * sCy[o];
-        uz += R.fD(2, c) * sC[o];
-      }
-      T J[3][3];
-#pragma unroll
-      for (int c = 0; c < 3; ++c)
-      {
-        T e[12];
-        load_edges(se[c], e);
-        J[c][0] = wx[0] * e[0] + wx[1] * e[1] + wx[2] * e[2] + wx[3] * e[3];
-        J[c][1] = wy[0] * e[4] + wy[1] * e[5] + wy[2] * e[6] + wy[3] * e[7];
-        J[c][2] = wz[0] * e[8] + wz[1] * e[9] + wz[2] * e[10] + wz[3] * e[11];
-      }
-      T adj[3][3];
-      adj[0][0] = J[1][1] * J[2][2] - J[1][2] * J[2][1];
-      adj[0][1] = J[0][2] * J[2][1] - J[0][1] * J[2][2];
-      adj[0][2] = J[0][1] * J[1][2] - J[0][2] * J[1][1];
-      adj[1][0] = J[1][2] * J[2][0] - J[1][0] * J[2][2];
-      adj[1][1] = J[0][0] * J[2][2] - J[0][2] * J[2][0];
-      adj[1][2] = J[0][2] * J[1][0] - J[0][0] * J[1][2];
-      adj[2][0] = J[1][0] * J[2][1] - J[1][1] * J[2][0];
-      adj[2][1] = J[0][1] * J[2][0] - J[0][0] * J[2][1];
-      adj[2][2] = J[0][0] * J[1][1] - J[0][1] * J[1][0];
-      const T det = J[0][0] * adj[0][0] + J[0][1] * adj[1][0] + J[0][2] * adj[2][0];
-      // G = w kappa |det| K K^T = w kappa adj adj^T / |det|, K = J^{-1}
-      const T sc = qw / fabs(det);
-      T G[3][3];
-#pragma unroll
-      for (int p = 0; p < 3; ++p)
-#pragma unroll
-        for (int q = p; q < 3; ++q)
-          G[p][q] = sc * (adj[p][0] * adj[q][0] + adj[p][1] * adj[q][1] + adj[p][2] * adj[q][2]);
-      // su, sA, sAd were last read before the previous barrier.
-      sA[t] = G[0][0] * ux + G[0][1] * uy + G[0][2] * uz;
-      sAd[t] = G[0][1] * ux + G[1][1] * uy + G[1][2] * uz;
-      su[t] = G[0][2] * ux + G[1][2] * uy + G[2][2] * uz;
-    }
-    __syncthreads();
-    // Transpose: contract z, then y, then x.
-    if (act)
-    {
-      T ex = 0, ey = 0, ez = 0;
+      T ex[5], ey[5], ez[5];
 #pragma unroll
       for (int q = 0; q < 5; ++q)
       {
-        const int o = 25 * q + 5 * t2 + t1;
-        ex += R.cB(2, q) * sA[o];
-        ey += R.cB(2, q) * sAd[o];
-        ez += R.cD(2, q) * su[o];
+        ex[q] = S0[25 * lb + 5 * q + la];
+        ey[q] = S1[25 * lb + 5 * q + la];
+        ez[q] = S5[25 * lb + 5 * q + la];
       }
-      sCx[t] = ex;
-      sCy[t] = ey;
-      sC[t] = ez;
+#pragma unroll
+      for (int a = 0; a < 5; ++a)
+      {
+        T x1 = 0, x2 = 0;
+#pragma unroll
+        for (int q = 0; q < 5; ++q)
+        {
+          x1 += Tb::B(q, a) * ex[q];
+          x2 += Tb::D(q, a) * ey[q] + Tb::B(q, a) * ez[q];
+        }
+        S2[25 * lb + 5 * a + la] = x1;
+        S3[25 * lb + 5 * a + la] = x2;
+      }
     }
     __syncthreads();
-    if (act)
+    // Phase 5: transpose x on the (y, z) = (la, lb) line; scatter.
+    if (L.valid)
     {
-      T x1 = 0, x2 = 0;
+      T x1[5], x2[5];
 #pragma unroll
       for (int q = 0; q < 5; ++q)
       {
-        const int o = 25 * t3 + 5 * q + t1;
-        x1 += R.cB(1, q) * sCx[o];
-        x2 += R.cD(1, q) * sCy[o] + R.cB(1, q) * sC[o];
+        x1[q] = S2[25 * lb + 5 * la + q];
+        x2[q] = S3[25 * lb + 5 * la + q];
       }
-      sA[t] = x1;
-      sAd[t] = x2;
-    }
-    __syncthreads();
-    if (act)
-    {
-      T ye = 0;
 #pragma unroll
-      for (int q = 0; q < 5; ++q)
+      for (int a = 0; a < 5; ++a)
       {
-        const int o = 25 * t3 + 5 * t2 + q;
-        ye += R.cD(0, q) * sA[o] + R.cB(0, q) * sAd[o];
+        T ye = 0;
+#pragma unroll
+        for (int q = 0; q < 5; ++q)
+          ye += Tb::D(q, a) * x1[q] + Tb::B(q, a) * x2[q];
+        y[L.base + a] = bnd[a] ? ucur[a] : yold[a] + ye;
       }
-      y[gid] = bnd ? ucur : yold + ye;
     }
   }
 }
@@ -451,6 +491,9 @@ int q4_apply(const dfx_q4_mesh_s& m, const T* u, T* y, cudaStream_t s, const int
 {
   if (int st = q4_prepare())
     return st;
+  DFX_REQUIRE((int64_t)m.nx * m.ny * m.nz < ((int64_t)1 << 31) && 4 * (int64_t)m.nx + 1 < (1 << 30)
+                  && 4 * (int64_t)m.ny + 1 < (1 << 30),
+              "Q4 mesh too large (%d x %d x %d cells)", m.nx, m.ny, m.nz);
   const int64_t n = q4_ndofs(m);
   DFX_CUDA(cudaMemsetAsync(y, 0, sizeof(T) * n, s));
   for (int c = 0; c < 8; ++c)
@@ -460,7 +503,7 @@ int q4_apply(const dfx_q4_mesh_s& m, const T* u, T* y, cudaStream_t s, const int
     const int64_t cells = hx * hy * hz;
     if (cells == 0)
       continue;
-    const int64_t grid = std::min<int64_t>(cells, q4_grid_limit<T>());
+    const int64_t grid = std::min<int64_t>((cells + kBatch - 1) / kBatch, q4_grid_limit<T>());
     k_q4_cells<T><<<(unsigned)grid, 128, 0, s>>>(m, u, y, ci, cj, ck, skip);
   }
   DFX_CHECK_LAUNCH();
