@@ -50,6 +50,10 @@ def parse():
                    help="requests of the bounded serving sample (0: skip)")
     p.add_argument("--serving-nmax", type=int, default=48)
     p.add_argument("--no-c3", action="store_true", help="skip the elasticity (c3) sample")
+    p.add_argument("--no-c4", action="store_true", help="skip the matrix-free Q4 (c4) sample")
+    p.add_argument("--c4-only", action="store_true",
+                   help="run only the matrix-free Q4 sample and print its JSON")
+    p.add_argument("--c4-n", type=int, default=64, help="Q4 hexahedra per direction")
     p.add_argument("--profile", action="store_true",
                    help="profiling target: a few launches of every hot kernel, no timing")
     return p.parse_args()
@@ -382,6 +386,96 @@ def c3_sample(steps=1, warmup=1):
     return out
 
 
+# Algorithmic FP32/FP64 operations of one cell of the sum-factorised Q4
+# action, counting an FMA as 2: 2000 FMAs of 1D contractions (x: 250,
+# y: 375, z: 375 forward; the same backward) and about 100 operations of
+# geometry per quadrature point (Jacobian columns 12, adjugate 27,
+# determinant 5, scale 3, G = adj adj^T 36, G grad 18).
+Q4_FLOP_PER_CELL = 2 * 2000 + 125 * 101
+
+
+def c4_sample(n=64, seed=4):
+    """Matrix-free Laplacian, Q4 Lagrange on the unit cube with n^3 hexahedra
+    (interior vertices perturbed by U(-0.05h, 0.05h)), Gauss-Legendre 5^3
+    quadrature, homogeneous Dirichlet boundary, b ~ U[-1, 1] on interior
+    nodes. The action timed alone in FP32 and FP64 (L2 flushed before each
+    launch, per-launch CUDA events), then CG to rtol 1e-10 (measured with
+    the FP64 action) in FP64 and in mixed precision (FP32 action and
+    vectors, residual replaced with the FP64 action)."""
+    import numpy as np
+    import torch
+
+    from dolfinx_gb300 import matrix_free as mf
+
+    stream = torch.cuda.current_stream()
+    v = mf.hex_box_vertices(n, perturb=0.05, seed=seed)
+    op = mf.Q4Laplacian(v, n)
+    bnd = torch.from_numpy(mf.boundary_mask(n, n, n)).cuda()
+    rng = np.random.default_rng(seed)
+    b = torch.from_numpy(rng.uniform(-1.0, 1.0, op.n)).cuda().masked_fill(bnd, 0.0)
+    cells = n ** 3
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # 2x L2
+
+    def per_launch_ms(fn, reps):
+        for _ in range(3):
+            fn()
+        tot = 0.0
+        for _ in range(reps):
+            flush.fill_(1)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            torch.cuda.synchronize()
+            tot += e0.elapsed_time(e1)
+        return tot / reps
+
+    u64 = torch.from_numpy(rng.standard_normal(op.n)).cuda().masked_fill(bnd, 0.0)
+    u32 = u64.float()
+    y64, y32 = torch.empty_like(u64), torch.empty_like(u32)
+    ms_a32 = per_launch_ms(lambda: op.apply(u32, y32), 10)
+    ms_a64 = per_launch_ms(lambda: op.apply(u64, y64), 3)
+    flop = Q4_FLOP_PER_CELL * cells
+    out = {"workload": f"Q4 Laplacian, unit cube {n}^3 hexahedra, 5% interior vertex noise",
+           "cells": cells, "dofs": op.n, "flop_per_cell": Q4_FLOP_PER_CELL,
+           "action_f32": {"ms": ms_a32, "tflops": flop / (ms_a32 * 1e-3) / 1e12,
+                          "gdof_per_s": op.n / (ms_a32 * 1e-3) / 1e9,
+                          "rel_diff_vs_f64": float((y32.double() - y64).norm() / y64.norm())},
+           "action_f64": {"ms": ms_a64, "tflops": flop / (ms_a64 * 1e-3) / 1e12,
+                          "gdof_per_s": op.n / (ms_a64 * 1e-3) / 1e9},
+           "alg_bytes_per_action_f32": op.n * 4 * 3 + (n + 1) ** 3 * 24,
+           "kernels_per_action": 8}
+    del u64, u32, y64, y32
+    x = torch.zeros_like(b)
+    solves = {}
+    for mode, reps in (("mixed", 2), ("fp64", 1)):
+        solver = mf.MatrixFreeCG(op, mode=mode)
+        if mode == "mixed":
+            x.zero_()
+            solver.solve(b, x, rtol=1e-10, raise_on_fail=False)
+
+        def step():
+            x.zero_()
+            return solver.solve(b, x, rtol=1e-10, raise_on_fail=False)
+
+        ms, res = _timed(step, reps, stream)
+        r = res[-1]
+        true_rel = float((b - op(x)).norm() / b.norm())
+        solves[mode] = {"ms_per_solve": ms, "gdof_per_s": op.n / (ms * 1e-3) / 1e9,
+                        "iterations": r.iterations, "status": r.status,
+                        "true_rel_residual_fp64": true_rel, "kernel_launches": r.kernel_launches}
+        if mode == "mixed":
+            xm = x.clone()
+    solves["rel_err_mixed_vs_fp64_solution"] = float((xm - x).norm() / x.norm())
+    solves["speedup_of_mixed"] = solves["fp64"]["ms_per_solve"] / solves["mixed"]["ms_per_solve"]
+    out["cg"] = solves
+    out["note"] = ("the reference applies this operator matrix-free in FP64 (the matrix-free "
+                   "demo); an assembled Q4 CSR would hold ~3.6e9 entries, so the FP64 path "
+                   "compared against is the FP64 matrix-free action")
+    return out
+
+
 def serving_sample(args):
     """Serving loop on a bounded stream drawn like the serving config (unit
     cubes, n log-uniform, P1/P2, Helmholtz k2 in [0, 10], lognormal kappa),
@@ -526,6 +620,11 @@ def run_ours(args):
     if not args.no_c3:
         c3 = c3_sample()
 
+    # ---- c4: matrix-free Q4 action and CG
+    c4 = None
+    if not args.no_c4:
+        c4 = c4_sample(args.c4_n)
+
     # ---- serving loop: bounded sample of the request stream (both modes)
     serving_out = None
     if args.serving_requests > 0:
@@ -567,6 +666,7 @@ def run_ours(args):
                                            "alg_bytes_per_launch": alg64, "launch_ms": ms64k,
                                            "traffic": profile_traffic("sell_f64_c2")},
                 "c3_elasticity": c3,
+                "c4_matrix_free_q4": c4,
                 "serving": serving_out,
                 "gpu_launches": launches,
                 "clocks": clocks,
@@ -603,6 +703,11 @@ def main():
     args = parse()
     if args.profile:
         run_profile(args)
+    elif args.c4_only:
+        import torch
+
+        torch.cuda.set_device(0)
+        print(json.dumps({"c4_matrix_free_q4": c4_sample(args.c4_n)}))
     elif args.impl == "reference":
         run_reference(args)
     else:
