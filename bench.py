@@ -388,10 +388,10 @@ def c3_sample(steps=1, warmup=1):
 
 # Algorithmic FP32/FP64 operations of one cell of the sum-factorised Q4
 # action, counting an FMA as 2: 2000 FMAs of 1D contractions (x: 250,
-# y: 375, z: 375 forward; the same backward) and about 100 operations of
-# geometry per quadrature point (Jacobian columns 12, adjugate 27,
-# determinant 5, scale 3, G = adj adj^T 36, G grad 18).
-Q4_FLOP_PER_CELL = 2 * 2000 + 125 * 101
+# y: 375, z: 375 forward; the same backward) and 80 operations of geometry
+# per quadrature point (Jacobian columns 12, adjugate 27, determinant 5,
+# scale 3, sc adj^T grad 18, adj (.) 15).
+Q4_FLOP_PER_CELL = 2 * 2000 + 125 * 80
 
 
 def c4_sample(n=64, seed=4):

@@ -118,6 +118,7 @@ class Q4Mesh(C.Structure):
         ("nz", C.c_int32),
         ("verts", C.c_void_p),
         ("kappa", C.c_double),
+        ("edges32", C.c_void_p),
     ]
 
 
@@ -172,6 +173,7 @@ _SIGS = {
                                   C.c_size_t, C.POINTER(CgInfo), _P]),
     "dfx_q4_num_dofs": (C.c_int64, [C.POINTER(Q4Mesh)]),
     "dfx_q4_action": (C.c_int, [C.POINTER(Q4Mesh), C.c_int32, _P, _P, _P]),
+    "dfx_q4_edges": (C.c_int, [C.POINTER(Q4Mesh), _P, _P]),
     "dfx_q4_cg_workspace_bytes": (C.c_size_t, [C.c_int64, C.c_int32]),
     "dfx_q4_cg_solve": (C.c_int, [C.POINTER(Q4Mesh), _P, _P, C.c_double, C.c_int32, C.c_int32,
                                   C.c_double, C.c_int32, _P, C.c_size_t, C.POINTER(CgInfo), _P]),

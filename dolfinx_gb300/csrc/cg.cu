@@ -929,7 +929,8 @@ int iteration_graph(const OpRef& o, T* x, const T* dinv, int64_t n, const Work<T
   GraphKey key{(int)o.kind * 4 + (sizeof(T) == 4) * 2 + (reliable ? 1 : 0),
                q4 ? (const void*)o.q4->verts
                   : (o.kind == kSell ? (const void*)o.op : (const void*)o.A->row_ptr),
-               q4 ? nullptr : (o.kind == kSell ? (const void*)o.op->vals : (const void*)o.A->vals),
+               q4 ? (const void*)o.q4->edges32
+                  : (o.kind == kSell ? (const void*)o.op->vals : (const void*)o.A->vals),
                o.kind == kCsr ? (const void*)o.A->cols : nullptr,
                (const void*)x,
                (const void*)dinv,

@@ -114,6 +114,33 @@ int upload_tables()
 constexpr int kBatch = 5;
 constexpr int kLattice = 125;
 
+// Shared-memory layouts of a cell's 5^3 values (x, y, z). Values written in
+// one phase and read in the next go through layout A (phases 1->2, 4->5:
+// lanes span (y, z), then (x, z)) or B (2->3, 3->4: lanes span (x, z), then
+// (x, y)); in FP32 the strides make every access of the 4 warps free of bank
+// conflicts (a 125-stride lattice gives 2-way conflicts). FP64 keeps the
+// compact lattice: that kernel is bound by the FP64 pipe.
+template <typename T>
+struct Lay
+{
+  static constexpr int ay = 33, az = 5, by = 5, bz = 37, cell = 185;
+};
+template <>
+struct Lay<double>
+{
+  static constexpr int ay = 5, az = 25, by = 5, bz = 25, cell = 125;
+};
+template <typename T>
+__device__ __forceinline__ int lay_a(int x, int y, int z)
+{
+  return x + Lay<T>::ay * y + Lay<T>::az * z;
+}
+template <typename T>
+__device__ __forceinline__ int lay_b(int x, int y, int z)
+{
+  return x + Lay<T>::by * y + Lay<T>::bz * z;
+}
+
 // The 12 edge components of one coordinate, read with 16-byte loads.
 __device__ __forceinline__ void load_edges(const float* p, float (&e)[12])
 {
@@ -160,84 +187,132 @@ __device__ __forceinline__ int edge_lo(int e)
 //   3. z: C, Cy, Cx -> grad at 5 points -> G grad -> transpose in z
 //   4. y transpose;  5. x transpose -> y += on the line (global).
 // Lines of phases 1/5 are (y, z) node rows, of 2/4 (x, z), of 3 (x, y).
+// One colour of cells (parity ci, cj, ck): hx x hy x hz cells, ordinal
+// b = x + hx (y + hy z). A thread's cell advances by kBatch x gridDim.x
+// ordinals per batch, given as mixed-radix digits (dx, dy, dz) so that the
+// kernel needs no integer division after its first cell.
+struct Colour
+{
+  int ci, cj, ck;
+  int hx, hy, hz;
+  int dx, dy, dz;
+};
+
+// x / y / z of a colour ordinal, advanced by the digits (dx, dy, dz).
+struct CellIter
+{
+  int x, y, z;
+  __device__ void advance(const Colour& col)
+  {
+    x += col.dx;
+    const int cx = x >= col.hx;
+    x -= cx ? col.hx : 0;
+    y += col.dy + cx;
+    const int cy = y >= col.hy;
+    y -= cy ? col.hy : 0;
+    z += col.dz + cy;
+  }
+};
+
+// x / |d| in the kernel's precision: the fast reciprocal path in FP32 (a
+// few ulp, far below the FP32 operator's own rounding), IEEE in FP64.
+__device__ __forceinline__ float div_abs(float x, float d) { return __fdividef(x, fabsf(d)); }
+__device__ __forceinline__ double div_abs(double x, double d) { return x / fabs(d); }
+
 template <typename T>
 __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2)
-    k_q4_cells(const dfx_q4_mesh_s m, const T* __restrict__ u, T* __restrict__ y, int ci, int cj,
-               int ck, const int32_t* __restrict__ skip)
+    k_q4_cells(const dfx_q4_mesh_s m, const T* __restrict__ u, T* __restrict__ y,
+               const Colour col, const int32_t* __restrict__ skip)
 {
   if (skip && __ldg(skip))
     return;
   using Tb = Tab<T>;
-  __shared__ T S[6][kBatch * kLattice];
+  __shared__ T S[6][kBatch * Lay<T>::cell];
   __shared__ __align__(16) T se[kBatch][3][12]; // edge vectors by cell and component
   __shared__ double sv[kBatch][24];
   const int t = threadIdx.x;
   const bool act = t < kBatch * kLattice / 5;
   const int c = act ? t / 25 : 0, l = t % 25;
   const int la = l % 5, lb = l / 5;
-  T* const S0 = S[0] + c * kLattice;
-  T* const S1 = S[1] + c * kLattice;
-  T* const S2 = S[2] + c * kLattice;
-  T* const S3 = S[3] + c * kLattice;
-  T* const S4 = S[4] + c * kLattice;
-  T* const S5 = S[5] + c * kLattice;
+  T* const S0 = S[0] + c * Lay<T>::cell;
+  T* const S1 = S[1] + c * Lay<T>::cell;
+  T* const S2 = S[2] + c * Lay<T>::cell;
+  T* const S3 = S[3] + c * Lay<T>::cell;
+  T* const S4 = S[4] + c * Lay<T>::cell;
+  T* const S5 = S[5] + c * Lay<T>::cell;
 
-  const int hx = (m.nx - ci + 1) / 2, hy = (m.ny - cj + 1) / 2, hz = (m.nz - ck + 1) / 2;
-  const int cells = hx * hy * hz; // < 2^31, checked on the host
+  const int cells = col.hx * col.hy * col.hz; // < 2^31, checked on the host
   const int batches = (cells + kBatch - 1) / kBatch;
   const int NX = 4 * m.nx + 1, NY = 4 * m.ny + 1, NZ = 4 * m.nz + 1;
-  // Lattice (y, z) coordinates of this thread's phase-1/5 line in cell
-  // (i, j, k), and the line's first node.
+  // This thread's cell (c of the batch) and its phase-1/5 line: nodes
+  // (4i + 0..4, 4j + la, 4k + lb).
   struct Line
   {
     int64_t base;
     bool row_bnd; // the whole line lies on a y or z boundary face
     bool x_lo, x_hi;
     bool valid;
+    int i, j, k;
   };
-  auto line_of = [&](int bt) -> Line
+  auto line_of = [&](const CellIter& it) -> Line
   {
-    Line L{0, false, false, false, false};
-    const int b = kBatch * bt + c;
-    if (!act || b >= cells)
+    Line L{0, false, false, false, false, 0, 0, 0};
+    if (!act || it.z >= col.hz)
       return L;
-    const int i = ci + 2 * (b % hx), j = cj + 2 * ((b / hx) % hy), k = ck + 2 * (b / (hx * hy));
-    const int J = 4 * j + la, K = 4 * k + lb;
-    L.base = ((int64_t)K * NY + J) * NX + 4 * (int64_t)i;
+    L.i = col.ci + 2 * it.x;
+    L.j = col.cj + 2 * it.y;
+    L.k = col.ck + 2 * it.z;
+    const int J = 4 * L.j + la, K = 4 * L.k + lb;
+    L.base = ((int64_t)K * NY + J) * NX + 4 * (int64_t)L.i;
     L.row_bnd = J == 0 || K == 0 || J == NY - 1 || K == NZ - 1;
-    L.x_lo = i == 0;
-    L.x_hi = i == m.nx - 1;
+    L.x_lo = L.i == 0;
+    L.x_hi = L.i == m.nx - 1;
     L.valid = true;
     return L;
   };
-  // One vertex coordinate of the batch (threads t < 120).
-  auto vert_of = [&](int bt) -> double
+  // Coordinate l (< 24) of the cell's 8 vertices, loaded by its thread l.
+  auto vert_of = [&](const Line& L) -> double
   {
-    const int cc = t / 24, r = t % 24, v = r / 3, comp = r % 3;
-    const int b = kBatch * bt + cc;
-    if (t >= kBatch * 24 || b >= cells)
+    if (!L.valid || l >= 24)
       return 0.0;
-    const int i = ci + 2 * (b % hx), j = cj + 2 * ((b / hx) % hy), k = ck + 2 * (b / (hx * hy));
-    const int64_t vi = i + (v & 1), vj = j + ((v >> 1) & 1), vk = k + ((v >> 2) & 1);
+    const int v = l / 3, comp = l % 3;
+    const int64_t vi = L.i + (v & 1), vj = L.j + ((v >> 1) & 1), vk = L.k + ((v >> 2) & 1);
     return m.verts[3 * ((vk * (m.ny + 1) + vj) * (m.nx + 1) + vi) + comp];
+  };
+  // FP32 kernel with precomputed edges: 16 bytes l (< 9) of the cell's 36.
+  const bool pre = sizeof(T) == 4 && m.edges32 != nullptr;
+  auto edges_of = [&](const Line& L) -> float4
+  {
+    if (!L.valid || l >= 9)
+      return make_float4(0.f, 0.f, 0.f, 0.f);
+    const int64_t cell = L.i + (int64_t)m.nx * (L.j + (int64_t)m.ny * L.k);
+    return __ldg(reinterpret_cast<const float4*>(m.edges32) + 9 * cell + l);
   };
 
   // Per-thread quadrature data of the phase-3 line (x = la, y = lb).
   const T X = Tb::G(la), Y = Tb::G(lb);
   const T qwl = Tb::W(la) * Tb::W(lb) * (T)m.kappa;
 
+  CellIter it;
+  {
+    const int b = kBatch * blockIdx.x + c;
+    it.x = b % col.hx;
+    it.y = (b / col.hx) % col.hy;
+    it.z = b / (col.hx * col.hy);
+  }
+  Line L = line_of(it);
   T un[5];
   double vn = 0.0;
-  {
-    const Line L = line_of(blockIdx.x);
+  float4 en = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (pre)
+    en = edges_of(L);
+  else
+    vn = vert_of(L);
 #pragma unroll
-    for (int a = 0; a < 5; ++a)
-      un[a] = L.valid ? u[L.base + a] : T(0);
-    vn = vert_of(blockIdx.x);
-  }
+  for (int a = 0; a < 5; ++a)
+    un[a] = L.valid ? u[L.base + a] : T(0);
   for (int bt = blockIdx.x; bt < batches; bt += gridDim.x)
   {
-    const Line L = line_of(bt);
     T ucur[5], yold[5];
     bool bnd[5];
 #pragma unroll
@@ -248,30 +323,37 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2)
       // No other CTA of this colour touches this cell's nodes.
       yold[a] = (L.valid && !bnd[a]) ? y[L.base + a] : T(0);
     }
-    if (t < kBatch * 24)
-      sv[t / 24][t % 24] = vn;
-    // Inputs of the next batch, in flight while this one is processed.
+    if constexpr (sizeof(T) == 4)
     {
-      const int nb = bt + gridDim.x;
-      if (nb < batches)
-      {
-        const Line N = line_of(nb);
+      if (pre && act && l < 9)
+        reinterpret_cast<float4*>(&se[c][0][0])[l] = en;
+    }
+    if (!pre && act && l < 24)
+      sv[c][l] = vn;
+    // Inputs of the next batch, in flight while this one is processed.
+    const Line Lc = L;
+    it.advance(col);
+    L = line_of(it);
+    if (bt + (int)gridDim.x < batches)
+    {
 #pragma unroll
-        for (int a = 0; a < 5; ++a)
-          un[a] = N.valid ? u[N.base + a] : T(0);
-        vn = vert_of(nb);
-      }
+      for (int a = 0; a < 5; ++a)
+        un[a] = L.valid ? u[L.base + a] : T(0);
+      if (pre)
+        en = edges_of(L);
+      else
+        vn = vert_of(L);
     }
     __syncthreads();
     // Edge vectors: differences of the FP64 vertices, rounded once to T.
-    for (int e = t; e < kBatch * 36; e += blockDim.x)
+    for (int e = pre ? kBatch * 36 : t; e < kBatch * 36; e += blockDim.x)
     {
       const int cc = e / 36, r = e % 36, comp = r / 12, ed = r % 12;
       const int lo = edge_lo(ed), hi = lo + (1 << (ed >> 2));
       se[cc][comp][ed] = (T)(sv[cc][3 * hi + comp] - sv[cc][3 * lo + comp]);
     }
     // Phase 1: contract x on the (y, z) = (la, lb) line.
-    if (L.valid)
+    if (Lc.valid)
     {
       T v[5];
 #pragma unroll
@@ -287,12 +369,12 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2)
           a0 += Tb::B(q, a) * v[a];
           a1 += Tb::D(q, a) * v[a];
         }
-        S0[25 * lb + 5 * la + q] = a0;
-        S1[25 * lb + 5 * la + q] = a1;
+        S0[lay_a<T>(q, la, lb)] = a0;
+        S1[lay_a<T>(q, la, lb)] = a1;
       }
     }
     __syncthreads();
-    const bool cv = act && kBatch * bt + c < cells;
+    const bool cv = Lc.valid;
     // Phase 2: contract y on the (x, z) = (la, lb) line.
     if (cv)
     {
@@ -300,8 +382,8 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2)
 #pragma unroll
       for (int b = 0; b < 5; ++b)
       {
-        va[b] = S0[25 * lb + 5 * b + la];
-        vd[b] = S1[25 * lb + 5 * b + la];
+        va[b] = S0[lay_a<T>(la, b, lb)];
+        vd[b] = S1[lay_a<T>(la, b, lb)];
       }
 #pragma unroll
       for (int q = 0; q < 5; ++q)
@@ -314,9 +396,9 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2)
           cy += Tb::D(q, b) * va[b];
           cx += Tb::B(q, b) * vd[b];
         }
-        S2[25 * lb + 5 * q + la] = c0;
-        S3[25 * lb + 5 * q + la] = cy;
-        S4[25 * lb + 5 * q + la] = cx;
+        S2[lay_b<T>(la, q, lb)] = c0;
+        S3[lay_b<T>(la, q, lb)] = cy;
+        S4[lay_b<T>(la, q, lb)] = cx;
       }
     }
     __syncthreads();
@@ -328,9 +410,9 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2)
 #pragma unroll
       for (int r = 0; r < 5; ++r)
       {
-        c0[r] = S2[25 * r + 5 * lb + la];
-        cy[r] = S3[25 * r + 5 * lb + la];
-        cx[r] = S4[25 * r + 5 * lb + la];
+        c0[r] = S2[lay_b<T>(la, lb, r)];
+        cy[r] = S3[lay_b<T>(la, lb, r)];
+        cx[r] = S4[lay_b<T>(la, lb, r)];
       }
       // Jacobian columns along the line: d/dX and d/dY are linear in Z,
       // d/dZ does not depend on Z.
@@ -381,18 +463,15 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2)
         adj[2][1] = J[0][1] * J[2][0] - J[0][0] * J[2][1];
         adj[2][2] = J[0][0] * J[1][1] - J[0][1] * J[1][0];
         const T det = J[0][0] * adj[0][0] + J[0][1] * adj[1][0] + J[0][2] * adj[2][0];
-        // G = w kappa |det| K K^T = w kappa adj adj^T / |det|, K = J^{-1}
-        const T sc = qwl * Tb::W(q) / fabs(det);
-        T G[3][3];
-#pragma unroll
-        for (int p = 0; p < 3; ++p)
-#pragma unroll
-          for (int pp = p; pp < 3; ++pp)
-            G[p][pp] = sc * (adj[p][0] * adj[pp][0] + adj[p][1] * adj[pp][1]
-                             + adj[p][2] * adj[pp][2]);
-        vx[q] = G[0][0] * ux + G[0][1] * uy + G[0][2] * uz;
-        vy[q] = G[0][1] * ux + G[1][1] * uy + G[1][2] * uz;
-        vz[q] = G[0][2] * ux + G[1][2] * uy + G[2][2] * uz;
+        // G grad = w kappa |det| K K^T grad = sc adj (adj^T grad), K = J^{-1} =
+        // adj / det, sc = w kappa / |det|.
+        const T sc = div_abs(qwl * Tb::W(q), det);
+        const T w0 = sc * (adj[0][0] * ux + adj[1][0] * uy + adj[2][0] * uz);
+        const T w1 = sc * (adj[0][1] * ux + adj[1][1] * uy + adj[2][1] * uz);
+        const T w2 = sc * (adj[0][2] * ux + adj[1][2] * uy + adj[2][2] * uz);
+        vx[q] = adj[0][0] * w0 + adj[0][1] * w1 + adj[0][2] * w2;
+        vy[q] = adj[1][0] * w0 + adj[1][1] * w1 + adj[1][2] * w2;
+        vz[q] = adj[2][0] * w0 + adj[2][1] * w1 + adj[2][2] * w2;
       }
 #pragma unroll
       for (int a = 0; a < 5; ++a)
@@ -405,9 +484,9 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2)
           ey += Tb::B(q, a) * vy[q];
           ez += Tb::D(q, a) * vz[q];
         }
-        S0[25 * a + 5 * lb + la] = ex;
-        S1[25 * a + 5 * lb + la] = ey;
-        S5[25 * a + 5 * lb + la] = ez;
+        S0[lay_b<T>(la, lb, a)] = ex;
+        S1[lay_b<T>(la, lb, a)] = ey;
+        S5[lay_b<T>(la, lb, a)] = ez;
       }
     }
     __syncthreads();
@@ -418,9 +497,9 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2)
 #pragma unroll
       for (int q = 0; q < 5; ++q)
       {
-        ex[q] = S0[25 * lb + 5 * q + la];
-        ey[q] = S1[25 * lb + 5 * q + la];
-        ez[q] = S5[25 * lb + 5 * q + la];
+        ex[q] = S0[lay_b<T>(la, q, lb)];
+        ey[q] = S1[lay_b<T>(la, q, lb)];
+        ez[q] = S5[lay_b<T>(la, q, lb)];
       }
 #pragma unroll
       for (int a = 0; a < 5; ++a)
@@ -432,20 +511,20 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2)
           x1 += Tb::B(q, a) * ex[q];
           x2 += Tb::D(q, a) * ey[q] + Tb::B(q, a) * ez[q];
         }
-        S2[25 * lb + 5 * a + la] = x1;
-        S3[25 * lb + 5 * a + la] = x2;
+        S2[lay_a<T>(la, a, lb)] = x1;
+        S3[lay_a<T>(la, a, lb)] = x2;
       }
     }
     __syncthreads();
     // Phase 5: transpose x on the (y, z) = (la, lb) line; scatter.
-    if (L.valid)
+    if (Lc.valid)
     {
       T x1[5], x2[5];
 #pragma unroll
       for (int q = 0; q < 5; ++q)
       {
-        x1[q] = S2[25 * lb + 5 * la + q];
-        x2[q] = S3[25 * lb + 5 * la + q];
+        x1[q] = S2[lay_a<T>(q, la, lb)];
+        x2[q] = S3[lay_a<T>(q, la, lb)];
       }
 #pragma unroll
       for (int a = 0; a < 5; ++a)
@@ -454,10 +533,30 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2)
 #pragma unroll
         for (int q = 0; q < 5; ++q)
           ye += Tb::D(q, a) * x1[q] + Tb::B(q, a) * x2[q];
-        y[L.base + a] = bnd[a] ? ucur[a] : yold[a] + ye;
+        y[Lc.base + a] = bnd[a] ? ucur[a] : yold[a] + ye;
       }
     }
   }
+}
+
+// Edge vectors of every cell in FP32, [cell][component][edge], cells
+// lexicographic: the differences of the FP64 vertices rounded once, exactly
+// what the colour kernel forms on the fly.
+__global__ void k_q4_edges(const dfx_q4_mesh_s m, float* __restrict__ edges, int64_t cells)
+{
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= cells * 36)
+    return;
+  const int64_t cell = g / 36;
+  const int r = (int)(g % 36), comp = r / 12, ed = r % 12;
+  const int64_t i = cell % m.nx, j = (cell / m.nx) % m.ny, k = cell / ((int64_t)m.nx * m.ny);
+  const int lo = edge_lo(ed), hi = lo + (1 << (ed >> 2));
+  auto coord = [&](int v)
+  {
+    const int64_t vi = i + (v & 1), vj = j + ((v >> 1) & 1), vk = k + ((v >> 2) & 1);
+    return m.verts[3 * ((vk * (m.ny + 1) + vj) * (m.nx + 1) + vi) + comp];
+  };
+  edges[g] = (float)(coord(hi) - coord(lo));
 }
 
 // Resident CTAs per SM of the colour kernel (queried once per type).
@@ -498,13 +597,22 @@ int q4_apply(const dfx_q4_mesh_s& m, const T* u, T* y, cudaStream_t s, const int
   DFX_CUDA(cudaMemsetAsync(y, 0, sizeof(T) * n, s));
   for (int c = 0; c < 8; ++c)
   {
-    const int ci = c & 1, cj = (c >> 1) & 1, ck = (c >> 2) & 1;
-    const int64_t hx = (m.nx - ci + 1) / 2, hy = (m.ny - cj + 1) / 2, hz = (m.nz - ck + 1) / 2;
-    const int64_t cells = hx * hy * hz;
+    Colour col;
+    col.ci = c & 1;
+    col.cj = (c >> 1) & 1;
+    col.ck = (c >> 2) & 1;
+    col.hx = (m.nx - col.ci + 1) / 2;
+    col.hy = (m.ny - col.cj + 1) / 2;
+    col.hz = (m.nz - col.ck + 1) / 2;
+    const int64_t cells = (int64_t)col.hx * col.hy * col.hz;
     if (cells == 0)
       continue;
     const int64_t grid = std::min<int64_t>((cells + kBatch - 1) / kBatch, q4_grid_limit<T>());
-    k_q4_cells<T><<<(unsigned)grid, 128, 0, s>>>(m, u, y, ci, cj, ck, skip);
+    const int64_t step = kBatch * grid;
+    col.dx = (int)(step % col.hx);
+    col.dy = (int)((step / col.hx) % col.hy);
+    col.dz = (int)(step / ((int64_t)col.hx * col.hy));
+    k_q4_cells<T><<<(unsigned)grid, 128, 0, s>>>(m, u, y, col, skip);
   }
   DFX_CHECK_LAUNCH();
   return DFX_OK;
@@ -518,6 +626,19 @@ template int q4_apply<double>(const dfx_q4_mesh_s&, const double*, double*, cuda
 
 extern "C" int64_t dfx_q4_num_dofs(const dfx_q4_mesh* m) { return m ? dfx::q4_ndofs(*m) : 0; }
 
+extern "C" int dfx_q4_edges(const dfx_q4_mesh* mesh, float* d_edges, void* stream)
+{
+  DFX_REQUIRE(mesh && d_edges, "arguments must be non-NULL");
+  DFX_REQUIRE(mesh->nx > 0 && mesh->ny > 0 && mesh->nz > 0 && mesh->verts, "invalid Q4 mesh");
+  DFX_REQUIRE(((uintptr_t)d_edges & 15) == 0, "edges must be 16-byte aligned");
+  const int64_t cells = (int64_t)mesh->nx * mesh->ny * mesh->nz;
+  const int64_t total = 36 * cells;
+  k_q4_edges<<<(unsigned)((total + 255) / 256), 256, 0, dfx::as_stream(stream)>>>(*mesh, d_edges,
+                                                                                   cells);
+  DFX_CHECK_LAUNCH();
+  return DFX_OK;
+}
+
 extern "C" int dfx_q4_action(const dfx_q4_mesh* mesh, int32_t dtype, const void* d_u, void* d_y,
                              void* stream)
 {
@@ -525,6 +646,7 @@ extern "C" int dfx_q4_action(const dfx_q4_mesh* mesh, int32_t dtype, const void*
   const dfx_q4_mesh_s& m = *mesh;
   DFX_REQUIRE(m.nx > 0 && m.ny > 0 && m.nz > 0 && m.verts, "invalid Q4 mesh");
   DFX_REQUIRE(d_u != d_y, "u and y must differ");
+  DFX_REQUIRE(((uintptr_t)m.edges32 & 15) == 0, "edges32 must be 16-byte aligned");
   cudaStream_t s = dfx::as_stream(stream);
   if (dtype == DFX_F64)
     return dfx::q4_apply<double>(m, (const double*)d_u, (double*)d_y, s);

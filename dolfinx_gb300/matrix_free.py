@@ -90,7 +90,10 @@ class Q4Laplacian:
     identity rows on the boundary. Vertex coordinates stay resident in HBM."""
 
     def __init__(self, verts, nx: int, ny: int | None = None, nz: int | None = None,
-                 kappa: float = 1.0, device="cuda"):
+                 kappa: float = 1.0, device="cuda", cache_edges: bool = True):
+        """cache_edges: keep the cells' FP32 edge vectors in HBM (36 floats
+        per cell) for the FP32 action instead of forming them from the FP64
+        vertices in every application (same results, bitwise)."""
         ny = nx if ny is None else ny
         nz = nx if nz is None else nz
         v = torch.as_tensor(np.ascontiguousarray(verts, np.float64))
@@ -98,8 +101,14 @@ class Q4Laplacian:
         self.verts = v.to(device)
         self.dims = (nx, ny, nz)
         self.kappa = float(kappa)
-        self._mesh = _capi.Q4Mesh(nx, ny, nz, self.verts.data_ptr(), self.kappa)
+        self._mesh = _capi.Q4Mesh(nx, ny, nz, self.verts.data_ptr(), self.kappa, None)
         self.n = int(_capi.lib().dfx_q4_num_dofs(C.byref(self._mesh)))
+        self.edges = None
+        if cache_edges:
+            self.edges = torch.empty(36 * nx * ny * nz, dtype=torch.float32, device=device)
+            _capi.check(_capi.lib().dfx_q4_edges(C.byref(self._mesh), _ptr(self.edges),
+                                                 _stream()))
+            self._mesh.edges32 = self.edges.data_ptr()
 
     def mesh(self):
         return self._mesh

@@ -389,9 +389,16 @@ typedef struct dfx_q4_mesh
   int32_t nx, ny, nz;
   const double* verts;  /* ((nx+1)(ny+1)(nz+1), 3) vertex coordinates */
   double kappa;
+  /* Optional (NULL: formed on the fly): the cells' edge vectors in FP32,
+   * 36 floats per cell, 16-byte aligned, written by dfx_q4_edges. Used by
+   * the FP32 action only; results are bitwise the same either way. */
+  const float* edges32;
 } dfx_q4_mesh;
 
 int64_t dfx_q4_num_dofs(const dfx_q4_mesh* mesh);
+/* Writes the 36 * nx * ny * nz FP32 edge components of dfx_q4_mesh.edges32
+ * (no counterpart in the reference: a cache of per-cell geometry). */
+int dfx_q4_edges(const dfx_q4_mesh* mesh, float* d_edges, void* stream);
 /* y = A u; u, y of `dtype` (DFX_F64 or DFX_F32; FP32 forms the geometry
  * and contractions in FP32 from FP64 vertex differences). */
 int dfx_q4_action(const dfx_q4_mesh* mesh, int32_t dtype, const void* d_u, void* d_y,

@@ -39,6 +39,17 @@ def test_q4_action_f32(cuda, oracle):
     assert_close(y, ref, rtol=2e-5)
 
 
+def test_q4_edge_cache_is_bitwise_neutral(cuda):
+    from dolfinx_gb300 import matrix_free as mf
+
+    dims = (6, 5, 4)
+    v = mf.hex_box_vertices(*dims, perturb=0.05, seed=12)
+    cached = mf.Q4Laplacian(v, *dims, cache_edges=True)
+    plain = mf.Q4Laplacian(v, *dims, cache_edges=False)
+    u = torch.from_numpy(np.random.default_rng(13).standard_normal(cached.n)).float().cuda()
+    assert torch.equal(cached(u), plain(u))
+
+
 def test_q4_action_symmetric_and_deterministic(cuda):
     dims = (8, 8, 8)
     mf, v, op = _setup(dims, seed=5)
