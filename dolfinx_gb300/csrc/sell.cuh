@@ -67,33 +67,104 @@ __device__ __forceinline__ ACC sell_row(const dfx_operator_s& op, const V* __res
   ACC acc = ACC(0);
   if constexpr (sizeof(V) == 4)
   {
+    // Chunks of kChunk pairs: the chunk's value/column loads are issued
+    // together (and the next chunk's before this chunk's gathers), then
+    // all its x gathers, then the FMAs in entry order. Measured on the P2
+    // Poisson operator of a 64^3 x 6 tetrahedral mesh: 79 us against 104 us
+    // for the same loop with loads, gathers and FMAs interleaved.
+    constexpr int kChunk = 4;
     const float2* v = reinterpret_cast<const float2*>(vals + b) + lane;
     const int np = len >> 1;
+    float2 vv[kChunk];
+#pragma unroll
+    for (int u = 0; u < kChunk; ++u)
+      vv[u] = u < np ? __ldcs(v + 32 * u) : make_float2(0.f, 0.f);
     if constexpr (COMP)
     {
       const ushort2* d = reinterpret_cast<const ushort2*>(op.delta + b) + lane;
       int32_t col = __ldg(op.first + 32 * (int64_t)s + lane);
-#pragma unroll 4
-      for (int j = 0; j < np; ++j)
+      ushort2 dd[kChunk];
+#pragma unroll
+      for (int u = 0; u < kChunk; ++u)
+        dd[u] = u < np ? __ldcs(d + 32 * u) : make_ushort2(0, 0);
+      for (int j0 = 0; j0 < np; j0 += kChunk)
       {
-        const float2 vv = __ldcs(v + 32 * j);
-        const ushort2 dd = __ldcs(d + 32 * j);
-        col += dd.x; // delta of entry 0 is stored as 0
-        acc = fma((ACC)vv.x, (ACC)__ldg(x + col), acc);
-        col += dd.y;
-        acc = fma((ACC)vv.y, (ACC)__ldg(x + col), acc);
+        float2 nv[kChunk];
+        ushort2 nd[kChunk];
+#pragma unroll
+        for (int u = 0; u < kChunk; ++u)
+        {
+          const bool ok = j0 + kChunk + u < np;
+          nv[u] = ok ? __ldcs(v + 32 * (j0 + kChunk + u)) : make_float2(0.f, 0.f);
+          nd[u] = ok ? __ldcs(d + 32 * (j0 + kChunk + u)) : make_ushort2(0, 0);
+        }
+        // Padding pairs past np have zero deltas: their gathers repeat a
+        // valid column and their values are zero.
+        int32_t c0[kChunk], c1[kChunk];
+#pragma unroll
+        for (int u = 0; u < kChunk; ++u)
+        {
+          col += dd[u].x; // delta of entry 0 is stored as 0
+          c0[u] = col;
+          col += dd[u].y;
+          c1[u] = col;
+        }
+        X x0[kChunk], x1[kChunk];
+#pragma unroll
+        for (int u = 0; u < kChunk; ++u)
+        {
+          x0[u] = __ldg(x + c0[u]);
+          x1[u] = __ldg(x + c1[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < kChunk; ++u)
+        {
+          if (j0 + u < np)
+          {
+            acc = fma((ACC)vv[u].x, (ACC)x0[u], acc);
+            acc = fma((ACC)vv[u].y, (ACC)x1[u], acc);
+          }
+          vv[u] = nv[u];
+          dd[u] = nd[u];
+        }
       }
     }
     else
     {
       const int2* c = reinterpret_cast<const int2*>(op.cols + b) + lane;
-#pragma unroll 4
-      for (int j = 0; j < np; ++j)
+      int2 cc[kChunk];
+#pragma unroll
+      for (int u = 0; u < kChunk; ++u)
+        cc[u] = u < np ? __ldcs(c + 32 * u) : make_int2(0, 0);
+      for (int j0 = 0; j0 < np; j0 += kChunk)
       {
-        const float2 vv = __ldcs(v + 32 * j);
-        const int2 cc = __ldcs(c + 32 * j);
-        acc = fma((ACC)vv.x, (ACC)__ldg(x + cc.x), acc);
-        acc = fma((ACC)vv.y, (ACC)__ldg(x + cc.y), acc);
+        float2 nv[kChunk];
+        int2 nc[kChunk];
+#pragma unroll
+        for (int u = 0; u < kChunk; ++u)
+        {
+          const bool ok = j0 + kChunk + u < np;
+          nv[u] = ok ? __ldcs(v + 32 * (j0 + kChunk + u)) : make_float2(0.f, 0.f);
+          nc[u] = ok ? __ldcs(c + 32 * (j0 + kChunk + u)) : make_int2(0, 0);
+        }
+        X x0[kChunk], x1[kChunk];
+#pragma unroll
+        for (int u = 0; u < kChunk; ++u)
+        {
+          x0[u] = __ldg(x + cc[u].x);
+          x1[u] = __ldg(x + cc[u].y);
+        }
+#pragma unroll
+        for (int u = 0; u < kChunk; ++u)
+        {
+          if (j0 + u < np)
+          {
+            acc = fma((ACC)vv[u].x, (ACC)x0[u], acc);
+            acc = fma((ACC)vv[u].y, (ACC)x1[u], acc);
+          }
+          vv[u] = nv[u];
+          cc[u] = nc[u];
+        }
       }
     }
   }
