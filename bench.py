@@ -46,9 +46,9 @@ def parse():
     p.add_argument("--inner-rtol", type=float, default=None,
                    help="reliable: residual drop between replacements (0.1); restart: inner rtol")
     p.add_argument("--ir-variant", default="reliable", choices=["reliable", "restart"])
-    p.add_argument("--serving-requests", type=int, default=100,
+    p.add_argument("--serving-requests", type=int, default=64,
                    help="requests of the bounded serving sample (0: skip)")
-    p.add_argument("--serving-nmax", type=int, default=48)
+    p.add_argument("--serving-nmax", type=int, default=96)
     p.add_argument("--no-c3", action="store_true", help="skip the elasticity (c3) sample")
     p.add_argument("--no-c4", action="store_true", help="skip the matrix-free Q4 (c4) sample")
     p.add_argument("--c4-only", action="store_true",
@@ -478,20 +478,35 @@ def c4_sample(n=64, seed=4):
 
 def serving_sample(args):
     """Serving loop on a bounded stream drawn like the serving config (unit
-    cubes, n log-uniform, P1/P2, Helmholtz k2 in [0, 10], lognormal kappa),
-    with n capped at --serving-nmax so that the sample ends in seconds. Two
+    cubes, n log-uniform in [8, 96], P1/P2, Helmholtz k2 in [0, 10],
+    lognormal kappa): --serving-requests requests instead of 10,000. Two
     arrival rates: 200/s (latency) and 5000/s (saturation: solves/s is the
-    capacity), each in FP64 and mixed precision."""
+    capacity), each in FP64 and mixed precision. The structures of every
+    (n, degree) are built once, before the first timed run, and shared by
+    the four runs; the budget keeps all of them resident (no rebuild inside
+    a timed run)."""
+    import time
+
     from dolfinx_gb300 import serving
 
     out = {"requests": args.serving_requests, "n_range": [8, args.serving_nmax], "runs": []}
+    budget = 200e9
+    t0 = time.perf_counter()
+    warm = serving.Server(mode="mixed", hbm_budget=budget)
+    try:
+        warm.prewarm(serving.make_requests(args.serving_requests, 200.0, seed=1,
+                                           n_range=(8, args.serving_nmax)))
+    finally:
+        warm.close()
+    out["structure_setup_s"] = time.perf_counter() - t0
     for rate in (200.0, 5000.0):
         reqs = serving.make_requests(args.serving_requests, rate, seed=1,
                                      n_range=(8, args.serving_nmax))
         res = {}
         for mode in ("fp64", "mixed"):
-            stats, _ = serving.serve(reqs, mode=mode, hbm_budget=64e9, max_wall_s=120.0)
-            res[mode] = {k: stats[k] for k in ("solves_per_s", "p50_ms", "p99_ms", "failed")}
+            stats, _ = serving.serve(reqs, mode=mode, hbm_budget=budget, max_wall_s=120.0)
+            res[mode] = {k: stats[k] for k in ("solves_per_s", "p50_ms", "p99_ms", "dofs_per_s",
+                                               "wall_s", "failed")}
         res["rate"] = rate
         res["mixed_over_fp64_solves"] = res["mixed"]["solves_per_s"] / res["fp64"]["solves_per_s"]
         out["runs"].append(res)
@@ -576,7 +591,8 @@ def run_ours(args):
     clocks = clk.summary()
     ms_max = max_over_ranks(ms)
     value = world * n_dofs / (ms_max * 1e-3) / 1e9
-    rel_err = float((P.x - x64).norm() / x64.norm())
+    x_ir = P.x.clone()
+    rel_err = float((x_ir - x64).norm() / x64.norm())
     launches = int(np.mean([7 + r.kernel_launches for r in res]))
 
     # ---- end to end through the public API with host buffers
@@ -615,6 +631,52 @@ def run_ours(args):
     ach32 = alg32 / (ms32 * 1e-3) / 1e9
     ach64 = alg64 / (ms64k * 1e-3) / 1e9
 
+    # ---- assembly: the matrix cell loop alone (values accumulate into the
+    # resident CSR; the zeroing of the values is not part of the kernel), and
+    # the right-hand side (vector cell loop + lifting + set_bc)
+    from dolfinx_gb300 import _capi as capi_mod
+    import ctypes as C
+
+    masm = P.masm
+    order, off, ncol = masm.colour
+    lib = capi_mod.lib()
+    sptr = C.c_void_p(stream.cuda_stream)
+    form_s, csr_s = masm.form, P.A.csr()
+
+    def matrix_kernel():
+        capi_mod.check(lib.dfx_assemble_matrix(C.byref(form_s), C.byref(csr_s),
+                                               C.c_void_p(masm.map.data_ptr()),
+                                               C.c_void_p(masm.markers.data_ptr()), masm.mode,
+                                               order, off, ncol, sptr))
+
+    rhs = P.rhs
+    r_order, r_off, r_ncol = rhs.colour
+
+    def vector_kernel():
+        capi_mod.check(lib.dfx_assemble_vector(C.byref(rhs.Lc), C.c_void_p(P.b.data_ptr()),
+                                               rhs.mode, r_order, r_off, r_ncol, sptr))
+
+    def lifting_kernel():
+        capi_mod.check(lib.dfx_apply_lifting(C.byref(rhs.ac), C.c_void_p(P.b.data_ptr()),
+                                             C.c_void_p(rhs.markers.data_ptr()),
+                                             C.c_void_p(rhs.g.data_ptr()), None, 1.0, rhs.mode,
+                                             r_order, r_off, r_ncol, sptr))
+
+    ms_asm = _kernel_ms(matrix_kernel, 10, stream)
+    ms_vec = _kernel_ms(vector_kernel, 10, stream)
+    ms_lift = _kernel_ms(lifting_kernel, 10, stream)
+    nc = m.num_cells
+    alg_asm = nc * 16 + m.num_nodes * 24 + nc * 10 * 4 + nc * 8 + nnz * 8
+    P.assemble()  # restore the matrix and vector of this step's inputs
+    ach_asm = alg_asm / (ms_asm * 1e-3) / 1e9
+
+    # ---- accuracy: both solutions against an FP64 solve to rtol 1e-13
+    P.fp64.refresh()
+    x_tight = torch.zeros_like(P.x)
+    res_tight = P.fp64.solve(P.b, x_tight, rtol=1e-13, max_iters=6000, raise_on_fail=False)
+    err_mixed_tight = float((x_ir - x_tight).norm() / x_tight.norm())
+    err_fp64_tight = float((x64 - x_tight).norm() / x_tight.norm())
+
     # ---- c3: elasticity through the same solvers (block CSR expanded)
     c3 = None
     if not args.no_c3:
@@ -647,6 +709,10 @@ def run_ours(args):
                            "outer_iterations": [r.outer_iterations for r in res],
                            "inner_iterations": [r.inner_iterations for r in res],
                            "rel_err_vs_fp64_solution": rel_err,
+                           "rel_err_vs_fp64_rtol_1e-13": err_mixed_tight,
+                           "fp64_plain_rel_err_vs_fp64_rtol_1e-13": err_fp64_tight,
+                           "fp64_rtol_1e-13_iterations": res_tight.iterations,
+                           "fp64_rtol_1e-13_status": res_tight.status,
                            "final_rel_residual_fp64": float(np.sqrt(res[-1].rnorm_sq
                                                                     / res[-1].rnorm0_sq))},
                 "fp64_plain": {"value": world * n_dofs / (ms64 * 1e-3) / 1e9, "unit": UNIT,
@@ -665,6 +731,13 @@ def run_ours(args):
                 "roofline_fp64_operator": {"achieved": ach64, "frac": ach64 / peak,
                                            "alg_bytes_per_launch": alg64, "launch_ms": ms64k,
                                            "traffic": profile_traffic("sell_f64_c2")},
+                "roofline_assembly": {"kernel": "k_cells_matrix<P2> (FP64 atomics, slot map)",
+                                      "achieved": ach_asm, "peak": peak, "unit": "GB/s",
+                                      "frac": ach_asm / peak, "alg_bytes_per_launch": alg_asm,
+                                      "launch_ms": ms_asm, "cells_per_s": nc / (ms_asm * 1e-3),
+                                      "traffic": profile_traffic("assemble_p2_c2"),
+                                      "bound": "fp64 pipe and L2 atomics (ncu), not hbm"},
+                "assemble_vector_ms": ms_vec, "apply_lifting_ms": ms_lift,
                 "c3_elasticity": c3,
                 "c4_matrix_free_q4": c4,
                 "serving": serving_out,

@@ -235,16 +235,44 @@ __device__ __forceinline__ void element_tensors(const dfx_form& a, const int32_t
   }
 }
 
-// Matrix assembly (LIFT = false) or lifting (LIFT = true) over a list of
-// cells (list == nullptr: cells [0, count)).
-template <int DEG, bool ELAST, bool MASS, bool COLOURED, bool LIFT>
+// Lifting rows of the nloc element tensors in sA
+// (fem/assemble_vector_impl.h:377-402): thread per element row,
+// b[r] -= alpha * sum_c Ae[r,c] (g[c] - x0[c]) over constrained columns c.
+template <int DEG, bool ELAST, bool COLOURED>
+__device__ __forceinline__ void lift_rows(const double* sA, const int32_t* sDof, const int8_t* sBc,
+                                          const int8_t* sActive, int nloc,
+                                          const double* __restrict__ g,
+                                          const double* __restrict__ x0, double alpha,
+                                          double* __restrict__ b)
+{
+  using T = Traits<DEG, ELAST>;
+  constexpr int ND = T::ND, BS = T::BS, N = T::N, NU = T::NU;
+  for (int e = threadIdx.x; e < nloc * N; e += blockDim.x)
+  {
+    const int cl = e / N, I = e % N;
+    if (!sActive[cl])
+      continue;
+    double acc = 0.0;
+    for (int J = 0; J < N; ++J)
+    {
+      if (!sBc[cl * N + J])
+        continue;
+      const int64_t jj = (int64_t)BS * sDof[cl * ND + J / BS] + J % BS;
+      const double gv = g[jj] - (x0 ? x0[jj] : 0.0);
+      acc += sA[cl * NU + (I <= J ? packed(I, J, N) : packed(J, I, N))] * gv;
+    }
+    if (acc != 0.0)
+      scatter_add<COLOURED>(b + (int64_t)BS * sDof[cl * ND + I / BS] + I % BS, -alpha * acc);
+  }
+}
+
+// Matrix assembly over a list of cells (list == nullptr: cells [0, count)).
+template <int DEG, bool ELAST, bool MASS, bool COLOURED>
 __global__ void __launch_bounds__(kThreads)
     k_cells_matrix(const dfx_form a, const int64_t* __restrict__ row_ptr,
                    const int32_t* __restrict__ cols, double* __restrict__ vals,
                    const uint8_t* __restrict__ map, const int8_t* __restrict__ bc,
-                   const double* __restrict__ g, const double* __restrict__ x0, double alpha,
-                   double* __restrict__ b, const int32_t* __restrict__ list, int32_t count,
-                   int* __restrict__ status)
+                   const int32_t* __restrict__ list, int32_t count, int* __restrict__ status)
 {
   using T = Traits<DEG, ELAST>;
   constexpr int ND = T::ND, BS = T::BS, N = T::N, NU = T::NU, CPB = T::CPB;
@@ -263,7 +291,7 @@ __global__ void __launch_bounds__(kThreads)
   if (threadIdx.x < nloc)
   {
     sCell[threadIdx.x] = list ? __ldg(list + base + threadIdx.x) : (int32_t)(base + threadIdx.x);
-    sActive[threadIdx.x] = LIFT ? 0 : 1;
+    sActive[threadIdx.x] = 1;
   }
   __syncthreads();
   for (int t = threadIdx.x; t < nloc * ND; t += blockDim.x)
@@ -271,70 +299,131 @@ __global__ void __launch_bounds__(kThreads)
     const int cl = t / ND, i = t % ND;
     const int32_t d = __ldg(a.dofmap + (int64_t)sCell[cl] * ND + i);
     sDof[t] = d;
-    if (!LIFT)
-      sRow[t] = __ldg(row_ptr + d);
-    bool any = false;
+    sRow[t] = __ldg(row_ptr + d);
 #pragma unroll
     for (int k = 0; k < BS; ++k)
-    {
-      const int8_t m = bc ? __ldg(bc + (int64_t)BS * d + k) : 0;
-      sBc[cl * N + BS * i + k] = m;
-      any |= (m != 0);
-    }
-    if (LIFT && any)
-      sActive[cl] = 1; // benign race: every writer stores 1
+      sBc[cl * N + BS * i + k] = bc ? __ldg(bc + (int64_t)BS * d + k) : 0;
   }
   __syncthreads();
   element_tensors<DEG, ELAST, MASS>(a, sCell, sActive, nloc, sA, sScratch);
 
-  if constexpr (!LIFT)
+  // Stage 2: scatter Ae into the CSR values, BC rows/columns zeroed
+  // (fem/assemble_matrix_impl.h:161-196).
+  constexpr int NN = ND * ND;
+  for (int e = threadIdx.x; e < nloc * N * N; e += blockDim.x)
   {
-    // Stage 2: scatter Ae into the CSR values, BC rows/columns zeroed
-    // (fem/assemble_matrix_impl.h:161-196).
-    constexpr int NN = ND * ND;
-    for (int e = threadIdx.x; e < nloc * N * N; e += blockDim.x)
+    const int cl = e / (N * N), IJ = e % (N * N), I = IJ / N, J = IJ % N;
+    if (sBc[cl * N + I] | sBc[cl * N + J])
+      continue;
+    const int i = I / BS, j = J / BS, k = I % BS, l = J % BS;
+    const double v = sA[cl * NU + (I <= J ? packed(I, J, N) : packed(J, I, N))];
+    int64_t pos;
+    if (map)
+      pos = sRow[cl * ND + i] + map[(int64_t)sCell[cl] * NN + i * ND + j];
+    else
     {
-      const int cl = e / (N * N), IJ = e % (N * N), I = IJ / N, J = IJ % N;
-      if (sBc[cl * N + I] | sBc[cl * N + J])
-        continue;
-      const int i = I / BS, j = J / BS, k = I % BS, l = J % BS;
-      const double v = sA[cl * NU + (I <= J ? packed(I, J, N) : packed(J, I, N))];
-      int64_t pos;
-      if (map)
-        pos = sRow[cl * ND + i] + map[(int64_t)sCell[cl] * NN + i * ND + j];
-      else
+      const int32_t di = sDof[cl * ND + i];
+      const int64_t rb = sRow[cl * ND + i], re = __ldg(row_ptr + di + 1);
+      pos = row_search(cols, rb, re, sDof[cl * ND + j]);
+      if (pos >= re || __ldg(cols + pos) != sDof[cl * ND + j])
       {
-        const int32_t di = sDof[cl * ND + i];
-        const int64_t rb = sRow[cl * ND + i], re = __ldg(row_ptr + di + 1);
-        pos = row_search(cols, rb, re, sDof[cl * ND + j]);
-        if (pos >= re || __ldg(cols + pos) != sDof[cl * ND + j])
-        {
-          atomicExch(status, (int)DFX_ERR_NOT_IN_SPARSITY);
-          continue;
-        }
+        atomicExch(status, (int)DFX_ERR_NOT_IN_SPARSITY);
+        continue;
       }
-      scatter_add<COLOURED>(vals + pos * (BS * BS) + k * BS + l, v);
     }
+    scatter_add<COLOURED>(vals + pos * (BS * BS) + k * BS + l, v);
   }
-  else
+}
+
+// Lifting with the constrained cells compacted inside the block. Only cells
+// with a constrained dof contribute (fem/assemble_vector_impl.h:377-384 skips
+// the others), and RCM order spreads them over the whole cell range, so a
+// launch with one element-kernel thread per cell would run the FP64 element
+// code in nearly every warp. Each block scans kLiftRange cells of the range
+// (or of `list`), appends the constrained ones to a shared queue in scan
+// order, and runs the element kernel on full batches of CPB queued cells.
+constexpr int kLiftRange = 2048;
+
+template <int DEG, bool ELAST, bool MASS, bool COLOURED>
+__global__ void __launch_bounds__(kThreads)
+    k_cells_lift(const dfx_form a, const int8_t* __restrict__ bc, const double* __restrict__ g,
+                 const double* __restrict__ x0, double alpha, double* __restrict__ b,
+                 const int32_t* __restrict__ list, int32_t count)
+{
+  using T = Traits<DEG, ELAST>;
+  constexpr int ND = T::ND, BS = T::BS, N = T::N, NU = T::NU, CPB = T::CPB;
+  constexpr int kWarps = kThreads / 32;
+  __shared__ double sA[CPB * NU];
+  __shared__ double sScratch[ELAST ? CPB * 132 : 1];
+  __shared__ int32_t sCell[CPB];
+  __shared__ int32_t sDof[CPB * ND];
+  __shared__ int8_t sBc[CPB * N];
+  __shared__ int8_t sActive[CPB];
+  __shared__ int32_t sQueue[kThreads + CPB];
+  __shared__ int32_t sWarpCount[kWarps];
+
+  const int64_t begin = (int64_t)blockIdx.x * kLiftRange;
+  const int64_t end = min((int64_t)count, begin + kLiftRange);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  int queued = 0; // block-uniform
+  for (int64_t c0 = begin; c0 < end; c0 += kThreads)
   {
-    // Lifting (fem/assemble_vector_impl.h:377-402): thread per element row.
-    for (int e = threadIdx.x; e < nloc * N; e += blockDim.x)
+    const int64_t idx = c0 + threadIdx.x;
+    int32_t cell = 0;
+    bool constrained = false;
+    if (idx < end)
     {
-      const int cl = e / N, I = e % N;
-      if (!sActive[cl])
-        continue;
-      double acc = 0.0;
-      for (int J = 0; J < N; ++J)
+      cell = list ? __ldg(list + idx) : (int32_t)idx;
+      const int32_t* dofs = a.dofmap + (int64_t)cell * ND;
+#pragma unroll
+      for (int i = 0; i < ND; ++i)
       {
-        if (!sBc[cl * N + J])
-          continue;
-        const int64_t jj = (int64_t)BS * sDof[cl * ND + J / BS] + J % BS;
-        const double gv = g[jj] - (x0 ? x0[jj] : 0.0);
-        acc += sA[cl * NU + (I <= J ? packed(I, J, N) : packed(J, I, N))] * gv;
+        const int64_t d = __ldg(dofs + i);
+#pragma unroll
+        for (int k = 0; k < BS; ++k)
+          constrained |= __ldg(bc + BS * d + k) != 0;
       }
-      if (acc != 0.0)
-        scatter_add<COLOURED>(b + (int64_t)BS * sDof[cl * ND + I / BS] + I % BS, -alpha * acc);
+    }
+    // Append in scan order: warp ballots, then warp offsets.
+    const unsigned ballot = __ballot_sync(0xffffffffu, constrained);
+    if (lane == 0)
+      sWarpCount[warp] = __popc(ballot);
+    __syncthreads();
+    int off = queued;
+    for (int w = 0; w < warp; ++w)
+      off += sWarpCount[w];
+    int added = 0;
+#pragma unroll
+    for (int w = 0; w < kWarps; ++w)
+      added += sWarpCount[w];
+    if (constrained)
+      sQueue[off + __popc(ballot & ((1u << lane) - 1u))] = cell;
+    queued += added;
+    __syncthreads();
+    const bool last = c0 + kThreads >= end;
+    while (queued >= CPB || (last && queued > 0))
+    {
+      const int nloc = queued < CPB ? queued : CPB;
+      queued -= nloc;
+      if (threadIdx.x < nloc)
+      {
+        sCell[threadIdx.x] = sQueue[queued + threadIdx.x];
+        sActive[threadIdx.x] = 1;
+      }
+      __syncthreads();
+      for (int t = threadIdx.x; t < nloc * ND; t += blockDim.x)
+      {
+        const int cl = t / ND, i = t % ND;
+        const int32_t d = __ldg(a.dofmap + (int64_t)sCell[cl] * ND + i);
+        sDof[t] = d;
+#pragma unroll
+        for (int k = 0; k < BS; ++k)
+          sBc[cl * N + BS * i + k] = __ldg(bc + (int64_t)BS * d + k);
+      }
+      __syncthreads();
+      element_tensors<DEG, ELAST, MASS>(a, sCell, sActive, nloc, sA, sScratch);
+      lift_rows<DEG, ELAST, COLOURED>(sA, sDof, sBc, sActive, nloc, g, x0, alpha, b);
+      __syncthreads();
     }
   }
 }
@@ -502,47 +591,73 @@ int read_status(int* status, cudaStream_t s)
   return h;
 }
 
-// Launch the matrix/lifting kernel for one cell list.
-template <int DEG, bool ELAST, bool MASS, bool COLOURED, bool LIFT>
+// Launch the matrix kernel for one cell list.
+template <int DEG, bool ELAST, bool MASS, bool COLOURED>
 void launch_cells(const dfx_form& a, const dfx_csr* A, const uint8_t* map, const int8_t* bc,
-                  const double* g, const double* x0, double alpha, double* b,
                   const int32_t* list, int32_t count, int* status, cudaStream_t s)
 {
   constexpr int CPB = Traits<DEG, ELAST>::CPB;
   if (count <= 0)
     return;
   const unsigned grid = (unsigned)((count + CPB - 1) / CPB);
-  k_cells_matrix<DEG, ELAST, MASS, COLOURED, LIFT><<<grid, kThreads, 0, s>>>(
-      a, A ? A->row_ptr : nullptr, A ? A->cols : nullptr, A ? (double*)A->vals : nullptr, map, bc,
-      g, x0, alpha, b, list, count, status);
+  k_cells_matrix<DEG, ELAST, MASS, COLOURED><<<grid, kThreads, 0, s>>>(
+      a, A->row_ptr, A->cols, (double*)A->vals, map, bc, list, count, status);
 }
 
-template <bool COLOURED, bool LIFT>
+template <bool COLOURED>
 void dispatch_cells(const dfx_form& a, const dfx_csr* A, const uint8_t* map, const int8_t* bc,
-                    const double* g, const double* x0, double alpha, double* b,
                     const int32_t* list, int32_t count, int* status, cudaStream_t s)
 {
   const bool mass = a.kind == DFX_FORM_POISSON && a.k2 != 0.0;
   if (a.kind == DFX_FORM_ELASTICITY)
-    launch_cells<2, true, false, COLOURED, LIFT>(a, A, map, bc, g, x0, alpha, b, list, count,
-                                                 status, s);
+    launch_cells<2, true, false, COLOURED>(a, A, map, bc, list, count, status, s);
   else if (a.degree == 1)
   {
     if (mass)
-      launch_cells<1, false, true, COLOURED, LIFT>(a, A, map, bc, g, x0, alpha, b, list, count,
-                                                   status, s);
+      launch_cells<1, false, true, COLOURED>(a, A, map, bc, list, count, status, s);
     else
-      launch_cells<1, false, false, COLOURED, LIFT>(a, A, map, bc, g, x0, alpha, b, list, count,
-                                                    status, s);
+      launch_cells<1, false, false, COLOURED>(a, A, map, bc, list, count, status, s);
   }
   else
   {
     if (mass)
-      launch_cells<2, false, true, COLOURED, LIFT>(a, A, map, bc, g, x0, alpha, b, list, count,
-                                                   status, s);
+      launch_cells<2, false, true, COLOURED>(a, A, map, bc, list, count, status, s);
     else
-      launch_cells<2, false, false, COLOURED, LIFT>(a, A, map, bc, g, x0, alpha, b, list, count,
-                                                    status, s);
+      launch_cells<2, false, false, COLOURED>(a, A, map, bc, list, count, status, s);
+  }
+}
+
+template <int DEG, bool ELAST, bool MASS, bool COLOURED>
+void launch_lift(const dfx_form& a, const int8_t* bc, const double* g, const double* x0,
+                 double alpha, double* b, const int32_t* list, int32_t count, cudaStream_t s)
+{
+  if (count <= 0)
+    return;
+  const unsigned grid = (unsigned)((count + kLiftRange - 1) / kLiftRange);
+  k_cells_lift<DEG, ELAST, MASS, COLOURED><<<grid, kThreads, 0, s>>>(a, bc, g, x0, alpha, b, list,
+                                                                    count);
+}
+
+template <bool COLOURED>
+void dispatch_lift(const dfx_form& a, const int8_t* bc, const double* g, const double* x0,
+                   double alpha, double* b, const int32_t* list, int32_t count, cudaStream_t s)
+{
+  const bool mass = a.kind == DFX_FORM_POISSON && a.k2 != 0.0;
+  if (a.kind == DFX_FORM_ELASTICITY)
+    launch_lift<2, true, false, COLOURED>(a, bc, g, x0, alpha, b, list, count, s);
+  else if (a.degree == 1)
+  {
+    if (mass)
+      launch_lift<1, false, true, COLOURED>(a, bc, g, x0, alpha, b, list, count, s);
+    else
+      launch_lift<1, false, false, COLOURED>(a, bc, g, x0, alpha, b, list, count, s);
+  }
+  else
+  {
+    if (mass)
+      launch_lift<2, false, true, COLOURED>(a, bc, g, x0, alpha, b, list, count, s);
+    else
+      launch_lift<2, false, false, COLOURED>(a, bc, g, x0, alpha, b, list, count, s);
   }
 }
 
@@ -599,15 +714,13 @@ extern "C" int dfx_assemble_matrix(const dfx_form* a, const dfx_csr* A, const ui
   if (!d_map)
     DFX_CUDA(cudaMemsetAsync(status, 0, sizeof(int), s));
   if (mode == DFX_MODE_ATOMIC)
-    dispatch_cells<false, false>(*a, A, d_map, d_bc, nullptr, nullptr, 0.0, nullptr, nullptr,
-                                 a->num_cells, status, s);
+    dispatch_cells<false>(*a, A, d_map, d_bc, nullptr, a->num_cells, status, s);
   else if (mode == DFX_MODE_COLOURED)
   {
     DFX_REQUIRE(d_order && colour_offsets && num_colours > 0, "coloured mode needs a colouring");
     for (int k = 0; k < num_colours; ++k)
-      dispatch_cells<true, false>(*a, A, d_map, d_bc, nullptr, nullptr, 0.0, nullptr,
-                                  d_order + colour_offsets[k],
-                                  colour_offsets[k + 1] - colour_offsets[k], status, s);
+      dispatch_cells<true>(*a, A, d_map, d_bc, d_order + colour_offsets[k],
+                           colour_offsets[k + 1] - colour_offsets[k], status, s);
   }
   else
     return dfx::fail(DFX_ERR_INVALID, "unknown assembly mode %d", mode);
@@ -629,15 +742,13 @@ extern "C" int dfx_apply_lifting(const dfx_form* a, double* d_b, const int8_t* d
     return DFX_OK;
   cudaStream_t s = dfx::as_stream(stream);
   if (mode == DFX_MODE_ATOMIC)
-    dispatch_cells<false, true>(*a, nullptr, nullptr, d_bc, d_g, d_x0, alpha, d_b, nullptr,
-                                a->num_cells, nullptr, s);
+    dispatch_lift<false>(*a, d_bc, d_g, d_x0, alpha, d_b, nullptr, a->num_cells, s);
   else if (mode == DFX_MODE_COLOURED)
   {
     DFX_REQUIRE(d_order && colour_offsets && num_colours > 0, "coloured mode needs a colouring");
     for (int k = 0; k < num_colours; ++k)
-      dispatch_cells<true, true>(*a, nullptr, nullptr, d_bc, d_g, d_x0, alpha, d_b,
-                                 d_order + colour_offsets[k],
-                                 colour_offsets[k + 1] - colour_offsets[k], nullptr, s);
+      dispatch_lift<true>(*a, d_bc, d_g, d_x0, alpha, d_b, d_order + colour_offsets[k],
+                          colour_offsets[k + 1] - colour_offsets[k], s);
   }
   else
     return dfx::fail(DFX_ERR_INVALID, "unknown assembly mode %d", mode);

@@ -459,9 +459,81 @@ __global__ void __launch_bounds__(kSellThreads)
   finish_pap(publish<T>(dot, T(0), w.red, &w.st->ticket[1], false), w.st);
 }
 
+// 16-byte vectors of the elementwise kernels.
+template <typename T>
+struct Vec16;
+template <>
+struct Vec16<float>
+{
+  using type = float4;
+  static constexpr int N = 4;
+};
+template <>
+struct Vec16<double>
+{
+  using type = double2;
+  static constexpr int N = 2;
+};
+
+// State update of the last warp of k_update: convergence test, beta, and
+// (reliable updates) the decision to pause for a residual replacement.
+template <bool RELIABLE>
+__device__ __forceinline__ void update_finish(const WarpFinal& f, CgState* st)
+{
+  if (!f.last || (threadIdx.x & 31) != 0)
+    return;
+  const double srr = f.s0, srz = f.s1;
+  st->rr = srr;
+  st->iter += 1;
+  bool pause = false;
+  if (srr / st->rr0 < st->rtol2)
+  {
+    st->done = 1;
+    if (RELIABLE)
+    {
+      st->status = kPauseConverged;
+      pause = true;
+    }
+  }
+  else if (!isfinite(srr))
+  {
+    st->status = DFX_ERR_BREAKDOWN;
+    st->done = 1;
+  }
+  else if (st->iter >= st->max_iter)
+  {
+    st->status = DFX_ERR_NOT_CONVERGED;
+    st->done = 1;
+  }
+  else if (RELIABLE
+           && (srr < st->delta2 * st->rmax2 || (st->forced > 0 && st->since + 1 >= st->forced)))
+  {
+    st->status = kPauseUpdate;
+    st->done = 1;
+    pause = true;
+  }
+  if (RELIABLE)
+    st->since = pause ? 0 : st->since + 1;
+  // A pause keeps rz = r_old.z_old: beta is formed after the residual
+  // has been replaced.
+  if (!pause)
+  {
+    st->beta = srz / st->rz;
+    st->rz = srz;
+    if (RELIABLE)
+      st->rmax2 = fmax(st->rmax2, srr);
+  }
+  st->ticket[2] = 0;
+  __threadfence();
+}
+
+// x += alpha p, r -= alpha y, r.r and r.z (z = D^{-1} r). vec: every array
+// is 16-byte aligned, and a thread moves 16 bytes per array and round over
+// a grid of one resident wave; otherwise 4 scalar entries per thread and
+// round.
 template <typename T, bool PRE, bool RELIABLE>
 __global__ void __launch_bounds__(kElemThreads)
-    k_update(T* __restrict__ x, const T* __restrict__ dinv, int64_t n, Work<T> w)
+    k_update(T* __restrict__ x, const T* __restrict__ dinv, int64_t n, Work<T> w, bool vec)
 {
   block_reduce_init();
 
@@ -469,96 +541,118 @@ __global__ void __launch_bounds__(kElemThreads)
     return;
   const T alpha = (T)__ldg(&w.st->alpha);
   T rr = 0, rz = 0;
-  constexpr int E = kElemPerThread;
-  const int64_t stride = (int64_t)gridDim.x * kElemThreads * E;
-  for (int64_t base = (int64_t)blockIdx.x * kElemThreads * E + threadIdx.x; base < n;
-       base += stride)
+  if (vec)
   {
-    T p[E], y[E], r[E], xv[E], d[E];
-#pragma unroll
-    for (int e = 0; e < E; ++e)
+    using V = typename Vec16<T>::type;
+    constexpr int L = Vec16<T>::N;
+    const int64_t nvec = n / L;
+    const int64_t stride = (int64_t)gridDim.x * kElemThreads;
+    for (int64_t v = (int64_t)blockIdx.x * kElemThreads + threadIdx.x; v < nvec; v += stride)
     {
-      const int64_t i = base + (int64_t)e * kElemThreads;
-      const bool ok = i < n;
-      p[e] = ok ? w.p[i] : T(0);
-      y[e] = ok ? w.y[i] : T(0);
-      r[e] = ok ? w.r[i] : T(0);
-      xv[e] = ok ? x[i] : T(0);
-      d[e] = (ok && PRE) ? dinv[i] : T(1);
+      V pv = reinterpret_cast<const V*>(w.p)[v];
+      V yv = reinterpret_cast<const V*>(w.y)[v];
+      V rv = reinterpret_cast<const V*>(w.r)[v];
+      V xv = reinterpret_cast<const V*>(x)[v];
+      V dv = pv;
+      if (PRE)
+        dv = reinterpret_cast<const V*>(dinv)[v];
+      const T* pe = reinterpret_cast<const T*>(&pv);
+      const T* ye = reinterpret_cast<const T*>(&yv);
+      const T* de = reinterpret_cast<const T*>(&dv);
+      T* re = reinterpret_cast<T*>(&rv);
+      T* xe = reinterpret_cast<T*>(&xv);
+#pragma unroll
+      for (int e = 0; e < L; ++e)
+      {
+        xe[e] = xe[e] + alpha * pe[e];
+        const T rn = re[e] - alpha * ye[e];
+        re[e] = rn;
+        rr += rn * rn;
+        rz += rn * (PRE ? de[e] * rn : rn);
+      }
+      reinterpret_cast<V*>(x)[v] = xv;
+      reinterpret_cast<V*>(w.r)[v] = rv;
     }
-#pragma unroll
-    for (int e = 0; e < E; ++e)
+    if (blockIdx.x == 0)
+      for (int64_t i = nvec * L + threadIdx.x; i < n; i += kElemThreads)
+      {
+        x[i] = x[i] + alpha * w.p[i];
+        const T rn = w.r[i] - alpha * w.y[i];
+        w.r[i] = rn;
+        rr += rn * rn;
+        rz += rn * (PRE ? dinv[i] * rn : rn);
+      }
+  }
+  else
+  {
+    constexpr int E = kElemPerThread;
+    const int64_t stride = (int64_t)gridDim.x * kElemThreads * E;
+    for (int64_t base = (int64_t)blockIdx.x * kElemThreads * E + threadIdx.x; base < n;
+         base += stride)
     {
-      const int64_t i = base + (int64_t)e * kElemThreads;
-      if (i >= n)
-        continue;
-      x[i] = xv[e] + alpha * p[e];
-      const T rn = r[e] - alpha * y[e];
-      w.r[i] = rn;
-      rr += rn * rn;
-      rz += rn * (PRE ? d[e] * rn : rn);
+      T p[E], y[E], r[E], xv[E], d[E];
+#pragma unroll
+      for (int e = 0; e < E; ++e)
+      {
+        const int64_t i = base + (int64_t)e * kElemThreads;
+        const bool ok = i < n;
+        p[e] = ok ? w.p[i] : T(0);
+        y[e] = ok ? w.y[i] : T(0);
+        r[e] = ok ? w.r[i] : T(0);
+        xv[e] = ok ? x[i] : T(0);
+        d[e] = (ok && PRE) ? dinv[i] : T(1);
+      }
+#pragma unroll
+      for (int e = 0; e < E; ++e)
+      {
+        const int64_t i = base + (int64_t)e * kElemThreads;
+        if (i >= n)
+          continue;
+        x[i] = xv[e] + alpha * p[e];
+        const T rn = r[e] - alpha * y[e];
+        w.r[i] = rn;
+        rr += rn * rn;
+        rz += rn * (PRE ? d[e] * rn : rn);
+      }
     }
   }
-  const WarpFinal f = publish<T>(rr, rz, w.red, &w.st->ticket[2], true);
-  if (f.last)
-  {
-    const double srr = f.s0, srz = f.s1;
-    if ((threadIdx.x & 31) == 0)
-    {
-      CgState* st = w.st;
-      st->rr = srr;
-      st->iter += 1;
-      bool pause = false;
-      if (srr / st->rr0 < st->rtol2)
-      {
-        st->done = 1;
-        if (RELIABLE)
-        {
-          st->status = kPauseConverged;
-          pause = true;
-        }
-      }
-      else if (!isfinite(srr))
-      {
-        st->status = DFX_ERR_BREAKDOWN;
-        st->done = 1;
-      }
-      else if (st->iter >= st->max_iter)
-      {
-        st->status = DFX_ERR_NOT_CONVERGED;
-        st->done = 1;
-      }
-      else if (RELIABLE
-               && (srr < st->delta2 * st->rmax2 || (st->forced > 0 && st->since + 1 >= st->forced)))
-      {
-        st->status = kPauseUpdate;
-        st->done = 1;
-        pause = true;
-      }
-      if (RELIABLE)
-        st->since = pause ? 0 : st->since + 1;
-      // A pause keeps rz = r_old.z_old: beta is formed after the residual
-      // has been replaced.
-      if (!pause)
-      {
-        st->beta = srz / st->rz;
-        st->rz = srz;
-        if (RELIABLE)
-          st->rmax2 = fmax(st->rmax2, srr);
-      }
-      st->ticket[2] = 0;
-      __threadfence();
-    }
-  }
+  update_finish<RELIABLE>(publish<T>(rr, rz, w.red, &w.st->ticket[2], true), w.st);
 }
 
+// p = z + beta p with z = D^{-1} r (vec: as in k_update).
 template <typename T, bool PRE>
 __global__ void __launch_bounds__(kElemThreads)
-    k_pupdate(const T* __restrict__ dinv, int64_t n, Work<T> w)
+    k_pupdate(const T* __restrict__ dinv, int64_t n, Work<T> w, bool vec)
 {
   if (is_done(w.st))
     return;
   const T beta = (T)__ldg(&w.st->beta);
+  if (vec)
+  {
+    using V = typename Vec16<T>::type;
+    constexpr int L = Vec16<T>::N;
+    const int64_t nvec = n / L;
+    const int64_t stride = (int64_t)gridDim.x * kElemThreads;
+    for (int64_t v = (int64_t)blockIdx.x * kElemThreads + threadIdx.x; v < nvec; v += stride)
+    {
+      V pv = reinterpret_cast<const V*>(w.p)[v];
+      V rv = reinterpret_cast<const V*>(w.r)[v];
+      V dv = rv;
+      if (PRE)
+        dv = reinterpret_cast<const V*>(dinv)[v];
+      T* pe = reinterpret_cast<T*>(&pv);
+      const T* re = reinterpret_cast<const T*>(&rv);
+      const T* de = reinterpret_cast<const T*>(&dv);
+#pragma unroll
+      for (int e = 0; e < L; ++e)
+        pe[e] = (PRE ? de[e] * re[e] : re[e]) + beta * pe[e];
+      reinterpret_cast<V*>(w.p)[v] = pv;
+    }
+    if (blockIdx.x == 0)
+      for (int64_t i = nvec * L + threadIdx.x; i < n; i += kElemThreads)
+        w.p[i] = (PRE ? dinv[i] * w.r[i] : w.r[i]) + beta * w.p[i];
+    return;
+  }
   constexpr int E = kElemPerThread;
   const int64_t stride = (int64_t)gridDim.x * kElemThreads * E;
   for (int64_t base = (int64_t)blockIdx.x * kElemThreads * E + threadIdx.x; base < n;
@@ -852,14 +946,50 @@ void enqueue_spmv_dot<float>(const OpRef& o, const Work<float>& w, cudaStream_t 
     k_spmv_dot_sell<float, float, false><<<sell_blocks(o.op->n), kSellThreads, 0, s>>>(*o.op, w);
 }
 
+bool aligned16(const void* p) { return ((uintptr_t)p & 15) == 0; }
+
+// Vectorised elementwise launch: 16-byte loads when every array allows it,
+// over one wave of resident blocks (at most 8 per SM with 256 threads, so
+// within max_blocks); the scalar path otherwise.
+template <typename T, typename Kern>
+int elementwise_grid(Kern kernel, int64_t n, bool vec)
+{
+  if (!vec)
+    return elem_grid(n);
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kElemThreads, 0)
+          != cudaSuccess
+      || per_sm < 1)
+    per_sm = 1;
+  const int64_t need = std::max<int64_t>(
+      1, (n / Vec16<T>::N + kElemThreads - 1) / kElemThreads);
+  return (int)std::min<int64_t>(need, (int64_t)std::min(per_sm, 8) * dfx::num_sms());
+}
+
+template <typename T>
+bool vector_ok(const T* x, const T* dinv, const Work<T>& w)
+{
+  return aligned16(x) && (!dinv || aligned16(dinv)) && aligned16(w.p) && aligned16(w.r)
+         && aligned16(w.y);
+}
+
 template <typename T>
 void enqueue_pupdate(const T* dinv, int64_t n, const Work<T>& w, cudaStream_t s)
 {
-  const int g = elem_grid(n);
+  const bool vec = vector_ok<T>(w.p, dinv, w);
   if (dinv)
-    k_pupdate<T, true><<<g, kElemThreads, 0, s>>>(dinv, n, w);
+    k_pupdate<T, true><<<elementwise_grid<T>(k_pupdate<T, true>, n, vec), kElemThreads, 0, s>>>(
+        dinv, n, w, vec);
   else
-    k_pupdate<T, false><<<g, kElemThreads, 0, s>>>(dinv, n, w);
+    k_pupdate<T, false><<<elementwise_grid<T>(k_pupdate<T, false>, n, vec), kElemThreads, 0,
+                          s>>>(dinv, n, w, vec);
+}
+
+template <typename T, bool PRE, bool RELIABLE>
+void launch_update(T* x, const T* dinv, int64_t n, const Work<T>& w, bool vec, cudaStream_t s)
+{
+  const int g = elementwise_grid<T>(k_update<T, PRE, RELIABLE>, n, vec);
+  k_update<T, PRE, RELIABLE><<<g, kElemThreads, 0, s>>>(x, dinv, n, w, vec);
 }
 
 template <typename T>
@@ -874,20 +1004,20 @@ void enqueue_iteration(const OpRef& o, T* x, const T* dinv, int64_t n, const Wor
   }
   else
     enqueue_spmv_dot<T>(o, w, s);
-  const int g = elem_grid(n);
+  const bool vec = vector_ok<T>(x, dinv, w);
   if (dinv)
   {
     if (reliable)
-      k_update<T, true, true><<<g, kElemThreads, 0, s>>>(x, dinv, n, w);
+      launch_update<T, true, true>(x, dinv, n, w, vec, s);
     else
-      k_update<T, true, false><<<g, kElemThreads, 0, s>>>(x, dinv, n, w);
+      launch_update<T, true, false>(x, dinv, n, w, vec, s);
   }
   else
   {
     if (reliable)
-      k_update<T, false, true><<<g, kElemThreads, 0, s>>>(x, dinv, n, w);
+      launch_update<T, false, true>(x, dinv, n, w, vec, s);
     else
-      k_update<T, false, false><<<g, kElemThreads, 0, s>>>(x, dinv, n, w);
+      launch_update<T, false, false>(x, dinv, n, w, vec, s);
   }
   enqueue_pupdate<T>(dinv, n, w, s);
 }

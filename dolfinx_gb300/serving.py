@@ -71,11 +71,16 @@ def make_requests(count: int, rate: float, seed: int = 0, n_range=(8, 96)) -> li
     return out
 
 
-def request_inputs(msh: mesh.Mesh, seed: int):
-    rng = np.random.default_rng(seed)
-    kappa = np.exp(rng.normal(0.0, 1.0, msh.num_cells))
-    f = rng.uniform(-1.0, 1.0, msh.num_nodes)
-    return kappa, f
+def request_inputs(msh: mesh.Mesh, seed: int, device="cuda"):
+    """kappa ~ lognormal(0, 1) per cell and f ~ U[-1, 1] per P1 node, drawn on
+    the device from the request's seed (on the current stream), so that a
+    request costs the host no sampling and no host->device copy of its
+    fields. The same seed gives the same fields, alone or in any mix."""
+    g = torch.Generator(device=device)
+    g.manual_seed(int(seed))
+    kappa = torch.randn(msh.num_cells, dtype=torch.float64, device=device, generator=g).exp_()
+    f = torch.rand(msh.num_nodes, dtype=torch.float64, device=device, generator=g)
+    return kappa, f.mul_(2.0).sub_(1.0)
 
 
 def _stream_ptr(s):
@@ -116,16 +121,42 @@ class Structure:
                 + self.mesh.num_nodes * 8 + int(_capi.lib().dfx_ir_workspace_bytes(n)))
 
 
+# Structures built in this process, shared by every server: a server counts
+# the ones it uses against its own HBM budget, and an eviction drops the
+# structure from this cache too, so that its memory is returned.
+_structure_cache: collections.OrderedDict = collections.OrderedDict()
+_structure_lock = threading.Lock()
+
+
+def cached_structure(n: int, degree: int) -> Structure:
+    key = (n, degree)
+    with _structure_lock:
+        st = _structure_cache.get(key)
+    if st is None:
+        built = Structure(n, degree)
+        with _structure_lock:
+            st = _structure_cache.setdefault(key, built)
+    return st
+
+
+def drop_structure(n: int, degree: int) -> None:
+    with _structure_lock:
+        _structure_cache.pop((n, degree), None)
+
+
+def clear_structure_cache() -> None:
+    with _structure_lock:
+        _structure_cache.clear()
+
+
 class Job:
     """One admitted request: its values and vectors on the device."""
 
     def __init__(self, req: Request, st: Structure, mode: str, stream, assembly: str = "atomic"):
         self.req, self.st, self.mode = req, st, mode
         V = st.V
-        kappa, f = request_inputs(st.mesh, req.seed)
         with torch.cuda.stream(stream):
-            self.kappa = torch.from_numpy(kappa).to("cuda", non_blocking=True)
-            self.f = torch.from_numpy(f).to("cuda", non_blocking=True)
+            self.kappa, self.f = request_inputs(st.mesh, req.seed)
             a = fem.poisson_form(V, self.kappa, k2=req.k2)
             L = fem.source_form(V, self.f)
             self.A = la.MatrixCSR(st.A0.row_ptr, st.A0.cols,
@@ -189,21 +220,22 @@ class Server:
         key = (n, degree)
         st = self.structures.get(key)
         if st is None:
-            st = Structure(n, degree)
+            st = cached_structure(n, degree)
             self.structures[key] = st
             self.used += st.bytes
-            self._evict()
+            self._evict(keep=key)
         self.structures.move_to_end(key)
         return st
 
-    def _evict(self):
+    def _evict(self, keep=None):
         for key in list(self.structures):
             if self.used <= self.budget:
                 break
             st = self.structures[key]
-            if st.users == 0:
+            if st.users == 0 and key != keep:
                 self.used -= st.bytes
                 del self.structures[key]
+                drop_structure(*key)
 
     def prewarm(self, requests):
         for key in sorted({(r.n, r.degree) for r in requests}):

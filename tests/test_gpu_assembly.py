@@ -129,6 +129,35 @@ def test_lifting_and_set_bc(cuda, oracle, capi, deg, bs, mode):
     assert_close(b.cpu().numpy(), ref)
 
 
+@pytest.mark.parametrize("mode", ["atomic", "coloured"])
+@pytest.mark.parametrize("deg,bs,shape", [(2, 1, (9, 8, 7)), (1, 1, (12, 9, 8)),
+                                          (2, 3, (8, 8, 6))])
+def test_lifting_over_several_scan_ranges(cuda, oracle, capi, deg, bs, shape, mode):
+    """Lifting compacts the constrained cells of each 2048-cell scan range in
+    shared memory: meshes of 2,304-5,184 cells span two or three ranges, and
+    constraints on one face only leave most batches partly filled."""
+    from dolfinx_gb300 import fem
+
+    m, V, kappa, f, rp, cols = problem(oracle, shape, deg, seed=11, bs=bs)
+    rng = np.random.default_rng(12)
+    X = V.tabulate_dof_coordinates()
+    nodes = np.flatnonzero(np.isclose(X[:, 1], 1)).astype(np.int32)
+    gfull = rng.standard_normal(V.num_dofs)
+    bc = fem.dirichletbc(gfull, nodes, V)
+    a = (fem.poisson_form(V, kappa) if bs == 1 else fem.elasticity_form(V, kappa, 0.3))
+    b0 = rng.standard_normal(V.num_dofs)
+    b = torch.from_numpy(b0.copy()).cuda()
+    fem.apply_lifting(b, [a], [[bc]], mode=mode)
+    mk = np.zeros(V.num_dofs, np.int8)
+    mk[bc.dofs] = 1
+    g = np.zeros(V.num_dofs)
+    g[bc.dofs] = gfull[bc.dofs]
+    ref = oracle.apply_lifting(b0.copy(), 0 if bs == 1 else 1, deg, m.cells, m.x, V.dofmap, mk, g,
+                               kappa=kappa, nu=0.3)
+    assert_close(b.cpu().numpy(), ref)
+    assert np.abs(b.cpu().numpy() - b0).max() > 0  # the constraint did lift
+
+
 def test_entry_not_in_sparsity(cuda, oracle, capi):
     from dolfinx_gb300 import fem, la
 

@@ -192,6 +192,29 @@ def test_operator_cg_matches_csr_cg(cuda, oracle, capi):
     assert rel < 1e-7
 
 
+def test_cg_vector_and_scalar_elementwise_paths(cuda, oracle, capi):
+    """The CG update kernels move 16-byte vectors when every array is 16-byte
+    aligned (with a scalar tail: n = 6,783 is odd) and fall back to scalar
+    loads otherwise; an x that starts 8 bytes into its allocation takes the
+    fallback. Both paths meet the stopping test in the oracle's SpMV."""
+    from dolfinx_gb300 import la
+
+    A, b, rp, cols = _c1_system(oracle, (10, 9, 8), 2, 31)
+    assert A.nrows % 2 == 1
+    x1, r1 = la.cg(A, b, rtol=1e-10)
+    buf = torch.zeros(A.nrows + 1, dtype=torch.float64, device="cuda")
+    x2 = buf[1:]
+    assert x2.data_ptr() % 16 == 8
+    x2, r2 = la.cg(A, b, x=x2, rtol=1e-10)
+    assert r1.status == 0 and r2.status == 0 and abs(r1.iterations - r2.iterations) <= 2
+    bh = b.cpu().numpy()
+    vals = A.vals.cpu().numpy()
+    for x in (x1, x2):
+        res = bh - oracle.spmv(rp, cols, vals, x.cpu().numpy())
+        assert np.linalg.norm(res) / np.linalg.norm(bh) < 1e-10 * 1.0001
+    assert (x1 - x2).norm() / x1.norm() < 1e-7
+
+
 @pytest.mark.parametrize("variant,inner_rtol", [("restart", 1e-3), ("restart", 1e-5),
                                                  ("reliable", 0.1), ("reliable", 0.01)])
 def test_iterative_refinement_reaches_fp64(cuda, oracle, capi, variant, inner_rtol):
