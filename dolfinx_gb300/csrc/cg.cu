@@ -15,8 +15,8 @@
 // Mixed precision: the refinement loop keeps the residual r = b - A x, its
 // norm and the update x += d in FP64 with the FP64 operator; the inner
 // solve A d = r runs the same PCG with FP32 values, FP32 vectors and the
-// 16-bit-column operator. Its dot products sum FP32 products per thread
-// (a thread owns ~16 entries) and reduce the per-thread sums in FP64.
+// 16-bit-column operator. Its dot products sum FP32 products per warp
+// (a lane owns ~16 entries) and reduce the warp sums in FP64.
 #include "la_kernels.cuh"
 #include "q4.cuh"
 #include "sell.cuh"
