@@ -129,6 +129,9 @@ _SIGS = {
     "dfx_mesh_create_box_tet": (C.c_int, [C.c_int32] * 3 + [_P, _P, C.c_int32, _P, _P]),
     "dfx_dofmap_create_tet": (C.c_int, [C.c_int32, _P, C.c_int32, _P, _P]),
     "dfx_sparsity_create": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, _P, _P, _P, _P]),
+    "dfx_sparsity_device_workspace_bytes": (C.c_size_t, [C.c_int32, C.c_int32, C.c_int32]),
+    "dfx_sparsity_create_device": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, _P, _P, _P, _P, _P,
+                                             C.c_size_t, _P]),
     "dfx_colour_cells": (C.c_int, [C.c_int32, C.c_int32, _P, C.c_int32, _P, _P, C.c_int32, _P]),
     "dfx_slot_map_bytes": (C.c_size_t, [C.POINTER(Form)]),
     "dfx_slot_map_create": (C.c_int, [C.POINTER(Form), C.POINTER(Csr), _P, _P]),
@@ -152,6 +155,8 @@ _SIGS = {
                                        C.c_int32, C.POINTER(CgInfo), _P]),
     "dfx_operator_create": (C.c_int, [C.POINTER(Csr), C.c_int32, C.c_int32, C.c_int32,
                                       C.POINTER(C.c_void_p), _P]),
+    "dfx_operator_create_ex": (C.c_int, [C.POINTER(Csr), C.c_int32, C.c_int32, C.c_int32,
+                                         C.c_int32, C.POINTER(C.c_void_p), _P]),
     "dfx_operator_update_values": (C.c_int, [_P, C.POINTER(Csr), _P]),
     "dfx_operator_apply": (C.c_int, [_P, _P, _P, _P]),
     "dfx_operator_apply_renumbered": (C.c_int, [_P, _P, _P, _P]),

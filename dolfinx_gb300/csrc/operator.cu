@@ -1,5 +1,7 @@
-// SELL-32-sigma operator: host-side builder, value refill and SpMV.
+// SELL-32-sigma operator: builders (device, host fallback), value refill
+// and SpMV.
 #include "la_kernels.cuh"
+#include "scan.cuh"
 #include "sell.cuh"
 
 #include <algorithm>
@@ -9,7 +11,6 @@
 
 namespace
 {
-constexpr int kThreads = 256;
 
 template <typename F>
 void parallel_for(int64_t n, F&& f)
@@ -98,6 +99,258 @@ int upload(T** dst, const std::vector<T>& src, cudaStream_t s)
     DFX_CUDA(cudaMemcpyAsync(*dst, src.data(), sizeof(T) * src.size(), cudaMemcpyHostToDevice, s));
   return DFX_OK;
 }
+
+// ---------------------------------------------------------------- device build
+// The device builder computes the same arrays as the host builder below:
+// the same stable length order per window, slice lengths, renumbered and
+// sorted columns, padding and 16-bit deltas. Rows longer than kDevMaxRow
+// entries, or windows wider than kDevMaxSigma rows, go to the host builder.
+constexpr int kDevMaxRow = 256;
+constexpr int kDevMaxSigma = 4096;
+constexpr int kGapStatus = 100; // internal: a column gap above 65535
+constexpr int kUseHost = -1;    // internal: the device build does not take this matrix
+
+// Stable length-descending order inside each window of sigma rows (the
+// host builder's std::stable_sort): the rank of row i is the number of rows
+// of its window that are longer, or as long and earlier.
+__global__ void k_window_perm(const int64_t* __restrict__ rp, int32_t n, int32_t sigma,
+                              int32_t* __restrict__ perm, int* __restrict__ status)
+{
+  extern __shared__ int32_t slen[];
+  const int64_t w0 = (int64_t)blockIdx.x * sigma;
+  const int cnt = (int)min((int64_t)sigma, (int64_t)n - w0);
+  for (int i = threadIdx.x; i < cnt; i += blockDim.x)
+  {
+    const int64_t len = rp[w0 + i + 1] - rp[w0 + i];
+    if (len > kDevMaxRow)
+      atomicExch(status, (int)DFX_ERR_UNSUPPORTED);
+    slen[i] = (int32_t)min(len, (int64_t)INT32_MAX);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < cnt; i += blockDim.x)
+  {
+    const int32_t li = slen[i];
+    int rank = 0;
+    for (int j = 0; j < cnt; ++j)
+    {
+      const int32_t lj = slen[j];
+      rank += (lj > li) || (lj == li && j < i);
+    }
+    perm[w0 + rank] = (int32_t)(w0 + i);
+  }
+}
+
+__global__ void k_invert(const int32_t* __restrict__ perm, int32_t* __restrict__ iperm, int32_t n)
+{
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n)
+    iperm[perm[i]] = (int32_t)i;
+}
+
+// 32 x (longest row of the slice), rounded up to even for k-pairs.
+__global__ void k_slice_len(const int64_t* __restrict__ rp, const int32_t* __restrict__ perm,
+                            int32_t n, int32_t ns, int pairs, int64_t* __restrict__ out)
+{
+  const int64_t sl = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (sl >= ns)
+    return;
+  int64_t len = 0;
+  for (int l = 0; l < 32; ++l)
+  {
+    const int64_t i = 32 * sl + l;
+    if (i < n)
+    {
+      const int32_t r = perm[i];
+      len = max(len, rp[r + 1] - rp[r]);
+    }
+  }
+  if (pairs)
+    len += len & 1;
+  out[sl] = 32 * len;
+}
+
+// One thread per (renumbered) row of the padded slices: the row's columns
+// renumbered by iperm and sorted (insertion sort, rows of at most
+// kDevMaxRow entries), then its slots: CSR entry or -1, column or delta.
+template <bool COMP, bool PAIRS>
+__global__ void __launch_bounds__(128)
+    k_sell_fill(const int64_t* __restrict__ rp, const int32_t* __restrict__ cols,
+                const int32_t* __restrict__ perm, const int32_t* __restrict__ iperm,
+                const int64_t* __restrict__ sp, int32_t n, int32_t ns, int32_t* __restrict__ map,
+                int32_t* __restrict__ scols, uint16_t* __restrict__ sdelta,
+                int32_t* __restrict__ sfirst, int* __restrict__ status)
+{
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 32 * (int64_t)ns)
+    return;
+  const int64_t sl = i >> 5;
+  const int l = (int)(i & 31);
+  const int64_t base = sp[sl];
+  const int64_t len = (sp[sl + 1] - base) >> 5;
+  int32_t key[kDevMaxRow], val[kDevMaxRow];
+  int cnt = 0;
+  if (i < n)
+  {
+    const int32_t r = perm[i];
+    const int64_t b = rp[r];
+    const int64_t e = rp[r + 1];
+    if (e - b > kDevMaxRow)
+      return; // reported by k_window_perm
+    cnt = (int)(e - b);
+    for (int k = 0; k < cnt; ++k)
+    {
+      const int32_t c = iperm[cols[b + k]];
+      int p = k;
+      while (p > 0 && key[p - 1] > c)
+      {
+        key[p] = key[p - 1];
+        val[p] = val[p - 1];
+        --p;
+      }
+      key[p] = c;
+      val[p] = (int32_t)(b + k);
+    }
+  }
+  int32_t prev = cnt == 0 ? (int32_t)min(i, (int64_t)n - 1) : key[0];
+  if (COMP)
+    sfirst[32 * sl + l] = prev;
+  for (int64_t k = 0; k < len; ++k)
+  {
+    const int64_t slot = PAIRS ? base + 64 * (k >> 1) + 2 * l + (k & 1) : base + 32 * k + l;
+    const bool real = k < cnt;
+    const int32_t c = real ? key[k] : prev;
+    map[slot] = real ? val[k] : -1;
+    if (COMP)
+    {
+      const int64_t d = k ? (int64_t)c - prev : 0;
+      if (d < 0 || d > 65535)
+        atomicExch(status, kGapStatus);
+      sdelta[slot] = (uint16_t)max((int64_t)0, min(d, (int64_t)65535));
+    }
+    else
+      scols[slot] = c;
+    prev = c;
+  }
+}
+
+int read_status(int* status, cudaStream_t s)
+{
+  int h = 0;
+  DFX_CUDA(cudaMemcpyAsync(&h, status, sizeof(int), cudaMemcpyDeviceToHost, s));
+  DFX_CUDA(cudaStreamSynchronize(s));
+  return h;
+}
+
+// Structure of op built on the device; kUseHost: use the host builder.
+int build_structure_device(const dfx_csr* A, dfx_operator_s* op, bool pairs, bool compress,
+                           cudaStream_t s)
+{
+  const int32_t n = op->n, ns = op->nslices, sigma = op->sigma;
+  if (sigma > kDevMaxSigma)
+    return kUseHost;
+  int* status = dfx::device_status_page();
+  DFX_REQUIRE(status, "could not allocate the status page");
+  DFX_CUDA(cudaMemsetAsync(status, 0, sizeof(int), s));
+  DFX_CUDA(cudaMalloc(&op->perm, sizeof(int32_t) * std::max(n, 1)));
+  DFX_CUDA(cudaMalloc(&op->iperm, sizeof(int32_t) * std::max(n, 1)));
+  DFX_CUDA(cudaMalloc(&op->slice_ptr, sizeof(int64_t) * ((size_t)ns + 1)));
+  int64_t* lens = nullptr;
+  int64_t* scratch = nullptr;
+  DFX_CUDA(cudaMalloc(&lens, sizeof(int64_t) * std::max(ns, 1)));
+  const cudaError_t e = cudaMalloc(&scratch, sizeof(int64_t) * dfx::scan_scratch_count(ns));
+  if (e != cudaSuccess)
+  {
+    cudaFree(lens);
+    return dfx::cuda_fail(e, "cudaMalloc", __FILE__, __LINE__);
+  }
+  int st = DFX_OK;
+  int64_t nslots = 0;
+  if (n > 0)
+  {
+    const int nwin = (n + sigma - 1) / sigma;
+    k_window_perm<<<nwin, 256, sizeof(int32_t) * sigma, s>>>(A->row_ptr, n, sigma, op->perm,
+                                                             status);
+    k_invert<<<(n + 255) / 256, 256, 0, s>>>(op->perm, op->iperm, n);
+    k_slice_len<<<(ns + 127) / 128, 128, 0, s>>>(A->row_ptr, op->perm, n, ns, pairs ? 1 : 0,
+                                                  lens);
+    st = dfx::exclusive_scan(lens, op->slice_ptr, ns, scratch, s);
+    if (!st && cudaGetLastError() != cudaSuccess)
+      st = dfx::fail(DFX_ERR_CUDA, "operator structure kernels failed to launch");
+    if (!st && cudaMemcpyAsync(&nslots, op->slice_ptr + ns, sizeof(int64_t),
+                               cudaMemcpyDeviceToHost, s) != cudaSuccess)
+      st = dfx::fail(DFX_ERR_CUDA, "slice pointer read-back failed");
+    if (!st)
+      st = read_status(status, s);
+  }
+  else if (cudaMemsetAsync(op->slice_ptr, 0, sizeof(int64_t), s) != cudaSuccess)
+    st = dfx::fail(DFX_ERR_CUDA, "slice pointer reset failed");
+  cudaStreamSynchronize(s);
+  cudaFree(lens);
+  cudaFree(scratch);
+  if (st == DFX_ERR_UNSUPPORTED)
+    return kUseHost; // a row is too long for the device build
+  if (st)
+    return st;
+  DFX_REQUIRE(nslots < INT32_MAX, "operator too large");
+  op->nslots = nslots;
+  const size_t ms = (size_t)std::max<int64_t>(nslots, 1);
+  DFX_CUDA(cudaMalloc(&op->map, sizeof(int32_t) * ms));
+  if (compress)
+  {
+    DFX_CUDA(cudaMalloc(&op->delta, sizeof(uint16_t) * ms));
+    DFX_CUDA(cudaMalloc(&op->first, sizeof(int32_t) * std::max<size_t>(32 * (size_t)ns, 1)));
+  }
+  else
+    DFX_CUDA(cudaMalloc(&op->cols, sizeof(int32_t) * ms));
+  if (ns > 0)
+  {
+    const unsigned grid = (unsigned)((32 * (int64_t)ns + 127) / 128);
+    if (compress)
+      k_sell_fill<true, true><<<grid, 128, 0, s>>>(A->row_ptr, A->cols, op->perm, op->iperm,
+                                                   op->slice_ptr, n, ns, op->map, nullptr,
+                                                   op->delta, op->first, status);
+    else if (pairs)
+      k_sell_fill<false, true><<<grid, 128, 0, s>>>(A->row_ptr, A->cols, op->perm, op->iperm,
+                                                    op->slice_ptr, n, ns, op->map, op->cols,
+                                                    nullptr, nullptr, status);
+    else
+      k_sell_fill<false, false><<<grid, 128, 0, s>>>(A->row_ptr, A->cols, op->perm, op->iperm,
+                                                     op->slice_ptr, n, ns, op->map, op->cols,
+                                                     nullptr, nullptr, status);
+    DFX_CHECK_LAUNCH();
+    const int h = read_status(status, s);
+    if (h == kGapStatus)
+      return dfx::fail(DFX_ERR_UNSUPPORTED,
+                       "a row has a column gap above 65535: use 32-bit columns");
+    if (h)
+      return dfx::fail(h, "operator structure build failed");
+  }
+  return DFX_OK;
+}
+} // namespace
+
+namespace
+{
+// Values and scratch of a built structure; on success *out = op and the
+// values are filled from A's FP64 values when it has them.
+int finish_create(dfx_operator_s* op, const dfx_csr* A, dfx_operator* out, void* stream)
+{
+  const size_t vb = op->dtype == DFX_F64 ? 8 : 4;
+  int st = DFX_OK;
+  if (cudaMalloc(&op->vals, vb * std::max<int64_t>(op->nslots, 1)) != cudaSuccess)
+    st = dfx::fail(DFX_ERR_NO_MEMORY, "operator values: out of device memory");
+  if (!st && cudaMalloc(&op->tmp, vb * 2 * std::max<int64_t>(op->n, 1)) != cudaSuccess)
+    st = dfx::fail(DFX_ERR_NO_MEMORY, "operator scratch: out of device memory");
+  if (st)
+  {
+    free_op(op);
+    return st;
+  }
+  *out = op;
+  if (A->vals && A->dtype == DFX_F64)
+    return dfx_operator_update_values(op, A, stream);
+  return DFX_OK;
+}
 } // namespace
 
 namespace dfx
@@ -131,6 +384,13 @@ int sell_spmv(const dfx_operator_s& op, const void* x, void* y, cudaStream_t s)
 extern "C" int dfx_operator_create(const dfx_csr* A, int32_t sigma, int32_t dtype,
                                    int32_t compress_cols, dfx_operator* out, void* stream)
 {
+  return dfx_operator_create_ex(A, sigma, dtype, compress_cols, DFX_BUILD_AUTO, out, stream);
+}
+
+extern "C" int dfx_operator_create_ex(const dfx_csr* A, int32_t sigma, int32_t dtype,
+                                      int32_t compress_cols, int32_t build, dfx_operator* out,
+                                      void* stream)
+{
   if (int st = dfx::check_csr(A))
     return st;
   DFX_REQUIRE(out, "output handle is NULL");
@@ -141,8 +401,31 @@ extern "C" int dfx_operator_create(const dfx_csr* A, int32_t sigma, int32_t dtyp
   DFX_REQUIRE(!compress_cols || dtype == DFX_F32, "16-bit columns are for FP32 operators");
   DFX_REQUIRE(sigma >= 32 && sigma % 32 == 0, "sigma must be a positive multiple of 32");
   DFX_REQUIRE(A->nnz < INT32_MAX, "matrix too large for the operator slot map");
+  DFX_REQUIRE(build == DFX_BUILD_AUTO || build == DFX_BUILD_DEVICE || build == DFX_BUILD_HOST,
+              "unknown build place %d", build);
   cudaStream_t s = dfx::as_stream(stream);
   const int32_t n = A->nrows;
+  if (build != DFX_BUILD_HOST)
+  {
+    auto* op = new dfx_operator_s();
+    cudaGetDevice(&op->device);
+    op->n = n;
+    op->nslices = (n + 31) / 32;
+    op->sigma = sigma;
+    op->dtype = dtype;
+    op->compressed = compress_cols ? 1 : 0;
+    op->csr_nnz = A->nnz;
+    const int st = build_structure_device(A, op, dtype == DFX_F32, compress_cols != 0, s);
+    if (st == DFX_OK)
+      return finish_create(op, A, out, stream);
+    free_op(op);
+    if (st != kUseHost)
+      return st;
+    if (build == DFX_BUILD_DEVICE)
+      return dfx::fail(DFX_ERR_UNSUPPORTED,
+                       "the device build takes rows of at most %d entries and sigma <= %d",
+                       kDevMaxRow, kDevMaxSigma);
+  }
   std::vector<int64_t> rp(n + 1);
   std::vector<int32_t> cols(A->nnz);
   DFX_CUDA(cudaMemcpyAsync(rp.data(), A->row_ptr, sizeof(int64_t) * (n + 1), cudaMemcpyDeviceToHost,
@@ -263,11 +546,6 @@ extern "C" int dfx_operator_create(const dfx_csr* A, int32_t sigma, int32_t dtyp
     st = upload(&op->first, sfirst, s);
   if (!st && !compress_cols)
     st = upload(&op->cols, scols, s);
-  const size_t vb = dtype == DFX_F64 ? 8 : 4;
-  if (!st && cudaMalloc(&op->vals, vb * std::max<int64_t>(nslots, 1)) != cudaSuccess)
-    st = dfx::fail(DFX_ERR_NO_MEMORY, "operator values: out of device memory");
-  if (!st && cudaMalloc(&op->tmp, vb * 2 * std::max<int64_t>(n, 1)) != cudaSuccess)
-    st = dfx::fail(DFX_ERR_NO_MEMORY, "operator scratch: out of device memory");
   if (!st)
   {
     cudaError_t e = cudaStreamSynchronize(s); // host vectors die at return
@@ -279,10 +557,7 @@ extern "C" int dfx_operator_create(const dfx_csr* A, int32_t sigma, int32_t dtyp
     free_op(op);
     return st;
   }
-  *out = op;
-  if (A->vals && A->dtype == DFX_F64)
-    return dfx_operator_update_values(op, A, stream);
-  return DFX_OK;
+  return finish_create(op, A, out, stream);
 }
 
 extern "C" int dfx_operator_update_values(dfx_operator op, const dfx_csr* A, void* stream)

@@ -37,6 +37,7 @@ class FunctionSpace:
         self.device = device
         self._dofmap_dev = None
         self._sparsity = None
+        self._sparsity_dev = None
         self._colouring = None
 
     @property
@@ -79,6 +80,26 @@ class FunctionSpace:
                                               cols.ctypes.data, C.byref(nnz)))
             self._sparsity = (rp, cols)
         return self._sparsity
+
+    def sparsity_device(self):
+        """(row_ptr, cols) of the same pattern as device tensors, built on the
+        device from the device dofmap (cached). Equal to ``sparsity()`` bit
+        for bit; used by ``create_matrix`` for spaces on a GPU."""
+        if self._sparsity_dev is None:
+            nd, nc, n = self.ndofs_cell, self.mesh.num_cells, self.num_nodes
+            L = _capi.lib()
+            dm = self.dofmap_device()
+            wb = int(L.dfx_sparsity_device_workspace_bytes(n, nc, nd))
+            work = torch.empty(wb, dtype=torch.uint8, device=self.device)
+            rp = torch.empty(n + 1, dtype=torch.int64, device=self.device)
+            nnz = C.c_int64(0)
+            _capi.check(L.dfx_sparsity_create_device(n, nc, nd, _ptr(dm), _ptr(rp), None,
+                                                     C.byref(nnz), _ptr(work), wb, _stream()))
+            cols = torch.empty(nnz.value, dtype=torch.int32, device=self.device)
+            _capi.check(L.dfx_sparsity_create_device(n, nc, nd, _ptr(dm), _ptr(rp), _ptr(cols),
+                                                     C.byref(nnz), _ptr(work), wb, _stream()))
+            self._sparsity_dev = (rp, cols)
+        return self._sparsity_dev
 
     def colouring(self, max_colours: int = 256):
         """Cell colouring for deterministic assembly: (order on device, offsets)."""
@@ -232,12 +253,23 @@ def _colour_args(V: FunctionSpace, mode: int):
 
 
 def create_matrix(a: Form) -> MatrixCSR:
-    """Matrix with the form's sparsity pattern, values zero (create_matrix)."""
-    rp, cols = a.V.sparsity()
+    """Matrix with the form's sparsity pattern, values zero (create_matrix).
+    The pattern is built on the device for spaces on a GPU; a space whose
+    rows exceed the device builder's limit uses the host builder."""
     dev = a.V.device
     bs = a.V.bs
-    vals = torch.zeros(cols.size * bs * bs, dtype=torch.float64, device=dev)
-    return MatrixCSR(torch.from_numpy(rp).to(dev), torch.from_numpy(cols).to(dev), vals, bs)
+    rp = cols = None
+    if torch.device(dev).type == "cuda":
+        try:
+            rp, cols = a.V.sparsity_device()
+        except _capi.DfxError as e:
+            if e.code != _capi.DFX_ERR_UNSUPPORTED:
+                raise
+    if rp is None:
+        rph, colsh = a.V.sparsity()
+        rp, cols = torch.from_numpy(rph).to(dev), torch.from_numpy(colsh).to(dev)
+    vals = torch.zeros(cols.numel() * bs * bs, dtype=torch.float64, device=dev)
+    return MatrixCSR(rp, cols, vals, bs)
 
 
 def bc_markers(V: FunctionSpace, bcs) -> torch.Tensor | None:

@@ -189,7 +189,10 @@ class SellOperator:
     with update_values() after re-assembly."""
 
     def __init__(self, A: MatrixCSR, dtype=torch.float64, sigma: int = 256,
-                 compress_cols: bool | None = None, share_of: "SellOperator | None" = None):
+                 compress_cols: bool | None = None, share_of: "SellOperator | None" = None,
+                 build: int = 0):
+        """build: where the structure is built (0 device with host fallback,
+        1 device only, 2 host); every place gives the same operator."""
         self.A, self.dtype, self.sigma = A, dtype, sigma
         h = C.c_void_p()
         if share_of is not None:
@@ -204,9 +207,9 @@ class SellOperator:
         if compress_cols is None:
             compress_cols = dtype == torch.float32
         dt = _capi.F64 if dtype == torch.float64 else _capi.F32
-        _capi.check(_capi.lib().dfx_operator_create(C.byref(A.csr()), sigma, dt,
-                                                    int(bool(compress_cols)), C.byref(h),
-                                                    _stream()))
+        _capi.check(_capi.lib().dfx_operator_create_ex(C.byref(A.csr()), sigma, dt,
+                                                       int(bool(compress_cols)), int(build),
+                                                       C.byref(h), _stream()))
         self.handle = h
         self.compressed = bool(compress_cols)
 

@@ -128,6 +128,21 @@ int dfx_sparsity_create(int32_t nrows, int32_t num_cells, int32_t ndofs,
                         const int32_t* dofmap, int64_t* row_ptr, int32_t* cols,
                         int64_t* nnz);
 
+/* The same pattern built on the device from a device dofmap (same
+ * reference functions): d_row_ptr and d_cols equal dfx_sparsity_create's
+ * bit for bit. Two-phase: with d_cols == NULL it writes d_row_ptr
+ * (nrows+1) and *nnz; then call again with d_cols (nnz) and the d_row_ptr
+ * of the first call. d_work: dfx_sparsity_device_workspace_bytes() bytes,
+ * 256-byte aligned. A row whose cells hold more than 1024 dofs in total
+ * returns DFX_ERR_UNSUPPORTED (use the host builder). Synchronises
+ * `stream`. */
+size_t dfx_sparsity_device_workspace_bytes(int32_t nrows, int32_t num_cells,
+                                           int32_t ndofs);
+int dfx_sparsity_create_device(int32_t nrows, int32_t num_cells, int32_t ndofs,
+                               const int32_t* d_dofmap, int64_t* d_row_ptr,
+                               int32_t* d_cols, int64_t* nnz, void* d_work,
+                               size_t work_bytes, void* stream);
+
 /* Greedy cell colouring for DFX_MODE_COLOURED: no two cells of one colour
  * share a dof. order: (num_cells) cells grouped by colour, offsets:
  * (max_colours+1). Returns the colour count in *num_colours. */
@@ -274,6 +289,20 @@ typedef struct dfx_operator_s* dfx_operator;
 
 int dfx_operator_create(const dfx_csr* A, int32_t sigma, int32_t value_dtype,
                         int32_t compress_cols, dfx_operator* op, void* stream);
+/* Where dfx_operator_create_ex builds the structure. DFX_BUILD_AUTO (what
+ * dfx_operator_create does): on the device, or on the host when a row has
+ * more than 256 entries or sigma > 4096. DFX_BUILD_DEVICE refuses such
+ * matrices with DFX_ERR_UNSUPPORTED. DFX_BUILD_HOST: the host builder.
+ * Every place gives the same arrays bit for bit. */
+enum
+{
+  DFX_BUILD_AUTO = 0,
+  DFX_BUILD_DEVICE = 1,
+  DFX_BUILD_HOST = 2
+};
+int dfx_operator_create_ex(const dfx_csr* A, int32_t sigma, int32_t value_dtype,
+                           int32_t compress_cols, int32_t build, dfx_operator* op,
+                           void* stream);
 /* Refill the operator's values from A's FP64 values (after re-assembly). */
 int dfx_operator_update_values(dfx_operator op, const dfx_csr* A, void* stream);
 /* y = A x in the original numbering (x, y of the operator's dtype). */
