@@ -91,7 +91,8 @@ class Problem:
     the plain FP64 path (sliced-ELL FP64 operator, Jacobi-PCG) and the
     mixed-precision path (FP32 inner PCG inside FP64 refinement)."""
 
-    def __init__(self, m, kappa, f, mode="atomic", inner_rtol=None, variant="reliable"):
+    def __init__(self, m, kappa, f, mode="atomic", inner_rtol=None, variant="reliable",
+                 tune=True):
         import numpy as np
         import torch
 
@@ -112,8 +113,21 @@ class Problem:
         self.b = torch.zeros(self.V.num_dofs, dtype=torch.float64, device="cuda")
         self.x = torch.zeros_like(self.b)
         self.masm.assemble()
-        self.fp64 = la.OperatorCGSolver(self.A, jacobi=True)
-        self.ir = la.IRSolver(self.A, jacobi=True, inner_rtol=inner_rtol, variant=variant)
+        # Launch shapes from the autotuner (outside any timed region): cells
+        # per block of the assembly, window sigma of the solver operators, and
+        # the row split of the CSR SpMV (MatrixCSR::mult).
+        from dolfinx_gb300 import autotune
+
+        self.tuning = {}
+        sigma = 256
+        if tune:
+            self.tuning["assembly"] = autotune.tune_assembly(self.masm)
+            self.tuning["sigma"] = autotune.tune_sigma(self.A)
+            self.tuning["csr_spmv"] = autotune.tune_spmv(self.A)
+            sigma = self.tuning["sigma"]["sigma"]
+        self.fp64 = la.OperatorCGSolver(self.A, jacobi=True, sigma=sigma)
+        self.ir = la.IRSolver(self.A, jacobi=True, inner_rtol=inner_rtol, variant=variant,
+                              sigma=sigma)
         self.last = None
 
     def assemble(self):
@@ -777,6 +791,7 @@ def run_ours(args):
                                       "traffic": profile_traffic("assemble_p2_c2"),
                                       "bound": "fp64 pipe and L2 atomics (ncu), not hbm"},
                 "assemble_vector_ms": ms_vec, "apply_lifting_ms": ms_lift,
+                "autotune": P.tuning,
                 "setup_c2": setup,
                 "c3_elasticity": c3,
                 "c4_matrix_free_q4": c4,

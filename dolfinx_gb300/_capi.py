@@ -153,6 +153,14 @@ _SIGS = {
                                C.c_size_t, C.POINTER(CgInfo), _P]),
     "dfx_cg_solve_noalloc": (C.c_int, [C.POINTER(Csr), _P, _P, _P, C.c_double, C.c_int32,
                                        C.c_int32, C.POINTER(CgInfo), _P]),
+    "dfx_tune_assembly": (C.c_int, [C.POINTER(Form), C.POINTER(Csr), _P, _P, C.c_int32, _P, _P,
+                                    C.c_int32, _P, C.POINTER(C.c_int32), _P, _P]),
+    "dfx_set_cells_per_block": (C.c_int, [C.POINTER(Form), C.c_int32, C.c_int32]),
+    "dfx_get_cells_per_block": (C.c_int, [C.POINTER(Form), C.c_int32, C.POINTER(C.c_int32)]),
+    "dfx_tune_spmv": (C.c_int, [C.POINTER(Csr), _P, _P, C.POINTER(C.c_int32), _P, _P]),
+    "dfx_set_spmv_lanes": (C.c_int, [C.POINTER(Csr), C.c_int32]),
+    "dfx_get_spmv_lanes": (C.c_int, [C.POINTER(Csr), C.POINTER(C.c_int32)]),
+    "dfx_tune_clear": (C.c_int, []),
     "dfx_operator_create": (C.c_int, [C.POINTER(Csr), C.c_int32, C.c_int32, C.c_int32,
                                       C.POINTER(C.c_void_p), _P]),
     "dfx_operator_create_ex": (C.c_int, [C.POINTER(Csr), C.c_int32, C.c_int32, C.c_int32,

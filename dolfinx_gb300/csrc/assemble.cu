@@ -266,16 +266,18 @@ __device__ __forceinline__ void lift_rows(const double* sA, const int32_t* sDof,
   }
 }
 
-// Matrix assembly over a list of cells (list == nullptr: cells [0, count)).
-template <int DEG, bool ELAST, bool MASS, bool COLOURED>
+// Matrix assembly over a list of cells (list == nullptr: cells [0, count)),
+// CPB cells per block (the autotuner's choice, at most kThreads).
+template <int DEG, bool ELAST, bool MASS, bool COLOURED, int CPB>
 __global__ void __launch_bounds__(kThreads)
     k_cells_matrix(const dfx_form a, const int64_t* __restrict__ row_ptr,
                    const int32_t* __restrict__ cols, double* __restrict__ vals,
                    const uint8_t* __restrict__ map, const int8_t* __restrict__ bc,
                    const int32_t* __restrict__ list, int32_t count, int* __restrict__ status)
 {
+  static_assert(CPB <= kThreads, "stage 1 runs one thread per cell");
   using T = Traits<DEG, ELAST>;
-  constexpr int ND = T::ND, BS = T::BS, N = T::N, NU = T::NU, CPB = T::CPB;
+  constexpr int ND = T::ND, BS = T::BS, N = T::N, NU = T::NU;
   __shared__ double sA[CPB * NU];
   __shared__ double sScratch[ELAST ? CPB * 132 : 1];
   __shared__ int32_t sCell[CPB];
@@ -591,39 +593,94 @@ int read_status(int* status, cudaStream_t s)
   return h;
 }
 
-// Launch the matrix kernel for one cell list.
+// Cells per block: candidates of the autotuner and the default, per form.
+// Scalar forms: 16, 32 (default) or 64 cells; elasticity (30 x 30 element
+// tensors): 2, 4 (default) or 8.
+constexpr int kCpbScalar[3] = {16, 32, 64};
+constexpr int kCpbElast[3] = {2, 4, 8};
+
+const int* cpb_candidates(const dfx_form& a)
+{
+  return a.kind == DFX_FORM_ELASTICITY ? kCpbElast : kCpbScalar;
+}
+
+int default_cpb(const dfx_form& a) { return cpb_candidates(a)[1]; }
+
+bool valid_cpb(const dfx_form& a, int c)
+{
+  const int* k = cpb_candidates(a);
+  return c == k[0] || c == k[1] || c == k[2];
+}
+
+// Autotuner key of a matrix assembly: form kind, degree, mass term, mode.
+int64_t assembly_key(const dfx_form& a, int32_t mode)
+{
+  const int mass = a.kind == DFX_FORM_POISSON && a.k2 != 0.0;
+  return (((int64_t)a.kind * 4 + a.degree) * 2 + mass) * 2 + mode;
+}
+
+int cells_per_block(const dfx_form& a, int32_t mode)
+{
+  const int t = dfx::tuned_get(dfx::kTuneAssembly, a.num_cells, assembly_key(a, mode), 0);
+  return t ? t : default_cpb(a);
+}
+
+template <int DEG, bool ELAST, bool MASS, bool COLOURED, int CPB>
+void launch_cells_cpb(const dfx_form& a, const dfx_csr* A, const uint8_t* map, const int8_t* bc,
+                      const int32_t* list, int32_t count, int* status, cudaStream_t s)
+{
+  const unsigned grid = (unsigned)((count + CPB - 1) / CPB);
+  k_cells_matrix<DEG, ELAST, MASS, COLOURED, CPB><<<grid, kThreads, 0, s>>>(
+      a, A->row_ptr, A->cols, (double*)A->vals, map, bc, list, count, status);
+}
+
+// Launch the matrix kernel for one cell list with cpb cells per block.
 template <int DEG, bool ELAST, bool MASS, bool COLOURED>
 void launch_cells(const dfx_form& a, const dfx_csr* A, const uint8_t* map, const int8_t* bc,
-                  const int32_t* list, int32_t count, int* status, cudaStream_t s)
+                  const int32_t* list, int32_t count, int* status, int cpb, cudaStream_t s)
 {
-  constexpr int CPB = Traits<DEG, ELAST>::CPB;
   if (count <= 0)
     return;
-  const unsigned grid = (unsigned)((count + CPB - 1) / CPB);
-  k_cells_matrix<DEG, ELAST, MASS, COLOURED><<<grid, kThreads, 0, s>>>(
-      a, A->row_ptr, A->cols, (double*)A->vals, map, bc, list, count, status);
+  if constexpr (ELAST)
+  {
+    if (cpb == 2)
+      launch_cells_cpb<DEG, ELAST, MASS, COLOURED, 2>(a, A, map, bc, list, count, status, s);
+    else if (cpb == 8)
+      launch_cells_cpb<DEG, ELAST, MASS, COLOURED, 8>(a, A, map, bc, list, count, status, s);
+    else
+      launch_cells_cpb<DEG, ELAST, MASS, COLOURED, 4>(a, A, map, bc, list, count, status, s);
+  }
+  else
+  {
+    if (cpb == 16)
+      launch_cells_cpb<DEG, ELAST, MASS, COLOURED, 16>(a, A, map, bc, list, count, status, s);
+    else if (cpb == 64)
+      launch_cells_cpb<DEG, ELAST, MASS, COLOURED, 64>(a, A, map, bc, list, count, status, s);
+    else
+      launch_cells_cpb<DEG, ELAST, MASS, COLOURED, 32>(a, A, map, bc, list, count, status, s);
+  }
 }
 
 template <bool COLOURED>
 void dispatch_cells(const dfx_form& a, const dfx_csr* A, const uint8_t* map, const int8_t* bc,
-                    const int32_t* list, int32_t count, int* status, cudaStream_t s)
+                    const int32_t* list, int32_t count, int* status, int cpb, cudaStream_t s)
 {
   const bool mass = a.kind == DFX_FORM_POISSON && a.k2 != 0.0;
   if (a.kind == DFX_FORM_ELASTICITY)
-    launch_cells<2, true, false, COLOURED>(a, A, map, bc, list, count, status, s);
+    launch_cells<2, true, false, COLOURED>(a, A, map, bc, list, count, status, cpb, s);
   else if (a.degree == 1)
   {
     if (mass)
-      launch_cells<1, false, true, COLOURED>(a, A, map, bc, list, count, status, s);
+      launch_cells<1, false, true, COLOURED>(a, A, map, bc, list, count, status, cpb, s);
     else
-      launch_cells<1, false, false, COLOURED>(a, A, map, bc, list, count, status, s);
+      launch_cells<1, false, false, COLOURED>(a, A, map, bc, list, count, status, cpb, s);
   }
   else
   {
     if (mass)
-      launch_cells<2, false, true, COLOURED>(a, A, map, bc, list, count, status, s);
+      launch_cells<2, false, true, COLOURED>(a, A, map, bc, list, count, status, cpb, s);
     else
-      launch_cells<2, false, false, COLOURED>(a, A, map, bc, list, count, status, s);
+      launch_cells<2, false, false, COLOURED>(a, A, map, bc, list, count, status, cpb, s);
   }
 }
 
@@ -695,10 +752,36 @@ extern "C" int dfx_slot_map_create(const dfx_form* a, const dfx_csr* A, uint8_t*
   return read_status(status, s);
 }
 
-extern "C" int dfx_assemble_matrix(const dfx_form* a, const dfx_csr* A, const uint8_t* d_map,
-                                   const int8_t* d_bc, int32_t mode, const int32_t* d_order,
-                                   const int32_t* colour_offsets, int32_t num_colours,
-                                   void* stream)
+namespace
+{
+// dfx_assemble_matrix with cpb cells per block (arguments checked).
+int assemble_matrix_cpb(const dfx_form* a, const dfx_csr* A, const uint8_t* d_map,
+                        const int8_t* d_bc, int32_t mode, const int32_t* d_order,
+                        const int32_t* colour_offsets, int32_t num_colours, int cpb,
+                        cudaStream_t s)
+{
+  int* status = dfx::device_status_page();
+  DFX_REQUIRE(status, "could not allocate the status page");
+  if (!d_map)
+    DFX_CUDA(cudaMemsetAsync(status, 0, sizeof(int), s));
+  if (mode == DFX_MODE_ATOMIC)
+    dispatch_cells<false>(*a, A, d_map, d_bc, nullptr, a->num_cells, status, cpb, s);
+  else if (mode == DFX_MODE_COLOURED)
+  {
+    DFX_REQUIRE(d_order && colour_offsets && num_colours > 0, "coloured mode needs a colouring");
+    for (int k = 0; k < num_colours; ++k)
+      dispatch_cells<true>(*a, A, d_map, d_bc, d_order + colour_offsets[k],
+                           colour_offsets[k + 1] - colour_offsets[k], status, cpb, s);
+  }
+  else
+    return dfx::fail(DFX_ERR_INVALID, "unknown assembly mode %d", mode);
+  DFX_CHECK_LAUNCH();
+  if (!d_map)
+    return read_status(status, s);
+  return DFX_OK;
+}
+
+int check_matrix_args(const dfx_form* a, const dfx_csr* A)
 {
   if (int st = check_form(a, true))
     return st;
@@ -706,27 +789,91 @@ extern "C" int dfx_assemble_matrix(const dfx_form* a, const dfx_csr* A, const ui
   DFX_REQUIRE(A->dtype == DFX_F64, "assembly writes FP64 values");
   DFX_REQUIRE(A->bs == form_bs(a), "matrix block size %d does not match the form (%d)", A->bs,
               form_bs(a));
+  return DFX_OK;
+}
+} // namespace
+
+extern "C" int dfx_assemble_matrix(const dfx_form* a, const dfx_csr* A, const uint8_t* d_map,
+                                   const int8_t* d_bc, int32_t mode, const int32_t* d_order,
+                                   const int32_t* colour_offsets, int32_t num_colours,
+                                   void* stream)
+{
+  if (int st = check_matrix_args(a, A))
+    return st;
   if (a->num_cells == 0)
     return DFX_OK;
+  return assemble_matrix_cpb(a, A, d_map, d_bc, mode, d_order, colour_offsets, num_colours,
+                             cells_per_block(*a, mode), dfx::as_stream(stream));
+}
+
+extern "C" int dfx_tune_assembly(const dfx_form* a, const dfx_csr* A, const uint8_t* d_map,
+                                 const int8_t* d_bc, int32_t mode, const int32_t* d_order,
+                                 const int32_t* colour_offsets, int32_t num_colours,
+                                 double* d_scratch_vals, int32_t* best, float* ms, void* stream)
+{
+  if (int st = check_matrix_args(a, A))
+    return st;
+  DFX_REQUIRE(d_scratch_vals && best, "scratch values and best must be non-NULL");
+  DFX_REQUIRE(mode == DFX_MODE_ATOMIC || mode == DFX_MODE_COLOURED, "unknown assembly mode %d",
+              mode);
   cudaStream_t s = dfx::as_stream(stream);
-  int* status = dfx::device_status_page();
-  DFX_REQUIRE(status, "could not allocate the status page");
-  if (!d_map)
-    DFX_CUDA(cudaMemsetAsync(status, 0, sizeof(int), s));
-  if (mode == DFX_MODE_ATOMIC)
-    dispatch_cells<false>(*a, A, d_map, d_bc, nullptr, a->num_cells, status, s);
-  else if (mode == DFX_MODE_COLOURED)
+  dfx_csr scratch = *A;
+  scratch.vals = d_scratch_vals; // the candidates accumulate here, not into A
+  const int* cand = cpb_candidates(*a);
+  constexpr int kReps = 3;
+  cudaEvent_t e0, e1;
+  DFX_CUDA(cudaEventCreate(&e0));
+  DFX_CUDA(cudaEventCreate(&e1));
+  int pick = 0;
+  float pick_ms = 0.0f;
+  int st = DFX_OK;
+  for (int c = 0; c < 3 && !st; ++c)
   {
-    DFX_REQUIRE(d_order && colour_offsets && num_colours > 0, "coloured mode needs a colouring");
-    for (int k = 0; k < num_colours; ++k)
-      dispatch_cells<true>(*a, A, d_map, d_bc, d_order + colour_offsets[k],
-                           colour_offsets[k + 1] - colour_offsets[k], status, s);
+    st = assemble_matrix_cpb(a, &scratch, d_map, d_bc, mode, d_order, colour_offsets,
+                             num_colours, cand[c], s); // warm-up
+    if (!st && cudaEventRecord(e0, s) != cudaSuccess)
+      st = dfx::fail(DFX_ERR_CUDA, "event record failed");
+    for (int r = 0; r < kReps && !st; ++r)
+      st = assemble_matrix_cpb(a, &scratch, d_map, d_bc, mode, d_order, colour_offsets,
+                               num_colours, cand[c], s);
+    float t = 0.0f;
+    if (!st && (cudaEventRecord(e1, s) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess
+                || cudaEventElapsedTime(&t, e0, e1) != cudaSuccess))
+      st = dfx::fail(DFX_ERR_CUDA, "assembly timing failed");
+    t /= kReps;
+    if (ms)
+      ms[c] = t;
+    if (!st && (pick == 0 || t < pick_ms))
+    {
+      pick = cand[c];
+      pick_ms = t;
+    }
   }
-  else
-    return dfx::fail(DFX_ERR_INVALID, "unknown assembly mode %d", mode);
-  DFX_CHECK_LAUNCH();
-  if (!d_map)
-    return read_status(status, s);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st)
+    return st;
+  dfx::tuned_set(dfx::kTuneAssembly, a->num_cells, assembly_key(*a, mode), 0, pick);
+  *best = pick;
+  return DFX_OK;
+}
+
+extern "C" int dfx_set_cells_per_block(const dfx_form* a, int32_t mode, int32_t cpb)
+{
+  if (int st = check_form(a, true))
+    return st;
+  DFX_REQUIRE(cpb == 0 || valid_cpb(*a, cpb),
+              "cells per block %d is not a candidate for this form", cpb);
+  dfx::tuned_set(dfx::kTuneAssembly, a->num_cells, assembly_key(*a, mode), 0, cpb);
+  return DFX_OK;
+}
+
+extern "C" int dfx_get_cells_per_block(const dfx_form* a, int32_t mode, int32_t* cpb)
+{
+  if (int st = check_form(a, true))
+    return st;
+  DFX_REQUIRE(cpb, "cpb must be non-NULL");
+  *cpb = cells_per_block(*a, mode);
   return DFX_OK;
 }
 

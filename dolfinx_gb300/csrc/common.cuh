@@ -23,6 +23,14 @@ int* device_status_page();
 
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// Launch parameters picked by the autotuner, per device and workload key
+// (a process-wide table; 0 = no entry). what: kTuneAssembly (cells per
+// block of the matrix assembly kernel) or kTuneSpmv (lanes per CSR row).
+constexpr int kTuneAssembly = 1;
+constexpr int kTuneSpmv = 2;
+int tuned_get(int what, int64_t k0, int64_t k1, int64_t k2);
+void tuned_set(int what, int64_t k0, int64_t k1, int64_t k2, int value); // 0 removes
+
 } // namespace dfx
 
 #define DFX_CUDA(call)                                                         \

@@ -60,14 +60,21 @@ __global__ void k_sum_partials(const double* __restrict__ partial, int n, double
 
 namespace dfx
 {
-int launch_spmv(const dfx_csr* A, const void* x, void* y, double beta, cudaStream_t s)
+int spmv_lanes(const dfx_csr* A)
+{
+  const int t = tuned_get(kTuneSpmv, A->nrows, A->nnz, 4 * A->bs + A->dtype);
+  return t ? t : spmv_lanes_heuristic(A);
+}
+
+int launch_spmv(const dfx_csr* A, const void* x, void* y, double beta, cudaStream_t s, int lanes)
 {
   const bool acc = beta != 0.0;
   if (A->nrows == 0)
     return DFX_OK;
   if (A->bs == 1)
   {
-    const int lanes = spmv_lanes(A);
+    if (lanes == 0)
+      lanes = spmv_lanes(A);
     const int rows_per_block = kSpmvThreads / lanes;
     const unsigned grid = (unsigned)((A->nrows + rows_per_block - 1) / rows_per_block);
     if (A->dtype == DFX_F64)
@@ -159,6 +166,71 @@ extern "C" int dfx_spmv(const dfx_csr* A, const void* d_x, void* d_y, double bet
   DFX_REQUIRE(beta == 0.0 || beta == 1.0, "beta must be 0 or 1");
   DFX_REQUIRE(d_x && d_y, "x and y must be non-NULL");
   return dfx::launch_spmv(A, d_x, d_y, beta, dfx::as_stream(stream));
+}
+
+extern "C" int dfx_tune_spmv(const dfx_csr* A, const void* d_x, void* d_y, int32_t* best_lanes,
+                             float* ms, void* stream)
+{
+  if (int st = dfx::check_csr(A))
+    return st;
+  DFX_REQUIRE(A->bs == 1, "the row split applies to scalar CSR matrices");
+  DFX_REQUIRE(d_x && d_y && best_lanes, "x, y and best_lanes must be non-NULL");
+  cudaStream_t s = dfx::as_stream(stream);
+  constexpr int kCand[4] = {4, 8, 16, 32};
+  constexpr int kReps = 5;
+  cudaEvent_t e0, e1;
+  DFX_CUDA(cudaEventCreate(&e0));
+  DFX_CUDA(cudaEventCreate(&e1));
+  int best = 0;
+  float best_ms = 0.0f;
+  int st = DFX_OK;
+  for (int c = 0; c < 4 && !st; ++c)
+  {
+    st = dfx::launch_spmv(A, d_x, d_y, 0.0, s, kCand[c]); // warm-up
+    if (!st && cudaEventRecord(e0, s) != cudaSuccess)
+      st = dfx::fail(DFX_ERR_CUDA, "event record failed");
+    for (int r = 0; r < kReps && !st; ++r)
+      st = dfx::launch_spmv(A, d_x, d_y, 0.0, s, kCand[c]);
+    float t = 0.0f;
+    if (!st && (cudaEventRecord(e1, s) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess
+                || cudaEventElapsedTime(&t, e0, e1) != cudaSuccess))
+      st = dfx::fail(DFX_ERR_CUDA, "SpMV timing failed");
+    t /= kReps;
+    if (ms)
+      ms[c] = t;
+    if (!st && (best == 0 || t < best_ms))
+    {
+      best = kCand[c];
+      best_ms = t;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st)
+    return st;
+  dfx::tuned_set(dfx::kTuneSpmv, A->nrows, A->nnz, 4 * A->bs + A->dtype, best);
+  *best_lanes = best;
+  return DFX_OK;
+}
+
+extern "C" int dfx_set_spmv_lanes(const dfx_csr* A, int32_t lanes)
+{
+  if (int st = dfx::check_csr(A))
+    return st;
+  DFX_REQUIRE(A->bs == 1, "the row split applies to scalar CSR matrices");
+  DFX_REQUIRE(lanes == 0 || lanes == 4 || lanes == 8 || lanes == 16 || lanes == 32,
+              "lanes per row must be 4, 8, 16 or 32 (0: default)");
+  dfx::tuned_set(dfx::kTuneSpmv, A->nrows, A->nnz, 4 * A->bs + A->dtype, lanes);
+  return DFX_OK;
+}
+
+extern "C" int dfx_get_spmv_lanes(const dfx_csr* A, int32_t* lanes)
+{
+  if (int st = dfx::check_csr(A))
+    return st;
+  DFX_REQUIRE(lanes, "lanes must be non-NULL");
+  *lanes = A->bs == 1 ? dfx::spmv_lanes(A) : 8;
+  return DFX_OK;
 }
 
 extern "C" int dfx_csr_values_to_f32(const dfx_csr* A, float* d_vals32, void* stream)

@@ -15,11 +15,18 @@ namespace dfx
 {
 constexpr int kSpmvThreads = 256;
 
-int launch_spmv(const dfx_csr* A, const void* x, void* y, double beta, cudaStream_t s);
+// y (+)= A x with `lanes` lanes per row (scalar CSR; 0: spmv_lanes(A)).
+int launch_spmv(const dfx_csr* A, const void* x, void* y, double beta, cudaStream_t s,
+                int lanes = 0);
 int check_csr(const dfx_csr* A);
 
+// Lanes per row of a scalar CSR matrix: the autotuner's choice for this
+// matrix shape (dfx_tune_spmv / dfx_set_spmv_lanes) if there is one, else
+// spmv_lanes_heuristic.
+int spmv_lanes(const dfx_csr* A);
+
 // Lanes per row for a scalar CSR matrix from its mean row length.
-inline int spmv_lanes(const dfx_csr* A)
+inline int spmv_lanes_heuristic(const dfx_csr* A)
 {
   const double avg = A->nrows ? (double)A->nnz / A->nrows : 0.0;
   if (avg <= 6)

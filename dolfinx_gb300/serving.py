@@ -43,7 +43,7 @@ from dataclasses import dataclass, field
 import numpy as np
 import torch
 
-from . import _capi, fem, la, mesh
+from . import _capi, autotune, fem, la, mesh
 
 
 @dataclass
@@ -90,7 +90,9 @@ def _stream_ptr(s):
 class Structure:
     """Everything of one (n, degree) that requests share."""
 
-    def __init__(self, n: int, degree: int, device="cuda"):
+    def __init__(self, n: int, degree: int, device="cuda", tune: bool = True):
+        """tune: time the launch-shape candidates on this structure (cells per
+        block of the assembly, sliced-ELL window sigma) and use the fastest."""
         self.n, self.degree = n, degree
         self.mesh = mesh.create_unit_cube(n, n, n)
         self.V = fem.functionspace(self.mesh, ("Lagrange", degree), device=device)
@@ -101,8 +103,14 @@ class Structure:
         self.asm = fem.MatrixAssembler(a, [self.bc])  # slot map, markers, structure
         self.A0 = self.asm.A
         self.A0.vals.fill_(1.0)  # any values: the operators copy only the structure here
-        self.op64 = la.SellOperator(self.A0, torch.float64)
-        self.op32 = la.SellOperator(self.A0, torch.float32, compress_cols=True)
+        sigma = 256
+        self.tuning = {}
+        if tune:
+            self.tuning["assembly"] = autotune.tune_assembly(self.asm)
+            self.tuning["sigma"] = autotune.tune_sigma(self.A0)
+            sigma = self.tuning["sigma"]["sigma"]
+        self.op64 = la.SellOperator(self.A0, torch.float64, sigma)
+        self.op32 = la.SellOperator(self.A0, torch.float32, sigma, compress_cols=True)
         self.ndofs = self.V.num_dofs
         self.nnz = self.A0.nnz
         self.mesh.device(device)

@@ -276,6 +276,40 @@ int dfx_cg_solve_noalloc(const dfx_csr* A, const double* d_b, double* d_x,
                          const double* d_dinv, double rtol, int32_t max_iters,
                          int32_t check_every, dfx_cg_info* info, void* stream);
 
+/* -------------------------------------------------------------- autotuner
+ * No reference counterpart: the launch shapes of the assembly and CSR SpMV
+ * kernels on this GPU. The library keeps one process-wide table of choices
+ * per device and workload; a workload without an entry uses the defaults
+ * (32 cells per block, 4 for elasticity; lanes per row from the mean row
+ * length). */
+
+/* Times the matrix assembly kernel with 16, 32 and 64 cells per block (2, 4
+ * and 8 for elasticity), accumulating into d_scratch_vals (A->nnz*bs*bs
+ * doubles; A's values are not touched). Records the fastest for this form
+ * (kind, degree, mass term, number of cells) and mode, and returns it in
+ * *best. ms (3 floats, may be NULL) receives each candidate's mean time per
+ * assembly. Synchronises `stream`. */
+int dfx_tune_assembly(const dfx_form* a, const dfx_csr* A, const uint8_t* d_map,
+                      const int8_t* d_bc, int32_t mode, const int32_t* d_order,
+                      const int32_t* colour_offsets, int32_t num_colours,
+                      double* d_scratch_vals, int32_t* best, float* ms, void* stream);
+/* Pin (cpb = one of the candidates) or reset (cpb = 0) the choice; read the
+ * choice in force. */
+int dfx_set_cells_per_block(const dfx_form* a, int32_t mode, int32_t cpb);
+int dfx_get_cells_per_block(const dfx_form* a, int32_t mode, int32_t* cpb);
+
+/* Row split of the scalar CSR SpMV (dfx_spmv and the CSR CG): times 4, 8,
+ * 16 and 32 lanes per row on d_y = A d_x (d_y is overwritten), records the
+ * fastest for matrices of this shape (rows, entries, dtype) and returns it
+ * in *best_lanes. ms (4 floats, may be NULL) receives the mean times.
+ * Synchronises `stream`. */
+int dfx_tune_spmv(const dfx_csr* A, const void* d_x, void* d_y, int32_t* best_lanes,
+                  float* ms, void* stream);
+int dfx_set_spmv_lanes(const dfx_csr* A, int32_t lanes); /* 0: default */
+int dfx_get_spmv_lanes(const dfx_csr* A, int32_t* lanes);
+/* Forget every recorded choice. */
+int dfx_tune_clear(void);
+
 /* ------------------------------------------------- sliced-ELL operator
  * The solver-side copy of a scalar MatrixCSR: rows sorted by length
  * within windows of `sigma` rows (a multiple of 32), the system renumbered
