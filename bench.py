@@ -54,6 +54,8 @@ def parse():
     p.add_argument("--c4-only", action="store_true",
                    help="run only the matrix-free Q4 sample and print its JSON")
     p.add_argument("--c4-n", type=int, default=64, help="Q4 hexahedra per direction")
+    p.add_argument("--profile-step", action="store_true",
+                   help="run one mixed-precision c2 step only (for an ncu launch list)")
     p.add_argument("--profile", action="store_true",
                    help="profiling target: a few launches of every hot kernel, no timing")
     return p.parse_args()
@@ -827,8 +829,27 @@ def run_profile(args):
     print(json.dumps({"profile": "ok", "inner_iterations": r.inner_iterations}))
 
 
+def run_profile_step(args):
+    """One full mixed-precision c2 step (assembly, right-hand side, operator
+    refresh, solve to rtol 1e-10) after the set-up and autotuning: the run
+    behind the kernel launch list."""
+    import torch
+
+    torch.cuda.set_device(0)
+    m, kappa, f = make_inputs(args.n, seed=0)
+    P = Problem(m, kappa, f, mode=args.mode, inner_rtol=args.inner_rtol, variant=args.ir_variant)
+    torch.cuda.synchronize()
+    r = P.step_ir()
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_step": "ok", "inner_iterations": r.inner_iterations,
+                      "outer_iterations": r.outer_iterations}))
+
+
 def main():
     args = parse()
+    if args.profile_step:
+        run_profile_step(args)
+        return
     if args.profile:
         run_profile(args)
     elif args.c4_only:
