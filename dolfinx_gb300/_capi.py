@@ -26,6 +26,7 @@ FORM_POISSON = 0
 FORM_ELASTICITY = 1
 FORM_SOURCE = 2
 FORM_BODYFORCE = 3
+FORM_FACET_MASS = 4
 
 MODE_ATOMIC = 0
 MODE_COLOURED = 1
@@ -133,6 +134,13 @@ _SIGS = {
     "dfx_sparsity_create_device": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, _P, _P, _P, _P, _P,
                                              C.c_size_t, _P]),
     "dfx_colour_cells": (C.c_int, [C.c_int32, C.c_int32, _P, C.c_int32, _P, _P, C.c_int32, _P]),
+    "dfx_exterior_facets_tet": (C.c_int, [C.c_int32, _P, _P, C.POINTER(C.c_int32)]),
+    "dfx_assemble_vector_facets": (C.c_int, [C.POINTER(Form), _P, C.c_int32, _P, _P]),
+    "dfx_assemble_matrix_facets": (C.c_int, [C.POINTER(Form), _P, C.c_int32, C.POINTER(Csr), _P,
+                                             _P, _P]),
+    "dfx_assemble_scalar_workspace_bytes": (C.c_size_t, [C.c_int32]),
+    "dfx_assemble_scalar": (C.c_int, [C.POINTER(Form), _P, C.POINTER(C.c_double), _P, C.c_size_t,
+                                      _P]),
     "dfx_slot_map_bytes": (C.c_size_t, [C.POINTER(Form)]),
     "dfx_slot_map_create": (C.c_int, [C.POINTER(Form), C.POINTER(Csr), _P, _P]),
     "dfx_assemble_matrix": (C.c_int, [C.POINTER(Form), C.POINTER(Csr), _P, _P, C.c_int32, _P, _P,

@@ -972,3 +972,361 @@ extern "C" int dfx_set_diagonal(const dfx_csr* A, const int32_t* d_dofs, int32_t
   DFX_CHECK_LAUNCH();
   return read_status(status, s);
 }
+
+// ------------------------------------------------------------------------
+// Exterior facet integrals and functionals.
+//
+// An exterior-facet domain is a list of (cell, local facet) pairs, facet f
+// of a tetrahedron being the triangle opposite its vertex f (Basix
+// numbering; fem/utils.h:155-162). The integrals use the exact P1/P2
+// triangle integrals of area A (products of barycentrics,
+// \int l0^a l1^b l2^c = 2A a! b! c! / (a+b+c+2)!), one thread per facet and
+// FP64 atomics into the caller's vector or CSR values.
+// ------------------------------------------------------------------------
+namespace
+{
+// Local vertices of facet f, and the local P2 edge opposite each of them
+// inside the facet (the edge joining the other two; edges in Basix order).
+__constant__ int kFacetVerts[4][3] = {{1, 2, 3}, {0, 2, 3}, {0, 1, 3}, {0, 1, 2}};
+__constant__ int kFacetEdges[4][3] = {{0, 1, 2}, {0, 3, 4}, {1, 3, 5}, {2, 4, 5}};
+
+// Facet vertices' coordinates (3 x 3) and area.
+__device__ __forceinline__ double facet_geometry(const dfx_form& a, int32_t c, int f, int* lv,
+                                                 int32_t* gnode)
+{
+  const int4 xd = __ldg(reinterpret_cast<const int4*>(a.x_dofmap) + c);
+  const int32_t nodes[4] = {xd.x, xd.y, xd.z, xd.w};
+  double p[3][3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+  {
+    lv[k] = kFacetVerts[f][k];
+    gnode[k] = nodes[lv[k]];
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+      p[k][d] = __ldg(a.x + 3 * (int64_t)gnode[k] + d);
+  }
+  const double u[3] = {p[1][0] - p[0][0], p[1][1] - p[0][1], p[1][2] - p[0][2]};
+  const double v[3] = {p[2][0] - p[0][0], p[2][1] - p[0][1], p[2][2] - p[0][2]};
+  const double n0 = u[1] * v[2] - u[2] * v[1];
+  const double n1 = u[2] * v[0] - u[0] * v[2];
+  const double n2 = u[0] * v[1] - u[1] * v[0];
+  return 0.5 * sqrt(n0 * n0 + n1 * n1 + n2 * n2);
+}
+
+// b += \int_F g v ds, g a P1 coefficient (per geometry node, or g_const):
+// P1: A/12 (g_i + S); P2 vertex: A/60 (3 g_i - S); P2 edge opposite
+// vertex i: A/15 (2 S - g_i), S = g_0 + g_1 + g_2.
+template <int DEG>
+__global__ void k_facets_vector(const dfx_form a, const int32_t* __restrict__ facets,
+                                int32_t nf, double* __restrict__ b)
+{
+  constexpr int ND = DEG == 1 ? 4 : 10;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nf)
+    return;
+  const int2 cf = __ldg(reinterpret_cast<const int2*>(facets) + t);
+  int lv[3];
+  int32_t gn[3];
+  const double A = facet_geometry(a, cf.x, cf.y, lv, gn);
+  double g[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+    g[k] = a.f ? __ldg(a.f + gn[k]) : a.f_const[0];
+  const double S = g[0] + g[1] + g[2];
+  const int32_t* dofs = a.dofmap + (int64_t)ND * cf.x;
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+  {
+    const double vk = DEG == 1 ? A / 12.0 * (g[k] + S) : A / 60.0 * (3.0 * g[k] - S);
+    atomicAdd(b + __ldg(dofs + lv[k]), vk);
+    if (DEG == 2)
+      atomicAdd(b + __ldg(dofs + 4 + kFacetEdges[cf.y][k]), A / 15.0 * (2.0 * S - g[k]));
+  }
+}
+
+// A += \int_F alpha u v ds (alpha per cell or constant) through the cell
+// slot map; constrained rows and columns are skipped
+// (fem/assemble_matrix_impl.h:265-379). Facet mass in units of A: P1
+// (1 + delta_ij)/12; P2 (vertices, then the edge opposite each vertex)
+// 1/180 x {6 diagonal, -1 vertex-vertex, -4 vertex-opposite edge, 0
+// vertex-adjacent edge, 32 edge diagonal, 16 edge-edge}.
+template <int DEG>
+__global__ void k_facets_matrix(const dfx_form a, const int32_t* __restrict__ facets,
+                                int32_t nf, const int64_t* __restrict__ row_ptr,
+                                const int32_t* __restrict__ cols, double* __restrict__ vals,
+                                const uint8_t* __restrict__ map, const int8_t* __restrict__ bc,
+                                int* __restrict__ status)
+{
+  constexpr int ND = DEG == 1 ? 4 : 10;
+  constexpr int NF = DEG == 1 ? 3 : 6; // facet dofs
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nf)
+    return;
+  const int2 cf = __ldg(reinterpret_cast<const int2*>(facets) + t);
+  int lv[3];
+  int32_t gn[3];
+  const double A = facet_geometry(a, cf.x, cf.y, lv, gn);
+  const double s = (a.kappa ? __ldg(a.kappa + cf.x) : a.kappa_const) * A;
+  int loc[NF];
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+  {
+    loc[k] = lv[k];
+    if (DEG == 2)
+      loc[3 + k] = 4 + kFacetEdges[cf.y][k];
+  }
+  const int32_t* dofs = a.dofmap + (int64_t)ND * cf.x;
+  for (int i = 0; i < NF; ++i)
+  {
+    const int32_t di = __ldg(dofs + loc[i]);
+    if (bc && __ldg(bc + di))
+      continue;
+    const int64_t rb = __ldg(row_ptr + di);
+    for (int j = 0; j < NF; ++j)
+    {
+      const int32_t dj = __ldg(dofs + loc[j]);
+      if (bc && __ldg(bc + dj))
+        continue;
+      double m;
+      if (DEG == 1)
+        m = (i == j ? 2.0 : 1.0) / 12.0;
+      else
+      {
+        const bool vi = i < 3, vj = j < 3;
+        const int ii = i % 3, jj = j % 3;
+        if (vi && vj)
+          m = i == j ? 6.0 : -1.0;
+        else if (!vi && !vj)
+          m = i == j ? 32.0 : 16.0;
+        else
+          m = ii == jj ? -4.0 : 0.0;
+        m /= 180.0;
+      }
+      int64_t pos;
+      if (map)
+        pos = rb + map[((int64_t)cf.x * ND + loc[i]) * ND + loc[j]];
+      else
+      {
+        const int64_t re = __ldg(row_ptr + di + 1);
+        pos = row_search(cols, rb, re, dj);
+        if (pos >= re || __ldg(cols + pos) != dj)
+        {
+          atomicExch(status, (int)DFX_ERR_NOT_IN_SPARSITY);
+          continue;
+        }
+      }
+      atomicAdd(vals + pos, s * m);
+    }
+  }
+}
+
+// Functional cell loop (fem/assemble_scalar_impl.h:32-61): per cell
+// a(u_e, u_e) with the Poisson/Helmholtz element tensor, or L(u_e) with the
+// P1-source element vector; block partial sums in FP64, each block's
+// warps summed in a fixed order.
+template <int DEG, bool SOURCE, bool MASS>
+__global__ void __launch_bounds__(kThreads)
+    k_cells_scalar(const dfx_form a, const double* __restrict__ u, double* __restrict__ part)
+{
+  constexpr int ND = DEG == 1 ? 4 : 10;
+  constexpr int NU = ND * (ND + 1) / 2;
+  __shared__ double sh[kThreads / 32];
+  double v = 0.0;
+  for (int64_t c = (int64_t)blockIdx.x * kThreads + threadIdx.x; c < a.num_cells;
+       c += (int64_t)gridDim.x * kThreads)
+  {
+    double xc[12];
+    load_cell_coords(a, c, xc);
+    double ue[ND];
+#pragma unroll
+    for (int i = 0; i < ND; ++i)
+      ue[i] = __ldg(u + __ldg(a.dofmap + c * ND + i));
+    if constexpr (SOURCE)
+    {
+      double f[4];
+      const int4 xd = __ldg(reinterpret_cast<const int4*>(a.x_dofmap) + c);
+      if (a.f)
+      {
+        f[0] = __ldg(a.f + xd.x);
+        f[1] = __ldg(a.f + xd.y);
+        f[2] = __ldg(a.f + xd.z);
+        f[3] = __ldg(a.f + xd.w);
+      }
+      else
+        f[0] = f[1] = f[2] = f[3] = a.f_const[0];
+      double be[ND];
+      const double adet = tet_absdet(xc);
+      if constexpr (DEG == 1)
+        tet_p1_source(f, adet, be);
+      else
+        tet_p2_source(f, adet, be);
+#pragma unroll
+      for (int i = 0; i < ND; ++i)
+        v += be[i] * ue[i];
+    }
+    else
+    {
+      const double kap = a.kappa ? __ldg(a.kappa + c) : a.kappa_const;
+      double G[6];
+      const double adet = tet_metric(xc, kap, G);
+      double Ae[NU];
+      if constexpr (DEG == 1)
+        tet_p1_poisson_upper<MASS>(G, a.k2 * adet, Ae);
+      else
+        tet_p2_poisson_upper<MASS>(G, a.k2 * adet, Ae);
+#pragma unroll
+      for (int i = 0; i < ND; ++i)
+      {
+        double r = 0.0;
+#pragma unroll
+        for (int j = i + 1; j < ND; ++j)
+          r += Ae[packed(i, j, ND)] * ue[j];
+        v += ue[i] * (Ae[packed(i, i, ND)] * ue[i] + 2.0 * r);
+      }
+    }
+  }
+  v = dfx::warp_sum(v);
+  if ((threadIdx.x & 31) == 0)
+    sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0)
+  {
+    double s = 0.0;
+    for (int w = 0; w < kThreads / 32; ++w)
+      s += sh[w];
+    part[blockIdx.x] = s;
+  }
+}
+
+// Sum of the block partials in index order (one thread: a few thousand
+// values at most).
+__global__ void k_sum_partials(const double* __restrict__ part, int n, double* __restrict__ out)
+{
+  if (threadIdx.x == 0 && blockIdx.x == 0)
+  {
+    double s = 0.0;
+    for (int i = 0; i < n; ++i)
+      s += part[i];
+    *out = s;
+  }
+}
+
+int scalar_blocks(int32_t num_cells)
+{
+  const int need = (num_cells + kThreads - 1) / kThreads;
+  return std::max(1, std::min(need, 8 * dfx::num_sms()));
+}
+
+int check_facet_form(const dfx_form* a, int32_t kind, const int32_t* d_facets, int32_t nf)
+{
+  DFX_REQUIRE(a, "form is NULL");
+  DFX_REQUIRE(a->kind == kind, "form kind %d is not %d", a->kind, kind);
+  DFX_REQUIRE(a->degree == 1 || a->degree == 2, "degree %d not supported", a->degree);
+  DFX_REQUIRE(nf >= 0, "negative facet count");
+  DFX_REQUIRE(nf == 0 || (d_facets && a->x_dofmap && a->x && a->dofmap),
+              "facets and form arrays must be non-NULL");
+  DFX_REQUIRE(((uintptr_t)d_facets & 7) == 0, "facets must be 8-byte aligned");
+  DFX_REQUIRE(((uintptr_t)a->x_dofmap & 15) == 0, "x_dofmap must be 16-byte aligned");
+  return DFX_OK;
+}
+} // namespace
+
+extern "C" int dfx_assemble_vector_facets(const dfx_form* L, const int32_t* d_facets,
+                                          int32_t num_facets, double* d_b, void* stream)
+{
+  if (int st = check_facet_form(L, DFX_FORM_SOURCE, d_facets, num_facets))
+    return st;
+  DFX_REQUIRE(d_b, "b must be non-NULL");
+  if (num_facets == 0)
+    return DFX_OK;
+  const unsigned grid = (unsigned)((num_facets + kThreads - 1) / kThreads);
+  cudaStream_t s = dfx::as_stream(stream);
+  if (L->degree == 1)
+    k_facets_vector<1><<<grid, kThreads, 0, s>>>(*L, d_facets, num_facets, d_b);
+  else
+    k_facets_vector<2><<<grid, kThreads, 0, s>>>(*L, d_facets, num_facets, d_b);
+  DFX_CHECK_LAUNCH();
+  return DFX_OK;
+}
+
+extern "C" int dfx_assemble_matrix_facets(const dfx_form* a, const int32_t* d_facets,
+                                          int32_t num_facets, const dfx_csr* A,
+                                          const uint8_t* d_map, const int8_t* d_bc, void* stream)
+{
+  if (int st = check_facet_form(a, DFX_FORM_FACET_MASS, d_facets, num_facets))
+    return st;
+  DFX_REQUIRE(A && A->row_ptr && A->cols && A->vals, "matrix must be non-NULL");
+  DFX_REQUIRE(A->dtype == DFX_F64 && A->bs == 1, "facet mass assembles scalar FP64 matrices");
+  if (num_facets == 0)
+    return DFX_OK;
+  cudaStream_t s = dfx::as_stream(stream);
+  int* status = dfx::device_status_page();
+  DFX_REQUIRE(status, "could not allocate the status page");
+  DFX_CUDA(cudaMemsetAsync(status, 0, sizeof(int), s));
+  const unsigned grid = (unsigned)((num_facets + kThreads - 1) / kThreads);
+  if (a->degree == 1)
+    k_facets_matrix<1><<<grid, kThreads, 0, s>>>(*a, d_facets, num_facets, A->row_ptr, A->cols,
+                                                 (double*)A->vals, d_map, d_bc, status);
+  else
+    k_facets_matrix<2><<<grid, kThreads, 0, s>>>(*a, d_facets, num_facets, A->row_ptr, A->cols,
+                                                 (double*)A->vals, d_map, d_bc, status);
+  DFX_CHECK_LAUNCH();
+  if (!d_map)
+    return read_status(status, s);
+  return DFX_OK;
+}
+
+extern "C" size_t dfx_assemble_scalar_workspace_bytes(int32_t num_cells)
+{
+  if (num_cells < 0)
+    return 0;
+  return sizeof(double) * ((size_t)scalar_blocks(num_cells) + 1);
+}
+
+extern "C" int dfx_assemble_scalar(const dfx_form* M, const double* d_u, double* value,
+                                   void* d_work, size_t work_bytes, void* stream)
+{
+  DFX_REQUIRE(M && value, "form and value must be non-NULL");
+  DFX_REQUIRE(M->kind == DFX_FORM_POISSON || M->kind == DFX_FORM_SOURCE,
+              "functionals: a(u, u) of a Poisson/Helmholtz form or L(u) of a source form");
+  if (int st = check_form(M, M->kind == DFX_FORM_POISSON))
+    return st;
+  *value = 0.0;
+  if (M->num_cells == 0)
+    return DFX_OK;
+  DFX_REQUIRE(d_u, "u must be non-NULL");
+  const int nb = scalar_blocks(M->num_cells);
+  DFX_REQUIRE(d_work && work_bytes >= sizeof(double) * ((size_t)nb + 1),
+              "workspace too small");
+  double* part = (double*)d_work;
+  cudaStream_t s = dfx::as_stream(stream);
+  const bool mass = M->kind == DFX_FORM_POISSON && M->k2 != 0.0;
+  if (M->kind == DFX_FORM_SOURCE)
+  {
+    if (M->degree == 1)
+      k_cells_scalar<1, true, false><<<nb, kThreads, 0, s>>>(*M, d_u, part);
+    else
+      k_cells_scalar<2, true, false><<<nb, kThreads, 0, s>>>(*M, d_u, part);
+  }
+  else if (M->degree == 1)
+  {
+    if (mass)
+      k_cells_scalar<1, false, true><<<nb, kThreads, 0, s>>>(*M, d_u, part);
+    else
+      k_cells_scalar<1, false, false><<<nb, kThreads, 0, s>>>(*M, d_u, part);
+  }
+  else
+  {
+    if (mass)
+      k_cells_scalar<2, false, true><<<nb, kThreads, 0, s>>>(*M, d_u, part);
+    else
+      k_cells_scalar<2, false, false><<<nb, kThreads, 0, s>>>(*M, d_u, part);
+  }
+  DFX_CHECK_LAUNCH();
+  k_sum_partials<<<1, 32, 0, s>>>(part, nb, part + nb);
+  DFX_CHECK_LAUNCH();
+  DFX_CUDA(cudaMemcpyAsync(value, part + nb, sizeof(double), cudaMemcpyDeviceToHost, s));
+  DFX_CUDA(cudaStreamSynchronize(s));
+  return DFX_OK;
+}

@@ -462,3 +462,62 @@ extern "C" int dfx_colour_cells(int32_t num_cells, int32_t nd, const int32_t* do
   *num_colours = ncol;
   return DFX_OK;
 }
+
+extern "C" int dfx_exterior_facets_tet(int32_t num_cells, const int32_t* cells, int32_t* facets,
+                                       int32_t* num_facets)
+{
+  if (num_cells < 0 || !num_facets || (num_cells > 0 && (!cells || !facets)))
+    return dfx::fail(DFX_ERR_INVALID, "invalid exterior facet arguments");
+  const int64_t nf = 4 * (int64_t)num_cells;
+  // Facets keyed by their sorted vertex triple (three 21-bit fields when
+  // every vertex index fits, else two words); a facet seen once is
+  // exterior (mesh/utils.cpp:61-89).
+  int64_t vmax = 0;
+  for (int64_t i = 0; i < nf; ++i)
+  {
+    if (cells[i] < 0)
+      return dfx::fail(DFX_ERR_INVALID, "negative vertex index in cell %lld",
+                       (long long)(i / 4));
+    vmax = std::max<int64_t>(vmax, cells[i]);
+  }
+  const bool pack = vmax < (int64_t(1) << 21);
+  std::vector<std::pair<uint64_t, uint64_t>> keys(nf);
+  for (int64_t c = 0; c < num_cells; ++c)
+    for (int f = 0; f < 4; ++f)
+    {
+      uint64_t v[3];
+      for (int k = 0; k < 3; ++k)
+        v[k] = (uint64_t)cells[4 * c + kFacets[f][k]];
+      std::sort(v, v + 3);
+      const uint64_t idx = (uint64_t)(4 * c + f);
+      keys[4 * c + f] = pack ? std::make_pair((v[0] << 42) | (v[1] << 21) | v[2], idx)
+                             : std::make_pair((v[0] << 32) | v[1], (v[2] << 32) | idx);
+    }
+  std::sort(keys.begin(), keys.end());
+  auto same = [&](int64_t a, int64_t b)
+  {
+    if (pack)
+      return keys[a].first == keys[b].first;
+    return keys[a].first == keys[b].first && (keys[a].second >> 32) == (keys[b].second >> 32);
+  };
+  std::vector<uint8_t> exterior(nf, 0);
+  for (int64_t i = 0; i < nf;)
+  {
+    int64_t j = i + 1;
+    while (j < nf && same(i, j))
+      ++j;
+    if (j - i == 1)
+      exterior[pack ? keys[i].second : (keys[i].second & 0xffffffffu)] = 1;
+    i = j;
+  }
+  int32_t n = 0;
+  for (int64_t i = 0; i < nf; ++i)
+    if (exterior[i])
+    {
+      facets[2 * (int64_t)n] = (int32_t)(i / 4);
+      facets[2 * (int64_t)n + 1] = (int32_t)(i % 4);
+      ++n;
+    }
+  *num_facets = n;
+  return DFX_OK;
+}

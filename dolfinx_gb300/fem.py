@@ -182,21 +182,28 @@ def dirichletbc(value, dofs, V: FunctionSpace) -> DirichletBC:
 
 @dataclass
 class Form:
-    """A built-in form on a function space (cell integral only)."""
+    """A built-in form on a function space: a cell integral, or an
+    exterior-facet integral when ``facets`` holds its (cell, local facet)
+    domain on the device."""
 
     kind: int
     V: FunctionSpace
-    kappa: torch.Tensor | None = None  # per-cell coefficient (kappa or E)
+    kappa: torch.Tensor | None = None  # per-cell coefficient (kappa, E or alpha)
     kappa_const: float = 1.0
     k2: float = 0.0
     nu: float = 0.3
     f: torch.Tensor | None = None  # P1 source values on the geometry nodes
     f_const: tuple = (0.0, 0.0, 0.0)
+    facets: torch.Tensor | None = None  # (num_facets, 2) int32: exterior-facet integral
     _cache: dict = field(default_factory=dict, repr=False)
 
     @property
     def rank(self) -> int:
-        return 2 if self.kind in (_capi.FORM_POISSON, _capi.FORM_ELASTICITY) else 1
+        return 2 if self.kind in (_capi.FORM_POISSON, _capi.FORM_ELASTICITY,
+                                  _capi.FORM_FACET_MASS) else 1
+
+    def __add__(self, other):
+        return FormSum([self]) + other
 
     def cstruct(self) -> _capi.Form:
         V = self.V
@@ -207,6 +214,30 @@ class Form:
                           None if self.kappa is None else self.kappa.data_ptr(),
                           float(self.kappa_const), float(self.k2), float(self.nu),
                           None if self.f is None else self.f.data_ptr(), fc)
+
+
+class FormSum:
+    """Terms of one form on one space, e.g. a cell integral plus an
+    exterior-facet integral (a form with dx and ds parts): assembled into
+    one tensor, cell terms first."""
+
+    def __init__(self, terms):
+        self.terms = list(terms)
+        self.V = self.terms[0].V
+        assert all(t.V is self.V for t in self.terms), "terms on different spaces"
+        assert len({t.rank for t in self.terms}) == 1, "terms of different rank"
+
+    @property
+    def rank(self) -> int:
+        return self.terms[0].rank
+
+    def __add__(self, other):
+        more = other.terms if isinstance(other, FormSum) else [other]
+        return FormSum(self.terms + more)
+
+
+def _terms(a):
+    return a.terms if isinstance(a, FormSum) else [a]
 
 
 def _dev(v, V):
@@ -233,6 +264,32 @@ def source_form(V: FunctionSpace, f=1.0) -> Form:
     """L(v) = int f v dx, f constant or P1 values on the geometry nodes."""
     return Form(_capi.FORM_SOURCE, V, f=_dev(f, V),
                 f_const=(float(f) if np.isscalar(f) else 0.0, 0.0, 0.0))
+
+
+def _facets(V: FunctionSpace, facets):
+    if facets is None:
+        facets = V.mesh.exterior_facets()
+    t = torch.as_tensor(np.ascontiguousarray(facets, np.int32)) if not torch.is_tensor(facets) \
+        else facets
+    return t.to(device=V.device, dtype=torch.int32).contiguous()
+
+
+def facet_source_form(V: FunctionSpace, g=1.0, facets=None) -> Form:
+    """L(v) = int_F g v ds over exterior facets (all boundary facets by
+    default); g constant or P1 values on the geometry nodes."""
+    assert V.bs == 1
+    return Form(_capi.FORM_SOURCE, V, f=_dev(g, V),
+                f_const=(float(g) if np.isscalar(g) else 0.0, 0.0, 0.0),
+                facets=_facets(V, facets))
+
+
+def facet_mass_form(V: FunctionSpace, alpha=1.0, facets=None) -> Form:
+    """a(u,v) = int_F alpha u v ds over exterior facets (a Robin term);
+    alpha constant or per cell (the cell of each facet)."""
+    assert V.bs == 1
+    return Form(_capi.FORM_FACET_MASS, V, kappa=_dev(alpha, V),
+                kappa_const=float(alpha) if np.isscalar(alpha) else 1.0,
+                facets=_facets(V, facets))
 
 
 def body_force_form(V: FunctionSpace, f=(0.0, 0.0, -1.0)) -> Form:
@@ -282,37 +339,53 @@ def bc_markers(V: FunctionSpace, bcs) -> torch.Tensor | None:
 
 
 class MatrixAssembler:
-    """Reusable matrix assembly for one form: the cell->slot map, BC markers
-    and colouring are computed once (serving-style reuse)."""
+    """Reusable matrix assembly for one form (or a sum of cell and
+    exterior-facet terms): the cell->slot map, BC markers and colouring are
+    computed once (serving-style reuse). Facet terms scatter with FP64
+    atomics in either mode."""
 
-    def __init__(self, a: Form, bcs=(), diagonal: float = 1.0, mode: str = "atomic",
+    def __init__(self, a, bcs=(), diagonal: float = 1.0, mode: str = "atomic",
                  A: MatrixCSR | None = None, use_slot_map: bool = True):
         self.a, self.bcs, self.diagonal, self.mode = a, list(bcs), float(diagonal), _mode(mode)
-        self.A = create_matrix(a) if A is None else A
-        self.form = a.cstruct()
-        self.markers = bc_markers(a.V, self.bcs)
+        self.terms = _terms(a)
+        V = self.terms[0].V
+        self.A = create_matrix(self.terms[0]) if A is None else A
+        self.forms = [t.cstruct() for t in self.terms]
+        cells = [cs for t, cs in zip(self.terms, self.forms) if t.facets is None]
+        # The slot map depends only on the dofmap and the pattern: a facet-only
+        # form builds it through a cell form of the same space.
+        self.form = cells[0] if cells else Form(_capi.FORM_POISSON, V).cstruct()
+        self.markers = bc_markers(V, self.bcs)
         self.map = None
         if use_slot_map:
             nb = int(_capi.lib().dfx_slot_map_bytes(C.byref(self.form)))
-            self.map = torch.empty(nb, dtype=torch.uint8, device=a.V.device)
+            self.map = torch.empty(nb, dtype=torch.uint8, device=V.device)
             _capi.check(_capi.lib().dfx_slot_map_create(C.byref(self.form), C.byref(self.A.csr()),
                                                         _ptr(self.map), _stream()))
-        self.colour = _colour_args(a.V, self.mode)
-        bc_dofs = [bc.dofs for bc in self.bcs if bc.V is a.V]
-        self.diag_dofs = (torch.from_numpy(np.unique(np.concatenate(bc_dofs))).to(a.V.device)
+        self.colour = _colour_args(V, self.mode)
+        bc_dofs = [bc.dofs for bc in self.bcs if bc.V is V]
+        self.diag_dofs = (torch.from_numpy(np.unique(np.concatenate(bc_dofs))).to(V.device)
                           if bc_dofs else None)
 
     def assemble(self, zero: bool = True) -> MatrixCSR:
         if zero:
             self.A.vals.zero_()
         order, off, ncol = self.colour
-        _capi.check(_capi.lib().dfx_assemble_matrix(C.byref(self.form), C.byref(self.A.csr()),
-                                                    _ptr(self.map), _ptr(self.markers), self.mode,
-                                                    order, off, ncol, _stream()))
+        L = _capi.lib()
+        for t, cs in zip(self.terms, self.forms):
+            if t.facets is None:
+                _capi.check(L.dfx_assemble_matrix(C.byref(cs), C.byref(self.A.csr()),
+                                                  _ptr(self.map), _ptr(self.markers), self.mode,
+                                                  order, off, ncol, _stream()))
+            else:
+                _capi.check(L.dfx_assemble_matrix_facets(C.byref(cs), _ptr(t.facets),
+                                                         int(t.facets.shape[0]),
+                                                         C.byref(self.A.csr()), _ptr(self.map),
+                                                         _ptr(self.markers), _stream()))
         if self.diag_dofs is not None:
-            _capi.check(_capi.lib().dfx_set_diagonal(C.byref(self.A.csr()), _ptr(self.diag_dofs),
-                                                     int(self.diag_dofs.numel()), self.diagonal,
-                                                     _stream()))
+            _capi.check(L.dfx_set_diagonal(C.byref(self.A.csr()), _ptr(self.diag_dofs),
+                                           int(self.diag_dofs.numel()), self.diagonal,
+                                           _stream()))
         return self.A
 
 
@@ -324,17 +397,53 @@ def assemble_matrix(a: Form, bcs=(), diagonal: float = 1.0, mode: str = "atomic"
     return MatrixAssembler(a, bcs, diagonal, mode, use_slot_map=use_slot_map).assemble(zero=True)
 
 
-def assemble_vector(L: Form, b: torch.Tensor | None = None, mode: str = "atomic") -> torch.Tensor:
-    """b += assembled linear form (a new zero vector when b is None)."""
+def assemble_vector(L, b: torch.Tensor | None = None, mode: str = "atomic") -> torch.Tensor:
+    """b += assembled linear form (a new zero vector when b is None); cell
+    and exterior-facet terms. Facet terms scatter with FP64 atomics."""
     V = L.V
     if b is None:
         b = torch.zeros(V.num_dofs, dtype=torch.float64, device=V.device)
     m = _mode(mode)
-    order, off, ncol = _colour_args(V, m)
-    cf = L.cstruct()
-    _capi.check(_capi.lib().dfx_assemble_vector(C.byref(cf), _ptr(b), m, order, off, ncol,
-                                                _stream()))
+    for t in _terms(L):
+        cf = t.cstruct()
+        if t.facets is None:
+            order, off, ncol = _colour_args(V, m)
+            _capi.check(_capi.lib().dfx_assemble_vector(C.byref(cf), _ptr(b), m, order, off, ncol,
+                                                        _stream()))
+        else:
+            _capi.check(_capi.lib().dfx_assemble_vector_facets(C.byref(cf), _ptr(t.facets),
+                                                               int(t.facets.shape[0]), _ptr(b),
+                                                               _stream()))
     return b
+
+
+@dataclass
+class Functional:
+    """M = a(u, u) for a Poisson/Helmholtz form, or M = L(u) for a source
+    form: a rank-0 form for ``assemble_scalar``."""
+
+    form: Form
+    u: torch.Tensor
+
+
+def functional(form: Form, u: torch.Tensor) -> Functional:
+    return Functional(form, u)
+
+
+def assemble_scalar(M: Functional) -> float:
+    """fem::assemble_scalar over the cells (cpp/dolfinx/fem/assembler.h:173-215,
+    cpp/dolfinx/fem/assemble_scalar_impl.h:32-61), summed in a fixed order."""
+    f = M.form
+    assert f.facets is None, "functionals are cell integrals"
+    L = _capi.lib()
+    nc = f.V.mesh.num_cells
+    wb = int(L.dfx_assemble_scalar_workspace_bytes(nc))
+    work = torch.empty(max(wb, 8), dtype=torch.uint8, device=f.V.device)
+    v = C.c_double(0.0)
+    cs = f.cstruct()
+    _capi.check(L.dfx_assemble_scalar(C.byref(cs), _ptr(M.u), C.byref(v), _ptr(work), wb,
+                                      _stream()))
+    return v.value
 
 
 def apply_lifting(b: torch.Tensor, a, bcs, x0=None, alpha: float = 1.0,
@@ -352,10 +461,13 @@ def apply_lifting(b: torch.Tensor, a, bcs, x0=None, alpha: float = 1.0,
         for bc in bcj:
             bc.set(g)
         order, off, ncol = _colour_args(V, m)
-        cf = aj.cstruct()
-        _capi.check(_capi.lib().dfx_apply_lifting(C.byref(cf), _ptr(b), _ptr(markers), _ptr(g),
-                                                  _ptr(x0j), float(alpha), m, order, off, ncol,
-                                                  _stream()))
+        for t in _terms(aj):
+            if t.facets is not None:
+                raise NotImplementedError("lifting of exterior-facet terms is not supported")
+            cf = t.cstruct()
+            _capi.check(_capi.lib().dfx_apply_lifting(C.byref(cf), _ptr(b), _ptr(markers),
+                                                      _ptr(g), _ptr(x0j), float(alpha), m, order,
+                                                      off, ncol, _stream()))
 
 
 def set_bc(b: torch.Tensor, bcs, x0: torch.Tensor | None = None, alpha: float = 1.0) -> None:

@@ -7,6 +7,7 @@ DOLFINx does on one rank; the work runs in the host part of libdfxgpu.
 
 from __future__ import annotations
 
+import ctypes as C
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -33,6 +34,19 @@ class Mesh:
     @property
     def num_nodes(self) -> int:
         return int(self.x.shape[0])
+
+    def exterior_facets(self) -> np.ndarray:
+        """(num_facets, 2) int32 (cell, local facet) pairs of the boundary,
+        sorted (mesh::exterior_facet_indices + compute_integration_domains,
+        cpp/dolfinx/mesh/utils.cpp:61-89, cpp/dolfinx/fem/utils.h:155-162);
+        local facet f is the triangle opposite vertex f. Cached."""
+        if "facets" not in self._dev:
+            out = np.empty((4 * self.num_cells, 2), np.int32)
+            nf = C.c_int32(0)
+            _capi.check(_capi.lib().dfx_exterior_facets_tet(self.num_cells, self.cells.ctypes.data,
+                                                            out.ctypes.data, C.byref(nf)))
+            self._dev["facets"] = out[: nf.value].copy()
+        return self._dev["facets"]
 
     def device(self, device="cuda"):
         """(x_dofmap, x) as device tensors (cached)."""

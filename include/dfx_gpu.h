@@ -51,7 +51,10 @@ enum dfx_form_kind
      f = f_const[0]) */
   DFX_FORM_SOURCE = 2,
   /* L(v) = \int f . v dx, f = f_const (vector P2, bs 3) */
-  DFX_FORM_BODYFORCE = 3
+  DFX_FORM_BODYFORCE = 3,
+  /* a(u,v) = \int_F alpha u v ds over exterior facets (Robin term), alpha =
+     kappa of the facet's cell or kappa_const; scalar P1/P2 */
+  DFX_FORM_FACET_MASS = 4
 };
 
 enum dfx_assembly_mode
@@ -275,6 +278,42 @@ int dfx_cg_solve(const dfx_csr* A, const double* d_b, double* d_x,
 int dfx_cg_solve_noalloc(const dfx_csr* A, const double* d_b, double* d_x,
                          const double* d_dinv, double rtol, int32_t max_iters,
                          int32_t check_every, dfx_cg_info* info, void* stream);
+
+/* ------------------------------------------ exterior facets, functionals */
+
+/* Exterior facets of a tetrahedral mesh as (cell, local facet) pairs: the
+ * integration domain of an exterior-facet integral on one rank
+ * (mesh::exterior_facet_indices, mesh/utils.cpp:61-89, facets with one
+ * attached cell; fem::compute_integration_domains, fem/utils.h:155-162).
+ * Local facet f is the triangle opposite vertex f. facets: capacity
+ * 8*num_cells int32; pairs sorted by (cell, facet); *num_facets = count.
+ * Host function. */
+int dfx_exterior_facets_tet(int32_t num_cells, const int32_t* cells, int32_t* facets,
+                            int32_t* num_facets);
+
+/* Exterior-facet vector loop (fem/assemble_vector_impl.h:160-215,
+ * 571-600): b += \int_F g v ds over the facets, L a DFX_FORM_SOURCE form
+ * (g = its P1 coefficient f, or f_const[0]), scalar P1/P2. FP64 atomics. */
+int dfx_assemble_vector_facets(const dfx_form* L, const int32_t* d_facets,
+                               int32_t num_facets, double* d_b, void* stream);
+
+/* Exterior-facet matrix loop (fem/assemble_matrix_impl.h:265-379):
+ * A += \int_F alpha u v ds, a a DFX_FORM_FACET_MASS form, scalar P1/P2;
+ * constrained rows and columns (d_bc) are skipped as in the cell loop.
+ * d_map: the cell -> slot map of the cell integral (or NULL: row search). */
+int dfx_assemble_matrix_facets(const dfx_form* a, const int32_t* d_facets,
+                               int32_t num_facets, const dfx_csr* A,
+                               const uint8_t* d_map, const int8_t* d_bc, void* stream);
+
+/* fem::assemble_scalar over cells (fem/assembler.h:173-215;
+ * fem/assemble_scalar_impl.h:32-61) for the functionals M = a(u, u) of a
+ * DFX_FORM_POISSON form (kappa |grad u|^2 + k2 u^2) and M = L(u) of a
+ * DFX_FORM_SOURCE form (f u). u: FE function on the form's dofmap. The
+ * sum is deterministic (fixed block and warp order). *value on the host;
+ * synchronises `stream`. */
+size_t dfx_assemble_scalar_workspace_bytes(int32_t num_cells);
+int dfx_assemble_scalar(const dfx_form* M, const double* d_u, double* value,
+                        void* d_work, size_t work_bytes, void* stream);
 
 /* -------------------------------------------------------------- autotuner
  * No reference counterpart: the launch shapes of the assembly and CSR SpMV

@@ -18,6 +18,7 @@
 // golden vectors under tests/golden/.
 
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -1067,3 +1068,224 @@ extern "C" int orc_q4_action(int nx, int ny, int nz, const double* verts, double
         }
   return 0;
 }
+
+//---------------------------------------------------------------------------
+// Exterior facet integrals and functionals
+//---------------------------------------------------------------------------
+namespace
+{
+// Quadrature on facet f of the reference tetrahedron: points in tet
+// reference coordinates and weights summing to 1/2 (the reference
+// triangle's area), from a collapsed Gauss rule with 4 points per
+// direction (exact to degree 6 on the triangle).
+struct FacetQuad
+{
+  std::vector<double> X; // 3 per point
+  std::vector<double> w;
+};
+
+const FacetQuad& facet_quadrature(int f)
+{
+  static const std::vector<FacetQuad> rules = []
+  {
+    std::vector<double> x, w;
+    gauss_legendre01(4, x, w);
+    const double V[4][3] = {{0, 0, 0}, {1, 0, 0}, {0, 1, 0}, {0, 0, 1}};
+    std::vector<FacetQuad> out(4);
+    for (int fi = 0; fi < 4; ++fi)
+    {
+      const double* a = V[kTetFacets[fi][0]];
+      const double* b = V[kTetFacets[fi][1]];
+      const double* c = V[kTetFacets[fi][2]];
+      for (int i = 0; i < 4; ++i)
+        for (int j = 0; j < 4; ++j)
+        {
+          const double s = x[i], t = x[j] * (1.0 - x[i]);
+          for (int k = 0; k < 3; ++k)
+            out[fi].X.push_back(a[k] + s * (b[k] - a[k]) + t * (c[k] - a[k]));
+          out[fi].w.push_back(w[i] * w[j] * (1.0 - x[i]));
+        }
+    }
+    return out;
+  }();
+  return rules[f];
+}
+
+// Physical area of facet f of a cell with vertex coordinates c (3 per
+// vertex).
+double facet_area(const double* c, int f)
+{
+  const double* a = c + 3 * kTetFacets[f][0];
+  const double* b = c + 3 * kTetFacets[f][1];
+  const double* d = c + 3 * kTetFacets[f][2];
+  const double u[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
+  const double v[3] = {d[0] - a[0], d[1] - a[1], d[2] - a[2]};
+  const double n[3] = {u[1] * v[2] - u[2] * v[1], u[2] * v[0] - u[0] * v[2],
+                       u[0] * v[1] - u[1] * v[0]};
+  return 0.5 * std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+}
+
+void cell_coords(const int32_t* x_dofmap, const double* x, int c, double* coords)
+{
+  for (int v = 0; v < 4; ++v)
+    for (int k = 0; k < 3; ++k)
+      coords[3 * v + k] = x[3 * (int64_t)x_dofmap[4 * c + v] + k];
+}
+} // namespace
+
+extern "C"
+{
+// Exterior facets of a tetrahedral mesh as (cell, local facet) pairs, the
+// integration domain of an exterior-facet integral on one rank:
+// mesh::exterior_facet_indices (cpp/dolfinx/mesh/utils.cpp:61-89: facets
+// with one attached cell) and compute_integration_domains
+// (cpp/dolfinx/fem/utils.h:155-162: each facet as (cell, local index)).
+// Pairs are written sorted by (cell, local facet). Returns the count.
+int orc_exterior_facets_tet(int nc, const int32_t* cells, int32_t* pairs)
+{
+  std::vector<std::array<int32_t, 5>> keys; // sorted vertices, cell, local
+  keys.reserve(4 * (size_t)nc);
+  for (int c = 0; c < nc; ++c)
+    for (int f = 0; f < 4; ++f)
+    {
+      std::array<int32_t, 3> v = {cells[4 * c + kTetFacets[f][0]],
+                                  cells[4 * c + kTetFacets[f][1]],
+                                  cells[4 * c + kTetFacets[f][2]]};
+      std::sort(v.begin(), v.end());
+      keys.push_back({v[0], v[1], v[2], c, f});
+    }
+  std::sort(keys.begin(), keys.end());
+  std::vector<std::pair<int32_t, int32_t>> out;
+  for (size_t i = 0; i < keys.size();)
+  {
+    size_t j = i + 1;
+    while (j < keys.size() && keys[j][0] == keys[i][0] && keys[j][1] == keys[i][1]
+           && keys[j][2] == keys[i][2])
+      ++j;
+    if (j - i == 1)
+      out.push_back({keys[i][3], keys[i][4]});
+    i = j;
+  }
+  std::sort(out.begin(), out.end());
+  for (size_t i = 0; i < out.size(); ++i)
+  {
+    pairs[2 * i] = out[i].first;
+    pairs[2 * i + 1] = out[i].second;
+  }
+  return (int)out.size();
+}
+
+// Exterior-facet vector loop (cpp/dolfinx/fem/assemble_vector_impl.h:
+// 160-215, 571-600): L(v) = \int_F g v ds with g a P1 coefficient (values
+// per geometry node; g == nullptr -> g_const), scalar P1/P2.
+void orc_assemble_vector_facets(int degree, int nf, const int32_t* pairs,
+                                const int32_t* x_dofmap, const double* x,
+                                const int32_t* dofmap, const double* g, double g_const,
+                                double* b)
+{
+  const int nd = tet_ndofs(degree);
+  double coords[12], phi[10], dphi[10][3], l[4], dl[4][3];
+  for (int e = 0; e < nf; ++e)
+  {
+    const int c = pairs[2 * e], f = pairs[2 * e + 1];
+    cell_coords(x_dofmap, x, c, coords);
+    const double two_area = 2.0 * facet_area(coords, f);
+    const FacetQuad& q = facet_quadrature(f);
+    double gc[4];
+    for (int v = 0; v < 4; ++v)
+      gc[v] = g ? g[x_dofmap[4 * c + v]] : g_const;
+    for (size_t p = 0; p < q.w.size(); ++p)
+    {
+      tabulate_tet(degree, &q.X[3 * p], phi, dphi);
+      tabulate_tet(1, &q.X[3 * p], l, dl);
+      const double gq = gc[0] * l[0] + gc[1] * l[1] + gc[2] * l[2] + gc[3] * l[3];
+      for (int i = 0; i < nd; ++i)
+        b[dofmap[(int64_t)nd * c + i]] += q.w[p] * two_area * gq * phi[i];
+    }
+  }
+}
+
+// Exterior-facet matrix loop (cpp/dolfinx/fem/assemble_matrix_impl.h:
+// 265-379): a(u, v) = \int_F alpha u v ds, alpha per cell of the facet
+// (alpha == nullptr -> alpha_const); rows and columns of constrained dofs
+// zeroed as in the cell loop; insertion by binary search.
+int orc_assemble_matrix_facets(int degree, int nf, const int32_t* pairs,
+                               const int32_t* x_dofmap, const double* x,
+                               const int32_t* dofmap, const double* alpha,
+                               double alpha_const, const int8_t* bc,
+                               const int64_t* row_ptr, const int32_t* cols, double* vals)
+{
+  const int nd = tet_ndofs(degree);
+  double coords[12], phi[10], dphi[10][3], Ae[100];
+  for (int e = 0; e < nf; ++e)
+  {
+    const int c = pairs[2 * e], f = pairs[2 * e + 1];
+    cell_coords(x_dofmap, x, c, coords);
+    const double two_area = 2.0 * facet_area(coords, f);
+    const double al = alpha ? alpha[c] : alpha_const;
+    const FacetQuad& q = facet_quadrature(f);
+    std::fill_n(Ae, 100, 0.0);
+    for (size_t p = 0; p < q.w.size(); ++p)
+    {
+      tabulate_tet(degree, &q.X[3 * p], phi, dphi);
+      for (int i = 0; i < nd; ++i)
+        for (int j = 0; j < nd; ++j)
+          Ae[i * nd + j] += q.w[p] * two_area * al * phi[i] * phi[j];
+    }
+    const int32_t* dofs = dofmap + (int64_t)nd * c;
+    for (int i = 0; i < nd; ++i)
+    {
+      if (bc && bc[dofs[i]])
+        continue;
+      const int32_t* c0 = cols + row_ptr[dofs[i]];
+      const int32_t* c1 = cols + row_ptr[dofs[i] + 1];
+      for (int j = 0; j < nd; ++j)
+      {
+        if (bc && bc[dofs[j]])
+          continue;
+        const int32_t* it = std::lower_bound(c0, c1, dofs[j]);
+        if (it == c1 || *it != dofs[j])
+          return ORC_ERR_NOT_IN_SPARSITY;
+        vals[it - cols] += Ae[i * nd + j];
+      }
+    }
+  }
+  return ORC_OK;
+}
+
+// Functional cell loop (cpp/dolfinx/fem/assemble_scalar_impl.h:32-61),
+// kind 0: M = a(u, u) = \int kappa |grad u|^2 + k2 u^2 dx; kind 1:
+// M = L(u) = \int f u dx with f a P1 coefficient (f == nullptr -> 1).
+double orc_assemble_scalar(int kind, int degree, int nc, const int32_t* x_dofmap,
+                           const double* x, const int32_t* dofmap, const double* kappa,
+                           double k2, const double* f, const double* u)
+{
+  const int nd = tet_ndofs(degree);
+  double coords[12], Ae[100], be[10], fc[4], ue[10];
+  double value = 0.0;
+  for (int c = 0; c < nc; ++c)
+  {
+    cell_coords(x_dofmap, x, c, coords);
+    for (int i = 0; i < nd; ++i)
+      ue[i] = u[dofmap[(int64_t)nd * c + i]];
+    if (kind == 0)
+    {
+      std::fill_n(Ae, 100, 0.0);
+      kernel_poisson(degree, Ae, kappa ? kappa[c] : 1.0, k2, coords);
+      for (int i = 0; i < nd; ++i)
+        for (int j = 0; j < nd; ++j)
+          value += ue[i] * Ae[i * nd + j] * ue[j];
+    }
+    else
+    {
+      for (int v = 0; v < 4; ++v)
+        fc[v] = f ? f[x_dofmap[4 * c + v]] : 1.0;
+      std::fill_n(be, 10, 0.0);
+      kernel_source(degree, be, fc, coords);
+      for (int i = 0; i < nd; ++i)
+        value += be[i] * ue[i];
+    }
+  }
+  return value;
+}
+} // extern "C"

@@ -81,6 +81,15 @@ def lib():
         L.orc_q4_tables.argtypes = [_f64p, _f64p, _f64p]
         L.orc_cg.argtypes = [C.c_int, C.c_int, _i64p, _i32p, _f64p, _f64p, _f64p, C.c_void_p,
                              C.c_double, C.c_int]
+        L.orc_exterior_facets_tet.argtypes = [C.c_int, _i32p, _i32p]
+        L.orc_assemble_vector_facets.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, _i32p,
+                                                 C.c_void_p, C.c_double, _f64p]
+        L.orc_assemble_matrix_facets.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, _i32p,
+                                                 C.c_void_p, C.c_double, C.c_void_p, _i64p,
+                                                 _i32p, _f64p]
+        L.orc_assemble_scalar.argtypes = [C.c_int, C.c_int, C.c_int, _i32p, _f64p, _i32p,
+                                          C.c_void_p, C.c_double, C.c_void_p, _f64p]
+        L.orc_assemble_scalar.restype = C.c_double
         _lib = L
     return _lib
 
@@ -257,3 +266,48 @@ def q4_action(n, verts, u, kappa=1.0, apply_bc=True):
     lib().orc_q4_action(nx, ny, nz, np.ascontiguousarray(verts, np.float64), float(kappa), u, y,
                         int(apply_bc))
     return y
+
+
+# ---------------------------------------------------------------- facets, functionals
+def exterior_facets(cells):
+    """(num_facets, 2) int32 array of (cell, local facet), sorted."""
+    cells = np.ascontiguousarray(cells, np.int32)
+    out = np.empty((4 * cells.shape[0], 2), np.int32)
+    nf = lib().orc_exterior_facets_tet(cells.shape[0], cells, out)
+    return out[:nf].copy()
+
+
+def assemble_vector_facets(degree, facets, cells, x, dofmap, n, g=None, g_const=1.0, b=None):
+    """b += \int_F g v ds over the given exterior facets (scalar P1/P2)."""
+    if b is None:
+        b = np.zeros(n, np.float64)
+    ga = None if g is None else np.ascontiguousarray(g, np.float64)
+    fa = np.ascontiguousarray(facets, np.int32)
+    lib().orc_assemble_vector_facets(degree, fa.shape[0], fa, np.ascontiguousarray(cells), x,
+                                     np.ascontiguousarray(dofmap), _ptr(ga), float(g_const), b)
+    return b
+
+
+def assemble_matrix_facets(degree, facets, cells, x, dofmap, row_ptr, cols, alpha=None,
+                           alpha_const=1.0, bc_markers=None, vals=None):
+    """vals += \int_F alpha u v ds over the given exterior facets."""
+    if vals is None:
+        vals = np.zeros(cols.size, np.float64)
+    al = None if alpha is None else np.ascontiguousarray(alpha, np.float64)
+    bcm = None if bc_markers is None else np.ascontiguousarray(bc_markers, np.int8)
+    fa = np.ascontiguousarray(facets, np.int32)
+    rc = lib().orc_assemble_matrix_facets(degree, fa.shape[0], fa, np.ascontiguousarray(cells), x,
+                                          np.ascontiguousarray(dofmap), _ptr(al),
+                                          float(alpha_const), _ptr(bcm), row_ptr, cols, vals)
+    if rc == 3:
+        raise RuntimeError("Entry not in sparsity")
+    return vals
+
+
+def assemble_scalar(kind, degree, cells, x, dofmap, u, kappa=None, k2=0.0, f=None):
+    """kind 0: a(u, u) = \int kappa |grad u|^2 + k2 u^2 dx; kind 1: \int f u dx."""
+    kap = None if kappa is None else np.ascontiguousarray(kappa, np.float64)
+    fa = None if f is None else np.ascontiguousarray(f, np.float64)
+    return lib().orc_assemble_scalar(kind, degree, cells.shape[0], np.ascontiguousarray(cells), x,
+                                     np.ascontiguousarray(dofmap), _ptr(kap), float(k2), _ptr(fa),
+                                     np.ascontiguousarray(u, np.float64))

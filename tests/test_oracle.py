@@ -167,3 +167,76 @@ def test_q4_action_exact_on_linears(oracle):
     a[bnd] = 0.0
     b[bnd] = 0.0
     assert abs(a @ oracle.q4_action(dims, v, b) - b @ oracle.q4_action(dims, v, a)) < 1e-11
+
+
+def _dof_coords(x, cells, dm, n, deg):
+    X = np.empty((n, 3))
+    e = np.array([[2, 3], [1, 3], [1, 2], [0, 3], [0, 2], [0, 1]])
+    xc = x[cells]
+    X[dm[:, :4].ravel()] = xc.reshape(-1, 3)
+    if deg == 2:
+        X[dm[:, 4:].ravel()] = (0.5 * (xc[:, e[:, 0]] + xc[:, e[:, 1]])).reshape(-1, 3)
+    return X
+
+
+@pytest.mark.parametrize("n", [(1, 1, 1), (3, 2, 4)])
+def test_exterior_facets_count_and_orientation(oracle, n):
+    # every boundary square of the box is split into two triangles
+    cells, x = oracle.create_box_tet(*n)
+    fac = oracle.exterior_facets(cells)
+    nx, ny, nz = n
+    assert fac.shape[0] == 4 * (nx * ny + ny * nz + nx * nz)
+    # each exterior facet lies on a face of the unit cube
+    loc = np.array([[1, 2, 3], [0, 2, 3], [0, 1, 3], [0, 1, 2]])
+    v = x[cells[fac[:, 0][:, None], loc[fac[:, 1]]]]  # (nf, 3, 3)
+    on = (np.isclose(v, 0) | np.isclose(v, 1)).all(1).any(1)
+    assert on.all()
+
+
+@pytest.mark.parametrize("deg", [1, 2])
+def test_facet_vector_totals(oracle, deg):
+    # sum_i b_i = \int_Gamma g ds: g = 1 gives the surface area of the box,
+    # g = x gives 3 on the unit cube (faces x=1: 1, y,z faces: 1/2 each)
+    cells, x = oracle.create_box_tet(3, 2, 4, p1=(1.5, 1.0, 2.0))
+    dm, n = oracle.dofmap_tet(cells, deg)
+    fac = oracle.exterior_facets(cells)
+    b = oracle.assemble_vector_facets(deg, fac, cells, x, dm, n)
+    assert abs(b.sum() - 2 * (1.5 * 1 + 1 * 2 + 1.5 * 2)) < 1e-12
+    if deg == 2:  # P2 vertex functions integrate to zero on a triangle
+        assert np.abs(b[dm[:, :4].ravel()]).max() < 1e-14
+    cells, x = oracle.create_box_tet(3, 3, 2)
+    dm, n = oracle.dofmap_tet(cells, deg)
+    fac = oracle.exterior_facets(cells)
+    b = oracle.assemble_vector_facets(deg, fac, cells, x, dm, n, g=x[:, 0].copy())
+    assert abs(b.sum() - 3.0) < 1e-12
+
+
+@pytest.mark.parametrize("deg", [1, 2])
+def test_facet_mass_totals(oracle, deg):
+    # 1^T M 1 = alpha |Gamma|; the facet mass is symmetric
+    cells, x = oracle.create_box_tet(2, 3, 2)
+    dm, n = oracle.dofmap_tet(cells, deg)
+    rp, cols = oracle.sparsity(n, dm)
+    fac = oracle.exterior_facets(cells)
+    M = oracle.assemble_matrix_facets(deg, fac, cells, x, dm, rp, cols, alpha_const=2.5)
+    assert abs(M.sum() - 2.5 * 6.0) < 1e-12
+    import scipy.sparse as sp
+    S = sp.csr_matrix((M, cols, rp), shape=(n, n))
+    assert abs(S - S.T).max() < 1e-15
+
+
+@pytest.mark.parametrize("deg", [1, 2])
+def test_functionals_on_polynomials(oracle, deg):
+    # a(1, 1) = k2 |Omega|; a(x, x) = \int kappa for linear x; L(1) = \int f
+    cells, x = oracle.create_box_tet(3, 2, 2)
+    dm, n = oracle.dofmap_tet(cells, deg)
+    X = _dof_coords(x, cells, dm, n, deg)
+    kappa = np.exp(np.random.default_rng(1).normal(0, 1, cells.shape[0]))
+    one = np.ones(n)
+    assert abs(oracle.assemble_scalar(0, deg, cells, x, dm, one, k2=3.0) - 3.0) < 1e-13
+    vol = np.abs(np.linalg.det(x[cells[:, 1:]] - x[cells[:, :1]])) / 6
+    ref = (kappa * vol).sum()
+    got = oracle.assemble_scalar(0, deg, cells, x, dm, X[:, 0].copy(), kappa=kappa)
+    assert abs(got - ref) < 1e-13 * ref
+    f = 1.0 + x[:, 1]  # \int (1 + y) dx = 1.5
+    assert abs(oracle.assemble_scalar(1, deg, cells, x, dm, one, f=f) - 1.5) < 1e-13

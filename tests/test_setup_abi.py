@@ -64,3 +64,11 @@ def test_invalid_box_is_rejected(capi):
         mesh.create_box(((0, 0, 0), (1, 1, 1)), (0, 1, 1))
     with pytest.raises(capi.DfxError, match="p\\[0\\] < p\\[1\\]"):
         mesh.create_box(((0, 0, 0), (1, 0, 1)), (1, 1, 1))
+
+
+@pytest.mark.parametrize("n", [(1, 1, 1), (3, 2, 4), (6, 5, 7)])
+def test_exterior_facets_match_oracle(capi, oracle, n):
+    from dolfinx_gb300 import mesh
+
+    m = mesh.create_unit_cube(*n)
+    np.testing.assert_array_equal(m.exterior_facets(), oracle.exterior_facets(m.cells))
