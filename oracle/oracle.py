@@ -278,7 +278,7 @@ def exterior_facets(cells):
 
 
 def assemble_vector_facets(degree, facets, cells, x, dofmap, n, g=None, g_const=1.0, b=None):
-    """b += \int_F g v ds over the given exterior facets (scalar P1/P2)."""
+    r"""b += \int_F g v ds over the given exterior facets (scalar P1/P2)."""
     if b is None:
         b = np.zeros(n, np.float64)
     ga = None if g is None else np.ascontiguousarray(g, np.float64)
@@ -290,7 +290,7 @@ def assemble_vector_facets(degree, facets, cells, x, dofmap, n, g=None, g_const=
 
 def assemble_matrix_facets(degree, facets, cells, x, dofmap, row_ptr, cols, alpha=None,
                            alpha_const=1.0, bc_markers=None, vals=None):
-    """vals += \int_F alpha u v ds over the given exterior facets."""
+    r"""vals += \int_F alpha u v ds over the given exterior facets."""
     if vals is None:
         vals = np.zeros(cols.size, np.float64)
     al = None if alpha is None else np.ascontiguousarray(alpha, np.float64)
@@ -305,7 +305,7 @@ def assemble_matrix_facets(degree, facets, cells, x, dofmap, row_ptr, cols, alph
 
 
 def assemble_scalar(kind, degree, cells, x, dofmap, u, kappa=None, k2=0.0, f=None):
-    """kind 0: a(u, u) = \int kappa |grad u|^2 + k2 u^2 dx; kind 1: \int f u dx."""
+    r"""kind 0: a(u, u) = \int kappa |grad u|^2 + k2 u^2 dx; kind 1: \int f u dx."""
     kap = None if kappa is None else np.ascontiguousarray(kappa, np.float64)
     fa = None if f is None else np.ascontiguousarray(f, np.float64)
     return lib().orc_assemble_scalar(kind, degree, cells.shape[0], np.ascontiguousarray(cells), x,
