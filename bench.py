@@ -622,6 +622,47 @@ def _kernel_ms(fn, reps, stream):
     return e0.elapsed_time(e1) / reps
 
 
+class Replicas:
+    """N independent replicas, one per GPU: each rank solves its own seeded
+    problem, with no collective on the data path. Timings are the max over
+    ranks and throughput counts every rank's dofs (weak scaling). The
+    collectives here are host bookkeeping on any backend (NCCL on the GPUs,
+    gloo in the CPU tests)."""
+
+    def __init__(self, world: int, device):
+        self.world, self.device = world, device
+
+    def barrier(self):
+        if self.world > 1:
+            import torch.distributed as dist
+
+            dist.barrier()
+
+    def _reduce(self, v: float, op) -> float:
+        import torch
+
+        t = torch.tensor([float(v)], dtype=torch.float64, device=self.device)
+        if self.world > 1:
+            import torch.distributed as dist
+
+            dist.all_reduce(t, op=op)
+        return float(t.item())
+
+    def max(self, v: float) -> float:
+        import torch.distributed as dist
+
+        return self._reduce(v, dist.ReduceOp.MAX)
+
+    def total(self, v: float) -> float:
+        import torch.distributed as dist
+
+        return self._reduce(v, dist.ReduceOp.SUM)
+
+    @staticmethod
+    def gdofs_per_s(total_dofs: float, ms_max: float) -> float:
+        return total_dofs / (ms_max * 1e-3) / 1e9
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -633,16 +674,8 @@ def run_ours(args):
     torch.cuda.set_device(local)
     if world > 1:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-
-    def barrier():
-        if world > 1:
-            dist.barrier()
-
-    def max_over_ranks(v):
-        t = torch.tensor([v], device="cuda")
-        if world > 1:
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    R = Replicas(world, "cuda")
+    barrier, max_over_ranks = R.barrier, R.max
 
     m, kappa, f = make_inputs(args.n, seed=rank)
     P = Problem(m, kappa, f, mode=args.mode, inner_rtol=args.inner_rtol, variant=args.ir_variant)
@@ -668,7 +701,8 @@ def run_ours(args):
         barrier()
     clocks = clk.summary()
     ms_max = max_over_ranks(ms)
-    value = world * n_dofs / (ms_max * 1e-3) / 1e9
+    all_dofs = R.total(n_dofs)
+    value = R.gdofs_per_s(all_dofs, ms_max)
     x_ir = P.x.clone()
     rel_err = float((x_ir - x64).norm() / x64.norm())
     launches = int(np.mean([7 + r.kernel_launches for r in res]))
@@ -688,7 +722,7 @@ def run_ours(args):
     barrier()
     ms_e2e, _ = _timed(e2e_step, args.steps, stream)
     barrier()
-    e2e_value = world * n_dofs / (max_over_ranks(ms_e2e) * 1e-3) / 1e9
+    e2e_value = R.gdofs_per_s(all_dofs, max_over_ranks(ms_e2e))
 
     # ---- roofline: the inner operator (FP32 sliced-ELL, 16-bit columns)
     # and the FP64 operator, each timed alone on its own numbering
@@ -797,7 +831,7 @@ def run_ours(args):
                            "fp64_rtol_1e-13_status": res_tight.status,
                            "final_rel_residual_fp64": float(np.sqrt(res[-1].rnorm_sq
                                                                     / res[-1].rnorm0_sq))},
-                "fp64_plain": {"value": world * n_dofs / (ms64 * 1e-3) / 1e9, "unit": UNIT,
+                "fp64_plain": {"value": R.gdofs_per_s(all_dofs, ms64), "unit": UNIT,
                                "ms_per_step": ms64,
                                "cg_iterations": [r.iterations for r in res64],
                                "speedup_of_mixed": ms64 / ms_max},
