@@ -107,6 +107,55 @@ __device__ __forceinline__ int64_t row_search(const int32_t* __restrict__ cols, 
   return (e < 0) ? -1 : e;
 }
 
+// Bulk asynchronous copy global -> shared memory (the 1D form of TMA),
+// completing on a CTA-local mbarrier. Both addresses 16-byte aligned, size
+// a multiple of 16.
+__device__ __forceinline__ uint32_t smem_addr(const void* p)
+{
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count)
+{
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count)
+               : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes)
+{
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes,
+                                         uint64_t* bar)
+{
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], "
+               "%2, [%3];" ::"r"(smem_addr(dst)),
+               "l"(src), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
+}
+
+// Wait for phase `parity` of the mbarrier, at most max_tries polls.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity, int max_tries)
+{
+  for (int i = 0; i < max_tries; ++i)
+  {
+    uint32_t done;
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(done)
+                 : "r"(smem_addr(bar)), "r"(parity)
+                 : "memory");
+    if (done)
+      return true;
+  }
+  return false;
+}
+
 template <bool COLOURED>
 __device__ __forceinline__ void scatter_add(double* p, double v)
 {
@@ -281,26 +330,51 @@ __global__ void __launch_bounds__(kThreads)
   __shared__ double sA[CPB * NU];
   __shared__ double sScratch[ELAST ? CPB * 132 : 1];
   __shared__ int32_t sCell[CPB];
-  __shared__ int32_t sDof[CPB * ND];
+  __shared__ __align__(16) int32_t sDof[CPB * ND];
   __shared__ int64_t sRow[CPB * ND];
   __shared__ int8_t sBc[CPB * N];
   __shared__ int8_t sActive[CPB];
+  __shared__ uint64_t sBar;
 
   const int64_t base = (int64_t)blockIdx.x * CPB;
   const int nloc = (int)(((int64_t)count - base) < CPB ? ((int64_t)count - base) : CPB);
   if (nloc <= 0)
     return;
+  // Stage 0. A full block of consecutive cells reads its dofmap rows as one
+  // contiguous span: one bulk copy into shared memory (CPB*ND*4 bytes, a
+  // multiple of 16 for every CPB candidate), when the dofmap is 16-byte
+  // aligned. Other blocks load the rows entry by entry.
+  constexpr uint32_t kRowBytes = (uint32_t)(CPB * ND * sizeof(int32_t));
+  static_assert(kRowBytes % 16 == 0, "bulk copies move multiples of 16 bytes");
+  const bool bulk = !list && nloc == CPB && (((uintptr_t)a.dofmap & 15) == 0);
+  if (bulk && threadIdx.x == 0)
+  {
+    mbar_init(&sBar, 1);
+    mbar_expect_tx(&sBar, kRowBytes);
+    bulk_g2s(sDof, a.dofmap + base * ND, kRowBytes, &sBar);
+  }
   if (threadIdx.x < nloc)
   {
     sCell[threadIdx.x] = list ? __ldg(list + base + threadIdx.x) : (int32_t)(base + threadIdx.x);
     sActive[threadIdx.x] = 1;
   }
   __syncthreads();
+  bool staged = bulk;
+  if (bulk && !mbar_wait(&sBar, 0, 1 << 20))
+  {
+    // The copy did not land in time: report it, let it finish (bounded),
+    // and load the rows directly; the copy writes the same values.
+    if (threadIdx.x == 0)
+      atomicExch(status, (int)DFX_ERR_TIMEOUT);
+    mbar_wait(&sBar, 0, 1 << 24);
+    staged = false;
+  }
   for (int t = threadIdx.x; t < nloc * ND; t += blockDim.x)
   {
     const int cl = t / ND, i = t % ND;
-    const int32_t d = __ldg(a.dofmap + (int64_t)sCell[cl] * ND + i);
-    sDof[t] = d;
+    const int32_t d = staged ? sDof[t] : __ldg(a.dofmap + (int64_t)sCell[cl] * ND + i);
+    if (!staged)
+      sDof[t] = d;
     sRow[t] = __ldg(row_ptr + d);
 #pragma unroll
     for (int k = 0; k < BS; ++k)
