@@ -565,6 +565,8 @@ extern "C" int dfx_operator_update_values(dfx_operator op, const dfx_csr* A, voi
   DFX_REQUIRE(op && A && A->vals, "operator and matrix must be non-NULL");
   DFX_REQUIRE(A->dtype == DFX_F64, "values are refilled from FP64 CSR values");
   DFX_REQUIRE(A->nnz == op->csr_nnz && A->nrows == op->n, "matrix does not match the operator");
+  if (op->nslots == 0)
+    return DFX_OK;
   cudaStream_t s = dfx::as_stream(stream);
   const unsigned grid = (unsigned)std::min<int64_t>((op->nslots + 255) / 256, 16 * dfx::num_sms());
   if (op->dtype == DFX_F64)

@@ -90,3 +90,16 @@ def test_assemble_scalar(cuda, oracle, capi, deg, k2):
     A = fem.assemble_matrix(fem.poisson_form(V, kappa, k2=k2))
     uAu = float(ud @ A.matvec(ud))
     assert abs(energy - uAu) <= 1e-12 * abs(uAu)
+
+
+def test_empty_facet_domain_and_functional_of_zero(cuda, oracle, capi):
+    from dolfinx_gb300 import fem
+
+    m, V, kappa, f, rp, cols = problem(oracle, (2, 2, 2), 2, seed=36)
+    none = np.zeros((0, 2), np.int32)
+    b = fem.assemble_vector(fem.facet_source_form(V, 1.0, facets=none))
+    assert torch.count_nonzero(b) == 0
+    A = fem.assemble_matrix(fem.facet_mass_form(V, 1.0, facets=none))
+    assert torch.count_nonzero(A.vals) == 0
+    zero = torch.zeros(V.num_dofs, dtype=torch.float64, device="cuda")
+    assert fem.assemble_scalar(fem.functional(fem.poisson_form(V, kappa), zero)) == 0.0

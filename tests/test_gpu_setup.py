@@ -145,3 +145,23 @@ def test_device_operator_long_row_falls_back_to_host(cuda, capi):
     assert auto.info() == host.info()
     x = torch.rand(nrows, dtype=torch.float64, device="cuda")
     assert torch.equal(auto.apply(x), host.apply(x))
+
+
+@pytest.mark.parametrize("nrows", [0, 5])
+def test_device_sparsity_without_cells(cuda, capi, nrows):
+    rp, cols = _device_sparsity(capi, nrows, np.zeros((0, 4), np.int32))
+    np.testing.assert_array_equal(rp, np.zeros(nrows + 1, np.int64))
+    assert cols.size == 0
+
+
+@pytest.mark.parametrize("build", [1, 2])
+def test_empty_operator(cuda, capi, build):
+    from dolfinx_gb300 import la
+
+    A = la.MatrixCSR(torch.zeros(1, dtype=torch.int64, device="cuda"),
+                     torch.zeros(0, dtype=torch.int32, device="cuda"),
+                     torch.zeros(0, dtype=torch.float64, device="cuda"), 1)
+    op = la.SellOperator(A, torch.float64, build=build)
+    assert op.info()["slots"] == 0
+    x = torch.zeros(0, dtype=torch.float64, device="cuda")
+    assert op.apply(x).numel() == 0

@@ -72,3 +72,14 @@ def test_exterior_facets_match_oracle(capi, oracle, n):
 
     m = mesh.create_unit_cube(*n)
     np.testing.assert_array_equal(m.exterior_facets(), oracle.exterior_facets(m.cells))
+
+
+def test_exterior_facets_of_no_cells(capi):
+    import ctypes as C
+
+    nf = C.c_int32(-1)
+    out = np.zeros(2, np.int32)
+    cells = np.zeros(4, np.int32)
+    capi.check(capi.lib().dfx_exterior_facets_tet(0, cells.ctypes.data, out.ctypes.data,
+                                                  C.byref(nf)))
+    assert nf.value == 0
