@@ -54,6 +54,8 @@ def parse():
     p.add_argument("--c4-only", action="store_true",
                    help="run only the matrix-free Q4 sample and print its JSON")
     p.add_argument("--c4-n", type=int, default=64, help="Q4 hexahedra per direction")
+    p.add_argument("--profile-q4", action="store_true",
+                   help="apply the Q4 operator only (for an ncu capture of k_q4_cells)")
     p.add_argument("--profile-step", action="store_true",
                    help="run one mixed-precision c2 step only (for an ncu launch list)")
     p.add_argument("--profile", action="store_true",
@@ -910,8 +912,32 @@ def run_profile_step(args):
                       "outer_iterations": r.outer_iterations}))
 
 
+def run_profile_q4(args):
+    """The Q4 operator on --c4-n^3 hexahedra, its FP32 and FP64 actions
+    applied twice each: the run behind an ncu capture of k_q4_cells."""
+    import numpy as np
+    import torch
+
+    from dolfinx_gb300 import matrix_free as mf
+
+    torch.cuda.set_device(0)
+    n = args.c4_n
+    op = mf.Q4Laplacian(mf.hex_box_vertices(n, perturb=0.05, seed=4), n)
+    u64 = torch.from_numpy(np.random.default_rng(4).standard_normal(op.n)).cuda()
+    u32 = u64.float()
+    y64, y32 = torch.empty_like(u64), torch.empty_like(u32)
+    for _ in range(2):
+        op.apply(u32, y32)
+        op.apply(u64, y64)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_q4": "ok", "cells": n ** 3, "dofs": op.n}))
+
+
 def main():
     args = parse()
+    if args.profile_q4:
+        run_profile_q4(args)
+        return
     if args.profile_step:
         run_profile_step(args)
         return
