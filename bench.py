@@ -49,15 +49,15 @@ def parse():
     p.add_argument("--serving-requests", type=int, default=64,
                    help="requests of the bounded serving sample (0: skip)")
     p.add_argument("--serving-nmax", type=int, default=96)
-    p.add_argument("--no-c3", action="store_true", help="skip the elasticity (c3) sample")
-    p.add_argument("--no-c4", action="store_true", help="skip the matrix-free Q4 (c4) sample")
-    p.add_argument("--c4-only", action="store_true",
+    p.add_argument("--no-elasticity", action="store_true", help="skip the elasticity sample")
+    p.add_argument("--no-q4", action="store_true", help="skip the matrix-free Q4 sample")
+    p.add_argument("--q4-only", action="store_true",
                    help="run only the matrix-free Q4 sample and print its JSON")
-    p.add_argument("--c4-n", type=int, default=64, help="Q4 hexahedra per direction")
+    p.add_argument("--q4-n", type=int, default=64, help="Q4 hexahedra per direction")
     p.add_argument("--profile-q4", action="store_true",
                    help="apply the Q4 operator only (for an ncu capture of k_q4_cells)")
     p.add_argument("--profile-step", action="store_true",
-                   help="run one mixed-precision c2 step only (for an ncu launch list)")
+                   help="run one mixed-precision P2 Poisson step only (for an ncu launch list)")
     p.add_argument("--profile", action="store_true",
                    help="profiling target: a few launches of every hot kernel, no timing")
     return p.parse_args()
@@ -91,7 +91,7 @@ def make_inputs(n, seed=0):
 
 
 class Problem:
-    """Device-resident c2 problem with reusable assemblers and both solvers:
+    """Device-resident P2 Poisson problem with reusable assemblers and both solvers:
     the plain FP64 path (sliced-ELL FP64 operator, Jacobi-PCG) and the
     mixed-precision path (FP32 inner PCG inside FP64 refinement)."""
 
@@ -348,7 +348,7 @@ def run_reference(args):
 
 
 # --------------------------------------------------------------------------- our arm
-def c3_sample(steps=1, warmup=1):
+def elasticity_sample(steps=1, warmup=1):
     """Linear elasticity, vector P2 on [0,4]x[0,1]^2 split into 96x24x24
     hexahedra x 6 tetrahedra (331,776 cells, 1,390,179 dofs), E lognormal
     (log 1e3, 0.5) per cell, nu = 0.3, body force (0,0,-1), clamped at x = 0.
@@ -415,7 +415,7 @@ def c3_sample(steps=1, warmup=1):
 Q4_FLOP_PER_CELL = 2 * 2000 + 125 * 80
 
 
-def c4_sample(n=64, seed=4):
+def q4_sample(n=64, seed=4):
     """Matrix-free Laplacian, Q4 Lagrange on the unit cube with n^3 hexahedra
     (interior vertices perturbed by U(-0.05h, 0.05h)), Gauss-Legendre 5^3
     quadrature, homogeneous Dirichlet boundary, b ~ U[-1, 1] on interior
@@ -498,7 +498,7 @@ def c4_sample(n=64, seed=4):
 
 
 def setup_sample(m):
-    """Structure set-up of the c2 space, host builders against device
+    """Structure set-up of the P2 space, host builders against device
     builders (sparsity pattern; FP64 and FP32 sliced-ELL operators), each
     on a fresh function space so that no cached pattern is reused."""
     import time
@@ -534,7 +534,7 @@ def setup_sample(m):
 
 
 def facets_sample(P):
-    """Exterior-facet loops and functionals on the c2 mesh: the Neumann
+    """Exterior-facet loops and functionals on the P2 Poisson mesh: the Neumann
     vector and the Robin facet mass over all 49,152 boundary facets, and
     a(u, u), L(u) over the 1.57M cells."""
     import torch
@@ -794,15 +794,15 @@ def run_ours(args):
     err_mixed_tight = float((x_ir - x_tight).norm() / x_tight.norm())
     err_fp64_tight = float((x64 - x_tight).norm() / x_tight.norm())
 
-    # ---- c3: elasticity through the same solvers (block CSR expanded)
-    c3 = None
-    if not args.no_c3:
-        c3 = c3_sample()
+    # ---- elasticity through the same solvers (block CSR expanded)
+    elasticity = None
+    if not args.no_elasticity:
+        elasticity = elasticity_sample()
 
-    # ---- c4: matrix-free Q4 action and CG
-    c4 = None
-    if not args.no_c4:
-        c4 = c4_sample(args.c4_n)
+    # ---- matrix-free Q4 action and CG
+    q4 = None
+    if not args.no_q4:
+        q4 = q4_sample(args.q4_n)
 
     # ---- structure set-up on the host and on the device
     setup = setup_sample(m)
@@ -848,22 +848,22 @@ def run_ours(args):
                              "frac": ach32 / peak, "peak_source": peak_kind,
                              "alg_bytes_per_launch": alg32, "launch_ms": ms32,
                              "padding": info32["padding"],
-                             "traffic": profile_traffic("sell_f32_c2")},
+                             "traffic": profile_traffic("sell_f32_p2_64")},
                 "roofline_fp64_operator": {"achieved": ach64, "frac": ach64 / peak,
                                            "alg_bytes_per_launch": alg64, "launch_ms": ms64k,
-                                           "traffic": profile_traffic("sell_f64_c2")},
+                                           "traffic": profile_traffic("sell_f64_p2_64")},
                 "roofline_assembly": {"kernel": "k_cells_matrix<P2> (FP64 atomics, slot map)",
                                       "achieved": ach_asm, "peak": peak, "unit": "GB/s",
                                       "frac": ach_asm / peak, "alg_bytes_per_launch": alg_asm,
                                       "launch_ms": ms_asm, "cells_per_s": nc / (ms_asm * 1e-3),
-                                      "traffic": profile_traffic("assemble_p2_c2"),
+                                      "traffic": profile_traffic("assemble_p2_64"),
                                       "bound": "latency: FP64 element tensors in one warp per block, FP64 atomic scatter (ncu); not hbm"},
                 "assemble_vector_ms": ms_vec, "apply_lifting_ms": ms_lift,
                 "autotune": P.tuning,
-                "setup_c2": setup,
-                "facets_c2": facets,
-                "c3_elasticity": c3,
-                "c4_matrix_free_q4": c4,
+                "setup_p2_64": setup,
+                "facets_p2_64": facets,
+                "elasticity_p2": elasticity,
+                "matrix_free_q4": q4,
                 "serving": serving_out,
                 "gpu_launches": launches,
                 "clocks": clocks,
@@ -897,7 +897,7 @@ def run_profile(args):
 
 
 def run_profile_step(args):
-    """One full mixed-precision c2 step (assembly, right-hand side, operator
+    """One full mixed-precision P2 Poisson step (assembly, right-hand side, operator
     refresh, solve to rtol 1e-10) after the set-up and autotuning: the run
     behind the kernel launch list."""
     import torch
@@ -913,7 +913,7 @@ def run_profile_step(args):
 
 
 def run_profile_q4(args):
-    """The Q4 operator on --c4-n^3 hexahedra, its FP32 and FP64 actions
+    """The Q4 operator on --q4-n^3 hexahedra, its FP32 and FP64 actions
     applied twice each: the run behind an ncu capture of k_q4_cells."""
     import numpy as np
     import torch
@@ -921,7 +921,7 @@ def run_profile_q4(args):
     from dolfinx_gb300 import matrix_free as mf
 
     torch.cuda.set_device(0)
-    n = args.c4_n
+    n = args.q4_n
     op = mf.Q4Laplacian(mf.hex_box_vertices(n, perturb=0.05, seed=4), n)
     u64 = torch.from_numpy(np.random.default_rng(4).standard_normal(op.n)).cuda()
     u32 = u64.float()
@@ -943,11 +943,11 @@ def main():
         return
     if args.profile:
         run_profile(args)
-    elif args.c4_only:
+    elif args.q4_only:
         import torch
 
         torch.cuda.set_device(0)
-        print(json.dumps({"c4_matrix_free_q4": c4_sample(args.c4_n)}))
+        print(json.dumps({"matrix_free_q4": q4_sample(args.q4_n)}))
     elif args.impl == "reference":
         run_reference(args)
     else:
