@@ -252,7 +252,8 @@ class SellOperator:
         perm = C.c_void_p()
         _capi.check(_capi.lib().dfx_operator_info(self.handle, C.byref(ns), C.byref(nsl),
                                                    C.byref(perm)))
-        return {"slots": ns.value, "slices": nsl.value, "padding": ns.value / self.A.nnz - 1}
+        pad = ns.value / self.A.nnz - 1 if self.A.nnz else 0.0
+        return {"slots": ns.value, "slices": nsl.value, "padding": pad}
 
     def __del__(self):
         h = getattr(self, "handle", None)
