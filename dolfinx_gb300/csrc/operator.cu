@@ -628,11 +628,12 @@ extern "C" int dfx_operator_info(dfx_operator op, int64_t* nslots, int32_t* nsli
 
 extern "C" int dfx_operator_apply(dfx_operator op, const void* d_x, void* d_y, void* stream)
 {
-  DFX_REQUIRE(op && d_x && d_y, "arguments must be non-NULL");
-  cudaStream_t s = dfx::as_stream(stream);
+  DFX_REQUIRE(op, "operator is NULL");
   const int32_t n = op->n;
   if (n == 0)
-    return DFX_OK;
+    return DFX_OK; // empty vectors may have NULL data
+  DFX_REQUIRE(d_x && d_y, "arguments must be non-NULL");
+  cudaStream_t s = dfx::as_stream(stream);
   const unsigned g = (unsigned)((n + 255) / 256);
   if (op->dtype == DFX_F64)
   {
@@ -659,6 +660,9 @@ extern "C" int dfx_operator_apply(dfx_operator op, const void* d_x, void* d_y, v
 extern "C" int dfx_operator_apply_renumbered(dfx_operator op, const void* d_x, void* d_y,
                                              void* stream)
 {
-  DFX_REQUIRE(op && d_x && d_y, "arguments must be non-NULL");
+  DFX_REQUIRE(op, "operator is NULL");
+  if (op->n == 0)
+    return DFX_OK; // empty vectors may have NULL data
+  DFX_REQUIRE(d_x && d_y, "arguments must be non-NULL");
   return dfx::sell_spmv(*op, d_x, d_y, dfx::as_stream(stream));
 }
