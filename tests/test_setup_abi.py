@@ -83,3 +83,57 @@ def test_exterior_facets_of_no_cells(capi):
     capi.check(capi.lib().dfx_exterior_facets_tet(0, cells.ctypes.data, out.ctypes.data,
                                                   C.byref(nf)))
     assert nf.value == 0
+
+
+def test_autotuner_table_host_logic(capi):
+    """The autotuner's table is host state: choices are keyed per workload
+    (form kind, degree, mass term, cells, mode; matrix shape), validated
+    against the candidates, and forgotten by dfx_tune_clear. Empty forms and
+    matrices reach it without a GPU."""
+    import ctypes as C
+
+    L = capi.lib()
+    capi.check(L.dfx_tune_clear())
+    f = capi.Form(capi.FORM_POISSON, 2, 0, 0, None, None, None, None, 1.0, 0.0, 0.3, None,
+                  (C.c_double * 3)())
+    v = C.c_int32(0)
+
+    def cpb(form, mode):
+        capi.check(L.dfx_get_cells_per_block(C.byref(form), mode, C.byref(v)))
+        return v.value
+
+    assert cpb(f, 0) == 32 and cpb(f, 1) == 32
+    capi.check(L.dfx_set_cells_per_block(C.byref(f), 0, 64))
+    assert cpb(f, 0) == 64 and cpb(f, 1) == 32  # modes are separate workloads
+    f.k2 = 1.0
+    assert cpb(f, 0) == 32  # the mass term is part of the key
+    assert L.dfx_set_cells_per_block(C.byref(f), 0, 48) == capi.DFX_ERR_INVALID
+    e = capi.Form(capi.FORM_ELASTICITY, 2, 0, 0, None, None, None, None, 1.0, 0.0, 0.3, None,
+                  (C.c_double * 3)())
+    assert cpb(e, 0) == 4
+    assert L.dfx_set_cells_per_block(C.byref(e), 0, 64) == capi.DFX_ERR_INVALID
+    capi.check(L.dfx_set_cells_per_block(C.byref(e), 0, 8))
+    assert cpb(e, 0) == 8
+    capi.check(L.dfx_set_cells_per_block(C.byref(e), 0, 0))  # back to the default
+    assert cpb(e, 0) == 4
+    A = capi.Csr(0, 0, 1, capi.F64, 0, None, None, None)
+    capi.check(L.dfx_get_spmv_lanes(C.byref(A), C.byref(v)))
+    assert v.value == 4  # mean row length 0
+    capi.check(L.dfx_set_spmv_lanes(C.byref(A), 16))
+    capi.check(L.dfx_get_spmv_lanes(C.byref(A), C.byref(v)))
+    assert v.value == 16
+    assert L.dfx_set_spmv_lanes(C.byref(A), 3) == capi.DFX_ERR_INVALID
+    capi.check(L.dfx_tune_clear())
+    f.k2 = 0.0
+    assert cpb(f, 0) == 32
+    capi.check(L.dfx_get_spmv_lanes(C.byref(A), C.byref(v)))
+    assert v.value == 4
+
+
+def test_device_sparsity_workspace_is_sized_by_the_problem(capi):
+    L = capi.lib()
+    small = L.dfx_sparsity_device_workspace_bytes(100, 50, 10)
+    big = L.dfx_sparsity_device_workspace_bytes(100000, 50000, 10)
+    assert 0 < small < big
+    assert big >= 50000 * 10 * 4  # the dof -> cell transpose
+    assert L.dfx_sparsity_device_workspace_bytes(-1, 0, 4) == 0
