@@ -108,6 +108,32 @@ def ref():
     return _ref
 
 
+REFLIB_LA = os.path.join(HERE, "_ref", "libdfxref_la.so")
+_ref_la = None
+
+
+def ref_la():
+    """The reference's own sparsity-pattern code, or None when not built."""
+    global _ref_la
+    if _ref_la is None and os.path.exists(REFLIB_LA):
+        R = C.CDLL(REFLIB_LA)
+        R.ref_sparsity.argtypes = [C.c_int32, C.c_int32, C.c_int32, _i32p, _i64p, C.c_void_p]
+        R.ref_sparsity.restype = C.c_int64
+        _ref_la = R
+    return _ref_la
+
+
+def ref_sparsity(n, dofmap):
+    """(row_ptr, cols) from the reference's SparsityPattern on one rank."""
+    R = ref_la()
+    dm = np.ascontiguousarray(dofmap, np.int32)
+    rp = np.empty(n + 1, np.int64)
+    nnz = R.ref_sparsity(n, dm.shape[0], dm.shape[1], dm, rp, None)
+    cols = np.empty(nnz, np.int32)
+    R.ref_sparsity(n, dm.shape[0], dm.shape[1], dm, rp, cols.ctypes.data)
+    return rp, cols
+
+
 def _ptr(a):
     return None if a is None else a.ctypes.data
 

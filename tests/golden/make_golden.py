@@ -2,8 +2,9 @@
 
 Runs where the DOLFINx source tree is available: it builds
 oracle/_ref/libdfxref.so from the reference's graph/ordering.cpp,
-common/sort.h and la/matrix_csr_impl.h (oracle/Makefile, target `ref`) and
-records their outputs on small seeded inputs. The test-suite then checks
+common/sort.h and la/matrix_csr_impl.h, and oracle/_ref/libdfxref_la.so
+from its la/SparsityPattern.cpp and common/IndexMap.cpp (oracle/Makefile,
+target `ref`), and records their outputs on small seeded inputs. The test-suite then checks
 the oracle restatement against these files on any machine.
 
     python tests/golden/make_golden.py
@@ -91,6 +92,16 @@ def main():
         out[f"spmv_y_{tag}"] = y
         out[f"csr_rowptr_{tag}"] = rp
         out[f"csr_cols_{tag}"] = cols
+    # 3. The cell sparsity pattern from the reference's own SparsityPattern
+    #    (la/SparsityPattern.cpp, one rank) for P1 and P2 dofmaps.
+    assert O.ref_la() is not None, "reference sparsity pattern did not build"
+    for tag, (n, deg) in {"p1": ((3, 4, 5), 1), "p2": ((4, 3, 2), 2)}.items():
+        cells, x = O.create_box_tet(*n)
+        dm, nn = O.dofmap_tet(cells, deg)
+        rp, cols = O.ref_sparsity(nn, dm)
+        out[f"sp_dofmap_{tag}"] = dm
+        out[f"sp_rowptr_{tag}"] = rp
+        out[f"sp_cols_{tag}"] = cols
     np.savez_compressed(os.path.join(HERE, "reference_golden.npz"), **out)
     print("wrote", len(out), "arrays")
 

@@ -165,3 +165,16 @@ def test_empty_operator(cuda, capi, build):
     assert op.info()["slots"] == 0
     x = torch.zeros(0, dtype=torch.float64, device="cuda")
     assert op.apply(x).numel() == 0
+
+
+@pytest.mark.parametrize("tag", ["p1", "p2"])
+def test_device_sparsity_matches_reference(cuda, capi, tag):
+    """The device builder against the reference's own SparsityPattern
+    (golden vectors written from la/SparsityPattern.cpp)."""
+    import os
+
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "reference_golden.npz"))
+    dm, rp_ref, cols_ref = g[f"sp_dofmap_{tag}"], g[f"sp_rowptr_{tag}"], g[f"sp_cols_{tag}"]
+    rp, cols = _device_sparsity(capi, rp_ref.size - 1, dm)
+    np.testing.assert_array_equal(rp, rp_ref)
+    np.testing.assert_array_equal(cols, cols_ref)

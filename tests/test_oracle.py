@@ -240,3 +240,28 @@ def test_functionals_on_polynomials(oracle, deg):
     assert abs(got - ref) < 1e-13 * ref
     f = 1.0 + x[:, 1]  # \int (1 + y) dx = 1.5
     assert abs(oracle.assemble_scalar(1, deg, cells, x, dm, one, f=f) - 1.5) < 1e-13
+
+
+@pytest.mark.parametrize("tag", ["p1", "p2"])
+def test_sparsity_matches_reference(oracle, golden, tag, capi):
+    """The cell sparsity pattern of the reference's own SparsityPattern
+    (la/SparsityPattern.cpp, compiled from its sources on one rank) against
+    the oracle and the product's host builder, bit for bit."""
+    import ctypes as C
+
+    dm = golden[f"sp_dofmap_{tag}"]
+    rp_ref, cols_ref = golden[f"sp_rowptr_{tag}"], golden[f"sp_cols_{tag}"]
+    n = rp_ref.size - 1
+    rp, cols = oracle.sparsity(n, dm)
+    np.testing.assert_array_equal(rp, rp_ref)
+    np.testing.assert_array_equal(cols, cols_ref)
+    rp2 = np.empty(n + 1, np.int64)
+    nnz = C.c_int64(0)
+    L = capi.lib()
+    capi.check(L.dfx_sparsity_create(n, dm.shape[0], dm.shape[1], dm.ctypes.data, rp2.ctypes.data,
+                                     None, C.byref(nnz)))
+    cols2 = np.empty(nnz.value, np.int32)
+    capi.check(L.dfx_sparsity_create(n, dm.shape[0], dm.shape[1], dm.ctypes.data, rp2.ctypes.data,
+                                     cols2.ctypes.data, C.byref(nnz)))
+    np.testing.assert_array_equal(rp2, rp_ref)
+    np.testing.assert_array_equal(cols2, cols_ref)
