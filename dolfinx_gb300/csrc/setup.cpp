@@ -50,6 +50,46 @@ void parallel_for(int64_t n, F&& f)
     t.join();
 }
 
+// Sort of a vector whose elements are all distinct under operator<: chunks
+// sorted on threads, then merged pairwise in rounds. With no equal elements
+// the result is the one order std::sort gives.
+template <typename T>
+void sort_distinct(std::vector<T>& v)
+{
+  const int64_t n = (int64_t)v.size();
+  const int nt = (int)std::min<int64_t>(num_threads(), std::max<int64_t>(1, n / 65536));
+  if (nt <= 1)
+  {
+    std::sort(v.begin(), v.end());
+    return;
+  }
+  std::vector<int64_t> b(nt + 1);
+  for (int t = 0; t <= nt; ++t)
+    b[t] = n * t / nt;
+  {
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; ++t)
+      th.emplace_back([&v, &b, t] { std::sort(v.begin() + b[t], v.begin() + b[t + 1]); });
+    for (auto& t : th)
+      t.join();
+  }
+  std::vector<T> tmp(n);
+  for (int w = 1; w < nt; w *= 2)
+  {
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; t += 2 * w)
+    {
+      const int64_t lo = b[t], mid = b[std::min(t + w, nt)], hi = b[std::min(t + 2 * w, nt)];
+      th.emplace_back([&v, &tmp, lo, mid, hi]
+                      { std::merge(v.begin() + lo, v.begin() + mid, v.begin() + mid,
+                                   v.begin() + hi, tmp.begin() + lo); });
+    }
+    for (auto& t : th)
+      t.join();
+    v.swap(tmp);
+  }
+}
+
 // Facet-connected dual graph in the order of build_local_dual_graph
 // (mesh/graphbuild.cpp:566-905, serial path): facets keyed by their
 // sorted vertex triple, stably sorted, matched pairs become edges,
@@ -60,27 +100,31 @@ void dual_graph(int64_t nc, const int64_t* cells, int64_t nverts, std::vector<in
   const int64_t nf = 4 * nc;
   const bool pack = nverts < (int64_t(1) << 21);
   std::vector<std::pair<uint64_t, uint64_t>> keys(nf); // (key hi, key lo | index)
-  for (int64_t c = 0; c < nc; ++c)
-    for (int f = 0; f < 4; ++f)
-    {
-      uint64_t v[3];
-      for (int k = 0; k < 3; ++k)
-        v[k] = (uint64_t)cells[4 * c + kFacets[f][k]];
-      if (v[0] > v[1])
-        std::swap(v[0], v[1]);
-      if (v[1] > v[2])
-        std::swap(v[1], v[2]);
-      if (v[0] > v[1])
-        std::swap(v[0], v[1]);
-      const uint64_t idx = (uint64_t)(4 * c + f);
-      if (pack)
-        keys[4 * c + f] = {(v[0] << 42) | (v[1] << 21) | v[2], idx};
-      else
-        keys[4 * c + f] = {(v[0] << 32) | v[1], (v[2] << 32) | idx};
-    }
+  parallel_for(nc,
+               [&](int64_t c0, int64_t c1)
+               {
+                 for (int64_t c = c0; c < c1; ++c)
+                   for (int f = 0; f < 4; ++f)
+                   {
+                     uint64_t v[3];
+                     for (int k = 0; k < 3; ++k)
+                       v[k] = (uint64_t)cells[4 * c + kFacets[f][k]];
+                     if (v[0] > v[1])
+                       std::swap(v[0], v[1]);
+                     if (v[1] > v[2])
+                       std::swap(v[1], v[2]);
+                     if (v[0] > v[1])
+                       std::swap(v[0], v[1]);
+                     const uint64_t idx = (uint64_t)(4 * c + f);
+                     if (pack)
+                       keys[4 * c + f] = {(v[0] << 42) | (v[1] << 21) | v[2], idx};
+                     else
+                       keys[4 * c + f] = {(v[0] << 32) | v[1], (v[2] << 32) | idx};
+                   }
+               });
   // (key, facet index) is a strict order, so an unstable sort gives the
   // stable-sort permutation of the reference.
-  std::sort(keys.begin(), keys.end());
+  sort_distinct(keys);
   auto same = [&](int64_t a, int64_t b)
   {
     if (pack)
@@ -493,7 +537,7 @@ extern "C" int dfx_exterior_facets_tet(int32_t num_cells, const int32_t* cells, 
       keys[4 * c + f] = pack ? std::make_pair((v[0] << 42) | (v[1] << 21) | v[2], idx)
                              : std::make_pair((v[0] << 32) | v[1], (v[2] << 32) | idx);
     }
-  std::sort(keys.begin(), keys.end());
+  sort_distinct(keys);
   auto same = [&](int64_t a, int64_t b)
   {
     if (pack)
