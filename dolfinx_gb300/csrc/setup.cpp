@@ -7,9 +7,11 @@
 #include "dfx_gpu.h"
 
 #include <algorithm>
+#include <atomic>
 #include <cstdarg>
 #include <cstdint>
 #include <cstring>
+#include <memory>
 #include <numeric>
 #include <thread>
 #include <vector>
@@ -354,45 +356,170 @@ extern "C" int dfx_mesh_create_box_tet(int32_t nx, int32_t ny, int32_t nz, const
   return DFX_OK;
 }
 
+namespace
+{
+void atomic_min(int64_t& a, int64_t v)
+{
+  std::atomic_ref<int64_t> r(a);
+  int64_t cur = r.load(std::memory_order_relaxed);
+  while (v < cur && !r.compare_exchange_weak(cur, v, std::memory_order_relaxed))
+  {
+  }
+}
+
+// Uninitialised array filled with `v` on threads.
+template <typename T>
+std::unique_ptr<T[]> filled(int64_t n, T v)
+{
+  std::unique_ptr<T[]> a(new T[std::max<int64_t>(n, 1)]);
+  parallel_for(n, [&](int64_t i0, int64_t i1) { std::fill(a.get() + i0, a.get() + i1, v); });
+  return a;
+}
+
+// Concurrent open-addressing table from edge keys (sorted vertex pair) to
+// the first position p = c*nd + local index at which the edge appears.
+// Slots are claimed with compare-and-swap; the position is a running
+// minimum, so the final table does not depend on the thread interleaving.
+struct EdgeFirst
+{
+  static constexpr uint64_t kEmpty = ~uint64_t(0);
+  uint64_t cap, mask;
+  std::unique_ptr<uint64_t[]> key;
+  std::unique_ptr<int64_t[]> first;
+  explicit EdgeFirst(int64_t n)
+  {
+    cap = 16;
+    while (cap < (uint64_t)(2 * n))
+      cap <<= 1;
+    mask = cap - 1;
+    key = filled<uint64_t>((int64_t)cap, kEmpty);
+    first = filled<int64_t>((int64_t)cap, INT64_MAX);
+  }
+  uint64_t slot(uint64_t k)
+  {
+    for (uint64_t h = (k * 0x9E3779B97F4A7C15ull) >> 17;; ++h)
+    {
+      const uint64_t i = h & mask;
+      std::atomic_ref<uint64_t> r(key[i]);
+      uint64_t cur = r.load(std::memory_order_acquire);
+      if (cur == k)
+        return i;
+      if (cur == kEmpty)
+      {
+        if (r.compare_exchange_strong(cur, k, std::memory_order_acq_rel))
+          return i;
+        if (cur == k)
+          return i;
+      }
+    }
+  }
+};
+} // namespace
+
 extern "C" int dfx_dofmap_create_tet(int32_t num_cells, const int32_t* cells, int32_t degree,
                                      int32_t* dofmap, int32_t* num_nodes)
 {
   if (degree != 1 && degree != 2)
     return dfx::fail(DFX_ERR_UNSUPPORTED, "Lagrange degree %d not supported", degree);
-  int32_t vmax = -1;
-  for (int64_t i = 0; i < 4 * (int64_t)num_cells; ++i)
-    vmax = std::max(vmax, cells[i]);
-  // Vertex dofs keyed by vertex, edge dofs by their sorted vertex pair;
-  // ids handed out in order of first appearance over the cell dofmap.
-  std::vector<int32_t> vid(vmax + 1, -1);
-  KeyMap emap(degree == 2 ? 7 * (int64_t)num_cells / 5 + 16 : 16);
-  int32_t cnt = 0;
+  const int64_t nc = num_cells;
   const int nd = degree == 1 ? 4 : 10;
-  for (int64_t c = 0; c < num_cells; ++c)
+  int32_t vmax = -1;
+  for (int64_t i = 0; i < 4 * nc; ++i)
   {
-    const int32_t* v = cells + 4 * c;
-    for (int i = 0; i < 4; ++i)
-    {
-      if (vid[v[i]] < 0)
-        vid[v[i]] = cnt++;
-      dofmap[nd * c + i] = vid[v[i]];
-    }
-    if (degree == 2)
-      for (int e = 0; e < 6; ++e)
-      {
-        uint64_t a = (uint32_t)v[kEdges[e][0]], b = (uint32_t)v[kEdges[e][1]];
-        if (a > b)
-          std::swap(a, b);
-        bool ins;
-        const int32_t id = emap.get((a << 32) | b, cnt, ins);
-        if (ins)
-          ++cnt;
-        dofmap[nd * c + 4 + e] = id;
-      }
+    if (cells[i] < 0)
+      return dfx::fail(DFX_ERR_INVALID, "negative vertex index in cell %lld", (long long)(i / 4));
+    vmax = std::max(vmax, cells[i]);
   }
-  // Ids were handed out in one pass over the local dofs of the cells in
-  // order, which is the reference's first-appearance numbering.
-  *num_nodes = cnt;
+  // Vertex dofs are keyed by vertex, edge dofs by their sorted vertex pair.
+  // The reference numbers them by first appearance over the cell dofmap
+  // (fem/dofmapbuilder.cpp:445-474). Here: (1) each entity's first position
+  // p = c*nd + i (atomic minimum, order-independent), (2) those positions
+  // marked, (3) the entity's number is the count of marks before its first
+  // position, (4) every position takes its entity's number.
+  const int64_t np = nd * nc;
+  std::unique_ptr<int64_t[]> vfirst = filled<int64_t>(vmax + 1, INT64_MAX);
+  EdgeFirst edges(degree == 2 ? 7 * nc / 5 + 16 : 1);
+  auto edge_key = [&](int64_t c, int e)
+  {
+    uint64_t a = (uint32_t)cells[4 * c + kEdges[e][0]], b = (uint32_t)cells[4 * c + kEdges[e][1]];
+    if (a > b)
+      std::swap(a, b);
+    return (a << 32) | b;
+  };
+  parallel_for(nc, [&](int64_t c0, int64_t c1)
+               {
+                 for (int64_t c = c0; c < c1; ++c)
+                 {
+                   for (int i = 0; i < 4; ++i)
+                     atomic_min(vfirst[cells[4 * c + i]], nd * c + i);
+                   if (degree == 2)
+                     for (int e = 0; e < 6; ++e)
+                       atomic_min(edges.first[edges.slot(edge_key(c, e))], nd * c + 4 + e);
+                 }
+               });
+  // (2) marks at first positions, (3) exclusive prefix counts in place.
+  std::unique_ptr<int32_t[]> number = filled<int32_t>(np, 0);
+  parallel_for(vmax + 1, [&](int64_t a, int64_t b)
+               {
+                 for (int64_t v = a; v < b; ++v)
+                   if (vfirst[v] != INT64_MAX)
+                     number[vfirst[v]] = 1;
+               });
+  if (degree == 2)
+    parallel_for((int64_t)edges.cap, [&](int64_t a, int64_t b)
+                 {
+                   for (int64_t i = a; i < b; ++i)
+                     if (edges.key[i] != EdgeFirst::kEmpty)
+                       number[edges.first[i]] = 1;
+                 });
+  const int nt = num_threads();
+  std::vector<int64_t> part(nt + 1, 0);
+  {
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; ++t)
+      th.emplace_back([&, t]
+                      {
+                        int64_t s = 0;
+                        for (int64_t p = np * t / nt; p < np * (t + 1) / nt; ++p)
+                          s += number[p];
+                        part[t + 1] = s;
+                      });
+    for (auto& t : th)
+      t.join();
+  }
+  for (int t = 0; t < nt; ++t)
+    part[t + 1] += part[t];
+  if (part[nt] > INT32_MAX)
+    return dfx::fail(DFX_ERR_UNSUPPORTED, "more than 2^31 dof nodes");
+  {
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; ++t)
+      th.emplace_back([&, t]
+                      {
+                        int64_t s = part[t];
+                        for (int64_t p = np * t / nt; p < np * (t + 1) / nt; ++p)
+                        {
+                          const int32_t m = number[p];
+                          number[p] = (int32_t)s;
+                          s += m;
+                        }
+                      });
+    for (auto& t : th)
+      t.join();
+  }
+  // (4) each position takes the number of its entity's first position.
+  parallel_for(nc, [&](int64_t c0, int64_t c1)
+               {
+                 for (int64_t c = c0; c < c1; ++c)
+                 {
+                   for (int i = 0; i < 4; ++i)
+                     dofmap[nd * c + i] = number[vfirst[cells[4 * c + i]]];
+                   if (degree == 2)
+                     for (int e = 0; e < 6; ++e)
+                       dofmap[nd * c + 4 + e] = number[edges.first[edges.slot(edge_key(c, e))]];
+                 }
+               });
+  *num_nodes = (int32_t)part[nt];
   return DFX_OK;
 }
 

@@ -47,6 +47,24 @@ def test_dofmap_and_sparsity_match_oracle(capi, oracle, n, deg):
     np.testing.assert_array_equal(cols, cols0)
 
 
+@pytest.mark.parametrize("deg", [1, 2])
+@pytest.mark.parametrize("n,reorder", [((24, 24, 24), True), ((30, 20, 26), False)])
+def test_dofmap_matches_oracle_on_threads(capi, oracle, n, reorder, deg):
+    """Boxes with tens of thousands of cells, so the dofmap's first-appearance
+    passes run on several threads; RCM order and the unordered build order
+    (a different cell order, so different first appearances). Two builds
+    must agree bit for bit."""
+    from dolfinx_gb300 import fem, mesh
+
+    m = mesh.create_box(((0, 0, 0), (1, 1, 1)), n, reorder=reorder)
+    dm, nn = oracle.dofmap_tet(m.cells, deg)
+    V = fem.functionspace(m, ("Lagrange", deg), device="cpu")
+    assert V.num_nodes == nn
+    np.testing.assert_array_equal(V.dofmap, dm)
+    V2 = fem.functionspace(m, ("Lagrange", deg), device="cpu")
+    np.testing.assert_array_equal(V2.dofmap, V.dofmap)
+
+
 def test_colouring_is_valid(capi):
     from dolfinx_gb300 import fem, mesh
 
