@@ -10,6 +10,7 @@
 #include <atomic>
 #include <cstdarg>
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <memory>
 #include <numeric>
@@ -27,8 +28,16 @@ namespace
 constexpr int kEdges[6][2] = {{2, 3}, {1, 3}, {1, 2}, {0, 3}, {0, 2}, {0, 1}};
 constexpr int kFacets[4][3] = {{1, 2, 3}, {0, 2, 3}, {0, 1, 3}, {0, 1, 2}};
 
+// Host threads of the set-up: DFX_NUM_THREADS when set (1-256), else the
+// hardware concurrency (at most 64). Every result is independent of it.
 int num_threads()
 {
+  if (const char* e = std::getenv("DFX_NUM_THREADS"))
+  {
+    const int v = std::atoi(e);
+    if (v >= 1 && v <= 256)
+      return v;
+  }
   unsigned n = std::thread::hardware_concurrency();
   return n == 0 ? 1 : (int)std::min(n, 64u);
 }

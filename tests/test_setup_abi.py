@@ -159,3 +159,37 @@ def test_device_sparsity_workspace_is_sized_by_the_problem(capi):
     assert 0 < small < big
     assert big >= 50000 * 10 * 4  # the dof -> cell transpose
     assert L.dfx_sparsity_device_workspace_bytes(-1, 0, 4) == 0
+
+
+_THREADS_SCRIPT = r"""
+import sys
+import numpy as np
+sys.path.insert(0, sys.argv[1])
+from dolfinx_gb300 import fem, mesh
+m = mesh.create_box(((0, 0, 0), (1, 1, 1)), (26, 22, 20))
+V = fem.functionspace(m, ("Lagrange", 2), device="cpu")
+np.savez(sys.argv[2], cells=m.cells, x=m.x, dofmap=V.dofmap, facets=m.exterior_facets())
+"""
+
+
+def test_host_setup_is_independent_of_the_thread_count(capi, tmp_path):
+    """Mesh (dual-graph sort), dofmap (first appearance) and exterior facets
+    built with 1, 3, 7 and 16 host threads are identical: the GPU host has a
+    different core count from the machine the parity tests ran on."""
+    import os
+    import subprocess
+    import sys
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    script = tmp_path / "build_mesh.py"
+    script.write_text(_THREADS_SCRIPT)
+    out = {}
+    for t in (1, 3, 7, 16):
+        f = tmp_path / f"t{t}.npz"
+        env = dict(os.environ, DFX_NUM_THREADS=str(t))
+        subprocess.run([sys.executable, str(script), root, str(f)], check=True, env=env,
+                       timeout=300)
+        out[t] = np.load(f)
+    for t in (3, 7, 16):
+        for k in ("cells", "x", "dofmap", "facets"):
+            np.testing.assert_array_equal(out[t][k], out[1][k])
