@@ -169,6 +169,14 @@ _SIGS = {
     "dfx_set_spmv_lanes": (C.c_int, [C.POINTER(Csr), C.c_int32]),
     "dfx_get_spmv_lanes": (C.c_int, [C.POINTER(Csr), C.POINTER(C.c_int32)]),
     "dfx_tune_clear": (C.c_int, []),
+    "dfx_tune_export": (C.c_int, [_P, C.c_int64, C.POINTER(C.c_int64)]),
+    "dfx_tune_import": (C.c_int, [_P, C.c_int64]),
+    "dfx_timing_record": (C.c_int, [C.c_char_p, C.c_double]),
+    "dfx_timing": (C.c_int, [C.c_char_p, C.POINTER(C.c_int32), C.POINTER(C.c_double)]),
+    "dfx_timing_num_tasks": (C.c_int, [C.POINTER(C.c_int32)]),
+    "dfx_timing_task": (C.c_int, [C.c_int32, C.c_char_p, C.c_int32, C.POINTER(C.c_int32),
+                                  C.POINTER(C.c_int32), C.POINTER(C.c_double)]),
+    "dfx_timing_clear": (C.c_int, []),
     "dfx_operator_create": (C.c_int, [C.POINTER(Csr), C.c_int32, C.c_int32, C.c_int32,
                                       C.POINTER(C.c_void_p), _P]),
     "dfx_operator_create_ex": (C.c_int, [C.POINTER(Csr), C.c_int32, C.c_int32, C.c_int32,

@@ -5,6 +5,7 @@
 // mesh ordering is itself pinned to the reference's compiled
 // graph/ordering.cpp and common/sort.h).
 #include "dfx_gpu.h"
+#include "timing.h"
 
 #include <algorithm>
 #include <atomic>
@@ -14,6 +15,7 @@
 #include <cstring>
 #include <memory>
 #include <numeric>
+#include <optional>
 #include <thread>
 #include <vector>
 
@@ -315,6 +317,7 @@ extern "C" int dfx_mesh_create_box_tet(int32_t nx, int32_t ny, int32_t nz, const
   const int64_t nc = 6 * nhex;
   if (nc > INT32_MAX / 4)
     return dfx::fail(DFX_ERR_INVALID, "mesh too large for int32 cell indices");
+  dfx::ScopedTimer timer("Build BoxMesh (tetrahedra)");
   // Lexicographic vertices (generation.h:332-377) and the 6-tet split of
   // each hexahedron sharing the v0-v7 diagonal (generation.h:404-420).
   const double ext[3] = {(p1[0] - p0[0]) / nx, (p1[1] - p0[1]) / ny, (p1[2] - p0[2]) / nz};
@@ -334,8 +337,14 @@ extern "C" int dfx_mesh_create_box_tet(int32_t nx, int32_t ny, int32_t nz, const
   if (reorder)
   {
     std::vector<int32_t> off, adj, r;
-    dual_graph(nc, cells.data(), nv, off, adj);
-    rcm(off, adj, r);
+    {
+      dfx::ScopedTimer t("Compute local part of mesh dual graph");
+      dual_graph(nc, cells.data(), nv, off, adj);
+    }
+    {
+      dfx::ScopedTimer t("Reverse Cuthill-McKee ordering");
+      rcm(off, adj, r);
+    }
     perm.resize(nc);
     for (int64_t c = 0; c < nc; ++c)
       perm[r[c]] = (int32_t)c;
@@ -439,6 +448,9 @@ extern "C" int dfx_dofmap_create_tet(int32_t num_cells, const int32_t* cells, in
       return dfx::fail(DFX_ERR_INVALID, "negative vertex index in cell %lld", (long long)(i / 4));
     vmax = std::max(vmax, cells[i]);
   }
+  dfx::ScopedTimer timer("Dofmap builder: build dofmap data");
+  std::optional<dfx::ScopedTimer> reorder(std::in_place,
+                                          "Dofmap builder: compute dof reordering map");
   // Vertex dofs are keyed by vertex, edge dofs by their sorted vertex pair.
   // The reference numbers them by first appearance over the cell dofmap
   // (fem/dofmapbuilder.cpp:445-474). Here: (1) each entity's first position
@@ -516,6 +528,7 @@ extern "C" int dfx_dofmap_create_tet(int32_t num_cells, const int32_t* cells, in
     for (auto& t : th)
       t.join();
   }
+  reorder.reset();
   // (4) each position takes the number of its entity's first position.
   parallel_for(nc, [&](int64_t c0, int64_t c1)
                {
@@ -538,6 +551,7 @@ extern "C" int dfx_sparsity_create(int32_t nrows, int32_t num_cells, int32_t nd,
 {
   if (nrows < 0 || num_cells < 0 || nd <= 0 || !row_ptr)
     return dfx::fail(DFX_ERR_INVALID, "invalid sparsity arguments");
+  dfx::ScopedTimer timer("Build sparsity");
   // Transpose dofmap: node -> cells.
   std::vector<int32_t> coff(nrows + 1, 0);
   for (int64_t i = 0; i < (int64_t)num_cells * nd; ++i)

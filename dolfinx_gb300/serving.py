@@ -92,7 +92,9 @@ class Structure:
 
     def __init__(self, n: int, degree: int, device="cuda", tune: bool = True):
         """tune: time the launch-shape candidates on this structure (cells per
-        block of the assembly, sliced-ELL window sigma) and use the fastest."""
+        block of the assembly, sliced-ELL window sigma) and use the fastest;
+        a choice already recorded for the workload (an earlier structure of
+        this size, or a loaded tuning cache file) is used without timing."""
         self.n, self.degree = n, degree
         self.mesh = mesh.create_unit_cube(n, n, n)
         self.V = fem.functionspace(self.mesh, ("Lagrange", degree), device=device)
@@ -106,8 +108,8 @@ class Structure:
         sigma = 256
         self.tuning = {}
         if tune:
-            self.tuning["assembly"] = autotune.tune_assembly(self.asm)
-            self.tuning["sigma"] = autotune.tune_sigma(self.A0)
+            self.tuning["assembly"] = autotune.tune_assembly(self.asm, reuse=True)
+            self.tuning["sigma"] = autotune.tune_sigma(self.A0, reuse=True)
             sigma = self.tuning["sigma"]["sigma"]
         self.op64 = la.SellOperator(self.A0, torch.float64, sigma)
         self.op32 = la.SellOperator(self.A0, torch.float32, sigma, compress_cols=True)

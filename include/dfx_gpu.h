@@ -348,6 +348,47 @@ int dfx_set_spmv_lanes(const dfx_csr* A, int32_t lanes); /* 0: default */
 int dfx_get_spmv_lanes(const dfx_csr* A, int32_t* lanes);
 /* Forget every recorded choice. */
 int dfx_tune_clear(void);
+/* The recorded choices as rows of 6 int64, (device, what, k0, k1, k2,
+ * value), in key order: what 1 = cells per block (k0 cells, k1 = 16 kind +
+ * 4 degree + 2 mass + mode, k2 0), what 2 = lanes per row (k0 rows, k1
+ * entries, k2 = 4 bs + dtype). With rows NULL only *num is written; with
+ * fewer than *num rows of room, DFX_ERR_NO_MEMORY and *num = the count
+ * needed. This is what a tuning cache file stores. */
+int dfx_tune_export(int64_t* rows, int64_t cap, int64_t* num);
+/* Add exported rows to the table, replacing entries of the same key. All
+ * rows are checked first (device >= 0; what 1 with a value among its form
+ * kind's candidates, what 2 with 4, 8, 16 or 32); on a bad row nothing is
+ * added and DFX_ERR_INVALID names it. */
+int dfx_tune_import(const int64_t* rows, int64_t num);
+
+/* ---------------------------------------------------------------- timings
+ * Named wall-clock timings of host work, accumulated per task for the life
+ * of the process: common::Timer / TimeLogger (common/Timer.h:38-141,
+ * common/TimeLogger.cpp:27-40). The host set-up above registers under the
+ * reference's task names: "Build BoxMesh (tetrahedra)"
+ * (mesh/generation.h:386), "Compute local part of mesh dual graph"
+ * (mesh/graphbuild.cpp:575), "Reverse Cuthill-McKee ordering"
+ * (graph/ordering.cpp:70), "Dofmap builder: build dofmap data"
+ * (fem/dofmapbuilder.cpp:666), "Dofmap builder: compute dof reordering map"
+ * (fem/dofmapbuilder.cpp:428) and "Build sparsity" (fem/utils.h:251; one
+ * repetition per dfx_sparsity_create call, so the count pass and the fill
+ * pass of one pattern are two). Device work is asynchronous and is timed
+ * with CUDA events by its caller instead. */
+
+/* One more repetition of `seconds` for `task` (a NUL-terminated name). */
+int dfx_timing_record(const char* task, double seconds);
+/* (repetitions, total seconds) of a task: dolfinx::timing
+ * (common/timing.h:36-38). DFX_ERR_INVALID, "No timings registered for task
+ * "<task>".", when it has none. */
+int dfx_timing(const char* task, int32_t* count, double* total_seconds);
+/* The tasks in byte-wise name order (dolfinx::timings(), common/timing.h:
+ * 42-46): their number, and the i-th. name receives at most name_cap bytes
+ * including the NUL (truncated if longer); *name_len the full length. */
+int dfx_timing_num_tasks(int32_t* num);
+int dfx_timing_task(int32_t i, char* name, int32_t name_cap, int32_t* name_len,
+                    int32_t* count, double* total_seconds);
+/* Forget every timing. */
+int dfx_timing_clear(void);
 
 /* ------------------------------------------------- sliced-ELL operator
  * The solver-side copy of a scalar MatrixCSR: rows sorted by length

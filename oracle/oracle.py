@@ -119,6 +119,10 @@ def ref_la():
         R = C.CDLL(REFLIB_LA)
         R.ref_sparsity.argtypes = [C.c_int32, C.c_int32, C.c_int32, _i32p, _i64p, C.c_void_p]
         R.ref_sparsity.restype = C.c_int64
+        R.ref_timing_record.argtypes = [C.c_char_p, C.c_double]
+        R.ref_timing_record.restype = None
+        R.ref_timing_table.argtypes = [C.c_int, C.c_char_p, C.c_int64]
+        R.ref_timing_table.restype = C.c_int64
         _ref_la = R
     return _ref_la
 
@@ -132,6 +136,22 @@ def ref_sparsity(n, dofmap):
     cols = np.empty(nnz, np.int32)
     R.ref_sparsity(n, dm.shape[0], dm.shape[1], dm, rp, cols.ctypes.data)
     return rp, cols
+
+
+def ref_timing_record(task, seconds):
+    """One more repetition of ``seconds`` for ``task`` in the reference's
+    TimeLogger (this process's)."""
+    ref_la().ref_timing_record(task.encode(), float(seconds))
+
+
+def ref_timing_table(reduction):
+    """The reference's summary table (TimeLogger::timing_table, reduced on
+    one rank; reduction 0/1/2 = average/max/min) as a string."""
+    R = ref_la()
+    n = R.ref_timing_table(reduction, None, 0)
+    buf = C.create_string_buffer(n + 1)
+    R.ref_timing_table(reduction, buf, n + 1)
+    return buf.raw[:n].decode()
 
 
 def _ptr(a):

@@ -3,12 +3,19 @@
 // compiled from its sources on one rank with the stand-in headers of
 // oracle/ref_shim_la/. TEST INFRASTRUCTURE ONLY: built into oracle/_ref/
 // by oracle/Makefile when the reference tree is present, used to write the
-// golden sparsity patterns under tests/golden/.
+// golden sparsity patterns under tests/golden/ and to check the timing
+// summary table against the reference's own TimeLogger and Table.
+#include <algorithm>
+#include <chrono>
 #include <cstdint>
+#include <cstring>
 #include <dolfinx/common/IndexMap.h>
+#include <dolfinx/common/Table.h>
+#include <dolfinx/common/TimeLogger.h>
 #include <dolfinx/la/SparsityPattern.h>
 #include <memory>
 #include <span>
+#include <string>
 
 extern "C"
 {
@@ -36,5 +43,30 @@ int64_t ref_sparsity(int32_t nrows, int32_t nc, int32_t nd, const int32_t* dofma
     for (std::size_t k = 0; k < edges.size(); ++k)
       cols[k] = edges[k];
   return (int64_t)edges.size();
+}
+
+// One more repetition of `seconds` for `task` in the reference's
+// TimeLogger (common/TimeLogger.cpp:27-40).
+void ref_timing_record(const char* task, double seconds)
+{
+  dolfinx::common::TimeLogger::instance().register_timing(
+      task, std::chrono::duration<double>(seconds));
+}
+
+// The table list_timings prints (common/TimeLogger.cpp:42-53) on one rank,
+// reduction 0/1/2 = average/max/min, without the surrounding newlines.
+// Writes at most cap bytes including a NUL; returns the full length.
+int64_t ref_timing_table(int reduction, char* buf, int64_t cap)
+{
+  const dolfinx::Table t = dolfinx::common::TimeLogger::instance().timing_table().reduce(
+      MPI_COMM_WORLD, static_cast<dolfinx::Table::Reduction>(reduction));
+  const std::string s = t.str();
+  if (cap > 0)
+  {
+    const std::size_t n = std::min<std::size_t>(s.size(), cap - 1);
+    std::memcpy(buf, s.data(), n);
+    buf[n] = '\0';
+  }
+  return (int64_t)s.size();
 }
 }
