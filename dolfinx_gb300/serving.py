@@ -56,6 +56,46 @@ class Request:
     arrival: float = 0.0  # seconds from the start of the stream
 
 
+# Largest n whose 6 n^3 tetrahedra keep every cell-vertex index in int32.
+MAX_N = 447
+
+
+def request_error(req: Request) -> str | None:
+    """Why a request cannot be served, or None: checked on the host before
+    any device work, so that a malformed request is refused alone instead of
+    stopping the loop."""
+    if isinstance(req.n, bool) or not isinstance(req.n, (int, np.integer)) or req.n < 1:
+        return f"n must be a positive integer (got {req.n!r})"
+    if req.n > MAX_N:
+        return f"n = {req.n}: mesh too large for int32 cell indices (n <= {MAX_N})"
+    if req.degree not in (1, 2):
+        return f"Lagrange degree {req.degree!r} not supported (1 or 2)"
+    try:
+        k2 = float(req.k2)
+    except (TypeError, ValueError):
+        return f"k2 must be a number (got {req.k2!r})"
+    if not math.isfinite(k2) or k2 < 0.0:
+        return f"k2 must be finite and >= 0 so that the operator is SPD (got {req.k2!r})"
+    if isinstance(req.seed, bool) or not isinstance(req.seed, (int, np.integer)) or \
+            not 0 <= req.seed < 2 ** 64:
+        return f"seed must be an integer in [0, 2^64) (got {req.seed!r})"
+    return None
+
+
+@dataclass
+class Rejected:
+    """A request refused without a solve: malformed, larger than the whole
+    HBM budget, or its set-up failed. status is a DFX_ERR_* code."""
+
+    req: Request
+    status: int
+    error: str
+    t_done: float
+    st: None = None
+    x: None = None
+    iterations: int = 0
+
+
 def make_requests(count: int, rate: float, seed: int = 0, n_range=(8, 96)) -> list[Request]:
     """Synthetic request stream: Poisson arrivals at `rate`/s, n log-uniform
     in n_range, P1/P2 with equal probability, k2 ~ U[0, 10]."""
@@ -237,9 +277,11 @@ class Server:
         self.structures.move_to_end(key)
         return st
 
-    def _evict(self, keep=None):
+    def _evict(self, keep=None, need: int = 0):
+        """Drop least recently used idle structures (other than `keep`) until
+        they and `need` more bytes fit under the budget."""
         for key in list(self.structures):
-            if self.used <= self.budget:
+            if self.used + need <= self.budget:
                 break
             st = self.structures[key]
             if st.users == 0 and key != keep:
@@ -253,18 +295,46 @@ class Server:
         torch.cuda.synchronize()
 
     # ------------------------------------------------------------ admission
-    def admit(self, req: Request) -> Job | None:
-        st = self.structure(req.n, req.degree)
+    def _reject(self, req: Request, status: int, error: str) -> Rejected:
+        rej = Rejected(req, int(status), error, time.perf_counter())
+        with self.lock:
+            self.finished.append(rej)
+        return rej
+
+    def admit(self, req: Request) -> Job | Rejected | None:
+        """A Job when the request is admitted; None when it must wait for
+        memory or a batch slot; a Rejected record when it can never run (its
+        structure and values exceed the whole budget) or its set-up failed."""
+        key = (req.n, req.degree)
+        try:
+            st = self.structure(*key)
+        except Exception as exc:
+            return self._reject(req, getattr(exc, "code", -1), f"structure set-up failed: {exc}")
         need = st.request_bytes()
         small = st.ndofs <= self.batch_max_dofs
+        if st.bytes + need > self.budget:
+            rej = self._reject(req, _capi.DFX_ERR_NO_MEMORY,
+                               f"needs {st.bytes + need} bytes with its structure; the HBM "
+                               f"budget is {self.budget:.0f}")
+            with self.lock:
+                self._evict()
+            return rej
         with self.lock:
+            if self.used + need > self.budget:
+                self._evict(keep=key, need=need)
             if self.used + need > self.budget:
                 return None
             if small and not self.free_slots:
                 return None
             self.used += need
             st.users += 1
-        job = Job(req, st, self.mode, self.stream_setup, self.assembly)
+        try:
+            job = Job(req, st, self.mode, self.stream_setup, self.assembly)
+        except Exception as exc:
+            with self.lock:
+                self.used -= need
+                st.users -= 1
+            return self._reject(req, getattr(exc, "code", -1), f"request set-up failed: {exc}")
         job.bytes = need
         if small:
             self.stream_setup.synchronize()
@@ -377,8 +447,12 @@ class Server:
                                    f"({len(self.finished)} of {total} done)")
             while pending and pending[0].arrival <= now:
                 r = pending.popleft()
-                waiting.append(r)
                 arrivals[r.rid] = t0 + r.arrival
+                err = request_error(r)
+                if err is None:
+                    waiting.append(r)
+                else:
+                    self._reject(r, _capi.DFX_ERR_INVALID, err)
             while waiting:
                 job = self.admit(waiting[0])
                 if job is None:
@@ -391,15 +465,21 @@ class Server:
             else:
                 time.sleep(0.0005)
         wall = time.perf_counter() - t0
-        lat = np.array([j.t_done - arrivals[j.req.rid] for j in self.finished])
-        bad = [j.req.rid for j in self.finished if j.status != 0]
+        served = [j for j in self.finished if not isinstance(j, Rejected)]
+        lat = np.array([j.t_done - arrivals[j.req.rid] for j in served])
+
+        def ms(v):
+            return float(v * 1e3) if len(lat) else None
+
         return {"mode": self.mode, "requests": total, "wall_s": wall,
-                "solves_per_s": total / wall,
-                "p50_ms": float(np.percentile(lat, 50) * 1e3),
-                "p99_ms": float(np.percentile(lat, 99) * 1e3),
-                "mean_ms": float(lat.mean() * 1e3),
-                "dofs_per_s": float(sum(j.st.ndofs for j in self.finished) / wall),
-                "failed": bad}
+                "solves_per_s": len(served) / wall,
+                "p50_ms": ms(np.percentile(lat, 50) if len(lat) else 0.0),
+                "p99_ms": ms(np.percentile(lat, 99) if len(lat) else 0.0),
+                "mean_ms": ms(lat.mean() if len(lat) else 0.0),
+                "dofs_per_s": float(sum(j.st.ndofs for j in served) / wall),
+                "failed": [j.req.rid for j in self.finished if j.status != 0],
+                "rejected": {j.req.rid: j.error for j in self.finished
+                             if isinstance(j, Rejected)}}
 
     def close(self):
         for _ in self.workers:

@@ -77,10 +77,14 @@ def test_admission_respects_the_hbm_budget(cuda, capi):
     srv = serving.Server(mode="mixed", hbm_budget=1e9)
     try:
         st = srv.structure(6, 1)
-        srv.budget = srv.used + st.request_bytes() - 1  # one byte short
-        assert srv.admit(serving.Request(0, 6, 1, 0.0, 1)) is None
-        srv.budget = srv.used + st.request_bytes()
-        assert srv.admit(serving.Request(1, 6, 1, 0.0, 1)) is not None
+        need = st.request_bytes()
+        srv.budget = srv.used + need - 1  # one byte short even alone: refused
+        rej = srv.admit(serving.Request(0, 6, 1, 0.0, 1))
+        assert isinstance(rej, serving.Rejected) and rej.status == capi.DFX_ERR_NO_MEMORY
+        srv.budget = srv.used + need  # exactly enough for one
+        job = srv.admit(serving.Request(1, 6, 1, 0.0, 1))
+        assert isinstance(job, serving.Job)
+        assert srv.admit(serving.Request(2, 6, 1, 0.0, 1)) is None  # waits for the first
     finally:
         srv.close()
 
