@@ -129,6 +129,29 @@ def test_cg_not_converged_reports(cuda, oracle, capi):
         la.cg(A, b, rtol=1e-14, max_iters=3)
 
 
+def test_nan_coefficient_reports_breakdown(cuda, oracle, capi):
+    """An injected fault: one cell's kappa is NaN. The solves end with an
+    error status (p.Ap or the residual is not finite) instead of returning
+    a NaN solution; the iteration caps bound every loop."""
+    from dolfinx_gb300 import fem, la
+
+    m, V, kappa, f, rp, cols = problem(oracle, (6, 6, 6), 1, seed=31)
+    kappa[m.num_cells // 2] = np.nan
+    X = V.tabulate_dof_coordinates()
+    bnd = np.flatnonzero(np.isclose(X, 0).any(1)).astype(np.int32)
+    bc = fem.dirichletbc(0.0, bnd, V)
+    A = fem.assemble_matrix(fem.poisson_form(V, kappa), bcs=[bc])
+    b = fem.assemble_vector(fem.source_form(V, f))
+    assert torch.isnan(A.vals).any() and torch.isfinite(b).all()
+    with pytest.raises(capi.DfxError) as e:
+        la.cg(A, b, rtol=1e-10, max_iters=500)
+    assert e.value.code == capi.DFX_ERR_BREAKDOWN
+    ir = la.IRSolver(A)
+    res = ir.solve(b, torch.zeros_like(b), rtol=1e-10, max_outer=3, max_inner=200,
+                   raise_on_fail=False)
+    assert res.status in (capi.DFX_ERR_BREAKDOWN, capi.DFX_ERR_NOT_CONVERGED)
+
+
 @pytest.mark.parametrize("sigma", [32, 256])
 def test_sell_operator_f64(cuda, oracle, capi, sigma):
     from dolfinx_gb300 import fem, la
