@@ -615,6 +615,69 @@ extern "C" int dfx_sparsity_create(int32_t nrows, int32_t num_cells, int32_t nd,
   return DFX_OK;
 }
 
+extern "C" int dfx_tabulate_dof_coordinates_tet(int32_t num_cells, const int32_t* cells,
+                                                int32_t num_vertices, const double* x,
+                                                const int32_t* dofmap, int32_t degree,
+                                                int32_t num_nodes, double* X)
+{
+  if (degree != 1 && degree != 2)
+    return dfx::fail(DFX_ERR_UNSUPPORTED, "Lagrange degree %d not supported", degree);
+  if (num_cells < 0 || num_vertices < 0 || num_nodes < 0 ||
+      (num_cells > 0 && (!cells || !x || !dofmap || !X)))
+    return dfx::fail(DFX_ERR_INVALID, "invalid dof coordinate arguments");
+  const int nd = degree == 1 ? 4 : 10;
+  const int64_t nc = num_cells;
+  // Index checks first, so that nothing is written for a bad mesh.
+  std::atomic<int64_t> bad{-1};
+  parallel_for(nc, [&](int64_t a, int64_t b)
+               {
+                 for (int64_t c = a; c < b; ++c)
+                 {
+                   bool ok = true;
+                   for (int i = 0; i < 4; ++i)
+                     ok &= cells[4 * c + i] >= 0 && cells[4 * c + i] < num_vertices;
+                   for (int i = 0; i < nd; ++i)
+                     ok &= dofmap[nd * c + i] >= 0 && dofmap[nd * c + i] < num_nodes;
+                   if (!ok)
+                   {
+                     int64_t e = -1;
+                     bad.compare_exchange_strong(e, c);
+                     return;
+                   }
+                 }
+               });
+  if (bad.load() >= 0)
+    return dfx::fail(DFX_ERR_INVALID, "cell %lld has a vertex or dof index out of range",
+                     (long long)bad.load());
+  // Each cell writes its nodes: the vertices, then the edge midpoints in
+  // Basix edge order (the P2 interpolation points pushed forward by the
+  // affine map). A node shared by several cells gets the same value from
+  // each, so the stores are relaxed atomics (no ordering is needed).
+  parallel_for(nc, [&](int64_t a, int64_t b)
+               {
+                 for (int64_t c = a; c < b; ++c)
+                 {
+                   double v[4][3];
+                   for (int i = 0; i < 4; ++i)
+                     for (int k = 0; k < 3; ++k)
+                       v[i][k] = x[3 * (int64_t)cells[4 * c + i] + k];
+                   for (int i = 0; i < 4; ++i)
+                     for (int k = 0; k < 3; ++k)
+                       std::atomic_ref<double>(X[3 * (int64_t)dofmap[nd * c + i] + k])
+                           .store(v[i][k], std::memory_order_relaxed);
+                   if (degree == 2)
+                     for (int e = 0; e < 6; ++e)
+                       for (int k = 0; k < 3; ++k)
+                       {
+                         const double m = 0.5 * (v[kEdges[e][0]][k] + v[kEdges[e][1]][k]);
+                         std::atomic_ref<double>(X[3 * (int64_t)dofmap[nd * c + 4 + e] + k])
+                             .store(m, std::memory_order_relaxed);
+                       }
+                 }
+               });
+  return DFX_OK;
+}
+
 extern "C" int dfx_colour_cells(int32_t num_cells, int32_t nd, const int32_t* dofmap,
                                 int32_t num_nodes, int32_t* order, int32_t* offsets,
                                 int32_t max_colours, int32_t* num_colours)

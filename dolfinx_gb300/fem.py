@@ -19,8 +19,6 @@ from . import _capi
 from .la import MatrixCSR, _ptr, _stream
 from .mesh import Mesh
 
-_EDGES = np.array([[2, 3], [1, 3], [1, 2], [0, 3], [0, 2], [0, 1]])
-
 
 class FunctionSpace:
     """Lagrange P1/P2 space (scalar or vector, bs 3) on a tetrahedral mesh."""
@@ -55,13 +53,17 @@ class FunctionSpace:
         return self._dofmap_dev
 
     def tabulate_dof_coordinates(self) -> np.ndarray:
-        """Coordinates of the dof nodes (vertices, then edge midpoints)."""
-        X = np.empty((self.num_nodes, 3))
-        xc = self.mesh.x[self.mesh.cells]  # (nc, 4, 3)
-        X[self.dofmap[:, :4].ravel()] = xc.reshape(-1, 3)
-        if self.degree == 2:
-            mid = 0.5 * (xc[:, _EDGES[:, 0]] + xc[:, _EDGES[:, 1]])
-            X[self.dofmap[:, 4:].ravel()] = mid.reshape(-1, 3)
+        """Coordinates of the dof nodes (vertices, then edge midpoints), one
+        row per node: FunctionSpace::tabulate_dof_coordinates
+        (fem/FunctionSpace.h:218-330), computed on host threads."""
+        X = np.zeros((self.num_nodes, 3))
+        m = self.mesh
+        cells = np.ascontiguousarray(m.cells, np.int32)
+        x = np.ascontiguousarray(m.x, np.float64)
+        dm = np.ascontiguousarray(self.dofmap, np.int32)
+        _capi.check(_capi.lib().dfx_tabulate_dof_coordinates_tet(
+            m.num_cells, cells.ctypes.data, x.shape[0], x.ctypes.data, dm.ctypes.data,
+            self.degree, self.num_nodes, X.ctypes.data))
         return X
 
     def sparsity(self):

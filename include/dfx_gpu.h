@@ -146,6 +146,17 @@ int dfx_sparsity_create_device(int32_t nrows, int32_t num_cells, int32_t ndofs,
                                int32_t* d_cols, int64_t* nnz, void* d_work,
                                size_t work_bytes, void* stream);
 
+/* FunctionSpace::tabulate_dof_coordinates (fem/FunctionSpace.h:218-330) for
+ * Lagrange P1/P2 on affine tetrahedra: X (num_nodes, 3) receives each dof
+ * node's point, the cell vertices and the edge midpoints 0.5 (a + b) in
+ * Basix edge order. Nodes that no cell holds are not written (the caller
+ * zeroes X, as the reference does). Every index is checked before anything
+ * is written. Host function, threaded. */
+int dfx_tabulate_dof_coordinates_tet(int32_t num_cells, const int32_t* cells,
+                                     int32_t num_vertices, const double* x,
+                                     const int32_t* dofmap, int32_t degree,
+                                     int32_t num_nodes, double* X);
+
 /* Greedy cell colouring for DFX_MODE_COLOURED: no two cells of one colour
  * share a dof. order: (num_cells) cells grouped by colour, offsets:
  * (max_colours+1). Returns the colour count in *num_colours. */

@@ -193,3 +193,48 @@ def test_host_setup_is_independent_of_the_thread_count(capi, tmp_path):
     for t in (3, 7, 16):
         for k in ("cells", "x", "dofmap", "facets"):
             np.testing.assert_array_equal(out[t][k], out[1][k])
+
+
+def _dof_coordinates_numpy(m, V):
+    """The dof points restated with numpy: vertices, then edge midpoints
+    0.5 (a + b) in Basix edge order, zero for nodes that no cell holds."""
+    edges = np.array([[2, 3], [1, 3], [1, 2], [0, 3], [0, 2], [0, 1]])
+    X = np.zeros((V.num_nodes, 3))
+    xc = m.x[m.cells]
+    X[V.dofmap[:, :4].ravel()] = xc.reshape(-1, 3)
+    if V.degree == 2:
+        X[V.dofmap[:, 4:].ravel()] = (0.5 * (xc[:, edges[:, 0]] + xc[:, edges[:, 1]])).reshape(-1, 3)
+    return X
+
+
+@pytest.mark.parametrize("deg", [1, 2])
+@pytest.mark.parametrize("n", [(1, 1, 1), (3, 4, 2), (20, 18, 16)])
+def test_dof_coordinates_match_numpy(capi, n, deg):
+    from dolfinx_gb300 import fem, mesh
+
+    m = mesh.create_box(((-1.0, 0.25, 0.0), (2.0, 1.0, 3.5)), n)
+    V = fem.functionspace(m, ("Lagrange", deg), device="cpu")
+    X = V.tabulate_dof_coordinates()
+    assert X.shape == (V.num_nodes, 3)
+    np.testing.assert_array_equal(X, _dof_coordinates_numpy(m, V))
+    if deg == 1:
+        np.testing.assert_array_equal(X[V.dofmap], m.x[m.cells])
+
+
+def test_dof_coordinates_checks_indices(capi):
+    L = capi.lib()
+    cells = np.array([[0, 1, 2, 3]], np.int32)
+    x = np.zeros((4, 3))
+    X = np.full((4, 3), 7.0)
+    dm = np.array([[0, 1, 2, 4]], np.int32)  # node 4 of 4
+    assert L.dfx_tabulate_dof_coordinates_tet(1, cells.ctypes.data, 4, x.ctypes.data,
+                                              dm.ctypes.data, 1, 4,
+                                              X.ctypes.data) == capi.DFX_ERR_INVALID
+    assert (X == 7.0).all()  # nothing written
+    assert L.dfx_tabulate_dof_coordinates_tet(1, cells.ctypes.data, 3, x.ctypes.data,
+                                              dm.ctypes.data, 1, 5,
+                                              X.ctypes.data) == capi.DFX_ERR_INVALID
+    assert L.dfx_tabulate_dof_coordinates_tet(1, cells.ctypes.data, 4, x.ctypes.data,
+                                              dm.ctypes.data, 3, 5,
+                                              X.ctypes.data) == capi.DFX_ERR_UNSUPPORTED
+    assert L.dfx_tabulate_dof_coordinates_tet(0, None, 0, None, None, 2, 0, None) == capi.DFX_OK
