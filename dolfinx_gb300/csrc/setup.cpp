@@ -104,15 +104,31 @@ void sort_distinct(std::vector<T>& v)
 }
 
 // Facet-connected dual graph in the order of build_local_dual_graph
-// (mesh/graphbuild.cpp:566-905, serial path): facets keyed by their
-// sorted vertex triple, stably sorted, matched pairs become edges,
-// adjacency filled in edge order.
+// (mesh/graphbuild.cpp:566-905, serial path). The reference sorts the facets
+// by their sorted vertex triple (stably), turns each run of equal facets into
+// the edges between its cells (pairs a < b in run order) and fills the
+// adjacency in edge order. So a cell's neighbours are, for each of its facets
+// in sorted order, the other cells of that facet's run in run order. Here:
+// the facet keys are sorted by a parallel bucket sort on the smallest vertex,
+// and each cell's list is filled from the runs on threads.
 void dual_graph(int64_t nc, const int64_t* cells, int64_t nverts, std::vector<int32_t>& off,
                 std::vector<int32_t>& adj)
 {
+  // (key hi, key lo | index), left uninitialised on allocation so that the
+  // threads that fill it touch its pages first.
+  struct Key
+  {
+    uint64_t first, second;
+    bool operator<(const Key& o) const
+    {
+      return first < o.first || (first == o.first && second < o.second);
+    }
+  };
   const int64_t nf = 4 * nc;
   const bool pack = nverts < (int64_t(1) << 21);
-  std::vector<std::pair<uint64_t, uint64_t>> keys(nf); // (key hi, key lo | index)
+  std::optional<dfx::ScopedTimer> stage(std::in_place,
+                                        "Compute local part of mesh dual graph: keys");
+  std::unique_ptr<Key[]> keys(new Key[nf]);
   parallel_for(nc,
                [&](int64_t c0, int64_t c1)
                {
@@ -135,44 +151,140 @@ void dual_graph(int64_t nc, const int64_t* cells, int64_t nverts, std::vector<in
                        keys[4 * c + f] = {(v[0] << 32) | v[1], (v[2] << 32) | idx};
                    }
                });
-  // (key, facet index) is a strict order, so an unstable sort gives the
-  // stable-sort permutation of the reference.
-  sort_distinct(keys);
+  // (key, facet index) is a strict order, so any sort gives the stable-sort
+  // permutation of the reference. Buckets by the smallest vertex are
+  // increasing in the key, so sorting each bucket sorts the whole.
+  stage.emplace("Compute local part of mesh dual graph: sort");
+  const int shift = pack ? 42 : 32;
+  const int64_t nb = std::max<int64_t>(1, std::min<int64_t>(nf / 2048, nverts));
+  auto bucket = [&](const Key& k) { return (int64_t)((k.first >> shift) * (uint64_t)nb / (uint64_t)nverts); };
+  const int nt = (int)std::min<int64_t>(num_threads(), std::max<int64_t>(1, nf / 65536));
+  std::vector<int64_t> cnt((size_t)nt * nb, 0), bstart(nb + 1, 0);
+  {
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; ++t)
+      th.emplace_back([&, t]
+                      {
+                        int64_t* h = cnt.data() + (size_t)t * nb;
+                        for (int64_t i = nf * t / nt; i < nf * (t + 1) / nt; ++i)
+                          ++h[bucket(keys[i])];
+                      });
+    for (auto& t : th)
+      t.join();
+  }
+  // cnt[t][b] becomes thread t's first slot in bucket b.
+  for (int64_t b = 0, s = 0; b < nb; ++b)
+  {
+    bstart[b] = s;
+    for (int t = 0; t < nt; ++t)
+    {
+      const int64_t c = cnt[(size_t)t * nb + b];
+      cnt[(size_t)t * nb + b] = s;
+      s += c;
+    }
+  }
+  bstart[nb] = nf;
+  std::unique_ptr<Key[]> sorted(new Key[nf]);
+  {
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; ++t)
+      th.emplace_back([&, t]
+                      {
+                        int64_t* h = cnt.data() + (size_t)t * nb;
+                        for (int64_t i = nf * t / nt; i < nf * (t + 1) / nt; ++i)
+                          sorted[h[bucket(keys[i])]++] = keys[i];
+                      });
+    for (auto& t : th)
+      t.join();
+  }
+  {
+    std::atomic<int64_t> next{0};
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; ++t)
+      th.emplace_back([&]
+                      {
+                        for (int64_t b; (b = next.fetch_add(64)) < nb;)
+                          for (int64_t e = std::min(b + 64, nb); b < e; ++b)
+                            std::sort(sorted.get() + bstart[b], sorted.get() + bstart[b + 1]);
+                      });
+    for (auto& t : th)
+      t.join();
+  }
+  keys.reset();
+  stage.emplace("Compute local part of mesh dual graph: adjacency");
   auto same = [&](int64_t a, int64_t b)
   {
     if (pack)
-      return keys[a].first == keys[b].first;
-    return keys[a].first == keys[b].first && (keys[a].second >> 32) == (keys[b].second >> 32);
+      return sorted[a].first == sorted[b].first;
+    return sorted[a].first == sorted[b].first &&
+           (sorted[a].second >> 32) == (sorted[b].second >> 32);
   };
-  auto index = [&](int64_t a) -> int64_t
-  { return pack ? (int64_t)keys[a].second : (int64_t)(keys[a].second & 0xffffffffu); };
-  std::vector<std::pair<int32_t, int32_t>> edges;
-  edges.reserve(2 * nc);
-  for (int64_t i = 0; i < nf;)
+  auto cell_at = [&](int64_t p) -> int32_t
   {
-    int64_t j = i + 1;
-    while (j < nf && same(i, j))
-      ++j;
-    for (int64_t a = i; a < j; ++a)
-      for (int64_t b = a + 1; b < j; ++b)
-        edges.push_back({(int32_t)(index(a) / 4), (int32_t)(index(b) / 4)});
-    i = j;
-  }
+    const uint64_t lo = sorted[p].second;
+    return (int32_t)((pack ? lo : (lo & 0xffffffffu)) / 4);
+  };
+  // Sorted position of every facet; the run around a position.
+  std::unique_ptr<int32_t[]> pos(new int32_t[nf]);
+  parallel_for(nf,
+               [&](int64_t a, int64_t b)
+               {
+                 for (int64_t p = a; p < b; ++p)
+                 {
+                   const uint64_t lo = sorted[p].second;
+                   pos[(int64_t)(pack ? lo : (lo & 0xffffffffu))] = (int32_t)p;
+                 }
+               });
+  auto run = [&](int64_t p, int64_t& lo, int64_t& hi)
+  {
+    lo = p;
+    while (lo > 0 && same(lo - 1, p))
+      --lo;
+    hi = p + 1;
+    while (hi < nf && same(hi, p))
+      ++hi;
+  };
+  auto cell_facets = [&](int64_t c, int32_t* q)
+  {
+    for (int f = 0; f < 4; ++f)
+      q[f] = pos[4 * c + f];
+    std::sort(q, q + 4);
+  };
   off.assign(nc + 1, 0);
-  for (auto& e : edges)
-  {
-    ++off[e.first + 1];
-    ++off[e.second + 1];
-  }
+  parallel_for(nc,
+               [&](int64_t a, int64_t b)
+               {
+                 for (int64_t c = a; c < b; ++c)
+                 {
+                   int64_t d = 0, lo, hi;
+                   for (int f = 0; f < 4; ++f)
+                   {
+                     run(pos[4 * c + f], lo, hi);
+                     d += hi - lo - 1;
+                   }
+                   off[c + 1] = (int32_t)d;
+                 }
+               });
   for (int64_t c = 0; c < nc; ++c)
     off[c + 1] += off[c];
   adj.resize(off[nc]);
-  std::vector<int32_t> pos(off.begin(), off.end() - 1);
-  for (auto& e : edges)
-  {
-    adj[pos[e.first]++] = e.second;
-    adj[pos[e.second]++] = e.first;
-  }
+  parallel_for(nc,
+               [&](int64_t a, int64_t b)
+               {
+                 for (int64_t c = a; c < b; ++c)
+                 {
+                   int32_t q[4];
+                   cell_facets(c, q);
+                   int64_t w = off[c], lo, hi;
+                   for (int f = 0; f < 4; ++f)
+                   {
+                     run(q[f], lo, hi);
+                     for (int64_t p = lo; p < hi; ++p)
+                       if (p != q[f])
+                         adj[w++] = cell_at(p);
+                   }
+                 }
+               });
 }
 
 // Rooted level structure; returns the number of levels, fills `ls` with
