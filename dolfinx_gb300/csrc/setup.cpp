@@ -44,6 +44,15 @@ int num_threads()
   return n == 0 ? 1 : (int)std::min(n, 64u);
 }
 
+void atomic_min(int64_t& a, int64_t v)
+{
+  std::atomic_ref<int64_t> r(a);
+  int64_t cur = r.load(std::memory_order_relaxed);
+  while (v < cur && !r.compare_exchange_weak(cur, v, std::memory_order_relaxed))
+  {
+  }
+}
+
 template <typename F>
 void parallel_for(int64_t n, F&& f)
 {
@@ -61,6 +70,66 @@ void parallel_for(int64_t n, F&& f)
   }
   for (auto& t : th)
     t.join();
+}
+
+// Uninitialised array filled with `v` on threads.
+template <typename T>
+std::unique_ptr<T[]> filled(int64_t n, T v)
+{
+  std::unique_ptr<T[]> a(new T[std::max<int64_t>(n, 1)]);
+  parallel_for(n, [&](int64_t i0, int64_t i1) { std::fill(a.get() + i0, a.get() + i1, v); });
+  return a;
+}
+
+// Numbers ids 0..nid-1 by their first position in id[0..np): the first id
+// seen gets 0, the next new one 1, and so on; ids that never appear get
+// -1. Returns the count. On threads: first positions by atomic minimum,
+// then a count of first positions before each one.
+int64_t number_by_first_appearance(int64_t np, const int32_t* id, int64_t nid, int32_t* number)
+{
+  std::unique_ptr<int64_t[]> first = filled<int64_t>(nid, INT64_MAX);
+  parallel_for(np, [&](int64_t a, int64_t b)
+               {
+                 for (int64_t p = a; p < b; ++p)
+                   atomic_min(first[id[p]], p);
+               });
+  std::unique_ptr<int8_t[]> mark = filled<int8_t>(np, 0);
+  parallel_for(nid, [&](int64_t a, int64_t b)
+               {
+                 for (int64_t v = a; v < b; ++v)
+                 {
+                   number[v] = -1;
+                   if (first[v] != INT64_MAX)
+                     mark[first[v]] = 1;
+                 }
+               });
+  const int nt = (int)std::min<int64_t>(num_threads(), std::max<int64_t>(1, np / 4096));
+  std::vector<int64_t> part(nt + 1, 0);
+  auto chunks = [&](auto&& f)
+  {
+    std::vector<std::thread> th;
+    for (int t = 0; t < nt; ++t)
+      th.emplace_back([&f, t, np, nt] { f(t, np * t / nt, np * (t + 1) / nt); });
+    for (auto& t : th)
+      t.join();
+  };
+  chunks([&](int t, int64_t a, int64_t b)
+         {
+           int64_t c = 0;
+           for (int64_t p = a; p < b; ++p)
+             c += mark[p];
+           part[t + 1] = c;
+         });
+  for (int t = 0; t < nt; ++t)
+    part[t + 1] += part[t];
+  chunks([&](int t, int64_t a, int64_t b)
+         {
+           int64_t c = part[t];
+           for (int64_t p = a; p < b; ++p)
+             if (mark[p])
+               number[id[p]] = (int32_t)c++;
+         });
+  return part[nt];
 }
 
 // Sort of a vector whose elements are all distinct under operator<: chunks
@@ -287,30 +356,147 @@ void dual_graph(int64_t nc, const int64_t* cells, int64_t nverts, std::vector<in
                });
 }
 
-// Rooted level structure; returns the number of levels, fills `ls` with
-// the nodes in level order and `lend` with level end offsets.
-int levels(const std::vector<int32_t>& off, const std::vector<int32_t>& adj, int s,
-           std::vector<int8_t>& mark, std::vector<int>& ls, std::vector<int>& lend)
+// A reusable barrier for a team of host threads: arrivals count up, the
+// last one starts the next generation; waiters spin briefly, then yield.
+class SpinBarrier
 {
-  std::fill(mark.begin(), mark.end(), 0);
-  ls.clear();
-  lend.clear();
-  ls.push_back(s);
-  mark[s] = 1;
-  size_t begin = 0;
-  while (begin < ls.size())
+public:
+  explicit SpinBarrier(int n) : n_(n) {}
+  void wait()
   {
-    const size_t end = ls.size();
-    lend.push_back((int)end);
-    for (size_t i = begin; i < end; ++i)
-      for (int k = off[ls[i]]; k < off[ls[i] + 1]; ++k)
-        if (!mark[adj[k]])
-        {
-          mark[adj[k]] = 1;
-          ls.push_back(adj[k]);
-        }
-    begin = end;
+    const int gen = gen_.load(std::memory_order_acquire);
+    if (count_.fetch_add(1, std::memory_order_acq_rel) + 1 == n_)
+    {
+      count_.store(0, std::memory_order_relaxed);
+      gen_.fetch_add(1, std::memory_order_release);
+      return;
+    }
+    for (int spin = 0; gen_.load(std::memory_order_acquire) == gen; ++spin)
+      if (spin > 256)
+        std::this_thread::yield();
   }
+
+private:
+  const int n_;
+  std::atomic<int> count_{0};
+  std::atomic<int> gen_{0};
+};
+
+// Breadth-first search from s over the nodes whose mark is 0, in the order
+// the serial queue gives: each level lists, for the nodes of the previous
+// level in order, their unmarked neighbours in adjacency order, a node
+// listed by the first that reaches it. With `sort_children`, each node's
+// new neighbours are sorted by degree with std::ranges::sort before they
+// are listed (the RCM queue of graph/ordering.cpp:148-170). `order`
+// receives the nodes level by level, `lend` the end of each level (as the
+// level structure of graph/ordering.cpp:22-57), and the nodes are marked.
+//
+// Large graphs run level by level on a team of threads, three barriers a
+// level: a node's owner is the least (position in the level, position in
+// the adjacency list) that reaches it (an atomic minimum); each thread
+// collects its part of the level's children in order, sorted per parent;
+// the parts are placed one after another. The owners and the inputs to
+// each sort are those of the serial queue, so the order is the same.
+int bfs(const std::vector<int32_t>& off, const std::vector<int32_t>& adj, int s,
+        bool sort_children, std::vector<int8_t>& mark, std::vector<int64_t>& owner,
+        std::vector<int>& order, std::vector<int>& lend)
+{
+  auto cmp = [&](int a, int b) { return off[a + 1] - off[a] < off[b + 1] - off[b]; };
+  const int64_t n = (int64_t)off.size() - 1;
+  const int nt = (int)std::min<int64_t>(num_threads(), std::max<int64_t>(1, n / 16384));
+  lend.clear();
+  if (nt <= 1)
+  {
+    order.clear();
+    order.push_back(s);
+    mark[s] = 1;
+    size_t begin = 0;
+    while (begin < order.size())
+    {
+      const size_t end = order.size();
+      lend.push_back((int)end);
+      for (size_t i = begin; i < end; ++i)
+      {
+        const size_t first = order.size();
+        for (int k = off[order[i]]; k < off[order[i] + 1]; ++k)
+          if (!mark[adj[k]])
+          {
+            mark[adj[k]] = 1;
+            order.push_back(adj[k]);
+          }
+        if (sort_children)
+          std::ranges::sort(order.begin() + first, order.end(), cmp);
+      }
+      begin = end;
+    }
+    return (int)lend.size();
+  }
+  order.resize(n);
+  order[0] = s;
+  mark[s] = 1;
+  std::vector<int64_t> part(nt, 0);
+  SpinBarrier sync(nt);
+  auto key = [](int64_t i, int64_t j) { return (i << 32) | j; };
+  int64_t end = 1;
+  auto team = [&](int t)
+  {
+    std::vector<int> kids;
+    for (int64_t fb = 0, fe = 1; fb < fe;)
+    {
+      const int64_t a = fb + (fe - fb) * t / nt, b = fb + (fe - fb) * (t + 1) / nt;
+      // (1) claim: each unmarked neighbour keeps its least (i, j).
+      for (int64_t i = a; i < b; ++i)
+      {
+        const int u = order[i];
+        for (int j = off[u]; j < off[u + 1]; ++j)
+          if (!mark[adj[j]])
+            atomic_min(owner[adj[j]], key(i - fb, j - off[u]));
+      }
+      sync.wait();
+      // (2) this thread's children, in order, sorted per parent.
+      kids.clear();
+      for (int64_t i = a; i < b; ++i)
+      {
+        const int u = order[i];
+        const size_t first = kids.size();
+        for (int j = off[u]; j < off[u + 1]; ++j)
+          if (owner[adj[j]] == key(i - fb, j - off[u]))
+            kids.push_back(adj[j]);
+        if (sort_children)
+          std::ranges::sort(kids.begin() + first, kids.end(), cmp);
+      }
+      part[t] = (int64_t)kids.size();
+      sync.wait();
+      // (3) place them after the level, mark them, clear their owners.
+      int64_t w = fe, total = 0;
+      for (int q = 0; q < nt; ++q)
+      {
+        w += q < t ? part[q] : 0;
+        total += part[q];
+      }
+      for (int k : kids)
+      {
+        order[w++] = k;
+        mark[k] = 1;
+        owner[k] = INT64_MAX;
+      }
+      if (t == 0)
+      {
+        lend.push_back((int)fe);
+        end = fe + total;
+      }
+      fb = fe;
+      fe += total;
+      sync.wait();
+    }
+  };
+  std::vector<std::thread> th;
+  for (int t = 1; t < nt; ++t)
+    th.emplace_back(team, t);
+  team(0);
+  for (auto& t : th)
+    t.join();
+  order.resize(end);
   return (int)lend.size();
 }
 
@@ -325,7 +511,14 @@ void rcm(const std::vector<int32_t>& off, const std::vector<int32_t>& adj,
   auto deg = [&](int a) { return off[a + 1] - off[a]; };
   auto cmp = [&](int a, int b) { return deg(a) < deg(b); };
   std::vector<int8_t> mark(n);
-  std::vector<int> ls, lend, ls2, lend2, rv, nbr;
+  std::vector<int64_t> owner(n, INT64_MAX);
+  std::vector<int> ls, lend, ls2, lend2, rv, rvend;
+  auto levels = [&](int s, std::vector<int>& order, std::vector<int>& ends)
+  {
+    dfx::ScopedTimer timer("Graph: create_level_structure");
+    std::fill(mark.begin(), mark.end(), 0);
+    return bfs(off, adj, s, false, mark, owner, order, ends);
+  };
   int count = 0;
   while (count < n)
   {
@@ -336,13 +529,13 @@ void rcm(const std::vector<int32_t>& off, const std::vector<int32_t>& adj,
         v = i;
         dmin = deg(i);
       }
-    int nl = levels(off, adj, v, mark, ls, lend);
+    int nl = levels(v, ls, lend);
     for (;;)
     {
       const int b = nl > 1 ? lend[nl - 2] : 0;
       const int s = *std::ranges::min_element(
           std::ranges::subrange(ls.begin() + b, ls.begin() + lend[nl - 1]), cmp);
-      const int nl2 = levels(off, adj, s, mark, ls2, lend2);
+      const int nl2 = levels(s, ls2, lend2);
       if (nl2 > nl)
       {
         v = s;
@@ -354,21 +547,7 @@ void rcm(const std::vector<int32_t>& off, const std::vector<int32_t>& adj,
         break;
     }
     std::fill(mark.begin(), mark.end(), 0);
-    rv.clear();
-    rv.push_back(v);
-    mark[v] = 1;
-    for (size_t cur = 0; cur < rv.size(); ++cur)
-    {
-      nbr.clear();
-      for (int k = off[rv[cur]]; k < off[rv[cur] + 1]; ++k)
-        if (!mark[adj[k]])
-        {
-          nbr.push_back(adj[k]);
-          mark[adj[k]] = 1;
-        }
-      std::ranges::sort(nbr, cmp);
-      rv.insert(rv.end(), nbr.begin(), nbr.end());
-    }
+    bfs(off, adj, v, true, mark, owner, rv, rvend);
     for (auto it = rv.rbegin(); it != rv.rend(); ++it)
       r[*it] = count++;
   }
@@ -433,79 +612,77 @@ extern "C" int dfx_mesh_create_box_tet(int32_t nx, int32_t ny, int32_t nz, const
   // Lexicographic vertices (generation.h:332-377) and the 6-tet split of
   // each hexahedron sharing the v0-v7 diagonal (generation.h:404-420).
   const double ext[3] = {(p1[0] - p0[0]) / nx, (p1[1] - p0[1]) / ny, (p1[2] - p0[2]) / nz};
-  std::vector<int64_t> cells(4 * nc);
-  for (int64_t i = 0; i < nhex; ++i)
-  {
-    const int64_t iz = i / ((int64_t)nx * ny), j = i % ((int64_t)nx * ny);
-    const int64_t iy = j / nx, ix = j % nx;
-    const int64_t v0 = iz * sqxy + iy * (nx + 1) + ix, v1 = v0 + 1;
-    const int64_t v2 = v0 + (nx + 1), v3 = v1 + (nx + 1);
-    const int64_t v4 = v0 + sqxy, v5 = v1 + sqxy, v6 = v2 + sqxy, v7 = v3 + sqxy;
-    const int64_t t[24] = {v0, v1, v3, v7, v0, v1, v7, v5, v0, v5, v7, v4,
-                           v0, v3, v2, v7, v0, v6, v4, v7, v0, v2, v6, v7};
-    std::memcpy(&cells[24 * i], t, sizeof(t));
-  }
+  std::unique_ptr<int64_t[]> cells(new int64_t[4 * nc]);
+  parallel_for(nhex, [&](int64_t i0, int64_t i1)
+               {
+                 for (int64_t i = i0; i < i1; ++i)
+                 {
+                   const int64_t iz = i / ((int64_t)nx * ny), j = i % ((int64_t)nx * ny);
+                   const int64_t iy = j / nx, ix = j % nx;
+                   const int64_t v0 = iz * sqxy + iy * (nx + 1) + ix, v1 = v0 + 1;
+                   const int64_t v2 = v0 + (nx + 1), v3 = v1 + (nx + 1);
+                   const int64_t v4 = v0 + sqxy, v5 = v1 + sqxy, v6 = v2 + sqxy,
+                                 v7 = v3 + sqxy;
+                   const int64_t t[24] = {v0, v1, v3, v7, v0, v1, v7, v5, v0, v5, v7, v4,
+                                          v0, v3, v2, v7, v0, v6, v4, v7, v0, v2, v6, v7};
+                   std::memcpy(&cells[24 * i], t, sizeof(t));
+                 }
+               });
   std::vector<int32_t> perm; // new -> old cell
   if (reorder)
   {
     std::vector<int32_t> off, adj, r;
     {
       dfx::ScopedTimer t("Compute local part of mesh dual graph");
-      dual_graph(nc, cells.data(), nv, off, adj);
+      dual_graph(nc, cells.get(), nv, off, adj);
     }
     {
       dfx::ScopedTimer t("Reverse Cuthill-McKee ordering");
       rcm(off, adj, r);
     }
     perm.resize(nc);
-    for (int64_t c = 0; c < nc; ++c)
-      perm[r[c]] = (int32_t)c;
+    parallel_for(nc, [&](int64_t a, int64_t b)
+                 {
+                   for (int64_t c = a; c < b; ++c)
+                     perm[r[c]] = (int32_t)c;
+                 });
   }
   // Geometry nodes numbered by first appearance over the (reordered)
-  // cells (fem/dofmapbuilder.cpp:440-474, no graph reordering).
-  std::vector<int32_t> node(nv, -1);
-  int32_t cnt = 0;
-  for (int64_t c = 0; c < nc; ++c)
-  {
-    const int64_t co = reorder ? perm[c] : c;
-    for (int k = 0; k < 4; ++k)
-    {
-      const int64_t v = cells[4 * co + k];
-      if (node[v] < 0)
-        node[v] = cnt++;
-      cells_out[4 * c + k] = node[v];
-    }
-  }
-  for (int64_t v = 0; v < nv; ++v)
-  {
-    const int64_t p = v % sqxy;
-    const int64_t idx[3] = {p % (nx + 1), p / (nx + 1), v / sqxy};
-    for (int i = 0; i < 3; ++i)
-      x_out[3 * (int64_t)node[v] + i] = p0[i] + (double)idx[i] * ext[i];
-  }
+  // cells (fem/dofmapbuilder.cpp:440-474, no graph reordering): the
+  // reordered cells' vertex ids go to cells_out, are numbered, and are
+  // replaced by their numbers.
+  parallel_for(nc, [&](int64_t a, int64_t b)
+               {
+                 for (int64_t c = a; c < b; ++c)
+                 {
+                   const int64_t co = reorder ? perm[c] : c;
+                   for (int k = 0; k < 4; ++k)
+                     cells_out[4 * c + k] = (int32_t)cells[4 * co + k];
+                 }
+               });
+  cells.reset();
+  std::unique_ptr<int32_t[]> node(new int32_t[nv]);
+  number_by_first_appearance(4 * nc, cells_out, nv, node.get());
+  parallel_for(4 * nc, [&](int64_t a, int64_t b)
+               {
+                 for (int64_t p = a; p < b; ++p)
+                   cells_out[p] = node[cells_out[p]];
+               });
+  parallel_for(nv, [&](int64_t a, int64_t b)
+               {
+                 for (int64_t v = a; v < b; ++v)
+                 {
+                   const int64_t p = v % sqxy;
+                   const int64_t idx[3] = {p % (nx + 1), p / (nx + 1), v / sqxy};
+                   for (int i = 0; i < 3; ++i)
+                     x_out[3 * (int64_t)node[v] + i] = p0[i] + (double)idx[i] * ext[i];
+                 }
+               });
   return DFX_OK;
 }
 
 namespace
 {
-void atomic_min(int64_t& a, int64_t v)
-{
-  std::atomic_ref<int64_t> r(a);
-  int64_t cur = r.load(std::memory_order_relaxed);
-  while (v < cur && !r.compare_exchange_weak(cur, v, std::memory_order_relaxed))
-  {
-  }
-}
-
-// Uninitialised array filled with `v` on threads.
-template <typename T>
-std::unique_ptr<T[]> filled(int64_t n, T v)
-{
-  std::unique_ptr<T[]> a(new T[std::max<int64_t>(n, 1)]);
-  parallel_for(n, [&](int64_t i0, int64_t i1) { std::fill(a.get() + i0, a.get() + i1, v); });
-  return a;
-}
-
 // Concurrent open-addressing table from edge keys (sorted vertex pair) to
 // the first position p = c*nd + local index at which the edge appears.
 // Slots are claimed with compare-and-swap; the position is a running

@@ -90,6 +90,8 @@ def test_host_setup_registers_reference_task_names(common):
     V = fem.functionspace(m, ("Lagrange", 2), device="cpu")
     V.sparsity()
     got = {k: n for k, (n, t) in common.timings().items()}
+    # the pseudo-peripheral root search runs two or more level structures
+    assert got.pop("Graph: create_level_structure") >= 2
     dual = "Compute local part of mesh dual graph"
     stages = {f"{dual}: {s}": 1 for s in ("keys", "sort", "adjacency")}
     assert got == {"Build BoxMesh (tetrahedra)": 1, dual: 1, **stages,
