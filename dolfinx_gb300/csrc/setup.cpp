@@ -690,24 +690,27 @@ namespace
 struct EdgeFirst
 {
   static constexpr uint64_t kEmpty = ~uint64_t(0);
+  struct Slot
+  {
+    uint64_t key;  // kEmpty when free
+    int64_t first; // first position; later the edge's dof number
+  };
   uint64_t cap, mask;
-  std::unique_ptr<uint64_t[]> key;
-  std::unique_ptr<int64_t[]> first;
+  std::unique_ptr<Slot[]> s; // key and position share a cache line
   explicit EdgeFirst(int64_t n)
   {
     cap = 16;
     while (cap < (uint64_t)(2 * n))
       cap <<= 1;
     mask = cap - 1;
-    key = filled<uint64_t>((int64_t)cap, kEmpty);
-    first = filled<int64_t>((int64_t)cap, INT64_MAX);
+    s = filled<Slot>((int64_t)cap, Slot{kEmpty, INT64_MAX});
   }
   uint64_t slot(uint64_t k)
   {
     for (uint64_t h = (k * 0x9E3779B97F4A7C15ull) >> 17;; ++h)
     {
       const uint64_t i = h & mask;
-      std::atomic_ref<uint64_t> r(key[i]);
+      std::atomic_ref<uint64_t> r(s[i].key);
       uint64_t cur = r.load(std::memory_order_acquire);
       if (cur == k)
         return i;
@@ -764,7 +767,12 @@ extern "C" int dfx_dofmap_create_tet(int32_t num_cells, const int32_t* cells, in
                      atomic_min(vfirst[cells[4 * c + i]], nd * c + i);
                    if (degree == 2)
                      for (int e = 0; e < 6; ++e)
-                       atomic_min(edges.first[edges.slot(edge_key(c, e))], nd * c + 4 + e);
+                     {
+                       // the edge's slot waits in its dofmap entry until (4)
+                       const uint64_t k = edges.slot(edge_key(c, e));
+                       dofmap[nd * c + 4 + e] = (int32_t)k;
+                       atomic_min(edges.s[k].first, nd * c + 4 + e);
+                     }
                  }
                });
   // (2) marks at first positions, (3) exclusive prefix counts in place.
@@ -779,8 +787,8 @@ extern "C" int dfx_dofmap_create_tet(int32_t num_cells, const int32_t* cells, in
     parallel_for((int64_t)edges.cap, [&](int64_t a, int64_t b)
                  {
                    for (int64_t i = a; i < b; ++i)
-                     if (edges.key[i] != EdgeFirst::kEmpty)
-                       number[edges.first[i]] = 1;
+                     if (edges.s[i].key != EdgeFirst::kEmpty)
+                       number[edges.s[i].first] = 1;
                  });
   const int nt = num_threads();
   std::vector<int64_t> part(nt + 1, 0);
@@ -818,16 +826,32 @@ extern "C" int dfx_dofmap_create_tet(int32_t num_cells, const int32_t* cells, in
       t.join();
   }
   reorder.reset();
-  // (4) each position takes the number of its entity's first position.
+  // (4) each entity takes the number of its first position, then every
+  // position takes its entity's number.
+  parallel_for(vmax + 1, [&](int64_t a, int64_t b)
+               {
+                 for (int64_t v = a; v < b; ++v)
+                   if (vfirst[v] != INT64_MAX)
+                     vfirst[v] = number[vfirst[v]];
+               });
+  if (degree == 2)
+    parallel_for((int64_t)edges.cap, [&](int64_t a, int64_t b)
+                 {
+                   for (int64_t i = a; i < b; ++i)
+                     if (edges.s[i].key != EdgeFirst::kEmpty)
+                       edges.s[i].first = number[edges.s[i].first];
+                 });
+  number.reset();
   parallel_for(nc, [&](int64_t c0, int64_t c1)
                {
                  for (int64_t c = c0; c < c1; ++c)
                  {
                    for (int i = 0; i < 4; ++i)
-                     dofmap[nd * c + i] = number[vfirst[cells[4 * c + i]]];
+                     dofmap[nd * c + i] = (int32_t)vfirst[cells[4 * c + i]];
                    if (degree == 2)
                      for (int e = 0; e < 6; ++e)
-                       dofmap[nd * c + 4 + e] = number[edges.first[edges.slot(edge_key(c, e))]];
+                       dofmap[nd * c + 4 + e] =
+                           (int32_t)edges.s[(uint32_t)dofmap[nd * c + 4 + e]].first;
                  }
                });
   *num_nodes = (int32_t)part[nt];
