@@ -132,59 +132,15 @@ int64_t number_by_first_appearance(int64_t np, const int32_t* id, int64_t nid, i
   return part[nt];
 }
 
-// Sort of a vector whose elements are all distinct under operator<: chunks
-// sorted on threads, then merged pairwise in rounds. With no equal elements
-// the result is the one order std::sort gives.
-template <typename T>
-void sort_distinct(std::vector<T>& v)
+// The facets of a tetrahedral mesh sorted by (key, facet index), the key
+// being the sorted vertex triple (three 21-bit fields when every vertex
+// index fits, else two words): equal facets are adjacent, in facet-index
+// order. Built on threads: keys, then a bucket sort on the smallest vertex
+// (buckets are increasing in the key, so sorting each bucket sorts all).
+struct SortedFacets
 {
-  const int64_t n = (int64_t)v.size();
-  const int nt = (int)std::min<int64_t>(num_threads(), std::max<int64_t>(1, n / 65536));
-  if (nt <= 1)
-  {
-    std::sort(v.begin(), v.end());
-    return;
-  }
-  std::vector<int64_t> b(nt + 1);
-  for (int t = 0; t <= nt; ++t)
-    b[t] = n * t / nt;
-  {
-    std::vector<std::thread> th;
-    for (int t = 0; t < nt; ++t)
-      th.emplace_back([&v, &b, t] { std::sort(v.begin() + b[t], v.begin() + b[t + 1]); });
-    for (auto& t : th)
-      t.join();
-  }
-  std::vector<T> tmp(n);
-  for (int w = 1; w < nt; w *= 2)
-  {
-    std::vector<std::thread> th;
-    for (int t = 0; t < nt; t += 2 * w)
-    {
-      const int64_t lo = b[t], mid = b[std::min(t + w, nt)], hi = b[std::min(t + 2 * w, nt)];
-      th.emplace_back([&v, &tmp, lo, mid, hi]
-                      { std::merge(v.begin() + lo, v.begin() + mid, v.begin() + mid,
-                                   v.begin() + hi, tmp.begin() + lo); });
-    }
-    for (auto& t : th)
-      t.join();
-    v.swap(tmp);
-  }
-}
-
-// Facet-connected dual graph in the order of build_local_dual_graph
-// (mesh/graphbuild.cpp:566-905, serial path). The reference sorts the facets
-// by their sorted vertex triple (stably), turns each run of equal facets into
-// the edges between its cells (pairs a < b in run order) and fills the
-// adjacency in edge order. So a cell's neighbours are, for each of its facets
-// in sorted order, the other cells of that facet's run in run order. Here:
-// the facet keys are sorted by a parallel bucket sort on the smallest vertex,
-// and each cell's list is filled from the runs on threads.
-void dual_graph(int64_t nc, const int64_t* cells, int64_t nverts, std::vector<int32_t>& off,
-                std::vector<int32_t>& adj)
-{
-  // (key hi, key lo | index), left uninitialised on allocation so that the
-  // threads that fill it touch its pages first.
+  // (key hi, key lo | facet index), left uninitialised on allocation so
+  // that the threads that fill it touch its pages first.
   struct Key
   {
     uint64_t first, second;
@@ -193,11 +149,28 @@ void dual_graph(int64_t nc, const int64_t* cells, int64_t nverts, std::vector<in
       return first < o.first || (first == o.first && second < o.second);
     }
   };
+  std::unique_ptr<Key[]> key;
+  int64_t n = 0;
+  bool pack = true;
+  bool same(int64_t a, int64_t b) const
+  {
+    if (pack)
+      return key[a].first == key[b].first;
+    return key[a].first == key[b].first && (key[a].second >> 32) == (key[b].second >> 32);
+  }
+  int64_t facet(int64_t p) const
+  {
+    return (int64_t)(pack ? key[p].second : (key[p].second & 0xffffffffu));
+  }
+};
+
+template <typename I>
+SortedFacets sort_facets(int64_t nc, const I* cells, int64_t nverts)
+{
+  using Key = SortedFacets::Key;
   const int64_t nf = 4 * nc;
-  const bool pack = nverts < (int64_t(1) << 21);
-  std::optional<dfx::ScopedTimer> stage(std::in_place,
-                                        "Compute local part of mesh dual graph: keys");
-  std::unique_ptr<Key[]> keys(new Key[nf]);
+  const bool pack = nverts <= (int64_t(1) << 21);
+  std::unique_ptr<Key[]> keys(new Key[std::max<int64_t>(nf, 1)]);
   parallel_for(nc,
                [&](int64_t c0, int64_t c1)
                {
@@ -221,26 +194,28 @@ void dual_graph(int64_t nc, const int64_t* cells, int64_t nverts, std::vector<in
                    }
                });
   // (key, facet index) is a strict order, so any sort gives the stable-sort
-  // permutation of the reference. Buckets by the smallest vertex are
-  // increasing in the key, so sorting each bucket sorts the whole.
-  stage.emplace("Compute local part of mesh dual graph: sort");
+  // permutation by key.
   const int shift = pack ? 42 : 32;
-  const int64_t nb = std::max<int64_t>(1, std::min<int64_t>(nf / 2048, nverts));
-  auto bucket = [&](const Key& k) { return (int64_t)((k.first >> shift) * (uint64_t)nb / (uint64_t)nverts); };
+  const int64_t nv = std::max<int64_t>(nverts, 1);
+  const int64_t nb = std::max<int64_t>(1, std::min<int64_t>(nf / 2048, nv));
+  auto bucket = [&](const Key& k)
+  { return (int64_t)((k.first >> shift) * (uint64_t)nb / (uint64_t)nv); };
   const int nt = (int)std::min<int64_t>(num_threads(), std::max<int64_t>(1, nf / 65536));
   std::vector<int64_t> cnt((size_t)nt * nb, 0), bstart(nb + 1, 0);
+  auto team = [&](auto&& f)
   {
     std::vector<std::thread> th;
     for (int t = 0; t < nt; ++t)
-      th.emplace_back([&, t]
-                      {
-                        int64_t* h = cnt.data() + (size_t)t * nb;
-                        for (int64_t i = nf * t / nt; i < nf * (t + 1) / nt; ++i)
-                          ++h[bucket(keys[i])];
-                      });
+      th.emplace_back([&f, t] { f(t); });
     for (auto& t : th)
       t.join();
-  }
+  };
+  team([&](int t)
+       {
+         int64_t* h = cnt.data() + (size_t)t * nb;
+         for (int64_t i = nf * t / nt; i < nf * (t + 1) / nt; ++i)
+           ++h[bucket(keys[i])];
+       });
   // cnt[t][b] becomes thread t's first slot in bucket b.
   for (int64_t b = 0, s = 0; b < nb; ++b)
   {
@@ -253,71 +228,59 @@ void dual_graph(int64_t nc, const int64_t* cells, int64_t nverts, std::vector<in
     }
   }
   bstart[nb] = nf;
-  std::unique_ptr<Key[]> sorted(new Key[nf]);
-  {
-    std::vector<std::thread> th;
-    for (int t = 0; t < nt; ++t)
-      th.emplace_back([&, t]
-                      {
-                        int64_t* h = cnt.data() + (size_t)t * nb;
-                        for (int64_t i = nf * t / nt; i < nf * (t + 1) / nt; ++i)
-                          sorted[h[bucket(keys[i])]++] = keys[i];
-                      });
-    for (auto& t : th)
-      t.join();
-  }
-  {
-    std::atomic<int64_t> next{0};
-    std::vector<std::thread> th;
-    for (int t = 0; t < nt; ++t)
-      th.emplace_back([&]
-                      {
-                        for (int64_t b; (b = next.fetch_add(64)) < nb;)
-                          for (int64_t e = std::min(b + 64, nb); b < e; ++b)
-                            std::sort(sorted.get() + bstart[b], sorted.get() + bstart[b + 1]);
-                      });
-    for (auto& t : th)
-      t.join();
-  }
+  SortedFacets out;
+  out.key.reset(new Key[std::max<int64_t>(nf, 1)]);
+  out.n = nf;
+  out.pack = pack;
+  team([&](int t)
+       {
+         int64_t* h = cnt.data() + (size_t)t * nb;
+         for (int64_t i = nf * t / nt; i < nf * (t + 1) / nt; ++i)
+           out.key[h[bucket(keys[i])]++] = keys[i];
+       });
   keys.reset();
+  std::atomic<int64_t> next{0};
+  team([&](int)
+       {
+         for (int64_t b; (b = next.fetch_add(64)) < nb;)
+           for (int64_t e = std::min(b + 64, nb); b < e; ++b)
+             std::sort(out.key.get() + bstart[b], out.key.get() + bstart[b + 1]);
+       });
+  return out;
+}
+
+// Facet-connected dual graph in the order of build_local_dual_graph
+// (mesh/graphbuild.cpp:566-905, serial path). The reference sorts the facets
+// by their sorted vertex triple (stably), turns each run of equal facets into
+// the edges between its cells (pairs a < b in run order) and fills the
+// adjacency in edge order. So a cell's neighbours are, for each of its facets
+// in sorted order, the other cells of that facet's run in run order: each
+// cell's list is filled from the runs on threads.
+void dual_graph(int64_t nc, const int64_t* cells, int64_t nverts, std::vector<int32_t>& off,
+                std::vector<int32_t>& adj)
+{
+  const int64_t nf = 4 * nc;
+  std::optional<dfx::ScopedTimer> stage(std::in_place,
+                                        "Compute local part of mesh dual graph: sort");
+  const SortedFacets sf = sort_facets(nc, cells, nverts);
   stage.emplace("Compute local part of mesh dual graph: adjacency");
-  auto same = [&](int64_t a, int64_t b)
-  {
-    if (pack)
-      return sorted[a].first == sorted[b].first;
-    return sorted[a].first == sorted[b].first &&
-           (sorted[a].second >> 32) == (sorted[b].second >> 32);
-  };
-  auto cell_at = [&](int64_t p) -> int32_t
-  {
-    const uint64_t lo = sorted[p].second;
-    return (int32_t)((pack ? lo : (lo & 0xffffffffu)) / 4);
-  };
+  auto cell_at = [&](int64_t p) { return (int32_t)(sf.facet(p) / 4); };
   // Sorted position of every facet; the run around a position.
-  std::unique_ptr<int32_t[]> pos(new int32_t[nf]);
+  std::unique_ptr<int32_t[]> pos(new int32_t[std::max<int64_t>(nf, 1)]);
   parallel_for(nf,
                [&](int64_t a, int64_t b)
                {
                  for (int64_t p = a; p < b; ++p)
-                 {
-                   const uint64_t lo = sorted[p].second;
-                   pos[(int64_t)(pack ? lo : (lo & 0xffffffffu))] = (int32_t)p;
-                 }
+                   pos[sf.facet(p)] = (int32_t)p;
                });
   auto run = [&](int64_t p, int64_t& lo, int64_t& hi)
   {
     lo = p;
-    while (lo > 0 && same(lo - 1, p))
+    while (lo > 0 && sf.same(lo - 1, p))
       --lo;
     hi = p + 1;
-    while (hi < nf && same(hi, p))
+    while (hi < nf && sf.same(hi, p))
       ++hi;
-  };
-  auto cell_facets = [&](int64_t c, int32_t* q)
-  {
-    for (int f = 0; f < 4; ++f)
-      q[f] = pos[4 * c + f];
-    std::sort(q, q + 4);
   };
   off.assign(nc + 1, 0);
   parallel_for(nc,
@@ -343,7 +306,9 @@ void dual_graph(int64_t nc, const int64_t* cells, int64_t nverts, std::vector<in
                  for (int64_t c = a; c < b; ++c)
                  {
                    int32_t q[4];
-                   cell_facets(c, q);
+                   for (int f = 0; f < 4; ++f)
+                     q[f] = pos[4 * c + f];
+                   std::sort(q, q + 4);
                    int64_t w = off[c], lo, hi;
                    for (int f = 0; f < 4; ++f)
                    {
@@ -1050,36 +1015,14 @@ extern "C" int dfx_exterior_facets_tet(int32_t num_cells, const int32_t* cells, 
                        (long long)(i / 4));
     vmax = std::max<int64_t>(vmax, cells[i]);
   }
-  const bool pack = vmax < (int64_t(1) << 21);
-  std::vector<std::pair<uint64_t, uint64_t>> keys(nf);
-  for (int64_t c = 0; c < num_cells; ++c)
-    for (int f = 0; f < 4; ++f)
-    {
-      uint64_t v[3];
-      for (int k = 0; k < 3; ++k)
-        v[k] = (uint64_t)cells[4 * c + kFacets[f][k]];
-      std::sort(v, v + 3);
-      const uint64_t idx = (uint64_t)(4 * c + f);
-      keys[4 * c + f] = pack ? std::make_pair((v[0] << 42) | (v[1] << 21) | v[2], idx)
-                             : std::make_pair((v[0] << 32) | v[1], (v[2] << 32) | idx);
-    }
-  sort_distinct(keys);
-  auto same = [&](int64_t a, int64_t b)
-  {
-    if (pack)
-      return keys[a].first == keys[b].first;
-    return keys[a].first == keys[b].first && (keys[a].second >> 32) == (keys[b].second >> 32);
-  };
-  std::vector<uint8_t> exterior(nf, 0);
-  for (int64_t i = 0; i < nf;)
-  {
-    int64_t j = i + 1;
-    while (j < nf && same(i, j))
-      ++j;
-    if (j - i == 1)
-      exterior[pack ? keys[i].second : (keys[i].second & 0xffffffffu)] = 1;
-    i = j;
-  }
+  const SortedFacets sf = sort_facets(num_cells, cells, vmax + 1);
+  std::unique_ptr<uint8_t[]> exterior = filled<uint8_t>(nf, 0);
+  parallel_for(nf, [&](int64_t a, int64_t b)
+               {
+                 for (int64_t p = a; p < b; ++p)
+                   if (!(p > 0 && sf.same(p - 1, p)) && !(p + 1 < nf && sf.same(p, p + 1)))
+                     exterior[sf.facet(p)] = 1;
+               });
   int32_t n = 0;
   for (int64_t i = 0; i < nf; ++i)
     if (exterior[i])

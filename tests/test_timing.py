@@ -93,7 +93,7 @@ def test_host_setup_registers_reference_task_names(common):
     # the pseudo-peripheral root search runs two or more level structures
     assert got.pop("Graph: create_level_structure") >= 2
     dual = "Compute local part of mesh dual graph"
-    stages = {f"{dual}: {s}": 1 for s in ("keys", "sort", "adjacency")}
+    stages = {f"{dual}: {s}": 1 for s in ("sort", "adjacency")}
     assert got == {"Build BoxMesh (tetrahedra)": 1, dual: 1, **stages,
                    "Reverse Cuthill-McKee ordering": 1, "Dofmap builder: build dofmap data": 1,
                    "Dofmap builder: compute dof reordering map": 1, "Build sparsity": 2}
