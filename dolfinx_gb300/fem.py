@@ -136,6 +136,23 @@ def locate_dofs_geometrical(V: FunctionSpace, marker) -> np.ndarray:
     return np.flatnonzero(marker(X.T)).astype(np.int32)
 
 
+# Local dofs in the closure of local facet f (the triangle opposite vertex
+# f): its three vertices, then (P2) its three edges in Basix edge order.
+_FACET_CLOSURE = np.array([[1, 2, 3, 4, 5, 6], [0, 2, 3, 4, 7, 8], [0, 1, 3, 5, 7, 9],
+                           [0, 1, 2, 6, 8, 9]], np.int32)
+
+
+def locate_dofs_facets(V: FunctionSpace, facets: np.ndarray) -> np.ndarray:
+    """Sorted node (block) indices in the closure of the given (cell, local
+    facet) pairs. With ``V.mesh.exterior_facets()`` these are the boundary
+    dofs that ``locate_dofs_topological(V, 2, exterior_facet_indices(...))``
+    gives (fem/DirichletBC.cpp, mesh/utils.cpp:61-89)."""
+    facets = np.asarray(facets, np.int32).reshape(-1, 2)
+    local = _FACET_CLOSURE[:, : (6 if V.degree == 2 else 3)]
+    dofs = V.dofmap[facets[:, :1], local[facets[:, 1]]]
+    return np.unique(dofs).astype(np.int32)
+
+
 class DirichletBC:
     """Dirichlet condition u = g on the given dof nodes (fem/DirichletBC.h)."""
 

@@ -238,3 +238,20 @@ def test_dof_coordinates_checks_indices(capi):
                                               dm.ctypes.data, 3, 5,
                                               X.ctypes.data) == capi.DFX_ERR_UNSUPPORTED
     assert L.dfx_tabulate_dof_coordinates_tet(0, None, 0, None, None, 2, 0, None) == capi.DFX_OK
+
+
+@pytest.mark.parametrize("deg", [1, 2])
+@pytest.mark.parametrize("n", [(1, 1, 1), (3, 4, 2), (7, 7, 7), (20, 9, 13)])
+def test_facet_closure_dofs_are_the_boundary_dofs(capi, n, deg):
+    """The dofs on the exterior facets of a unit box are exactly the dofs
+    whose point lies on its surface (a coordinate at 0 or 1)."""
+    from dolfinx_gb300 import fem, mesh
+
+    m = mesh.create_unit_cube(*n)
+    V = fem.functionspace(m, ("Lagrange", deg), device="cpu")
+    got = fem.locate_dofs_facets(V, m.exterior_facets())
+    X = V.tabulate_dof_coordinates()
+    ref = np.flatnonzero(np.isclose(X, 0.0).any(1) | np.isclose(X, 1.0).any(1))
+    np.testing.assert_array_equal(got, ref)
+    assert got.dtype == np.int32
+    assert fem.locate_dofs_facets(V, np.zeros((0, 2), np.int32)).size == 0
