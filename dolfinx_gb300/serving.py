@@ -243,7 +243,10 @@ class Server:
                  workers: int = 2, delta: float = 0.01, assembly: str = "atomic"):
         """assembly: "atomic" (FP64 atomics) or "coloured" (deterministic
         summation order, so a request's matrix is bitwise reproducible)."""
-        assert mode in ("mixed", "fp64")
+        if mode not in ("mixed", "fp64"):
+            raise ValueError(f'mode must be "mixed" or "fp64" (got {mode!r})')
+        if assembly not in ("atomic", "coloured", "colored"):
+            raise ValueError(f'assembly must be "atomic" or "coloured" (got {assembly!r})')
         self.assembly = assembly
         self.mode, self.budget, self.capacity = mode, hbm_budget, capacity
         self.quantum, self.batch_max_dofs, self.rtol = quantum, batch_max_dofs, rtol

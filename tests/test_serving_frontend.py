@@ -140,3 +140,11 @@ def test_a_failed_set_up_is_refused_and_returns_its_memory(front, capi):
     rej = srv.admit(serving.Request(1, 7, 1, 0.0, 1))  # its structure cannot be built
     assert rej.status == capi.DFX_ERR_UNSUPPORTED and "structure set-up failed" in rej.error
     assert [j.req.rid for j in srv.finished] == [0, 1]
+
+
+@pytest.mark.parametrize("kw,msg", [({"mode": "fp16"}, "mode"), ({"assembly": "serial"}, "assembly")])
+def test_server_rejects_unknown_modes_before_device_work(capi, kw, msg):
+    from dolfinx_gb300 import serving
+
+    with pytest.raises(ValueError, match=msg):
+        serving.Server(**kw)
