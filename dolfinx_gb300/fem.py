@@ -16,7 +16,7 @@ import numpy as np
 import torch
 
 from . import _capi
-from .la import MatrixCSR, _ptr, _stream
+from .la import MatrixCSR, _check_vec, _ptr, _stream
 from .mesh import Mesh
 
 
@@ -158,7 +158,13 @@ class DirichletBC:
 
     def __init__(self, value, dofs, V: FunctionSpace):
         self.V = V
-        dofs = np.unique(np.asarray(dofs, np.int32))
+        dofs = np.asarray(dofs).ravel()
+        if dofs.size and (dofs.min() < 0 or dofs.max() >= V.num_nodes):
+            # checked here: the device kernels must never see an index
+            # outside the space
+            raise ValueError(f"Dirichlet dofs must lie in [0, {V.num_nodes}) "
+                             f"(got {dofs.min()}..{dofs.max()})")
+        dofs = np.unique(dofs.astype(np.int32))
         bs = V.bs
         # _dofs0 unrolled by block size (fem/DirichletBC.h:357-359).
         self.dofs = (dofs[:, None] * bs + np.arange(bs, dtype=np.int32)[None, :]).ravel()
@@ -175,7 +181,8 @@ class DirichletBC:
                 g[self.dofs] = val[self.dofs % bs]
                 self.g = torch.from_numpy(g).to(dev)
             else:
-                assert val.size == n, "BC value must be a constant or a full dof vector"
+                if val.size != n:
+                    raise ValueError("BC value must be a constant or a full dof vector")
                 self.g = torch.from_numpy(val.copy()).to(dev)
             self.g_const = 0.0
         self.dofs_dev = torch.from_numpy(self.dofs).to(dev)
@@ -190,6 +197,10 @@ class DirichletBC:
         markers[self.dofs_dev.long()] = 1
 
     def set(self, x: torch.Tensor, x0: torch.Tensor | None = None, alpha: float = 1.0) -> None:
+        n, dev = self.V.num_dofs, self.dofs_dev.device
+        _check_vec(x, n, torch.float64, dev, "x")
+        if x0 is not None:
+            _check_vec(x0, n, torch.float64, dev, "x0")
         _capi.check(_capi.lib().dfx_set_bc(_ptr(x), x.numel(), _ptr(self.dofs_dev),
                                            int(self.dofs.size), _ptr(self.g), self.g_const,
                                            _ptr(x0), float(alpha), _stream()))
@@ -243,8 +254,10 @@ class FormSum:
     def __init__(self, terms):
         self.terms = list(terms)
         self.V = self.terms[0].V
-        assert all(t.V is self.V for t in self.terms), "terms on different spaces"
-        assert len({t.rank for t in self.terms}) == 1, "terms of different rank"
+        if not all(t.V is self.V for t in self.terms):
+            raise ValueError("terms on different spaces")
+        if len({t.rank for t in self.terms}) != 1:
+            raise ValueError("terms of different rank")
 
     @property
     def rank(self) -> int:
@@ -272,9 +285,19 @@ def poisson_form(V: FunctionSpace, kappa=1.0, k2: float = 0.0) -> Form:
                 kappa_const=float(kappa) if np.isscalar(kappa) else 1.0, k2=float(k2))
 
 
+def _require_vector_p2(V: FunctionSpace) -> None:
+    if V.bs != 3 or V.degree != 2:
+        raise ValueError("this form needs a vector P2 space (block size 3)")
+
+
+def _require_scalar(V: FunctionSpace) -> None:
+    if V.bs != 1:
+        raise ValueError("facet forms need a scalar space")
+
+
 def elasticity_form(V: FunctionSpace, E=1.0, nu: float = 0.3) -> Form:
     """a(u,v) = int sigma(u):eps(v) dx, E constant or per cell."""
-    assert V.bs == 3 and V.degree == 2
+    _require_vector_p2(V)
     return Form(_capi.FORM_ELASTICITY, V, kappa=_dev(E, V),
                 kappa_const=float(E) if np.isscalar(E) else 1.0, nu=float(nu))
 
@@ -296,7 +319,7 @@ def _facets(V: FunctionSpace, facets):
 def facet_source_form(V: FunctionSpace, g=1.0, facets=None) -> Form:
     """L(v) = int_F g v ds over exterior facets (all boundary facets by
     default); g constant or P1 values on the geometry nodes."""
-    assert V.bs == 1
+    _require_scalar(V)
     return Form(_capi.FORM_SOURCE, V, f=_dev(g, V),
                 f_const=(float(g) if np.isscalar(g) else 0.0, 0.0, 0.0),
                 facets=_facets(V, facets))
@@ -305,14 +328,14 @@ def facet_source_form(V: FunctionSpace, g=1.0, facets=None) -> Form:
 def facet_mass_form(V: FunctionSpace, alpha=1.0, facets=None) -> Form:
     """a(u,v) = int_F alpha u v ds over exterior facets (a Robin term);
     alpha constant or per cell (the cell of each facet)."""
-    assert V.bs == 1
+    _require_scalar(V)
     return Form(_capi.FORM_FACET_MASS, V, kappa=_dev(alpha, V),
                 kappa_const=float(alpha) if np.isscalar(alpha) else 1.0,
                 facets=_facets(V, facets))
 
 
 def body_force_form(V: FunctionSpace, f=(0.0, 0.0, -1.0)) -> Form:
-    assert V.bs == 3 and V.degree == 2
+    _require_vector_p2(V)
     return Form(_capi.FORM_BODYFORCE, V, f_const=tuple(float(v) for v in f))
 
 
@@ -422,6 +445,7 @@ def assemble_vector(L, b: torch.Tensor | None = None, mode: str = "atomic") -> t
     V = L.V
     if b is None:
         b = torch.zeros(V.num_dofs, dtype=torch.float64, device=V.device)
+    _check_vec(b, V.num_dofs, torch.float64, V.dofmap_device().device, "b")
     m = _mode(mode)
     for t in _terms(L):
         cf = t.cstruct()
@@ -453,7 +477,8 @@ def assemble_scalar(M: Functional) -> float:
     """fem::assemble_scalar over the cells (cpp/dolfinx/fem/assembler.h:173-215,
     cpp/dolfinx/fem/assemble_scalar_impl.h:32-61), summed in a fixed order."""
     f = M.form
-    assert f.facets is None, "functionals are cell integrals"
+    if f.facets is not None:
+        raise ValueError("functionals are cell integrals")
     L = _capi.lib()
     nc = f.V.mesh.num_cells
     wb = int(L.dfx_assemble_scalar_workspace_bytes(nc))
@@ -475,6 +500,10 @@ def apply_lifting(b: torch.Tensor, a, bcs, x0=None, alpha: float = 1.0,
         if aj is None or not bcj:
             continue
         V = aj.V
+        dev = V.dofmap_device().device
+        _check_vec(b, V.num_dofs, torch.float64, dev, "b")
+        if x0j is not None:
+            _check_vec(x0j, V.num_dofs, torch.float64, dev, "x0")
         markers = bc_markers(V, bcj)
         g = torch.zeros(V.num_dofs, dtype=torch.float64, device=V.device)
         for bc in bcj:
@@ -516,6 +545,7 @@ class RhsAssembler:
         if b is None:
             b = torch.zeros(V.num_dofs, dtype=torch.float64, device=V.device)
         else:
+            _check_vec(b, V.num_dofs, torch.float64, V.dofmap_device().device, "b")
             b.zero_()
         order, off, ncol = self.colour
         L = _capi.lib()

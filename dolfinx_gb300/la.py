@@ -24,13 +24,31 @@ def _ptr(t):
     return None if t is None else C.c_void_p(t.data_ptr())
 
 
+def _check_vec(t, n: int, dtype, device, name: str) -> None:
+    """A vector that a kernel reads or writes through a raw pointer must be a
+    contiguous CUDA tensor of `dtype` with n entries on `device`: checked on
+    the host, so that a wrong argument raises instead of reaching the GPU."""
+    if not torch.is_tensor(t):
+        raise TypeError(f"{name} must be a torch tensor")
+    if t.device.type != "cuda" or t.device != device:
+        raise ValueError(f"{name} must be on {device} (got {t.device})")
+    if t.dtype != dtype:
+        raise TypeError(f"{name} must be {dtype} (got {t.dtype})")
+    if not t.is_contiguous():
+        raise ValueError(f"{name} must be contiguous")
+    if t.numel() != n:
+        raise ValueError(f"{name} must have {n} entries (got {t.numel()})")
+
+
 class MatrixCSR:
     """CSR matrix with square bs x bs blocks (cpp/dolfinx/la/MatrixCSR.h:67-1017)."""
 
     def __init__(self, row_ptr: torch.Tensor, cols: torch.Tensor, vals: torch.Tensor, bs: int = 1,
                  ncols: int | None = None):
-        assert row_ptr.dtype == torch.int64 and cols.dtype == torch.int32
-        assert vals.dtype in (torch.float64, torch.float32)
+        if row_ptr.dtype != torch.int64 or cols.dtype != torch.int32:
+            raise TypeError("row_ptr must be int64 and cols int32")
+        if vals.dtype not in (torch.float64, torch.float32):
+            raise TypeError("values must be float64 or float32")
         self.row_ptr, self.cols, self.vals, self.bs = row_ptr, cols, vals, int(bs)
         self.nrows = int(row_ptr.numel() - 1)
         self.ncols = self.nrows if ncols is None else int(ncols)
@@ -58,14 +76,21 @@ class MatrixCSR:
     def set_value(self, v: float = 0.0) -> None:
         self.vals.fill_(v)
 
+    def _check_xy(self, x, y) -> None:
+        dev, dt = self.vals.device, self.vals.dtype
+        _check_vec(x, self.ncols * self.bs, dt, dev, "x")
+        _check_vec(y, self.nrows * self.bs, dt, dev, "y")
+
     def mult(self, x: torch.Tensor, y: torch.Tensor) -> None:
         """y += A x (MatrixCSR::mult)."""
+        self._check_xy(x, y)
         _capi.check(_capi.lib().dfx_spmv(C.byref(self.csr()), _ptr(x), _ptr(y), 1.0, _stream()))
 
     def matvec(self, x: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
         """Return A x (overwrites `out`)."""
         if out is None:
             out = torch.empty(self.nrows * self.bs, dtype=x.dtype, device=x.device)
+        self._check_xy(x, out)
         _capi.check(_capi.lib().dfx_spmv(C.byref(self.csr()), _ptr(x), _ptr(out), 0.0, _stream()))
         return out
 
@@ -77,7 +102,8 @@ class MatrixCSR:
 
     def expand_blocks(self, out: "MatrixCSR | None" = None) -> "MatrixCSR":
         """Scalar CSR of a block matrix (out: refresh its values only)."""
-        assert self.vals.dtype == torch.float64
+        if self.vals.dtype != torch.float64:
+            raise TypeError("expand_blocks needs float64 values")
         if out is None:
             dev = self.vals.device
             rp = torch.empty(self.nrows * self.bs + 1, dtype=torch.int64, device=dev)
@@ -128,6 +154,8 @@ class Vector:
 def inner_product(a: torch.Tensor, b: torch.Tensor) -> float:
     """la::inner_product (deterministic two-stage device reduction)."""
     n = a.numel()
+    _check_vec(a, n, torch.float64, a.device, "a")
+    _check_vec(b, n, torch.float64, a.device, "b")
     wb = _capi.lib().dfx_inner_product_workspace_bytes(n)
     work = torch.empty(int(wb) // 8 + 1, dtype=torch.float64, device=a.device)
     out = C.c_double(0.0)
@@ -158,7 +186,8 @@ class CGSolver:
     iterations; workspace allocated once and reused)."""
 
     def __init__(self, A: MatrixCSR, jacobi: bool = True, graph_iters: int = 20):
-        assert A.dtype == torch.float64
+        if A.dtype != torch.float64:
+            raise TypeError("CG needs a float64 matrix")
         self.A = A
         self.n = A.nrows * A.bs
         self.dinv = A.inverse_diagonal() if jacobi else None
@@ -173,6 +202,8 @@ class CGSolver:
 
     def solve(self, b: torch.Tensor, x: torch.Tensor, rtol: float = 1e-10,
               max_iters: int = 100000, raise_on_fail: bool = True) -> CGResult:
+        _check_vec(b, self.n, torch.float64, self.A.vals.device, "b")
+        _check_vec(x, self.n, torch.float64, self.A.vals.device, "x")
         info = _capi.CgInfo()
         rc = _capi.lib().dfx_cg_solve(C.byref(self.A.csr()), _ptr(b), _ptr(x), _ptr(self.dinv),
                                       float(rtol), int(max_iters), int(self.graph_iters),
@@ -198,12 +229,14 @@ class SellOperator:
         if share_of is not None:
             # same structure as share_of, own values (one set per request)
             self.dtype, self.sigma, self.compressed = share_of.dtype, share_of.sigma, share_of.compressed
+            self.n, self.device = share_of.n, share_of.device
             _capi.check(_capi.lib().dfx_operator_share(share_of.handle, C.byref(h)))
             self.source = share_of
             self.handle = h
             if A is not None:
                 self.update_values()
             return
+        self.n, self.device = A.nrows, A.vals.device
         if compress_cols is None:
             compress_cols = dtype == torch.float32
         dt = _capi.F64 if dtype == torch.float64 else _capi.F32
@@ -237,11 +270,15 @@ class SellOperator:
     def apply(self, x: torch.Tensor, y: torch.Tensor | None = None) -> torch.Tensor:
         if y is None:
             y = torch.empty_like(x)
+        _check_vec(x, self.n, self.dtype, self.device, "x")
+        _check_vec(y, self.n, self.dtype, self.device, "y")
         _capi.check(_capi.lib().dfx_operator_apply(self.handle, _ptr(x), _ptr(y), _stream()))
         return y
 
     def apply_renumbered(self, xp: torch.Tensor, yp: torch.Tensor) -> torch.Tensor:
         """The bare SpMV in the operator's numbering."""
+        _check_vec(xp, self.n, self.dtype, self.device, "xp")
+        _check_vec(yp, self.n, self.dtype, self.device, "yp")
         _capi.check(_capi.lib().dfx_operator_apply_renumbered(self.handle, _ptr(xp), _ptr(yp),
                                                               _stream()))
         return yp
@@ -287,6 +324,8 @@ class OperatorCGSolver:
                                                                 _ptr(self.dinv), _stream()))
 
     def solve(self, b, x, rtol=1e-10, max_iters=100000, raise_on_fail=True) -> CGResult:
+        _check_vec(b, self.n, torch.float64, self.op.device, "b")
+        _check_vec(x, self.n, torch.float64, self.op.device, "x")
         info = _capi.CgInfo()
         rc = _capi.lib().dfx_cg_solve_op(self.op.handle, _ptr(b), _ptr(x), _ptr(self.dinv),
                                          float(rtol), int(max_iters), int(self.graph_iters),
@@ -346,6 +385,8 @@ class IRSolver:
 
     def solve(self, b, x, rtol=1e-10, max_outer=200, max_inner=100000,
               raise_on_fail=True) -> IRResult:
+        _check_vec(b, self.n, torch.float64, self.op64.device, "b")
+        _check_vec(x, self.n, torch.float64, self.op64.device, "x")
         info = _capi.IrInfo()
         rc = _capi.lib().dfx_ir_solve(self.op64.handle, self.op32.handle, _ptr(b), _ptr(x),
                                       _ptr(self.dinv), float(rtol), float(self.inner_rtol),

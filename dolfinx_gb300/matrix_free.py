@@ -18,7 +18,7 @@ import numpy as np
 import torch
 
 from . import _capi
-from .la import CGResult, _ptr, _stream
+from .la import CGResult, _check_vec, _ptr, _stream
 
 
 def hex_box_vertices(nx: int, ny: int | None = None, nz: int | None = None,
@@ -97,7 +97,9 @@ class Q4Laplacian:
         ny = nx if ny is None else ny
         nz = nx if nz is None else nz
         v = torch.as_tensor(np.ascontiguousarray(verts, np.float64))
-        assert v.shape == ((nx + 1) * (ny + 1) * (nz + 1), 3)
+        if v.shape != ((nx + 1) * (ny + 1) * (nz + 1), 3):
+            raise ValueError(f"verts must be ({(nx + 1) * (ny + 1) * (nz + 1)}, 3), "
+                             f"got {tuple(v.shape)}")
         self.verts = v.to(device)
         self.dims = (nx, ny, nz)
         self.kappa = float(kappa)
@@ -114,8 +116,11 @@ class Q4Laplacian:
         return self._mesh
 
     def apply(self, u: torch.Tensor, y: torch.Tensor) -> None:
-        dt = {torch.float64: _capi.F64, torch.float32: _capi.F32}[u.dtype]
-        assert y.dtype == u.dtype and u.numel() == self.n and y.numel() == self.n
+        if u.dtype not in (torch.float64, torch.float32):
+            raise TypeError("u must be float64 or float32")
+        _check_vec(u, self.n, u.dtype, self.verts.device, "u")
+        _check_vec(y, self.n, u.dtype, self.verts.device, "y")
+        dt = _capi.F64 if u.dtype == torch.float64 else _capi.F32
         _capi.check(_capi.lib().dfx_q4_action(C.byref(self._mesh), dt, _ptr(u), _ptr(y),
                                               _stream()))
 
@@ -141,7 +146,8 @@ class MatrixFreeCG:
 
     def solve(self, b: torch.Tensor, x: torch.Tensor, rtol: float = 1e-10,
               max_iters: int = 100000, raise_on_fail: bool = True) -> CGResult:
-        assert b.dtype == torch.float64 and x.dtype == torch.float64
+        _check_vec(b, self.op.n, torch.float64, self.op.verts.device, "b")
+        _check_vec(x, self.op.n, torch.float64, self.op.verts.device, "x")
         info = _capi.CgInfo()
         rc = _capi.lib().dfx_q4_cg_solve(C.byref(self.op.mesh()), _ptr(b), _ptr(x), float(rtol),
                                          int(max_iters), int(self.mode), self.delta,
