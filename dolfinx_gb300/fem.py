@@ -272,16 +272,20 @@ def _terms(a):
     return a.terms if isinstance(a, FormSum) else [a]
 
 
-def _dev(v, V):
+def _dev(v, V, n: int, name: str):
+    """A coefficient on the device: None for a constant, else n float64
+    values (per cell or per geometry node; the kernels index all n)."""
     if v is None or np.isscalar(v):
         return None
     t = torch.as_tensor(np.asarray(v, np.float64)) if not torch.is_tensor(v) else v
-    return t.to(device=V.device, dtype=torch.float64).contiguous()
+    if t.numel() != n:
+        raise ValueError(f"{name} must be a constant or {n} values (got {t.numel()})")
+    return t.to(device=V.device, dtype=torch.float64).contiguous().reshape(-1)
 
 
 def poisson_form(V: FunctionSpace, kappa=1.0, k2: float = 0.0) -> Form:
     """a(u,v) = int kappa grad u.grad v + k2 u v dx; kappa constant or per cell."""
-    return Form(_capi.FORM_POISSON, V, kappa=_dev(kappa, V),
+    return Form(_capi.FORM_POISSON, V, kappa=_dev(kappa, V, V.mesh.num_cells, "kappa (per cell)"),
                 kappa_const=float(kappa) if np.isscalar(kappa) else 1.0, k2=float(k2))
 
 
@@ -298,21 +302,27 @@ def _require_scalar(V: FunctionSpace) -> None:
 def elasticity_form(V: FunctionSpace, E=1.0, nu: float = 0.3) -> Form:
     """a(u,v) = int sigma(u):eps(v) dx, E constant or per cell."""
     _require_vector_p2(V)
-    return Form(_capi.FORM_ELASTICITY, V, kappa=_dev(E, V),
+    return Form(_capi.FORM_ELASTICITY, V, kappa=_dev(E, V, V.mesh.num_cells, "E (per cell)"),
                 kappa_const=float(E) if np.isscalar(E) else 1.0, nu=float(nu))
 
 
 def source_form(V: FunctionSpace, f=1.0) -> Form:
     """L(v) = int f v dx, f constant or P1 values on the geometry nodes."""
-    return Form(_capi.FORM_SOURCE, V, f=_dev(f, V),
+    return Form(_capi.FORM_SOURCE, V, f=_dev(f, V, V.mesh.num_nodes, "f (per geometry node)"),
                 f_const=(float(f) if np.isscalar(f) else 0.0, 0.0, 0.0))
 
 
 def _facets(V: FunctionSpace, facets):
     if facets is None:
         facets = V.mesh.exterior_facets()
-    t = torch.as_tensor(np.ascontiguousarray(facets, np.int32)) if not torch.is_tensor(facets) \
-        else facets
+    t = torch.as_tensor(np.asarray(facets)) if not torch.is_tensor(facets) else facets
+    t = t.reshape(-1, 2) if t.numel() else t.reshape(0, 2)
+    if t.numel():
+        # (cell, local facet) pairs index the mesh in the kernels: checked here
+        lo, hi = t.min(0).values.tolist(), t.max(0).values.tolist()
+        if lo[0] < 0 or hi[0] >= V.mesh.num_cells or lo[1] < 0 or hi[1] > 3:
+            raise ValueError(f"facets must be (cell < {V.mesh.num_cells}, local facet < 4) "
+                             "pairs")
     return t.to(device=V.device, dtype=torch.int32).contiguous()
 
 
@@ -320,7 +330,7 @@ def facet_source_form(V: FunctionSpace, g=1.0, facets=None) -> Form:
     """L(v) = int_F g v ds over exterior facets (all boundary facets by
     default); g constant or P1 values on the geometry nodes."""
     _require_scalar(V)
-    return Form(_capi.FORM_SOURCE, V, f=_dev(g, V),
+    return Form(_capi.FORM_SOURCE, V, f=_dev(g, V, V.mesh.num_nodes, "g (per geometry node)"),
                 f_const=(float(g) if np.isscalar(g) else 0.0, 0.0, 0.0),
                 facets=_facets(V, facets))
 
@@ -329,7 +339,7 @@ def facet_mass_form(V: FunctionSpace, alpha=1.0, facets=None) -> Form:
     """a(u,v) = int_F alpha u v ds over exterior facets (a Robin term);
     alpha constant or per cell (the cell of each facet)."""
     _require_scalar(V)
-    return Form(_capi.FORM_FACET_MASS, V, kappa=_dev(alpha, V),
+    return Form(_capi.FORM_FACET_MASS, V, kappa=_dev(alpha, V, V.mesh.num_cells, "alpha (per cell)"),
                 kappa_const=float(alpha) if np.isscalar(alpha) else 1.0,
                 facets=_facets(V, facets))
 
@@ -479,6 +489,7 @@ def assemble_scalar(M: Functional) -> float:
     f = M.form
     if f.facets is not None:
         raise ValueError("functionals are cell integrals")
+    _check_vec(M.u, f.V.num_dofs, torch.float64, f.V.dofmap_device().device, "u")
     L = _capi.lib()
     nc = f.V.mesh.num_cells
     wb = int(L.dfx_assemble_scalar_workspace_bytes(nc))

@@ -87,3 +87,27 @@ def test_forms_check_their_space(capi):
         fem.facet_source_form(V3)
     with pytest.raises(ValueError, match="scalar space"):
         fem.facet_mass_form(V3)
+
+
+def test_coefficients_and_facets_are_sized_for_the_mesh(capi):
+    from dolfinx_gb300 import fem, mesh
+
+    m = mesh.create_unit_cube(2, 2, 2)
+    V = fem.functionspace(m, ("Lagrange", 2), device="cpu")
+    with pytest.raises(ValueError, match=rf"kappa \(per cell\) must be a constant or {m.num_cells}"):
+        fem.poisson_form(V, np.ones(m.num_cells - 1))
+    with pytest.raises(ValueError, match=rf"f \(per geometry node\).* {m.num_nodes} values"):
+        fem.source_form(V, np.ones(V.num_nodes))  # P2 nodes, not geometry nodes
+    with pytest.raises(ValueError, match="alpha"):
+        fem.facet_mass_form(V, np.ones(3))
+    with pytest.raises(ValueError, match="local facet < 4"):
+        fem.facet_source_form(V, 1.0, facets=np.array([[0, 4]]))
+    with pytest.raises(ValueError, match=rf"cell < {m.num_cells}"):
+        fem.facet_mass_form(V, 1.0, facets=np.array([[m.num_cells, 0]]))
+    with pytest.raises(ValueError, match="cell <"):
+        fem.facet_mass_form(V, 1.0, facets=np.array([[-1, 0]]))
+    # well-formed ones build (the space is on the host here)
+    assert fem.poisson_form(V, np.ones(m.num_cells)).kappa.numel() == m.num_cells
+    assert fem.source_form(V, np.ones(m.num_nodes)).f.numel() == m.num_nodes
+    assert fem.facet_source_form(V, 1.0, facets=np.zeros((0, 2), np.int32)).facets.shape == (0, 2)
+    assert fem.facet_mass_form(V, 2.0).facets.shape == (m.exterior_facets().shape[0], 2)
