@@ -401,6 +401,12 @@ class MatrixAssembler:
         self.a, self.bcs, self.diagonal, self.mode = a, list(bcs), float(diagonal), _mode(mode)
         self.terms = _terms(a)
         V = self.terms[0].V
+        if A is not None:
+            if A.nrows != V.num_nodes or A.ncols != V.num_nodes or A.bs != V.bs:
+                raise ValueError(f"A is {A.nrows}x{A.ncols} blocks of {A.bs}; the space needs "
+                                 f"{V.num_nodes}x{V.num_nodes} blocks of {V.bs}")
+            if A.vals.dtype != torch.float64 or A.vals.device.type != "cuda":
+                raise ValueError("A must hold float64 values on a CUDA device")
         self.A = create_matrix(self.terms[0]) if A is None else A
         self.forms = [t.cstruct() for t in self.terms]
         cells = [cs for t, cs in zip(self.terms, self.forms) if t.facets is None]

@@ -49,6 +49,13 @@ class MatrixCSR:
             raise TypeError("row_ptr must be int64 and cols int32")
         if vals.dtype not in (torch.float64, torch.float32):
             raise TypeError("values must be float64 or float32")
+        if not (row_ptr.device == cols.device == vals.device):
+            raise ValueError("row_ptr, cols and values must be on one device")
+        if row_ptr.dim() != 1 or row_ptr.numel() < 1 or cols.dim() != 1:
+            raise ValueError("row_ptr and cols must be 1-D, row_ptr non-empty")
+        if vals.numel() != cols.numel() * int(bs) * int(bs):
+            raise ValueError(f"{cols.numel()} entries of {bs}x{bs} blocks need "
+                             f"{cols.numel() * int(bs) * int(bs)} values (got {vals.numel()})")
         self.row_ptr, self.cols, self.vals, self.bs = row_ptr, cols, vals, int(bs)
         self.nrows = int(row_ptr.numel() - 1)
         self.ncols = self.nrows if ncols is None else int(ncols)

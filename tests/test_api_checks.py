@@ -111,3 +111,22 @@ def test_coefficients_and_facets_are_sized_for_the_mesh(capi):
     assert fem.source_form(V, np.ones(m.num_nodes)).f.numel() == m.num_nodes
     assert fem.facet_source_form(V, 1.0, facets=np.zeros((0, 2), np.int32)).facets.shape == (0, 2)
     assert fem.facet_mass_form(V, 2.0).facets.shape == (m.exterior_facets().shape[0], 2)
+
+
+def test_matrix_shapes_are_checked(capi):
+    from dolfinx_gb300 import fem, la, mesh
+
+    rp = torch.arange(5, dtype=torch.int64)
+    cols = torch.arange(4, dtype=torch.int32)
+    with pytest.raises(ValueError, match="need 36 values"):
+        la.MatrixCSR(rp, cols, torch.zeros(4, dtype=torch.float64), 3)
+    with pytest.raises(ValueError, match="1-D"):
+        la.MatrixCSR(rp.reshape(5, 1), cols, torch.zeros(4, dtype=torch.float64))
+    V = fem.functionspace(mesh.create_unit_cube(2, 2, 2), ("Lagrange", 1), device="cpu")
+    with pytest.raises(ValueError, match=rf"the space needs {V.num_nodes}x{V.num_nodes}"):
+        fem.MatrixAssembler(fem.poisson_form(V), A=_csr(4))
+    n = V.num_nodes
+    A = la.MatrixCSR(torch.arange(n + 1, dtype=torch.int64), torch.arange(n, dtype=torch.int32),
+                     torch.zeros(n, dtype=torch.float64))
+    with pytest.raises(ValueError, match="CUDA device"):
+        fem.MatrixAssembler(fem.poisson_form(V), A=A)
