@@ -24,6 +24,7 @@ import json
 import os
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -164,7 +165,9 @@ class Clocks:
     def __init__(self, index=0):
         self.index = index
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_bench_{os.getpid()}.csv")
+        # raw samples (the JSON line carries their summary); DFX_CLOCKS_DIR keeps them
+        out = os.environ.get("DFX_CLOCKS_DIR") or tempfile.gettempdir()
+        self.path = os.path.join(out, f"clocks_bench_{os.getpid()}.csv")
 
     def __enter__(self):
         try:
