@@ -59,8 +59,8 @@ def test_inner_product(cuda, capi):
 
 
 @pytest.mark.parametrize("deg", [1, 2])
-def test_cg_c1_pipeline(cuda, oracle, capi, deg):
-    """Full c1-style pipeline: assemble, lift, set_bc, Jacobi-CG; solution
+def test_cg_poisson_pipeline(cuda, oracle, capi, deg):
+    """The demo's full Poisson pipeline: assemble, lift, set_bc, Jacobi-CG; solution
     vs the oracle's CG on the oracle's system (rtol 1e-10)."""
     from dolfinx_gb300 import fem, la
 
@@ -186,7 +186,7 @@ def test_sell_operator_f32(cuda, oracle, capi, compress):
     assert_close(y, ref, rtol=2e-6)
 
 
-def _c1_system(oracle, n, deg, seed):
+def _poisson_system(oracle, n, deg, seed):
     from dolfinx_gb300 import fem
 
     m, V, kappa, f, rp, cols = problem(oracle, n, deg, seed=seed)
@@ -202,7 +202,7 @@ def _c1_system(oracle, n, deg, seed):
 def test_operator_cg_matches_csr_cg(cuda, oracle, capi):
     from dolfinx_gb300 import la
 
-    A, b, rp, cols = _c1_system(oracle, (10, 9, 8), 2, 31)
+    A, b, rp, cols = _poisson_system(oracle, (10, 9, 8), 2, 31)
     x1, r1 = la.cg(A, b, rtol=1e-10)
     s = la.OperatorCGSolver(A)
     x2 = torch.zeros_like(b)
@@ -222,7 +222,7 @@ def test_cg_vector_and_scalar_elementwise_paths(cuda, oracle, capi):
     fallback. Both paths meet the stopping test in the oracle's SpMV."""
     from dolfinx_gb300 import la
 
-    A, b, rp, cols = _c1_system(oracle, (10, 9, 8), 2, 31)
+    A, b, rp, cols = _poisson_system(oracle, (10, 9, 8), 2, 31)
     assert A.nrows % 2 == 1
     x1, r1 = la.cg(A, b, rtol=1e-10)
     buf = torch.zeros(A.nrows + 1, dtype=torch.float64, device="cuda")
@@ -246,7 +246,7 @@ def test_iterative_refinement_reaches_fp64(cuda, oracle, capi, variant, inner_rt
     both solves carry."""
     from dolfinx_gb300 import la
 
-    A, b, rp, cols = _c1_system(oracle, (12, 12, 12), 2, 32)
+    A, b, rp, cols = _poisson_system(oracle, (12, 12, 12), 2, 32)
     s64 = la.OperatorCGSolver(A)
     x64 = torch.zeros_like(b)
     s64.solve(b, x64, rtol=1e-12)
