@@ -256,7 +256,8 @@ SortedFacets sort_facets(int64_t nc, const I* cells, int64_t nverts)
 // adjacency in edge order. So a cell's neighbours are, for each of its facets
 // in sorted order, the other cells of that facet's run in run order: each
 // cell's list is filled from the runs on threads.
-void dual_graph(int64_t nc, const int64_t* cells, int64_t nverts, std::vector<int32_t>& off,
+template <typename I>
+void dual_graph(int64_t nc, const I* cells, int64_t nverts, std::vector<int32_t>& off,
                 std::vector<int32_t>& adj)
 {
   const int64_t nf = 4 * nc;
@@ -643,6 +644,25 @@ extern "C" int dfx_mesh_create_box_tet(int32_t nx, int32_t ny, int32_t nz, const
                      x_out[3 * (int64_t)node[v] + i] = p0[i] + (double)idx[i] * ext[i];
                  }
                });
+  return DFX_OK;
+}
+
+extern "C" int dfx_mesh_dual_graph_tet(int32_t num_cells, const int32_t* cells,
+                                       int32_t num_vertices, int32_t* offsets, int32_t* adj)
+{
+  if (num_cells < 0 || num_vertices < 0 || !offsets || (num_cells > 0 && (!cells || !adj)))
+    return dfx::fail(DFX_ERR_INVALID, "invalid dual graph arguments");
+  if ((int64_t)num_cells > INT32_MAX / 4)
+    return dfx::fail(DFX_ERR_INVALID, "mesh too large for int32 facet indices");
+  for (int64_t i = 0; i < 4 * (int64_t)num_cells; ++i)
+    if (cells[i] < 0 || cells[i] >= num_vertices)
+      return dfx::fail(DFX_ERR_INVALID, "cell %lld has a vertex index out of range",
+                       (long long)(i / 4));
+  dfx::ScopedTimer t("Compute local part of mesh dual graph");
+  std::vector<int32_t> off, a;
+  dual_graph(num_cells, cells, num_vertices, off, a);
+  std::copy(off.begin(), off.end(), offsets);
+  std::copy(a.begin(), a.end(), adj);
   return DFX_OK;
 }
 

@@ -48,6 +48,18 @@ class Mesh:
             self._dev["facets"] = out[: nf.value].copy()
         return self._dev["facets"]
 
+    def dual_graph(self) -> tuple[np.ndarray, np.ndarray]:
+        """(offsets, adjacency) int32 of the facet-connected dual graph
+        (mesh::build_local_dual_graph, cpp/dolfinx/mesh/graphbuild.cpp:566-905):
+        the cells that share a facet with each cell."""
+        nc = self.num_cells
+        off = np.empty(nc + 1, np.int32)
+        adj = np.empty(max(4 * nc, 1), np.int32)
+        cells = np.ascontiguousarray(self.cells, np.int32)
+        _capi.check(_capi.lib().dfx_mesh_dual_graph_tet(nc, cells.ctypes.data, self.num_nodes,
+                                                        off.ctypes.data, adj.ctypes.data))
+        return off, adj[: off[-1]].copy()
+
     def device(self, device="cuda"):
         """(x_dofmap, x) as device tensors (cached)."""
         import torch

@@ -117,6 +117,14 @@ int dfx_mesh_create_box_tet(int32_t nx, int32_t ny, int32_t nz, const double* p0
                             const double* p1, int32_t reorder, int32_t* cells,
                             double* x);
 
+/* mesh::build_local_dual_graph for one tetrahedral cell type, serial path
+ * (mesh/graphbuild.cpp:566-905): cells joined by a facet. offsets
+ * (num_cells+1); adj (capacity 4*num_cells) lists, for each cell, the other
+ * cells of each of its facets in sorted-facet order, as the reference's
+ * edge-by-edge fill gives. Host function, threaded. */
+int dfx_mesh_dual_graph_tet(int32_t num_cells, const int32_t* cells, int32_t num_vertices,
+                            int32_t* offsets, int32_t* adj);
+
 /* fem::create_dofmap for Lagrange P1/P2 on tetrahedra
  * (fem/utils.cpp:32-76, fem/dofmapbuilder.cpp:153-710). dofmap:
  * (num_cells, 4 or 10). Returns the number of dof nodes in *num_nodes. */

@@ -255,3 +255,29 @@ def test_facet_closure_dofs_are_the_boundary_dofs(capi, n, deg):
     np.testing.assert_array_equal(got, ref)
     assert got.dtype == np.int32
     assert fem.locate_dofs_facets(V, np.zeros((0, 2), np.int32)).size == 0
+
+
+# The two largest meshes take the threaded bucket sort with several threads.
+@pytest.mark.parametrize("n,reorder", [((1, 1, 1), True), ((3, 2, 4), True), ((7, 5, 6), False),
+                                       ((24, 24, 24), True), ((30, 20, 26), False)])
+def test_dual_graph_matches_oracle(capi, oracle, n, reorder):
+    from dolfinx_gb300 import mesh
+
+    m = mesh.create_box(((0, 0, 0), (1, 1, 1)), n, reorder=reorder)
+    off, adj = m.dual_graph()
+    off0, adj0 = oracle.dual_graph_tet(m.cells.astype(np.int64))
+    np.testing.assert_array_equal(off, off0)
+    np.testing.assert_array_equal(adj, adj0)
+    # each interior facet joins two cells: 4 nc - (boundary facets) = 2 edges
+    nb = 4 * (n[0] * n[1] + n[1] * n[2] + n[0] * n[2])
+    assert off[-1] == 4 * m.num_cells - nb
+
+
+def test_dual_graph_rejects_bad_cells(capi):
+    cells = np.array([[0, 1, 2, 7]], np.int32)
+    off = np.empty(2, np.int32)
+    adj = np.empty(4, np.int32)
+    assert capi.lib().dfx_mesh_dual_graph_tet(1, cells.ctypes.data, 5, off.ctypes.data,
+                                              adj.ctypes.data) == capi.DFX_ERR_INVALID
+    assert capi.lib().dfx_mesh_dual_graph_tet(0, None, 0, off.ctypes.data, None) == capi.DFX_OK
+    assert off[0] == 0
