@@ -129,6 +129,7 @@ _SIGS = {
     "dfx_abi_version": (C.c_int, []),
     "dfx_mesh_create_box_tet": (C.c_int, [C.c_int32] * 3 + [_P, _P, C.c_int32, _P, _P]),
     "dfx_mesh_dual_graph_tet": (C.c_int, [C.c_int32, _P, C.c_int32, _P, _P]),
+    "dfx_graph_reorder_rcm": (C.c_int, [C.c_int32, _P, _P, _P]),
     "dfx_dofmap_create_tet": (C.c_int, [C.c_int32, _P, C.c_int32, _P, _P]),
     "dfx_sparsity_create": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, _P, _P, _P, _P]),
     "dfx_sparsity_device_workspace_bytes": (C.c_size_t, [C.c_int32, C.c_int32, C.c_int32]),

@@ -666,6 +666,26 @@ extern "C" int dfx_mesh_dual_graph_tet(int32_t num_cells, const int32_t* cells,
   return DFX_OK;
 }
 
+extern "C" int dfx_graph_reorder_rcm(int32_t n, const int32_t* offsets, const int32_t* adj,
+                                     int32_t* perm)
+{
+  if (n < 0 || !offsets || (n > 0 && !perm) || offsets[0] != 0)
+    return dfx::fail(DFX_ERR_INVALID, "invalid graph arguments");
+  for (int32_t i = 0; i < n; ++i)
+    if (offsets[i + 1] < offsets[i])
+      return dfx::fail(DFX_ERR_INVALID, "offsets must not decrease (node %d)", i);
+  if (offsets[n] > 0 && !adj)
+    return dfx::fail(DFX_ERR_INVALID, "adjacency is NULL");
+  for (int32_t k = 0; k < offsets[n]; ++k)
+    if (adj[k] < 0 || adj[k] >= n)
+      return dfx::fail(DFX_ERR_INVALID, "edge %d points outside the graph", k);
+  dfx::ScopedTimer t("Reverse Cuthill-McKee ordering");
+  std::vector<int32_t> off(offsets, offsets + n + 1), a(adj, adj + offsets[n]), r;
+  rcm(off, a, r);
+  std::copy(r.begin(), r.end(), perm);
+  return DFX_OK;
+}
+
 namespace
 {
 // Concurrent open-addressing table from edge keys (sorted vertex pair) to

@@ -125,6 +125,14 @@ int dfx_mesh_create_box_tet(int32_t nx, int32_t ny, int32_t nz, const double* p0
 int dfx_mesh_dual_graph_tet(int32_t num_cells, const int32_t* cells, int32_t num_vertices,
                             int32_t* offsets, int32_t* adj);
 
+/* graph::reorder_rcm (graph/ordering.cpp:148-170): the reverse
+ * Cuthill-McKee permutation of a graph (offsets n+1, adjacency), perm[old]
+ * = new, with the reference's George-Liu pseudo-peripheral root and degree
+ * tie order. The graph is taken as given (symmetric, as a dual graph is).
+ * Host function; large graphs run level by level on threads. */
+int dfx_graph_reorder_rcm(int32_t n, const int32_t* offsets, const int32_t* adj,
+                          int32_t* perm);
+
 /* fem::create_dofmap for Lagrange P1/P2 on tetrahedra
  * (fem/utils.cpp:32-76, fem/dofmapbuilder.cpp:153-710). dofmap:
  * (num_cells, 4 or 10). Returns the number of dof nodes in *num_nodes. */

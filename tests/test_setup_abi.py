@@ -281,3 +281,67 @@ def test_dual_graph_rejects_bad_cells(capi):
                                               adj.ctypes.data) == capi.DFX_ERR_INVALID
     assert capi.lib().dfx_mesh_dual_graph_tet(0, None, 0, off.ctypes.data, None) == capi.DFX_OK
     assert off[0] == 0
+
+
+def _random_graph(n, deg, seed, components=1):
+    """A symmetric graph without self-loops or repeated edges, adjacency in
+    random order, in `components` parts: many equal degrees, so the RCM tie
+    order is exercised."""
+    rng = np.random.default_rng(seed)
+    part = n // components
+    src, dst = [], []
+    for c in range(components):
+        lo, hi = c * part, (c + 1) * part if c < components - 1 else n
+        m = (hi - lo) * deg // 2
+        a = rng.integers(lo, hi, m)
+        b = rng.integers(lo, hi, m)
+        keep = a != b
+        src.append(a[keep])
+        dst.append(b[keep])
+    a, b = np.concatenate(src), np.concatenate(dst)
+    e = np.unique(np.stack([np.minimum(a, b), np.maximum(a, b)], 1), axis=0)
+    u = np.concatenate([e[:, 0], e[:, 1]])
+    v = np.concatenate([e[:, 1], e[:, 0]])
+    order = rng.permutation(u.size)
+    u, v = u[order], v[order]
+    idx = np.argsort(u, kind="stable")
+    off = np.zeros(n + 1, np.int32)
+    np.add.at(off, u + 1, 1)
+    return np.cumsum(off).astype(np.int32), v[idx].astype(np.int32)
+
+
+@pytest.mark.parametrize("case", ["box", "random", "random_parts", "small"])
+def test_rcm_matches_reference(capi, oracle, case):
+    """The threaded RCM against the reference's own compiled graph::reorder_rcm
+    (and the oracle when the reference was not built): graphs large enough for
+    the level-synchronous team, with many degree ties and several components."""
+    from dolfinx_gb300 import graph, mesh
+
+    if case == "box":
+        off, adj = mesh.create_box(((0, 0, 0), (1, 1, 1)), (26, 22, 20), reorder=False).dual_graph()
+    elif case == "random":
+        off, adj = _random_graph(120000, 4, 7)
+    elif case == "random_parts":
+        off, adj = _random_graph(90000, 3, 8, components=5)
+    else:
+        off, adj = _random_graph(50, 3, 9, components=3)
+    perm = graph.reorder_rcm(off, adj)
+    n = off.size - 1
+    assert np.array_equal(np.sort(perm), np.arange(n))
+    R = oracle.ref()
+    if R is not None:
+        ref = np.empty(n, np.int32)
+        R.ref_reorder_rcm(n, off, np.ascontiguousarray(adj, np.int32), ref)
+    else:
+        ref = oracle.reorder_rcm(off, adj)
+    np.testing.assert_array_equal(perm, ref)
+
+
+def test_rcm_rejects_bad_graphs(capi):
+    from dolfinx_gb300 import graph
+
+    with pytest.raises(capi.DfxError, match="outside the graph"):
+        graph.reorder_rcm(np.array([0, 1, 2]), np.array([1, 5]))
+    with pytest.raises(capi.DfxError, match="must not decrease"):
+        graph.reorder_rcm(np.array([0, 2, 1, 2]), np.array([1, 2]))
+    assert graph.reorder_rcm(np.array([0]), np.zeros(0)).size == 0
