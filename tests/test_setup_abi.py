@@ -345,3 +345,29 @@ def test_rcm_rejects_bad_graphs(capi):
     with pytest.raises(capi.DfxError, match="must not decrease"):
         graph.reorder_rcm(np.array([0, 2, 1, 2]), np.array([1, 2]))
     assert graph.reorder_rcm(np.array([0]), np.zeros(0)).size == 0
+
+
+def test_a_plain_c_host_uses_the_abi(capi, tmp_path):
+    """tests/c_host_example.c, compiled as C11 against include/dfx_gpu.h and
+    linked to libdfxgpu.so, runs the host set-up through the C ABI."""
+    import os
+    import shutil
+    import subprocess
+
+    from dolfinx_gb300 import fem, mesh
+
+    cc = shutil.which("gcc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    libdir = os.path.dirname(capi.LIB_PATH)
+    exe = str(tmp_path / "c_host")
+    subprocess.run([cc, "-std=c11", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I",
+                    os.path.join(root, "include"), os.path.join(root, "tests", "c_host_example.c"),
+                    "-o", exe, "-L", libdir, "-ldfxgpu", f"-Wl,-rpath,{libdir}"], check=True,
+                   capture_output=True, timeout=120)
+    out = subprocess.run([exe], check=True, capture_output=True, text=True, timeout=120).stdout
+    V = fem.functionspace(mesh.create_unit_cube(4, 4, 4), ("Lagrange", 2), device="cpu")
+    rp, cols = V.sparsity()
+    assert out.split() == ["abi", "1", "cells", "384", "nodes", str(V.num_nodes), "nnz",
+                           str(cols.size), "facets", "192", "mesh_reps", "1"]
