@@ -3,13 +3,15 @@
 Host set-up (mesh, dofmaps, sparsity) and every device kernel live in the
 in-tree shared library ``_lib/libdfxgpu.so`` behind the C ABI of
 ``include/dfx_gpu.h``; this package is the Python mirror of the
-reference's ``dolfinx.mesh`` / ``dolfinx.fem`` / ``dolfinx.la`` calls.
-Torch supplies device memory and streams only.
+reference's ``dolfinx.mesh`` / ``dolfinx.fem`` / ``dolfinx.la`` /
+``dolfinx.graph`` / ``dolfinx.common`` calls, plus the matrix-free Q4
+operator, the serving loop and the autotuner. Torch supplies device memory
+and streams only.
 """
 
 from . import _capi  # noqa: F401
 
-__all__ = ["mesh", "fem", "la"]
+__all__ = ["mesh", "fem", "la", "graph", "common", "matrix_free", "serving", "autotune"]
 
 
 def __getattr__(name):
