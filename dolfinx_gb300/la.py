@@ -30,7 +30,9 @@ def _check_vec(t, n: int, dtype, device, name: str) -> None:
     the host, so that a wrong argument raises instead of reaching the GPU."""
     if not torch.is_tensor(t):
         raise TypeError(f"{name} must be a torch tensor")
-    if t.device.type != "cuda" or t.device != device:
+    if t.device.type != "cuda":
+        raise ValueError(f"{name} must be on a CUDA device (got {t.device})")
+    if t.device != device:
         raise ValueError(f"{name} must be on {device} (got {t.device})")
     if t.dtype != dtype:
         raise TypeError(f"{name} must be {dtype} (got {t.dtype})")
