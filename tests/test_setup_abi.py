@@ -371,3 +371,44 @@ def test_a_plain_c_host_uses_the_abi(capi, tmp_path):
     rp, cols = V.sparsity()
     assert out.split() == ["abi", "1", "cells", "384", "nodes", str(V.num_nodes), "nnz",
                            str(cols.size), "facets", "192", "mesh_reps", "1"]
+
+
+def test_the_cpp_mirror_header_on_the_host(capi, tmp_path):
+    """include/dolfinx_gb300.hpp (the C++ face of the library) compiles with
+    -pedantic -Werror into tests/cpp_host_example.cpp; the host set-up,
+    timings and error path run and agree with the Python path. The binary
+    runs with no visible GPU, where device work must raise, not fall back."""
+    import os
+    import shutil
+    import subprocess
+
+    from dolfinx_gb300 import fem, mesh
+
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("no C++ compiler")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    libdir = os.path.dirname(capi.LIB_PATH)
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    exe = str(tmp_path / "cpp_host")
+    subprocess.run([cxx, "-std=c++20", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I",
+                    os.path.join(root, "include"), "-I", os.path.join(cuda, "include"),
+                    os.path.join(root, "tests", "cpp_host_example.cpp"), "-o", exe, "-L", libdir,
+                    "-ldfxgpu", f"-Wl,-rpath,{libdir}", "-L", os.path.join(cuda, "lib64"),
+                    "-lcudart", f"-Wl,-rpath,{os.path.join(cuda, 'lib64')}"],
+                   check=True, capture_output=True, timeout=300)
+    env = dict(os.environ, CUDA_VISIBLE_DEVICES="")
+    out = subprocess.run([exe], check=True, capture_output=True, text=True, timeout=120,
+                         env=env).stdout
+    got = dict(line.split(" ", 1) for line in out.strip().splitlines())
+    m = mesh.create_unit_cube(4, 4, 4)
+    V = fem.functionspace(m, ("Lagrange", 2), device="cpu")
+    rp, cols = V.sparsity()
+    off, adj = m.dual_graph()
+    assert got["cells"] == str(m.num_cells) and got["vertices"] == str(m.num_nodes)
+    assert got["nodes"] == str(V.num_nodes) and got["nnz"] == str(cols.size)
+    assert got["dual_edges"] == str(adj.size) and got["rcm"] == str(m.num_cells)
+    assert got["coords"] == str(3 * V.num_nodes) and got["facets"] == "192"
+    assert got["timer_reps"] == "1" and got["mesh_reps"] == "1" and got["table_has_title"] == "1"
+    assert got["error"] == f"{capi.DFX_ERR_INVALID} At least one cell is required."
+    assert got["device"] == f"none {capi.DFX_ERR_CUDA}"
