@@ -815,5 +815,100 @@ inline CGResult cg(const MatrixCSR& A, const device_vector<double>& b, device_ve
                      &info, nullptr));
   return {info.iterations, info.status, info.rnorm0_sq, info.rnorm_sq};
 }
+
+/// The solvers' sliced-ELL copy of a scalar MatrixCSR (rows sorted by
+/// length in windows of sigma rows, 32-row column-major slices): FP64, or
+/// FP32 with 16-bit column deltas. Owns the library's operator.
+class SellOperator
+{
+public:
+  SellOperator(const MatrixCSR& A, bool fp32, int sigma = 256)
+  {
+    if (A.bs() != 1)
+      throw Error(DFX_ERR_UNSUPPORTED, "the solver operator takes scalar (bs 1) matrices");
+    const dfx_csr csr = A.csr();
+    check(dfx_operator_create(&csr, sigma, fp32 ? DFX_F32 : DFX_F64, fp32 ? 1 : 0, &op_,
+                              nullptr));
+    n_ = A.num_rows();
+  }
+  ~SellOperator()
+  {
+    if (op_)
+      dfx_operator_destroy(op_);
+  }
+  SellOperator(const SellOperator&) = delete;
+  SellOperator& operator=(const SellOperator&) = delete;
+  SellOperator(SellOperator&& o) noexcept : op_(std::exchange(o.op_, nullptr)), n_(o.n_) {}
+
+  /// Refill the values from A (after re-assembly).
+  void update_values(const MatrixCSR& A)
+  {
+    const dfx_csr csr = A.csr();
+    check(dfx_operator_update_values(op_, &csr, nullptr));
+  }
+  dfx_operator handle() const { return op_; }
+  std::int32_t size() const { return n_; }
+
+private:
+  dfx_operator op_ = nullptr;
+  std::int32_t n_ = 0;
+};
+
+struct IRResult
+{
+  int outer_iterations;
+  int inner_iterations;
+  int status;
+  double rnorm0_sq, rnorm_sq;
+};
+
+/// Mixed precision: FP32 Jacobi-PCG on the FP32 operator with the residual
+/// replaced by the FP64 residual b - A x each time it drops by inner_rtol
+/// (reliable updates; x += d in FP64). Stops at the FP64 test |b - A x| <
+/// rtol |b - A x0| of cg(). No reference counterpart; it wraps the demo's
+/// CG (demo/poisson_matrix_free/main.cpp:84-132).
+class IRSolver
+{
+public:
+  explicit IRSolver(const MatrixCSR& A, int sigma = 256, double inner_rtol = 0.03)
+      : op64_(A, false, sigma), op32_(A, true, sigma), dinv_(A.num_rows()),
+        inner_rtol_(inner_rtol)
+  {
+    wb_ = dfx_ir_workspace_bytes(A.num_rows());
+    work_.resize(wb_ / sizeof(double) + 1);
+    jacobi(A);
+  }
+  /// Re-read the values of A (after re-assembly).
+  void refresh(const MatrixCSR& A)
+  {
+    op64_.update_values(A);
+    op32_.update_values(A);
+    jacobi(A);
+  }
+  IRResult solve(const device_vector<double>& b, device_vector<double>& x, double rtol = 1e-10,
+                 int max_outer = 200, int max_inner = 100000)
+  {
+    const std::size_t n = (std::size_t)op64_.size();
+    if (b.size() != n || x.size() != n)
+      throw Error(DFX_ERR_INVALID, "b and x must have num_rows entries");
+    dfx_ir_info info{};
+    check(dfx_ir_solve(op64_.handle(), op32_.handle(), b.data(), x.data(), dinv_.data(), rtol,
+                       inner_rtol_, max_outer, max_inner, 0, DFX_IR_RELIABLE, work_.data(), wb_,
+                       &info, nullptr));
+    return {info.outer_iterations, info.inner_iterations, info.status, info.rnorm0_sq,
+            info.rnorm_sq};
+  }
+
+private:
+  void jacobi(const MatrixCSR& A)
+  {
+    const dfx_csr csr = A.csr();
+    check(dfx_jacobi_inverse_diagonal(&csr, dinv_.data(), nullptr));
+  }
+  SellOperator op64_, op32_;
+  device_vector<double> dinv_, work_;
+  std::size_t wb_ = 0;
+  double inner_rtol_;
+};
 } // namespace la
 } // namespace dolfinx_gb300

@@ -89,5 +89,10 @@ int main()
   dg::fem::set_bc(b, bcs);
   const dg::la::CGResult r = dg::la::cg(A, b, x, 1e-10);
   std::printf("device cg %d %d\n", r.iterations, r.status);
+  // the same system by FP32-inner / FP64-outer refinement
+  dg::la::IRSolver ir(A);
+  dg::device_vector<double> x2(V1->num_dofs());
+  const dg::la::IRResult r2 = ir.solve(b, x2, 1e-10);
+  std::printf("device ir %d %d %d\n", r2.inner_iterations, r2.outer_iterations, r2.status);
   return 0;
 }
