@@ -412,3 +412,24 @@ def test_the_cpp_mirror_header_on_the_host(capi, tmp_path):
     assert got["timer_reps"] == "1" and got["mesh_reps"] == "1" and got["table_has_title"] == "1"
     assert got["error"] == f"{capi.DFX_ERR_INVALID} At least one cell is required."
     assert got["device"] == f"none {capi.DFX_ERR_CUDA}"
+
+
+def test_ctypes_signatures_match_the_header(capi):
+    """Every function declared in include/dfx_gpu.h has a ctypes binding
+    with as many arguments as its prototype (a mismatch would shift the
+    arguments of a call silently)."""
+    import os
+    import re
+
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    h = open(os.path.join(root, "include", "dfx_gpu.h")).read()
+    h = re.sub(r"/\*.*?\*/", "", h, flags=re.S)
+    protos = {}
+    for m in re.finditer(r"\b(?:int|size_t|int64_t|const char\*)\s+(dfx_[a-z0-9_]+)\s*"
+                         r"\(([^;{]*?)\)\s*;", h, flags=re.S):
+        args = m.group(2).strip()
+        protos[m.group(1)] = 0 if args in ("", "void") else args.count(",") + 1
+    assert set(protos) == set(capi.declared_symbols())
+    assert set(protos) == set(capi._SIGS)
+    for name, (res, args) in capi._SIGS.items():
+        assert len(args) == protos[name], name
