@@ -433,3 +433,24 @@ def test_ctypes_signatures_match_the_header(capi):
     assert set(protos) == set(capi._SIGS)
     for name, (res, args) in capi._SIGS.items():
         assert len(args) == protos[name], name
+    # and each parameter's type: scalars exactly, pointers as pointers (to
+    # the same scalar where ctypes names it), library handles as void*
+    scalar = {"int32_t": C.c_int32, "int64_t": C.c_int64, "double": C.c_double,
+              "size_t": C.c_size_t, "float": C.c_float, "int": C.c_int}
+    for m in re.finditer(r"\b(?:int|size_t|int64_t|const char\*)\s+(dfx_[a-z0-9_]+)\s*"
+                         r"\(([^;{]*?)\)\s*;", h, flags=re.S):
+        name, params = m.group(1), m.group(2).strip()
+        if params in ("", "void"):
+            continue
+        for p, t in zip((" ".join(a.split()) for a in params.split(",")), capi._SIGS[name][1]):
+            base = p.replace("const ", "").split("*")[0].split()[0]
+            if "**" in p:
+                ok = getattr(t, "_type_", None) is C.c_void_p
+            elif "*" in p:
+                ok = t in (C.c_void_p, C.c_char_p) or (
+                    hasattr(t, "_type_") and scalar.get(base, t._type_) is t._type_)
+            elif base in ("dfx_operator", "dfx_batch"):
+                ok = t is C.c_void_p
+            else:
+                ok = scalar.get(base) is t
+            assert ok, (name, p, t)
