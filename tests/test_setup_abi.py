@@ -454,3 +454,6 @@ def test_ctypes_signatures_match_the_header(capi):
             else:
                 ok = scalar.get(base) is t
             assert ok, (name, p, t)
+    rets = {"int": C.c_int, "size_t": C.c_size_t, "int64_t": C.c_int64, "const char*": C.c_char_p}
+    for m in re.finditer(r"\b(int|size_t|int64_t|const char\*)\s+(dfx_[a-z0-9_]+)\s*\(", h):
+        assert capi._SIGS[m.group(2)][0] is rets[m.group(1)], m.group(2)
