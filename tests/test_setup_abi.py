@@ -17,9 +17,8 @@ def test_library_exports_header_symbols(capi):
     assert lib.dfx_abi_version() == 1
 
 
-# The two largest boxes put more than 65,536 facet keys on each of several
-# threads, so the dual graph's parallel sort and merges run (with an odd
-# chunk count on most machines).
+# The two largest boxes are large enough for the threaded paths: the dual
+# graph's bucket sort and run fill, and the level-synchronous RCM team.
 @pytest.mark.parametrize("n", [(1, 1, 1), (2, 3, 4), (7, 5, 6), (16, 16, 16), (24, 24, 24),
                                (30, 20, 26)])
 def test_mesh_matches_oracle(capi, oracle, n):
@@ -457,3 +456,52 @@ def test_ctypes_signatures_match_the_header(capi):
     rets = {"int": C.c_int, "size_t": C.c_size_t, "int64_t": C.c_int64, "const char*": C.c_char_p}
     for m in re.finditer(r"\b(int|size_t|int64_t|const char\*)\s+(dfx_[a-z0-9_]+)\s*\(", h):
         assert capi._SIGS[m.group(2)][0] is rets[m.group(1)], m.group(2)
+
+
+# ctypes structure of the binding -> (C struct name, C field names in order)
+_STRUCTS = {
+    "Form": ("dfx_form", ["kind", "degree", "num_cells", "num_nodes", "x_dofmap", "x", "dofmap",
+                          "kappa", "kappa_const", "k2", "nu", "f", "f_const"]),
+    "Csr": ("dfx_csr", ["nrows", "ncols", "bs", "dtype", "nnz", "row_ptr", "cols", "vals"]),
+    "CgInfo": ("dfx_cg_info", ["iterations", "status", "rnorm0_sq", "rnorm_sq",
+                               "kernel_launches"]),
+    "IrInfo": ("dfx_ir_info", ["outer_iterations", "inner_iterations", "status", "reserved",
+                               "rnorm0_sq", "rnorm_sq", "kernel_launches"]),
+    "BatchSystem": ("dfx_batch_system", ["op32", "op64", "b", "x", "dinv", "work", "rtol",
+                                         "delta", "max_iters", "mode"]),
+    "Q4Mesh": ("dfx_q4_mesh", ["nx", "ny", "nz", "verts", "kappa", "edges32"]),
+}
+
+
+def test_ctypes_structures_match_the_c_layout(capi, tmp_path):
+    """Each ctypes Structure of the binding has the size and field offsets
+    that a C compiler gives the struct of include/dfx_gpu.h (the kernels
+    read these structs by value or pointer)."""
+    import os
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    lines = ['#include "dfx_gpu.h"', "#include <stddef.h>", "#include <stdio.h>",
+             "int main(void) {"]
+    for py, (cs, fields) in _STRUCTS.items():
+        lines.append(f'  printf("{py} size %zu\\n", sizeof({cs}));')
+        for f in fields:
+            lines.append(f'  printf("{py} {f} %zu\\n", offsetof({cs}, {f}));')
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = str(tmp_path / "layout")
+    subprocess.run([cc, "-std=c11", "-I", os.path.join(root, "include"), str(src), "-o", exe],
+                   check=True, capture_output=True, timeout=120)
+    out = subprocess.run([exe], check=True, capture_output=True, text=True).stdout.split("\n")
+    got = {tuple(l.split()[:2]): int(l.split()[2]) for l in out if l.strip()}
+    for py, (cs, fields) in _STRUCTS.items():
+        T = getattr(capi, py)
+        assert [f[0] for f in T._fields_] == fields, py
+        assert C.sizeof(T) == got[(py, "size")], py
+        for f in fields:
+            assert getattr(T, f).offset == got[(py, f)], (py, f)
