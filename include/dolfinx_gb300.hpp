@@ -590,9 +590,38 @@ public:
     L.f_const_ = f;
     return L;
   }
+  /// L(v) = int_F g v ds over exterior facets given as (cell, local facet)
+  /// pairs (all boundary facets when empty); g per geometry node or g_const.
+  static Form facet_source(std::shared_ptr<const FunctionSpace> V, std::span<const double> g = {},
+                           double g_const = 1.0, std::span<const std::int32_t> facets = {})
+  {
+    Form L = source(std::move(V), g, g_const);
+    L.set_facets(facets);
+    return L;
+  }
+  /// a(u,v) = int_F alpha u v ds (a Robin term), alpha per cell or alpha_const.
+  static Form facet_mass(std::shared_ptr<const FunctionSpace> V,
+                         std::span<const double> alpha = {}, double alpha_const = 1.0,
+                         std::span<const std::int32_t> facets = {})
+  {
+    if (V->bs() != 1)
+      throw Error(DFX_ERR_INVALID, "facet forms need a scalar space");
+    Form a(DFX_FORM_FACET_MASS, std::move(V));
+    a.set_kappa(alpha, alpha_const);
+    a.set_facets(facets);
+    return a;
+  }
 
   const FunctionSpace& function_space() const { return *V_; }
-  bool bilinear() const { return kind_ == DFX_FORM_POISSON || kind_ == DFX_FORM_ELASTICITY; }
+  bool bilinear() const
+  {
+    return kind_ == DFX_FORM_POISSON || kind_ == DFX_FORM_ELASTICITY ||
+           kind_ == DFX_FORM_FACET_MASS;
+  }
+  /// An exterior-facet integral (else a cell integral).
+  bool on_facets() const { return num_facets_ >= 0; }
+  const std::int32_t* device_facets() const { return facets_.data(); }
+  std::int32_t num_facets() const { return num_facets_; }
 
   /// The dfx_form view for the C ABI (uploads the space on first use).
   dfx_form c() const
@@ -627,9 +656,26 @@ private:
     }
     kappa_const_ = c;
   }
+  void set_facets(std::span<const std::int32_t> facets)
+  {
+    if (V_->bs() != 1)
+      throw Error(DFX_ERR_INVALID, "facet forms need a scalar space");
+    std::vector<std::int32_t> f(facets.begin(), facets.end());
+    if (f.empty())
+      f = mesh::exterior_facets(V_->mesh());
+    if (f.size() % 2)
+      throw Error(DFX_ERR_INVALID, "facets must be (cell, local facet) pairs");
+    for (std::size_t i = 0; i < f.size(); i += 2)
+      if (f[i] < 0 || f[i] >= V_->mesh().num_cells || f[i + 1] < 0 || f[i + 1] > 3)
+        throw Error(DFX_ERR_INVALID, "facets must be (cell, local facet < 4) pairs in the mesh");
+    facets_.assign(f);
+    num_facets_ = (std::int32_t)(f.size() / 2);
+  }
   int kind_;
   std::shared_ptr<const FunctionSpace> V_;
   device_vector<double> kappa_, f_;
+  device_vector<std::int32_t> facets_;
+  std::int32_t num_facets_ = -1;
   double kappa_const_ = 1.0, k2_ = 0.0, nu_ = 0.3;
   std::array<double, 3> f_const_ = {0.0, 0.0, 0.0};
 };
@@ -737,8 +783,13 @@ inline void assemble_matrix(la::MatrixCSR& A, const Form& a, const BCs& bcs = {}
     l = detail::lifting_data(V, bcs);
   const dfx_form f = a.c();
   const dfx_csr csr = A.csr();
-  check(dfx_assemble_matrix(&f, &csr, nullptr, l ? l->markers.data() : nullptr, DFX_MODE_ATOMIC,
-                            nullptr, nullptr, 0, nullptr));
+  const std::int8_t* bc = l ? l->markers.data() : nullptr;
+  if (a.on_facets())
+    check(dfx_assemble_matrix_facets(&f, a.device_facets(), a.num_facets(), &csr, nullptr, bc,
+                                     nullptr));
+  else
+    check(dfx_assemble_matrix(&f, &csr, nullptr, bc, DFX_MODE_ATOMIC, nullptr, nullptr, 0,
+                              nullptr));
 }
 
 /// set_diagonal (fem/assembler.h:644-686): A[d, d] = diagonal on every
@@ -759,7 +810,27 @@ inline void assemble_vector(device_vector<double>& b, const Form& L)
   if (b.size() != (std::size_t)L.function_space().num_dofs())
     throw Error(DFX_ERR_INVALID, "b must have num_dofs entries");
   const dfx_form f = L.c();
-  check(dfx_assemble_vector(&f, b.data(), DFX_MODE_ATOMIC, nullptr, nullptr, 0, nullptr));
+  if (L.on_facets())
+    check(dfx_assemble_vector_facets(&f, L.device_facets(), L.num_facets(), b.data(), nullptr));
+  else
+    check(dfx_assemble_vector(&f, b.data(), DFX_MODE_ATOMIC, nullptr, nullptr, 0, nullptr));
+}
+
+/// fem::assemble_scalar over the cells (fem/assembler.h:173-215): a(u, u)
+/// of a Poisson/Helmholtz form or L(u) of a source form, summed in a fixed
+/// order.
+inline double assemble_scalar(const Form& M, const device_vector<double>& u)
+{
+  if (M.on_facets())
+    throw Error(DFX_ERR_UNSUPPORTED, "functionals are cell integrals");
+  if (u.size() != (std::size_t)M.function_space().num_dofs())
+    throw Error(DFX_ERR_INVALID, "u must have num_dofs entries");
+  const dfx_form f = M.c();
+  const std::size_t wb = dfx_assemble_scalar_workspace_bytes(f.num_cells);
+  device_vector<double> work(wb / sizeof(double) + 1);
+  double v = 0.0;
+  check(dfx_assemble_scalar(&f, u.data(), &v, work.data(), wb, nullptr));
+  return v;
 }
 
 /// fem::apply_lifting for one bilinear form (fem/assembler.h:336-421):
@@ -769,6 +840,8 @@ inline void apply_lifting(device_vector<double>& b, const Form& a, const BCs& bc
 {
   if (bcs.empty())
     return;
+  if (a.on_facets())
+    throw Error(DFX_ERR_UNSUPPORTED, "lifting of exterior-facet terms is not supported");
   const FunctionSpace& V = a.function_space();
   if (b.size() != (std::size_t)V.num_dofs() || (x0 && x0->size() != b.size()))
     throw Error(DFX_ERR_INVALID, "b (and x0) must have num_dofs entries");

@@ -94,5 +94,13 @@ int main()
   dg::device_vector<double> x2(V1->num_dofs());
   const dg::la::IRResult r2 = ir.solve(b, x2, 1e-10);
   std::printf("device ir %d %d %d\n", r2.inner_iterations, r2.outer_iterations, r2.status);
+  // the energy a(u, u) of the solution and a Neumann term on the boundary
+  std::printf("device energy %.6e\n", dg::fem::assemble_scalar(a, x));
+  dg::device_vector<double> bn(V1->num_dofs());
+  dg::fem::assemble_vector(bn, dg::fem::Form::facet_source(V1, {}, 1.0));
+  double area = 0.0; // sum_i int_F phi_i ds = the boundary's area, 6
+  for (double v : bn.to_host())
+    area += v;
+  std::printf("device boundary_area %.12f\n", area);
   return 0;
 }
