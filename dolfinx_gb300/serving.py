@@ -127,6 +127,20 @@ def _stream_ptr(s):
     return C.c_void_p(s.cuda_stream)
 
 
+def unit_cube_boundary_nodes(X: np.ndarray) -> np.ndarray:
+    """Nodes of a unit-cube space whose point (a row of X, every coordinate
+    in [0, 1] up to rounding) has a coordinate that np.isclose (default
+    tolerances) finds equal to 0 or to 1. On [0, 1] the coordinate closest
+    to 0 is the smallest and the one closest to 1 the largest, so isclose's
+    own test on those two gives the same answer as on all three, at a
+    fraction of the work."""
+    lo = np.minimum(np.minimum(X[:, 0], X[:, 1]), X[:, 2])
+    hi = np.maximum(np.maximum(X[:, 0], X[:, 1]), X[:, 2])
+    near0 = np.abs(lo) <= 1e-8 + 1e-5 * 0.0
+    near1 = np.abs(hi - 1.0) <= 1e-8 + 1e-5 * 1.0
+    return np.flatnonzero(near0 | near1).astype(np.int32)
+
+
 class Structure:
     """Everything of one (n, degree) that requests share."""
 
@@ -138,9 +152,8 @@ class Structure:
         self.n, self.degree = n, degree
         self.mesh = mesh.create_unit_cube(n, n, n)
         self.V = fem.functionspace(self.mesh, ("Lagrange", degree), device=device)
-        X = self.V.tabulate_dof_coordinates()
-        bnd = np.flatnonzero(np.isclose(X, 0.0).any(1) | np.isclose(X, 1.0).any(1))
-        self.bc = fem.dirichletbc(0.0, bnd.astype(np.int32), self.V)
+        bnd = unit_cube_boundary_nodes(self.V.tabulate_dof_coordinates())
+        self.bc = fem.dirichletbc(0.0, bnd, self.V)
         a = fem.poisson_form(self.V, 1.0, k2=1.0)
         self.asm = fem.MatrixAssembler(a, [self.bc])  # slot map, markers, structure
         self.A0 = self.asm.A

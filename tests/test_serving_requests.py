@@ -38,3 +38,22 @@ def test_request_stream_is_reproducible_and_rate_independent_in_content():
     # the same requests arrive faster at a higher rate
     assert [(r.n, r.degree, r.k2, r.seed) for r in a] == [(r.n, r.degree, r.k2, r.seed) for r in c]
     assert c[-1].arrival < a[-1].arrival
+
+
+def test_unit_cube_boundary_nodes_equal_isclose():
+    """The serving structures' boundary nodes (two column passes) are the
+    nodes np.isclose finds at 0 or 1, for P1/P2 boxes of several sizes and
+    for points at and just inside the tolerances."""
+    from dolfinx_gb300 import fem, mesh, serving
+
+    for n in (1, 3, 7, 49):
+        m = mesh.create_unit_cube(n, n, n)
+        for deg in (1, 2):
+            X = fem.functionspace(m, ("Lagrange", deg), device="cpu").tabulate_dof_coordinates()
+            ref = np.flatnonzero(np.isclose(X, 0.0).any(1) | np.isclose(X, 1.0).any(1))
+            np.testing.assert_array_equal(serving.unit_cube_boundary_nodes(X), ref)
+    t = 1e-8 + 1e-5
+    X = np.array([[0.5, 0.5, 1e-8], [0.5, 0.5, 1.1e-8], [1 - t, 0.5, 0.5],
+                  [1 - 1.01 * t, 0.5, 0.5], [1.0, 1.0, 1.0], [0.3, 0.6, 0.9]])
+    ref = np.flatnonzero(np.isclose(X, 0.0).any(1) | np.isclose(X, 1.0).any(1))
+    np.testing.assert_array_equal(serving.unit_cube_boundary_nodes(X), ref)
