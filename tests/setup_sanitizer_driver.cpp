@@ -1,6 +1,7 @@
-// Runs the threaded host set-up of libdfxgpu (box mesh + RCM, P2 dofmap,
-// dof coordinates, exterior facets, sparsity) on one box, for a build with
-// -fsanitize=thread. Argument: the box size n (n^3 x 6 cells).
+// Runs the threaded host set-up of libdfxgpu (box mesh + RCM, P1/P2 dofmaps,
+// dof coordinates, exterior facets, sparsity, colouring, dual graph, RCM) on
+// one box, for a build with -fsanitize=thread or with
+// -fsanitize=address,undefined. Argument: the box size n (n^3 x 6 cells).
 #include "dfx_gpu.h"
 
 #include <cstdarg>
@@ -50,6 +51,21 @@ int main(int argc, char** argv)
   std::vector<int32_t> cols(nnz);
   if (dfx_sparsity_create(nn, nc, 10, dm.data(), rp.data(), cols.data(), &nnz))
     return 6;
-  std::printf("nodes %d facets %d nnz %lld\n", nn, nf, (long long)nnz);
+  // the P1 dofmap, the cell colouring, and the dual graph + RCM entry points
+  std::vector<int32_t> dm1(4 * (size_t)nc);
+  int32_t nn1 = 0;
+  if (dfx_dofmap_create_tet(nc, cells.data(), 1, dm1.data(), &nn1))
+    return 7;
+  std::vector<int32_t> order(nc), offsets(257);
+  int32_t ncol = 0;
+  if (dfx_colour_cells(nc, 10, dm.data(), nn, order.data(), offsets.data(), 256, &ncol))
+    return 8;
+  std::vector<int32_t> off(nc + 1), adj(4 * (size_t)nc), perm(nc);
+  if (dfx_mesh_dual_graph_tet(nc, cells.data(), nv, off.data(), adj.data()))
+    return 9;
+  if (dfx_graph_reorder_rcm(nc, off.data(), adj.data(), perm.data()))
+    return 10;
+  std::printf("nodes %d facets %d nnz %lld p1 %d colours %d edges %d\n", nn, nf, (long long)nnz,
+              nn1, ncol, off[nc]);
   return 0;
 }
