@@ -69,3 +69,20 @@ def test_host_setup_is_memory_clean(asan, n, threads):
     out = _run(asan, n, threads, {"ASAN_OPTIONS": "detect_leaks=1:halt_on_error=1"})
     nodes = (2 * n + 1) ** 3
     assert out.startswith(f"nodes {nodes} facets {12 * n * n} ")
+
+
+@pytest.mark.parametrize("src", ["dolfinx_gb300/csrc/setup.cpp", "dolfinx_gb300/csrc/timing.cpp",
+                                 "dolfinx_gb300/csrc/tune.cpp", "oracle/dfx_oracle.cpp"])
+def test_host_sources_build_with_developer_flags(src):
+    """The reference's Developer build flags (-Wall -Wextra -Werror -pedantic,
+    cpp/cmake/modules/DolfinxDeveloperCompilerFlags.cmake) plus libstdc++
+    assertions: the host C++ compiles without a warning."""
+    cxx = shutil.which("g++")
+    if cxx is None:
+        pytest.skip("no g++")
+    cuda = os.environ.get("CUDA_HOME", "/usr/local/cuda")
+    p = subprocess.run([cxx, "-std=c++20", "-O2", "-Wall", "-Wextra", "-Werror", "-pedantic",
+                        "-D_GLIBCXX_ASSERTIONS", "-fsyntax-only", "-I",
+                        os.path.join(ROOT, "include"), "-I", os.path.join(cuda, "include"), "-I",
+                        CSRC, os.path.join(ROOT, src)], capture_output=True, text=True, timeout=300)
+    assert p.returncode == 0, p.stderr[-3000:]
