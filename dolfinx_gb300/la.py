@@ -263,12 +263,17 @@ class SellOperator:
         """v in the operator's (renumbered) numbering."""
         if out is None:
             out = torch.empty_like(v)
+        _check_vec(v, self.n, torch.float64, self.device, "v")
+        _check_vec(out, self.n, torch.float64, self.device, "out")
         _capi.check(_capi.lib().dfx_operator_permute(self.handle, _ptr(v), _ptr(out), 1, _stream()))
         return out
 
     def from_operator(self, v: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
+        """v back in the original numbering."""
         if out is None:
             out = torch.empty_like(v)
+        _check_vec(v, self.n, torch.float64, self.device, "v")
+        _check_vec(out, self.n, torch.float64, self.device, "out")
         _capi.check(_capi.lib().dfx_operator_permute(self.handle, _ptr(v), _ptr(out), 0, _stream()))
         return out
 
