@@ -45,7 +45,8 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--cpu-sample-cells", type=int, default=120000)
     p.add_argument("--inner-rtol", type=float, default=None,
-                   help="reliable: residual drop between replacements (0.1); restart: inner rtol")
+                   help="reliable: residual drop between replacements (default 0.03); "
+                        "restart: inner rtol (default 1e-4)")
     p.add_argument("--ir-variant", default="reliable", choices=["reliable", "restart"])
     p.add_argument("--serving-requests", type=int, default=64,
                    help="requests of the bounded serving sample (0: skip)")

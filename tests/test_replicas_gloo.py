@@ -63,3 +63,22 @@ def test_single_replica_needs_no_process_group():
     R = bench.Replicas(1, "cpu")
     R.barrier()
     assert R.max(7.0) == 7.0 and R.total(5.0) == 5.0
+
+
+def test_bench_defaults_and_host_helpers(monkeypatch):
+    """bench.py's defaults keep the run contract (1 GPU, at least 3 warm-up
+    steps, our implementation), and its host helpers read the committed
+    profile summary and the peak file."""
+    sys.path.insert(0, ROOT)
+    import bench
+
+    monkeypatch.setattr(sys, "argv", ["bench.py"])
+    a = bench.parse()
+    assert a.gpus == 1 and a.impl == "ours" and a.warmup >= 3 and a.steps >= 1
+    cfg = bench.workload_config(a, 2146689, 60859905)
+    assert cfg["cells"] == 6 * 64 ** 3 and cfg["dofs"] == 2146689 and cfg["nnz"] == 60859905
+    assert cfg["parallelism"] == "single"
+    peak, kind = bench.measured_peaks()
+    assert peak > 0 and kind in ("measured", "fallback")
+    assert bench.profile_traffic("sell_f32_p2_64") == 418223104
+    assert bench.profile_traffic("no such kernel") is None
