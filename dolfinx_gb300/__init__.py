@@ -11,7 +11,7 @@ and streams only.
 
 from . import _capi  # noqa: F401
 
-__all__ = ["mesh", "fem", "la", "graph", "common", "matrix_free", "serving", "autotune"]
+__all__ = ["mesh", "fem", "la", "graph", "common", "log", "matrix_free", "serving", "autotune"]
 
 
 def __getattr__(name):

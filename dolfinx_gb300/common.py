@@ -29,6 +29,7 @@ import typing
 from collections.abc import Callable
 
 from . import _capi
+from . import log as _log
 
 __all__ = ["Reduction", "Timer", "list_timings", "timed", "timing", "timing_table", "timings"]
 
@@ -46,6 +47,7 @@ class Reduction(enum.IntEnum):
 
 def _record(task: str, seconds: float) -> None:
     _capi.check(_capi.lib().dfx_timing_record(task.encode(), float(seconds)))
+    _log.logger.debug("Elapsed time: %s (%s)", float(seconds), task)
 
 
 def timing(task: str) -> tuple[int, datetime.timedelta]:

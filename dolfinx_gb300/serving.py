@@ -44,6 +44,7 @@ import numpy as np
 import torch
 
 from . import _capi, autotune, fem, la, mesh
+from . import log as _log
 
 
 @dataclass
@@ -312,6 +313,7 @@ class Server:
 
     # ------------------------------------------------------------ admission
     def _reject(self, req: Request, status: int, error: str) -> Rejected:
+        _log.logger.warning("request %s refused (status %s): %s", req.rid, status, error)
         rej = Rejected(req, int(status), error, time.perf_counter())
         with self.lock:
             self.finished.append(rej)

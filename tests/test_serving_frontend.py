@@ -148,3 +148,20 @@ def test_server_rejects_unknown_modes_before_device_work(capi, kw, msg):
 
     with pytest.raises(ValueError, match=msg):
         serving.Server(**kw)
+
+
+def test_refusals_are_logged_as_warnings(front, capi, tmp_path):
+    import logging
+    import sys
+
+    from dolfinx_gb300 import log as lg
+
+    serving, srv, sizes, dropped, built = front
+    path = tmp_path / "serving.log"
+    lg.set_output_file(str(path))
+    try:
+        srv.run([serving.Request(5, 8, 7, 0.0, 1)], max_wall_s=30.0)
+    finally:
+        lg._install(logging.StreamHandler(sys.stderr))
+    text = path.read_text()
+    assert "[WARNING] request 5 refused (status 1): Lagrange degree 7 not supported" in text
