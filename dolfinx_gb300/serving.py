@@ -197,7 +197,10 @@ def cached_structure(n: int, degree: int) -> Structure:
     with _structure_lock:
         st = _structure_cache.get(key)
     if st is None:
+        t0 = time.perf_counter()
         built = Structure(n, degree)
+        _log.logger.info("structure n=%s P%s built in %.3f s (%s dofs)", n, degree,
+                         time.perf_counter() - t0, built.ndofs)
         with _structure_lock:
             st = _structure_cache.setdefault(key, built)
     return st
@@ -305,6 +308,8 @@ class Server:
                 self.used -= st.bytes
                 del self.structures[key]
                 drop_structure(*key)
+                _log.logger.info("structure n=%s P%s evicted (%s bytes)", key[0], key[1],
+                                 st.bytes)
 
     def prewarm(self, requests):
         for key in sorted({(r.n, r.degree) for r in requests}):
