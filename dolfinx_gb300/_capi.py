@@ -139,6 +139,7 @@ _SIGS = {
     "dfx_tabulate_dof_coordinates_tet": (C.c_int, [C.c_int32, _P, C.c_int32, _P, _P, C.c_int32,
                                                    C.c_int32, _P]),
     "dfx_exterior_facets_tet": (C.c_int, [C.c_int32, _P, _P, C.POINTER(C.c_int32)]),
+    "dfx_interior_facets_tet": (C.c_int, [C.c_int32, _P, _P, C.POINTER(C.c_int32)]),
     "dfx_assemble_vector_facets": (C.c_int, [C.POINTER(Form), _P, C.c_int32, _P, _P]),
     "dfx_assemble_matrix_facets": (C.c_int, [C.POINTER(Form), _P, C.c_int32, C.POINTER(Csr), _P,
                                              _P, _P]),

@@ -1038,6 +1038,22 @@ extern "C" int dfx_colour_cells(int32_t num_cells, int32_t nd, const int32_t* do
   return DFX_OK;
 }
 
+namespace
+{
+// Largest vertex index of `nc` tetrahedra, or an error for a negative one.
+int tet_vertex_max(int32_t nc, const int32_t* cells, int64_t* vmax)
+{
+  *vmax = 0;
+  for (int64_t i = 0; i < 4 * (int64_t)nc; ++i)
+  {
+    if (cells[i] < 0)
+      return dfx::fail(DFX_ERR_INVALID, "negative vertex index in cell %lld", (long long)(i / 4));
+    *vmax = std::max<int64_t>(*vmax, cells[i]);
+  }
+  return DFX_OK;
+}
+} // namespace
+
 extern "C" int dfx_exterior_facets_tet(int32_t num_cells, const int32_t* cells, int32_t* facets,
                                        int32_t* num_facets)
 {
@@ -1048,13 +1064,8 @@ extern "C" int dfx_exterior_facets_tet(int32_t num_cells, const int32_t* cells, 
   // every vertex index fits, else two words); a facet seen once is
   // exterior (mesh/utils.cpp:61-89).
   int64_t vmax = 0;
-  for (int64_t i = 0; i < nf; ++i)
-  {
-    if (cells[i] < 0)
-      return dfx::fail(DFX_ERR_INVALID, "negative vertex index in cell %lld",
-                       (long long)(i / 4));
-    vmax = std::max<int64_t>(vmax, cells[i]);
-  }
+  if (const int rc = tet_vertex_max(num_cells, cells, &vmax); rc != DFX_OK)
+    return rc;
   const SortedFacets sf = sort_facets(num_cells, cells, vmax + 1);
   std::unique_ptr<uint8_t[]> exterior = filled<uint8_t>(nf, 0);
   parallel_for(nf, [&](int64_t a, int64_t b)
@@ -1069,6 +1080,46 @@ extern "C" int dfx_exterior_facets_tet(int32_t num_cells, const int32_t* cells, 
     {
       facets[2 * (int64_t)n] = (int32_t)(i / 4);
       facets[2 * (int64_t)n + 1] = (int32_t)(i % 4);
+      ++n;
+    }
+  *num_facets = n;
+  return DFX_OK;
+}
+
+extern "C" int dfx_interior_facets_tet(int32_t num_cells, const int32_t* cells, int32_t* facets,
+                                       int32_t* num_facets)
+{
+  if (num_cells < 0 || !num_facets || (num_cells > 0 && (!cells || !facets)))
+    return dfx::fail(DFX_ERR_INVALID, "invalid interior facet arguments");
+  const int64_t nf = 4 * (int64_t)num_cells;
+  // A facet is interior when exactly two (cell, local facet) entries share
+  // its vertex triple (fem/utils.cpp:223-254: facets with two attached
+  // cells). The sort puts the two next to each other, the smaller
+  // (cell, local facet) first; that one records its partner.
+  int64_t vmax = 0;
+  if (const int rc = tet_vertex_max(num_cells, cells, &vmax); rc != DFX_OK)
+    return rc;
+  const SortedFacets sf = sort_facets(num_cells, cells, vmax + 1);
+  std::unique_ptr<int64_t[]> partner = filled<int64_t>(nf, -1);
+  parallel_for(nf, [&](int64_t a, int64_t b)
+               {
+                 for (int64_t p = a; p < b; ++p)
+                   if (p + 1 < nf && sf.same(p, p + 1) && !(p > 0 && sf.same(p - 1, p))
+                       && !(p + 2 < nf && sf.same(p + 1, p + 2)))
+                   {
+                     const int64_t i = sf.facet(p), j = sf.facet(p + 1);
+                     partner[std::min(i, j)] = std::max(i, j);
+                   }
+               });
+  int32_t n = 0;
+  for (int64_t i = 0; i < nf; ++i)
+    if (const int64_t j = partner[i]; j >= 0)
+    {
+      int32_t* q = facets + 4 * (int64_t)n;
+      q[0] = (int32_t)(i / 4);
+      q[1] = (int32_t)(i % 4);
+      q[2] = (int32_t)(j / 4);
+      q[3] = (int32_t)(j % 4);
       ++n;
     }
   *num_facets = n;

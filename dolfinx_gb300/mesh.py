@@ -48,6 +48,21 @@ class Mesh:
             self._dev["facets"] = out[: nf.value].copy()
         return self._dev["facets"]
 
+    def interior_facets(self) -> np.ndarray:
+        """(num_facets, 4) int32 (cell0, local facet0, cell1, local facet1)
+        of the facets shared by two cells: the integration domain of an
+        interior-facet integral (fem::compute_integration_domains,
+        cpp/dolfinx/fem/utils.cpp:223-254). (cell0, facet0) < (cell1,
+        facet1) within a row; rows sorted. Cached."""
+        if "interior_facets" not in self._dev:
+            out = np.empty((2 * self.num_cells, 4), np.int32)
+            nf = C.c_int32(0)
+            cells = np.ascontiguousarray(self.cells, np.int32)
+            _capi.check(_capi.lib().dfx_interior_facets_tet(self.num_cells, cells.ctypes.data,
+                                                            out.ctypes.data, C.byref(nf)))
+            self._dev["interior_facets"] = out[: nf.value].copy()
+        return self._dev["interior_facets"]
+
     def dual_graph(self) -> tuple[np.ndarray, np.ndarray]:
         """(offsets, adjacency) int32 of the facet-connected dual graph
         (mesh::build_local_dual_graph, cpp/dolfinx/mesh/graphbuild.cpp:566-905):

@@ -318,6 +318,17 @@ int dfx_cg_solve_noalloc(const dfx_csr* A, const double* d_b, double* d_x,
 int dfx_exterior_facets_tet(int32_t num_cells, const int32_t* cells, int32_t* facets,
                             int32_t* num_facets);
 
+/* Interior facets of a tetrahedral mesh: the integration domain of an
+ * interior-facet integral on one rank (fem::compute_integration_domains,
+ * fem/utils.cpp:223-254: facets with two attached cells, each written as
+ * (cell0, local facet0, cell1, local facet1)). A facet shared by more
+ * than two cells is left out, as in the reference. facets: capacity
+ * 8*num_cells int32; (cell0, facet0) < (cell1, facet1) within each
+ * entry, entries sorted by (cell0, facet0); *num_facets = count. Host
+ * function. */
+int dfx_interior_facets_tet(int32_t num_cells, const int32_t* cells, int32_t* facets,
+                            int32_t* num_facets);
+
 /* Exterior-facet vector loop (fem/assemble_vector_impl.h:160-215,
  * 571-600): b += \int_F g v ds over the facets, L a DFX_FORM_SOURCE form
  * (g = its P1 coefficient f, or f_const[0]), scalar P1/P2. FP64 atomics. */

@@ -369,6 +369,18 @@ inline std::vector<std::int32_t> exterior_facets(const Mesh& m)
   f.resize(2 * (std::size_t)nf);
   return f;
 }
+
+/// Interior facets as (cell0, local facet0, cell1, local facet1), sorted:
+/// the interior-facet integration domain (compute_integration_domains,
+/// fem/utils.cpp:223-254).
+inline std::vector<std::int32_t> interior_facets(const Mesh& m)
+{
+  std::vector<std::int32_t> f(8 * (std::size_t)m.num_cells);
+  std::int32_t nf = 0;
+  check(dfx_interior_facets_tet(m.num_cells, m.cells.data(), f.data(), &nf));
+  f.resize(4 * (std::size_t)nf);
+  return f;
+}
 } // namespace mesh
 
 // ---------------------------------------------------------------- graph

@@ -22,6 +22,7 @@
 #include <cmath>
 #include <cstdint>
 #include <cstring>
+#include <map>
 #include <numeric>
 #include <unordered_map>
 #include <vector>
@@ -1172,6 +1173,38 @@ int orc_exterior_facets_tet(int nc, const int32_t* cells, int32_t* pairs)
     pairs[2 * i] = out[i].first;
     pairs[2 * i + 1] = out[i].second;
   }
+  return (int)out.size();
+}
+
+// Interior facets of a tetrahedral mesh, the integration domain of an
+// interior-facet integral on one rank (cpp/dolfinx/fem/utils.cpp:223-254:
+// each facet with exactly two attached cells, written as (cell0, local
+// facet0, cell1, local facet1)). Entries hold (cell0, facet0) <
+// (cell1, facet1) and are sorted by (cell0, facet0). Returns the count.
+int orc_interior_facets_tet(int nc, const int32_t* cells, int32_t* quads)
+{
+  // (sorted vertex triple) -> every (cell, local facet) with that triple
+  std::map<std::array<int32_t, 3>, std::vector<std::pair<int32_t, int32_t>>> owners;
+  for (int c = 0; c < nc; ++c)
+    for (int f = 0; f < 4; ++f)
+    {
+      std::array<int32_t, 3> v = {cells[4 * c + kTetFacets[f][0]],
+                                  cells[4 * c + kTetFacets[f][1]],
+                                  cells[4 * c + kTetFacets[f][2]]};
+      std::sort(v.begin(), v.end());
+      owners[v].push_back({c, f});
+    }
+  std::vector<std::array<int32_t, 4>> out;
+  for (auto& [v, cf] : owners)
+    if (cf.size() == 2)
+    {
+      std::sort(cf.begin(), cf.end());
+      out.push_back({cf[0].first, cf[0].second, cf[1].first, cf[1].second});
+    }
+  std::sort(out.begin(), out.end());
+  for (size_t i = 0; i < out.size(); ++i)
+    for (int k = 0; k < 4; ++k)
+      quads[4 * i + k] = out[i][k];
   return (int)out.size();
 }
 

@@ -82,6 +82,7 @@ def lib():
         L.orc_cg.argtypes = [C.c_int, C.c_int, _i64p, _i32p, _f64p, _f64p, _f64p, C.c_void_p,
                              C.c_double, C.c_int]
         L.orc_exterior_facets_tet.argtypes = [C.c_int, _i32p, _i32p]
+        L.orc_interior_facets_tet.argtypes = [C.c_int, _i32p, _i32p]
         L.orc_assemble_vector_facets.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, _i32p,
                                                  C.c_void_p, C.c_double, _f64p]
         L.orc_assemble_matrix_facets.argtypes = [C.c_int, C.c_int, _i32p, _i32p, _f64p, _i32p,
@@ -320,6 +321,15 @@ def exterior_facets(cells):
     cells = np.ascontiguousarray(cells, np.int32)
     out = np.empty((4 * cells.shape[0], 2), np.int32)
     nf = lib().orc_exterior_facets_tet(cells.shape[0], cells, out)
+    return out[:nf].copy()
+
+
+def interior_facets(cells):
+    """(num_facets, 4) int32 array of (cell0, local facet0, cell1, local
+    facet1), sorted."""
+    cells = np.ascontiguousarray(cells, np.int32)
+    out = np.empty((max(2 * cells.shape[0], 1), 4), np.int32)
+    nf = lib().orc_interior_facets_tet(cells.shape[0], cells, out)
     return out[:nf].copy()
 
 

@@ -25,10 +25,12 @@ int main()
   const dg::fem::SparsityPattern sp = dg::fem::create_sparsity_pattern(*V);
   const std::vector<double> X = V->tabulate_dof_coordinates();
   const std::vector<std::int32_t> facets = dg::mesh::exterior_facets(*m);
+  const std::vector<std::int32_t> inner = dg::mesh::interior_facets(*m);
   std::printf("cells %d\nvertices %d\nnodes %d\nnnz %zu\ndual_edges %zu\nrcm %zu\n",
               m->num_cells, m->num_vertices, V->num_nodes(), sp.cols.size(), adj.size(),
               perm.size());
-  std::printf("coords %zu\nfacets %zu\n", X.size(), facets.size() / 2);
+  std::printf("coords %zu\nfacets %zu\ninterior_facets %zu\n", X.size(), facets.size() / 2,
+              inner.size() / 4);
 
   // timings
   {

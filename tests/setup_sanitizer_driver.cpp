@@ -51,7 +51,8 @@ int main(int argc, char** argv)
   std::vector<int32_t> cols(nnz);
   if (dfx_sparsity_create(nn, nc, 10, dm.data(), rp.data(), cols.data(), &nnz))
     return 6;
-  // the P1 dofmap, the cell colouring, and the dual graph + RCM entry points
+  // the P1 dofmap, the cell colouring, the dual graph + RCM entry points and
+  // the interior facets (each cell facet exterior or one side of one)
   std::vector<int32_t> dm1(4 * (size_t)nc);
   int32_t nn1 = 0;
   if (dfx_dofmap_create_tet(nc, cells.data(), 1, dm1.data(), &nn1))
@@ -65,7 +66,13 @@ int main(int argc, char** argv)
     return 9;
   if (dfx_graph_reorder_rcm(nc, off.data(), adj.data(), perm.data()))
     return 10;
-  std::printf("nodes %d facets %d nnz %lld p1 %d colours %d edges %d\n", nn, nf, (long long)nnz,
-              nn1, ncol, off[nc]);
+  std::vector<int32_t> fi(8 * (size_t)nc);
+  int32_t nfi = 0;
+  if (dfx_interior_facets_tet(nc, cells.data(), fi.data(), &nfi))
+    return 11;
+  if (2 * nfi + nf != 4 * nc)
+    return 12;
+  std::printf("nodes %d facets %d interior %d nnz %lld p1 %d colours %d edges %d\n", nn, nf,
+              nfi, (long long)nnz, nn1, ncol, off[nc]);
   return 0;
 }

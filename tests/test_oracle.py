@@ -193,6 +193,24 @@ def test_exterior_facets_count_and_orientation(oracle, n):
     assert on.all()
 
 
+@pytest.mark.parametrize("n", [(1, 1, 1), (3, 2, 4)])
+def test_interior_facets_pair_cells_on_one_triangle(oracle, n):
+    # 6 tetrahedra per box cell, 4 facets each: every facet not on the
+    # boundary is shared by exactly two distinct cells, on the same triangle
+    cells, x = oracle.create_box_tet(*n)
+    fi = oracle.interior_facets(cells)
+    nx, ny, nz = n
+    assert 2 * fi.shape[0] == 24 * nx * ny * nz - 4 * (nx * ny + ny * nz + nx * nz)
+    loc = np.array([[1, 2, 3], [0, 2, 3], [0, 1, 3], [0, 1, 2]])
+    t0 = np.sort(cells[fi[:, 0][:, None], loc[fi[:, 1]]], axis=1)
+    t1 = np.sort(cells[fi[:, 2][:, None], loc[fi[:, 3]]], axis=1)
+    np.testing.assert_array_equal(t0, t1)
+    assert (fi[:, 0] < fi[:, 2]).all()
+    assert (np.diff(fi[:, 0] * 4 + fi[:, 1]) > 0).all()
+    # no triangle appears twice
+    assert np.unique(t0, axis=0).shape[0] == fi.shape[0]
+
+
 @pytest.mark.parametrize("deg", [1, 2])
 def test_facet_vector_totals(oracle, deg):
     # sum_i b_i = \int_Gamma g ds: g = 1 gives the surface area of the box,

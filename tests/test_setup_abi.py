@@ -106,6 +106,43 @@ def test_exterior_facets_of_no_cells(capi):
     assert nf.value == 0
 
 
+@pytest.mark.parametrize("n", [(1, 1, 1), (3, 2, 4), (6, 5, 7), (24, 24, 24)])
+def test_interior_facets_match_oracle(capi, oracle, n):
+    from dolfinx_gb300 import mesh
+
+    m = mesh.create_unit_cube(*n)
+    got = m.interior_facets()
+    np.testing.assert_array_equal(got, oracle.interior_facets(m.cells))
+    # every facet of every cell is either exterior or one side of an interior facet
+    assert 2 * got.shape[0] + m.exterior_facets().shape[0] == 4 * m.num_cells
+
+
+def test_interior_facets_edge_cases(capi):
+    import ctypes as C
+
+    def interior(cells):
+        cells = np.ascontiguousarray(cells, np.int32)
+        nc = cells.size // 4
+        out = np.full((max(2 * nc, 1), 4), -7, np.int32)
+        nf = C.c_int32(-1)
+        capi.check(capi.lib().dfx_interior_facets_tet(nc, cells.ctypes.data, out.ctypes.data,
+                                                      C.byref(nf)))
+        return out[: nf.value]
+
+    assert interior(np.zeros(4, np.int32)[:0]).shape == (0, 4)
+    assert interior([[0, 1, 2, 3]]).shape == (0, 4)
+    # two cells glued on the triangle {1, 2, 3}: opposite vertex 0 in cell 0,
+    # opposite vertex 4 (local 3) in cell 1
+    np.testing.assert_array_equal(interior([[0, 1, 2, 3], [1, 2, 3, 4]]), [[0, 0, 1, 3]])
+    # the same triangle in a third cell: not an interior facet (three cells)
+    assert interior([[0, 1, 2, 3], [1, 2, 3, 4], [3, 2, 1, 5]]).shape == (0, 4)
+    with pytest.raises(capi.DfxError, match="negative vertex index in cell 1"):
+        interior([[0, 1, 2, 3], [1, 2, -3, 4]])
+    nf = C.c_int32(0)
+    with pytest.raises(capi.DfxError, match="invalid interior facet arguments"):
+        capi.check(capi.lib().dfx_interior_facets_tet(-1, None, None, C.byref(nf)))
+
+
 def test_autotuner_table_host_logic(capi):
     """The autotuner's table is host state: choices are keyed per workload
     (form kind, degree, mass term, cells, mode; matrix shape), validated
@@ -408,6 +445,7 @@ def test_the_cpp_mirror_header_on_the_host(capi, tmp_path):
     assert got["nodes"] == str(V.num_nodes) and got["nnz"] == str(cols.size)
     assert got["dual_edges"] == str(adj.size) and got["rcm"] == str(m.num_cells)
     assert got["coords"] == str(3 * V.num_nodes) and got["facets"] == "192"
+    assert got["interior_facets"] == str(m.interior_facets().shape[0]) == "672"
     assert got["timer_reps"] == "1" and got["mesh_reps"] == "1" and got["table_has_title"] == "1"
     assert got["error"] == f"{capi.DFX_ERR_INVALID} At least one cell is required."
     assert got["device"] == f"none {capi.DFX_ERR_CUDA}"

@@ -57,3 +57,4 @@ def test_random_box_matches_oracle(capi, oracle, threads_env, i, n):
         assert V.num_nodes == nn
         np.testing.assert_array_equal(V.dofmap, dm)
     np.testing.assert_array_equal(m.exterior_facets(), oracle.exterior_facets(m.cells))
+    np.testing.assert_array_equal(m.interior_facets(), oracle.interior_facets(m.cells))

@@ -1,7 +1,7 @@
 """Race and memory checks for the threaded host set-up. Its sources are built
 into a small driver (tests/setup_sanitizer_driver.cpp) that runs box mesh +
-RCM, P1/P2 dofmaps, dof coordinates, exterior facets, sparsity, colouring,
-the dual graph and RCM entry points:
+RCM, P1/P2 dofmaps, dof coordinates, exterior and interior facets, sparsity,
+colouring, the dual graph and RCM entry points:
 - with ThreadSanitizer, on a box large enough for every thread team, at two
   thread counts;
 - with AddressSanitizer + UndefinedBehaviorSanitizer and libstdc++'s
