@@ -10,6 +10,7 @@ The bilinear/linear forms are the built-in element kernels of libdfxgpu
 from __future__ import annotations
 
 import ctypes as C
+import enum
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -140,6 +141,42 @@ def locate_dofs_geometrical(V: FunctionSpace, marker) -> np.ndarray:
 # f): its three vertices, then (P2) its three edges in Basix edge order.
 _FACET_CLOSURE = np.array([[1, 2, 3, 4, 5, 6], [0, 2, 3, 4, 7, 8], [0, 1, 3, 5, 7, 9],
                            [0, 1, 2, 6, 8, 9]], np.int32)
+
+
+class IntegralType(enum.IntEnum):
+    """Integral types with the reference's values (fem/Form.h:39-46)."""
+
+    cell = 0
+    exterior_facet = 1
+    interior_facet = 2
+    vertex = 3
+    ridge = 4
+
+
+def compute_integration_domains(integral_type: IntegralType, mesh: Mesh,
+                                entities: np.ndarray | None = None) -> np.ndarray:
+    """Flat int32 integration entities (fem/utils.cpp:153-275) of one rank:
+    cell indices for ``cell``; (cell, local facet) pairs for
+    ``exterior_facet``; (cell0, local facet0, cell1, local facet1) for
+    ``interior_facet``. The meshes here number no facets, so facet
+    domains cover every exterior or interior facet, sorted by cell; for
+    cells, ``entities`` (sorted cell indices) selects a subset. Vertex and
+    ridge domains are not supported."""
+    integral_type = IntegralType(integral_type)
+    if integral_type in (IntegralType.vertex, IntegralType.ridge):
+        raise ValueError(f"{integral_type.name} integration domains are not supported")
+    if integral_type == IntegralType.cell:
+        if entities is None:
+            return np.arange(mesh.num_cells, dtype=np.int32)
+        cells = np.asarray(entities, np.int32).ravel()
+        if cells.size and (cells.min() < 0 or cells.max() >= mesh.num_cells):
+            raise ValueError(f"cell indices must lie in [0, {mesh.num_cells})")
+        return cells.copy()
+    if entities is not None:
+        raise ValueError("facet domains take no entities: the mesh numbers no facets")
+    if integral_type == IntegralType.exterior_facet:
+        return mesh.exterior_facets().ravel().copy()
+    return mesh.interior_facets().ravel().copy()
 
 
 def locate_dofs_facets(V: FunctionSpace, facets: np.ndarray) -> np.ndarray:

@@ -115,6 +115,14 @@ def test_interior_facets_match_oracle(capi, oracle, n):
     np.testing.assert_array_equal(got, oracle.interior_facets(m.cells))
     # every facet of every cell is either exterior or one side of an interior facet
     assert 2 * got.shape[0] + m.exterior_facets().shape[0] == 4 * m.num_cells
+    # the cell pairs are the edges of the facet-connected dual graph
+    off, adj = m.dual_graph()
+    src = np.repeat(np.arange(m.num_cells), np.diff(off))
+    edges = np.stack([src, adj], 1)
+    edges = edges[edges[:, 0] < edges[:, 1]]
+    pairs = got[:, [0, 2]]
+    np.testing.assert_array_equal(np.unique(pairs, axis=0), np.unique(edges, axis=0))
+    assert np.unique(pairs, axis=0).shape[0] == pairs.shape[0]
 
 
 def test_interior_facets_edge_cases(capi):
@@ -543,3 +551,29 @@ def test_ctypes_structures_match_the_c_layout(capi, tmp_path):
         assert C.sizeof(T) == got[(py, "size")], py
         for f in fields:
             assert getattr(T, f).offset == got[(py, f)], (py, f)
+
+
+def test_compute_integration_domains(capi, oracle):
+    """fem.compute_integration_domains: flat int32 entities per integral
+    type, with the reference's IntegralType values."""
+    from dolfinx_gb300 import fem, mesh
+
+    m = mesh.create_unit_cube(3, 2, 2)
+    T = fem.IntegralType
+    assert [T.cell, T.exterior_facet, T.interior_facet, T.vertex, T.ridge] == list(range(5))
+    cells = fem.compute_integration_domains(T.cell, m)
+    assert cells.dtype == np.int32
+    np.testing.assert_array_equal(cells, np.arange(m.num_cells))
+    np.testing.assert_array_equal(fem.compute_integration_domains(T.cell, m, [2, 5, 7]),
+                                  [2, 5, 7])
+    ext = fem.compute_integration_domains(T.exterior_facet, m)
+    np.testing.assert_array_equal(ext, oracle.exterior_facets(m.cells).ravel())
+    inner = fem.compute_integration_domains(2, m)
+    assert inner.dtype == np.int32 and inner.ndim == 1
+    np.testing.assert_array_equal(inner, oracle.interior_facets(m.cells).ravel())
+    with pytest.raises(ValueError, match="cell indices must lie"):
+        fem.compute_integration_domains(T.cell, m, [m.num_cells])
+    with pytest.raises(ValueError, match="take no entities"):
+        fem.compute_integration_domains(T.interior_facet, m, [0])
+    with pytest.raises(ValueError, match="ridge integration domains are not supported"):
+        fem.compute_integration_domains(T.ridge, m)
