@@ -72,6 +72,61 @@ void parallel_for(int64_t n, F&& f)
     t.join();
 }
 
+// Runs f(b) for every block b in [0, nb) on threads, consecutive blocks
+// to a thread.
+template <typename F>
+void for_each_block(int64_t nb, F&& f)
+{
+  const int nt = (int)std::min<int64_t>(num_threads(), nb);
+  if (nt <= 1)
+  {
+    for (int64_t b = 0; b < nb; ++b)
+      f(b);
+    return;
+  }
+  std::vector<std::thread> th;
+  for (int t = 0; t < nt; ++t)
+    th.emplace_back(
+        [&f, t, nt, nb]
+        {
+          for (int64_t b = nb * t / nt; b < nb * (t + 1) / nt; ++b)
+            f(b);
+        });
+  for (auto& t : th)
+    t.join();
+}
+
+// Stream compaction: emit(k, i) for the k-th index i in [0, n), in
+// increasing order, that satisfies keep(i); returns the count. Fixed
+// blocks are counted on threads, offset by a prefix sum and written on
+// threads, so the output does not depend on the thread count.
+template <typename Keep, typename Emit>
+int64_t compact(int64_t n, const Keep& keep, const Emit& emit)
+{
+  constexpr int64_t kBlock = int64_t(1) << 16;
+  const int64_t nb = (n + kBlock - 1) / kBlock;
+  std::vector<int64_t> start(nb + 1, 0);
+  for_each_block(nb,
+                 [&](int64_t b)
+                 {
+                   int64_t c = 0;
+                   for (int64_t i = b * kBlock, e = std::min(n, i + kBlock); i < e; ++i)
+                     c += keep(i) ? 1 : 0;
+                   start[b + 1] = c;
+                 });
+  for (int64_t b = 0; b < nb; ++b)
+    start[b + 1] += start[b];
+  for_each_block(nb,
+                 [&](int64_t b)
+                 {
+                   int64_t k = start[b];
+                   for (int64_t i = b * kBlock, e = std::min(n, i + kBlock); i < e; ++i)
+                     if (keep(i))
+                       emit(k++, i);
+                 });
+  return start[nb];
+}
+
 // Uninitialised array filled with `v` on threads.
 template <typename T>
 std::unique_ptr<T[]> filled(int64_t n, T v)
@@ -1074,15 +1129,17 @@ extern "C" int dfx_exterior_facets_tet(int32_t num_cells, const int32_t* cells, 
                    if (!(p > 0 && sf.same(p - 1, p)) && !(p + 1 < nf && sf.same(p, p + 1)))
                      exterior[sf.facet(p)] = 1;
                });
-  int32_t n = 0;
-  for (int64_t i = 0; i < nf; ++i)
-    if (exterior[i])
-    {
-      facets[2 * (int64_t)n] = (int32_t)(i / 4);
-      facets[2 * (int64_t)n + 1] = (int32_t)(i % 4);
-      ++n;
-    }
-  *num_facets = n;
+  const int64_t n = compact(
+      nf, [&](int64_t i) { return exterior[i] != 0; },
+      [&](int64_t k, int64_t i)
+      {
+        facets[2 * k] = (int32_t)(i / 4);
+        facets[2 * k + 1] = (int32_t)(i % 4);
+      });
+  if (n > INT32_MAX)
+    return dfx::fail(DFX_ERR_INVALID, "%lld exterior facets overflow the int32 count",
+                     (long long)n);
+  *num_facets = (int32_t)n;
   return DFX_OK;
 }
 
@@ -1111,17 +1168,20 @@ extern "C" int dfx_interior_facets_tet(int32_t num_cells, const int32_t* cells, 
                      partner[std::min(i, j)] = std::max(i, j);
                    }
                });
-  int32_t n = 0;
-  for (int64_t i = 0; i < nf; ++i)
-    if (const int64_t j = partner[i]; j >= 0)
-    {
-      int32_t* q = facets + 4 * (int64_t)n;
-      q[0] = (int32_t)(i / 4);
-      q[1] = (int32_t)(i % 4);
-      q[2] = (int32_t)(j / 4);
-      q[3] = (int32_t)(j % 4);
-      ++n;
-    }
-  *num_facets = n;
+  const int64_t n = compact(
+      nf, [&](int64_t i) { return partner[i] >= 0; },
+      [&](int64_t k, int64_t i)
+      {
+        const int64_t j = partner[i];
+        int32_t* q = facets + 4 * k;
+        q[0] = (int32_t)(i / 4);
+        q[1] = (int32_t)(i % 4);
+        q[2] = (int32_t)(j / 4);
+        q[3] = (int32_t)(j % 4);
+      });
+  if (n > INT32_MAX)
+    return dfx::fail(DFX_ERR_INVALID, "%lld interior facets overflow the int32 count",
+                     (long long)n);
+  *num_facets = (int32_t)n;
   return DFX_OK;
 }

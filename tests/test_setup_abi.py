@@ -212,13 +212,14 @@ sys.path.insert(0, sys.argv[1])
 from dolfinx_gb300 import fem, mesh
 m = mesh.create_box(((0, 0, 0), (1, 1, 1)), (26, 22, 20))
 V = fem.functionspace(m, ("Lagrange", 2), device="cpu")
-np.savez(sys.argv[2], cells=m.cells, x=m.x, dofmap=V.dofmap, facets=m.exterior_facets())
+np.savez(sys.argv[2], cells=m.cells, x=m.x, dofmap=V.dofmap, facets=m.exterior_facets(),
+         interior=m.interior_facets())
 """
 
 
 def test_host_setup_is_independent_of_the_thread_count(capi, tmp_path):
-    """Mesh (dual-graph sort), dofmap (first appearance) and exterior facets
-    built with 1, 3, 7 and 16 host threads are identical: the GPU host has a
+    """Mesh (dual-graph sort), dofmap (first appearance), exterior and
+    interior facets built with 1, 3, 7 and 16 host threads are identical: the GPU host has a
     different core count from the machine the parity tests ran on."""
     import os
     import subprocess
@@ -235,7 +236,7 @@ def test_host_setup_is_independent_of_the_thread_count(capi, tmp_path):
                        timeout=300)
         out[t] = np.load(f)
     for t in (3, 7, 16):
-        for k in ("cells", "x", "dofmap", "facets"):
+        for k in ("cells", "x", "dofmap", "facets", "interior"):
             np.testing.assert_array_equal(out[t][k], out[1][k])
 
 
