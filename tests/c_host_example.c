@@ -22,7 +22,7 @@ int main(void)
   double* x = malloc(sizeof(double) * 3 * nv);
   int32_t* dofmap = malloc(sizeof(int32_t) * 10 * nc);
   int32_t* facets = malloc(sizeof(int32_t) * 8 * nc);
-  int32_t nodes = 0, nf = 0, reps = 0;
+  int32_t nodes = 0, nf = 0, ni = 0, reps = 0;
   int64_t nnz = 0;
   double seconds = 0.0;
   if (!cells || !x || !dofmap || !facets)
@@ -39,14 +39,17 @@ int main(void)
     return fail("sparsity fill");
   if (dfx_exterior_facets_tet(nc, cells, facets, &nf) != DFX_OK)
     return fail("facets");
+  /* the facets buffer is reused: interior facets need as much room */
+  if (dfx_interior_facets_tet(nc, cells, facets, &ni) != DFX_OK)
+    return fail("interior facets");
   if (dfx_timing("Build BoxMesh (tetrahedra)", &reps, &seconds) != DFX_OK)
     return fail("timing");
   /* an invalid box is refused with the reference's message */
   if (dfx_mesh_create_box_tet(0, 1, 1, p0, p1, 1, cells, x) != DFX_ERR_INVALID ||
       strcmp(dfx_last_error(), "At least one cell is required.") != 0)
     return 3;
-  printf("abi %d cells %d nodes %d nnz %lld facets %d mesh_reps %d\n", dfx_abi_version(), nc,
-         nodes, (long long)nnz, nf, reps);
+  printf("abi %d cells %d nodes %d nnz %lld facets %d interior %d mesh_reps %d\n",
+         dfx_abi_version(), nc, nodes, (long long)nnz, nf, ni, reps);
   free(cols);
   free(row_ptr);
   free(facets);

@@ -415,7 +415,8 @@ def test_a_plain_c_host_uses_the_abi(capi, tmp_path):
     V = fem.functionspace(mesh.create_unit_cube(4, 4, 4), ("Lagrange", 2), device="cpu")
     rp, cols = V.sparsity()
     assert out.split() == ["abi", "1", "cells", "384", "nodes", str(V.num_nodes), "nnz",
-                           str(cols.size), "facets", "192", "mesh_reps", "1"]
+                           str(cols.size), "facets", "192", "interior", "672",
+                           "mesh_reps", "1"]
 
 
 def test_the_cpp_mirror_header_on_the_host(capi, tmp_path):
