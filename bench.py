@@ -7,7 +7,8 @@ per-cell kappa ~ lognormal(0, 1) and f ~ U[-1, 1] per P1 node from one
 seed, u = 0 on x = 0 and x = 1. A step assembles the CSR matrix (values
 zeroed, cell loop, diagonal of constrained rows), the right-hand side
 (assemble_vector + apply_lifting + set_bc) and solves with
-Jacobi-preconditioned CG to rtol 1e-10. Mesh, sparsity pattern and
+Jacobi-preconditioned CG to relative residual 2.5e-11 (relative error
+below 1e-10 against the converged FP64 solution). Mesh, sparsity pattern and
 cell->slot map are built once, outside the timed region, as a serving
 loop keeps them resident.
 
@@ -30,8 +31,16 @@ import time
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
-METRIC = "GDoF/s assembly+CG (P2 Poisson, Jacobi-PCG rtol 1e-10)"
+METRIC = "GDoF/s assembly+CG (P2 Poisson, Jacobi-PCG to 1e-10 relative error)"
 UNIT = "GDoF/s"
+# Relative residual at which a step's solve stops, in both the plain FP64
+# and the mixed-precision path (and the CPU baseline). At rtol 1e-10 the
+# solutions of this system are only within ~2.5e-10 of the converged
+# solution; 2.5e-11 brings both below 1e-10 relative error, the accuracy the
+# speed-up is stated at. Both errors are measured every run against an
+# FP64 solve to rtol 1e-13 and printed in the config block.
+STEP_RTOL = 2.5e-11
+ERR_BOUND = 1e-10
 
 
 def parse():
@@ -43,7 +52,6 @@ def parse():
     p.add_argument("--n", type=int, default=64, help="hexahedra per direction")
     p.add_argument("--mode", default="atomic", choices=["atomic", "coloured"])
     p.add_argument("--no-cpu-baseline", action="store_true")
-    p.add_argument("--cpu-sample-cells", type=int, default=120000)
     p.add_argument("--inner-rtol", type=float, default=None,
                    help="reliable: residual drop between replacements (default 0.03); "
                         "restart: inner rtol (default 1e-4)")
@@ -67,8 +75,10 @@ def parse():
 
 def workload_config(args, n_dofs=None, nnz=None):
     n = args.n
-    cfg = {"workload": f"P2 Poisson unit cube {n}^3x6 tets, lognormal kappa, Jacobi-PCG rtol 1e-10",
-           "cells": 6 * n ** 3, "degree": 2, "rtol": 1e-10, "seed": 0,
+    cfg = {"workload": f"P2 Poisson unit cube {n}^3x6 tets, lognormal kappa, Jacobi-PCG to "
+                       f"1e-10 relative error",
+           "cells": 6 * n ** 3, "degree": 2, "rtol": STEP_RTOL, "error_bound": ERR_BOUND,
+           "seed": 0,
            "l2": "matrix values (nnz*8 B) exceed the 129 MB L2; no flush between steps",
            "assembly_mode": args.mode, "ir_variant": args.ir_variant,
            "parallelism": "replicas" if args.gpus > 1 else "single"}
@@ -144,14 +154,14 @@ class Problem:
         self.assemble()
         self.fp64.refresh()
         self.x.zero_()
-        self.last = self.fp64.solve(self.b, self.x, rtol=1e-10)
+        self.last = self.fp64.solve(self.b, self.x, rtol=STEP_RTOL)
         return self.last
 
     def step_ir(self):
         self.assemble()
         self.ir.refresh()
         self.x.zero_()
-        self.last = self.ir.solve(self.b, self.x, rtol=1e-10)
+        self.last = self.ir.solve(self.b, self.x, rtol=STEP_RTOL)
         return self.last
 
 
@@ -234,125 +244,128 @@ def profile_traffic(name):
 
 
 # --------------------------------------------------------------------------- CPU baseline
-def cpu_baseline(m, kappa, f, P, iters, sample_cells):
-    """Oracle (CPU restatement of the reference loops) timed on a bounded
-    sample: the matrix cell loop over `sample_cells` cells, the vector cell
-    loop over the same cells, and 3 CSR SpMV passes, extrapolated to one
-    full step with the GPU run's CG iteration count."""
+def host_threads():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def p2_boundary_dofs(cells, x, dofmap):
+    """Dofs of the P2 space on x = 0 and x = 1 (vertex dofs at the vertices,
+    edge dofs at the edge midpoints, Basix edge order)."""
     import numpy as np
 
-    from oracle import oracle as O
+    nn = int(dofmap.max()) + 1
+    X = np.zeros((nn, 3))
+    X[dofmap[:, :4]] = x[cells]
+    for e, (a, b) in enumerate(((2, 3), (1, 3), (1, 2), (0, 3), (0, 2), (0, 1))):
+        X[dofmap[:, 4 + e]] = 0.5 * (x[cells[:, a]] + x[cells[:, b]])
+    return np.flatnonzero(np.isclose(X[:, 0], 0.0) | np.isclose(X[:, 0], 1.0)).astype(np.int32)
 
-    O.build(with_ref=False)
-    V = P.V
-    rp = P.A.row_ptr.cpu().numpy()
-    cols = P.A.cols.cpu().numpy()
-    vals = np.zeros(cols.size)
-    nc = m.num_cells
-    s = min(sample_cells, nc)
-    cells = np.ascontiguousarray(m.cells[:s])
-    dm = np.ascontiguousarray(V.dofmap[:s])
-    t0 = time.perf_counter()
-    O.assemble_matrix(0, 2, cells, m.x, dm, rp, cols, kappa=kappa[:s], vals=vals)
-    t_mat = (time.perf_counter() - t0) * nc / s
-    t0 = time.perf_counter()
-    O.assemble_vector(0, 2, cells, m.x, dm, V.num_nodes, f=f)
-    t_vec = (time.perf_counter() - t0) * nc / s
-    A = P.A.vals.cpu().numpy()
-    xv = np.random.default_rng(0).standard_normal(V.num_nodes)
-    t0 = time.perf_counter()
-    for _ in range(3):
-        O.spmv(rp, cols, A, xv)
-    t_spmv = (time.perf_counter() - t0) / 3
-    n = V.num_nodes
-    t0 = time.perf_counter()
-    for _ in range(3):  # the 5 BLAS-1 passes of a PCG iteration
-        y = xv * 1.0001 + xv
-        float(np.dot(y, xv))
-        float(np.dot(xv, xv))
-        y *= 0.5
-    t_blas = (time.perf_counter() - t0) / 3
-    t_step = t_mat + t_vec + iters * (t_spmv + t_blas)
-    return {"value": n / t_step / 1e9, "unit": UNIT, "cores": 1, "kind": "port",
-            "sample": f"oracle matrix+vector cell loops over {s} of {nc} cells and 3 CSR SpMV "
-                      f"passes of {rp[-1]} nnz, extrapolated to a full step with {iters} CG "
-                      f"iterations",
-            "seconds_per_step": t_step}
+
+class CpuStep:
+    """One full step of the workload on the host cores with the oracle (the
+    CPU restatement of the reference loops): matrix cell loop, set_diagonal,
+    vector cell loop, lifting, set_bc and Jacobi-PCG from zero to the same
+    relative residual as the GPU path. The cell loops run on a thread team
+    in colour classes and the CG splits rows over the same threads; the
+    reference itself assembles serially per MPI rank and needs MPI, Basix
+    and FFCx, which are not available, so the oracle stands in for it."""
+
+    def __init__(self, cells, x, dofmap, row_ptr, cols, kappa, f, threads):
+        import numpy as np
+
+        from oracle import oracle as O
+
+        O.build(with_ref=False)
+        self.O = O
+        self.cells = np.ascontiguousarray(cells, np.int32)
+        self.x = np.ascontiguousarray(x, np.float64)
+        self.dofmap = np.ascontiguousarray(dofmap, np.int32)
+        self.row_ptr = np.ascontiguousarray(row_ptr, np.int64)
+        self.cols = np.ascontiguousarray(cols, np.int32)
+        self.kappa, self.f = kappa, f
+        self.n = self.row_ptr.size - 1
+        self.bnd = p2_boundary_dofs(self.cells, self.x, self.dofmap)
+        self.colours = O.colour_cells(self.dofmap, self.n)
+        self.threads = threads
+        self.vals = np.empty(self.cols.size)
+        self.b = np.empty(self.n)
+        self.u = np.empty(self.n)
+
+    def step(self):
+        """Returns (seconds, CG iterations, [matrix, rhs, solve] seconds)."""
+        t0 = time.perf_counter()
+        it, sec, _, _, _ = self.O.poisson_step_threaded(
+            2, self.cells, self.x, self.dofmap, self.n, self.bnd, self.row_ptr, self.cols,
+            self.colours, kappa=self.kappa, f=self.f, rtol=STEP_RTOL, threads=self.threads,
+            vals=self.vals, b=self.b, u=self.u)
+        return time.perf_counter() - t0, it, [float(v) for v in sec]
+
+    def sample(self):
+        return (f"full step ({self.cells.shape[0]} cells assembled, matrix + rhs + lifting + "
+                f"set_bc, Jacobi-PCG to rtol {STEP_RTOL}) on {self.threads} host threads")
+
+
+def cpu_baseline(m, kappa, f, P):
+    """The oracle's full step on every host core, timed once."""
+    cs = CpuStep(m.cells, m.x, P.V.dofmap, P.A.row_ptr.cpu().numpy(), P.A.cols.cpu().numpy(),
+                 kappa, f, host_threads())
+    sec, it, parts = cs.step()
+    return {"value": P.V.num_dofs / sec / 1e9, "unit": UNIT, "cores": cs.threads, "kind": "port",
+            "sample": cs.sample(), "seconds_per_step": sec, "cg_iterations": it,
+            "seconds_matrix_rhs_solve": parts}
 
 
 # --------------------------------------------------------------------------- reference arm
-def _ref_worker(args_tuple):
-    n, sample_cells, iters_hint = args_tuple
-    import numpy as np
-
-    sys.path.insert(0, ROOT)
-    from oracle import oracle as O
-
-    O.build(with_ref=False)
-    cells, x = O.create_box_tet(n, n, n)
-    dm, nn = O.dofmap_tet(cells, 2)
-    nc = cells.shape[0]
-    rng = np.random.default_rng(0)
-    kappa = np.exp(rng.normal(0.0, 1.0, nc))
-    f = rng.uniform(-1.0, 1.0, x.shape[0])
-    s = min(sample_cells, nc)
-    # Sparsity of the sample cells only (bounded CPU work).
-    rp, cols = O.sparsity(nn, np.ascontiguousarray(dm[:s]))
-    vals = np.zeros(cols.size)
-    t0 = time.perf_counter()
-    O.assemble_matrix(0, 2, np.ascontiguousarray(cells[:s]), x, np.ascontiguousarray(dm[:s]), rp,
-                      cols, kappa=kappa[:s], vals=vals)
-    O.assemble_vector(0, 2, np.ascontiguousarray(cells[:s]), x, np.ascontiguousarray(dm[:s]), nn,
-                      f=f)
-    t_cells = (time.perf_counter() - t0) * nc / s
-    # SpMV cost per entry from the sample matrix, scaled to the full nnz
-    # (28.35 entries per row for P2 tets). Only the sample's rows are kept:
-    # the empty rows of the other cells would add per-row loop overhead that
-    # the scaling would multiply.
-    lens = np.diff(rp)
-    rows = np.flatnonzero(lens)
-    rp_s = np.concatenate([[0], np.cumsum(lens[rows])]).astype(np.int64)
-    xv = rng.standard_normal(nn)
-    t0 = time.perf_counter()
-    for _ in range(3):
-        O.spmv(rp_s, cols, vals, xv)
-    t_spmv = (time.perf_counter() - t0) / 3 * (28.35 * nn) / max(cols.size, 1)
-    return nn, t_cells, t_spmv
-
-
 def run_reference(args):
     """The reference's CPU path (the oracle restatement of its loops; the
-    reference itself needs MPI/Basix/FFCx and does not build here), as N
-    single-thread replicas, one per host core, on bounded samples."""
-    import multiprocessing as mp
+    reference itself needs MPI/Basix/FFCx and does not build here) on every
+    host core: W untimed and K timed full steps of the same workload, each
+    assembling all cells and solving to the same relative residual as the
+    GPU arm."""
+    import numpy as np
+
+    from oracle import oracle as O
 
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    cores = os.cpu_count() or 1
-    iters = 1236  # FP64 Jacobi-PCG iterations of this system at rtol 1e-10 (measured on GB300)
-    ctx = mp.get_context("spawn")
-    sample = max(2000, args.cpu_sample_cells // 8)
-    t0 = time.perf_counter()
-    with ctx.Pool(cores) as pool:
-        res = pool.map(_ref_worker, [(args.n, sample, iters)] * cores)
-    wall = time.perf_counter() - t0
-    nn = res[0][0]
-    per = [nn / (tc + iters * ts * 1.15) for _, tc, ts in res]
-    value = sum(per) / 1e9
+    O.build(with_ref=False)
+    t_start = time.perf_counter()
+    n = args.n
+    cells, x = O.create_box_tet(n, n, n)
+    dm, nn = O.dofmap_tet(cells, 2)
+    rp, cols = O.sparsity(nn, dm)
+    rng = np.random.default_rng(0)
+    kappa = np.exp(rng.normal(0.0, 1.0, cells.shape[0]))
+    f = rng.uniform(-1.0, 1.0, x.shape[0])
+    cs = CpuStep(cells, x, dm, rp, cols, kappa, f, host_threads())
+    setup_s = time.perf_counter() - t_start
+    for _ in range(args.warmup):
+        cs.step()
+    times, iters, parts = [], [], []
+    for _ in range(args.steps):
+        sec, it, pt = cs.step()
+        times.append(sec)
+        iters.append(it)
+        parts.append(pt)
+    total = sum(times)
+    value = nn * len(times) / total / 1e9
+    cpu = {"value": value, "unit": UNIT, "cores": cs.threads, "kind": "port",
+           "sample": cs.sample(), "cg_iterations": iters,
+           "seconds_matrix_rhs_solve": [float(np.median([p[i] for p in parts])) for i in range(3)]}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic (seeded)", "config": workload_config(args, nn),
-            "ms_per_step": 1e3 * nn / (value * 1e9) if value else None,
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
-                             "sample": f"{cores} single-thread replicas; each times the oracle's "
-                                       f"matrix+vector cell loops over {sample} cells and 3 "
-                                       f"SpMV passes, extrapolated to a full step with {iters} "
-                                       f"CG iterations (BLAS-1 as 15% of SpMV)"},
+            "data": "synthetic (seeded lognormal kappa, uniform f)",
+            "config": workload_config(args, nn, rp[-1]),
+            "ms_per_step": 1e3 * total / len(times),
+            "cpu_baseline": cpu,
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0},
-            "wall_s": wall}
+            "setup_s": setup_s, "wall_s": time.perf_counter() - t_start}
     print(json.dumps(line))
 
 
@@ -362,8 +375,8 @@ def elasticity_sample(steps=1, warmup=1):
     hexahedra x 6 tetrahedra (331,776 cells, 1,390,179 dofs), E lognormal
     (log 1e3, 0.5) per cell, nu = 0.3, body force (0,0,-1), clamped at x = 0.
     Block (3x3) CSR assembly, expansion to the scalar CSR, then plain FP64
-    Jacobi-PCG and FP32-inner / FP64-outer refinement, both to rtol 1e-10
-    evaluated in FP64."""
+    Jacobi-PCG and FP64 flexible CG with FP32 PCG corrections, both to the
+    step's relative residual evaluated in FP64."""
     import numpy as np
     import torch
 
@@ -382,7 +395,10 @@ def elasticity_sample(steps=1, warmup=1):
     S = A.expand_blocks()
     b = rhs.assemble()
     fp64 = la.OperatorCGSolver(S)
-    ir = la.IRSolver(S, inner_rtol=0.01)
+    # FP32 arithmetic alone stalls on this system (the FP32 recurrence
+    # loses accuracy at the level of its smallest eigenvalue): flexible FP64
+    # CG with FP32 PCG corrections to a 0.1 residual drop each.
+    ir = la.IRSolver(S, variant="flexible", inner_rtol=0.1)
     x = torch.zeros_like(b)
     stream = torch.cuda.current_stream()
 
@@ -392,7 +408,10 @@ def elasticity_sample(steps=1, warmup=1):
         rhs.assemble(b)
         solver.refresh()
         x.zero_()
-        return solver.solve(b, x, rtol=1e-10, raise_on_fail=False)
+        if solver is ir:
+            return solver.solve(b, x, rtol=STEP_RTOL, max_outer=400, max_inner=4000,
+                                raise_on_fail=False)
+        return solver.solve(b, x, rtol=STEP_RTOL, raise_on_fail=False)
 
     out = {"workload": "vector P2 elasticity, box 4x1x1, 96x24x24x6 tets", "cells": m.num_cells,
            "dofs": V.num_dofs, "blocks": A.nnz, "scalar_nnz": S.nnz}
@@ -404,15 +423,25 @@ def elasticity_sample(steps=1, warmup=1):
         out[name] = {"ms_per_step": ms, "gdof_per_s": V.num_dofs / (ms * 1e-3) / 1e9,
                      "iterations": [q.iterations for q in res], "status": r.status,
                      "final_rel_residual": float(np.sqrt(r.rnorm_sq / r.rnorm0_sq))}
+        if name == "mixed":
+            out[name]["outer_iterations"] = [q.outer_iterations for q in res]
+            out[name]["variant"] = "flexible CG (FP64) with FP32 Jacobi-PCG corrections"
         if name == "fp64_plain":
             x64 = x.clone()
     out["rel_err_vs_fp64_solution"] = float((x - x64).norm() / x64.norm())
+    # Both against a converged FP64 solve (rtol 1e-13).
+    fp64.refresh()
+    xt = torch.zeros_like(b)
+    rt = fp64.solve(b, xt, rtol=1e-13, max_iters=40000, raise_on_fail=False)
+    out["rel_err_vs_converged_fp64"] = {"mixed": float((x - xt).norm() / xt.norm()),
+                                        "fp64_plain": float((x64 - xt).norm() / xt.norm()),
+                                        "converged_status": rt.status}
     # A speed-up only means something when both solves reached the tolerance.
     ok = out["fp64_plain"]["status"] == 0 and out["mixed"]["status"] == 0
     out["speedup_of_mixed"] = (out["fp64_plain"]["ms_per_step"] / out["mixed"]["ms_per_step"]
                                if ok else None)
-    out["note"] = ("status 4 = the FP32-valued inner solve stagnated before rtol 1e-10: its "
-                   "entry rounding exceeds the smallest eigenvalue of this system")
+    out["note"] = ("FP32 arithmetic limits an FP32 CG on this system near its smallest "
+                   "eigenvalue, so the FP32 solves act as a preconditioner of FP64 flexible CG")
     return out
 
 
@@ -824,16 +853,29 @@ def run_ours(args):
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(m, kappa, f, P, int(np.median([r.iterations for r in res64])),
-                           args.cpu_sample_cells)
+        cpu = cpu_baseline(m, kappa, f, P)
 
     if rank == 0:
+        config = workload_config(args, n_dofs, nnz)
+        # The accuracy the speed-up is stated at: both timed solutions against
+        # the converged FP64 solution (rtol 1e-13), and the plain FP64 path.
+        config["rel_err_vs_converged_fp64"] = {"mixed": err_mixed_tight,
+                                               "fp64_plain": err_fp64_tight,
+                                               "mixed_vs_fp64_plain": rel_err,
+                                               "within_bound": bool(err_mixed_tight <= ERR_BOUND
+                                                                    and err_fp64_tight
+                                                                    <= ERR_BOUND)}
+        config["fp64_plain_ms_per_step"] = ms64
+        config["speedup_vs_fp64_plain"] = ms64 / ms_max
+        config["cg_iterations"] = {"mixed_fp32_inner": int(np.median([r.inner_iterations
+                                                                       for r in res])),
+                                   "fp64_plain": int(np.median([r.iterations for r in res64]))}
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
                 "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_max,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                 "dtype": "f64 (FP32 inner solve, FP64 residual/update)",
                 "data": "synthetic (seeded lognormal kappa, uniform f)",
-                "config": workload_config(args, n_dofs, nnz),
+                "config": config,
                 "solver": {"path": "FP32-inner / FP64-outer iterative refinement",
                            "variant": args.ir_variant, "inner_rtol": P.ir.inner_rtol,
                            "outer_iterations": [r.outer_iterations for r in res],

@@ -36,6 +36,7 @@ F32 = 1
 
 IR_RESTART = 0
 IR_RELIABLE = 1
+IR_FLEXIBLE = 2
 
 
 class DfxError(RuntimeError):

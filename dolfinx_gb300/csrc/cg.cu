@@ -745,6 +745,177 @@ __global__ void k_ir_correct(double* __restrict__ x, float* __restrict__ d, int6
   }
 }
 
+// ---- Flexible CG outer loop (DFX_IR_FLEXIBLE). The outer iteration is
+// FP64 CG in which the preconditioned residual z is the inner FP32 PCG's
+// correction d ~ A^{-1} r; since that correction depends nonlinearly on r,
+// each new direction is A-orthogonalised against the previous one
+// explicitly (truncated flexible CG, one stored direction):
+//   p = z - (z.q_old / p_old.q_old) p_old,  q = A p,
+//   alpha = p.r / p.q,  x += alpha p,  r -= alpha q.
+// All outer vectors, products and scalars are FP64; the outer stopping test
+// is the FP64 recursive residual, confirmed by the true residual b - A x.
+
+// r = b - A x in FP64 (kept in r64 and handed to the inner solve in FP32),
+// |r|^2; `first` sets |r0|^2. done = 1 when |r|^2 / |r0|^2 < rtol^2.
+__global__ void __launch_bounds__(kSellThreads)
+    k_fcg_residual(const dfx_operator_s op, const double* __restrict__ b,
+                   const double* __restrict__ x, double* __restrict__ r64,
+                   float* __restrict__ r32, CgState* st, Red red, int first)
+{
+  block_reduce_init();
+
+  const int lane = threadIdx.x & 31;
+  const dfx::SliceRange sr = dfx::block_slices(op.nslices);
+  double rr = 0.0;
+  for (int32_t s = sr.begin; s < sr.end; s += sr.step)
+  {
+    const double ax = dfx::sell_row<double, double, double, false>(op, (const double*)op.vals, x,
+                                                                   s, lane);
+    const int32_t row = 32 * s + lane;
+    if (row < op.n)
+    {
+      const double r = b[row] - ax;
+      r64[row] = r;
+      r32[row] = (float)r;
+      rr += r * r;
+    }
+  }
+  const WarpFinal f = publish<double>(rr, 0.0, red, &st->ticket[3], false);
+  if (f.last && lane == 0)
+  {
+    const double srr = f.s0;
+    if (first)
+      st->rr0 = srr;
+    st->rr = srr;
+    st->status = DFX_OK;
+    st->done = 0;
+    if (srr == 0.0 || srr / st->rr0 < st->rtol2)
+      st->done = 1;
+    else if (!isfinite(srr))
+    {
+      st->status = DFX_ERR_BREAKDOWN;
+      st->done = 1;
+    }
+    st->ticket[3] = 0;
+    __threadfence();
+  }
+}
+
+// gamma = z.q_old with z = d; beta = gamma / (p_old.q_old).
+__global__ void __launch_bounds__(kElemThreads)
+    k_fcg_gamma(const float* __restrict__ d, const double* __restrict__ q, int64_t n, CgState* st,
+                Red red)
+{
+  block_reduce_init();
+
+  double g = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    g += (double)d[i] * q[i];
+  const WarpFinal f = publish<double>(g, 0.0, red, &st->ticket[0], false);
+  if (f.last && (threadIdx.x & 31) == 0)
+  {
+    st->beta = f.s0 / st->pAp;
+    st->ticket[0] = 0;
+    __threadfence();
+  }
+}
+
+// p = d - beta p_old (first direction: p = d).
+__global__ void k_fcg_direction(const float* __restrict__ d, double* __restrict__ p, int64_t n,
+                                const CgState* st, int first)
+{
+  const double beta = first ? 0.0 : __ldg(&st->beta);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = first ? (double)d[i] : (double)d[i] - beta * p[i];
+}
+
+// q = A p with the FP64 operator, p.q and p.r; alpha = p.r / p.q.
+__global__ void __launch_bounds__(kSellThreads)
+    k_fcg_spmv(const dfx_operator_s op, const double* __restrict__ p, double* __restrict__ q,
+               const double* __restrict__ r, CgState* st, Red red)
+{
+  block_reduce_init();
+
+  const int lane = threadIdx.x & 31;
+  const dfx::SliceRange sr = dfx::block_slices(op.nslices);
+  double pq = 0.0, pr = 0.0;
+  for (int32_t s = sr.begin; s < sr.end; s += sr.step)
+  {
+    const double ap = dfx::sell_row<double, double, double, false>(op, (const double*)op.vals, p,
+                                                                   s, lane);
+    const int32_t row = 32 * s + lane;
+    if (row < op.n)
+    {
+      q[row] = ap;
+      const double pv = p[row];
+      pq += pv * ap;
+      pr += pv * r[row];
+    }
+  }
+  const WarpFinal f = publish<double>(pq, pr, red, &st->ticket[1], true);
+  if (f.last && lane == 0)
+  {
+    st->pAp = f.s0;
+    if (!(f.s0 > 0.0) || !isfinite(f.s0) || !isfinite(f.s1))
+    {
+      st->alpha = 0.0;
+      st->status = DFX_ERR_BREAKDOWN;
+      st->done = 1;
+    }
+    else
+      st->alpha = f.s1 / f.s0;
+    st->ticket[1] = 0;
+    __threadfence();
+  }
+}
+
+// x += alpha p, r -= alpha q, |r|^2, r handed to the inner solve in FP32;
+// convergence test on the recursive FP64 residual.
+__global__ void __launch_bounds__(kElemThreads)
+    k_fcg_update(double* __restrict__ x, double* __restrict__ r, const double* __restrict__ p,
+                 const double* __restrict__ q, float* __restrict__ r32, int64_t n, CgState* st,
+                 Red red)
+{
+  block_reduce_init();
+
+  if (is_done(st))
+    return;
+  const double alpha = __ldg(&st->alpha);
+  double rr = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+  {
+    x[i] += alpha * p[i];
+    const double rn = r[i] - alpha * q[i];
+    r[i] = rn;
+    r32[i] = (float)rn;
+    rr += rn * rn;
+  }
+  const WarpFinal f = publish<double>(rr, 0.0, red, &st->ticket[2], false);
+  if (f.last && (threadIdx.x & 31) == 0)
+  {
+    const double srr = f.s0;
+    st->rr = srr;
+    st->iter += 1;
+    if (srr / st->rr0 < st->rtol2)
+      st->done = 1;
+    else if (!isfinite(srr))
+    {
+      st->status = DFX_ERR_BREAKDOWN;
+      st->done = 1;
+    }
+    else if (st->iter >= st->max_iter)
+    {
+      st->status = DFX_ERR_NOT_CONVERGED;
+      st->done = 1;
+    }
+    st->ticket[2] = 0;
+    __threadfence();
+  }
+}
+
 // Last warp of a residual replacement: the replaced |r|^2 and r.z decide
 // whether the solve has converged, and give beta.
 __device__ __forceinline__ void rel_finish(const WarpFinal& f, CgState* st)
@@ -1194,6 +1365,9 @@ size_t ir_work_bytes(int64_t n)
   c.take<double>(n); // dinv (unused FP64 copy kept for symmetry with op solve)
   c.take<float>(n);  // d
   c.take<float>(n);  // dinv32
+  c.take<double>(n); // flexible outer loop: r
+  c.take<double>(n); // p
+  c.take<double>(n); // q = A p
   return c.used;
 }
 
@@ -1321,8 +1495,9 @@ extern "C" int dfx_ir_solve(dfx_operator op64, dfx_operator op32, const double* 
     return st;
   DFX_REQUIRE(inner_rtol > 0.0 && inner_rtol < 1.0 && max_inner > 0,
               "inner_rtol must be in (0, 1) and max_inner positive");
-  DFX_REQUIRE(variant == DFX_IR_RESTART || variant == DFX_IR_RELIABLE, "unknown variant %d",
-              variant);
+  DFX_REQUIRE(variant == DFX_IR_RESTART || variant == DFX_IR_RELIABLE
+                  || variant == DFX_IR_FLEXIBLE,
+              "unknown variant %d", variant);
   const int64_t n = op64->n;
   DFX_REQUIRE(wbytes >= ir_work_bytes(n), "workspace too small (%zu < %zu)", wbytes,
               ir_work_bytes(n));
@@ -1341,6 +1516,9 @@ extern "C" int dfx_ir_solve(dfx_operator op64, dfx_operator op32, const double* 
   c.take<double>(n);
   float* d32 = c.take<float>(n);
   float* dinv32 = d_dinv ? c.take<float>(n) : nullptr;
+  double* r64 = c.take<double>(n);
+  double* p64 = c.take<double>(n);
+  double* q64 = c.take<double>(n);
   const unsigned g = (unsigned)((n + 255) / 256);
   k_gather<double, double><<<g, 256, 0, s>>>(d_x, xp, op64->perm, (int32_t)n);
   k_gather<double, double><<<g, 256, 0, s>>>(d_b, bp, op64->perm, (int32_t)n);
@@ -1348,6 +1526,7 @@ extern "C" int dfx_ir_solve(dfx_operator op64, dfx_operator op32, const double* 
     k_gather<double, float><<<g, 256, 0, s>>>(d_dinv, dinv32, op64->perm, (int32_t)n);
   DFX_CHECK_LAUNCH();
   const bool reliable = variant == DFX_IR_RELIABLE;
+  const bool flexible = variant == DFX_IR_FLEXIBLE;
   OpRef o{kSell, nullptr, op32};
   cudaGraphExec_t exec;
   if (int st = iteration_graph<float>(o, d32, dinv32, n, w, K, reliable, &exec))
@@ -1357,7 +1536,69 @@ extern "C" int dfx_ir_solve(dfx_operator op64, dfx_operator op32, const double* 
   int64_t kernels = 2 + (dinv32 ? 1 : 0);
   CgState* h = nullptr;
   CgState ho{};
-  if (!reliable)
+  if (flexible)
+  {
+    // Flexible CG: each outer iteration takes the inner FP32 PCG solve of
+    // A d = r (to inner_rtol, at most max_inner iterations) as its
+    // preconditioned residual. A converged recursive residual is confirmed
+    // by the true residual; if that disagrees, the outer loop restarts from
+    // it.
+    if (int e = reset_work(outer, ored, w.blocks, s))
+      return e;
+    if (int e = reset_work(w.st, w.red, w.blocks, s))
+      return e;
+    k_state_init<<<1, 1, 0, s>>>(outer, rtol * rtol, 0.0, max_outer, 0);
+    const int eg = elem_grid(n);
+    auto true_residual = [&](int first) -> int
+    {
+      k_fcg_residual<<<sell_blocks(n), kSellThreads, 0, s>>>(*op64, bp, xp, r64, w.r, outer,
+                                                             ored, first);
+      DFX_CHECK_LAUNCH();
+      kernels += 1;
+      return read_state(outer, &h, s);
+    };
+    kernels += 1;
+    bool restart = true;
+    if (!(st = true_residual(1)) && !h->done)
+    {
+      for (;;)
+      {
+        enqueue_init<float>(w.r, nullptr, d32, dinv32, n, w, inner_rtol, max_inner, s);
+        DFX_CHECK_LAUNCH();
+        kernels += 1;
+        if ((st = run_to_done(exec, w.st, max_inner, K, &h, s, &kernels)))
+          break;
+        inner_total += h->iter;
+        if (!restart)
+        {
+          k_fcg_gamma<<<eg, kElemThreads, 0, s>>>(d32, q64, n, outer, ored);
+          kernels += 1;
+        }
+        k_fcg_direction<<<blocks, kThreads, 0, s>>>(d32, p64, n, outer, restart ? 1 : 0);
+        k_fcg_spmv<<<sell_blocks(n), kSellThreads, 0, s>>>(*op64, p64, q64, r64, outer, ored);
+        k_fcg_update<<<eg, kElemThreads, 0, s>>>(xp, r64, p64, q64, w.r, n, outer, ored);
+        DFX_CHECK_LAUNCH();
+        kernels += 3;
+        if ((st = read_state(outer, &h, s)))
+          break;
+        restart = false;
+        if (h->done)
+        {
+          if (h->status != DFX_OK)
+            break;
+          if ((st = true_residual(0)) || h->done)
+            break;
+          restart = true; // the recursive residual drifted: restart from b - A x
+        }
+      }
+    }
+    if (h)
+    {
+      ho = *h;
+      outer_count = ho.iter;
+    }
+  }
+  else if (!reliable)
   {
     // Restarted refinement: each correction is a fresh FP32 PCG solve.
     if (int e = reset_work(outer, ored, w.blocks, s))

@@ -373,13 +373,15 @@ class IRSolver:
     def __init__(self, A: MatrixCSR, jacobi: bool = True, graph_iters: int = 20,
                  sigma: int = 256, inner_rtol: float | None = None, compress_cols: bool = True,
                  variant: str = "reliable"):
-        self.variant = {"restart": _capi.IR_RESTART, "reliable": _capi.IR_RELIABLE}[variant]
+        self.variant = {"restart": _capi.IR_RESTART, "reliable": _capi.IR_RELIABLE,
+                        "flexible": _capi.IR_FLEXIBLE}[variant]
         if inner_rtol is None:
             # Reliable updates: replace the residual each time |r| drops by this
             # factor. On the P2 Poisson problem of a 64^3 x 6 mesh the inner
             # iteration count does not depend on it (~1,360 from 0.3 down to 0.01),
-            # and 0.03 needs the fewest FP64 replacements.
-            inner_rtol = 0.03 if self.variant == _capi.IR_RELIABLE else 1e-4
+            # and 0.03 needs the fewest FP64 replacements. Flexible CG: each
+            # inner FP32 solve reduces its residual by this factor.
+            inner_rtol = {_capi.IR_RELIABLE: 0.03, _capi.IR_FLEXIBLE: 0.1}.get(self.variant, 1e-4)
         self.A = A
         self.op64 = SellOperator(A, torch.float64, sigma)
         self.op32 = SellOperator(A, torch.float32, sigma, compress_cols=compress_cols)

@@ -483,13 +483,21 @@ int dfx_cg_solve_op(dfx_operator op, const double* d_b, double* d_x,
  *                    (reliable updates); x += d in FP64 at each replacement,
  *                    the search direction is kept; max_outer caps the
  *                    replacements, max_inner the FP32 iterations.
+ *   DFX_IR_FLEXIBLE: FP64 flexible CG (one stored direction) whose
+ *                    preconditioner is an FP32 PCG solve of A d = r to
+ *                    inner_rtol (at most max_inner iterations each); the
+ *                    outer vectors, products and update stay FP64. It
+ *                    converges where the FP32 recurrence alone stalls
+ *                    (FP32 rounding comparable to the smallest eigenvalue);
+ *                    max_outer caps the outer iterations.
  * Stops when |b - A x|^2 / |b - A x0|^2 < rtol^2 evaluated in FP64 -- the
  * stopping test of dfx_cg_solve. op64 and op32 must be built from the same
  * matrix with the same sigma. */
 enum dfx_ir_variant
 {
   DFX_IR_RESTART = 0,
-  DFX_IR_RELIABLE = 1
+  DFX_IR_RELIABLE = 1,
+  DFX_IR_FLEXIBLE = 2
 };
 typedef struct dfx_ir_info
 {

@@ -18,6 +18,7 @@
 // golden vectors under tests/golden/.
 
 #include <algorithm>
+#include <chrono>
 #include <array>
 #include <cmath>
 #include <cstdint>
@@ -649,6 +650,58 @@ struct orc_form
   double nu;           // Poisson ratio, elasticity
 };
 
+// One cell of the matrix cell loop (cpp/dolfinx/fem/assemble_matrix_impl.h:
+// 92-200): coordinates, element tensor, BC rows/columns zeroed, insertion
+// by binary search (cpp/dolfinx/la/matrix_csr_impl.h:67-109). Ae holds
+// (nd bs)^2 scratch values.
+static int matrix_cell(const orc_form* form, int c, const int32_t* x_dofmap, const double* x,
+                const int32_t* dofmap, const int8_t* bc, const int64_t* row_ptr,
+                const int32_t* cols, double* vals, double* Ae)
+{
+  const int nd = tet_ndofs(form->degree);
+  const int bs = form->kind == 1 ? 3 : 1;
+  const int n = nd * bs;
+  double coords[12];
+  for (int v = 0; v < 4; ++v)
+    for (int k = 0; k < 3; ++k)
+      coords[3 * v + k] = x[3 * (int64_t)x_dofmap[4 * (int64_t)c + v] + k];
+  std::fill_n(Ae, n * n, 0.0);
+  const double kap = form->kappa ? form->kappa[c] : 1.0;
+  if (form->kind == 0)
+    kernel_poisson(form->degree, Ae, kap, form->k2, coords);
+  else
+    kernel_elasticity(Ae, kap, form->nu, coords);
+  const int32_t* dofs = dofmap + (int64_t)nd * c;
+  if (bc)
+  {
+    for (int i = 0; i < nd; ++i)
+      for (int k = 0; k < bs; ++k)
+        if (bc[bs * dofs[i] + k])
+        {
+          std::fill_n(Ae + n * (bs * i + k), n, 0.0);
+          for (int r = 0; r < n; ++r)
+            Ae[r * n + bs * i + k] = 0.0;
+        }
+  }
+  for (int i = 0; i < nd; ++i)
+  {
+    const int32_t row = dofs[i];
+    const int32_t* c0 = cols + row_ptr[row];
+    const int32_t* c1 = cols + row_ptr[row + 1];
+    for (int j = 0; j < nd; ++j)
+    {
+      const int32_t* it = std::lower_bound(c0, c1, dofs[j]);
+      if (it == c1 || *it != dofs[j])
+        return ORC_ERR_NOT_IN_SPARSITY;
+      const int64_t d = (it - cols) * bs * bs;
+      for (int a = 0; a < bs; ++a)
+        for (int b = 0; b < bs; ++b)
+          vals[d + a * bs + b] += Ae[(bs * i + a) * n + bs * j + b];
+    }
+  }
+  return ORC_OK;
+}
+
 // Matrix cell loop (cpp/dolfinx/fem/assemble_matrix_impl.h:92-200) with
 // insertion by binary search (cpp/dolfinx/la/matrix_csr_impl.h:67-109).
 // dofmap holds node (block) indices; bc is indexed by bs*node + k.
@@ -657,51 +710,11 @@ int orc_assemble_matrix(const orc_form* form, int nc, const int32_t* x_dofmap,
                         const int8_t* bc, const int64_t* row_ptr,
                         const int32_t* cols, double* vals)
 {
-  const int nd = tet_ndofs(form->degree);
-  const int bs = form->kind == 1 ? 3 : 1;
-  const int n = nd * bs;
+  const int n = tet_ndofs(form->degree) * (form->kind == 1 ? 3 : 1);
   std::vector<double> Ae(n * n);
-  double coords[12];
   for (int c = 0; c < nc; ++c)
-  {
-    for (int v = 0; v < 4; ++v)
-      for (int k = 0; k < 3; ++k)
-        coords[3 * v + k] = x[3 * (int64_t)x_dofmap[4 * c + v] + k];
-    std::fill(Ae.begin(), Ae.end(), 0.0);
-    const double kap = form->kappa ? form->kappa[c] : 1.0;
-    if (form->kind == 0)
-      kernel_poisson(form->degree, Ae.data(), kap, form->k2, coords);
-    else
-      kernel_elasticity(Ae.data(), kap, form->nu, coords);
-    const int32_t* dofs = dofmap + (int64_t)nd * c;
-    if (bc)
-    {
-      for (int i = 0; i < nd; ++i)
-        for (int k = 0; k < bs; ++k)
-          if (bc[bs * dofs[i] + k])
-          {
-            std::fill_n(Ae.begin() + n * (bs * i + k), n, 0.0);
-            for (int r = 0; r < n; ++r)
-              Ae[r * n + bs * i + k] = 0.0;
-          }
-    }
-    for (int i = 0; i < nd; ++i)
-    {
-      const int32_t row = dofs[i];
-      const int32_t* c0 = cols + row_ptr[row];
-      const int32_t* c1 = cols + row_ptr[row + 1];
-      for (int j = 0; j < nd; ++j)
-      {
-        const int32_t* it = std::lower_bound(c0, c1, dofs[j]);
-        if (it == c1 || *it != dofs[j])
-          return ORC_ERR_NOT_IN_SPARSITY;
-        const int64_t d = (it - cols) * bs * bs;
-        for (int a = 0; a < bs; ++a)
-          for (int b = 0; b < bs; ++b)
-            vals[d + a * bs + b] += Ae[(bs * i + a) * n + bs * j + b];
-      }
-    }
-  }
+    if (int st = matrix_cell(form, c, x_dofmap, x, dofmap, bc, row_ptr, cols, vals, Ae.data()))
+      return st;
   return ORC_OK;
 }
 
@@ -1320,5 +1333,321 @@ double orc_assemble_scalar(int kind, int degree, int nc, const int32_t* x_dofmap
     }
   }
   return value;
+}
+} // extern "C"
+
+//---------------------------------------------------------------------------
+// One full step of the P2 Poisson benchmark workload on host threads: the
+// CPU baseline timed beside the GPU. The reference assembles serially per
+// MPI rank; here the same per-cell work (matrix_cell, the vector and
+// lifting loops above) is shared by a thread team in colour classes --
+// cells of one class share no dof, so no two threads add into the same
+// entry -- and the solve is the demo's CG (cpp/demo/poisson_matrix_free/
+// main.cpp:84-132) with Jacobi preconditioning, rows split across the
+// threads and dot products summed per thread, then over the threads in
+// index order (the result does not depend on thread timing).
+//---------------------------------------------------------------------------
+#include <barrier>
+#include <thread>
+
+namespace
+{
+// Element vector of the P1-coefficient source on cell c (the vector cell
+// loop of orc_assemble_vector, one cell).
+void vector_cell(int degree, int c, const int32_t* x_dofmap, const double* x,
+                 const int32_t* dofmap, const double* f, double* b)
+{
+  const int nd = tet_ndofs(degree);
+  double be[30], coords[12], fc[4];
+  for (int v = 0; v < 4; ++v)
+  {
+    for (int k = 0; k < 3; ++k)
+      coords[3 * v + k] = x[3 * (int64_t)x_dofmap[4 * (int64_t)c + v] + k];
+    fc[v] = f ? f[x_dofmap[4 * (int64_t)c + v]] : 1.0;
+  }
+  std::fill_n(be, 30, 0.0);
+  kernel_source(degree, be, fc, coords);
+  const int32_t* dofs = dofmap + (int64_t)nd * c;
+  for (int i = 0; i < nd; ++i)
+    b[dofs[i]] += be[i];
+}
+
+// Lifting of one scalar cell with homogeneous-or-not BC values g (the
+// loop body of orc_apply_lifting, x0 = 0, alpha = 1).
+void lifting_cell(const orc_form* form, int c, const int32_t* x_dofmap, const double* x,
+                  const int32_t* dofmap, const int8_t* bc, const double* g, double* b,
+                  double* Ae)
+{
+  const int nd = tet_ndofs(form->degree);
+  const int32_t* dofs = dofmap + (int64_t)nd * c;
+  bool has = false;
+  for (int i = 0; i < nd && !has; ++i)
+    has = bc[dofs[i]] != 0;
+  if (!has)
+    return;
+  double coords[12];
+  for (int v = 0; v < 4; ++v)
+    for (int k = 0; k < 3; ++k)
+      coords[3 * v + k] = x[3 * (int64_t)x_dofmap[4 * (int64_t)c + v] + k];
+  std::fill_n(Ae, nd * nd, 0.0);
+  kernel_poisson(form->degree, Ae, form->kappa ? form->kappa[c] : 1.0, form->k2, coords);
+  for (int j = 0; j < nd; ++j)
+  {
+    if (!bc[dofs[j]])
+      continue;
+    const double gj = g ? g[dofs[j]] : 0.0;
+    for (int i = 0; i < nd; ++i)
+      b[dofs[i]] -= Ae[i * nd + j] * gj;
+  }
+}
+
+double now_s()
+{
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch())
+      .count();
+}
+} // namespace
+
+extern "C"
+{
+// Greedy first-fit colouring of the cells in cell order: no two cells of a
+// colour share a dof. order: (nc) cells grouped by colour; offsets:
+// (max_colours + 1). Returns the number of colours, or -1 when more than
+// min(max_colours, 256) are needed.
+int orc_colour_cells(int nc, int nd, const int32_t* dofmap, int ndofs, int32_t* order,
+                     int32_t* offsets, int max_colours)
+{
+  const int cap = std::min(max_colours, 256);
+  std::vector<std::array<uint64_t, 4>> used(ndofs, {0, 0, 0, 0});
+  std::vector<int32_t> colour(nc);
+  int ncol = 0;
+  for (int c = 0; c < nc; ++c)
+  {
+    std::array<uint64_t, 4> m{0, 0, 0, 0};
+    for (int i = 0; i < nd; ++i)
+      for (int w = 0; w < 4; ++w)
+        m[w] |= used[dofmap[(int64_t)nd * c + i]][w];
+    int col = -1;
+    for (int w = 0; w < 4 && col < 0; ++w)
+      if (~m[w])
+        col = 64 * w + __builtin_ctzll(~m[w]);
+    if (col < 0 || col >= cap)
+      return -1;
+    colour[c] = col;
+    ncol = std::max(ncol, col + 1);
+    for (int i = 0; i < nd; ++i)
+      used[dofmap[(int64_t)nd * c + i]][col >> 6] |= uint64_t(1) << (col & 63);
+  }
+  std::fill_n(offsets, ncol + 1, 0);
+  for (int c = 0; c < nc; ++c)
+    ++offsets[colour[c] + 1];
+  for (int k = 0; k < ncol; ++k)
+    offsets[k + 1] += offsets[k];
+  std::vector<int32_t> pos(offsets, offsets + ncol);
+  for (int c = 0; c < nc; ++c)
+    order[pos[colour[c]]++] = c;
+  return ncol;
+}
+
+// One step of the scalar Poisson workload on `nthreads` threads: A = 0,
+// matrix cell loop, A[d, d] = 1 on the constrained dofs, b = 0, vector cell
+// loop (P1 coefficient f), lifting with BC values g, b[d] = g[d] on the
+// constrained dofs, then Jacobi-PCG from u = 0 to |r|/|r0| < rtol. The
+// colour classes (corder, coff, ncol) come from orc_colour_cells.
+// seconds[0..2] receive the matrix, right-hand side and solve times.
+// Returns the CG iteration count (negative: not converged in kmax), or
+// -1000000 - status on an insertion error.
+int orc_poisson_step_threaded(const orc_form* form, int nc, const int32_t* x_dofmap,
+                              const double* x, const int32_t* dofmap, int ndofs,
+                              const int8_t* bc, int nbc, const int32_t* bc_dofs,
+                              const double* g, const double* f, const int64_t* row_ptr,
+                              const int32_t* cols, double* vals, double* b, double* u,
+                              const int32_t* corder, const int32_t* coff, int ncol, double rtol,
+                              int kmax, int nthreads, double* seconds)
+{
+  const int T = std::max(1, nthreads);
+  const int64_t n = ndofs;
+  const int64_t nnz = row_ptr[n];
+  const int nd = tet_ndofs(form->degree);
+  std::vector<double> r(n), p(n), y(n), dinv(n);
+  // Row blocks with about nnz / T entries each.
+  std::vector<int64_t> rb(T + 1, n);
+  rb[0] = 0;
+  {
+    int t = 1;
+    for (int64_t i = 0; i < n && t < T; ++i)
+      if (row_ptr[i] >= nnz * t / T)
+        rb[t++] = i;
+  }
+  struct alignas(64) Part
+  {
+    double v[3];
+    int err;
+  };
+  std::vector<Part> part(T);
+  std::barrier sync(T);
+  double t0 = now_s(), t1 = 0, t2 = 0, t3 = 0;
+  int result = 0;
+  auto work = [&](int t)
+  {
+    std::vector<double> Ae(nd * nd);
+    auto range = [&](int64_t lo, int64_t hi, int64_t& a, int64_t& e)
+    {
+      a = lo + (hi - lo) * t / T;
+      e = lo + (hi - lo) * (t + 1) / T;
+    };
+    int64_t a, e;
+    // ---- matrix
+    range(0, nnz, a, e);
+    std::fill(vals + a, vals + e, 0.0);
+    part[t].err = 0;
+    sync.arrive_and_wait();
+    for (int k = 0; k < ncol; ++k)
+    {
+      range(coff[k], coff[k + 1], a, e);
+      for (int64_t q = a; q < e; ++q)
+        if (int st = matrix_cell(form, corder[q], x_dofmap, x, dofmap, bc, row_ptr, cols, vals,
+                                 Ae.data()))
+          part[t].err = st;
+      sync.arrive_and_wait();
+    }
+    if (t == 0)
+    {
+      for (int i = 0; i < nbc; ++i)
+      {
+        const int32_t d = bc_dofs[i];
+        const int32_t* c0 = cols + row_ptr[d];
+        const int32_t* c1 = cols + row_ptr[d + 1];
+        const int32_t* it = std::lower_bound(c0, c1, d);
+        if (it == c1 || *it != d)
+          part[0].err = ORC_ERR_NOT_IN_SPARSITY;
+        else
+          vals[it - cols] = 1.0;
+      }
+      t1 = now_s();
+    }
+    // ---- right-hand side
+    range(0, n, a, e);
+    std::fill(b + a, b + e, 0.0);
+    sync.arrive_and_wait();
+    for (int k = 0; k < ncol; ++k)
+    {
+      range(coff[k], coff[k + 1], a, e);
+      for (int64_t q = a; q < e; ++q)
+        vector_cell(form->degree, corder[q], x_dofmap, x, dofmap, f, b);
+      sync.arrive_and_wait();
+    }
+    for (int k = 0; k < ncol; ++k)
+    {
+      range(coff[k], coff[k + 1], a, e);
+      for (int64_t q = a; q < e; ++q)
+        lifting_cell(form, corder[q], x_dofmap, x, dofmap, bc, g, b, Ae.data());
+      sync.arrive_and_wait();
+    }
+    if (t == 0)
+    {
+      for (int i = 0; i < nbc; ++i)
+        b[bc_dofs[i]] = g ? g[bc_dofs[i]] : 0.0;
+      t2 = now_s();
+    }
+    sync.arrive_and_wait();
+    // ---- Jacobi-PCG, u0 = 0: r = b, z = D^{-1} r, p = z
+    const int64_t r0 = rb[t], r1 = rb[t + 1];
+    double rr = 0, rz = 0;
+    for (int64_t i = r0; i < r1; ++i)
+    {
+      double dg = 0.0;
+      for (int64_t j = row_ptr[i]; j < row_ptr[i + 1]; ++j)
+        if (cols[j] == i)
+          dg = vals[j];
+      dinv[i] = 1.0 / dg;
+      u[i] = 0.0;
+      r[i] = b[i];
+      p[i] = dinv[i] * r[i];
+      rr += r[i] * r[i];
+      rz += r[i] * p[i];
+    }
+    part[t].v[0] = rr;
+    part[t].v[1] = rz;
+    sync.arrive_and_wait();
+    auto total = [&](int which)
+    {
+      double s = 0.0;
+      for (int q = 0; q < T; ++q)
+        s += part[q].v[which];
+      return s;
+    };
+    const double rr0 = total(0);
+    double rzo = total(1);
+    int k = 0;
+    int out = 0;
+    if (rr0 == 0.0)
+      out = 0;
+    else
+      for (;;)
+      {
+        if (k >= kmax)
+        {
+          out = -k;
+          break;
+        }
+        ++k;
+        sync.arrive_and_wait(); // p complete, every thread has read the totals
+        double py = 0;
+        for (int64_t i = r0; i < r1; ++i)
+        {
+          double vi = 0.0;
+          for (int64_t j = row_ptr[i]; j < row_ptr[i + 1]; ++j)
+            vi += vals[j] * p[cols[j]];
+          y[i] = vi;
+          py += p[i] * vi;
+        }
+        part[t].v[2] = py;
+        sync.arrive_and_wait();
+        const double alpha = rzo / total(2);
+        double rrn = 0, rzn = 0;
+        for (int64_t i = r0; i < r1; ++i)
+        {
+          u[i] += alpha * p[i];
+          r[i] -= alpha * y[i];
+          rrn += r[i] * r[i];
+          rzn += r[i] * dinv[i] * r[i];
+        }
+        part[t].v[0] = rrn;
+        part[t].v[1] = rzn;
+        sync.arrive_and_wait();
+        const double rrt = total(0), rzt = total(1);
+        if (rrt / rr0 < rtol * rtol)
+        {
+          out = k;
+          break;
+        }
+        const double beta = rzt / rzo;
+        rzo = rzt;
+        for (int64_t i = r0; i < r1; ++i)
+          p[i] = dinv[i] * r[i] + beta * p[i];
+      }
+    if (t == 0)
+    {
+      t3 = now_s();
+      result = out;
+    }
+  };
+  std::vector<std::thread> team;
+  for (int t = 1; t < T; ++t)
+    team.emplace_back(work, t);
+  work(0);
+  for (auto& th : team)
+    th.join();
+  for (int t = 0; t < T; ++t)
+    if (part[t].err)
+      return -1000000 - part[t].err;
+  if (seconds)
+  {
+    seconds[0] = t1 - t0;
+    seconds[1] = t2 - t1;
+    seconds[2] = t3 - t2;
+  }
+  return result;
 }
 } // extern "C"

@@ -19,7 +19,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "liboracle.so")
 REFLIB = os.path.join(HERE, "_ref", "libdfxref.so")
-REF_SRC = "/root/reference"
+# The DOLFINx source tree the reference pieces are compiled from; absent on
+# hosts that only run the prebuilt oracle.
+REF_SRC = os.environ.get("DOLFINX_SOURCE_DIR", "/root/reference")
 
 _i32p = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")
 _i64p = np.ctypeslib.ndpointer(np.int64, flags="C_CONTIGUOUS")
@@ -91,6 +93,11 @@ def lib():
         L.orc_assemble_scalar.argtypes = [C.c_int, C.c_int, C.c_int, _i32p, _f64p, _i32p,
                                           C.c_void_p, C.c_double, C.c_void_p, _f64p]
         L.orc_assemble_scalar.restype = C.c_double
+        L.orc_colour_cells.argtypes = [C.c_int, C.c_int, _i32p, C.c_int, _i32p, _i32p, C.c_int]
+        L.orc_poisson_step_threaded.argtypes = [
+            C.POINTER(_Form), C.c_int, _i32p, _f64p, _i32p, C.c_int, _i8p, C.c_int, _i32p,
+            C.c_void_p, C.c_void_p, _i64p, _i32p, _f64p, _f64p, _f64p, _i32p, _i32p, C.c_int,
+            C.c_double, C.c_int, C.c_int, _f64p]
         _lib = L
     return _lib
 
@@ -367,3 +374,43 @@ def assemble_scalar(kind, degree, cells, x, dofmap, u, kappa=None, k2=0.0, f=Non
     return lib().orc_assemble_scalar(kind, degree, cells.shape[0], np.ascontiguousarray(cells), x,
                                      np.ascontiguousarray(dofmap), _ptr(kap), float(k2), _ptr(fa),
                                      np.ascontiguousarray(u, np.float64))
+
+
+def colour_cells(dofmap, ndofs, max_colours=256):
+    """Greedy first-fit cell colouring in cell order (no two cells of a
+    colour share a dof): (order, offsets) of the colour classes."""
+    dm = np.ascontiguousarray(dofmap, np.int32)
+    order = np.empty(dm.shape[0], np.int32)
+    off = np.zeros(max_colours + 1, np.int32)
+    k = lib().orc_colour_cells(dm.shape[0], dm.shape[1], dm, int(ndofs), order, off, max_colours)
+    if k < 0:
+        raise RuntimeError("cell colouring needs more than %d colours" % max_colours)
+    return order, off[:k + 1].copy()
+
+
+def poisson_step_threaded(degree, cells, x, dofmap, ndofs, bc_dofs, row_ptr, cols, colours,
+                          kappa=None, f=None, g=None, rtol=1e-10, kmax=100000, threads=1,
+                          vals=None, b=None, u=None):
+    """One full step of the scalar Poisson workload on host threads (matrix,
+    right-hand side with lifting and set_bc, Jacobi-PCG from zero). Returns
+    (iterations, seconds[matrix, rhs, solve], vals, b, u)."""
+    nc = cells.shape[0]
+    kap = None if kappa is None else np.ascontiguousarray(kappa, np.float64)
+    form = _form(0, degree, kap, 0.0, 0.3)
+    bcd = np.ascontiguousarray(bc_dofs, np.int32)
+    mk = np.zeros(ndofs, np.int8)
+    mk[bcd] = 1
+    fa = None if f is None else np.ascontiguousarray(f, np.float64)
+    ga = None if g is None else np.ascontiguousarray(g, np.float64)
+    vals = np.empty(cols.size) if vals is None else vals
+    b = np.empty(ndofs) if b is None else b
+    u = np.empty(ndofs) if u is None else u
+    order, off = colours
+    sec = np.zeros(3)
+    it = lib().orc_poisson_step_threaded(
+        C.byref(form), nc, np.ascontiguousarray(cells), x, np.ascontiguousarray(dofmap),
+        int(ndofs), mk, bcd.size, bcd, _ptr(ga), _ptr(fa), row_ptr, cols, vals, b, u, order,
+        off, off.size - 1, float(rtol), int(kmax), int(threads), sec)
+    if it <= -1000000:
+        raise RuntimeError("Entry not in sparsity")
+    return it, sec, vals, b, u

@@ -239,7 +239,8 @@ def test_cg_vector_and_scalar_elementwise_paths(cuda, oracle, capi):
 
 
 @pytest.mark.parametrize("variant,inner_rtol", [("restart", 1e-3), ("restart", 1e-5),
-                                                 ("reliable", 0.1), ("reliable", 0.01)])
+                                                 ("reliable", 0.1), ("reliable", 0.01),
+                                                 ("flexible", 0.1), ("flexible", 0.3)])
 def test_iterative_refinement_reaches_fp64(cuda, oracle, capi, variant, inner_rtol):
     """FP32-inner refinement meets the FP64 stopping test (|r|/|r0| < 1e-10
     in FP64) and agrees with the plain FP64 CG solution to the accuracy
@@ -278,7 +279,7 @@ def test_block_expansion_and_elasticity_refinement(cuda, oracle, capi):
     x = torch.from_numpy(np.random.default_rng(0).standard_normal(V.num_dofs)).cuda()
     assert_close(S.matvec(x).cpu().numpy(), A.matvec(x).cpu().numpy(), rtol=1e-14)
     vals = A.vals.cpu().numpy()
-    for solver in (la.OperatorCGSolver(S), la.IRSolver(S)):
+    for solver in (la.OperatorCGSolver(S), la.IRSolver(S), la.IRSolver(S, variant="flexible")):
         xs = torch.zeros_like(b)
         solver.solve(b, xs, rtol=1e-10)
         bh = b.cpu().numpy()

@@ -283,3 +283,44 @@ def test_sparsity_matches_reference(oracle, golden, tag, capi):
                                      cols2.ctypes.data, C.byref(nnz)))
     np.testing.assert_array_equal(rp2, rp_ref)
     np.testing.assert_array_equal(cols2, cols_ref)
+
+
+def test_threaded_step_matches_serial_oracle(oracle):
+    """The threaded full step behind the CPU baseline (colour-class cell
+    loops, row-split Jacobi-PCG) gives the serial oracle's matrix and
+    right-hand side, independently of the thread count, and solves to the
+    requested residual."""
+    cells, x = oracle.create_box_tet(6, 5, 4)
+    dm, nn = oracle.dofmap_tet(cells, 2)
+    rp, cols = oracle.sparsity(nn, dm)
+    rng = np.random.default_rng(5)
+    kappa = np.exp(rng.normal(0, 1, cells.shape[0]))
+    f = rng.uniform(-1, 1, x.shape[0])
+    X = np.zeros((nn, 3))
+    X[dm[:, :4]] = x[cells]
+    for e, (a, b) in enumerate(((2, 3), (1, 3), (1, 2), (0, 3), (0, 2), (0, 1))):
+        X[dm[:, 4 + e]] = 0.5 * (x[cells[:, a]] + x[cells[:, b]])
+    bnd = np.flatnonzero(np.isclose(X[:, 0], 0) | np.isclose(X[:, 0], 1)).astype(np.int32)
+    order, off = oracle.colour_cells(dm, nn)
+    # no two cells of a colour share a dof
+    for k in range(off.size - 1):
+        d = dm[order[off[k]:off[k + 1]]].ravel()
+        assert np.unique(d).size == d.size
+    assert np.array_equal(np.sort(order), np.arange(cells.shape[0]))
+    runs = [oracle.poisson_step_threaded(2, cells, x, dm, nn, bnd, rp, cols, (order, off),
+                                         kappa=kappa, f=f, rtol=1e-11, threads=t)
+            for t in (1, 3)]
+    assert np.array_equal(runs[0][2], runs[1][2]) and np.array_equal(runs[0][3], runs[1][3])
+    mk = np.zeros(nn, np.int8)
+    mk[bnd] = 1
+    A = oracle.assemble_matrix(0, 2, cells, x, dm, rp, cols, kappa=kappa, bc_markers=mk)
+    oracle.set_diagonal(1, rp, cols, A, bnd)
+    b = oracle.assemble_vector(0, 2, cells, x, dm, nn, f=f)
+    oracle.apply_lifting(b, 0, 2, cells, x, dm, mk, np.zeros(nn), kappa=kappa)
+    oracle.set_bc(b, bnd, np.zeros(nn))
+    for it, sec, vals, bt, u in runs:
+        assert it > 0 and all(s >= 0 for s in sec)
+        assert np.abs(vals - A).max() <= 1e-14 * np.abs(A).max()
+        assert np.abs(bt - b).max() <= 1e-14 * np.abs(b).max()
+        r = b - oracle.spmv(rp, cols, A, u)
+        assert np.linalg.norm(r) / np.linalg.norm(b) < 1e-11 * 1.001

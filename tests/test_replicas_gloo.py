@@ -82,3 +82,24 @@ def test_bench_defaults_and_host_helpers(monkeypatch):
     assert peak > 0 and kind in ("measured", "fallback")
     assert bench.profile_traffic("sell_f32_p2_64") == 418223104
     assert bench.profile_traffic("no such kernel") is None
+
+
+def test_reference_arm_times_full_steps(monkeypatch, capsys):
+    """bench.py --impl reference runs W + K full steps of the oracle on the
+    host threads and prints one JSON line whose timed region is the steps
+    it ran (no extrapolation)."""
+    import json
+
+    sys.path.insert(0, ROOT)
+    import bench
+
+    monkeypatch.setattr(sys, "argv", ["bench.py", "--impl", "reference", "--n", "4",
+                                      "--steps", "2", "--warmup", "1"])
+    bench.run_reference(bench.parse())
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["steps"] == 2 and line["warmup"] == 1
+    assert line["value"] > 0 and line["ms_per_step"] > 0
+    cpu = line["cpu_baseline"]
+    assert cpu["kind"] == "port" and cpu["cores"] >= 1 and "full step" in cpu["sample"]
+    assert len(cpu["cg_iterations"]) == 2 and min(cpu["cg_iterations"]) > 0
+    assert line["ms_per_step"] * 1e-3 * 2 <= line["wall_s"]
