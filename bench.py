@@ -375,8 +375,9 @@ def elasticity_sample(steps=1, warmup=1):
     hexahedra x 6 tetrahedra (331,776 cells, 1,390,179 dofs), E lognormal
     (log 1e3, 0.5) per cell, nu = 0.3, body force (0,0,-1), clamped at x = 0.
     Block (3x3) CSR assembly, expansion to the scalar CSR, then plain FP64
-    Jacobi-PCG and FP64 flexible CG with FP32 PCG corrections, both to the
-    step's relative residual evaluated in FP64."""
+    Jacobi-PCG and the same PCG on the split operator (two FP32 words per
+    value, FP32-pipe products), both to the step's relative residual
+    evaluated in FP64."""
     import numpy as np
     import torch
 
@@ -395,10 +396,13 @@ def elasticity_sample(steps=1, warmup=1):
     S = A.expand_blocks()
     b = rhs.assemble()
     fp64 = la.OperatorCGSolver(S)
-    # FP32 arithmetic alone stalls on this system (the FP32 recurrence
-    # loses accuracy at the level of its smallest eigenvalue): flexible FP64
-    # CG with FP32 PCG corrections to a 0.1 residual drop each.
-    ir = la.IRSolver(S, variant="flexible", inner_rtol=0.1)
+    # FP32 arithmetic cannot carry this system: its FP32 PCG loses accuracy at
+    # the level of the smallest eigenvalue, and FP32 corrections inside FP64
+    # refinement (reliable updates, or flexible CG) stall or need hundreds of
+    # thousands of FP32 iterations. The matrix is therefore applied as two
+    # FP32 words per value on the FP32 pipe (error-free products): the FP64
+    # SpMV of this system is bound by the FP64 pipe, not by HBM.
+    ir = la.OperatorCGSolver(S, split=True)
     x = torch.zeros_like(b)
     stream = torch.cuda.current_stream()
 
@@ -408,9 +412,6 @@ def elasticity_sample(steps=1, warmup=1):
         rhs.assemble(b)
         solver.refresh()
         x.zero_()
-        if solver is ir:
-            return solver.solve(b, x, rtol=STEP_RTOL, max_outer=400, max_inner=4000,
-                                raise_on_fail=False)
         return solver.solve(b, x, rtol=STEP_RTOL, raise_on_fail=False)
 
     out = {"workload": "vector P2 elasticity, box 4x1x1, 96x24x24x6 tets", "cells": m.num_cells,
@@ -424,8 +425,8 @@ def elasticity_sample(steps=1, warmup=1):
                      "iterations": [q.iterations for q in res], "status": r.status,
                      "final_rel_residual": float(np.sqrt(r.rnorm_sq / r.rnorm0_sq))}
         if name == "mixed":
-            out[name]["outer_iterations"] = [q.outer_iterations for q in res]
-            out[name]["variant"] = "flexible CG (FP64) with FP32 Jacobi-PCG corrections"
+            out[name]["variant"] = ("FP64 Jacobi-PCG; matrix as two FP32 words per value, "
+                                    "FP32-pipe products with error-free transformations")
         if name == "fp64_plain":
             x64 = x.clone()
     out["rel_err_vs_fp64_solution"] = float((x - x64).norm() / x64.norm())
@@ -440,8 +441,15 @@ def elasticity_sample(steps=1, warmup=1):
     ok = out["fp64_plain"]["status"] == 0 and out["mixed"]["status"] == 0
     out["speedup_of_mixed"] = (out["fp64_plain"]["ms_per_step"] / out["mixed"]["ms_per_step"]
                                if ok else None)
-    out["note"] = ("FP32 arithmetic limits an FP32 CG on this system near its smallest "
-                   "eigenvalue, so the FP32 solves act as a preconditioner of FP64 flexible CG")
+    out["note"] = ("FP32 values and FP32 arithmetic cannot reach 1e-10 on this system at a "
+                   "useful cost; the mixed path keeps FP64 vectors and forms the products on "
+                   "the FP32 pipe from two FP32 words per value")
+    # The two SpMVs alone (renumbered vectors), L2 flushed by the 933 MB of values.
+    xr = torch.rand(S.nrows, dtype=torch.float64, device="cuda")
+    yr = torch.empty_like(xr)
+    out["spmv_ms"] = {"fp64": _kernel_ms(lambda: fp64.op.apply_renumbered(xr, yr), 10, stream),
+                      "split_fp32_words": _kernel_ms(lambda: ir.op.apply_renumbered(xr, yr), 10,
+                                                     stream)}
     return out
 
 

@@ -33,6 +33,7 @@ MODE_COLOURED = 1
 
 F64 = 0
 F32 = 1
+F32X2 = 2
 
 IR_RESTART = 0
 IR_RELIABLE = 1
@@ -208,6 +209,8 @@ _SIGS = {
                                   C.c_size_t, C.POINTER(CgInfo), _P]),
     "dfx_q4_num_dofs": (C.c_int64, [C.POINTER(Q4Mesh)]),
     "dfx_q4_action": (C.c_int, [C.POINTER(Q4Mesh), C.c_int32, _P, _P, _P]),
+    "dfx_q4_action_tc": (C.c_int, [C.POINTER(Q4Mesh), _P, _P, _P]),
+    "dfx_q4_tc_check": (C.c_int, [_P]),
     "dfx_q4_edges": (C.c_int, [C.POINTER(Q4Mesh), _P, _P]),
     "dfx_q4_cg_workspace_bytes": (C.c_size_t, [C.c_int64, C.c_int32]),
     "dfx_q4_cg_solve": (C.c_int, [C.POINTER(Q4Mesh), _P, _P, C.c_double, C.c_int32, C.c_int32,

@@ -134,7 +134,20 @@ struct Work
   T* p;
   T* y;
   int blocks;
+  // FP64 solves on a split operator (DFX_F32X2): p's FP32 words, hi (n)
+  // then lo (n), written wherever p is, read by the SpMV.
+  float* ph = nullptr;
 };
+
+// p[i] and, when the solve keeps them, its FP32 words.
+template <typename T>
+__device__ __forceinline__ void store_p(const Work<T>& w, int64_t n, int64_t i, T v)
+{
+  w.p[i] = v;
+  if constexpr (sizeof(T) == 8)
+    if (w.ph)
+      dfx::split_f64(v, w.ph[i], w.ph[n + i]);
+}
 
 template <typename T>
 Work<T> carve_work(Carver& c, int64_t n)
@@ -334,7 +347,7 @@ __global__ void __launch_bounds__(kThreads)
     if (!Ax)
       x[i] = T(0);
     w.r[i] = r;
-    w.p[i] = z;
+    store_p<T>(w, n, i, z);
     rr += r * r;
     rz += r * z;
   }
@@ -457,6 +470,34 @@ __global__ void __launch_bounds__(kSellThreads)
     }
   }
   finish_pap(publish<T>(dot, T(0), w.red, &w.st->ticket[1], false), w.st);
+}
+
+// y = A p, p.y -- split operator (DFX_F32X2): FP32-pipe products of the
+// FP32 words of the values and of p, FP64 y and dot.
+template <bool COMP>
+__global__ void __launch_bounds__(kSellThreads)
+    k_spmv_dot_sell_split(const dfx_operator_s op, Work<double> w)
+{
+  block_reduce_init();
+
+  if (is_done(w.st))
+    return;
+  const int lane = threadIdx.x & 31;
+  const dfx::SliceRange sr = dfx::block_slices(op.nslices);
+  const float* vh = (const float*)op.vals;
+  double dot = 0;
+  for (int32_t s = sr.begin; s < sr.end; s += sr.step)
+  {
+    const double acc = dfx::sell_row_split<COMP>(op, vh, vh + op.nslots, w.ph, w.ph + op.n, s,
+                                                 lane);
+    const int32_t row = 32 * s + lane;
+    if (row < op.n)
+    {
+      w.y[row] = acc;
+      dot += acc * w.p[row];
+    }
+  }
+  finish_pap(publish<double>(dot, 0.0, w.red, &w.st->ticket[1], false), w.st);
 }
 
 // 16-byte vectors of the elementwise kernels.
@@ -647,10 +688,20 @@ __global__ void __launch_bounds__(kElemThreads)
       for (int e = 0; e < L; ++e)
         pe[e] = (PRE ? de[e] * re[e] : re[e]) + beta * pe[e];
       reinterpret_cast<V*>(w.p)[v] = pv;
+      if constexpr (sizeof(T) == 8)
+        if (w.ph)
+        {
+          float2 h, l;
+          dfx::split_f64(pe[0], h.x, l.x);
+          dfx::split_f64(pe[1], h.y, l.y);
+          reinterpret_cast<float2*>(w.ph)[v] = h;
+          w.ph[n + 2 * v] = l.x; // n + 2 v may be odd: no 8-byte store
+          w.ph[n + 2 * v + 1] = l.y;
+        }
     }
     if (blockIdx.x == 0)
       for (int64_t i = nvec * L + threadIdx.x; i < n; i += kElemThreads)
-        w.p[i] = (PRE ? dinv[i] * w.r[i] : w.r[i]) + beta * w.p[i];
+        store_p<T>(w, n, i, (PRE ? dinv[i] * w.r[i] : w.r[i]) + beta * w.p[i]);
     return;
   }
   constexpr int E = kElemPerThread;
@@ -673,7 +724,7 @@ __global__ void __launch_bounds__(kElemThreads)
     {
       const int64_t i = base + (int64_t)e * kElemThreads;
       if (i < n)
-        w.p[i] = (PRE ? d[e] * r[e] : r[e]) + beta * p[e];
+        store_p<T>(w, n, i, (PRE ? d[e] * r[e] : r[e]) + beta * p[e]);
     }
   }
 }
@@ -1048,6 +1099,13 @@ __global__ void k_gather(const TI* __restrict__ in, TO* __restrict__ out,
     out[i] = (TO)in[perm[i]];
 }
 
+__global__ void k_split_words(const double* __restrict__ x, float* __restrict__ out, int64_t n)
+{
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n)
+    dfx::split_f64(x[i], out[i], out[n + i]);
+}
+
 __global__ void k_scatter(const double* __restrict__ in, double* __restrict__ out,
                           const int32_t* __restrict__ perm, int32_t n)
 {
@@ -1070,6 +1128,7 @@ struct OpRef
   const dfx_csr* A;          // kCsr
   const dfx_operator_s* op;  // kSell
   const dfx_q4_mesh* q4;     // kQ4 (matrix-free action)
+  int q4_tc = 0;             // kQ4, FP32: the tensor-core action
 };
 
 template <typename T>
@@ -1081,6 +1140,14 @@ void enqueue_spmv_dot<double>(const OpRef& o, const Work<double>& w, cudaStream_
   const int blocks = stride_grid();
   if (o.kind == kSell)
   {
+    if (o.op->dtype == DFX_F32X2)
+    {
+      if (o.op->compressed)
+        k_spmv_dot_sell_split<true><<<sell_blocks(o.op->n), kSellThreads, 0, s>>>(*o.op, w);
+      else
+        k_spmv_dot_sell_split<false><<<sell_blocks(o.op->n), kSellThreads, 0, s>>>(*o.op, w);
+      return;
+    }
     k_spmv_dot_sell<double, double, false><<<sell_blocks(o.op->n), kSellThreads, 0, s>>>(*o.op,
                                                                                        w);
     return;
@@ -1170,7 +1237,15 @@ void enqueue_iteration(const OpRef& o, T* x, const T* dinv, int64_t n, const Wor
   if (o.kind == kQ4)
   {
     // The colour kernels return at once when the state is done.
-    dfx::q4_apply<T>(*o.q4, w.p, w.y, s, &w.st->done);
+    if constexpr (sizeof(T) == 4)
+    {
+      if (o.q4_tc)
+        dfx::q4_apply_tc(*o.q4, w.p, w.y, s, &w.st->done);
+      else
+        dfx::q4_apply<T>(*o.q4, w.p, w.y, s, &w.st->done);
+    }
+    else
+      dfx::q4_apply<T>(*o.q4, w.p, w.y, s, &w.st->done);
     k_dot_pap<T><<<elem_grid(n), kElemThreads, 0, s>>>(n, w);
   }
   else
@@ -1227,7 +1302,7 @@ int iteration_graph(const OpRef& o, T* x, const T* dinv, int64_t n, const Work<T
                     bool reliable, cudaGraphExec_t* out)
 {
   const bool q4 = o.kind == kQ4;
-  GraphKey key{(int)o.kind * 4 + (sizeof(T) == 4) * 2 + (reliable ? 1 : 0),
+  GraphKey key{(int)o.kind * 8 + (o.q4_tc ? 4 : 0) + (sizeof(T) == 4) * 2 + (reliable ? 1 : 0),
                q4 ? (const void*)o.q4->verts
                   : (o.kind == kSell ? (const void*)o.op : (const void*)o.A->row_ptr),
                q4 ? (const void*)o.q4->edges32
@@ -1240,7 +1315,8 @@ int iteration_graph(const OpRef& o, T* x, const T* dinv, int64_t n, const Work<T
                K,
                w.blocks,
                o.kind == kCsr ? o.A->bs : 1,
-               q4 ? (int64_t)o.q4->nx | ((int64_t)o.q4->ny << 21) | ((int64_t)o.q4->nz << 42) : 0,
+               q4 ? (int64_t)o.q4->nx | ((int64_t)o.q4->ny << 21) | ((int64_t)o.q4->nz << 42)
+                  : (o.kind == kSell ? (int64_t)o.op->serial : 0),
                q4 ? o.q4->kappa : 0.0};
   auto& g_graphs = t_graphs.graphs;
   auto it = g_graphs.find(key);
@@ -1351,6 +1427,7 @@ size_t op_work_bytes(int64_t n)
   c.take<double>(n); // x
   c.take<double>(n); // b
   c.take<double>(n); // dinv
+  c.take<float>(2 * n); // p's FP32 words (split operators)
   return c.used;
 }
 
@@ -1427,7 +1504,8 @@ extern "C" int dfx_cg_solve_op(dfx_operator op, const double* d_b, double* d_x,
                                void* stream)
 {
   DFX_REQUIRE(op, "operator is NULL");
-  DFX_REQUIRE(op->dtype == DFX_F64, "dfx_cg_solve_op needs an FP64 operator");
+  DFX_REQUIRE(op->dtype == DFX_F64 || op->dtype == DFX_F32X2,
+              "dfx_cg_solve_op needs an FP64 or split (DFX_F32X2) operator");
   if (int st = check_solve_args(d_b, d_x, d_work, rtol, max_iters))
     return st;
   const int64_t n = op->n;
@@ -1442,6 +1520,8 @@ extern "C" int dfx_cg_solve_op(dfx_operator op, const double* d_b, double* d_x,
   double* xp = c.take<double>(n);
   double* bp = c.take<double>(n);
   double* dp = d_dinv ? c.take<double>(n) : nullptr;
+  if (op->dtype == DFX_F32X2)
+    w.ph = c.take<float>(2 * n);
   const unsigned g = (unsigned)((n + 255) / 256);
   if (int st = reset_work(w.st, w.red, w.blocks, s))
     return st;
@@ -1449,7 +1529,15 @@ extern "C" int dfx_cg_solve_op(dfx_operator op, const double* d_b, double* d_x,
   k_gather<double, double><<<g, 256, 0, s>>>(d_b, bp, op->perm, (int32_t)n);
   if (dp)
     k_gather<double, double><<<g, 256, 0, s>>>(d_dinv, dp, op->perm, (int32_t)n);
-  if (int st = dfx::sell_spmv(*op, xp, w.y, s))
+  if (w.ph)
+  {
+    // A x0 from x0's FP32 words (the buffer of p's words is free until
+    // k_init writes p).
+    k_split_words<<<g, 256, 0, s>>>(xp, w.ph, n);
+    if (int st = dfx::sell_spmv(*op, w.ph, w.y, s))
+      return st;
+  }
+  else if (int st = dfx::sell_spmv(*op, xp, w.y, s))
     return st;
   enqueue_init<double>(bp, w.y, xp, dp, n, w, rtol, max_iters, s);
   DFX_CHECK_LAUNCH();
@@ -1458,7 +1546,7 @@ extern "C" int dfx_cg_solve_op(dfx_operator op, const double* d_b, double* d_x,
   if (int st = iteration_graph<double>(o, xp, dp, n, w, K, false, &exec))
     return st;
   CgState* h;
-  int64_t kernels = 5 + (dp ? 1 : 0);
+  int64_t kernels = 5 + (dp ? 1 : 0) + (w.ph ? 1 : 0);
   int st = run_to_done(exec, w.st, max_iters, K, &h, s, &kernels);
   CgState hs = *h;
   k_scatter<<<g, 256, 0, s>>>(xp, d_x, op->perm, (int32_t)n);
@@ -1747,7 +1835,7 @@ size_t q4_work_bytes(int64_t n, int mode)
 
 extern "C" size_t dfx_q4_cg_workspace_bytes(int64_t n, int32_t mode)
 {
-  return (mode == 0 || mode == 1) ? q4_work_bytes(n, mode) : 0;
+  return (mode >= 0 && mode <= 2) ? q4_work_bytes(n, mode) : 0;
 }
 
 extern "C" int dfx_q4_cg_solve(const dfx_q4_mesh* mesh, const double* d_b, double* d_x,
@@ -1759,7 +1847,8 @@ extern "C" int dfx_q4_cg_solve(const dfx_q4_mesh* mesh, const double* d_b, doubl
               "invalid Q4 mesh");
   if (int st = check_solve_args(d_b, d_x, d_work, rtol, max_iters))
     return st;
-  DFX_REQUIRE(mode == 0 || mode == 1, "mode must be 0 (FP64) or 1 (mixed), got %d", mode);
+  DFX_REQUIRE(mode >= 0 && mode <= 2,
+              "mode must be 0 (FP64), 1 (mixed) or 2 (mixed, tensor cores), got %d", mode);
   DFX_REQUIRE(mode == 0 || (delta > 0.0 && delta < 1.0), "delta must be in (0, 1)");
   const int64_t n = dfx::q4_ndofs(*mesh);
   DFX_REQUIRE(wbytes >= q4_work_bytes(n, mode), "workspace too small (%zu < %zu)", wbytes,
@@ -1770,7 +1859,7 @@ extern "C" int dfx_q4_cg_solve(const dfx_q4_mesh* mesh, const double* d_b, doubl
     return st;
   cudaStream_t s = dfx::as_stream(stream);
   const int K = graph_iters > 0 ? graph_iters : 20;
-  const OpRef o{kQ4, nullptr, nullptr, mesh};
+  const OpRef o{kQ4, nullptr, nullptr, mesh, mode == 2 ? 1 : 0};
   Carver c{(char*)d_work};
   CgState* h = nullptr;
   int64_t kernels = 0;
@@ -1857,6 +1946,9 @@ extern "C" int dfx_q4_cg_solve(const dfx_q4_mesh* mesh, const double* d_b, doubl
   }
   if (st)
     return st;
+  if (mode == 2)
+    if (int e = dfx::q4_tc_check())
+      return e;
   return report(h, info, kernels);
 }
 

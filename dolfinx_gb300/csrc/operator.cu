@@ -5,6 +5,7 @@
 #include "sell.cuh"
 
 #include <algorithm>
+#include <atomic>
 #include <numeric>
 #include <thread>
 #include <vector>
@@ -38,6 +39,46 @@ __global__ void k_fill(const int32_t* __restrict__ map, const double* __restrict
   {
     const int32_t m = __ldcs(map + i);
     __stcs(out + i, m >= 0 ? (V)__ldg(csr + m) : V(0));
+  }
+}
+
+// Split values (DFX_F32X2): hi = fl32(v) at i, lo = fl32(v - hi) at n + i.
+__global__ void k_fill_split(const int32_t* __restrict__ map, const double* __restrict__ csr,
+                             float* __restrict__ out, int64_t n)
+{
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+  {
+    const int32_t m = __ldcs(map + i);
+    float hi = 0.f, lo = 0.f;
+    if (m >= 0)
+      dfx::split_f64(__ldg(csr + m), hi, lo);
+    __stcs(out + i, hi);
+    __stcs(out + n + i, lo);
+  }
+}
+
+// (hi, lo) FP32 words of an FP64 vector: hi at i, lo at n + i.
+__global__ void k_split(const double* __restrict__ x, float* __restrict__ out, int32_t n)
+{
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n)
+    dfx::split_f64(x[i], out[i], out[n + i]);
+}
+
+template <bool COMP>
+__global__ void __launch_bounds__(128)
+    k_sell_spmv_split(const dfx_operator_s op, const float* __restrict__ x, double* __restrict__ y)
+{
+  const int lane = threadIdx.x & 31;
+  const dfx::SliceRange sr = dfx::block_slices(op.nslices);
+  const float* vh = (const float*)op.vals;
+  for (int32_t s = sr.begin; s < sr.end; s += sr.step)
+  {
+    const double acc = dfx::sell_row_split<COMP>(op, vh, vh + op.nslots, x, x + op.n, s, lane);
+    const int32_t row = 32 * s + lane;
+    if (row < op.n)
+      y[row] = acc;
   }
 }
 
@@ -335,11 +376,10 @@ namespace
 // values are filled from A's FP64 values when it has them.
 int finish_create(dfx_operator_s* op, const dfx_csr* A, dfx_operator* out, void* stream)
 {
-  const size_t vb = op->dtype == DFX_F64 ? 8 : 4;
   int st = DFX_OK;
-  if (cudaMalloc(&op->vals, vb * std::max<int64_t>(op->nslots, 1)) != cudaSuccess)
+  if (cudaMalloc(&op->vals, dfx::value_bytes(*op)) != cudaSuccess)
     st = dfx::fail(DFX_ERR_NO_MEMORY, "operator values: out of device memory");
-  if (!st && cudaMalloc(&op->tmp, vb * 2 * std::max<int64_t>(op->n, 1)) != cudaSuccess)
+  if (!st && cudaMalloc(&op->tmp, dfx::scratch_bytes(*op)) != cudaSuccess)
     st = dfx::fail(DFX_ERR_NO_MEMORY, "operator scratch: out of device memory");
   if (st)
   {
@@ -362,6 +402,27 @@ int sell_grid(int32_t nslices) { return std::max(1, (nslices + 3) / 4); }
 
 int max_grid_blocks() { return 64 * num_sms(); }
 
+uint64_t next_operator_serial()
+{
+  static std::atomic<uint64_t> counter{0};
+  return ++counter;
+}
+
+size_t value_bytes(const dfx_operator_s& op)
+{
+  const size_t per = op.dtype == DFX_F32 ? 4 : 8; // F64, or two FP32 words
+  return per * (size_t)std::max<int64_t>(op.nslots, 1);
+}
+
+// dfx_operator_apply's permuted x and y (and, split operators, x's words).
+size_t scratch_bytes(const dfx_operator_s& op)
+{
+  const size_t n = (size_t)std::max<int32_t>(op.n, 1);
+  if (op.dtype == DFX_F32)
+    return 4 * 2 * n;
+  return 8 * (op.dtype == DFX_F32X2 ? 3 : 2) * n;
+}
+
 int sell_spmv(const dfx_operator_s& op, const void* x, void* y, cudaStream_t s)
 {
   const unsigned grid = (unsigned)sell_grid(op.nslices);
@@ -370,6 +431,13 @@ int sell_spmv(const dfx_operator_s& op, const void* x, void* y, cudaStream_t s)
   if (op.dtype == DFX_F64)
     k_sell_spmv<double, double, double, false><<<grid, 128, 0, s>>>(
         op, (const double*)op.vals, (const double*)x, (double*)y);
+  else if (op.dtype == DFX_F32X2)
+  {
+    if (op.compressed)
+      k_sell_spmv_split<true><<<grid, 128, 0, s>>>(op, (const float*)x, (double*)y);
+    else
+      k_sell_spmv_split<false><<<grid, 128, 0, s>>>(op, (const float*)x, (double*)y);
+  }
   else if (op.compressed)
     k_sell_spmv<float, float, float, true><<<grid, 128, 0, s>>>(
         op, (const float*)op.vals, (const float*)x, (float*)y);
@@ -397,8 +465,10 @@ extern "C" int dfx_operator_create_ex(const dfx_csr* A, int32_t sigma, int32_t d
   *out = nullptr;
   DFX_REQUIRE(A->bs == 1, "the sliced-ELL operator takes scalar (bs 1) matrices");
   DFX_REQUIRE(A->nrows == A->ncols, "matrix must be square");
-  DFX_REQUIRE(dtype == DFX_F64 || dtype == DFX_F32, "unknown value type %d", dtype);
-  DFX_REQUIRE(!compress_cols || dtype == DFX_F32, "16-bit columns are for FP32 operators");
+  DFX_REQUIRE(dtype == DFX_F64 || dtype == DFX_F32 || dtype == DFX_F32X2,
+              "unknown value type %d", dtype);
+  DFX_REQUIRE(!compress_cols || dtype != DFX_F64,
+              "16-bit columns are for operators with FP32 words");
   DFX_REQUIRE(sigma >= 32 && sigma % 32 == 0, "sigma must be a positive multiple of 32");
   DFX_REQUIRE(A->nnz < INT32_MAX, "matrix too large for the operator slot map");
   DFX_REQUIRE(build == DFX_BUILD_AUTO || build == DFX_BUILD_DEVICE || build == DFX_BUILD_HOST,
@@ -408,6 +478,7 @@ extern "C" int dfx_operator_create_ex(const dfx_csr* A, int32_t sigma, int32_t d
   if (build != DFX_BUILD_HOST)
   {
     auto* op = new dfx_operator_s();
+    op->serial = dfx::next_operator_serial();
     cudaGetDevice(&op->device);
     op->n = n;
     op->nslices = (n + 31) / 32;
@@ -415,7 +486,7 @@ extern "C" int dfx_operator_create_ex(const dfx_csr* A, int32_t sigma, int32_t d
     op->dtype = dtype;
     op->compressed = compress_cols ? 1 : 0;
     op->csr_nnz = A->nnz;
-    const int st = build_structure_device(A, op, dtype == DFX_F32, compress_cols != 0, s);
+    const int st = build_structure_device(A, op, dtype != DFX_F64, compress_cols != 0, s);
     if (st == DFX_OK)
       return finish_create(op, A, out, stream);
     free_op(op);
@@ -454,7 +525,7 @@ extern "C" int dfx_operator_create_ex(const dfx_csr* A, int32_t sigma, int32_t d
   const int32_t ns = (n + 31) / 32;
   // FP32 operators store entries in k-pairs per lane (8-byte loads), so
   // their slices have an even length.
-  const bool pairs = dtype == DFX_F32;
+  const bool pairs = dtype != DFX_F64;
   std::vector<int64_t> sp(ns + 1, 0);
   for (int32_t sl = 0; sl < ns; ++sl)
   {
@@ -523,6 +594,7 @@ extern "C" int dfx_operator_create_ex(const dfx_csr* A, int32_t sigma, int32_t d
                      "a row has a column gap above 65535: use 32-bit columns");
 
   auto* op = new dfx_operator_s();
+  op->serial = dfx::next_operator_serial();
   cudaGetDevice(&op->device);
   op->n = n;
   op->nslices = ns;
@@ -572,6 +644,9 @@ extern "C" int dfx_operator_update_values(dfx_operator op, const dfx_csr* A, voi
   if (op->dtype == DFX_F64)
     k_fill<double><<<grid, 256, 0, s>>>(op->map, (const double*)A->vals, (double*)op->vals,
                                         op->nslots);
+  else if (op->dtype == DFX_F32X2)
+    k_fill_split<<<grid, 256, 0, s>>>(op->map, (const double*)A->vals, (float*)op->vals,
+                                      op->nslots);
   else
     k_fill<float><<<grid, 256, 0, s>>>(op->map, (const double*)A->vals, (float*)op->vals,
                                        op->nslots);
@@ -594,14 +669,14 @@ extern "C" int dfx_operator_share(dfx_operator src, dfx_operator* out)
   DFX_REQUIRE(src->owns_structure, "share the source operator, not a share");
   *out = nullptr;
   auto* op = new dfx_operator_s(*src);
+  op->serial = dfx::next_operator_serial();
   op->owns_structure = 0;
   op->shares = 0;
   op->source = src;
   op->vals = nullptr;
   op->tmp = nullptr;
-  const size_t vb = op->dtype == DFX_F64 ? 8 : 4;
-  if (cudaMalloc(&op->vals, vb * std::max<int64_t>(op->nslots, 1)) != cudaSuccess
-      || cudaMalloc(&op->tmp, vb * 2 * std::max<int64_t>(op->n, 1)) != cudaSuccess)
+  if (cudaMalloc(&op->vals, dfx::value_bytes(*op)) != cudaSuccess
+      || cudaMalloc(&op->tmp, dfx::scratch_bytes(*op)) != cudaSuccess)
   {
     if (op->vals)
       cudaFree(op->vals);
@@ -644,6 +719,17 @@ extern "C" int dfx_operator_apply(dfx_operator op, const void* d_x, void* d_y, v
       return st;
     k_permute<double><<<g, 256, 0, s>>>(yp, (double*)d_y, op->perm, n, 1);
   }
+  else if (op->dtype == DFX_F32X2)
+  {
+    double* xp = (double*)op->tmp;
+    double* yp = xp + n;
+    float* xs = (float*)(yp + n);
+    k_permute<double><<<g, 256, 0, s>>>((const double*)d_x, xp, op->perm, n, 0);
+    k_split<<<g, 256, 0, s>>>(xp, xs, n);
+    if (int st = dfx::sell_spmv(*op, xs, yp, s))
+      return st;
+    k_permute<double><<<g, 256, 0, s>>>(yp, (double*)d_y, op->perm, n, 1);
+  }
   else
   {
     float* xp = (float*)op->tmp;
@@ -664,5 +750,14 @@ extern "C" int dfx_operator_apply_renumbered(dfx_operator op, const void* d_x, v
   if (op->n == 0)
     return DFX_OK; // empty vectors may have NULL data
   DFX_REQUIRE(d_x && d_y, "arguments must be non-NULL");
-  return dfx::sell_spmv(*op, d_x, d_y, dfx::as_stream(stream));
+  cudaStream_t s = dfx::as_stream(stream);
+  if (op->dtype == DFX_F32X2)
+  {
+    // FP64 vectors: x's FP32 words go to the operator's scratch first.
+    float* xs = (float*)((double*)op->tmp + 2 * (int64_t)op->n);
+    k_split<<<(unsigned)((op->n + 255) / 256), 256, 0, s>>>((const double*)d_x, xs, op->n);
+    DFX_CHECK_LAUNCH();
+    return dfx::sell_spmv(*op, xs, d_y, s);
+  }
+  return dfx::sell_spmv(*op, d_x, d_y, s);
 }

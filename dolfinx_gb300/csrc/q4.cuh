@@ -26,6 +26,15 @@ template <typename T>
 int q4_apply(const dfx_q4_mesh_s& m, const T* u, T* y, cudaStream_t s,
              const int32_t* skip = nullptr);
 
+// y = A u in FP32 with the basis contractions on the tensor cores
+// (tcgen05, TF32 with a three-term split); same launches as q4_apply<float>.
+int q4_apply_tc(const dfx_q4_mesh_s& m, const float* u, float* y, cudaStream_t s,
+                const int32_t* skip = nullptr);
+
+// DFX_ERR_TIMEOUT (and the flag cleared) when a tensor-core kernel gave up
+// waiting for an MMA since the last check; synchronous.
+int q4_tc_check();
+
 inline int64_t q4_ndofs(const dfx_q4_mesh_s& m)
 {
   return (4 * (int64_t)m.nx + 1) * (4 * (int64_t)m.ny + 1) * (4 * (int64_t)m.nz + 1);

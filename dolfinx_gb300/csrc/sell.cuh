@@ -39,12 +39,16 @@ struct dfx_operator_s
   uint16_t* delta = nullptr;    // (nslots), compressed operators
   int32_t* first = nullptr;     // (32 * nslices), compressed operators
   int32_t* map = nullptr;       // (nslots) CSR entry or -1
-  void* vals = nullptr;         // (nslots) f64 or f32
+  void* vals = nullptr;         // (nslots) f64 or f32; DFX_F32X2: hi (nslots) then lo (nslots)
   void* tmp = nullptr;          // 2 n scratch values for dfx_operator_apply
   int device = 0;
   // Structure sharing (dfx_operator_share): a share points at its source's
   // structure arrays and owns only its values; the source counts its shares
   // and may not be destroyed while any is alive.
+  // Process-wide creation number: cached CUDA graphs bake the operator's
+  // arrays into their launches, so they are keyed by this number and not
+  // by addresses, which a later operator may reuse.
+  uint64_t serial = 0;
   int32_t owns_structure = 1;
   int32_t shares = 0;
   dfx_operator_s* source = nullptr;
@@ -52,6 +56,9 @@ struct dfx_operator_s
 
 namespace dfx
 {
+// A new operator serial (never 0).
+uint64_t next_operator_serial();
+
 #ifdef __CUDACC__
 // Row sum of lane `lane` of slice `s` (row 32 s + lane, padded slices).
 // FP64 operators: entry k of the lane at slice_ptr[s] + 32 k + lane.
@@ -181,6 +188,109 @@ __device__ __forceinline__ ACC sell_row(const dfx_operator_s& op, const V* __res
 #endif
 
 #ifdef __CUDACC__
+// Row sum of a split operator (DFX_F32X2): each FP64 value is carried as
+// two FP32 words, hi = fl32(v) and lo = fl32(v - hi), stored in two arrays
+// of the FP32 pair layout (vals and vals + nslots), and x likewise (xh, xl).
+// Products and the running sum use the FP32 pipe with error-free
+// transformations: hi*hi exactly as a sum of two floats (fma), the cross
+// terms hi*lo + lo*hi into a low-order accumulator, and the high-order
+// accumulator updated by a two-sum whose rounding error also goes to the
+// low-order one. The result carries ~2^-44 relative error, far below what
+// CG needs -- FP64-equivalent arithmetic without the FP64 pipe, which runs
+// at 1/58 of the FP32 rate on this part.
+template <bool COMP>
+__device__ __forceinline__ double sell_row_split(const dfx_operator_s& op,
+                                                 const float* __restrict__ vh,
+                                                 const float* __restrict__ vl,
+                                                 const float* __restrict__ xh,
+                                                 const float* __restrict__ xl, int32_t s,
+                                                 int lane)
+{
+  const int64_t b = __ldg(op.slice_ptr + s);
+  const int len = (int)((__ldg(op.slice_ptr + s + 1) - b) >> 5);
+  const int np = len >> 1;
+  const float2* ph = reinterpret_cast<const float2*>(vh + b) + lane;
+  const float2* pl = reinterpret_cast<const float2*>(vl + b) + lane;
+  float S = 0.f, L = 0.f;
+  // The _rn intrinsics keep the compiler from contracting the product
+  // into the sums, which would break the exactness of the two-sum.
+  auto add = [&](float ah, float al, float x0, float x1)
+  {
+    const float p = __fmul_rn(ah, x0);
+    const float e = fmaf(ah, x0, -p);
+    const float t = fmaf(ah, x1, fmaf(al, x0, e));
+    const float u = __fadd_rn(S, p);
+    const float bp = __fsub_rn(u, S);
+    const float err = __fadd_rn(__fsub_rn(S, __fsub_rn(u, bp)), __fsub_rn(p, bp));
+    S = u;
+    L += err + t;
+  };
+  if constexpr (COMP)
+  {
+    const ushort2* d = reinterpret_cast<const ushort2*>(op.delta + b) + lane;
+    int32_t col = __ldg(op.first + 32 * (int64_t)s + lane);
+    constexpr int kChunk = 2;
+    for (int j0 = 0; j0 < np; j0 += kChunk)
+    {
+      float2 hv[kChunk], lv[kChunk];
+      ushort2 dd[kChunk];
+#pragma unroll
+      for (int u = 0; u < kChunk; ++u)
+      {
+        const bool ok = j0 + u < np;
+        hv[u] = ok ? __ldcs(ph + 32 * (j0 + u)) : make_float2(0.f, 0.f);
+        lv[u] = ok ? __ldcs(pl + 32 * (j0 + u)) : make_float2(0.f, 0.f);
+        dd[u] = ok ? __ldcs(d + 32 * (j0 + u)) : make_ushort2(0, 0);
+      }
+      int32_t c0[kChunk], c1[kChunk];
+#pragma unroll
+      for (int u = 0; u < kChunk; ++u)
+      {
+        col += dd[u].x;
+        c0[u] = col;
+        col += dd[u].y;
+        c1[u] = col;
+      }
+      float a0[kChunk], a1[kChunk], b0[kChunk], b1[kChunk];
+#pragma unroll
+      for (int u = 0; u < kChunk; ++u)
+      {
+        a0[u] = __ldg(xh + c0[u]);
+        b0[u] = __ldg(xl + c0[u]);
+        a1[u] = __ldg(xh + c1[u]);
+        b1[u] = __ldg(xl + c1[u]);
+      }
+#pragma unroll
+      for (int u = 0; u < kChunk; ++u)
+      {
+        add(hv[u].x, lv[u].x, a0[u], b0[u]);
+        add(hv[u].y, lv[u].y, a1[u], b1[u]);
+      }
+    }
+  }
+  else
+  {
+    const int2* c = reinterpret_cast<const int2*>(op.cols + b) + lane;
+    for (int j = 0; j < np; ++j)
+    {
+      const float2 hv = __ldcs(ph + 32 * j), lv = __ldcs(pl + 32 * j);
+      const int2 cc = __ldcs(c + 32 * j);
+      add(hv.x, lv.x, __ldg(xh + cc.x), __ldg(xl + cc.x));
+      add(hv.y, lv.y, __ldg(xh + cc.y), __ldg(xl + cc.y));
+    }
+  }
+  return (double)S + (double)L;
+}
+
+// Splits an FP64 vector into the (hi, lo) FP32 words a split operator reads.
+__device__ __forceinline__ void split_f64(double v, float& hi, float& lo)
+{
+  hi = __double2float_rn(v);
+  lo = __double2float_rn(v - (double)hi);
+}
+#endif
+
+#ifdef __CUDACC__
 // Slices of this block: a contiguous run, so that the rows one SM works on
 // are neighbours and their x gathers hit the same L1 lines. Warps of the
 // block interleave inside the run.
@@ -205,6 +315,12 @@ __device__ __forceinline__ SliceRange block_slices(int32_t nslices)
 int sell_grid(int32_t nslices);
 int max_grid_blocks();
 
-// Launch y = A x on renumbered vectors (both of length op.n).
+// Launch y = A x on renumbered vectors (both of length op.n). A split
+// operator (DFX_F32X2) takes x as its FP32 words, hi (n) then lo (n), and
+// writes y in FP64.
 int sell_spmv(const dfx_operator_s& op, const void* x, void* y, cudaStream_t s);
+
+// Bytes of an operator's value array and of its scratch vectors.
+size_t value_bytes(const dfx_operator_s& op);
+size_t scratch_bytes(const dfx_operator_s& op);
 } // namespace dfx

@@ -225,19 +225,25 @@ class CGSolver:
 
 class SellOperator:
     """Sliced-ELL (SELL-32-sigma) solver copy of a scalar MatrixCSR: FP64, or
-    FP32 with 16-bit column deltas. Values are refreshed from the CSR values
-    with update_values() after re-assembly."""
+    FP32 with 16-bit column deltas, or (split=True) each FP64 value as two
+    FP32 words multiplied on the FP32 pipe with error-free transformations
+    -- FP64-equivalent products on FP64 vectors. Values are refreshed from
+    the CSR values with update_values() after re-assembly."""
 
     def __init__(self, A: MatrixCSR, dtype=torch.float64, sigma: int = 256,
                  compress_cols: bool | None = None, share_of: "SellOperator | None" = None,
-                 build: int = 0):
+                 build: int = 0, split: bool = False):
         """build: where the structure is built (0 device with host fallback,
         1 device only, 2 host); every place gives the same operator."""
         self.A, self.dtype, self.sigma = A, dtype, sigma
+        self.split = bool(split)
+        if self.split and dtype != torch.float64:
+            raise ValueError("a split operator acts on FP64 vectors")
         h = C.c_void_p()
         if share_of is not None:
             # same structure as share_of, own values (one set per request)
             self.dtype, self.sigma, self.compressed = share_of.dtype, share_of.sigma, share_of.compressed
+            self.split = share_of.split
             self.n, self.device = share_of.n, share_of.device
             _capi.check(_capi.lib().dfx_operator_share(share_of.handle, C.byref(h)))
             self.source = share_of
@@ -247,8 +253,10 @@ class SellOperator:
             return
         self.n, self.device = A.nrows, A.vals.device
         if compress_cols is None:
-            compress_cols = dtype == torch.float32
+            compress_cols = dtype == torch.float32 or self.split
         dt = _capi.F64 if dtype == torch.float64 else _capi.F32
+        if self.split:
+            dt = _capi.F32X2
         _capi.check(_capi.lib().dfx_operator_create_ex(C.byref(A.csr()), sigma, dt,
                                                        int(bool(compress_cols)), int(build),
                                                        C.byref(h), _stream()))
@@ -318,12 +326,14 @@ class SellOperator:
 
 class OperatorCGSolver:
     """FP64 Jacobi-PCG on the sliced-ELL operator (same iteration and
-    stopping test as CGSolver)."""
+    stopping test as CGSolver). split=True applies the matrix as two FP32
+    words per value on the FP32 pipe (SellOperator(split=True)); vectors,
+    dot products and updates stay FP64."""
 
     def __init__(self, A: MatrixCSR, jacobi: bool = True, graph_iters: int = 20,
-                 sigma: int = 256):
+                 sigma: int = 256, split: bool = False):
         self.A = A
-        self.op = SellOperator(A, torch.float64, sigma)
+        self.op = SellOperator(A, torch.float64, sigma, split=split)
         self.n = A.nrows
         self.dinv = A.inverse_diagonal() if jacobi else None
         wb = int(_capi.lib().dfx_cg_op_workspace_bytes(self.n))

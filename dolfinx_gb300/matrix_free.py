@@ -124,6 +124,18 @@ class Q4Laplacian:
         _capi.check(_capi.lib().dfx_q4_action(C.byref(self._mesh), dt, _ptr(u), _ptr(y),
                                               _stream()))
 
+    def apply_tc(self, u: torch.Tensor, y: torch.Tensor) -> None:
+        """FP32 action with the basis contractions on the tensor cores
+        (tcgen05, TF32 words split hi + lo); same operator as apply()."""
+        _check_vec(u, self.n, torch.float32, self.verts.device, "u")
+        _check_vec(y, self.n, torch.float32, self.verts.device, "y")
+        _capi.check(_capi.lib().dfx_q4_action_tc(C.byref(self._mesh), _ptr(u), _ptr(y),
+                                                 _stream()))
+
+    def check_tc(self) -> None:
+        """Raises if a tensor-core launch stopped early (its MMA wait ran out)."""
+        _capi.check(_capi.lib().dfx_q4_tc_check(_stream()))
+
     def __call__(self, u: torch.Tensor) -> torch.Tensor:
         y = torch.empty_like(u)
         self.apply(u, y)
@@ -133,12 +145,13 @@ class Q4Laplacian:
 class MatrixFreeCG:
     """CG on the Q4 action (unpreconditioned, as the demo's). mode "fp64":
     FP64 throughout; mode "mixed": FP32 action and vectors with residual
-    replacement by the FP64 action whenever |r| has dropped by `delta`."""
+    replacement by the FP64 action whenever |r| has dropped by `delta`;
+    mode "mixed_tc": "mixed" with the tensor-core FP32 action."""
 
     def __init__(self, op: Q4Laplacian, mode: str = "mixed", delta: float = 0.1,
                  graph_iters: int = 20):
         self.op = op
-        self.mode = {"fp64": 0, "mixed": 1}[mode]
+        self.mode = {"fp64": 0, "mixed": 1, "mixed_tc": 2}[mode]
         self.delta = float(delta)
         self.graph_iters = graph_iters
         wb = int(_capi.lib().dfx_q4_cg_workspace_bytes(op.n, self.mode))

@@ -66,7 +66,11 @@ enum dfx_assembly_mode
 enum dfx_dtype
 {
   DFX_F64 = 0,
-  DFX_F32 = 1
+  DFX_F32 = 1,
+  /* Operators only: an FP64 value carried as two FP32 words, hi = fl32(v)
+   * and lo = fl32(v - hi), multiplied on the FP32 pipe with error-free
+   * transformations (FP64-equivalent products; vectors stay FP64). */
+  DFX_F32X2 = 2
 };
 
 /* A form on a tetrahedral mesh, all arrays on the device.
@@ -592,10 +596,20 @@ int dfx_q4_edges(const dfx_q4_mesh* mesh, float* d_edges, void* stream);
  * and contractions in FP32 from FP64 vertex differences). */
 int dfx_q4_action(const dfx_q4_mesh* mesh, int32_t dtype, const void* d_u, void* d_y,
                   void* stream);
+/* y = A u in FP32 with every 1D basis contraction on the tensor cores
+ * (tcgen05.mma kind::tf32; each operand split as hi + lo so that the
+ * three products hi*hi + lo*hi + hi*lo keep FP32-level accuracy); the
+ * geometry stays on the CUDA cores. Same operator and results (to FP32
+ * rounding) as dfx_q4_action(DFX_F32). */
+int dfx_q4_action_tc(const dfx_q4_mesh* mesh, const float* d_u, float* d_y, void* stream);
+/* Synchronises `stream`; DFX_ERR_TIMEOUT if a tensor-core kernel stopped
+ * early because an MMA completion wait ran out (its y is then invalid). */
+int dfx_q4_tc_check(void* stream);
 /* CG on the Q4 action (the demo's unpreconditioned CG, main.cpp:84-132).
  * mode 0: FP64 throughout; mode 1: FP32 action and vectors with FP64
  * reliable updates (FP64 action for the residual, x += d in FP64) when |r|
- * has dropped by `delta`. Stops at |b - A x|^2/|b - A x0|^2 < rtol^2 in FP64. */
+ * has dropped by `delta`; mode 2: mode 1 with the tensor-core FP32 action
+ * (dfx_q4_action_tc). Stops at |b - A x|^2/|b - A x0|^2 < rtol^2 in FP64. */
 size_t dfx_q4_cg_workspace_bytes(int64_t n, int32_t mode);
 int dfx_q4_cg_solve(const dfx_q4_mesh* mesh, const double* d_b, double* d_x, double rtol,
                     int32_t max_iters, int32_t mode, double delta, int32_t graph_iters,

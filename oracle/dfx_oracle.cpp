@@ -1465,6 +1465,8 @@ int orc_poisson_step_threaded(const orc_form* form, int nc, const int32_t* x_dof
                               const int32_t* corder, const int32_t* coff, int ncol, double rtol,
                               int kmax, int nthreads, double* seconds)
 {
+  if (ncol < 1 || coff[0] != 0 || coff[ncol] != nc)
+    return -1000000 - ORC_ERR_INVALID; // the colour classes must cover the nc cells
   const int T = std::max(1, nthreads);
   const int64_t n = ndofs;
   const int64_t nnz = row_ptr[n];

@@ -411,6 +411,8 @@ def poisson_step_threaded(degree, cells, x, dofmap, ndofs, bc_dofs, row_ptr, col
         C.byref(form), nc, np.ascontiguousarray(cells), x, np.ascontiguousarray(dofmap),
         int(ndofs), mk, bcd.size, bcd, _ptr(ga), _ptr(fa), row_ptr, cols, vals, b, u, order,
         off, off.size - 1, float(rtol), int(kmax), int(threads), sec)
+    if it == -1000001:
+        raise ValueError("the colour classes do not cover the cells")
     if it <= -1000000:
         raise RuntimeError("Entry not in sparsity")
     return it, sec, vals, b, u

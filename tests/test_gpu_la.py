@@ -186,6 +186,60 @@ def test_sell_operator_f32(cuda, oracle, capi, compress):
     assert_close(y, ref, rtol=2e-6)
 
 
+@pytest.mark.parametrize("compress", [False, True])
+def test_sell_operator_split_is_fp64_accurate(cuda, oracle, capi, compress):
+    """The split operator (each value as two FP32 words, FP32-pipe products
+    with error-free transformations) gives the FP64 product to ~1e-13 --
+    FP64 accuracy, far from FP32's 1e-7 -- in both numberings, for n even
+    and odd, and after a value refresh."""
+    from dolfinx_gb300 import fem, la
+
+    for shape in ((6, 5, 7), (5, 5, 4)):
+        m, V, kappa, f, rp, cols = problem(oracle, shape, 2, seed=23)
+        A = fem.assemble_matrix(fem.poisson_form(V, kappa))
+        op = la.SellOperator(A, torch.float64, 256, compress_cols=compress, split=True)
+        x = np.random.default_rng(3).standard_normal(V.num_dofs)
+        y = op.apply(torch.from_numpy(x).cuda()).cpu().numpy()
+        ref = oracle.spmv(rp, cols, A.vals.cpu().numpy(), x)
+        assert_close(y, ref, rtol=1e-13)
+        xp = op.to_operator(torch.from_numpy(x).cuda())
+        yp = op.apply_renumbered(xp, torch.empty_like(xp))
+        assert_close(op.from_operator(yp).cpu().numpy(), ref, rtol=1e-13)
+        A.vals.mul_(3.0)
+        op.update_values()
+        y = op.apply(torch.from_numpy(x).cuda()).cpu().numpy()
+        assert_close(y, 3 * ref, rtol=1e-13)
+
+
+def test_split_operator_cg_matches_fp64(cuda, oracle, capi):
+    """FP64 Jacobi-PCG on the split operator takes the FP64 operator's
+    iteration count (within 2) and meets the stopping test in the oracle's
+    FP64 SpMV, on a Poisson system and a clamped elasticity system."""
+    from dolfinx_gb300 import fem, la
+
+    A, b, rp, cols = _poisson_system(oracle, (10, 9, 8), 2, 31)
+    systems = [(A, b, rp, cols, 1)]
+    m, V, E, f, rpe, colse = problem(oracle, (8, 3, 3), 2, bs=3, seed=13)
+    X = V.tabulate_dof_coordinates()
+    clamp = np.flatnonzero(np.isclose(X[:, 0], 0)).astype(np.int32)
+    bc = fem.dirichletbc(np.zeros(3), clamp, V)
+    a = fem.elasticity_form(V, 1e3 * E, 0.3)
+    Ae = fem.assemble_matrix(a, bcs=[bc])
+    be = fem.RhsAssembler(fem.body_force_form(V, (0, 0, -1)), a, [bc]).assemble()
+    S = Ae.expand_blocks()
+    systems.append((S, be, S.row_ptr.cpu().numpy(), S.cols.cpu().numpy(), 1))
+    for M, rhs, r_p, c_s, bs in systems:
+        x64 = torch.zeros_like(rhs)
+        r64 = la.OperatorCGSolver(M).solve(rhs, x64, rtol=1e-11)
+        xs = torch.zeros_like(rhs)
+        rs = la.OperatorCGSolver(M, split=True).solve(rhs, xs, rtol=1e-11)
+        assert rs.status == 0 and abs(rs.iterations - r64.iterations) <= 2, (rs, r64)
+        bh = rhs.cpu().numpy()
+        res = bh - oracle.spmv(r_p, c_s, M.vals.cpu().numpy(), xs.cpu().numpy(), bs=bs)
+        assert np.linalg.norm(res) / np.linalg.norm(bh) < 1e-11 * 1.001
+        assert (xs - x64).norm().item() / x64.norm().item() < 1e-9
+
+
 def _poisson_system(oracle, n, deg, seed):
     from dolfinx_gb300 import fem
 

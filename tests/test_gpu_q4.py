@@ -39,6 +39,48 @@ def test_q4_action_f32(cuda, oracle):
     assert_close(y, ref, rtol=2e-5)
 
 
+@pytest.mark.parametrize("dims,cache", [((3, 3, 3), True), ((2, 3, 4), False),
+                                        ((5, 4, 3), True)])
+def test_q4_action_tensor_cores(cuda, oracle, dims, cache):
+    """The tcgen05 action (TF32 words split hi + lo, three products per MMA)
+    matches the oracle's full-quadrature FP64 element loop to FP32 accuracy,
+    and the CUDA-core FP32 action to a few FP32 ulps, on odd and even
+    meshes, with and without the edge cache."""
+    from dolfinx_gb300 import matrix_free as mf
+
+    v = mf.hex_box_vertices(*dims, perturb=0.05, seed=7)
+    op = mf.Q4Laplacian(v, *dims, kappa=1.5, cache_edges=cache)
+    u = np.random.default_rng(8).standard_normal(op.n)
+    u32 = torch.from_numpy(u).float().cuda()
+    y = torch.empty_like(u32)
+    op.apply_tc(u32, y)
+    op.check_tc()
+    ref = oracle.q4_action(dims, v, u, kappa=1.5)
+    assert_close(y.double().cpu().numpy(), ref, rtol=2e-5)
+    assert_close(y.double().cpu().numpy(), op(u32).double().cpu().numpy(), rtol=5e-6)
+
+
+def test_q4_tensor_core_cg(cuda):
+    """Mixed CG on the tensor-core action meets the FP64 stopping test and
+    agrees with the CUDA-core mixed CG and the FP64 CG."""
+    from dolfinx_gb300 import matrix_free as mf
+
+    dims = (8, 8, 8)
+    v = mf.hex_box_vertices(*dims, perturb=0.05, seed=9)
+    op = mf.Q4Laplacian(v, *dims)
+    bnd = torch.from_numpy(mf.boundary_mask(*dims)).cuda()
+    b = torch.from_numpy(np.random.default_rng(10).uniform(-1, 1, op.n)).cuda().masked_fill(bnd, 0)
+    xs = {}
+    for mode in ("fp64", "mixed", "mixed_tc"):
+        x = torch.zeros_like(b)
+        r = mf.MatrixFreeCG(op, mode=mode).solve(b, x, rtol=1e-10)
+        assert r.status == 0
+        assert ((b - op(x)).norm() / b.norm()).item() < 1e-10 * 1.001
+        xs[mode] = x
+    for mode in ("mixed", "mixed_tc"):
+        assert ((xs[mode] - xs["fp64"]).norm() / xs["fp64"].norm()).item() < 1e-8
+
+
 def test_q4_edge_cache_is_bitwise_neutral(cuda):
     from dolfinx_gb300 import matrix_free as mf
 
