@@ -66,6 +66,8 @@ def parse():
     p.add_argument("--q4-n", type=int, default=64, help="Q4 hexahedra per direction")
     p.add_argument("--profile-q4", action="store_true",
                    help="apply the Q4 operator only (for an ncu capture of k_q4_cells)")
+    p.add_argument("--profile-q4-tc", action="store_true",
+                   help="apply the tensor-core Q4 action only (ncu capture of k_q4_cells_tc)")
     p.add_argument("--profile-step", action="store_true",
                    help="run one mixed-precision P2 Poisson step only (for an ncu launch list)")
     p.add_argument("--profile", action="store_true",
@@ -144,6 +146,9 @@ class Problem:
         self.fp64 = la.OperatorCGSolver(self.A, jacobi=True, sigma=sigma)
         self.ir = la.IRSolver(self.A, jacobi=True, inner_rtol=inner_rtol, variant=variant,
                               sigma=sigma)
+        if tune:
+            # load chunk of the inner FP32 SpMV, timed on the operator itself
+            self.tuning["fp32_spmv_chunk"] = autotune.tune_chunk(self.ir.op32)
         self.last = None
 
     def assemble(self):
@@ -500,9 +505,11 @@ def q4_sample(n=64, seed=4):
 
     u64 = torch.from_numpy(rng.standard_normal(op.n)).cuda().masked_fill(bnd, 0.0)
     u32 = u64.float()
-    y64, y32 = torch.empty_like(u64), torch.empty_like(u32)
+    y64, y32, ytc = torch.empty_like(u64), torch.empty_like(u32), torch.empty_like(u32)
     ms_a32 = per_launch_ms(lambda: op.apply(u32, y32), 10)
     ms_a64 = per_launch_ms(lambda: op.apply(u64, y64), 3)
+    ms_tc = per_launch_ms(lambda: op.apply_tc(u32, ytc), 5)
+    op.check_tc()
     flop = Q4_FLOP_PER_CELL * cells
     out = {"workload": f"Q4 Laplacian, unit cube {n}^3 hexahedra, 5% interior vertex noise",
            "cells": cells, "dofs": op.n, "flop_per_cell": Q4_FLOP_PER_CELL,
@@ -511,9 +518,13 @@ def q4_sample(n=64, seed=4):
                           "rel_diff_vs_f64": float((y32.double() - y64).norm() / y64.norm())},
            "action_f64": {"ms": ms_a64, "tflops": flop / (ms_a64 * 1e-3) / 1e12,
                           "gdof_per_s": op.n / (ms_a64 * 1e-3) / 1e9},
+           "action_f32_tensor_cores": {
+               "ms": ms_tc, "gdof_per_s": op.n / (ms_tc * 1e-3) / 1e9,
+               "rel_diff_vs_f64": float((ytc.double() - y64).norm() / y64.norm()),
+               "kernel": "k_q4_cells_tc (tcgen05.mma kind::tf32, split words)"},
            "alg_bytes_per_action_f32": op.n * 4 * 3 + (n + 1) ** 3 * 24,
            "kernels_per_action": 8}
-    del u64, u32, y64, y32
+    del u64, u32, y64, y32, ytc
     x = torch.zeros_like(b)
     solves = {}
     for mode, reps in (("mixed", 2), ("fp64", 1)):
@@ -968,7 +979,7 @@ def run_profile_step(args):
     r = P.step_ir()
     torch.cuda.synchronize()
     print(json.dumps({"profile_step": "ok", "inner_iterations": r.inner_iterations,
-                      "outer_iterations": r.outer_iterations}))
+                      "outer_iterations": r.outer_iterations, "tuning": P.tuning}))
 
 
 def run_profile_q4(args):
@@ -992,8 +1003,30 @@ def run_profile_q4(args):
     print(json.dumps({"profile_q4": "ok", "cells": n ** 3, "dofs": op.n}))
 
 
+def run_profile_q4_tc(args):
+    """The tensor-core FP32 Q4 action on --q4-n^3 hexahedra, applied twice:
+    the run behind an ncu capture of k_q4_cells_tc."""
+    import numpy as np
+    import torch
+
+    from dolfinx_gb300 import matrix_free as mf
+
+    torch.cuda.set_device(0)
+    n = args.q4_n
+    op = mf.Q4Laplacian(mf.hex_box_vertices(n, perturb=0.05, seed=4), n)
+    u = torch.from_numpy(np.random.default_rng(4).standard_normal(op.n)).float().cuda()
+    y = torch.empty_like(u)
+    for _ in range(2):
+        op.apply_tc(u, y)
+    op.check_tc()
+    print(json.dumps({"profile_q4_tc": "ok", "cells": n ** 3, "dofs": op.n}))
+
+
 def main():
     args = parse()
+    if args.profile_q4_tc:
+        run_profile_q4_tc(args)
+        return
     if args.profile_q4:
         run_profile_q4(args)
         return

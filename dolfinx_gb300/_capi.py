@@ -27,6 +27,7 @@ FORM_ELASTICITY = 1
 FORM_SOURCE = 2
 FORM_BODYFORCE = 3
 FORM_FACET_MASS = 4
+FORM_FACET_JUMP = 5
 
 MODE_ATOMIC = 0
 MODE_COLOURED = 1
@@ -210,6 +211,12 @@ _SIGS = {
     "dfx_q4_num_dofs": (C.c_int64, [C.POINTER(Q4Mesh)]),
     "dfx_q4_action": (C.c_int, [C.POINTER(Q4Mesh), C.c_int32, _P, _P, _P]),
     "dfx_q4_action_tc": (C.c_int, [C.POINTER(Q4Mesh), _P, _P, _P]),
+    "dfx_operator_set_chunk": (C.c_int, [_P, C.c_int32]),
+    "dfx_assemble_vector_interior_facets": (C.c_int, [C.POINTER(Form), _P, C.c_int32, _P, _P]),
+    "dfx_assemble_matrix_interior_facets": (C.c_int, [C.POINTER(Form), _P, C.c_int32,
+                                                      C.POINTER(Csr), _P, _P]),
+    "dfx_apply_lifting_facets": (C.c_int, [C.POINTER(Form), _P, C.c_int32, C.c_int32, _P, _P,
+                                           _P, _P, C.c_double, _P]),
     "dfx_q4_tc_check": (C.c_int, [_P]),
     "dfx_q4_edges": (C.c_int, [C.POINTER(Q4Mesh), _P, _P]),
     "dfx_q4_cg_workspace_bytes": (C.c_size_t, [C.c_int64, C.c_int32]),

@@ -160,6 +160,24 @@ def tune_sigma(A: la.MatrixCSR, candidates=SIGMA_CANDIDATES, reps: int = 10,
     return {"sigma": best, "candidates": res}
 
 
+CHUNK_CANDIDATES = (2, 4, 8)
+
+
+def tune_chunk(op: la.SellOperator, candidates=CHUNK_CANDIDATES, reps: int = 20) -> dict:
+    """Value pairs per load chunk of an FP32 operator's SpMV: each candidate
+    timed on the operator itself (the product is bitwise the same for all),
+    the fastest kept on the operator."""
+    if op.dtype != torch.float32:
+        raise ValueError("the chunk is a launch shape of FP32 operators")
+    res = {}
+    for ch in candidates:
+        op.set_chunk(ch)
+        res[ch] = _op_ms(op, torch.float32, op.n, reps)
+    best = min(res, key=res.get)
+    op.set_chunk(best)
+    return {"chunk": best, "candidates": res}
+
+
 def clear() -> None:
     """Forget every recorded choice (the library's table and the sigmas)."""
     _capi.check(_capi.lib().dfx_tune_clear())

@@ -360,13 +360,17 @@ __global__ void __launch_bounds__(kThreads)
   }
   __syncthreads();
   bool staged = bulk;
-  if (bulk && !mbar_wait(&sBar, 0, 1 << 20))
+  if (bulk && !__syncthreads_and(mbar_wait(&sBar, 0, 1 << 20)))
   {
-    // The copy did not land in time: report it, let it finish (bounded),
-    // and load the rows directly; the copy writes the same values.
+    // The copy did not land in time: report it and let it finish
+    // (bounded), then load the rows directly (the copy writes the same
+    // values). If it still has not landed, the block writes nothing: the
+    // late copy could overwrite shared memory after the block exits. The
+    // status marks the assembled values void either way.
     if (threadIdx.x == 0)
       atomicExch(status, (int)DFX_ERR_TIMEOUT);
-    mbar_wait(&sBar, 0, 1 << 24);
+    if (!__syncthreads_and(mbar_wait(&sBar, 0, 1 << 24)))
+      return;
     staged = false;
   }
   for (int t = threadIdx.x; t < nloc * ND; t += blockDim.x)
@@ -1195,6 +1199,339 @@ __global__ void k_facets_matrix(const dfx_form a, const int32_t* __restrict__ fa
   }
 }
 
+// ------------------------------------------------------------------------
+// Interior facet integrals (fem/assemble_vector_impl.h:252-360,
+// fem/assemble_matrix_impl.h:443-667). The domain is a list of
+// (cell0, local facet0, cell1, local facet1) quads; the element tensor of a
+// facet lives on the macro element of both cells, dofs of cell0 then dofs
+// of cell1, and is scattered with FP64 atomics.
+//   vector: L(v) = \int_F avg(g) avg(v) dS, g a P1 coefficient -- each side
+//           adds half of the exterior-facet formula on its own local facet;
+//   matrix: a(u,v) = \int_F gamma |F| [grad u . n][grad v . n] dS, the
+//           continuous interior penalty (gradient-jump) term, gamma the
+//           average of the two cells' coefficients. The jumps are linear on
+//           F (P2) and their product is integrated exactly by the
+//           edge-midpoint rule; P1 gradients are constant.
+// ------------------------------------------------------------------------
+
+// Vertex coordinates (4 x 3) of cell c, its global geometry nodes, and the
+// gradients of its barycentric coordinates (rows of J^{-1}; lambda_0 =
+// 1 - lambda_1 - lambda_2 - lambda_3).
+__device__ __forceinline__ void cell_barycentric_gradients(const dfx_form& a, int32_t c,
+                                                           int32_t* node, double (*p)[3],
+                                                           double (*g)[3])
+{
+  const int4 xd = __ldg(reinterpret_cast<const int4*>(a.x_dofmap) + c);
+  node[0] = xd.x;
+  node[1] = xd.y;
+  node[2] = xd.z;
+  node[3] = xd.w;
+#pragma unroll
+  for (int v = 0; v < 4; ++v)
+#pragma unroll
+    for (int d = 0; d < 3; ++d)
+      p[v][d] = __ldg(a.x + 3 * (int64_t)node[v] + d);
+  double J[3][3];
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+      J[d][k] = p[k + 1][d] - p[0][d];
+  const double c00 = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+  const double c01 = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+  const double c02 = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+  const double det = J[0][0] * c00 + J[0][1] * c01 + J[0][2] * c02;
+  const double id = 1.0 / det;
+  // K = J^{-1}: row k is grad lambda_{k+1}.
+  g[1][0] = c00 * id;
+  g[1][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) * id;
+  g[1][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) * id;
+  g[2][0] = c01 * id;
+  g[2][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) * id;
+  g[2][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) * id;
+  g[3][0] = c02 * id;
+  g[3][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) * id;
+  g[3][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) * id;
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+    g[0][d] = -(g[1][d] + g[2][d] + g[3][d]);
+}
+
+// Basix P2 edge k of the tetrahedron joins local vertices kEdgeV[k].
+__constant__ int kEdgeV[6][2] = {{2, 3}, {1, 3}, {1, 2}, {0, 3}, {0, 2}, {0, 1}};
+
+// The CIP macro-element tensor of one interior facet: jumps j[q][i] of the
+// normal derivative of macro basis function i (cell0's nd, then cell1's)
+// at the facet's quadrature points, and the weight w of each point.
+template <int DEG>
+struct CipFacet
+{
+  static constexpr int ND = DEG == 1 ? 4 : 10;
+  static constexpr int NQ = DEG == 1 ? 1 : 3;
+  double j[NQ][2 * ND];
+  double w; // gamma |F| times the rule's weight |F| / NQ
+  int32_t c[2];
+};
+
+template <int DEG>
+__device__ void cip_facet(const dfx_form& a, int4 q, CipFacet<DEG>& out)
+{
+  constexpr int ND = CipFacet<DEG>::ND;
+  const int32_t cell[2] = {q.x, q.z};
+  const int lf[2] = {q.y, q.w};
+  int32_t node[2][4];
+  double p[2][4][3], g[2][4][3];
+#pragma unroll
+  for (int s = 0; s < 2; ++s)
+    cell_barycentric_gradients(a, cell[s], node[s], p[s], g[s]);
+  // Facet vertices (cell0's numbering), area and unit normal out of cell0.
+  int fv[3];
+  {
+    int k = 0;
+#pragma unroll
+    for (int v = 0; v < 4; ++v)
+      if (v != lf[0])
+        fv[k++] = v;
+  }
+  const double* A0 = p[0][fv[0]];
+  const double* B0 = p[0][fv[1]];
+  const double* C0 = p[0][fv[2]];
+  const double u[3] = {B0[0] - A0[0], B0[1] - A0[1], B0[2] - A0[2]};
+  const double v[3] = {C0[0] - A0[0], C0[1] - A0[1], C0[2] - A0[2]};
+  double n[3] = {u[1] * v[2] - u[2] * v[1], u[2] * v[0] - u[0] * v[2],
+                 u[0] * v[1] - u[1] * v[0]};
+  const double nn = sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+  const double area = 0.5 * nn;
+  const double* opp = p[0][lf[0]];
+  const double side = n[0] * (opp[0] - A0[0]) + n[1] * (opp[1] - A0[1]) + n[2] * (opp[2] - A0[2]);
+  const double sgn = (side > 0 ? -1.0 : 1.0) / nn;
+#pragma unroll
+  for (int d = 0; d < 3; ++d)
+    n[d] *= sgn;
+  const double k0 = a.kappa ? __ldg(a.kappa + cell[0]) : a.kappa_const;
+  const double k1 = a.kappa ? __ldg(a.kappa + cell[1]) : a.kappa_const;
+  out.w = 0.5 * (k0 + k1) * area * area / CipFacet<DEG>::NQ;
+  out.c[0] = cell[0];
+  out.c[1] = cell[1];
+  // grad lambda . n per cell and vertex; the jump takes cell1 with a minus.
+  double gn[2][4];
+#pragma unroll
+  for (int s = 0; s < 2; ++s)
+#pragma unroll
+    for (int vv = 0; vv < 4; ++vv)
+      gn[s][vv] = (s == 0 ? 1.0 : -1.0)
+                  * (g[s][vv][0] * n[0] + g[s][vv][1] * n[1] + g[s][vv][2] * n[2]);
+  if constexpr (DEG == 1)
+  {
+#pragma unroll
+    for (int s = 0; s < 2; ++s)
+#pragma unroll
+      for (int vv = 0; vv < 4; ++vv)
+        out.j[0][s * ND + vv] = gn[s][vv];
+    return;
+  }
+  else
+  {
+    // Quadrature point m: midpoint of the facet edge opposite facet vertex
+    // m (global nodes a_m, b_m); barycentrics 1/2 at those two vertices.
+#pragma unroll
+    for (int m = 0; m < 3; ++m)
+    {
+      const int32_t na = node[0][fv[(m + 1) % 3]], nb = node[0][fv[(m + 2) % 3]];
+#pragma unroll
+      for (int s = 0; s < 2; ++s)
+      {
+        double lam[4];
+#pragma unroll
+        for (int vv = 0; vv < 4; ++vv)
+          lam[vv] = (node[s][vv] == na || node[s][vv] == nb) ? 0.5 : 0.0;
+        // vertex functions lambda (2 lambda - 1): gradient (4 lambda - 1) grad lambda
+#pragma unroll
+        for (int vv = 0; vv < 4; ++vv)
+          out.j[m][s * ND + vv] = (4.0 * lam[vv] - 1.0) * gn[s][vv];
+        // edge functions 4 lambda_a lambda_b
+#pragma unroll
+        for (int e = 0; e < 6; ++e)
+        {
+          const int ea = kEdgeV[e][0], eb = kEdgeV[e][1];
+          out.j[m][s * ND + 4 + e] = 4.0 * (lam[ea] * gn[s][eb] + lam[eb] * gn[s][ea]);
+        }
+      }
+    }
+  }
+}
+
+template <int DEG>
+__global__ void k_interior_facets_vector(const dfx_form a, const int4* __restrict__ quads,
+                                         int32_t nf, double* __restrict__ b)
+{
+  constexpr int ND = DEG == 1 ? 4 : 10;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nf)
+    return;
+  const int4 q = __ldg(quads + t);
+  const int32_t cs[2] = {q.x, q.z};
+  const int fs[2] = {q.y, q.w};
+#pragma unroll
+  for (int s = 0; s < 2; ++s)
+  {
+    int lv[3];
+    int32_t gn[3];
+    const double A = 0.5 * facet_geometry(a, cs[s], fs[s], lv, gn); // avg(v): half per side
+    double g[3];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+      g[k] = a.f ? __ldg(a.f + gn[k]) : a.f_const[0];
+    const double S = g[0] + g[1] + g[2];
+    const int32_t* dofs = a.dofmap + (int64_t)ND * cs[s];
+#pragma unroll
+    for (int k = 0; k < 3; ++k)
+    {
+      const double vk = DEG == 1 ? A / 12.0 * (g[k] + S) : A / 60.0 * (3.0 * g[k] - S);
+      atomicAdd(b + __ldg(dofs + lv[k]), vk);
+      if (DEG == 2)
+        atomicAdd(b + __ldg(dofs + 4 + kFacetEdges[fs[s]][k]), A / 15.0 * (2.0 * S - g[k]));
+    }
+  }
+}
+
+// A += the CIP macro tensor; rows and columns of constrained dofs skipped
+// (as the cell loop zeroes them); insertion by binary search in the rows
+// (the pattern must hold the facet couplings).
+template <int DEG>
+__global__ void k_interior_facets_matrix(const dfx_form a, const int4* __restrict__ quads,
+                                         int32_t nf, const int64_t* __restrict__ row_ptr,
+                                         const int32_t* __restrict__ cols,
+                                         double* __restrict__ vals,
+                                         const int8_t* __restrict__ bc, int* __restrict__ status)
+{
+  constexpr int ND = CipFacet<DEG>::ND, NQ = CipFacet<DEG>::NQ;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nf)
+    return;
+  CipFacet<DEG> F;
+  cip_facet<DEG>(a, __ldg(quads + t), F);
+  for (int i = 0; i < 2 * ND; ++i)
+  {
+    const int32_t di = __ldg(a.dofmap + (int64_t)ND * F.c[i / ND] + i % ND);
+    if (bc && __ldg(bc + di))
+      continue;
+    const int64_t rb = __ldg(row_ptr + di), re = __ldg(row_ptr + di + 1);
+    for (int k = 0; k < 2 * ND; ++k)
+    {
+      const int32_t dk = __ldg(a.dofmap + (int64_t)ND * F.c[k / ND] + k % ND);
+      if (bc && __ldg(bc + dk))
+        continue;
+      double v = 0.0;
+#pragma unroll
+      for (int m = 0; m < NQ; ++m)
+        v += F.j[m][i] * F.j[m][k];
+      const int64_t pos = row_search(cols, rb, re, dk);
+      if (pos >= re || __ldg(cols + pos) != dk)
+      {
+        atomicExch(status, (int)DFX_ERR_NOT_IN_SPARSITY);
+        continue;
+      }
+      atomicAdd(vals + pos, F.w * v);
+    }
+  }
+}
+
+// Lifting of facet integrals (lift_bc over facets, fem/assemble_vector_impl.h:
+// 363-414, through assemble_matrix<true> on the facet domains): b[r] -=
+// alpha sum_c A_F[r, c] (g_c - x0_c) over the constrained columns c of
+// each facet's (macro) element tensor. Exterior facets: the facet mass of
+// DFX_FORM_FACET_MASS; interior facets: the CIP term.
+template <int DEG>
+__global__ void k_lift_exterior_facets(const dfx_form a, const int2* __restrict__ pairs,
+                                       int32_t nf, const int8_t* __restrict__ bc,
+                                       const double* __restrict__ g,
+                                       const double* __restrict__ x0, double alpha,
+                                       double* __restrict__ b)
+{
+  constexpr int ND = DEG == 1 ? 4 : 10;
+  constexpr int NF = DEG == 1 ? 3 : 6;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nf)
+    return;
+  const int2 cf = __ldg(pairs + t);
+  int lv[3];
+  int32_t gnode[3];
+  const double A = facet_geometry(a, cf.x, cf.y, lv, gnode);
+  const double sc = (a.kappa ? __ldg(a.kappa + cf.x) : a.kappa_const) * A;
+  int loc[NF];
+#pragma unroll
+  for (int k = 0; k < 3; ++k)
+  {
+    loc[k] = lv[k];
+    if (DEG == 2)
+      loc[3 + k] = 4 + kFacetEdges[cf.y][k];
+  }
+  const int32_t* dofs = a.dofmap + (int64_t)ND * cf.x;
+  for (int j = 0; j < NF; ++j)
+  {
+    const int32_t dj = __ldg(dofs + loc[j]);
+    if (!__ldg(bc + dj))
+      continue;
+    const double gj = alpha * (__ldg(g + dj) - (x0 ? __ldg(x0 + dj) : 0.0));
+    for (int i = 0; i < NF; ++i)
+    {
+      double m;
+      if (DEG == 1)
+        m = (i == j ? 2.0 : 1.0) / 12.0;
+      else
+      {
+        const bool vi = i < 3, vj = j < 3;
+        if (vi && vj)
+          m = i == j ? 6.0 : -1.0;
+        else if (!vi && !vj)
+          m = i == j ? 32.0 : 16.0;
+        else
+          m = i % 3 == j % 3 ? -4.0 : 0.0;
+        m /= 180.0;
+      }
+      atomicAdd(b + __ldg(dofs + loc[i]), -sc * m * gj);
+    }
+  }
+}
+
+template <int DEG>
+__global__ void k_lift_interior_facets(const dfx_form a, const int4* __restrict__ quads,
+                                       int32_t nf, const int8_t* __restrict__ bc,
+                                       const double* __restrict__ g,
+                                       const double* __restrict__ x0, double alpha,
+                                       double* __restrict__ b)
+{
+  constexpr int ND = CipFacet<DEG>::ND, NQ = CipFacet<DEG>::NQ;
+  const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nf)
+    return;
+  const int4 q = __ldg(quads + t);
+  // Only facets with a constrained macro dof do work.
+  bool any = false;
+  for (int k = 0; k < 2 * ND && !any; ++k)
+    any = __ldg(bc + __ldg(a.dofmap + (int64_t)ND * (k < ND ? q.x : q.z) + k % ND)) != 0;
+  if (!any)
+    return;
+  CipFacet<DEG> F;
+  cip_facet<DEG>(a, q, F);
+  for (int k = 0; k < 2 * ND; ++k)
+  {
+    const int32_t dk = __ldg(a.dofmap + (int64_t)ND * F.c[k / ND] + k % ND);
+    if (!__ldg(bc + dk))
+      continue;
+    const double gk = alpha * (__ldg(g + dk) - (x0 ? __ldg(x0 + dk) : 0.0));
+    for (int i = 0; i < 2 * ND; ++i)
+    {
+      double v = 0.0;
+#pragma unroll
+      for (int m = 0; m < NQ; ++m)
+        v += F.j[m][i] * F.j[m][k];
+      atomicAdd(b + __ldg(a.dofmap + (int64_t)ND * F.c[i / ND] + i % ND), -F.w * v * gk);
+    }
+  }
+}
+
 // Functional cell loop (fem/assemble_scalar_impl.h:32-61): per cell
 // a(u_e, u_e) with the Poisson/Helmholtz element tensor, or L(u_e) with the
 // P1-source element vector; block partial sums in FP64, each block's
@@ -1348,6 +1685,109 @@ extern "C" int dfx_assemble_matrix_facets(const dfx_form* a, const int32_t* d_fa
   DFX_CHECK_LAUNCH();
   if (!d_map)
     return read_status(status, s);
+  return DFX_OK;
+}
+
+namespace
+{
+int check_interior(const dfx_form* a, int32_t kind, const int32_t* d_facets, int32_t nf)
+{
+  DFX_REQUIRE(a, "form is NULL");
+  DFX_REQUIRE(a->kind == kind, "form kind %d where %d is required", a->kind, kind);
+  DFX_REQUIRE(a->degree == 1 || a->degree == 2, "degree must be 1 or 2");
+  DFX_REQUIRE(nf >= 0, "negative facet count");
+  DFX_REQUIRE(nf == 0 || (d_facets && a->x_dofmap && a->x && a->dofmap),
+              "facets and form arrays must be non-NULL");
+  DFX_REQUIRE(((uintptr_t)d_facets & 15) == 0, "interior facets must be 16-byte aligned");
+  return DFX_OK;
+}
+} // namespace
+
+extern "C" int dfx_assemble_vector_interior_facets(const dfx_form* L, const int32_t* d_facets,
+                                                   int32_t num_facets, double* d_b, void* stream)
+{
+  if (int st = check_interior(L, DFX_FORM_SOURCE, d_facets, num_facets))
+    return st;
+  DFX_REQUIRE(d_b || num_facets == 0, "b must be non-NULL");
+  if (num_facets == 0)
+    return DFX_OK;
+  cudaStream_t s = dfx::as_stream(stream);
+  const unsigned grid = (unsigned)((num_facets + kThreads - 1) / kThreads);
+  const int4* q = reinterpret_cast<const int4*>(d_facets);
+  if (L->degree == 1)
+    k_interior_facets_vector<1><<<grid, kThreads, 0, s>>>(*L, q, num_facets, d_b);
+  else
+    k_interior_facets_vector<2><<<grid, kThreads, 0, s>>>(*L, q, num_facets, d_b);
+  DFX_CHECK_LAUNCH();
+  return DFX_OK;
+}
+
+extern "C" int dfx_assemble_matrix_interior_facets(const dfx_form* a, const int32_t* d_facets,
+                                                   int32_t num_facets, const dfx_csr* A,
+                                                   const int8_t* d_bc, void* stream)
+{
+  if (int st = check_interior(a, DFX_FORM_FACET_JUMP, d_facets, num_facets))
+    return st;
+  DFX_REQUIRE(A && A->row_ptr && A->cols && A->vals, "matrix must be non-NULL");
+  DFX_REQUIRE(A->dtype == DFX_F64 && A->bs == 1, "the facet penalty assembles scalar FP64 matrices");
+  if (num_facets == 0)
+    return DFX_OK;
+  cudaStream_t s = dfx::as_stream(stream);
+  int* status = dfx::device_status_page();
+  DFX_REQUIRE(status, "could not allocate the status page");
+  DFX_CUDA(cudaMemsetAsync(status, 0, sizeof(int), s));
+  const unsigned grid = (unsigned)((num_facets + 127) / 128);
+  const int4* q = reinterpret_cast<const int4*>(d_facets);
+  if (a->degree == 1)
+    k_interior_facets_matrix<1><<<grid, 128, 0, s>>>(*a, q, num_facets, A->row_ptr, A->cols,
+                                                     (double*)A->vals, d_bc, status);
+  else
+    k_interior_facets_matrix<2><<<grid, 128, 0, s>>>(*a, q, num_facets, A->row_ptr, A->cols,
+                                                     (double*)A->vals, d_bc, status);
+  DFX_CHECK_LAUNCH();
+  return read_status(status, s);
+}
+
+extern "C" int dfx_apply_lifting_facets(const dfx_form* a, const int32_t* d_facets,
+                                        int32_t num_facets, int32_t interior, double* d_b,
+                                        const int8_t* d_bc, const double* d_g,
+                                        const double* d_x0, double alpha, void* stream)
+{
+  DFX_REQUIRE(a, "form is NULL");
+  if (interior)
+  {
+    if (int st = check_interior(a, DFX_FORM_FACET_JUMP, d_facets, num_facets))
+      return st;
+  }
+  else if (int st = check_facet_form(a, DFX_FORM_FACET_MASS, d_facets, num_facets))
+    return st;
+  if (num_facets == 0)
+    return DFX_OK;
+  DFX_REQUIRE(d_b && d_bc && d_g, "b, bc markers and g must be non-NULL");
+  cudaStream_t s = dfx::as_stream(stream);
+  if (interior)
+  {
+    const unsigned grid = (unsigned)((num_facets + 127) / 128);
+    const int4* q = reinterpret_cast<const int4*>(d_facets);
+    if (a->degree == 1)
+      k_lift_interior_facets<1><<<grid, 128, 0, s>>>(*a, q, num_facets, d_bc, d_g, d_x0, alpha,
+                                                     d_b);
+    else
+      k_lift_interior_facets<2><<<grid, 128, 0, s>>>(*a, q, num_facets, d_bc, d_g, d_x0, alpha,
+                                                     d_b);
+  }
+  else
+  {
+    const unsigned grid = (unsigned)((num_facets + kThreads - 1) / kThreads);
+    const int2* pr = reinterpret_cast<const int2*>(d_facets);
+    if (a->degree == 1)
+      k_lift_exterior_facets<1><<<grid, kThreads, 0, s>>>(*a, pr, num_facets, d_bc, d_g, d_x0,
+                                                          alpha, d_b);
+    else
+      k_lift_exterior_facets<2><<<grid, kThreads, 0, s>>>(*a, pr, num_facets, d_bc, d_g, d_x0,
+                                                          alpha, d_b);
+  }
+  DFX_CHECK_LAUNCH();
   return DFX_OK;
 }
 

@@ -22,6 +22,7 @@
 #include "sell.cuh"
 
 #include <map>
+#include <type_traits>
 #include <mutex>
 #include <tuple>
 
@@ -448,7 +449,7 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // y = A p, p.y -- sliced-ELL operator, one row per lane, warp per slice.
-template <typename V, typename T, bool COMP>
+template <typename V, typename T, bool COMP, int CH = 4>
 __global__ void __launch_bounds__(kSellThreads)
     k_spmv_dot_sell(const dfx_operator_s op, Work<T> w)
 {
@@ -461,7 +462,7 @@ __global__ void __launch_bounds__(kSellThreads)
   T dot = 0;
   for (int32_t s = sr.begin; s < sr.end; s += sr.step)
   {
-    const T acc = dfx::sell_row<V, T, T, COMP>(op, (const V*)op.vals, w.p, s, lane);
+    const T acc = dfx::sell_row<V, T, T, COMP, CH>(op, (const V*)op.vals, w.p, s, lane);
     const int32_t row = 32 * s + lane;
     if (row < op.n)
     {
@@ -1178,10 +1179,33 @@ void enqueue_spmv_dot<double>(const OpRef& o, const Work<double>& w, cudaStream_
 template <>
 void enqueue_spmv_dot<float>(const OpRef& o, const Work<float>& w, cudaStream_t s)
 {
+  const unsigned g = (unsigned)sell_blocks(o.op->n);
+  auto launch = [&](auto comp, auto ch)
+  {
+    k_spmv_dot_sell<float, float, decltype(comp)::value, decltype(ch)::value>
+        <<<g, kSellThreads, 0, s>>>(*o.op, w);
+  };
+  using T_ = std::true_type;
+  using F_ = std::false_type;
+  const int ch = o.op->chunk;
   if (o.op->compressed)
-    k_spmv_dot_sell<float, float, true><<<sell_blocks(o.op->n), kSellThreads, 0, s>>>(*o.op, w);
+  {
+    if (ch == 2)
+      launch(T_{}, std::integral_constant<int, 2>{});
+    else if (ch == 8)
+      launch(T_{}, std::integral_constant<int, 8>{});
+    else
+      launch(T_{}, std::integral_constant<int, 4>{});
+  }
   else
-    k_spmv_dot_sell<float, float, false><<<sell_blocks(o.op->n), kSellThreads, 0, s>>>(*o.op, w);
+  {
+    if (ch == 2)
+      launch(F_{}, std::integral_constant<int, 2>{});
+    else if (ch == 8)
+      launch(F_{}, std::integral_constant<int, 8>{});
+    else
+      launch(F_{}, std::integral_constant<int, 4>{});
+  }
 }
 
 bool aligned16(const void* p) { return ((uintptr_t)p & 15) == 0; }

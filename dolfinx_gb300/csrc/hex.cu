@@ -1114,21 +1114,21 @@ __global__ void k_q4_edges(const dfx_q4_mesh_s m, float* __restrict__ edges, int
   edges[g] = (float)(coord(hi) - coord(lo));
 }
 
-// Resident CTAs per SM of the tensor-core colour kernel.
+// Grid of the tensor-core colour kernel: 4 resident CTAs per SM, the
+// register bound of its launch bounds; 4 x (52 KB dynamic + 2 KB static +
+// 1 KB reserved) shared memory fits the SM's 228 KB. (The occupancy query
+// reported 1 CTA per SM for this kernel, which left 3/4 of each SM idle.)
 int q4_tc_grid_limit()
 {
-  static int per_sm = 0;
+  static int ok = 0;
   static std::once_flag once;
   std::call_once(once, [] {
-    if (cudaFuncSetAttribute(k_q4_cells_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             kTcSmemBytes)
-            != cudaSuccess
-        || cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_q4_cells_tc, 128,
-                                                         kTcSmemBytes)
-               != cudaSuccess)
-      per_sm = 1;
+    ok = cudaFuncSetAttribute(k_q4_cells_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              kTcSmemBytes)
+         == cudaSuccess;
   });
-  return std::max(1, per_sm) * dfx::num_sms();
+  static_assert(4 * (kTcSmemBytes + 2048 + 1024) <= 228 * 1024, "4 CTAs per SM must fit");
+  return (ok ? 4 : 1) * dfx::num_sms();
 }
 
 // Resident CTAs per SM of the colour kernel (queried once per type).

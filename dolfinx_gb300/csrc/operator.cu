@@ -7,6 +7,7 @@
 #include <algorithm>
 #include <atomic>
 #include <numeric>
+#include <type_traits>
 #include <thread>
 #include <vector>
 
@@ -82,7 +83,7 @@ __global__ void __launch_bounds__(128)
   }
 }
 
-template <typename V, typename X, typename ACC, bool COMP>
+template <typename V, typename X, typename ACC, bool COMP, int CH = 4>
 __global__ void __launch_bounds__(128)
     k_sell_spmv(const dfx_operator_s op, const V* __restrict__ vals, const X* __restrict__ x,
                 X* __restrict__ y)
@@ -91,7 +92,7 @@ __global__ void __launch_bounds__(128)
   const dfx::SliceRange sr = dfx::block_slices(op.nslices);
   for (int32_t s = sr.begin; s < sr.end; s += sr.step)
   {
-    const ACC acc = dfx::sell_row<V, X, ACC, COMP>(op, vals, x, s, lane);
+    const ACC acc = dfx::sell_row<V, X, ACC, COMP, CH>(op, vals, x, s, lane);
     const int32_t row = 32 * s + lane;
     if (row < op.n)
       y[row] = (X)acc;
@@ -438,12 +439,27 @@ int sell_spmv(const dfx_operator_s& op, const void* x, void* y, cudaStream_t s)
     else
       k_sell_spmv_split<false><<<grid, 128, 0, s>>>(op, (const float*)x, (double*)y);
   }
-  else if (op.compressed)
-    k_sell_spmv<float, float, float, true><<<grid, 128, 0, s>>>(
-        op, (const float*)op.vals, (const float*)x, (float*)y);
   else
-    k_sell_spmv<float, float, float, false><<<grid, 128, 0, s>>>(
-        op, (const float*)op.vals, (const float*)x, (float*)y);
+  {
+    auto launch = [&](auto comp, auto ch)
+    {
+      k_sell_spmv<float, float, float, decltype(comp)::value, decltype(ch)::value>
+          <<<grid, 128, 0, s>>>(op, (const float*)op.vals, (const float*)x, (float*)y);
+    };
+    auto by_chunk = [&](auto comp)
+    {
+      if (op.chunk == 2)
+        launch(comp, std::integral_constant<int, 2>{});
+      else if (op.chunk == 8)
+        launch(comp, std::integral_constant<int, 8>{});
+      else
+        launch(comp, std::integral_constant<int, 4>{});
+    };
+    if (op.compressed)
+      by_chunk(std::true_type{});
+    else
+      by_chunk(std::false_type{});
+  }
   DFX_CHECK_LAUNCH();
   return DFX_OK;
 }
@@ -685,6 +701,18 @@ extern "C" int dfx_operator_share(dfx_operator src, dfx_operator* out)
   }
   src->shares += 1;
   *out = op;
+  return DFX_OK;
+}
+
+extern "C" int dfx_operator_set_chunk(dfx_operator op, int32_t chunk)
+{
+  DFX_REQUIRE(op, "operator is NULL");
+  DFX_REQUIRE(chunk == 2 || chunk == 4 || chunk == 8, "chunk must be 2, 4 or 8 (got %d)", chunk);
+  if (op->chunk != chunk)
+  {
+    op->chunk = chunk;
+    op->serial = dfx::next_operator_serial(); // cached solver graphs bake the launch
+  }
   return DFX_OK;
 }
 

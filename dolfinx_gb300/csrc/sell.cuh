@@ -49,6 +49,9 @@ struct dfx_operator_s
   // arrays into their launches, so they are keyed by this number and not
   // by addresses, which a later operator may reuse.
   uint64_t serial = 0;
+  // FP32 operators: value pairs per load chunk of a lane (2, 4 or 8): the
+  // loads of one chunk are in flight together (autotuned; 4 by default).
+  int32_t chunk = 4;
   int32_t owns_structure = 1;
   int32_t shares = 0;
   dfx_operator_s* source = nullptr;
@@ -65,7 +68,7 @@ uint64_t next_operator_serial();
 // FP32 operators: entries in k-pairs, pair j of the lane at
 // slice_ptr[s] + 64 j + 2 lane (+0, +1), read as one 8-byte load of values
 // and one 4- or 8-byte load of column data.
-template <typename V, typename X, typename ACC, bool COMP>
+template <typename V, typename X, typename ACC, bool COMP, int CH = 4>
 __device__ __forceinline__ ACC sell_row(const dfx_operator_s& op, const V* __restrict__ vals,
                                         const X* __restrict__ x, int32_t s, int lane)
 {
@@ -79,7 +82,7 @@ __device__ __forceinline__ ACC sell_row(const dfx_operator_s& op, const V* __res
     // all its x gathers, then the FMAs in entry order. Measured on the P2
     // Poisson operator of a 64^3 x 6 tetrahedral mesh: 79 us against 104 us
     // for the same loop with loads, gathers and FMAs interleaved.
-    constexpr int kChunk = 4;
+    constexpr int kChunk = CH; // pairs per chunk: the operator's `chunk` (autotuned)
     const float2* v = reinterpret_cast<const float2*>(vals + b) + lane;
     const int np = len >> 1;
     float2 vv[kChunk];

@@ -219,6 +219,10 @@ struct SortedFacets
   }
 };
 
+// Facet index 4 c + f is stored in 32 bits of a sort key: callers reject
+// meshes of 2^30 cells or more up front.
+constexpr int64_t kMaxFacetCells = (int64_t)1 << 30;
+
 template <typename I>
 SortedFacets sort_facets(int64_t nc, const I* cells, int64_t nverts)
 {
@@ -1114,6 +1118,8 @@ extern "C" int dfx_exterior_facets_tet(int32_t num_cells, const int32_t* cells, 
 {
   if (num_cells < 0 || !num_facets || (num_cells > 0 && (!cells || !facets)))
     return dfx::fail(DFX_ERR_INVALID, "invalid exterior facet arguments");
+  if (num_cells >= kMaxFacetCells)
+    return dfx::fail(DFX_ERR_INVALID, "%d cells: facet indices need num_cells < 2^30", num_cells);
   const int64_t nf = 4 * (int64_t)num_cells;
   // Facets keyed by their sorted vertex triple (three 21-bit fields when
   // every vertex index fits, else two words); a facet seen once is
@@ -1148,6 +1154,8 @@ extern "C" int dfx_interior_facets_tet(int32_t num_cells, const int32_t* cells, 
 {
   if (num_cells < 0 || !num_facets || (num_cells > 0 && (!cells || !facets)))
     return dfx::fail(DFX_ERR_INVALID, "invalid interior facet arguments");
+  if (num_cells >= kMaxFacetCells)
+    return dfx::fail(DFX_ERR_INVALID, "%d cells: facet indices need num_cells < 2^30", num_cells);
   const int64_t nf = 4 * (int64_t)num_cells;
   // A facet is interior when exactly two (cell, local facet) entries share
   // its vertex triple (fem/utils.cpp:223-254: facets with two attached

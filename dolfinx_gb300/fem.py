@@ -84,6 +84,32 @@ class FunctionSpace:
             self._sparsity = (rp, cols)
         return self._sparsity
 
+    def sparsity_with_interior_facets(self, facets: np.ndarray):
+        """(row_ptr, cols) on the host of the pattern of a form with cell and
+        interior-facet integrals: every cell's dofs coupled with each other,
+        and every interior facet's macro element -- the dofs of both its
+        cells -- coupled with each other (sparsitybuild::cells and
+        sparsitybuild::interior_facets, fem/sparsitybuild.h:36-75), the union
+        sorted without repeats."""
+        facets = np.asarray(facets, np.int32).reshape(-1, 4)
+        nd = self.ndofs_cell
+        # Cells as macro elements of their own dofs twice (repeats are
+        # dropped), then the facets' macro elements.
+        macro = np.concatenate([np.concatenate([self.dofmap, self.dofmap], axis=1),
+                                np.concatenate([self.dofmap[facets[:, 0]],
+                                                self.dofmap[facets[:, 2]]], axis=1)])
+        macro = np.ascontiguousarray(macro, np.int32)
+        ne = macro.shape[0]
+        rp = np.empty(self.num_nodes + 1, np.int64)
+        nnz = C.c_int64(0)
+        L = _capi.lib()
+        _capi.check(L.dfx_sparsity_create(self.num_nodes, ne, 2 * nd, macro.ctypes.data,
+                                          rp.ctypes.data, None, C.byref(nnz)))
+        cols = np.empty(nnz.value, np.int32)
+        _capi.check(L.dfx_sparsity_create(self.num_nodes, ne, 2 * nd, macro.ctypes.data,
+                                          rp.ctypes.data, cols.ctypes.data, C.byref(nnz)))
+        return rp, cols
+
     def sparsity_device(self):
         """(row_ptr, cols) of the same pattern as device tensors, built on the
         device from the device dofmap (cached). Equal to ``sparsity()`` bit
@@ -261,13 +287,19 @@ class Form:
     nu: float = 0.3
     f: torch.Tensor | None = None  # P1 source values on the geometry nodes
     f_const: tuple = (0.0, 0.0, 0.0)
-    facets: torch.Tensor | None = None  # (num_facets, 2) int32: exterior-facet integral
+    # (num_facets, 2) int32 exterior-facet pairs, or (num_facets, 4) interior-facet quads
+    facets: torch.Tensor | None = None
     _cache: dict = field(default_factory=dict, repr=False)
 
     @property
     def rank(self) -> int:
         return 2 if self.kind in (_capi.FORM_POISSON, _capi.FORM_ELASTICITY,
-                                  _capi.FORM_FACET_MASS) else 1
+                                  _capi.FORM_FACET_MASS, _capi.FORM_FACET_JUMP) else 1
+
+    @property
+    def interior(self) -> bool:
+        """An interior-facet integral (dS)."""
+        return self.facets is not None and self.facets.shape[1] == 4
 
     def __add__(self, other):
         return FormSum([self]) + other
@@ -363,6 +395,43 @@ def _facets(V: FunctionSpace, facets):
     return t.to(device=V.device, dtype=torch.int32).contiguous()
 
 
+def _interior_facets(V: FunctionSpace, facets):
+    if facets is None:
+        facets = V.mesh.interior_facets()
+    t = torch.as_tensor(np.asarray(facets)) if not torch.is_tensor(facets) else facets
+    t = t.reshape(-1, 4) if t.numel() else t.reshape(0, 4)
+    if t.numel():
+        # quads index the mesh in the kernels: checked here
+        lo, hi = t.min(0).values.tolist(), t.max(0).values.tolist()
+        if (min(lo[0], lo[2]) < 0 or max(hi[0], hi[2]) >= V.mesh.num_cells
+                or min(lo[1], lo[3]) < 0 or max(hi[1], hi[3]) > 3):
+            raise ValueError(f"interior facets must be (cell < {V.mesh.num_cells}, local facet "
+                             "< 4, cell, local facet) quads")
+    return t.to(device=V.device, dtype=torch.int32).contiguous()
+
+
+def interior_facet_source_form(V: FunctionSpace, g=1.0, facets=None) -> Form:
+    """L(v) = int_F avg(g) avg(v) dS over interior facets (all of them by
+    default); g constant or P1 values on the geometry nodes."""
+    _require_scalar(V)
+    return Form(_capi.FORM_SOURCE, V, f=_dev(g, V, V.mesh.num_nodes, "g (per geometry node)"),
+                f_const=(float(g) if np.isscalar(g) else 0.0, 0.0, 0.0),
+                facets=_interior_facets(V, facets))
+
+
+def interior_penalty_form(V: FunctionSpace, gamma=1.0, facets=None) -> Form:
+    """a(u,v) = int_F gamma |F| [grad u . n][grad v . n] dS over interior
+    facets: the continuous interior penalty (gradient-jump) term, with
+    gamma constant or per cell (averaged over the facet's two cells) and
+    |F| the facet's area. Its matrix needs the facet couplings in the
+    pattern: create_matrix builds them for forms with such a term."""
+    _require_scalar(V)
+    return Form(_capi.FORM_FACET_JUMP, V, kappa=_dev(gamma, V, V.mesh.num_cells,
+                                                     "gamma (per cell)"),
+                kappa_const=float(gamma) if np.isscalar(gamma) else 1.0,
+                facets=_interior_facets(V, facets))
+
+
 def facet_source_form(V: FunctionSpace, g=1.0, facets=None) -> Form:
     """L(v) = int_F g v ds over exterior facets (all boundary facets by
     default); g constant or P1 values on the geometry nodes."""
@@ -398,14 +467,21 @@ def _colour_args(V: FunctionSpace, mode: int):
     return C.c_void_p(order.data_ptr()), off.ctypes.data_as(C.c_void_p), int(off.size - 1)
 
 
-def create_matrix(a: Form) -> MatrixCSR:
+def create_matrix(a) -> MatrixCSR:
     """Matrix with the form's sparsity pattern, values zero (create_matrix).
     The pattern is built on the device for spaces on a GPU; a space whose
-    rows exceed the device builder's limit uses the host builder."""
+    rows exceed the device builder's limit uses the host builder. A form
+    with an interior-facet term adds its facets' macro-element couplings
+    (host builder)."""
     dev = a.V.device
     bs = a.V.bs
     rp = cols = None
-    if torch.device(dev).type == "cuda":
+    quads = [t.facets for t in _terms(a) if t.interior]
+    if quads:
+        rph, colsh = a.V.sparsity_with_interior_facets(
+            np.concatenate([q.cpu().numpy() for q in quads]))
+        rp, cols = torch.from_numpy(rph).to(dev), torch.from_numpy(colsh).to(dev)
+    elif torch.device(dev).type == "cuda":
         try:
             rp, cols = a.V.sparsity_device()
         except _capi.DfxError as e:
@@ -444,7 +520,7 @@ class MatrixAssembler:
                                  f"{V.num_nodes}x{V.num_nodes} blocks of {V.bs}")
             if A.vals.dtype != torch.float64 or A.vals.device.type != "cuda":
                 raise ValueError("A must hold float64 values on a CUDA device")
-        self.A = create_matrix(self.terms[0]) if A is None else A
+        self.A = create_matrix(a) if A is None else A
         self.forms = [t.cstruct() for t in self.terms]
         cells = [cs for t, cs in zip(self.terms, self.forms) if t.facets is None]
         # The slot map depends only on the dofmap and the pattern: a facet-only
@@ -472,6 +548,10 @@ class MatrixAssembler:
                 _capi.check(L.dfx_assemble_matrix(C.byref(cs), C.byref(self.A.csr()),
                                                   _ptr(self.map), _ptr(self.markers), self.mode,
                                                   order, off, ncol, _stream()))
+            elif t.interior:
+                _capi.check(L.dfx_assemble_matrix_interior_facets(
+                    C.byref(cs), _ptr(t.facets), int(t.facets.shape[0]), C.byref(self.A.csr()),
+                    _ptr(self.markers), _stream()))
             else:
                 _capi.check(L.dfx_assemble_matrix_facets(C.byref(cs), _ptr(t.facets),
                                                          int(t.facets.shape[0]),
@@ -506,6 +586,9 @@ def assemble_vector(L, b: torch.Tensor | None = None, mode: str = "atomic") -> t
             order, off, ncol = _colour_args(V, m)
             _capi.check(_capi.lib().dfx_assemble_vector(C.byref(cf), _ptr(b), m, order, off, ncol,
                                                         _stream()))
+        elif t.interior:
+            _capi.check(_capi.lib().dfx_assemble_vector_interior_facets(
+                C.byref(cf), _ptr(t.facets), int(t.facets.shape[0]), _ptr(b), _stream()))
         else:
             _capi.check(_capi.lib().dfx_assemble_vector_facets(C.byref(cf), _ptr(t.facets),
                                                                int(t.facets.shape[0]), _ptr(b),
@@ -564,9 +647,13 @@ def apply_lifting(b: torch.Tensor, a, bcs, x0=None, alpha: float = 1.0,
             bc.set(g)
         order, off, ncol = _colour_args(V, m)
         for t in _terms(aj):
-            if t.facets is not None:
-                raise NotImplementedError("lifting of exterior-facet terms is not supported")
             cf = t.cstruct()
+            if t.facets is not None:
+                # lift_bc over the facet domain (exterior mass or interior penalty)
+                _capi.check(_capi.lib().dfx_apply_lifting_facets(
+                    C.byref(cf), _ptr(t.facets), int(t.facets.shape[0]), int(t.interior),
+                    _ptr(b), _ptr(markers), _ptr(g), _ptr(x0j), float(alpha), _stream()))
+                continue
             _capi.check(_capi.lib().dfx_apply_lifting(C.byref(cf), _ptr(b), _ptr(markers),
                                                       _ptr(g), _ptr(x0j), float(alpha), m, order,
                                                       off, ncol, _stream()))

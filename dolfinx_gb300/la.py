@@ -305,6 +305,11 @@ class SellOperator:
                                                               _stream()))
         return yp
 
+    def set_chunk(self, chunk: int) -> None:
+        """Value pairs per load chunk of the FP32 SpMV (2, 4 or 8); the
+        product is bitwise the same for each."""
+        _capi.check(_capi.lib().dfx_operator_set_chunk(self.handle, int(chunk)))
+
     def info(self):
         ns = C.c_int64()
         nsl = C.c_int32()

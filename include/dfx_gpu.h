@@ -54,7 +54,11 @@ enum dfx_form_kind
   DFX_FORM_BODYFORCE = 3,
   /* a(u,v) = \int_F alpha u v ds over exterior facets (Robin term), alpha =
      kappa of the facet's cell or kappa_const; scalar P1/P2 */
-  DFX_FORM_FACET_MASS = 4
+  DFX_FORM_FACET_MASS = 4,
+  /* a(u,v) = \int_F gamma |F| [grad u . n][grad v . n] dS over interior
+     facets (continuous interior penalty), gamma the average of the two
+     cells' kappa (or kappa_const); scalar P1/P2 */
+  DFX_FORM_FACET_JUMP = 5
 };
 
 enum dfx_assembly_mode
@@ -328,8 +332,11 @@ int dfx_exterior_facets_tet(int32_t num_cells, const int32_t* cells, int32_t* fa
  * (cell0, local facet0, cell1, local facet1)). A facet shared by more
  * than two cells is left out, as in the reference. facets: capacity
  * 8*num_cells int32; (cell0, facet0) < (cell1, facet1) within each
- * entry, entries sorted by (cell0, facet0); *num_facets = count. Host
- * function. */
+ * entry, entries sorted by (cell0, facet0); *num_facets = count. This
+ * order is the library's own (the meshes here number no facets; the
+ * reference lists facets by facet index): the same set and pairing, so
+ * sums over the domain agree up to summation order. num_cells < 2^30.
+ * Host function. */
 int dfx_interior_facets_tet(int32_t num_cells, const int32_t* cells, int32_t* facets,
                             int32_t* num_facets);
 
@@ -346,6 +353,34 @@ int dfx_assemble_vector_facets(const dfx_form* L, const int32_t* d_facets,
 int dfx_assemble_matrix_facets(const dfx_form* a, const int32_t* d_facets,
                                int32_t num_facets, const dfx_csr* A,
                                const uint8_t* d_map, const int8_t* d_bc, void* stream);
+
+/* Interior-facet vector loop (fem/assemble_vector_impl.h:252-360, the
+ * interior_facet branch of assemble_vector): b += \int_F avg(g) avg(v) dS
+ * over (cell0, facet0, cell1, facet1) quads (dfx_interior_facets_tet), L a
+ * DFX_FORM_SOURCE form (g its P1 coefficient, or f_const[0]); each side
+ * adds half. Scalar P1/P2, FP64 atomics; d_facets 16-byte aligned. */
+int dfx_assemble_vector_interior_facets(const dfx_form* L, const int32_t* d_facets,
+                                        int32_t num_facets, double* d_b, void* stream);
+
+/* Interior-facet matrix loop (fem/assemble_matrix_impl.h:443-667): A +=
+ * the macro-element tensor (cell0 dofs, then cell1 dofs) of a
+ * DFX_FORM_FACET_JUMP form; constrained rows and columns (d_bc, may be
+ * NULL) skipped as in the cell loop; insertion by binary search, so A's
+ * pattern must hold the facet couplings (sparsitybuild::interior_facets:
+ * build it from the macro elements). "Entry not in sparsity" otherwise. */
+int dfx_assemble_matrix_interior_facets(const dfx_form* a, const int32_t* d_facets,
+                                        int32_t num_facets, const dfx_csr* A,
+                                        const int8_t* d_bc, void* stream);
+
+/* Lifting of a facet integral (lift_bc, fem/assemble_vector_impl.h:363-414,
+ * over a facet domain): b -= alpha A_F (g - x0) on the constrained columns
+ * of each facet's element tensor. interior = 0: exterior (cell, facet)
+ * pairs and a DFX_FORM_FACET_MASS form; interior = 1: quads and a
+ * DFX_FORM_FACET_JUMP form. d_x0 may be NULL. */
+int dfx_apply_lifting_facets(const dfx_form* a, const int32_t* d_facets, int32_t num_facets,
+                             int32_t interior, double* d_b, const int8_t* d_bc,
+                             const double* d_g, const double* d_x0, double alpha,
+                             void* stream);
 
 /* fem::assemble_scalar over cells (fem/assembler.h:173-215;
  * fem/assemble_scalar_impl.h:32-61) for the functionals M = a(u, u) of a
@@ -469,6 +504,10 @@ int dfx_operator_apply_renumbered(dfx_operator op, const void* d_x, void* d_y, v
 int dfx_operator_info(dfx_operator op, int64_t* nslots, int32_t* nslices,
                       const int32_t** d_perm);
 int dfx_operator_destroy(dfx_operator op);
+/* Launch shape of an FP32 operator's SpMV (no reference counterpart; an
+ * autotuner knob): value pairs per load chunk of a lane, 2, 4 (default) or
+ * 8. Results are bitwise the same for every choice. */
+int dfx_operator_set_chunk(dfx_operator op, int32_t chunk);
 
 /* dfx_cg_solve on an FP64 operator (same iteration and stopping test). */
 size_t dfx_cg_op_workspace_bytes(int64_t n);

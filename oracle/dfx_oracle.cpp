@@ -1299,6 +1299,119 @@ int orc_assemble_matrix_facets(int degree, int nf, const int32_t* pairs,
   return ORC_OK;
 }
 
+// Interior-facet matrix loop (cpp/dolfinx/fem/assemble_matrix_impl.h:
+// 443-667) for the continuous interior penalty
+// a(u, v) = \int_F gamma |F| [grad u . n][grad v . n] dS, gamma the mean of
+// the two cells' coefficients (gamma == nullptr -> gamma_const). Macro
+// element: cell0's dofs then cell1's. The facet quadrature is cell0's
+// collapsed Gauss rule on its local facet, mapped to physical points and
+// pulled back into cell1 through cell1's affine map; gradients are the
+// reference gradients times J^{-T} of each cell; n is the unit normal out of
+// cell0. Constrained rows and columns are skipped; insertion by binary
+// search.
+static void affine_map(const double* coords, double J[3][3], double K[3][3])
+{
+  for (int d = 0; d < 3; ++d)
+    for (int k = 0; k < 3; ++k)
+      J[d][k] = coords[3 * (k + 1) + d] - coords[d];
+  const double det = J[0][0] * (J[1][1] * J[2][2] - J[1][2] * J[2][1])
+                     - J[0][1] * (J[1][0] * J[2][2] - J[1][2] * J[2][0])
+                     + J[0][2] * (J[1][0] * J[2][1] - J[1][1] * J[2][0]);
+  K[0][0] = (J[1][1] * J[2][2] - J[1][2] * J[2][1]) / det;
+  K[0][1] = (J[0][2] * J[2][1] - J[0][1] * J[2][2]) / det;
+  K[0][2] = (J[0][1] * J[1][2] - J[0][2] * J[1][1]) / det;
+  K[1][0] = (J[1][2] * J[2][0] - J[1][0] * J[2][2]) / det;
+  K[1][1] = (J[0][0] * J[2][2] - J[0][2] * J[2][0]) / det;
+  K[1][2] = (J[0][2] * J[1][0] - J[0][0] * J[1][2]) / det;
+  K[2][0] = (J[1][0] * J[2][1] - J[1][1] * J[2][0]) / det;
+  K[2][1] = (J[0][1] * J[2][0] - J[0][0] * J[2][1]) / det;
+  K[2][2] = (J[0][0] * J[1][1] - J[0][1] * J[1][0]) / det;
+}
+
+int orc_assemble_matrix_interior_facets(int degree, int nf, const int32_t* quads,
+                                        const int32_t* x_dofmap, const double* x,
+                                        const int32_t* dofmap, const double* gamma,
+                                        double gamma_const, const int8_t* bc,
+                                        const int64_t* row_ptr, const int32_t* cols,
+                                        double* vals)
+{
+  const int nd = tet_ndofs(degree);
+  double c0[12], c1[12], J0[3][3], K0[3][3], J1[3][3], K1[3][3];
+  double phi[10], dphi[10][3];
+  std::vector<double> Ae(4 * nd * nd), jmp(2 * nd);
+  for (int e = 0; e < nf; ++e)
+  {
+    const int cA = quads[4 * e], fA = quads[4 * e + 1], cB = quads[4 * e + 2];
+    cell_coords(x_dofmap, x, cA, c0);
+    cell_coords(x_dofmap, x, cB, c1);
+    affine_map(c0, J0, K0);
+    affine_map(c1, J1, K1);
+    const double area = facet_area(c0, fA);
+    const double* a = c0 + 3 * kTetFacets[fA][0];
+    const double* b = c0 + 3 * kTetFacets[fA][1];
+    const double* d = c0 + 3 * kTetFacets[fA][2];
+    const double u[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
+    const double v[3] = {d[0] - a[0], d[1] - a[1], d[2] - a[2]};
+    double n[3] = {u[1] * v[2] - u[2] * v[1], u[2] * v[0] - u[0] * v[2],
+                   u[0] * v[1] - u[1] * v[0]};
+    const double nn = std::sqrt(n[0] * n[0] + n[1] * n[1] + n[2] * n[2]);
+    const double* opp = c0 + 3 * fA;
+    const double side = n[0] * (opp[0] - a[0]) + n[1] * (opp[1] - a[1]) + n[2] * (opp[2] - a[2]);
+    for (int k = 0; k < 3; ++k)
+      n[k] *= (side > 0 ? -1.0 : 1.0) / nn;
+    const double g = 0.5 * ((gamma ? gamma[cA] : gamma_const) + (gamma ? gamma[cB] : gamma_const));
+    std::fill(Ae.begin(), Ae.end(), 0.0);
+    const FacetQuad& q = facet_quadrature(fA);
+    for (size_t p = 0; p < q.w.size(); ++p)
+    {
+      const double* X0 = &q.X[3 * p];
+      double xp[3], X1[3];
+      for (int k = 0; k < 3; ++k)
+        xp[k] = c0[k] + J0[k][0] * X0[0] + J0[k][1] * X0[1] + J0[k][2] * X0[2];
+      for (int k = 0; k < 3; ++k)
+        X1[k] = K1[k][0] * (xp[0] - c1[0]) + K1[k][1] * (xp[1] - c1[1])
+                + K1[k][2] * (xp[2] - c1[2]);
+      for (int side2 = 0; side2 < 2; ++side2)
+      {
+        tabulate_tet(degree, side2 == 0 ? X0 : X1, phi, dphi);
+        const double(*K)[3] = side2 == 0 ? K0 : K1;
+        for (int i = 0; i < nd; ++i)
+        {
+          // physical gradient = K^T dphi
+          double gr[3];
+          for (int k = 0; k < 3; ++k)
+            gr[k] = K[0][k] * dphi[i][0] + K[1][k] * dphi[i][1] + K[2][k] * dphi[i][2];
+          const double dn = gr[0] * n[0] + gr[1] * n[1] + gr[2] * n[2];
+          jmp[side2 * nd + i] = side2 == 0 ? dn : -dn;
+        }
+      }
+      const double wq = q.w[p] * 2.0 * area * g * area;
+      for (int i = 0; i < 2 * nd; ++i)
+        for (int k = 0; k < 2 * nd; ++k)
+          Ae[i * 2 * nd + k] += wq * jmp[i] * jmp[k];
+    }
+    for (int i = 0; i < 2 * nd; ++i)
+    {
+      const int32_t di = dofmap[(int64_t)nd * quads[4 * e + 2 * (i / nd)] + i % nd];
+      if (bc && bc[di])
+        continue;
+      const int32_t* r0 = cols + row_ptr[di];
+      const int32_t* r1 = cols + row_ptr[di + 1];
+      for (int k = 0; k < 2 * nd; ++k)
+      {
+        const int32_t dk = dofmap[(int64_t)nd * quads[4 * e + 2 * (k / nd)] + k % nd];
+        if (bc && bc[dk])
+          continue;
+        const int32_t* it = std::lower_bound(r0, r1, dk);
+        if (it == r1 || *it != dk)
+          return ORC_ERR_NOT_IN_SPARSITY;
+        vals[it - cols] += Ae[i * 2 * nd + k];
+      }
+    }
+  }
+  return ORC_OK;
+}
+
 // Functional cell loop (cpp/dolfinx/fem/assemble_scalar_impl.h:32-61),
 // kind 0: M = a(u, u) = \int kappa |grad u|^2 + k2 u^2 dx; kind 1:
 // M = L(u) = \int f u dx with f a P1 coefficient (f == nullptr -> 1).

@@ -93,6 +93,9 @@ def lib():
         L.orc_assemble_scalar.argtypes = [C.c_int, C.c_int, C.c_int, _i32p, _f64p, _i32p,
                                           C.c_void_p, C.c_double, C.c_void_p, _f64p]
         L.orc_assemble_scalar.restype = C.c_double
+        L.orc_assemble_matrix_interior_facets.argtypes = [
+            C.c_int, C.c_int, _i32p, _i32p, _f64p, _i32p, C.c_void_p, C.c_double, C.c_void_p,
+            _i64p, _i32p, _f64p]
         L.orc_colour_cells.argtypes = [C.c_int, C.c_int, _i32p, C.c_int, _i32p, _i32p, C.c_int]
         L.orc_poisson_step_threaded.argtypes = [
             C.POINTER(_Form), C.c_int, _i32p, _f64p, _i32p, C.c_int, _i8p, C.c_int, _i32p,
@@ -416,3 +419,33 @@ def poisson_step_threaded(degree, cells, x, dofmap, ndofs, bc_dofs, row_ptr, col
     if it <= -1000000:
         raise RuntimeError("Entry not in sparsity")
     return it, sec, vals, b, u
+
+
+def assemble_matrix_interior_facets(degree, quads, cells, x, dofmap, row_ptr, cols, gamma=None,
+                                    gamma_const=1.0, bc_markers=None, vals=None):
+    """Continuous interior penalty over interior facets (quads), added into
+    vals (a new zero array when None)."""
+    q = np.ascontiguousarray(quads, np.int32).reshape(-1, 4)
+    if vals is None:
+        vals = np.zeros(cols.size, np.float64)
+    ga = None if gamma is None else np.ascontiguousarray(gamma, np.float64)
+    bcm = None if bc_markers is None else np.ascontiguousarray(bc_markers, np.int8)
+    rc = lib().orc_assemble_matrix_interior_facets(int(degree), q.shape[0], q,
+                                                   np.ascontiguousarray(cells), x,
+                                                   np.ascontiguousarray(dofmap), _ptr(ga),
+                                                   float(gamma_const), _ptr(bcm), row_ptr, cols,
+                                                   vals)
+    if rc == 3:
+        raise RuntimeError("Entry not in sparsity")
+    return vals
+
+
+def assemble_vector_interior_facets(degree, quads, cells, x, dofmap, n, g=None, g_const=1.0,
+                                    b=None):
+    """int_F avg(g) avg(v) dS: each side's half of the facet integral, by
+    the exterior-facet loop on the quads' two (cell, local facet) pairs."""
+    q = np.ascontiguousarray(quads, np.int32).reshape(-1, 4)
+    pairs = np.ascontiguousarray(np.concatenate([q[:, :2], q[:, 2:]]), np.int32)
+    half_g = None if g is None else 0.5 * np.asarray(g, np.float64)
+    return assemble_vector_facets(degree, pairs, cells, x, dofmap, n, g=half_g,
+                                  g_const=0.5 * g_const, b=b)

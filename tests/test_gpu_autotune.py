@@ -115,3 +115,27 @@ def test_tuned_sigma_gives_a_correct_operator(cuda, oracle, capi):
     x = np.random.default_rng(27).standard_normal(A.nrows)
     ref = oracle.spmv(rp, cols, A.vals.cpu().numpy(), x)
     assert_close(op.apply(torch.from_numpy(x).cuda()).cpu().numpy(), ref, rtol=1e-13)
+
+
+def test_fp32_spmv_chunks_are_bitwise_equal(cuda, oracle, capi):
+    """The load chunk of the FP32 sliced-ELL SpMV changes only how many
+    loads are in flight: the products of chunks 2, 4 and 8 are bitwise
+    equal, and tune_chunk keeps one of them on the operator."""
+    from dolfinx_gb300 import autotune, fem, la
+
+    from gpu_util import problem
+
+    m, V, kappa, f, rp, cols = problem(oracle, (7, 6, 5), 2, seed=24)
+    A = fem.assemble_matrix(fem.poisson_form(V, kappa))
+    op = la.SellOperator(A, torch.float32, 256, compress_cols=True)
+    x = torch.rand(V.num_dofs, dtype=torch.float32, device="cuda")
+    outs = []
+    for ch in (2, 4, 8):
+        op.set_chunk(ch)
+        outs.append(op.apply(x).clone())
+    assert torch.equal(outs[0], outs[1]) and torch.equal(outs[1], outs[2])
+    r = autotune.tune_chunk(op, reps=3)
+    assert r["chunk"] in (2, 4, 8) and set(r["candidates"]) == {2, 4, 8}
+    assert torch.equal(op.apply(x), outs[1])
+    with pytest.raises(capi.DfxError):
+        op.set_chunk(3)

@@ -236,7 +236,10 @@ def test_split_operator_cg_matches_fp64(cuda, oracle, capi):
         assert rs.status == 0 and abs(rs.iterations - r64.iterations) <= 2, (rs, r64)
         bh = rhs.cpu().numpy()
         res = bh - oracle.spmv(r_p, c_s, M.vals.cpu().numpy(), xs.cpu().numpy(), bs=bs)
-        assert np.linalg.norm(res) / np.linalg.norm(bh) < 1e-11 * 1.001
+        # The stopping test reads the recursive residual, which carries the
+        # split products' ~1e-14 rounding: the true residual may sit a few
+        # percent above rtol.
+        assert np.linalg.norm(res) / np.linalg.norm(bh) < 1e-11 * 1.05
         assert (xs - x64).norm().item() / x64.norm().item() < 1e-9
 
 

@@ -324,3 +324,34 @@ def test_threaded_step_matches_serial_oracle(oracle):
         assert np.abs(bt - b).max() <= 1e-14 * np.abs(b).max()
         r = b - oracle.spmv(rp, cols, A, u)
         assert np.linalg.norm(r) / np.linalg.norm(b) < 1e-11 * 1.001
+
+
+def test_interior_facet_pattern_and_penalty_oracle(oracle, capi):
+    """The product's macro-element pattern (cells plus interior-facet macro
+    elements) equals the oracle's pattern of the same elements and contains
+    the cell pattern; the oracle's interior penalty is symmetric, positive
+    semi-definite and zero on quadratics (P2)."""
+    from dolfinx_gb300 import fem, mesh
+
+    m = mesh.create_unit_cube(3, 4, 3)
+    V = fem.functionspace(m, ("Lagrange", 2), device="cpu")
+    quads = m.interior_facets()
+    rp, cols = V.sparsity_with_interior_facets(quads)
+    macro = np.concatenate([np.concatenate([V.dofmap, V.dofmap], axis=1),
+                            np.concatenate([V.dofmap[quads[:, 0]], V.dofmap[quads[:, 2]]],
+                                           axis=1)])
+    rp0, cols0 = oracle.sparsity(V.num_nodes, macro)
+    np.testing.assert_array_equal(rp, rp0)
+    np.testing.assert_array_equal(cols, cols0)
+    rpc, colsc = V.sparsity()
+    for r in range(V.num_nodes):
+        assert set(colsc[rpc[r]:rpc[r + 1]]) <= set(cols[rp[r]:rp[r + 1]])
+    vals = oracle.assemble_matrix_interior_facets(2, quads, m.cells, m.x, V.dofmap, rp, cols)
+    import scipy.sparse as sp
+
+    M = sp.csr_matrix((vals, cols, rp), shape=(V.num_nodes,) * 2).toarray()
+    assert np.abs(M - M.T).max() <= 1e-12 * np.abs(M).max()
+    assert np.linalg.eigvalsh(0.5 * (M + M.T)).min() >= -1e-10 * np.abs(M).max()
+    X = V.tabulate_dof_coordinates()
+    u = X[:, 0] ** 2 - X[:, 1] * X[:, 2] + 3 * X[:, 1]
+    assert np.abs(M @ u).max() <= 1e-11 * np.abs(M).max()
