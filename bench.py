@@ -59,6 +59,11 @@ def parse():
     p.add_argument("--serving-requests", type=int, default=64,
                    help="requests of the bounded serving sample (0: skip)")
     p.add_argument("--serving-nmax", type=int, default=96)
+    p.add_argument("--serving-sweep", action="store_true",
+                   help="serving only: every arrival rate of the serving config, "
+                        "--serving-requests requests per run, --serving-repeats runs per "
+                        "rate and mode; prints one JSON line")
+    p.add_argument("--serving-repeats", type=int, default=3)
     p.add_argument("--no-elasticity", action="store_true", help="skip the elasticity sample")
     p.add_argument("--no-q4", action="store_true", help="skip the matrix-free Q4 sample")
     p.add_argument("--q4-only", action="store_true",
@@ -653,6 +658,61 @@ def serving_sample(args):
     return out
 
 
+SERVING_RATES = (100.0, 200.0, 500.0, 1000.0, 2000.0, 5000.0)
+
+
+def serving_sweep(args):
+    """The serving stream at every arrival rate of the serving config: for
+    each mode (plain FP64, mixed precision) one server, which first builds
+    and tunes the structures of every (n, degree) the draws contain, then
+    serves --serving-repeats runs of --serving-requests requests per rate
+    (each repeat its own request draw: seeds 100 + repeat). The server's
+    HBM budget (120 GB of structures and request values) is below what all
+    178 structures of n in [8, 96] need, so least-recently used structures
+    are evicted and rebuilt when a later request needs them, inside the
+    timed runs, as a long-running server would. Reports per rate and mode
+    the median, min and max of solves/s, p50 and p99 latency."""
+    import statistics
+    import time
+
+    import torch
+
+    from dolfinx_gb300 import serving
+
+    torch.cuda.set_device(0)
+    budget = 120e9
+    nreq, reps = args.serving_requests, args.serving_repeats
+    draws = {(rate, r): serving.make_requests(nreq, rate, seed=100 + r,
+                                               n_range=(8, args.serving_nmax))
+             for rate in SERVING_RATES for r in range(reps)}
+    everything = [q for reqs in draws.values() for q in reqs]
+    out = {"requests_per_run": nreq, "repeats": reps, "n_range": [8, args.serving_nmax],
+           "hbm_budget_bytes": budget, "distinct_structures": len({(q.n, q.degree)
+                                                                   for q in everything}),
+           "structure_setup_s": {}, "rates": [{"rate": rate} for rate in SERVING_RATES]}
+    for mode in ("fp64", "mixed"):
+        serving.clear_structure_cache()
+        torch.cuda.empty_cache()
+        srv = serving.Server(mode=mode, hbm_budget=budget)
+        try:
+            t0 = time.perf_counter()
+            srv.prewarm(everything)
+            out["structure_setup_s"][mode] = time.perf_counter() - t0
+            for row, rate in zip(out["rates"], SERVING_RATES):
+                runs = [srv.run(draws[(rate, r)], max_wall_s=600.0) for r in range(reps)]
+                row[mode] = {k: {"median": statistics.median(st[k] for st in runs),
+                                 "min": min(st[k] for st in runs),
+                                 "max": max(st[k] for st in runs)}
+                             for k in ("solves_per_s", "p50_ms", "p99_ms", "dofs_per_s")}
+                row[mode]["failed"] = sum(len(st["failed"]) for st in runs)
+        finally:
+            srv.close()
+    for row in out["rates"]:
+        row["mixed_over_fp64_solves_median"] = (row["mixed"]["solves_per_s"]["median"]
+                                                / row["fp64"]["solves_per_s"]["median"])
+    print(json.dumps({"serving_sweep": out}))
+
+
 def _timed(fn, steps, stream):
     import torch
 
@@ -1024,6 +1084,9 @@ def run_profile_q4_tc(args):
 
 def main():
     args = parse()
+    if args.serving_sweep:
+        serving_sweep(args)
+        return
     if args.profile_q4_tc:
         run_profile_q4_tc(args)
         return

@@ -26,8 +26,22 @@ int fail(int code, const char* fmt, ...)
 
 int cuda_fail(cudaError_t e, const char* what, const char* file, int line)
 {
+  // A failed allocation is not sticky: consume it, so that the next launch
+  // check of this thread does not report it again as its own failure.
+  if (e == cudaErrorMemoryAllocation)
+  {
+    (void)cudaGetLastError();
+    return fail(DFX_ERR_NO_MEMORY, "CUDA error %s (%s) in %s at %s:%d", cudaGetErrorName(e),
+                cudaGetErrorString(e), what, file, line);
+  }
   return fail(DFX_ERR_CUDA, "CUDA error %s (%s) in %s at %s:%d", cudaGetErrorName(e),
               cudaGetErrorString(e), what, file, line);
+}
+
+int no_memory(const char* what)
+{
+  (void)cudaGetLastError(); // the failed allocation, not sticky: consume it
+  return fail(DFX_ERR_NO_MEMORY, "%s: out of device memory", what);
 }
 
 void clear_error() { g_last_error[0] = 0; }

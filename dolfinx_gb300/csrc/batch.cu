@@ -454,7 +454,7 @@ extern "C" int dfx_batch_create(int32_t capacity, dfx_batch* out)
       || cudaMalloc(&b->d_active, sizeof(int32_t) * (capacity + 1)) != cudaSuccess
       || cudaMallocHost(&b->h_active, sizeof(int32_t) * (capacity + 1)) != cudaSuccess
       || cudaMallocHost(&b->h_states, sizeof(BatchState) * capacity) != cudaSuccess)
-    st = dfx::fail(DFX_ERR_NO_MEMORY, "batch context: out of memory");
+    st = dfx::no_memory("batch context");
   if (!st)
   {
     cudaMemset(b->d_states, 0, sizeof(BatchState) * capacity);

@@ -19,6 +19,8 @@ int num_sms();
 
 // A small per-device status page owned by the library (allocated once per
 // device on first use): device kernels record error codes there.
+// DFX_ERR_NO_MEMORY after a failed allocation (the error is consumed).
+int no_memory(const char* what);
 int* device_status_page();
 
 inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }

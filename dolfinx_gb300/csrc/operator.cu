@@ -379,9 +379,9 @@ int finish_create(dfx_operator_s* op, const dfx_csr* A, dfx_operator* out, void*
 {
   int st = DFX_OK;
   if (cudaMalloc(&op->vals, dfx::value_bytes(*op)) != cudaSuccess)
-    st = dfx::fail(DFX_ERR_NO_MEMORY, "operator values: out of device memory");
+    st = dfx::no_memory("operator values");
   if (!st && cudaMalloc(&op->tmp, dfx::scratch_bytes(*op)) != cudaSuccess)
-    st = dfx::fail(DFX_ERR_NO_MEMORY, "operator scratch: out of device memory");
+    st = dfx::no_memory("operator scratch");
   if (st)
   {
     free_op(op);
@@ -697,7 +697,7 @@ extern "C" int dfx_operator_share(dfx_operator src, dfx_operator* out)
     if (op->vals)
       cudaFree(op->vals);
     delete op;
-    return dfx::fail(DFX_ERR_NO_MEMORY, "operator values: out of device memory");
+    return dfx::no_memory("operator values");
   }
   src->shares += 1;
   *out = op;

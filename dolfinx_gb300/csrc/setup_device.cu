@@ -371,3 +371,246 @@ extern "C" int dfx_sparsity_create_device(int32_t nrows, int32_t num_cells, int3
                      kRowCap);
   return h;
 }
+
+// ---------------------------------------------------------------------------
+// Lagrange P1/P2 dofmap of a tetrahedral mesh on the device: the numbering
+// of fem::create_dofmap (fem/dofmapbuilder.cpp:440-474, no reordering
+// function), i.e. dofs numbered by their first appearance in the cell loop
+// where cell c lists its dofs as (4 vertices, 6 edges in Basix order). The
+// host builder (setup.cpp) and this one use the same definition, so their
+// dofmaps are identical bit for bit:
+//   1. every entity's first position p = c nd + i, by atomic minimum
+//      (vertices by index; edges in an open-addressing table keyed by the
+//      sorted vertex pair);
+//   2. a mark at each first position, an exclusive scan of the marks;
+//   3. every position takes the scan value at its entity's first position.
+namespace
+{
+__constant__ int kDevEdges[6][2] = {{2, 3}, {1, 3}, {1, 2}, {0, 3}, {0, 2}, {0, 1}};
+constexpr uint64_t kEdgeEmpty = ~uint64_t(0);
+constexpr int kEdgeProbes = 1 << 12; // bounded probing; a full table reports UNSUPPORTED
+
+struct DofmapWork
+{
+  unsigned long long* vfirst; // num_vertices
+  unsigned long long* ekey;   // cap
+  unsigned long long* efirst; // cap
+  int64_t* mark;              // np + 1
+  int64_t* scratch;
+  int64_t cap;
+  size_t bytes;
+};
+
+int64_t edge_capacity(int64_t nc)
+{
+  // A Kuhn-split box has ~7/6 edges per cell, any tetrahedral mesh far
+  // fewer than 6: a power of two at least 2.5 edges per cell keeps the
+  // load of box meshes below one half.
+  int64_t cap = 1024;
+  while (cap < 5 * nc / 2 + 16)
+    cap <<= 1;
+  return cap;
+}
+
+DofmapWork carve_dofmap(void* base, int64_t nc, int64_t nv, int degree)
+{
+  DofmapWork w{};
+  char* p = (char*)base;
+  size_t off = 0;
+  auto take = [&](size_t b) -> char*
+  {
+    char* r = p ? p + off : nullptr;
+    off += a256(b);
+    return r;
+  };
+  const int nd = degree == 1 ? 4 : 10;
+  const int64_t np = nd * nc;
+  w.cap = degree == 2 ? edge_capacity(nc) : 1;
+  w.vfirst = (unsigned long long*)take(8 * (size_t)std::max<int64_t>(nv, 1));
+  w.ekey = (unsigned long long*)take(8 * (size_t)w.cap);
+  w.efirst = (unsigned long long*)take(8 * (size_t)w.cap);
+  w.mark = (int64_t*)take(8 * (size_t)(np + 1));
+  w.scratch = (int64_t*)take(8 * (size_t)dfx::scan_scratch_count(np + 1));
+  w.bytes = off;
+  return w;
+}
+
+__device__ __forceinline__ uint64_t mix64(uint64_t k)
+{
+  k ^= k >> 33;
+  k *= 0xff51afd7ed558ccdULL;
+  k ^= k >> 33;
+  k *= 0xc4ceb9fe1a85ec53ULL;
+  k ^= k >> 33;
+  return k;
+}
+
+__global__ void k_dofmap_init(DofmapWork w, int64_t nv)
+{
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += stride)
+    w.vfirst[i] = ~0ULL;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < w.cap; i += stride)
+  {
+    w.ekey[i] = kEdgeEmpty;
+    w.efirst[i] = ~0ULL;
+  }
+}
+
+// Step 1; edge dofs keep their table slot in the dofmap until step 3.
+template <int DEG>
+__global__ void k_dofmap_first(const int32_t* __restrict__ cells, int64_t nc, int64_t nv,
+                               DofmapWork w, int32_t* __restrict__ dofmap, int* status)
+{
+  constexpr int ND = DEG == 1 ? 4 : 10;
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc)
+    return;
+  const int4 v4 = __ldg(reinterpret_cast<const int4*>(cells) + c);
+  const int32_t v[4] = {v4.x, v4.y, v4.z, v4.w};
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+  {
+    if (v[i] < 0 || v[i] >= nv)
+    {
+      atomicExch(status, (int)DFX_ERR_INVALID);
+      return;
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+    atomicMin(w.vfirst + v[i], (unsigned long long)(ND * c + i));
+  if constexpr (DEG == 2)
+  {
+#pragma unroll
+    for (int e = 0; e < 6; ++e)
+    {
+      uint64_t a = (uint32_t)v[kDevEdges[e][0]], b = (uint32_t)v[kDevEdges[e][1]];
+      if (a > b)
+      {
+        const uint64_t t = a;
+        a = b;
+        b = t;
+      }
+      const uint64_t key = (a << 32) | b;
+      uint64_t slot = mix64(key) & (uint64_t)(w.cap - 1);
+      bool placed = false;
+      for (int probe = 0; probe < kEdgeProbes; ++probe)
+      {
+        const unsigned long long prev = atomicCAS(w.ekey + slot, kEdgeEmpty, key);
+        if (prev == kEdgeEmpty || prev == key)
+        {
+          placed = true;
+          break;
+        }
+        slot = (slot + 1) & (uint64_t)(w.cap - 1);
+      }
+      if (!placed)
+      {
+        atomicExch(status, (int)DFX_ERR_UNSUPPORTED);
+        return;
+      }
+      atomicMin(w.efirst + slot, (unsigned long long)(ND * c + 4 + e));
+      dofmap[ND * c + 4 + e] = (int32_t)slot;
+    }
+  }
+}
+
+// Step 2: marks at the first positions (the mark array was zeroed).
+__global__ void k_dofmap_mark(DofmapWork w, int64_t nv)
+{
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nv; i += stride)
+    if (w.vfirst[i] != ~0ULL)
+      w.mark[w.vfirst[i]] = 1;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < w.cap; i += stride)
+    if (w.ekey[i] != kEdgeEmpty)
+      w.mark[w.efirst[i]] = 1;
+}
+
+// Step 3 (mark now holds the exclusive scan).
+template <int DEG>
+__global__ void k_dofmap_number(const int32_t* __restrict__ cells, int64_t nc, DofmapWork w,
+                                int32_t* __restrict__ dofmap)
+{
+  constexpr int ND = DEG == 1 ? 4 : 10;
+  const int64_t c = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= nc)
+    return;
+  const int4 v4 = __ldg(reinterpret_cast<const int4*>(cells) + c);
+  const int32_t v[4] = {v4.x, v4.y, v4.z, v4.w};
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+    dofmap[ND * c + i] = (int32_t)w.mark[w.vfirst[v[i]]];
+  if constexpr (DEG == 2)
+#pragma unroll
+    for (int e = 0; e < 6; ++e)
+    {
+      const int32_t slot = dofmap[ND * c + 4 + e];
+      dofmap[ND * c + 4 + e] = (int32_t)w.mark[w.efirst[slot]];
+    }
+}
+} // namespace
+
+extern "C" size_t dfx_dofmap_device_workspace_bytes(int32_t num_cells, int32_t num_vertices,
+                                                    int32_t degree)
+{
+  if (num_cells < 0 || num_vertices < 0 || (degree != 1 && degree != 2))
+    return 0;
+  return carve_dofmap(nullptr, num_cells, num_vertices, degree).bytes;
+}
+
+extern "C" int dfx_dofmap_create_tet_device(int32_t num_cells, const int32_t* d_cells,
+                                            int32_t num_vertices, int32_t degree,
+                                            int32_t* d_dofmap, int32_t* num_nodes, void* d_work,
+                                            size_t work_bytes, void* stream)
+{
+  DFX_REQUIRE(degree == 1 || degree == 2, "Lagrange degree %d not supported", degree);
+  DFX_REQUIRE(num_cells >= 0 && num_vertices >= 0 && num_nodes, "invalid dofmap arguments");
+  DFX_REQUIRE(num_cells == 0 || (d_cells && d_dofmap), "cells and dofmap must be non-NULL");
+  DFX_REQUIRE((int64_t)num_cells * (degree == 1 ? 4 : 10) < INT32_MAX, "dofmap too large");
+  DFX_REQUIRE(((uintptr_t)d_cells & 15) == 0, "cells must be 16-byte aligned");
+  const DofmapWork need = carve_dofmap(nullptr, num_cells, num_vertices, degree);
+  DFX_REQUIRE(d_work && work_bytes >= need.bytes, "workspace too small (%zu < %zu bytes)",
+              work_bytes, need.bytes);
+  DFX_REQUIRE(((uintptr_t)d_work & 255) == 0, "workspace must be 256-byte aligned");
+  *num_nodes = 0;
+  if (num_cells == 0)
+    return DFX_OK;
+  cudaStream_t s = dfx::as_stream(stream);
+  const DofmapWork w = carve_dofmap(d_work, num_cells, num_vertices, degree);
+  const int nd = degree == 1 ? 4 : 10;
+  const int64_t np = (int64_t)nd * num_cells;
+  int* status = dfx::device_status_page();
+  DFX_REQUIRE(status, "could not allocate the status page");
+  DFX_CUDA(cudaMemsetAsync(status, 0, sizeof(int), s));
+  const unsigned sg = (unsigned)(8 * dfx::num_sms());
+  const unsigned cg = (unsigned)((num_cells + 255) / 256);
+  k_dofmap_init<<<sg, 256, 0, s>>>(w, num_vertices);
+  if (degree == 1)
+    k_dofmap_first<1><<<cg, 256, 0, s>>>(d_cells, num_cells, num_vertices, w, d_dofmap, status);
+  else
+    k_dofmap_first<2><<<cg, 256, 0, s>>>(d_cells, num_cells, num_vertices, w, d_dofmap, status);
+  DFX_CHECK_LAUNCH();
+  if (int h = read_status(status, s))
+  {
+    if (h == DFX_ERR_INVALID)
+      return dfx::fail(DFX_ERR_INVALID, "cell vertex index out of range [0, %d)", num_vertices);
+    return dfx::fail(DFX_ERR_UNSUPPORTED, "edge table full: use the host builder");
+  }
+  DFX_CUDA(cudaMemsetAsync(w.mark, 0, sizeof(int64_t) * (size_t)(np + 1), s));
+  k_dofmap_mark<<<sg, 256, 0, s>>>(w, num_vertices);
+  DFX_CHECK_LAUNCH();
+  if (int st = dfx::exclusive_scan(w.mark, w.mark, np, w.scratch, s))
+    return st;
+  if (degree == 1)
+    k_dofmap_number<1><<<cg, 256, 0, s>>>(d_cells, num_cells, w, d_dofmap);
+  else
+    k_dofmap_number<2><<<cg, 256, 0, s>>>(d_cells, num_cells, w, d_dofmap);
+  DFX_CHECK_LAUNCH();
+  int64_t total = 0;
+  DFX_CUDA(cudaMemcpyAsync(&total, w.mark + np, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  DFX_CUDA(cudaStreamSynchronize(s));
+  *num_nodes = (int32_t)total;
+  return DFX_OK;
+}

@@ -26,18 +26,43 @@ class FunctionSpace:
 
     def __init__(self, mesh: Mesh, degree: int, bs: int = 1, device="cuda"):
         self.mesh, self.degree, self.bs = mesh, int(degree), int(bs)
-        nd = 4 if degree == 1 else 10
-        self.dofmap = np.empty((mesh.num_cells, nd), np.int32)
-        n = C.c_int32(0)
-        _capi.check(_capi.lib().dfx_dofmap_create_tet(mesh.num_cells, mesh.cells.ctypes.data,
-                                                      self.degree, self.dofmap.ctypes.data,
-                                                      C.byref(n)))
-        self.num_nodes = int(n.value)
         self.device = device
         self._dofmap_dev = None
+        nd = 4 if degree == 1 else 10
+        built = False
+        if torch.device(device).type == "cuda" and mesh.num_cells > 0:
+            # the numbering on the device (bit-identical to the host builder)
+            built = self._dofmap_on_device(nd)
+        if not built:
+            self.dofmap = np.empty((mesh.num_cells, nd), np.int32)
+            n = C.c_int32(0)
+            _capi.check(_capi.lib().dfx_dofmap_create_tet(mesh.num_cells,
+                                                          mesh.cells.ctypes.data, self.degree,
+                                                          self.dofmap.ctypes.data, C.byref(n)))
+            self.num_nodes = int(n.value)
         self._sparsity = None
         self._sparsity_dev = None
         self._colouring = None
+
+    def _dofmap_on_device(self, nd: int) -> bool:
+        """dfx_dofmap_create_tet_device; False when its edge table overflows
+        (the host builder then applies)."""
+        m = self.mesh
+        cells, _ = m.device(self.device)
+        L = _capi.lib()
+        wb = int(L.dfx_dofmap_device_workspace_bytes(m.num_cells, m.num_nodes, self.degree))
+        work = torch.empty(wb, dtype=torch.uint8, device=self.device)
+        dm = torch.empty((m.num_cells, nd), dtype=torch.int32, device=self.device)
+        n = C.c_int32(0)
+        rc = L.dfx_dofmap_create_tet_device(m.num_cells, _ptr(cells), m.num_nodes, self.degree,
+                                            _ptr(dm), C.byref(n), _ptr(work), wb, _stream())
+        if rc == _capi.DFX_ERR_UNSUPPORTED:
+            return False
+        _capi.check(rc)
+        self.num_nodes = int(n.value)
+        self._dofmap_dev = dm
+        self.dofmap = dm.cpu().numpy()
+        return True
 
     @property
     def num_dofs(self) -> int:

@@ -308,8 +308,11 @@ class Server:
                 self.used -= st.bytes
                 del self.structures[key]
                 drop_structure(*key)
-                _log.logger.info("structure n=%s P%s evicted (%s bytes)", key[0], key[1],
-                                 st.bytes)
+                del st
+                # The structure's tensors go back to torch's cache; return them
+                # to the device so the library's own allocations can use them.
+                torch.cuda.empty_cache()
+                _log.logger.info("structure n=%s P%s evicted", key[0], key[1])
 
     def prewarm(self, requests):
         for key in sorted({(r.n, r.degree) for r in requests}):

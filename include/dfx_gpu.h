@@ -147,6 +147,18 @@ int dfx_graph_reorder_rcm(int32_t n, const int32_t* offsets, const int32_t* adj,
 int dfx_dofmap_create_tet(int32_t num_cells, const int32_t* cells, int32_t degree,
                           int32_t* dofmap, int32_t* num_nodes);
 
+/* The same dofmap built on the device (fem::create_dofmap numbering:
+ * first appearance in the cell loop, fem/dofmapbuilder.cpp:440-474):
+ * bit-identical to dfx_dofmap_create_tet. d_cells 16-byte aligned, vertex
+ * indices in [0, num_vertices); d_dofmap (num_cells x 4 or 10). Workspace
+ * of dfx_dofmap_device_workspace_bytes, 256-byte aligned. Returns
+ * DFX_ERR_UNSUPPORTED when the edge table overflows (meshes with more than
+ * ~2.5 edges per cell): the host builder then applies. Synchronises. */
+size_t dfx_dofmap_device_workspace_bytes(int32_t num_cells, int32_t num_vertices, int32_t degree);
+int dfx_dofmap_create_tet_device(int32_t num_cells, const int32_t* d_cells, int32_t num_vertices,
+                                 int32_t degree, int32_t* d_dofmap, int32_t* num_nodes,
+                                 void* d_work, size_t work_bytes, void* stream);
+
 /* fem::create_sparsity_pattern + SparsityPattern::finalize
  * (fem/utils.h:197-314, la/SparsityPattern.cpp:264-491) for a cell integral
  * with the same dofmap on both sides. Two-phase: call with cols == NULL to

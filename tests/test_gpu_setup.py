@@ -178,3 +178,57 @@ def test_device_sparsity_matches_reference(cuda, capi, tag):
     rp, cols = _device_sparsity(capi, rp_ref.size - 1, dm)
     np.testing.assert_array_equal(rp, rp_ref)
     np.testing.assert_array_equal(cols, cols_ref)
+
+
+@pytest.mark.parametrize("deg", [1, 2])
+@pytest.mark.parametrize("n,reorder", [((1, 1, 1), True), ((5, 3, 4), True), ((24, 24, 24), True),
+                                       ((30, 20, 26), False)])
+def test_device_dofmap_matches_host(cuda, capi, oracle, n, reorder, deg):
+    """The device dofmap builder (first positions by atomic minimum, an edge
+    hash table, a scan) gives the host builder's and the oracle's numbering
+    bit for bit, in RCM and in build order."""
+    from dolfinx_gb300 import fem, mesh
+
+    m = mesh.create_box(((0, 0, 0), (1, 1, 1)), n, reorder=reorder)
+    Vd = fem.functionspace(m, ("Lagrange", deg))          # built on the device
+    Vh = fem.functionspace(m, ("Lagrange", deg), device="cpu")
+    assert Vd._dofmap_dev is not None
+    assert Vd.num_nodes == Vh.num_nodes
+    np.testing.assert_array_equal(Vd.dofmap, Vh.dofmap)
+    np.testing.assert_array_equal(Vd.dofmap_device().cpu().numpy(), Vh.dofmap)
+    dm, nn = oracle.dofmap_tet(m.cells, deg)
+    assert nn == Vd.num_nodes
+    np.testing.assert_array_equal(Vd.dofmap, dm)
+
+
+def test_device_dofmap_p2_64_matches_golden(cuda, capi):
+    """The 64^3 P2 dofmap built on the device has the golden digest."""
+    import hashlib
+    import json
+    import os
+
+    from dolfinx_gb300 import fem, mesh
+
+    ref = json.load(open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                                      "config_structure.json")))["c2_p2_unit_cube_64"]
+    V = fem.functionspace(mesh.create_unit_cube(64, 64, 64), ("Lagrange", 2))
+    assert V._dofmap_dev is not None and V.num_nodes == ref["num_nodes"]
+    got = hashlib.sha256(np.ascontiguousarray(V.dofmap_device().cpu().numpy()).tobytes())
+    assert got.hexdigest() == ref["dofmap"]
+
+
+def test_device_dofmap_rejects_bad_vertices(cuda, capi):
+    import ctypes as C
+
+    import torch
+
+    cells = torch.tensor([[0, 1, 2, 7]], dtype=torch.int32, device="cuda")
+    lib = capi.lib()
+    wb = int(lib.dfx_dofmap_device_workspace_bytes(1, 4, 2))
+    work = torch.empty(wb, dtype=torch.uint8, device="cuda")
+    dm = torch.empty((1, 10), dtype=torch.int32, device="cuda")
+    n = C.c_int32(0)
+    rc = lib.dfx_dofmap_create_tet_device(1, C.c_void_p(cells.data_ptr()), 4, 2,
+                                          C.c_void_p(dm.data_ptr()), C.byref(n),
+                                          C.c_void_p(work.data_ptr()), wb, None)
+    assert rc == capi.DFX_ERR_INVALID
