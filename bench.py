@@ -73,6 +73,9 @@ def parse():
                    help="apply the Q4 operator only (for an ncu capture of k_q4_cells)")
     p.add_argument("--profile-q4-tc", action="store_true",
                    help="apply the tensor-core Q4 action only (ncu capture of k_q4_cells_tc)")
+    p.add_argument("--profile-split", type=int, default=0, metavar="NY",
+                   help="elasticity on a 4NY x NY x NY box: apply the FP64 and the split "
+                        "FP32-word operators twice each (ncu capture of k_sell_spmv_split)")
     p.add_argument("--profile-step", action="store_true",
                    help="run one mixed-precision P2 Poisson step only (for an ncu launch list)")
     p.add_argument("--profile", action="store_true",
@@ -1035,6 +1038,9 @@ def run_profile_step(args):
     torch.cuda.set_device(0)
     m, kappa, f = make_inputs(args.n, seed=0)
     P = Problem(m, kappa, f, mode=args.mode, inner_rtol=args.inner_rtol, variant=args.ir_variant)
+    # Launch shapes timed under a profiler are not the plain run's: pin the
+    # FP32 SpMV's load chunk to the plain run's choice.
+    P.ir.op32.set_chunk(4)
     torch.cuda.synchronize()
     r = P.step_ir()
     torch.cuda.synchronize()
@@ -1082,8 +1088,38 @@ def run_profile_q4_tc(args):
     print(json.dumps({"profile_q4_tc": "ok", "cells": n ** 3, "dofs": op.n}))
 
 
+def run_profile_split(args):
+    """Vector P2 elasticity on [0,4]x[0,1]^2 with 4NY x NY x NY hexahedra x 6,
+    expanded to the scalar CSR; the FP64 and the split operators applied
+    twice each: the run behind an ncu capture of k_sell_spmv_split."""
+    import numpy as np
+    import torch
+
+    from dolfinx_gb300 import fem, la, mesh
+
+    torch.cuda.set_device(0)
+    ny = args.profile_split
+    m = mesh.create_box(((0.0, 0.0, 0.0), (4.0, 1.0, 1.0)), (4 * ny, ny, ny))
+    V = fem.functionspace(m, ("Lagrange", 2, (3,)))
+    E = np.exp(np.random.default_rng(3).normal(np.log(1e3), 0.5, m.num_cells))
+    S = fem.assemble_matrix(fem.elasticity_form(V, torch.from_numpy(E).cuda(), 0.3)).expand_blocks()
+    o64 = la.SellOperator(S, torch.float64, 1024)
+    osp = la.SellOperator(S, torch.float64, 1024, split=True)
+    x = torch.rand(S.nrows, dtype=torch.float64, device="cuda")
+    y = torch.empty_like(x)
+    for _ in range(2):
+        o64.apply_renumbered(x, y)
+        osp.apply_renumbered(x, y)
+    torch.cuda.synchronize()
+    print(json.dumps({"profile_split": "ok", "rows": S.nrows, "nnz": S.nnz,
+                      "slots": osp.info()["slots"]}))
+
+
 def main():
     args = parse()
+    if args.profile_split:
+        run_profile_split(args)
+        return
     if args.serving_sweep:
         serving_sweep(args)
         return

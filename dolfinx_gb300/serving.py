@@ -251,15 +251,28 @@ class Job:
     def solution(self) -> torch.Tensor:
         return self.op64.from_operator(self.xp)
 
+    def release_device(self) -> None:
+        """Drop the request's device buffers (matrix values, operator values,
+        vectors, coefficients) once its solution is on the host: a finished
+        request keeps only x, its status and its timings."""
+        for name in ("A", "op64", "op32", "b", "dinv", "bp", "dp", "xp", "kappa", "f"):
+            setattr(self, name, None)
+
 
 class Server:
     """Continuous-batching server (one GPU)."""
 
     def __init__(self, mode: str = "mixed", hbm_budget: float = 64e9, capacity: int = 512,
                  quantum: int = 25, batch_max_dofs: int = 65536, rtol: float = 1e-10,
-                 workers: int = 2, delta: float = 0.01, assembly: str = "atomic"):
+                 workers: int = 2, delta: float = 0.01, assembly: str = "atomic",
+                 retain_systems: bool = False):
         """assembly: "atomic" (FP64 atomics) or "coloured" (deterministic
-        summation order, so a request's matrix is bitwise reproducible)."""
+        summation order, so a request's matrix is bitwise reproducible).
+        retain_systems: finished requests keep their device matrix and
+        vectors (for checks); by default they are released when the
+        solution reaches the host, so a long stream holds only the requests
+        in flight."""
+        self.retain_systems = bool(retain_systems)
         if mode not in ("mixed", "fp64"):
             raise ValueError(f'mode must be "mixed" or "fp64" (got {mode!r})')
         if assembly not in ("atomic", "coloured", "colored"):
@@ -381,6 +394,8 @@ class Server:
         return job
 
     def _release(self, job: Job):
+        if not self.retain_systems:
+            job.release_device()
         with self.lock:
             self.used -= job.bytes
             job.st.users -= 1

@@ -624,14 +624,44 @@ public:
     return a;
   }
 
+  /// L(v) = int_F avg(g) avg(v) dS over interior facets given as (cell0,
+  /// facet0, cell1, facet1) quads (all of them when empty).
+  static Form interior_facet_source(std::shared_ptr<const FunctionSpace> V,
+                                    std::span<const double> g = {}, double g_const = 1.0,
+                                    std::span<const std::int32_t> facets = {})
+  {
+    Form L = source(std::move(V), g, g_const);
+    L.set_interior_facets(facets);
+    return L;
+  }
+  /// a(u,v) = int_F gamma |F| [grad u . n][grad v . n] dS (continuous
+  /// interior penalty), gamma per cell (averaged over the facet's two
+  /// cells) or gamma_const. Its matrix needs the facets' macro-element
+  /// couplings: create_matrix adds them.
+  static Form interior_penalty(std::shared_ptr<const FunctionSpace> V,
+                               std::span<const double> gamma = {}, double gamma_const = 1.0,
+                               std::span<const std::int32_t> facets = {})
+  {
+    if (V->bs() != 1)
+      throw Error(DFX_ERR_INVALID, "facet forms need a scalar space");
+    Form a(DFX_FORM_FACET_JUMP, std::move(V));
+    a.set_kappa(gamma, gamma_const);
+    a.set_interior_facets(facets);
+    return a;
+  }
+
   const FunctionSpace& function_space() const { return *V_; }
   bool bilinear() const
   {
     return kind_ == DFX_FORM_POISSON || kind_ == DFX_FORM_ELASTICITY ||
-           kind_ == DFX_FORM_FACET_MASS;
+           kind_ == DFX_FORM_FACET_MASS || kind_ == DFX_FORM_FACET_JUMP;
   }
-  /// An exterior-facet integral (else a cell integral).
+  /// A facet integral, exterior or interior (else a cell integral).
   bool on_facets() const { return num_facets_ >= 0; }
+  /// An interior-facet integral (dS).
+  bool interior() const { return interior_; }
+  /// The interior facets as host quads (for the sparsity pattern).
+  const std::vector<std::int32_t>& host_facets() const { return host_facets_; }
   const std::int32_t* device_facets() const { return facets_.data(); }
   std::int32_t num_facets() const { return num_facets_; }
 
@@ -683,7 +713,26 @@ private:
     facets_.assign(f);
     num_facets_ = (std::int32_t)(f.size() / 2);
   }
+  void set_interior_facets(std::span<const std::int32_t> facets)
+  {
+    if (V_->bs() != 1)
+      throw Error(DFX_ERR_INVALID, "facet forms need a scalar space");
+    std::vector<std::int32_t> f(facets.begin(), facets.end());
+    if (f.empty())
+      f = mesh::interior_facets(V_->mesh());
+    if (f.size() % 4)
+      throw Error(DFX_ERR_INVALID, "interior facets must be (cell, facet, cell, facet) quads");
+    for (std::size_t i = 0; i < f.size(); i += 2)
+      if (f[i] < 0 || f[i] >= V_->mesh().num_cells || f[i + 1] < 0 || f[i + 1] > 3)
+        throw Error(DFX_ERR_INVALID, "interior facets must be quads of cells of the mesh");
+    facets_.assign(f);
+    num_facets_ = (std::int32_t)(f.size() / 4);
+    interior_ = true;
+    host_facets_ = std::move(f);
+  }
   int kind_;
+  bool interior_ = false;
+  std::vector<std::int32_t> host_facets_;
   std::shared_ptr<const FunctionSpace> V_;
   device_vector<double> kappa_, f_;
   device_vector<std::int32_t> facets_;
@@ -777,7 +826,33 @@ inline Lifting lifting_data(const FunctionSpace& V, const BCs& bcs)
 /// A zeroed matrix with the sparsity pattern of the form's space.
 inline la::MatrixCSR create_matrix(const Form& a)
 {
-  return la::MatrixCSR(create_sparsity_pattern(a.function_space()), a.function_space().bs());
+  if (!a.interior())
+    return la::MatrixCSR(create_sparsity_pattern(a.function_space()), a.function_space().bs());
+  // sparsitybuild::cells + interior_facets: the cells, each listed twice so
+  // that every element has 2 nd dofs (repeats are dropped), then every
+  // facet's macro element (both cells' dofs).
+  const FunctionSpace& V = a.function_space();
+  const int nd = V.degree() == 1 ? 4 : 10;
+  const std::span<const std::int32_t> dm = V.dofmap();
+  const std::vector<std::int32_t>& q = a.host_facets();
+  const std::int64_t nc = V.mesh().num_cells, nf = (std::int64_t)q.size() / 4;
+  std::vector<std::int32_t> macro((std::size_t)(nc + nf) * 2 * nd);
+  for (std::int64_t c = 0; c < nc; ++c)
+    for (int k = 0; k < 2 * nd; ++k)
+      macro[(std::size_t)c * 2 * nd + k] = dm[(std::size_t)c * nd + k % nd];
+  for (std::int64_t e = 0; e < nf; ++e)
+    for (int k = 0; k < 2 * nd; ++k)
+      macro[(std::size_t)(nc + e) * 2 * nd + k] =
+          dm[(std::size_t)q[4 * e + 2 * (k / nd)] * nd + k % nd];
+  SparsityPattern sp;
+  sp.row_ptr.resize((std::size_t)V.num_nodes() + 1);
+  std::int64_t nnz = 0;
+  check(dfx_sparsity_create(V.num_nodes(), (std::int32_t)(nc + nf), 2 * nd, macro.data(),
+                            sp.row_ptr.data(), nullptr, &nnz));
+  sp.cols.resize((std::size_t)nnz);
+  check(dfx_sparsity_create(V.num_nodes(), (std::int32_t)(nc + nf), 2 * nd, macro.data(),
+                            sp.row_ptr.data(), sp.cols.data(), &nnz));
+  return la::MatrixCSR(sp, V.bs());
 }
 
 /// fem::assemble_matrix (fem/assembler.h:513-602): A += the cell
@@ -796,7 +871,10 @@ inline void assemble_matrix(la::MatrixCSR& A, const Form& a, const BCs& bcs = {}
   const dfx_form f = a.c();
   const dfx_csr csr = A.csr();
   const std::int8_t* bc = l ? l->markers.data() : nullptr;
-  if (a.on_facets())
+  if (a.interior())
+    check(dfx_assemble_matrix_interior_facets(&f, a.device_facets(), a.num_facets(), &csr, bc,
+                                              nullptr));
+  else if (a.on_facets())
     check(dfx_assemble_matrix_facets(&f, a.device_facets(), a.num_facets(), &csr, nullptr, bc,
                                      nullptr));
   else
@@ -822,7 +900,10 @@ inline void assemble_vector(device_vector<double>& b, const Form& L)
   if (b.size() != (std::size_t)L.function_space().num_dofs())
     throw Error(DFX_ERR_INVALID, "b must have num_dofs entries");
   const dfx_form f = L.c();
-  if (L.on_facets())
+  if (L.interior())
+    check(dfx_assemble_vector_interior_facets(&f, L.device_facets(), L.num_facets(), b.data(),
+                                              nullptr));
+  else if (L.on_facets())
     check(dfx_assemble_vector_facets(&f, L.device_facets(), L.num_facets(), b.data(), nullptr));
   else
     check(dfx_assemble_vector(&f, b.data(), DFX_MODE_ATOMIC, nullptr, nullptr, 0, nullptr));
@@ -852,13 +933,19 @@ inline void apply_lifting(device_vector<double>& b, const Form& a, const BCs& bc
 {
   if (bcs.empty())
     return;
-  if (a.on_facets())
-    throw Error(DFX_ERR_UNSUPPORTED, "lifting of exterior-facet terms is not supported");
   const FunctionSpace& V = a.function_space();
   if (b.size() != (std::size_t)V.num_dofs() || (x0 && x0->size() != b.size()))
     throw Error(DFX_ERR_INVALID, "b (and x0) must have num_dofs entries");
   const detail::Lifting l = detail::lifting_data(V, bcs);
   const dfx_form f = a.c();
+  if (a.on_facets())
+  {
+    // lift_bc over the facet domain (exterior mass or interior penalty)
+    check(dfx_apply_lifting_facets(&f, a.device_facets(), a.num_facets(), a.interior() ? 1 : 0,
+                                   b.data(), l.markers.data(), l.g.data(),
+                                   x0 ? x0->data() : nullptr, alpha, nullptr));
+    return;
+  }
   check(dfx_apply_lifting(&f, b.data(), l.markers.data(), l.g.data(), x0 ? x0->data() : nullptr,
                           alpha, DFX_MODE_ATOMIC, nullptr, nullptr, 0, nullptr));
 }

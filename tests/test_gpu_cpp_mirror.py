@@ -2,7 +2,8 @@
 assembles and solves P1 Poisson on a 4^3 x 6 box through it (matrix,
 diagonal, vector, lifting, set_bc, FP64 CG, FP32-inner refinement), then
 takes a(u, u) and the Neumann vector of 1 on the boundary, whose entries sum
-to the boundary's area."""
+to the boundary's area, and assembles the interior penalty on its
+macro-element pattern (zero on a linear function) and lifts through it."""
 
 import os
 import shutil
@@ -41,3 +42,5 @@ def test_cpp_mirror_assembles_and_solves(cuda, capi, tmp_path):
     assert ir_status == 0 and inner > 0
     assert float(got["energy"][0]) > 0.0
     assert abs(float(got["boundary_area"][0]) - 6.0) < 1e-12
+    assert float(got["penalty_linear"][0]) < 1e-10
+    assert got["penalty_lifting_ok"] == ["1"]

@@ -29,7 +29,8 @@ def test_batched_cg_meets_fp64_stopping_test(cuda, oracle, capi, mode):
 
     reqs = [serving.Request(i, n, d, k2, 100 + i) for i, (n, d, k2) in
             enumerate([(6, 1, 0.0), (5, 2, 3.0), (9, 1, 7.5), (4, 2, 0.5)])]
-    stats, jobs = serving.serve(reqs, mode=mode, hbm_budget=8e9, quantum=10)
+    stats, jobs = serving.serve(reqs, mode=mode, hbm_budget=8e9, quantum=10,
+                                retain_systems=True)
     assert stats["failed"] == []
     for job in jobs:
         assert job.slot is not None  # all went through the batched kernel
@@ -63,7 +64,8 @@ def test_whole_gpu_path_for_large_requests(cuda, oracle, capi):
     from dolfinx_gb300 import serving
 
     reqs = [serving.Request(0, 12, 2, 1.0, 5), serving.Request(1, 5, 1, 2.0, 6)]
-    stats, jobs = serving.serve(reqs, mode="mixed", hbm_budget=8e9, batch_max_dofs=2000)
+    stats, jobs = serving.serve(reqs, mode="mixed", hbm_budget=8e9, batch_max_dofs=2000,
+                                retain_systems=True)
     assert stats["failed"] == []
     big = [j for j in jobs if j.req.rid == 0][0]
     assert big.slot is None  # above batch_max_dofs: whole-GPU solver
@@ -97,7 +99,7 @@ def test_concurrent_whole_gpu_workers(cuda, oracle, capi):
     reqs = [serving.Request(i, 9 + i % 3, 1 + i % 2, 0.5 * i, 40 + i, 0.0) for i in range(6)]
     for mode in ("mixed", "fp64"):
         stats, jobs = serving.serve(reqs, mode=mode, hbm_budget=8e9, batch_max_dofs=100,
-                                    workers=2)
+                                    workers=2, retain_systems=True)
         assert stats["failed"] == []
         assert all(j.slot is None for j in jobs)
         for job in jobs:
