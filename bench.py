@@ -670,11 +670,12 @@ def serving_sweep(args):
     and tunes the structures of every (n, degree) the draws contain, then
     serves --serving-repeats runs of --serving-requests requests per rate
     (each repeat its own request draw: seeds 100 + repeat). The server's
-    HBM budget (120 GB of structures and request values) is below what all
-    178 structures of n in [8, 96] need, so least-recently used structures
-    are evicted and rebuilt when a later request needs them, inside the
-    timed runs, as a long-running server would. Reports per rate and mode
-    the median, min and max of solves/s, p50 and p99 latency."""
+    HBM budget is 200 GB of structures and request values, counted from the
+    tensors and operators each one holds; should the structures a stream
+    needs not fit, least-recently used ones are evicted and rebuilt when a
+    later request needs them, inside the timed runs, as a long-running
+    server would. Reports per rate and mode the median, min and max of
+    solves/s, p50 and p99 latency, and the structures' total bytes."""
     import statistics
     import time
 
@@ -683,7 +684,7 @@ def serving_sweep(args):
     from dolfinx_gb300 import serving
 
     torch.cuda.set_device(0)
-    budget = 120e9
+    budget = 200e9
     nreq, reps = args.serving_requests, args.serving_repeats
     draws = {(rate, r): serving.make_requests(nreq, rate, seed=100 + r,
                                                n_range=(8, args.serving_nmax))
@@ -701,6 +702,7 @@ def serving_sweep(args):
             t0 = time.perf_counter()
             srv.prewarm(everything)
             out["structure_setup_s"][mode] = time.perf_counter() - t0
+            out.setdefault("structures_resident_bytes", {})[mode] = srv.used
             for row, rate in zip(out["rates"], SERVING_RATES):
                 runs = [srv.run(draws[(rate, r)], max_wall_s=600.0) for r in range(reps)]
                 row[mode] = {k: {"median": statistics.median(st[k] for st in runs),
@@ -710,6 +712,7 @@ def serving_sweep(args):
                 row[mode]["failed"] = sum(len(st["failed"]) for st in runs)
         finally:
             srv.close()
+            del srv
     for row in out["rates"]:
         row["mixed_over_fp64_solves_median"] = (row["mixed"]["solves_per_s"]["median"]
                                                 / row["fp64"]["solves_per_s"]["median"])

@@ -133,6 +133,14 @@ _SIGS = {
     "dfx_mesh_create_box_tet": (C.c_int, [C.c_int32] * 3 + [_P, _P, C.c_int32, _P, _P]),
     "dfx_mesh_dual_graph_tet": (C.c_int, [C.c_int32, _P, C.c_int32, _P, _P]),
     "dfx_graph_reorder_rcm": (C.c_int, [C.c_int32, _P, _P, _P]),
+    "dfx_mesh_dual_graph_tet_device_workspace_bytes": (C.c_size_t, [C.c_int32, C.c_int32]),
+    "dfx_mesh_dual_graph_tet_device": (C.c_int, [C.c_int32, _P, C.c_int32, _P, _P, _P,
+                                                 C.c_size_t, _P]),
+    "dfx_graph_reorder_rcm_device_workspace_bytes": (C.c_size_t, [C.c_int32]),
+    "dfx_graph_reorder_rcm_device": (C.c_int, [C.c_int32, _P, _P, _P, _P, C.c_size_t, _P]),
+    "dfx_mesh_create_box_tet_device_workspace_bytes": (C.c_size_t, [C.c_int32] * 4),
+    "dfx_mesh_create_box_tet_device": (C.c_int, [C.c_int32] * 3 + [_P, _P, C.c_int32, _P, _P, _P,
+                                                                   C.c_size_t, _P]),
     "dfx_dofmap_create_tet": (C.c_int, [C.c_int32, _P, C.c_int32, _P, _P]),
     "dfx_sparsity_create": (C.c_int, [C.c_int32, C.c_int32, C.c_int32, _P, _P, _P, _P]),
     "dfx_sparsity_device_workspace_bytes": (C.c_size_t, [C.c_int32, C.c_int32, C.c_int32]),
@@ -195,6 +203,8 @@ _SIGS = {
     "dfx_operator_info": (C.c_int, [_P, C.POINTER(C.c_int64), C.POINTER(C.c_int32),
                                     C.POINTER(C.c_void_p)]),
     "dfx_operator_destroy": (C.c_int, [_P]),
+    "dfx_operator_device_bytes": (C.c_int, [_P, C.POINTER(C.c_size_t)]),
+    "dfx_operator_release_values": (C.c_int, [_P]),
     "dfx_operator_share": (C.c_int, [_P, C.POINTER(C.c_void_p)]),
     "dfx_operator_permute": (C.c_int, [_P, _P, _P, C.c_int32, _P]),
     "dfx_batch_workspace_bytes": (C.c_size_t, [C.c_int64, C.c_int32]),

@@ -54,7 +54,11 @@ def _compile(src: str, verbose_ptxas: bool) -> str:
         if verbose_ptxas:
             cmd.insert(1, "-Xptxas=-v")
     else:
-        cmd = ["g++", "-O3", "-std=c++20", "-fPIC", "-Wall", "-I", INCLUDE,
+        # -ffp-contract=off: a*b+c rounds twice on aarch64 as on x86-64
+        # (no FMA contraction), so the host set-up gives the same doubles
+        # on both, and the same as the device's explicitly unfused
+        # arithmetic where the two must agree bit for bit.
+        cmd = ["g++", "-O3", "-std=c++20", "-fPIC", "-Wall", "-ffp-contract=off", "-I", INCLUDE,
                "-I", "/usr/local/cuda/include", "-c", src, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:

@@ -493,6 +493,8 @@ extern "C" int dfx_batch_set(dfx_batch b, int32_t slot, const dfx_batch_system* 
                                  && sys->op32->nslices == sys->op64->nslices
                                  && sys->op32->sigma == sys->op64->sigma),
               "FP32 and FP64 operators must share one structure");
+  DFX_REQUIRE(sys->op64->vals && (sys->mode == 0 || sys->op32->vals),
+              "operator values were released (dfx_operator_release_values): use a share");
   DFX_REQUIRE(sys->b && sys->x && sys->work, "b, x and work must be non-NULL");
   DFX_REQUIRE(((uintptr_t)sys->work & 255) == 0, "workspace must be 256-byte aligned");
   DFX_REQUIRE(sys->rtol > 0.0 && sys->max_iters > 0, "rtol and max_iters must be positive");

@@ -449,8 +449,12 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // y = A p, p.y -- sliced-ELL operator, one row per lane, warp per slice.
+// 12 resident blocks per SM (48 warps) for chunks of up to 4 loads: the SpMV
+// is bound by the latency of its loads, and with more registers per thread (48
+// when left to ptxas) only 10 blocks fit and the FP32 inner iteration ran
+// ~9 us slower at P2 64^3. Chunks of 8 keep 8 blocks so that they do not spill.
 template <typename V, typename T, bool COMP, int CH = 4>
-__global__ void __launch_bounds__(kSellThreads)
+__global__ void __launch_bounds__(kSellThreads, CH >= 8 ? 8 : 12)
     k_spmv_dot_sell(const dfx_operator_s op, Work<T> w)
 {
   block_reduce_init();
@@ -1530,6 +1534,7 @@ extern "C" int dfx_cg_solve_op(dfx_operator op, const double* d_b, double* d_x,
   DFX_REQUIRE(op, "operator is NULL");
   DFX_REQUIRE(op->dtype == DFX_F64 || op->dtype == DFX_F32X2,
               "dfx_cg_solve_op needs an FP64 or split (DFX_F32X2) operator");
+  DFX_REQUIRE(op->vals, "operator values were released (dfx_operator_release_values): use a share");
   if (int st = check_solve_args(d_b, d_x, d_work, rtol, max_iters))
     return st;
   const int64_t n = op->n;
@@ -1603,6 +1608,7 @@ extern "C" int dfx_ir_solve(dfx_operator op64, dfx_operator op32, const double* 
   DFX_REQUIRE(op64->n == op32->n && op64->sigma == op32->sigma && op64->nslices == op32->nslices
                   && op64->csr_nnz == op32->csr_nnz,
               "inner and outer operators must come from the same matrix and sigma");
+  DFX_REQUIRE(op64->vals && op32->vals, "operator values were released (dfx_operator_release_values): use a share");
   if (int st = check_solve_args(d_b, d_x, d_work, rtol, max_outer))
     return st;
   DFX_REQUIRE(inner_rtol > 0.0 && inner_rtol < 1.0 && max_inner > 0,

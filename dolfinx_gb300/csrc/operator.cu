@@ -120,12 +120,16 @@ void free_op(dfx_operator_s* op)
   cudaGetDevice(&cur);
   cudaSetDevice(op->device);
   if (op->owns_structure)
+  {
     for (void* p : {(void*)op->perm, (void*)op->iperm, (void*)op->slice_ptr, (void*)op->cols,
                     (void*)op->delta, (void*)op->first, (void*)op->map})
       if (p)
         cudaFree(p);
+  }
   else if (op->source)
+  {
     op->source->shares -= 1;
+  }
   for (void* p : {op->vals, op->tmp})
     if (p)
       cudaFree(p);
@@ -651,6 +655,7 @@ extern "C" int dfx_operator_create_ex(const dfx_csr* A, int32_t sigma, int32_t d
 extern "C" int dfx_operator_update_values(dfx_operator op, const dfx_csr* A, void* stream)
 {
   DFX_REQUIRE(op && A && A->vals, "operator and matrix must be non-NULL");
+  DFX_REQUIRE(op->vals, "operator values were released (dfx_operator_release_values): use a share");
   DFX_REQUIRE(A->dtype == DFX_F64, "values are refilled from FP64 CSR values");
   DFX_REQUIRE(A->nnz == op->csr_nnz && A->nrows == op->n, "matrix does not match the operator");
   if (op->nslots == 0)
@@ -729,9 +734,48 @@ extern "C" int dfx_operator_info(dfx_operator op, int64_t* nslots, int32_t* nsli
   return DFX_OK;
 }
 
+extern "C" int dfx_operator_release_values(dfx_operator op)
+{
+  DFX_REQUIRE(op, "operator is NULL");
+  DFX_REQUIRE(op->owns_structure, "only a structure's own operator releases its values");
+  int cur = 0;
+  cudaGetDevice(&cur);
+  cudaSetDevice(op->device);
+  for (void* p : {op->vals, op->tmp})
+    if (p)
+      cudaFree(p);
+  cudaSetDevice(cur);
+  op->vals = nullptr;
+  op->tmp = nullptr;
+  op->serial = dfx::next_operator_serial();
+  return DFX_OK;
+}
+
+extern "C" int dfx_operator_device_bytes(dfx_operator op, size_t* bytes)
+{
+  DFX_REQUIRE(op && bytes, "arguments must be non-NULL");
+  // The allocations of the build (structure, owners only) and of
+  // finish_create / dfx_operator_share (values and scratch, every operator).
+  size_t b = op->vals ? dfx::value_bytes(*op) + dfx::scratch_bytes(*op) : 0;
+  if (op->owns_structure)
+  {
+    const size_t n = (size_t)std::max<int32_t>(op->n, 1);
+    const size_t ms = (size_t)std::max<int64_t>(op->nslots, 1);
+    b += 2 * sizeof(int32_t) * n + sizeof(int64_t) * ((size_t)op->nslices + 1);
+    b += sizeof(int32_t) * ms; // map
+    if (op->delta)
+      b += sizeof(uint16_t) * ms + sizeof(int32_t) * std::max<size_t>(32 * (size_t)op->nslices, 1);
+    if (op->cols)
+      b += sizeof(int32_t) * ms;
+  }
+  *bytes = b;
+  return DFX_OK;
+}
+
 extern "C" int dfx_operator_apply(dfx_operator op, const void* d_x, void* d_y, void* stream)
 {
   DFX_REQUIRE(op, "operator is NULL");
+  DFX_REQUIRE(op->vals, "operator values were released (dfx_operator_release_values): use a share");
   const int32_t n = op->n;
   if (n == 0)
     return DFX_OK; // empty vectors may have NULL data
@@ -775,6 +819,7 @@ extern "C" int dfx_operator_apply_renumbered(dfx_operator op, const void* d_x, v
                                              void* stream)
 {
   DFX_REQUIRE(op, "operator is NULL");
+  DFX_REQUIRE(op->vals, "operator values were released (dfx_operator_release_values): use a share");
   if (op->n == 0)
     return DFX_OK; // empty vectors may have NULL data
   DFX_REQUIRE(d_x && d_y, "arguments must be non-NULL");

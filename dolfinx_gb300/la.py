@@ -236,6 +236,7 @@ class SellOperator:
         """build: where the structure is built (0 device with host fallback,
         1 device only, 2 host); every place gives the same operator."""
         self.A, self.dtype, self.sigma = A, dtype, sigma
+        self.csr_nnz = A.nnz if A is not None else share_of.csr_nnz
         self.split = bool(split)
         if self.split and dtype != torch.float64:
             raise ValueError("a split operator acts on FP64 vectors")
@@ -316,8 +317,23 @@ class SellOperator:
         perm = C.c_void_p()
         _capi.check(_capi.lib().dfx_operator_info(self.handle, C.byref(ns), C.byref(nsl),
                                                    C.byref(perm)))
-        pad = ns.value / self.A.nnz - 1 if self.A.nnz else 0.0
+        pad = ns.value / self.csr_nnz - 1 if self.csr_nnz else 0.0
         return {"slots": ns.value, "slices": nsl.value, "padding": pad}
+
+    def release_values(self) -> None:
+        """Free the values and scratch of a structure-owning operator that is
+        only shared from: its shares keep their own values, and applying or
+        solving with this operator raises afterwards. The operator lets go
+        of its matrix too."""
+        _capi.check(_capi.lib().dfx_operator_release_values(self.handle))
+        self.A = None
+
+    def device_bytes(self) -> int:
+        """Device memory the operator holds (values and scratch; the
+        structure arrays too unless it is a share)."""
+        b = C.c_size_t(0)
+        _capi.check(_capi.lib().dfx_operator_device_bytes(self.handle, C.byref(b)))
+        return int(b.value)
 
     def __del__(self):
         h = getattr(self, "handle", None)

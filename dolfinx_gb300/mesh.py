@@ -2,7 +2,8 @@
 for tetrahedral boxes (cpp/dolfinx/mesh/generation.h:104-134, 380-426).
 
 The cells are RCM-reordered and the geometry nodes numbered exactly as
-DOLFINx does on one rank; the work runs in the host part of libdfxgpu.
+DOLFINx does on one rank. The work runs in the host part of libdfxgpu, or
+with ``device="cuda"`` on the GPU (the same mesh bit for bit).
 """
 
 from __future__ import annotations
@@ -63,10 +64,13 @@ class Mesh:
             self._dev["interior_facets"] = out[: nf.value].copy()
         return self._dev["interior_facets"]
 
-    def dual_graph(self) -> tuple[np.ndarray, np.ndarray]:
+    def dual_graph(self, device=None):
         """(offsets, adjacency) int32 of the facet-connected dual graph
         (mesh::build_local_dual_graph, cpp/dolfinx/mesh/graphbuild.cpp:566-905):
-        the cells that share a facet with each cell."""
+        the cells that share a facet with each cell. With a CUDA `device`
+        the graph is built there and returned as device tensors."""
+        if device is not None and _is_cuda(device):
+            return dual_graph_device(self.device(device)[0], self.num_nodes)
         nc = self.num_cells
         off = np.empty(nc + 1, np.int32)
         adj = np.empty(max(4 * nc, 1), np.int32)
@@ -86,7 +90,41 @@ class Mesh:
         return self._dev[key]
 
 
-def create_box(points, n, cell_type=CellType.tetrahedron, reorder: bool = True) -> Mesh:
+def _is_cuda(device) -> bool:
+    import torch
+
+    return torch.device(device).type == "cuda"
+
+
+def _work(nbytes: int, device):
+    import torch
+
+    return torch.empty(max(int(nbytes), 1), dtype=torch.uint8, device=device)
+
+
+def dual_graph_device(cells, num_vertices: int):
+    """Device (offsets, adjacency) int32 tensors of the facet dual graph of
+    device cells (num_cells, 4); see Mesh.dual_graph."""
+    import torch
+
+    from .la import _ptr, _stream
+
+    nc = int(cells.shape[0])
+    cells = cells.contiguous()
+    off = torch.empty(nc + 1, dtype=torch.int32, device=cells.device)
+    adj = torch.empty(max(4 * nc, 1), dtype=torch.int32, device=cells.device)
+    L = _capi.lib()
+    wb = int(L.dfx_mesh_dual_graph_tet_device_workspace_bytes(nc, int(num_vertices)))
+    work = _work(wb, cells.device)
+    _capi.check(L.dfx_mesh_dual_graph_tet_device(nc, _ptr(cells), int(num_vertices), _ptr(off),
+                                                 _ptr(adj), _ptr(work), wb, _stream()))
+    return off, adj[: int(off[-1])]
+
+
+def create_box(points, n, cell_type=CellType.tetrahedron, reorder: bool = True,
+               device=None) -> Mesh:
+    """device: None or a CPU device builds on host threads; a CUDA device
+    builds the same mesh on the GPU (and keeps its device copy)."""
     if cell_type != CellType.tetrahedron:
         raise ValueError("only tetrahedral boxes are on the GPU hot path")
     nx, ny, nz = (int(v) for v in n)
@@ -94,6 +132,8 @@ def create_box(points, n, cell_type=CellType.tetrahedron, reorder: bool = True) 
     p1 = np.ascontiguousarray(points[1], np.float64)
     nc = 6 * nx * ny * nz
     nv = (nx + 1) * (ny + 1) * (nz + 1)
+    if device is not None and _is_cuda(device):
+        return _create_box_device(nx, ny, nz, p0, p1, reorder, device)
     cells = np.empty((nc, 4), np.int32)
     x = np.empty((nv, 3), np.float64)
     _capi.check(_capi.lib().dfx_mesh_create_box_tet(nx, ny, nz, p0.ctypes.data, p1.ctypes.data,
@@ -101,5 +141,32 @@ def create_box(points, n, cell_type=CellType.tetrahedron, reorder: bool = True) 
     return Mesh(cells, x)
 
 
-def create_unit_cube(nx, ny, nz, cell_type=CellType.tetrahedron, reorder: bool = True) -> Mesh:
-    return create_box(((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)), (nx, ny, nz), cell_type, reorder)
+def _create_box_device(nx, ny, nz, p0, p1, reorder, device) -> Mesh:
+    import torch
+
+    from .la import _ptr, _stream
+
+    if min(nx, ny, nz) < 1:
+        raise _capi.DfxError(_capi.DFX_ERR_INVALID, "At least one cell is required.")
+    L = _capi.lib()
+    wb = int(L.dfx_mesh_create_box_tet_device_workspace_bytes(nx, ny, nz, int(reorder)))
+    if wb == 0:
+        raise _capi.DfxError(_capi.DFX_ERR_INVALID, "mesh too large for int32 cell indices")
+    nc = 6 * nx * ny * nz
+    nv = (nx + 1) * (ny + 1) * (nz + 1)
+    cells = torch.empty((nc, 4), dtype=torch.int32, device=device)
+    x = torch.empty((nv, 3), dtype=torch.float64, device=device)
+    work = _work(wb, device)
+    _capi.check(L.dfx_mesh_create_box_tet_device(nx, ny, nz, p0.ctypes.data, p1.ctypes.data,
+                                                 int(reorder), _ptr(cells), _ptr(x), _ptr(work),
+                                                 wb, _stream()))
+    del work
+    m = Mesh(cells.cpu().numpy(), x.cpu().numpy())
+    m._dev[str(device)] = (cells, x)
+    return m
+
+
+def create_unit_cube(nx, ny, nz, cell_type=CellType.tetrahedron, reorder: bool = True,
+                     device=None) -> Mesh:
+    return create_box(((0.0, 0.0, 0.0), (1.0, 1.0, 1.0)), (nx, ny, nz), cell_type, reorder,
+                      device)

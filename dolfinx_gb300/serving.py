@@ -34,6 +34,7 @@ from __future__ import annotations
 
 import collections
 import ctypes as C
+import gc
 import math
 import queue
 import threading
@@ -142,6 +143,38 @@ def unit_cube_boundary_nodes(X: np.ndarray) -> np.ndarray:
     return np.flatnonzero(near0 | near1).astype(np.int32)
 
 
+def device_bytes(*roots) -> int:
+    """Device memory held by the CUDA tensors and sliced-ELL operators
+    reachable from `roots` through this package's objects, dicts, lists and
+    tuples; each tensor storage and each operator is counted once."""
+    seen: set[int] = set()
+    storages: dict[int, int] = {}
+    ops: dict[int, int] = {}
+    stack = list(roots)
+    while stack:
+        o = stack.pop()
+        if id(o) in seen or o is None:
+            continue
+        seen.add(id(o))
+        if isinstance(o, torch.Tensor):
+            if o.is_cuda:
+                st = o.untyped_storage()
+                storages[st.data_ptr()] = st.nbytes()
+            continue
+        if isinstance(o, dict):
+            stack.extend(o.values())
+            continue
+        if isinstance(o, (list, tuple)):
+            stack.extend(o)
+            continue
+        if not type(o).__module__.startswith(__package__ or "dolfinx_gb300"):
+            continue
+        if isinstance(o, la.SellOperator) and getattr(o, "handle", None) is not None:
+            ops[o.handle.value] = o.device_bytes()
+        stack.extend(getattr(o, "__dict__", {}).values())
+    return sum(storages.values()) + sum(ops.values())
+
+
 class Structure:
     """Everything of one (n, degree) that requests share."""
 
@@ -151,14 +184,14 @@ class Structure:
         a choice already recorded for the workload (an earlier structure of
         this size, or a loaded tuning cache file) is used without timing."""
         self.n, self.degree = n, degree
-        self.mesh = mesh.create_unit_cube(n, n, n)
+        self.mesh = mesh.create_unit_cube(n, n, n, device=device)
         self.V = fem.functionspace(self.mesh, ("Lagrange", degree), device=device)
         bnd = unit_cube_boundary_nodes(self.V.tabulate_dof_coordinates())
         self.bc = fem.dirichletbc(0.0, bnd, self.V)
         a = fem.poisson_form(self.V, 1.0, k2=1.0)
         self.asm = fem.MatrixAssembler(a, [self.bc])  # slot map, markers, structure
         self.A0 = self.asm.A
-        self.A0.vals.fill_(1.0)  # any values: the operators copy only the structure here
+        self.A0.vals.fill_(1.0)  # any values: tuning times the kernels on them
         sigma = 256
         self.tuning = {}
         if tune:
@@ -169,10 +202,18 @@ class Structure:
         self.op32 = la.SellOperator(self.A0, torch.float32, sigma, compress_cols=True)
         self.ndofs = self.V.num_dofs
         self.nnz = self.A0.nnz
+        # Every request holds its own matrix and operator values: the
+        # structure keeps the pattern only (CSR row pointers and columns, the
+        # operators' structure arrays), about half of what it would hold with
+        # values.
+        self.op64.release_values()
+        self.op32.release_values()
+        self.row_ptr, self.cols = self.A0.row_ptr, self.A0.cols
+        self.asm.A = None
+        self.A0 = None
         self.mesh.device(device)
-        self.bytes = (self.A0.row_ptr.numel() * 8 + self.A0.cols.numel() * 4 + self.nnz * 8
-                      + self.asm.map.numel() + 3 * self.ops_slots() * 4 + self.ops_slots() * 6
-                      + self.V.dofmap.nbytes + self.mesh.cells.nbytes + self.mesh.x.nbytes)
+        # Everything above that lives on the device: tensors and operators.
+        self.bytes = device_bytes(self)
         self.users = 0
 
     def ops_slots(self):
@@ -226,8 +267,9 @@ class Job:
             self.kappa, self.f = request_inputs(st.mesh, req.seed)
             a = fem.poisson_form(V, self.kappa, k2=req.k2)
             L = fem.source_form(V, self.f)
-            self.A = la.MatrixCSR(st.A0.row_ptr, st.A0.cols,
-                                  torch.zeros_like(st.A0.vals), 1)
+            self.A = la.MatrixCSR(st.row_ptr, st.cols,
+                                  torch.zeros(st.nnz, dtype=torch.float64,
+                                              device=st.cols.device), 1)
             asm = st.asm
             amode = fem._mode(assembly)
             order, off, ncol = fem._colour_args(V, amode)
@@ -255,7 +297,7 @@ class Job:
         """Drop the request's device buffers (matrix values, operator values,
         vectors, coefficients) once its solution is on the host: a finished
         request keeps only x, its status and its timings."""
-        for name in ("A", "op64", "op32", "b", "dinv", "bp", "dp", "xp", "kappa", "f"):
+        for name in ("A", "op64", "op32", "b", "dinv", "bp", "dp", "xp", "kappa", "f", "work"):
             setattr(self, name, None)
 
 
@@ -322,8 +364,10 @@ class Server:
                 del self.structures[key]
                 drop_structure(*key)
                 del st
-                # The structure's tensors go back to torch's cache; return them
-                # to the device so the library's own allocations can use them.
+                # Collect cycles so the structure's operators and tensors are
+                # freed now, and return torch's cached blocks to the device so
+                # the library's own allocations can use them.
+                gc.collect()
                 torch.cuda.empty_cache()
                 _log.logger.info("structure n=%s P%s evicted", key[0], key[1])
 
@@ -529,6 +573,14 @@ class Server:
             w.join(timeout=30)
         _capi.lib().dfx_batch_destroy(self.batch)
         self.batch = None
+        # Drop this server's hold on its structures and finished requests,
+        # so that a cache clear returns their memory.
+        self.structures.clear()
+        self.active.clear()
+        self.finished = []
+        self.used = 0
+        gc.collect()
+        torch.cuda.empty_cache()
 
 
 def serve(requests, mode="mixed", max_wall_s: float = 600.0, **kw) -> tuple[dict, list[Job]]:

@@ -141,6 +141,40 @@ int dfx_mesh_dual_graph_tet(int32_t num_cells, const int32_t* cells, int32_t num
 int dfx_graph_reorder_rcm(int32_t n, const int32_t* offsets, const int32_t* adj,
                           int32_t* perm);
 
+/* The same three set-up steps on the device, bit-identical to the host
+ * functions above (the same definitions, see mesh_device.cu):
+ *
+ * dfx_mesh_create_box_tet_device: d_cells (num_cells x 4 int32, 16-byte
+ * aligned) and d_x (num_vertices x 3 doubles) in device memory, the mesh
+ * of dfx_mesh_create_box_tet. Coordinates are p0 + i * (p1 - p0) / n
+ * without a fused multiply-add, as the reference's expression compiles on
+ * x86-64 (mesh/generation.h:332-377).
+ *
+ * dfx_mesh_dual_graph_tet_device: device offsets (num_cells + 1) and
+ * adjacency (capacity 4 num_cells) of dfx_mesh_dual_graph_tet. Returns
+ * DFX_ERR_UNSUPPORTED when a facet is shared by more than two cells (the
+ * host function applies).
+ *
+ * dfx_graph_reorder_rcm_device: device offsets/adjacency in, device perm
+ * (perm[old] = new) out, as dfx_graph_reorder_rcm. Returns
+ * DFX_ERR_UNSUPPORTED for a node of degree above 16 (the degree sort then
+ * follows libstdc++'s introsort, which the device does not restate).
+ *
+ * Each takes a device workspace of its *_workspace_bytes (256-byte
+ * aligned), runs on `stream` and synchronises it before returning. */
+size_t dfx_mesh_create_box_tet_device_workspace_bytes(int32_t nx, int32_t ny, int32_t nz,
+                                                      int32_t reorder);
+int dfx_mesh_create_box_tet_device(int32_t nx, int32_t ny, int32_t nz, const double* p0,
+                                   const double* p1, int32_t reorder, int32_t* d_cells,
+                                   double* d_x, void* d_work, size_t work_bytes, void* stream);
+size_t dfx_mesh_dual_graph_tet_device_workspace_bytes(int32_t num_cells, int32_t num_vertices);
+int dfx_mesh_dual_graph_tet_device(int32_t num_cells, const int32_t* d_cells,
+                                   int32_t num_vertices, int32_t* d_offsets, int32_t* d_adj,
+                                   void* d_work, size_t work_bytes, void* stream);
+size_t dfx_graph_reorder_rcm_device_workspace_bytes(int32_t n);
+int dfx_graph_reorder_rcm_device(int32_t n, const int32_t* d_offsets, const int32_t* d_adj,
+                                 int32_t* d_perm, void* d_work, size_t work_bytes, void* stream);
+
 /* fem::create_dofmap for Lagrange P1/P2 on tetrahedra
  * (fem/utils.cpp:32-76, fem/dofmapbuilder.cpp:153-710). dofmap:
  * (num_cells, 4 or 10). Returns the number of dof nodes in *num_nodes. */
@@ -516,6 +550,16 @@ int dfx_operator_apply_renumbered(dfx_operator op, const void* d_x, void* d_y, v
 int dfx_operator_info(dfx_operator op, int64_t* nslots, int32_t* nslices,
                       const int32_t** d_perm);
 int dfx_operator_destroy(dfx_operator op);
+/* Free the values and scratch of an operator that owns its structure and
+ * serves only as the source of shares (dfx_operator_share), e.g. a cached
+ * structure whose requests each hold their own values. Afterwards the
+ * operator can be shared, permuted, queried and destroyed; applying it,
+ * refilling it or solving with it returns DFX_ERR_INVALID. */
+int dfx_operator_release_values(dfx_operator op);
+/* Device bytes the operator holds: its values and scratch, and for an
+ * operator that owns its structure (not a share) the structure arrays. For
+ * HBM accounting (no reference counterpart). */
+int dfx_operator_device_bytes(dfx_operator op, size_t* bytes);
 /* Launch shape of an FP32 operator's SpMV (no reference counterpart; an
  * autotuner knob): value pairs per load chunk of a lane, 2, 4 (default) or
  * 8. Results are bitwise the same for every choice. */

@@ -205,6 +205,49 @@ def test_device_sparsity_workspace_is_sized_by_the_problem(capi):
     assert L.dfx_sparsity_device_workspace_bytes(-1, 0, 4) == 0
 
 
+def test_device_mesh_workspaces_are_sized_by_the_problem(capi):
+    """Workspace sizes of the device box mesh, dual graph and RCM (host
+    functions): growing with the problem, 0 for invalid sizes and for boxes
+    whose cell indices overflow int32."""
+    L = capi.lib()
+    box = L.dfx_mesh_create_box_tet_device_workspace_bytes
+    assert 0 < box(2, 2, 2, 1) < box(64, 64, 64, 1)
+    assert box(64, 64, 64, 0) < box(64, 64, 64, 1)  # no dual graph, no ordering
+    nc = 6 * 64 ** 3
+    assert box(64, 64, 64, 1) >= 4 * nc * 4 * 2  # the box's cells and the reordered cells
+    assert box(0, 1, 1, 1) == 0 and box(448, 448, 448, 1) == 0
+    dual = L.dfx_mesh_dual_graph_tet_device_workspace_bytes
+    assert 0 < dual(10, 20) < dual(10000, 3000)
+    assert dual(10000, 3000) >= 2 * 4 * 10000 * 4  # facet lists and twins
+    assert dual(-1, 0) == 0
+    rcm = L.dfx_graph_reorder_rcm_device_workspace_bytes
+    assert 0 < rcm(0) < rcm(1000) < rcm(10 ** 6)
+    assert rcm(-1) == 0
+
+
+def test_device_mesh_entries_check_arguments_on_the_host(capi):
+    """Arguments are checked before any device work, so these calls need no
+    GPU: an empty box, inverted corners, a NULL output, a short workspace."""
+    import ctypes as C
+
+    L = capi.lib()
+    p0 = np.zeros(3)
+    p1 = np.ones(3)
+    buf = C.c_void_p(256)  # never dereferenced: each call fails its checks first
+    assert L.dfx_mesh_create_box_tet_device(0, 1, 1, p0.ctypes.data, p1.ctypes.data, 1, buf, buf,
+                                            buf, 1 << 30, None) == capi.DFX_ERR_INVALID
+    assert L.dfx_mesh_create_box_tet_device(1, 1, 1, p1.ctypes.data, p0.ctypes.data, 1, buf, buf,
+                                            buf, 1 << 30, None) == capi.DFX_ERR_INVALID
+    assert L.dfx_mesh_create_box_tet_device(1, 1, 1, p0.ctypes.data, p1.ctypes.data, 1, None, buf,
+                                            buf, 1 << 30, None) == capi.DFX_ERR_INVALID
+    assert L.dfx_mesh_create_box_tet_device(4, 4, 4, p0.ctypes.data, p1.ctypes.data, 1, buf, buf,
+                                            buf, 16, None) == capi.DFX_ERR_INVALID
+    assert L.dfx_graph_reorder_rcm_device(10, buf, buf, buf, buf, 16, None) == \
+        capi.DFX_ERR_INVALID
+    assert L.dfx_mesh_dual_graph_tet_device(10, buf, 40, buf, buf, buf, 16, None) == \
+        capi.DFX_ERR_INVALID
+
+
 _THREADS_SCRIPT = r"""
 import sys
 import numpy as np
