@@ -34,12 +34,16 @@ sys.path.insert(0, ROOT)
 METRIC = "GDoF/s assembly+CG (P2 Poisson, Jacobi-PCG to 1e-10 relative error)"
 UNIT = "GDoF/s"
 # Relative residual at which a step's solve stops, in both the plain FP64
-# and the mixed-precision path (and the CPU baseline). At rtol 1e-10 the
-# solutions of this system are only within ~2.5e-10 of the converged
-# solution; 2.5e-11 brings both below 1e-10 relative error, the accuracy the
-# speed-up is stated at. Both errors are measured every run against an
-# FP64 solve to rtol 1e-13 and printed in the config block.
-STEP_RTOL = 2.5e-11
+# and the mixed-precision path (and the CPU baseline). The bound the
+# speed-up is stated at: the mixed solution within 1e-10 (relative) of the
+# plain FP64 solution. Measured over 12 last-bit perturbations of the 64^3
+# matrix (bench.py --accuracy-trials 12): at rtol 2.5e-11 the two solutions
+# differ by 1.05-1.15e-10 (none within the bound; another set of trials had
+# one at 3.1e-10, whose FP32 inner solve stopped ~75 iterations early); at
+# 1e-11 by 3.5-4.3e-11; at 5e-12 by 1.9-2.1e-11, a margin of four against
+# such early stops. Both solutions and their distance are measured every run
+# (and against an FP64 solve to rtol 1e-13) and printed in the config block.
+STEP_RTOL = 5e-12
 ERR_BOUND = 1e-10
 
 
@@ -80,6 +84,9 @@ def parse():
                    help="run one mixed-precision P2 Poisson step only (for an ncu launch list)")
     p.add_argument("--profile", action="store_true",
                    help="profiling target: a few launches of every hot kernel, no timing")
+    p.add_argument("--accuracy-trials", type=int, default=0, metavar="N",
+                   help="N last-bit perturbations of the P2 Poisson matrix: iterations and "
+                        "errors of both paths at several stopping tolerances")
     return p.parse_args()
 
 
@@ -632,8 +639,12 @@ def serving_sample(args):
     capacity), each in FP64 and mixed precision. The structures of every
     (n, degree) are built once, before the first timed run, and shared by
     the four runs; the budget keeps all of them resident (no rebuild inside
-    a timed run)."""
+    a timed run). Requests stop at the step's relative residual (STEP_RTOL,
+    below the config's 1e-10), and each mixed solution is compared with the
+    FP64 solution of the same request: the bound is 1e-10 relative."""
     import time
+
+    import numpy as np
 
     from dolfinx_gb300 import serving
 
@@ -651,13 +662,25 @@ def serving_sample(args):
         reqs = serving.make_requests(args.serving_requests, rate, seed=1,
                                      n_range=(8, args.serving_nmax))
         res = {}
+        sols = {}
         for mode in ("fp64", "mixed"):
-            stats, _ = serving.serve(reqs, mode=mode, hbm_budget=budget, max_wall_s=120.0)
+            stats, jobs = serving.serve(reqs, mode=mode, hbm_budget=budget, max_wall_s=120.0,
+                                        rtol=STEP_RTOL)
             res[mode] = {k: stats[k] for k in ("solves_per_s", "p50_ms", "p99_ms", "dofs_per_s",
                                                "wall_s", "failed")}
+            sols[mode] = {j.req.rid: j.x for j in jobs if getattr(j, "x", None) is not None}
+            del jobs
         res["rate"] = rate
         res["mixed_over_fp64_solves"] = res["mixed"]["solves_per_s"] / res["fp64"]["solves_per_s"]
+        diffs = [float((sols["mixed"][r] - x).norm() / x.norm())
+                 for r, x in sols["fp64"].items() if r in sols["mixed"] and float(x.norm()) > 0]
+        res["mixed_vs_fp64_rel_err"] = {"requests": len(diffs),
+                                        "max": max(diffs) if diffs else None,
+                                        "median": float(np.median(diffs)) if diffs else None,
+                                        "within_bound": bool(diffs) and max(diffs) <= ERR_BOUND}
+        del sols
         out["runs"].append(res)
+    out["rtol"] = STEP_RTOL
     return out
 
 
@@ -691,13 +714,14 @@ def serving_sweep(args):
              for rate in SERVING_RATES for r in range(reps)}
     everything = [q for reqs in draws.values() for q in reqs]
     out = {"requests_per_run": nreq, "repeats": reps, "n_range": [8, args.serving_nmax],
+           "rtol": STEP_RTOL,
            "hbm_budget_bytes": budget, "distinct_structures": len({(q.n, q.degree)
                                                                    for q in everything}),
            "structure_setup_s": {}, "rates": [{"rate": rate} for rate in SERVING_RATES]}
     for mode in ("fp64", "mixed"):
         serving.clear_structure_cache()
         torch.cuda.empty_cache()
-        srv = serving.Server(mode=mode, hbm_budget=budget)
+        srv = serving.Server(mode=mode, hbm_budget=budget, rtol=STEP_RTOL)
         try:
             t0 = time.perf_counter()
             srv.prewarm(everything)
@@ -947,7 +971,9 @@ def run_ours(args):
         config["rel_err_vs_converged_fp64"] = {"mixed": err_mixed_tight,
                                                "fp64_plain": err_fp64_tight,
                                                "mixed_vs_fp64_plain": rel_err,
-                                               "within_bound": bool(err_mixed_tight <= ERR_BOUND
+                                               "within_bound": bool(rel_err <= ERR_BOUND
+                                                                    and err_mixed_tight
+                                                                    <= ERR_BOUND
                                                                     and err_fp64_tight
                                                                     <= ERR_BOUND)}
         config["fp64_plain_ms_per_step"] = ms64
@@ -1118,8 +1144,71 @@ def run_profile_split(args):
                       "slots": osp.info()["slots"]}))
 
 
+def accuracy_trials(args):
+    """Robustness of the accuracy bound. The FP32 inner iterations of the
+    mixed solve react chaotically to last-bit changes of the matrix (the FP64
+    atomic assembly gives such changes from run to run), so one run does not
+    show where a stopping tolerance leaves the error. Each trial multiplies
+    kappa by 1 + 1e-15 N(0, 1) per cell (seeded), re-assembles, and solves with
+    both paths at each tolerance; errors are against an FP64 solve of the
+    unperturbed system to rtol 1e-13 (the perturbation moves the solution by
+    ~1e-15). Prints min / median / max per tolerance."""
+    import numpy as np
+    import torch
+
+    from dolfinx_gb300 import la
+
+    torch.cuda.set_device(0)
+    m, kappa, f = make_inputs(args.n)
+    P = Problem(m, kappa, f, mode=args.mode)
+    P.assemble()
+    ref = la.OperatorCGSolver(P.A, jacobi=True, sigma=P.tuning["sigma"]["sigma"])
+    ref.refresh()
+    xc = torch.zeros_like(P.b)
+    ref.solve(P.b, xc, rtol=1e-13)
+    nrm = float(torch.linalg.norm(xc))
+    kap0 = P.kappa.clone()
+    rng = np.random.default_rng(7)
+    rtols = (2.5e-11, 1e-11, STEP_RTOL)
+    rows = {r: [] for r in rtols}
+    for _ in range(args.accuracy_trials):
+        pert = torch.from_numpy(1.0 + 1e-15 * rng.standard_normal(kap0.numel())).cuda()
+        P.kappa.copy_(kap0 * pert)
+        for rtol in rtols:
+            P.assemble()
+            P.ir.refresh()
+            P.fp64.refresh()
+            xm = torch.zeros_like(P.b)
+            rm = P.ir.solve(P.b, xm, rtol=rtol)
+            xf = torch.zeros_like(P.b)
+            rf = P.fp64.solve(P.b, xf, rtol=rtol)
+            rows[rtol].append((rm.inner_iterations, rf.iterations,
+                               float(torch.linalg.norm(xm - xc)) / nrm,
+                               float(torch.linalg.norm(xf - xc)) / nrm,
+                               float(torch.linalg.norm(xm - xf) / torch.linalg.norm(xf))))
+    P.kappa.copy_(kap0)
+
+    def stats(v):
+        return {"min": min(v), "median": float(np.median(v)), "max": max(v)}
+
+    out = {}
+    for rtol, rs in rows.items():
+        cols = list(zip(*rs))
+        out[f"{rtol:g}"] = {"mixed_inner_iterations": stats(cols[0]),
+                            "fp64_iterations": stats(cols[1]),
+                            "err_mixed_vs_converged": stats(cols[2]),
+                            "err_fp64_vs_converged": stats(cols[3]),
+                            "mixed_vs_fp64_plain": stats(cols[4]),
+                            "trials_within_bound": int(sum(e <= ERR_BOUND for e in cols[4]))}
+    print(json.dumps({"accuracy_trials": {"trials": args.accuracy_trials, "workload":
+                                          workload_config(args)["workload"], "by_rtol": out}}))
+
+
 def main():
     args = parse()
+    if args.accuracy_trials:
+        accuracy_trials(args)
+        return
     if args.profile_split:
         run_profile_split(args)
         return

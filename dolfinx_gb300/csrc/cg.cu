@@ -8,7 +8,13 @@
 //   3. p = z + b p
 // Reductions are two-stage and deterministic: per-block partial sums in
 // FP64, then the last block to finish (atomic ticket) sums the partials in
-// index order and updates the scalar state in device memory. Scalars never
+// index order and updates the scalar state in device memory. The FP32
+// sliced-ELL SpMV is the exception: its blocks are short (one slice per
+// warp), and the ticket at the end of each one held the block's slot for
+// the length of a device-wide atomic (86 us against 74 us without it at P2
+// 64^3); its warps store their p.y partials in fixed slots and a small
+// fourth kernel reduces them the same deterministic way. The FP64 SpMV,
+// twice as long, keeps the fused ticket: a fourth launch cost it more. Scalars never
 // leave the device; every kernel returns at once when the state says done,
 // so a CUDA graph of K iterations is replayed until the host reads done.
 //
@@ -135,9 +141,12 @@ struct Work
   T* p;
   T* y;
   int blocks;
-  // FP64 solves on a split operator (DFX_F32X2): p's FP32 words, hi (n)
-  // then lo (n), written wherever p is, read by the SpMV.
+  // FP64 solves on a split operator (DFX_F32X2): p's FP32 words, (hi, lo)
+  // side by side per row, written wherever p is, read by the SpMV.
   float* ph = nullptr;
+  // Per-warp p.y partials of the sliced-ELL SpMV (one slot per warp of its
+  // grid), summed by k_pap_reduce.
+  double* wpart = nullptr;
 };
 
 // p[i] and, when the solve keeps them, its FP32 words.
@@ -147,7 +156,11 @@ __device__ __forceinline__ void store_p(const Work<T>& w, int64_t n, int64_t i, 
   w.p[i] = v;
   if constexpr (sizeof(T) == 8)
     if (w.ph)
-      dfx::split_f64(v, w.ph[i], w.ph[n + i]);
+    {
+      float2 hl;
+      dfx::split_f64(v, hl.x, hl.y);
+      reinterpret_cast<float2*>(w.ph)[i] = hl;
+    }
 }
 
 template <typename T>
@@ -160,6 +173,7 @@ Work<T> carve_work(Carver& c, int64_t n)
   w.r = c.take<T>(n);
   w.p = c.take<T>(n);
   w.y = c.take<T>(n);
+  w.wpart = c.take<double>((size_t)sell_blocks(n) * (kSellThreads / 32));
   return w;
 }
 
@@ -448,16 +462,33 @@ __global__ void __launch_bounds__(kThreads)
   finish_pap(publish<double>(dot, 0.0, w.red, &w.st->ticket[1], false), w.st);
 }
 
+// The warp's p.y partial into its fixed slot (FP32 kernels: the lanes'
+// FP32 partials summed in FP32, as one FP64 value).
+template <typename T>
+__device__ __forceinline__ void store_warp_partial(T dot, const Work<T>& w)
+{
+  const T sum = dfx::warp_sum(dot);
+  if ((threadIdx.x & 31) == 0)
+    w.wpart[(blockIdx.x * blockDim.x + threadIdx.x) >> 5] = (double)sum;
+}
+
 // y = A p, p.y -- sliced-ELL operator, one row per lane, warp per slice.
-// 12 resident blocks per SM (48 warps) for chunks of up to 4 loads: the SpMV
-// is bound by the latency of its loads, and with more registers per thread (48
-// when left to ptxas) only 10 blocks fit and the FP32 inner iteration ran
-// ~9 us slower at P2 64^3. Chunks of 8 keep 8 blocks so that they do not spill.
+// The SpMV is bound by the latency of its loads, so its register budget
+// (resident warps) is set by measurement at P2 64^3: the FP64 kernel at 12
+// blocks per SM (40 registers; 64 when left to ptxas, 295 -> 246 ms per
+// plain FP64 step), the FP32 kernel at 10 (48 registers: 150.0 -> 147.1 ms
+// per mixed step against 12 blocks). Chunks of 8 keep 8 blocks so that they
+// do not spill.
+template <typename T, int CH>
+constexpr int kSellMinBlocks = CH >= 8 ? 8 : (sizeof(T) == 4 ? 10 : 12);
+
 template <typename V, typename T, bool COMP, int CH = 4>
-__global__ void __launch_bounds__(kSellThreads, CH >= 8 ? 8 : 12)
+__global__ void __launch_bounds__(kSellThreads, kSellMinBlocks<T, CH>)
     k_spmv_dot_sell(const dfx_operator_s op, Work<T> w)
 {
-  block_reduce_init();
+  constexpr bool kSplitReduce = sizeof(T) == 4; // p.y summed by k_pap_reduce
+  if constexpr (!kSplitReduce)
+    block_reduce_init();
 
   if (is_done(w.st))
     return;
@@ -474,13 +505,46 @@ __global__ void __launch_bounds__(kSellThreads, CH >= 8 ? 8 : 12)
       dot += acc * w.p[row];
     }
   }
-  finish_pap(publish<T>(dot, T(0), w.red, &w.st->ticket[1], false), w.st);
+  if constexpr (kSplitReduce)
+    store_warp_partial<T>(dot, w);
+  else
+    finish_pap(publish<T>(dot, T(0), w.red, &w.st->ticket[1], false), w.st);
+}
+
+// p.Ap from the sliced-ELL SpMV's per-warp partials: each thread adds a
+// fixed set of kPapPer slots, then publish()'s deterministic two-level
+// reduction; the last warp sets alpha (finish_pap).
+constexpr int kPapThreads = 256;
+constexpr int kPapPer = 4;
+int pap_blocks(int64_t n)
+{
+  const int64_t parts = (int64_t)sell_blocks(n) * (kSellThreads / 32);
+  return (int)std::max<int64_t>(1, (parts + kPapThreads * kPapPer - 1) / (kPapThreads * kPapPer));
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kPapThreads) k_pap_reduce(Work<T> w, int nparts)
+{
+  block_reduce_init();
+
+  if (is_done(w.st))
+    return;
+  double v = 0.0;
+  const int base = blockIdx.x * (kPapThreads * kPapPer) + threadIdx.x;
+#pragma unroll
+  for (int k = 0; k < kPapPer; ++k)
+  {
+    const int i = base + k * kPapThreads;
+    if (i < nparts)
+      v += __ldcg(w.wpart + i);
+  }
+  finish_pap(publish<double>(v, 0.0, w.red, &w.st->ticket[1], false), w.st);
 }
 
 // y = A p, p.y -- split operator (DFX_F32X2): FP32-pipe products of the
 // FP32 words of the values and of p, FP64 y and dot.
 template <bool COMP>
-__global__ void __launch_bounds__(kSellThreads)
+__global__ void __launch_bounds__(kSellThreads, 12)
     k_spmv_dot_sell_split(const dfx_operator_s op, Work<double> w)
 {
   block_reduce_init();
@@ -493,8 +557,8 @@ __global__ void __launch_bounds__(kSellThreads)
   double dot = 0;
   for (int32_t s = sr.begin; s < sr.end; s += sr.step)
   {
-    const double acc = dfx::sell_row_split<COMP>(op, vh, vh + op.nslots, w.ph, w.ph + op.n, s,
-                                                 lane);
+    const double acc = dfx::sell_row_split<COMP>(op, vh, vh + op.nslots,
+                                                 reinterpret_cast<const float2*>(w.ph), s, lane);
     const int32_t row = 32 * s + lane;
     if (row < op.n)
     {
@@ -696,12 +760,11 @@ __global__ void __launch_bounds__(kElemThreads)
       if constexpr (sizeof(T) == 8)
         if (w.ph)
         {
-          float2 h, l;
-          dfx::split_f64(pe[0], h.x, l.x);
-          dfx::split_f64(pe[1], h.y, l.y);
-          reinterpret_cast<float2*>(w.ph)[v] = h;
-          w.ph[n + 2 * v] = l.x; // n + 2 v may be odd: no 8-byte store
-          w.ph[n + 2 * v + 1] = l.y;
+          // rows 2v and 2v+1: (hi, lo, hi, lo) in one 16-byte store
+          float4 hl;
+          dfx::split_f64(pe[0], hl.x, hl.y);
+          dfx::split_f64(pe[1], hl.z, hl.w);
+          reinterpret_cast<float4*>(w.ph)[v] = hl;
         }
     }
     if (blockIdx.x == 0)
@@ -1108,7 +1171,7 @@ __global__ void k_split_words(const double* __restrict__ x, float* __restrict__ 
 {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n)
-    dfx::split_f64(x[i], out[i], out[n + i]);
+    dfx::split_f64(x[i], out[2 * i], out[2 * i + 1]);
 }
 
 __global__ void k_scatter(const double* __restrict__ in, double* __restrict__ out,
@@ -1139,6 +1202,18 @@ struct OpRef
 template <typename T>
 void enqueue_spmv_dot(const OpRef& o, const Work<T>& w, cudaStream_t s);
 
+template <typename T>
+void enqueue_pap_reduce(int64_t n, const Work<T>& w, cudaStream_t s)
+{
+  const int nparts = sell_blocks(n) * (kSellThreads / 32);
+  k_pap_reduce<T><<<pap_blocks(n), kPapThreads, 0, s>>>(w, nparts);
+}
+
+// Kernels of one PCG iteration: the FP32 sliced-ELL operator adds the p.Ap
+// reduction kernel to the three.
+constexpr int kFusedIterKernels = 3;
+constexpr int kF32SellIterKernels = 4;
+
 template <>
 void enqueue_spmv_dot<double>(const OpRef& o, const Work<double>& w, cudaStream_t s)
 {
@@ -1151,10 +1226,10 @@ void enqueue_spmv_dot<double>(const OpRef& o, const Work<double>& w, cudaStream_
         k_spmv_dot_sell_split<true><<<sell_blocks(o.op->n), kSellThreads, 0, s>>>(*o.op, w);
       else
         k_spmv_dot_sell_split<false><<<sell_blocks(o.op->n), kSellThreads, 0, s>>>(*o.op, w);
-      return;
     }
-    k_spmv_dot_sell<double, double, false><<<sell_blocks(o.op->n), kSellThreads, 0, s>>>(*o.op,
-                                                                                       w);
+    else
+      k_spmv_dot_sell<double, double, false><<<sell_blocks(o.op->n), kSellThreads, 0, s>>>(
+          *o.op, w);
     return;
   }
   const dfx_csr* A = o.A;
@@ -1210,6 +1285,7 @@ void enqueue_spmv_dot<float>(const OpRef& o, const Work<float>& w, cudaStream_t 
     else
       launch(F_{}, std::integral_constant<int, 4>{});
   }
+  enqueue_pap_reduce<float>(o.op->n, w, s);
 }
 
 bool aligned16(const void* p) { return ((uintptr_t)p & 15) == 0; }
@@ -1406,7 +1482,7 @@ int read_state(const CgState* d, CgState** h, cudaStream_t s)
 // iterations and the state is done at max_iter at the latest, so the loop
 // bound only guards against a corrupted state.
 int run_to_done(cudaGraphExec_t exec, const CgState* dst, int max_iters, int K, CgState** h,
-                cudaStream_t s, int64_t* kernels, int per_iter = 3)
+                cudaStream_t s, int64_t* kernels, int per_iter)
 {
   const int64_t max_launches = (int64_t)max_iters / K + 2;
   for (int64_t launch = 0;; ++launch)
@@ -1519,7 +1595,7 @@ extern "C" int dfx_cg_solve(const dfx_csr* A, const double* d_b, double* d_x,
     return st;
   CgState* h;
   int64_t kernels = 2;
-  if (int st = run_to_done(exec, w.st, max_iters, K, &h, s, &kernels))
+  if (int st = run_to_done(exec, w.st, max_iters, K, &h, s, &kernels, kFusedIterKernels))
     return st;
   return report(h, info, kernels);
 }
@@ -1576,7 +1652,7 @@ extern "C" int dfx_cg_solve_op(dfx_operator op, const double* d_b, double* d_x,
     return st;
   CgState* h;
   int64_t kernels = 5 + (dp ? 1 : 0) + (w.ph ? 1 : 0);
-  int st = run_to_done(exec, w.st, max_iters, K, &h, s, &kernels);
+  int st = run_to_done(exec, w.st, max_iters, K, &h, s, &kernels, kFusedIterKernels);
   CgState hs = *h;
   k_scatter<<<g, 256, 0, s>>>(xp, d_x, op->perm, (int32_t)n);
   DFX_CHECK_LAUNCH();
@@ -1684,7 +1760,7 @@ extern "C" int dfx_ir_solve(dfx_operator op64, dfx_operator op32, const double* 
         enqueue_init<float>(w.r, nullptr, d32, dinv32, n, w, inner_rtol, max_inner, s);
         DFX_CHECK_LAUNCH();
         kernels += 1;
-        if ((st = run_to_done(exec, w.st, max_inner, K, &h, s, &kernels)))
+        if ((st = run_to_done(exec, w.st, max_inner, K, &h, s, &kernels, kF32SellIterKernels)))
           break;
         inner_total += h->iter;
         if (!restart)
@@ -1736,7 +1812,7 @@ extern "C" int dfx_ir_solve(dfx_operator op64, dfx_operator op32, const double* 
         break;
       enqueue_init<float>(w.r, nullptr, d32, dinv32, n, w, inner_rtol, max_inner, s);
       DFX_CHECK_LAUNCH();
-      if ((st = run_to_done(exec, w.st, max_inner, K, &h, s, &kernels)))
+      if ((st = run_to_done(exec, w.st, max_inner, K, &h, s, &kernels, kF32SellIterKernels)))
         break;
       inner_total += h->iter;
       // A stalled or broken-down inner solve still yields a usable correction.
@@ -1782,7 +1858,7 @@ extern "C" int dfx_ir_solve(dfx_operator op64, dfx_operator op32, const double* 
         enqueue_pupdate<float>(dinv32, n, w, s);
         DFX_CHECK_LAUNCH();
         kernels += 1;
-        if ((st = run_to_done(exec, w.st, max_inner, K, &h, s, &kernels)))
+        if ((st = run_to_done(exec, w.st, max_inner, K, &h, s, &kernels, kF32SellIterKernels)))
           break;
         const int32_t why = h->status;
         k_ir_correct<<<blocks, kThreads, 0, s>>>(xp, d32, n);

@@ -59,16 +59,16 @@ __global__ void k_fill_split(const int32_t* __restrict__ map, const double* __re
   }
 }
 
-// (hi, lo) FP32 words of an FP64 vector: hi at i, lo at n + i.
+// (hi, lo) FP32 words of an FP64 vector, side by side: hi at 2i, lo at 2i+1.
 __global__ void k_split(const double* __restrict__ x, float* __restrict__ out, int32_t n)
 {
   const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n)
-    dfx::split_f64(x[i], out[i], out[n + i]);
+    dfx::split_f64(x[i], out[2 * (int64_t)i], out[2 * (int64_t)i + 1]);
 }
 
 template <bool COMP>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, 12)
     k_sell_spmv_split(const dfx_operator_s op, const float* __restrict__ x, double* __restrict__ y)
 {
   const int lane = threadIdx.x & 31;
@@ -76,7 +76,8 @@ __global__ void __launch_bounds__(128)
   const float* vh = (const float*)op.vals;
   for (int32_t s = sr.begin; s < sr.end; s += sr.step)
   {
-    const double acc = dfx::sell_row_split<COMP>(op, vh, vh + op.nslots, x, x + op.n, s, lane);
+    const double acc = dfx::sell_row_split<COMP>(op, vh, vh + op.nslots,
+                                                 reinterpret_cast<const float2*>(x), s, lane);
     const int32_t row = 32 * s + lane;
     if (row < op.n)
       y[row] = acc;

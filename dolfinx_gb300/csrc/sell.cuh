@@ -193,7 +193,8 @@ __device__ __forceinline__ ACC sell_row(const dfx_operator_s& op, const V* __res
 #ifdef __CUDACC__
 // Row sum of a split operator (DFX_F32X2): each FP64 value is carried as
 // two FP32 words, hi = fl32(v) and lo = fl32(v - hi), stored in two arrays
-// of the FP32 pair layout (vals and vals + nslots), and x likewise (xh, xl).
+// of the FP32 pair layout (vals and vals + nslots); x's words sit side by
+// side, (hi, lo) per row, so an entry gathers them in one 8-byte load.
 // Products and the running sum use the FP32 pipe with error-free
 // transformations: hi*hi exactly as a sum of two floats (fma), the cross
 // terms hi*lo + lo*hi into a low-order accumulator, and the high-order
@@ -205,8 +206,7 @@ template <bool COMP>
 __device__ __forceinline__ double sell_row_split(const dfx_operator_s& op,
                                                  const float* __restrict__ vh,
                                                  const float* __restrict__ vl,
-                                                 const float* __restrict__ xh,
-                                                 const float* __restrict__ xl, int32_t s,
+                                                 const float2* __restrict__ xw, int32_t s,
                                                  int lane)
 {
   const int64_t b = __ldg(op.slice_ptr + s);
@@ -254,20 +254,19 @@ __device__ __forceinline__ double sell_row_split(const dfx_operator_s& op,
         col += dd[u].y;
         c1[u] = col;
       }
-      float a0[kChunk], a1[kChunk], b0[kChunk], b1[kChunk];
+      // x's (hi, lo) words sit together: one 8-byte gather per entry.
+      float2 x0[kChunk], x1[kChunk];
 #pragma unroll
       for (int u = 0; u < kChunk; ++u)
       {
-        a0[u] = __ldg(xh + c0[u]);
-        b0[u] = __ldg(xl + c0[u]);
-        a1[u] = __ldg(xh + c1[u]);
-        b1[u] = __ldg(xl + c1[u]);
+        x0[u] = __ldg(xw + c0[u]);
+        x1[u] = __ldg(xw + c1[u]);
       }
 #pragma unroll
       for (int u = 0; u < kChunk; ++u)
       {
-        add(hv[u].x, lv[u].x, a0[u], b0[u]);
-        add(hv[u].y, lv[u].y, a1[u], b1[u]);
+        add(hv[u].x, lv[u].x, x0[u].x, x0[u].y);
+        add(hv[u].y, lv[u].y, x1[u].x, x1[u].y);
       }
     }
   }
@@ -278,8 +277,9 @@ __device__ __forceinline__ double sell_row_split(const dfx_operator_s& op,
     {
       const float2 hv = __ldcs(ph + 32 * j), lv = __ldcs(pl + 32 * j);
       const int2 cc = __ldcs(c + 32 * j);
-      add(hv.x, lv.x, __ldg(xh + cc.x), __ldg(xl + cc.x));
-      add(hv.y, lv.y, __ldg(xh + cc.y), __ldg(xl + cc.y));
+      const float2 x0 = __ldg(xw + cc.x), x1 = __ldg(xw + cc.y);
+      add(hv.x, lv.x, x0.x, x0.y);
+      add(hv.y, lv.y, x1.x, x1.y);
     }
   }
   return (double)S + (double)L;
@@ -319,7 +319,7 @@ int sell_grid(int32_t nslices);
 int max_grid_blocks();
 
 // Launch y = A x on renumbered vectors (both of length op.n). A split
-// operator (DFX_F32X2) takes x as its FP32 words, hi (n) then lo (n), and
+// operator (DFX_F32X2) takes x as its FP32 words, (hi, lo) per row, and
 // writes y in FP64.
 int sell_spmv(const dfx_operator_s& op, const void* x, void* y, cudaStream_t s);
 
