@@ -44,6 +44,10 @@ UNIT = "GDoF/s"
 # such early stops. Both solutions and their distance are measured every run
 # (and against an FP64 solve to rtol 1e-13) and printed in the config block.
 STEP_RTOL = 5e-12
+# Serving requests (Poisson/Helmholtz, P1/P2, n in [8, 96]) stop at 2e-12:
+# over the 64-request sample at 5e-12 one whole-GPU request (n = 95, P1)
+# ended 1.14e-10 from its FP64 solution; at 2e-12 the worst was 4.4e-11.
+SERVING_RTOL = 2e-12
 ERR_BOUND = 1e-10
 
 
@@ -639,9 +643,9 @@ def serving_sample(args):
     capacity), each in FP64 and mixed precision. The structures of every
     (n, degree) are built once, before the first timed run, and shared by
     the four runs; the budget keeps all of them resident (no rebuild inside
-    a timed run). Requests stop at the step's relative residual (STEP_RTOL,
-    below the config's 1e-10), and each mixed solution is compared with the
-    FP64 solution of the same request: the bound is 1e-10 relative."""
+    a timed run). Requests stop at relative residual SERVING_RTOL (below the
+    config's 1e-10), and each mixed solution is compared with the FP64
+    solution of the same request: the bound is 1e-10 relative."""
     import time
 
     import numpy as np
@@ -665,7 +669,7 @@ def serving_sample(args):
         sols = {}
         for mode in ("fp64", "mixed"):
             stats, jobs = serving.serve(reqs, mode=mode, hbm_budget=budget, max_wall_s=120.0,
-                                        rtol=STEP_RTOL)
+                                        rtol=SERVING_RTOL)
             res[mode] = {k: stats[k] for k in ("solves_per_s", "p50_ms", "p99_ms", "dofs_per_s",
                                                "wall_s", "failed")}
             sols[mode] = {j.req.rid: j.x for j in jobs if getattr(j, "x", None) is not None}
@@ -680,7 +684,7 @@ def serving_sample(args):
                                         "within_bound": bool(diffs) and max(diffs) <= ERR_BOUND}
         del sols
         out["runs"].append(res)
-    out["rtol"] = STEP_RTOL
+    out["rtol"] = SERVING_RTOL
     return out
 
 
@@ -714,14 +718,14 @@ def serving_sweep(args):
              for rate in SERVING_RATES for r in range(reps)}
     everything = [q for reqs in draws.values() for q in reqs]
     out = {"requests_per_run": nreq, "repeats": reps, "n_range": [8, args.serving_nmax],
-           "rtol": STEP_RTOL,
+           "rtol": SERVING_RTOL,
            "hbm_budget_bytes": budget, "distinct_structures": len({(q.n, q.degree)
                                                                    for q in everything}),
            "structure_setup_s": {}, "rates": [{"rate": rate} for rate in SERVING_RATES]}
     for mode in ("fp64", "mixed"):
         serving.clear_structure_cache()
         torch.cuda.empty_cache()
-        srv = serving.Server(mode=mode, hbm_budget=budget, rtol=STEP_RTOL)
+        srv = serving.Server(mode=mode, hbm_budget=budget, rtol=SERVING_RTOL)
         try:
             t0 = time.perf_counter()
             srv.prewarm(everything)

@@ -511,34 +511,70 @@ __global__ void __launch_bounds__(kSellThreads, kSellMinBlocks<T, CH>)
     finish_pap(publish<T>(dot, T(0), w.red, &w.st->ticket[1], false), w.st);
 }
 
-// p.Ap from the sliced-ELL SpMV's per-warp partials: each thread adds a
-// fixed set of kPapPer slots, then publish()'s deterministic two-level
-// reduction; the last warp sets alpha (finish_pap).
+// p.Ap from the sliced-ELL SpMV's per-warp partials, in one short latency
+// chain: each thread adds a fixed set of kPapPer slots (loads issued
+// together, added in slot order), warps and then the block reduce by
+// shuffles in a fixed pattern, and the last block to arrive (ticket) adds
+// the block partials in block order and sets alpha (finish_pap). At most
+// 32 blocks, so that one warp finishes.
 constexpr int kPapThreads = 256;
-constexpr int kPapPer = 4;
+constexpr int kPapPer = 16;
+constexpr int kPapMaxBlocks = 32;
 int pap_blocks(int64_t n)
 {
   const int64_t parts = (int64_t)sell_blocks(n) * (kSellThreads / 32);
-  return (int)std::max<int64_t>(1, (parts + kPapThreads * kPapPer - 1) / (kPapThreads * kPapPer));
+  const int64_t per_block = (int64_t)kPapThreads * kPapPer;
+  return (int)std::max<int64_t>(1, (parts + per_block - 1) / per_block);
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kPapThreads) k_pap_reduce(Work<T> w, int nparts)
+__global__ void __launch_bounds__(kPapThreads) k_pap_reduce(Work<T> w, int nparts, int per_thread)
 {
-  block_reduce_init();
-
+  __shared__ double wsum[kPapThreads / 32];
+  __shared__ int last;
   if (is_done(w.st))
     return;
-  double v = 0.0;
-  const int base = blockIdx.x * (kPapThreads * kPapPer) + threadIdx.x;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  // slots blockIdx.x * (per_thread * kPapThreads) + k * kPapThreads + threadIdx.x
+  const int64_t base = (int64_t)blockIdx.x * per_thread * kPapThreads + threadIdx.x;
+  double part[kPapPer];
 #pragma unroll
   for (int k = 0; k < kPapPer; ++k)
   {
-    const int i = base + k * kPapThreads;
+    const int64_t i = base + (int64_t)k * kPapThreads;
+    part[k] = (k < per_thread && i < nparts) ? __ldcg(w.wpart + i) : 0.0;
+  }
+  double v = 0.0;
+#pragma unroll
+  for (int k = 0; k < kPapPer; ++k)
+    v += part[k];
+  for (int k = kPapPer; k < per_thread; ++k)
+  {
+    const int64_t i = base + (int64_t)k * kPapThreads;
     if (i < nparts)
       v += __ldcg(w.wpart + i);
   }
-  finish_pap(publish<double>(v, 0.0, w.red, &w.st->ticket[1], false), w.st);
+  v = dfx::warp_sum(v);
+  if (lane == 0)
+    wsum[warp] = v;
+  __syncthreads();
+  if (warp != 0)
+    return;
+  v = lane < kPapThreads / 32 ? wsum[lane] : 0.0;
+  v = dfx::warp_sum(v);
+  if (lane == 0)
+  {
+    w.red.part0[blockIdx.x] = v;
+    __threadfence();
+    last = atomicAdd(&w.st->ticket[1], 1u) == gridDim.x - 1;
+  }
+  __syncwarp();
+  if (!last)
+    return;
+  __threadfence();
+  double s = lane < (int)gridDim.x ? __ldcg(w.red.part0 + lane) : 0.0;
+  s = dfx::warp_sum(s);
+  finish_pap(WarpFinal{true, s, 0.0}, w.st);
 }
 
 // y = A p, p.y -- split operator (DFX_F32X2): FP32-pipe products of the
@@ -1206,7 +1242,15 @@ template <typename T>
 void enqueue_pap_reduce(int64_t n, const Work<T>& w, cudaStream_t s)
 {
   const int nparts = sell_blocks(n) * (kSellThreads / 32);
-  k_pap_reduce<T><<<pap_blocks(n), kPapThreads, 0, s>>>(w, nparts);
+  int blocks = pap_blocks(n);
+  int per_thread = kPapPer;
+  if (blocks > kPapMaxBlocks)
+  {
+    // very large systems: more slots per thread, at most 32 blocks
+    blocks = kPapMaxBlocks;
+    per_thread = (int)((nparts + (int64_t)blocks * kPapThreads - 1) / ((int64_t)blocks * kPapThreads));
+  }
+  k_pap_reduce<T><<<blocks, kPapThreads, 0, s>>>(w, nparts, per_thread);
 }
 
 // Kernels of one PCG iteration: the FP32 sliced-ELL operator adds the p.Ap

@@ -342,3 +342,35 @@ def test_block_expansion_and_elasticity_refinement(cuda, oracle, capi):
         bh = b.cpu().numpy()
         r = bh - oracle.spmv(rp, cols, vals, xs.cpu().numpy(), bs=3)
         assert np.linalg.norm(r) / np.linalg.norm(bh) < 1e-10 * 1.001
+
+
+def test_refinement_on_a_system_above_four_million_rows(cuda, capi):
+    """The p.Ap reduction of the FP32 sliced-ELL iteration takes more than
+    16 partial slots per thread above ~4.2M rows (at most 32 blocks): P2 on
+    82^3 x 6 tetrahedra has 4,492,125 rows. The mixed solve meets the FP64
+    stopping test and lands within 1e-10 of the plain FP64 solution."""
+    from dolfinx_gb300 import fem, la, mesh
+
+    m = mesh.create_unit_cube(82, 82, 82, device="cuda")
+    V = fem.functionspace(m, ("Lagrange", 2))
+    assert V.num_dofs == 165 ** 3
+    X = V.tabulate_dof_coordinates()
+    bnd = np.flatnonzero(np.isclose(X[:, 0], 0.0) | np.isclose(X[:, 0], 1.0)).astype(np.int32)
+    bc = fem.dirichletbc(0.0, bnd, V)
+    rng = np.random.default_rng(5)
+    kappa = torch.from_numpy(np.exp(rng.normal(0.0, 1.0, m.num_cells))).cuda()
+    f = torch.from_numpy(rng.uniform(-1.0, 1.0, m.num_nodes)).cuda()
+    a = fem.poisson_form(V, kappa)
+    A = fem.assemble_matrix(a, [bc])
+    b = fem.RhsAssembler(fem.source_form(V, f), a, [bc]).assemble()
+    s64 = la.OperatorCGSolver(A, jacobi=True, sigma=1024)
+    x64 = torch.zeros_like(b)
+    r64 = s64.solve(b, x64, rtol=5e-12)
+    ir = la.IRSolver(A, jacobi=True, sigma=1024)
+    x = torch.zeros_like(b)
+    r = ir.solve(b, x, rtol=5e-12)
+    assert r64.status == 0 and r.status == 0
+    y = A.matvec(x)
+    assert ((b - y).norm() / b.norm()).item() < 5e-12 * 1.0001
+    rel = ((x - x64).norm() / x64.norm()).item()
+    assert rel < 1e-10, rel
