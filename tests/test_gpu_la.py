@@ -374,3 +374,30 @@ def test_refinement_on_a_system_above_four_million_rows(cuda, capi):
     assert ((b - y).norm() / b.norm()).item() < 5e-12 * 1.0001
     rel = ((x - x64).norm() / x64.norm()).item()
     assert rel < 1e-10, rel
+
+
+def test_released_operator_is_shared_but_not_applied(cuda, oracle, capi):
+    """dfx_operator_release_values: the source keeps its structure (shares
+    work and permute), its own values and scratch are freed
+    (dfx_operator_device_bytes drops by them), and applying or solving with
+    it is refused with DFX_ERR_INVALID, not run on freed memory."""
+    from dolfinx_gb300 import la
+
+    A, b, rp, cols = _poisson_system(oracle, (6, 5, 4), 2, 17)
+    src = la.SellOperator(A, torch.float32, 64, compress_cols=True)
+    before = src.device_bytes()
+    slots = src.info()["slots"]
+    src.release_values()
+    after = src.device_bytes()
+    # values (4 B per slot) and scratch (2 n floats) are gone
+    assert before - after == 4 * slots + 8 * A.nrows
+    x = torch.rand(A.nrows, dtype=torch.float32, device="cuda")
+    with pytest.raises(capi.DfxError) as e:
+        src.apply(x)
+    assert e.value.code == capi.DFX_ERR_INVALID
+    share = src.share(A)
+    assert share.device_bytes() == 4 * slots + 8 * A.nrows
+    y = share.apply(x)
+    ref = A.matvec(x.double()).float()
+    assert torch.allclose(y, ref, rtol=1e-5, atol=1e-6 * ref.abs().max().item())
+    assert torch.equal(share.to_operator(b), src.to_operator(b))

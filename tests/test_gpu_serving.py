@@ -104,3 +104,19 @@ def test_concurrent_whole_gpu_workers(cuda, oracle, capi):
         assert all(j.slot is None for j in jobs)
         for job in jobs:
             assert _residual(oracle, job) < 1e-10 * 1.001
+
+
+def test_structure_counts_what_it_holds(cuda, capi):
+    """A serving structure keeps the pattern only (its operators' values
+    released, no CSR values) and its byte count is what its tensors and
+    operators hold on the device."""
+    from dolfinx_gb300 import serving
+
+    st = serving.Structure(7, 2)
+    assert st.A0 is None and st.asm.A is None
+    ops = st.op64.device_bytes() + st.op32.device_bytes()
+    slots = st.ops_slots()
+    # structure arrays only: FP64 map + columns (8 B/slot), FP32 map + deltas (6 B/slot)
+    assert ops >= 14 * slots and ops < 14 * slots + 64 * st.ndofs + (1 << 20)
+    assert st.bytes == serving.device_bytes(st)
+    assert st.bytes > ops + st.nnz * 4  # and the CSR pattern, slot map, dofmap, mesh
