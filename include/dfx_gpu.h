@@ -341,21 +341,24 @@ int dfx_cg_solve(const dfx_csr* A, const double* d_b, double* d_x,
 
 /* dfx_cg_solve for callers that cannot allocate memory. No counterpart in
  * the reference. Some callers may not allocate at all once they are
- * running: a host that captures its work into CUDA graphs after its own
- * memory pool is set up, a plugin whose host application owns every
- * allocation, a real-time loop that forbids allocation after start-up.
- * This entry point calls no cudaMalloc, cudaMallocHost, cudaFree or graph
- * instantiation: its scratch (state, reduction buffers and the vectors r,
- * p, y) is a fixed 13 MiB array in the library's device image, present on
- * every GPU that loads the library until the process exits, and it reads
- * the solver state into pageable host memory every `check_every`
- * iterations (0: 20). At most 524288 scalar unknowns; larger systems are
- * rejected with DFX_ERR_INVALID. The first call on a device looks up the
- * array's device address (cudaGetSymbolAddress) with that device current;
- * make that first call before any stream capture. All calls share the one
- * array, so calls whose work overlaps on the GPU (other streams or host
- * threads) race; serialise them. Same iteration, stopping test and results
- * as dfx_cg_solve. */
+ * running: a host that has handed all device memory to its own pool and
+ * solves between that set-up and its later graph capture, a plugin whose
+ * host application owns every allocation, a real-time loop that forbids
+ * allocation after start-up. This entry point calls no cudaMalloc,
+ * cudaMallocHost, cudaFree or graph instantiation: its scratch (state,
+ * reduction buffers and the vectors r, p, y) is a fixed 13 MiB array in
+ * the library's device image, present on every GPU that loads the library
+ * until the process exits, and it reads the solver state into pageable
+ * host memory every `check_every` iterations (0: 20). Every call therefore
+ * synchronises its stream: no call may be made while its stream (or the
+ * legacy default stream) is being captured. At most 524288 scalar
+ * unknowns; larger systems are rejected with DFX_ERR_INVALID. The first
+ * call on a device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current and keeps it for the
+ * process; a host that calls cudaDeviceReset must not call this entry
+ * point again afterwards. All calls share the one array, so calls whose
+ * work overlaps on the GPU (other streams or host threads) race; serialise
+ * them. Same iteration, stopping test and results as dfx_cg_solve. */
 int dfx_cg_solve_noalloc(const dfx_csr* A, const double* d_b, double* d_x,
                          const double* d_dinv, double rtol, int32_t max_iters,
                          int32_t check_every, dfx_cg_info* info, void* stream);
