@@ -12,9 +12,12 @@
 // sliced-ELL SpMV is the exception: its blocks are short (one slice per
 // warp), and the ticket at the end of each one held the block's slot for
 // the length of a device-wide atomic (86 us against 74 us without it at P2
-// 64^3); its warps store their p.y partials in fixed slots and a small
-// fourth kernel reduces them the same deterministic way. The FP64 SpMV,
-// twice as long, keeps the fused ticket: a fourth launch cost it more. Scalars never
+// 64^3); its warps store their p.y partials in fixed slots. By default one
+// cooperative kernel then does the rest of the iteration (k_update_fused:
+// the p.y sum, the x/r update and the p update, with grid-wide barriers),
+// so the FP32 iteration is two kernels; otherwise a small fourth kernel
+// reduces the partials. The FP64 SpMV, twice as long, keeps the fused
+// ticket: a fourth launch cost it more. Scalars never
 // leave the device; every kernel returns at once when the state says done,
 // so a CUDA graph of K iterations is replayed until the host reads done.
 //
@@ -27,6 +30,7 @@
 #include "q4.cuh"
 #include "sell.cuh"
 
+#include <atomic>
 #include <map>
 #include <type_traits>
 #include <mutex>
@@ -55,6 +59,9 @@ struct CgState
   int32_t since;   // iterations since the last reliable update
   int32_t forced;  // reliable updates: replace at least every `forced` iterations (0: never)
   unsigned int ticket[4];
+  // Grid-wide barrier of the fused FP32 update (arrivals, generation).
+  unsigned int bar_count;
+  unsigned int bar_gen;
 };
 
 // Reliable updates with an assembled FP64 operator: a residual replacement
@@ -147,6 +154,9 @@ struct Work
   // Per-warp p.y partials of the sliced-ELL SpMV (one slot per warp of its
   // grid), summed by k_pap_reduce.
   double* wpart = nullptr;
+  // Per-block partial sums of the fused FP32 update: p.y, r.r, r.z (three
+  // rows of `blocks`).
+  double* bpart = nullptr;
 };
 
 // p[i] and, when the solve keeps them, its FP32 words.
@@ -174,6 +184,7 @@ Work<T> carve_work(Carver& c, int64_t n)
   w.p = c.take<T>(n);
   w.y = c.take<T>(n);
   w.wpart = c.take<double>((size_t)sell_blocks(n) * (kSellThreads / 32));
+  w.bpart = c.take<double>(3 * (size_t)w.blocks);
   return w;
 }
 
@@ -833,6 +844,322 @@ __global__ void __launch_bounds__(kElemThreads)
   }
 }
 
+
+// ---------------------------------------------------------------- fused update
+// The FP32 sliced-ELL inner iteration in two kernels: the SpMV (per-warp
+// p.y partials) and one cooperative launch that does what k_pap_reduce,
+// k_update and k_pupdate do, with two grid-wide barriers in place of two
+// kernel boundaries:
+//   A. p.y: block b adds a fixed range of the SpMV's warp partials;
+//      barrier; every block adds the block partials in index order (the
+//      same order in every block, so all blocks hold the same alpha);
+//   B. x += alpha p, r -= alpha y, z = D^{-1} r; r.r and r.z per block;
+//      barrier; every block adds them in index order and takes the same
+//      convergence / replacement decision as update_finish;
+//   C. p = z + beta p from the values phase B kept in registers (entries
+//      past EV float4 per thread are read again).
+// Block 0 alone writes the state, after the last barrier. The launch is
+// cooperative (all blocks resident), so the barrier waits end; each wait
+// is bounded all the same and gives up with DFX_ERR_TIMEOUT.
+constexpr int kBarrierPolls = 1 << 22;    // polls of one barrier wait (x 64 ns sleeps)
+
+// Grid-wide barrier; false in every thread of the block when its wait gave
+// up. All threads of every block call it.
+__device__ __forceinline__ bool grid_barrier(CgState* st)
+{
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0)
+  {
+    ok = 1;
+    volatile unsigned int* gen = &st->bar_gen;
+    const unsigned int g = *gen;
+    __threadfence();
+    if (atomicAdd(&st->bar_count, 1u) == gridDim.x - 1)
+    {
+      st->bar_count = 0;
+      __threadfence();
+      *gen = g + 1;
+    }
+    else
+    {
+      int i = 0;
+      while (*gen == g)
+      {
+        if (++i > kBarrierPolls)
+        {
+          ok = 0;
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+// Block sum in a fixed order (lane, then warp); thread 0 holds the result.
+__device__ __forceinline__ double fused_block_sum(double v, double* sh)
+{
+  v = dfx::warp_sum(v);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0)
+    sh[warp] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (warp == 0)
+  {
+    t = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.0;
+    t = dfx::warp_sum(t);
+  }
+  __syncthreads();
+  return t;
+}
+
+// Block sum of FP32 partials: each warp adds its lanes in FP32, the warp
+// sums are added in FP64 in warp order; thread 0 holds the result.
+__device__ __forceinline__ double fused_block_sum_f32(float v, double* sh)
+{
+  v = dfx::warp_sum(v);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0)
+    sh[warp] = (double)v;
+  __syncthreads();
+  double t = 0.0;
+  if (warp == 0)
+  {
+    t = lane < (int)(blockDim.x >> 5) ? sh[lane] : 0.0;
+    t = dfx::warp_sum(t);
+  }
+  __syncthreads();
+  return t;
+}
+
+// Sum of row k of the block partials (gridDim.x values) in index order,
+// the same in every block; every thread receives it.
+__device__ __forceinline__ double fused_grid_total(const double* part, double* sh, double* bc)
+{
+  double v = 0.0;
+  for (unsigned i = threadIdx.x; i < gridDim.x; i += blockDim.x)
+    v += __ldcg(part + i);
+  v = fused_block_sum(v, sh);
+  if (threadIdx.x == 0)
+    *bc = v;
+  __syncthreads();
+  const double t = *bc;
+  __syncthreads();
+  return t;
+}
+
+template <bool PRE, bool RELIABLE, int kFusedThreads, int kFusedEV>
+__global__ void __launch_bounds__(kFusedThreads, 1)
+    k_update_fused(float* __restrict__ x, const float* __restrict__ dinv, int64_t n,
+                   Work<float> w, int nparts)
+{
+  __shared__ double sh[32];
+  __shared__ double bc;
+  CgState* st = w.st;
+  if (is_done(st))
+    return;
+  // State read before the first barrier: block 0 writes it only after the
+  // last one.
+  const double rz_old = __ldg(&st->rz), rr0 = __ldg(&st->rr0), rtol2 = __ldg(&st->rtol2);
+  const double delta2 = __ldg(&st->delta2), rmax2 = __ldg(&st->rmax2);
+  const int iter = __ldg(&st->iter), max_iter = __ldg(&st->max_iter);
+  const int forced = __ldg(&st->forced), since = __ldg(&st->since);
+  const unsigned G = gridDim.x;
+
+  // A. p.y
+  {
+    const int64_t per = ((int64_t)nparts + G - 1) / G;
+    const int64_t b0 = (int64_t)blockIdx.x * per;
+    const int64_t b1 = b0 + per < nparts ? b0 + per : nparts;
+    double a = 0.0;
+    for (int64_t i = b0 + threadIdx.x; i < b1; i += kFusedThreads)
+      a += __ldcg(w.wpart + i);
+    a = fused_block_sum(a, sh);
+    if (threadIdx.x == 0)
+      w.bpart[blockIdx.x] = a;
+  }
+  if (!grid_barrier(st))
+  {
+    if (threadIdx.x == 0)
+    {
+      st->status = DFX_ERR_TIMEOUT;
+      st->done = 1;
+    }
+    return;
+  }
+  const double pAp = fused_grid_total(w.bpart, sh, &bc);
+  if (!(pAp > 0.0) || !isfinite(pAp))
+  {
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+    {
+      st->pAp = pAp;
+      st->status = DFX_ERR_BREAKDOWN;
+      st->done = 1;
+    }
+    return;
+  }
+  const float alpha = (float)(rz_old / pAp);
+
+  // B. x, r; z = D^{-1} r
+  const int64_t nvec = n / 4;
+  const int64_t T = (int64_t)G * kFusedThreads;
+  const int64_t t0 = (int64_t)blockIdx.x * kFusedThreads + threadIdx.x;
+  float4 keep_p[kFusedEV], keep_z[kFusedEV];
+  float rr = 0.f, rz = 0.f;
+  auto step = [&](float4& pv, float4 yv, float4& rv, float4& xv, float4 dv, float4& zv)
+  {
+    xv.x += alpha * pv.x;
+    xv.y += alpha * pv.y;
+    xv.z += alpha * pv.z;
+    xv.w += alpha * pv.w;
+    rv.x -= alpha * yv.x;
+    rv.y -= alpha * yv.y;
+    rv.z -= alpha * yv.z;
+    rv.w -= alpha * yv.w;
+    zv = PRE ? make_float4(dv.x * rv.x, dv.y * rv.y, dv.z * rv.z, dv.w * rv.w) : rv;
+    rr += rv.x * rv.x + rv.y * rv.y + rv.z * rv.z + rv.w * rv.w;
+    rz += rv.x * zv.x + rv.y * zv.y + rv.z * zv.z + rv.w * zv.w;
+  };
+  const float4* P4 = reinterpret_cast<const float4*>(w.p);
+  const float4* Y4 = reinterpret_cast<const float4*>(w.y);
+  float4* R4 = reinterpret_cast<float4*>(w.r);
+  float4* X4 = reinterpret_cast<float4*>(x);
+  const float4* D4 = reinterpret_cast<const float4*>(dinv);
+#pragma unroll
+  for (int k = 0; k < kFusedEV; ++k)
+  {
+    const int64_t v = t0 + k * T;
+    if (v < nvec)
+    {
+      float4 pv = P4[v], yv = Y4[v], rv = R4[v], xv = X4[v];
+      const float4 dv = PRE ? D4[v] : pv;
+      step(pv, yv, rv, xv, dv, keep_z[k]);
+      keep_p[k] = pv;
+      X4[v] = xv;
+      R4[v] = rv;
+    }
+  }
+  for (int64_t v = t0 + kFusedEV * T; v < nvec; v += T)
+  {
+    float4 pv = P4[v], yv = Y4[v], rv = R4[v], xv = X4[v], zv;
+    const float4 dv = PRE ? D4[v] : pv;
+    step(pv, yv, rv, xv, dv, zv);
+    X4[v] = xv;
+    R4[v] = rv;
+  }
+  if (blockIdx.x == 0)
+    for (int64_t i = nvec * 4 + threadIdx.x; i < n; i += kFusedThreads)
+    {
+      x[i] += alpha * w.p[i];
+      const float rn = w.r[i] - alpha * w.y[i];
+      w.r[i] = rn;
+      rr += rn * rn;
+      rz += rn * (PRE ? dinv[i] * rn : rn);
+    }
+  {
+    const double brr = fused_block_sum_f32(rr, sh);
+    const double brz = fused_block_sum_f32(rz, sh);
+    if (threadIdx.x == 0)
+    {
+      w.bpart[G + blockIdx.x] = brr;
+      w.bpart[2 * G + blockIdx.x] = brz;
+    }
+  }
+  if (!grid_barrier(st))
+  {
+    if (threadIdx.x == 0)
+    {
+      st->status = DFX_ERR_TIMEOUT;
+      st->done = 1;
+    }
+    return;
+  }
+  const double srr = fused_grid_total(w.bpart + G, sh, &bc);
+  const double srz = fused_grid_total(w.bpart + 2 * G, sh, &bc);
+
+  // The decision of update_finish, taken alike in every block.
+  bool done = false, pause = false;
+  int status = DFX_OK;
+  if (srr / rr0 < rtol2)
+  {
+    done = true;
+    if (RELIABLE)
+    {
+      status = kPauseConverged;
+      pause = true;
+    }
+  }
+  else if (!isfinite(srr))
+  {
+    status = DFX_ERR_BREAKDOWN;
+    done = true;
+  }
+  else if (iter + 1 >= max_iter)
+  {
+    status = DFX_ERR_NOT_CONVERGED;
+    done = true;
+  }
+  else if (RELIABLE && (srr < delta2 * rmax2 || (forced > 0 && since + 1 >= forced)))
+  {
+    status = kPauseUpdate;
+    done = true;
+    pause = true;
+  }
+  const double beta = srz / rz_old;
+  if (blockIdx.x == 0 && threadIdx.x == 0)
+  {
+    st->pAp = pAp;
+    st->alpha = rz_old / pAp;
+    st->rr = srr;
+    st->iter = iter + 1;
+    if (done)
+    {
+      st->status = status;
+      st->done = 1;
+    }
+    if (RELIABLE)
+      st->since = pause ? 0 : since + 1;
+    if (!pause)
+    {
+      st->beta = beta;
+      st->rz = srz;
+      if (RELIABLE)
+        st->rmax2 = fmax(rmax2, srr);
+    }
+  }
+  if (done)
+    return;
+
+  // C. p = z + beta p
+  const float fb = (float)beta;
+  float4* PW = reinterpret_cast<float4*>(w.p);
+#pragma unroll
+  for (int k = 0; k < kFusedEV; ++k)
+  {
+    const int64_t v = t0 + k * T;
+    if (v < nvec)
+    {
+      const float4 z = keep_z[k], q = keep_p[k];
+      PW[v] = make_float4(z.x + fb * q.x, z.y + fb * q.y, z.z + fb * q.z, z.w + fb * q.w);
+    }
+  }
+  for (int64_t v = t0 + kFusedEV * T; v < nvec; v += T)
+  {
+    const float4 q = P4[v], r = R4[v];
+    const float4 d = PRE ? D4[v] : r;
+    const float4 z = PRE ? make_float4(d.x * r.x, d.y * r.y, d.z * r.z, d.w * r.w) : r;
+    PW[v] = make_float4(z.x + fb * q.x, z.y + fb * q.y, z.z + fb * q.z, z.w + fb * q.w);
+  }
+  if (blockIdx.x == 0)
+    for (int64_t i = nvec * 4 + threadIdx.x; i < n; i += kFusedThreads)
+      w.p[i] = (PRE ? dinv[i] * w.r[i] : w.r[i]) + fb * w.p[i];
+}
+
 // Outer residual of the refinement: r = b - A x in FP64 with the FP64
 // operator, |r|^2 in FP64, r handed to the inner solve in FP32. The outer
 // state counts residual evaluations; the first one sets |r0|^2.
@@ -1299,8 +1626,17 @@ void enqueue_spmv_dot<double>(const OpRef& o, const Work<double>& w, cudaStream_
   }
 }
 
+// The FP32 sliced-ELL SpMV with per-warp p.y partials (no reduction).
+void enqueue_spmv_f32(const OpRef& o, const Work<float>& w, cudaStream_t s);
+
 template <>
 void enqueue_spmv_dot<float>(const OpRef& o, const Work<float>& w, cudaStream_t s)
+{
+  enqueue_spmv_f32(o, w, s);
+  enqueue_pap_reduce<float>(o.op->n, w, s);
+}
+
+void enqueue_spmv_f32(const OpRef& o, const Work<float>& w, cudaStream_t s)
 {
   const unsigned g = (unsigned)sell_blocks(o.op->n);
   auto launch = [&](auto comp, auto ch)
@@ -1329,7 +1665,6 @@ void enqueue_spmv_dot<float>(const OpRef& o, const Work<float>& w, cudaStream_t 
     else
       launch(F_{}, std::integral_constant<int, 4>{});
   }
-  enqueue_pap_reduce<float>(o.op->n, w, s);
 }
 
 bool aligned16(const void* p) { return ((uintptr_t)p & 15) == 0; }
@@ -1378,10 +1713,83 @@ void launch_update(T* x, const T* dinv, int64_t n, const Work<T>& w, bool vec, c
   k_update<T, PRE, RELIABLE><<<g, kElemThreads, 0, s>>>(x, dinv, n, w, vec);
 }
 
+// The fused FP32 update (k_update_fused) in place of k_pap_reduce, k_update
+// and k_pupdate: on unless the calling host thread switched it off, and off
+// for good in this process if a graph with its cooperative launch could not
+// be built. Per host thread, because the cooperative kernel holds the
+// registers of every SM while it runs: whole-GPU solves that run
+// concurrently from several threads and streams (the serving workers) would
+// take turns on the GPU. Measured on the serving sample: 33.1 solves/s
+// fused against 38.3 unfused.
+thread_local int t_fused_update = 1;
+std::atomic<int> g_fused_broken{0};
+
+bool fused_update_on() { return t_fused_update != 0 && g_fused_broken.load() == 0; }
+
+template <bool PRE, bool RELIABLE, int kFusedThreads, int kFusedEV>
+void launch_fused_as(float* x, const float* dinv, int64_t n, const Work<float>& w, cudaStream_t s)
+{
+  auto kern = k_update_fused<PRE, RELIABLE, kFusedThreads, kFusedEV>;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kFusedThreads, 0)
+          != cudaSuccess
+      || per_sm < 1)
+    per_sm = 1;
+  const int64_t nvec = n / 4;
+  const int64_t need = std::max<int64_t>(
+      1, (nvec + (int64_t)kFusedEV * kFusedThreads - 1) / ((int64_t)kFusedEV * kFusedThreads));
+  const int64_t cap = std::min<int64_t>((int64_t)dfx::num_sms(), w.blocks);
+  const unsigned g = (unsigned)std::min(need, cap);
+  cudaLaunchConfig_t cfg{};
+  cfg.gridDim = dim3(g);
+  cfg.blockDim = dim3(kFusedThreads);
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kern, x, dinv, n, w, sell_blocks(n) * (kSellThreads / 32));
+}
+
+// One 512-thread block per SM, four float4 per thread kept in registers
+// between phases B and C. Measured at P2 64^3 (mixed step): 143.6 ms
+// against 147.2 ms for the four-kernel iteration; 256 threads at two or
+// three blocks per SM measured 146.2 and 151.4 ms (more arrivals at each
+// barrier), 1024 threads with two float4 per thread 154.8 ms.
+template <bool PRE, bool RELIABLE>
+void launch_fused(float* x, const float* dinv, int64_t n, const Work<float>& w, cudaStream_t s)
+{
+  launch_fused_as<PRE, RELIABLE, 512, 4>(x, dinv, n, w, s);
+}
+
+// Kernels of one FP32 sliced-ELL iteration.
+int f32_sell_iter_kernels() { return fused_update_on() ? 2 : kF32SellIterKernels; }
+
 template <typename T>
 void enqueue_iteration(const OpRef& o, T* x, const T* dinv, int64_t n, const Work<T>& w,
                        bool reliable, cudaStream_t s)
 {
+  if constexpr (sizeof(T) == 4)
+    if (o.kind == kSell && fused_update_on() && vector_ok<T>(x, dinv, w))
+    {
+      enqueue_spmv_f32(o, w, s);
+      if (dinv)
+      {
+        if (reliable)
+          launch_fused<true, true>(x, dinv, n, w, s);
+        else
+          launch_fused<true, false>(x, dinv, n, w, s);
+      }
+      else
+      {
+        if (reliable)
+          launch_fused<false, true>(x, dinv, n, w, s);
+        else
+          launch_fused<false, false>(x, dinv, n, w, s);
+      }
+      return;
+    }
   if (o.kind == kQ4)
   {
     // The colour kernels return at once when the state is done.
@@ -1450,7 +1858,9 @@ int iteration_graph(const OpRef& o, T* x, const T* dinv, int64_t n, const Work<T
                     bool reliable, cudaGraphExec_t* out)
 {
   const bool q4 = o.kind == kQ4;
-  GraphKey key{(int)o.kind * 8 + (o.q4_tc ? 4 : 0) + (sizeof(T) == 4) * 2 + (reliable ? 1 : 0),
+  const bool fused = sizeof(T) == 4 && o.kind == kSell && fused_update_on();
+  GraphKey key{(fused ? 64 : 0) + (int)o.kind * 8 + (o.q4_tc ? 4 : 0) + (sizeof(T) == 4) * 2
+                   + (reliable ? 1 : 0),
                q4 ? (const void*)o.q4->verts
                   : (o.kind == kSell ? (const void*)o.op : (const void*)o.A->row_ptr),
                q4 ? (const void*)o.q4->edges32
@@ -1486,10 +1896,19 @@ int iteration_graph(const OpRef& o, T* x, const T* dinv, int64_t n, const Work<T
     ce = cudaStreamEndCapture(cs, &graph);
   }
   cudaStreamDestroy(cs);
-  DFX_CUDA(ce);
   cudaGraphExec_t exec;
-  ce = cudaGraphInstantiate(&exec, graph, 0);
-  cudaGraphDestroy(graph);
+  if (ce == cudaSuccess)
+  {
+    ce = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+  }
+  if (ce != cudaSuccess && fused)
+  {
+    // No graph with the cooperative launch here: the unfused iteration.
+    (void)cudaGetLastError();
+    g_fused_broken.store(1);
+    return iteration_graph<T>(o, x, dinv, n, w, K, reliable, out);
+  }
   DFX_CUDA(ce);
   if (g_graphs.size() >= 32)
   {
@@ -1804,7 +2223,7 @@ extern "C" int dfx_ir_solve(dfx_operator op64, dfx_operator op32, const double* 
         enqueue_init<float>(w.r, nullptr, d32, dinv32, n, w, inner_rtol, max_inner, s);
         DFX_CHECK_LAUNCH();
         kernels += 1;
-        if ((st = run_to_done(exec, w.st, max_inner, K, &h, s, &kernels, kF32SellIterKernels)))
+        if ((st = run_to_done(exec, w.st, max_inner, K, &h, s, &kernels, f32_sell_iter_kernels())))
           break;
         inner_total += h->iter;
         if (!restart)
@@ -1856,7 +2275,7 @@ extern "C" int dfx_ir_solve(dfx_operator op64, dfx_operator op32, const double* 
         break;
       enqueue_init<float>(w.r, nullptr, d32, dinv32, n, w, inner_rtol, max_inner, s);
       DFX_CHECK_LAUNCH();
-      if ((st = run_to_done(exec, w.st, max_inner, K, &h, s, &kernels, kF32SellIterKernels)))
+      if ((st = run_to_done(exec, w.st, max_inner, K, &h, s, &kernels, f32_sell_iter_kernels())))
         break;
       inner_total += h->iter;
       // A stalled or broken-down inner solve still yields a usable correction.
@@ -1902,7 +2321,7 @@ extern "C" int dfx_ir_solve(dfx_operator op64, dfx_operator op32, const double* 
         enqueue_pupdate<float>(dinv32, n, w, s);
         DFX_CHECK_LAUNCH();
         kernels += 1;
-        if ((st = run_to_done(exec, w.st, max_inner, K, &h, s, &kernels, kF32SellIterKernels)))
+        if ((st = run_to_done(exec, w.st, max_inner, K, &h, s, &kernels, f32_sell_iter_kernels())))
           break;
         const int32_t why = h->status;
         k_ir_correct<<<blocks, kThreads, 0, s>>>(xp, d32, n);
@@ -2195,4 +2614,17 @@ extern "C" int dfx_cg_solve_noalloc(const dfx_csr* A, const double* d_b, double*
     kernels += 3 * (int64_t)K;
   }
   return report(&h, info, kernels);
+}
+
+extern "C" int dfx_set_cg_fused_update(int32_t on)
+{
+  t_fused_update = on ? 1 : 0;
+  return DFX_OK;
+}
+
+extern "C" int dfx_get_cg_fused_update(int32_t* on)
+{
+  DFX_REQUIRE(on, "on is NULL");
+  *on = fused_update_on() ? 1 : 0;
+  return DFX_OK;
 }

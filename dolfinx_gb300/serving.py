@@ -458,6 +458,11 @@ class Server:
     # ------------------------------------------------------------ solving
     def _worker(self):
         stream = torch.cuda.Stream()
+        # Whole-GPU solves run concurrently from several workers: the
+        # four-kernel FP32 iteration, not the fused cooperative one, which
+        # holds every SM while it runs (measured: 38.3 solves/s against
+        # 33.1 on the 64-request sample).
+        _capi.check(_capi.lib().dfx_set_cg_fused_update(0))
         while True:
             job = self.large_q.get()
             if job is None:

@@ -568,6 +568,18 @@ int dfx_operator_device_bytes(dfx_operator op, size_t* bytes);
  * 8. Results are bitwise the same for every choice. */
 int dfx_operator_set_chunk(dfx_operator op, int32_t chunk);
 
+/* Launch setting of the FP32 inner iteration (no reference counterpart),
+ * for the calling host thread: on = 1 (default) runs each iteration as two
+ * kernels, the SpMV and one cooperative kernel for the p.Ap reduction, the
+ * x/r update with its dot products and the p update (grid-wide barriers in
+ * place of kernel boundaries); on = 0 runs the four-kernel iteration. Same
+ * recurrence; the dot products are summed in another fixed order. The
+ * cooperative kernel holds every SM while it runs, so threads that solve
+ * concurrently on several streams should switch it off. Applies to solves
+ * the thread starts after the call. */
+int dfx_set_cg_fused_update(int32_t on);
+int dfx_get_cg_fused_update(int32_t* on);
+
 /* dfx_cg_solve on an FP64 operator (same iteration and stopping test). */
 size_t dfx_cg_op_workspace_bytes(int64_t n);
 int dfx_cg_solve_op(dfx_operator op, const double* d_b, double* d_x,

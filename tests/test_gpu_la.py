@@ -1,6 +1,8 @@
 """GPU parity: SpMV (FP64, FP32 values, 3x3 blocks), Jacobi diagonal,
 inner product and CG against the oracle."""
 
+import ctypes as C
+
 import numpy as np
 import pytest
 import torch
@@ -324,6 +326,76 @@ def test_iterative_refinement_reaches_fp64(cuda, oracle, capi, variant, inner_rt
     assert np.linalg.norm(res) / np.linalg.norm(bh) < 1e-12 * 1.0001
     rel = (x - x64).norm().item() / x64.norm().item()
     assert rel < 1e-10, rel
+
+
+def _fused_vs_unfused(capi, A, b, residual):
+    """IR solves of A x = b with the fused FP32 update on and off."""
+    from dolfinx_gb300 import la
+
+    L = capi.lib()
+    out = {}
+    try:
+        for fused in (1, 0):
+            capi.check(L.dfx_set_cg_fused_update(fused))
+            on = C.c_int32(-1)
+            capi.check(L.dfx_get_cg_fused_update(C.byref(on)))
+            assert on.value == fused
+            ir = la.IRSolver(A, jacobi=True)
+            x = torch.zeros_like(b)
+            r = ir.solve(b, x, rtol=1e-11)
+            assert r.status == 0
+            assert residual(x) < 1e-11 * 1.0001
+            out[fused] = (r, x)
+    finally:
+        capi.check(L.dfx_set_cg_fused_update(1))
+    (r1, x1), (r0, x0) = out[1], out[0]
+    assert abs(r1.inner_iterations - r0.inner_iterations) <= max(2, r0.inner_iterations // 100)
+    assert (x1 - x0).norm().item() / x0.norm().item() < 1e-9
+    # two kernels per inner iteration against four
+    assert r1.kernel_launches < r0.kernel_launches
+
+
+@pytest.mark.parametrize("n", [(12, 12, 12), (23, 21, 19)])
+def test_fused_update_matches_four_kernel_iteration(cuda, oracle, capi, n):
+    """The two-kernel FP32 inner iteration (SpMV + one cooperative kernel
+    with grid-wide barriers) and the four-kernel one run the same
+    recurrence: both meet the FP64 stopping test in the oracle's SpMV, with
+    inner iteration counts within 1 % and solutions within the accuracy the
+    solves carry. (23, 21, 19) P2 has a ragged tail (n % 4 = 3)."""
+    A, b, rp, cols = _poisson_system(oracle, n, 2, 33)
+    bh = b.cpu().numpy()
+
+    def residual(x):
+        res = bh - oracle.spmv(rp, cols, A.vals.cpu().numpy(), x.cpu().numpy())
+        return np.linalg.norm(res) / np.linalg.norm(bh)
+
+    _fused_vs_unfused(capi, A, b, residual)
+
+
+def test_fused_update_large_system(cuda, capi):
+    """A P2 system of 1.77M unknowns: more float4 per thread than the fused
+    kernel keeps in registers between its phases, so part of p, r and D^-1
+    is read again for the p update. Residuals in the library's FP64 CSR
+    SpMV (itself checked against the oracle)."""
+    from dolfinx_gb300 import fem, la, mesh
+
+    m = mesh.create_unit_cube(60, 60, 60)
+    V = fem.functionspace(m, ("Lagrange", 2))
+    rng = np.random.default_rng(5)
+    kappa = torch.from_numpy(np.exp(rng.normal(0.0, 1.0, m.num_cells))).cuda()
+    f = torch.from_numpy(rng.uniform(-1, 1, m.num_nodes)).cuda()
+    X = V.tabulate_dof_coordinates()
+    bnd = np.flatnonzero(np.isclose(X[:, 0], 0) | np.isclose(X[:, 0], 1)).astype(np.int32)
+    bc = fem.dirichletbc(0.0, bnd, V)
+    a = fem.poisson_form(V, kappa)
+    A = fem.assemble_matrix(a, bcs=[bc])
+    b = fem.RhsAssembler(fem.source_form(V, f), a, [bc]).assemble()
+    assert V.num_dofs // 4 > 152 * 512 * 4
+
+    def residual(x):
+        return (b - A.matvec(x)).norm().item() / b.norm().item()
+
+    _fused_vs_unfused(capi, A, b, residual)
 
 
 def test_block_expansion_and_elasticity_refinement(cuda, oracle, capi):
