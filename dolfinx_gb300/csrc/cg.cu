@@ -971,6 +971,31 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
   const int forced = __ldg(&st->forced), since = __ldg(&st->since);
   const unsigned G = gridDim.x;
 
+  // The entries this thread keeps: p, y, r and D^{-1} are loaded before
+  // phase A, so that their loads are in flight across the p.y reduction
+  // and the first barrier.
+  const int64_t nvec = n / 4;
+  const int64_t T = (int64_t)G * kFusedThreads;
+  const int64_t t0 = (int64_t)blockIdx.x * kFusedThreads + threadIdx.x;
+  const float4* P4 = reinterpret_cast<const float4*>(w.p);
+  const float4* Y4 = reinterpret_cast<const float4*>(w.y);
+  float4* R4 = reinterpret_cast<float4*>(w.r);
+  float4* X4 = reinterpret_cast<float4*>(x);
+  const float4* D4 = reinterpret_cast<const float4*>(dinv);
+  float4 kp[kFusedEV], ky[kFusedEV], kr[kFusedEV], kd[kFusedEV];
+#pragma unroll
+  for (int k = 0; k < kFusedEV; ++k)
+  {
+    const int64_t v = t0 + k * T;
+    if (v < nvec)
+    {
+      kp[k] = P4[v];
+      ky[k] = Y4[v];
+      kr[k] = R4[v];
+      kd[k] = PRE ? D4[v] : kp[k];
+    }
+  }
+
   // A. p.y
   {
     const int64_t per = ((int64_t)nparts + G - 1) / G;
@@ -1006,10 +1031,6 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
   const float alpha = (float)(rz_old / pAp);
 
   // B. x, r; z = D^{-1} r
-  const int64_t nvec = n / 4;
-  const int64_t T = (int64_t)G * kFusedThreads;
-  const int64_t t0 = (int64_t)blockIdx.x * kFusedThreads + threadIdx.x;
-  float4 keep_p[kFusedEV], keep_z[kFusedEV];
   float rr = 0.f, rz = 0.f;
   auto step = [&](float4& pv, float4 yv, float4& rv, float4& xv, float4 dv, float4& zv)
   {
@@ -1025,32 +1046,59 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
     rr += rv.x * rv.x + rv.y * rv.y + rv.z * rv.z + rv.w * rv.w;
     rz += rv.x * zv.x + rv.y * zv.y + rv.z * zv.z + rv.w * zv.w;
   };
-  const float4* P4 = reinterpret_cast<const float4*>(w.p);
-  const float4* Y4 = reinterpret_cast<const float4*>(w.y);
-  float4* R4 = reinterpret_cast<float4*>(w.r);
-  float4* X4 = reinterpret_cast<float4*>(x);
-  const float4* D4 = reinterpret_cast<const float4*>(dinv);
-#pragma unroll
-  for (int k = 0; k < kFusedEV; ++k)
   {
-    const int64_t v = t0 + k * T;
-    if (v < nvec)
+    float4 kx[kFusedEV];
+#pragma unroll
+    for (int k = 0; k < kFusedEV; ++k)
     {
-      float4 pv = P4[v], yv = Y4[v], rv = R4[v], xv = X4[v];
-      const float4 dv = PRE ? D4[v] : pv;
-      step(pv, yv, rv, xv, dv, keep_z[k]);
-      keep_p[k] = pv;
-      X4[v] = xv;
-      R4[v] = rv;
+      const int64_t v = t0 + k * T;
+      if (v < nvec)
+        kx[k] = X4[v];
+    }
+#pragma unroll
+    for (int k = 0; k < kFusedEV; ++k)
+    {
+      const int64_t v = t0 + k * T;
+      if (v < nvec)
+      {
+        float4 z;
+        step(kp[k], ky[k], kr[k], kx[k], kd[k], z);
+        X4[v] = kx[k];
+        R4[v] = kr[k];
+      }
     }
   }
-  for (int64_t v = t0 + kFusedEV * T; v < nvec; v += T)
+  // Entries past the kept ones, kRem float4 per round with every load of
+  // the round issued first.
+  constexpr int kRem = 2;
+  for (int64_t v0 = t0 + kFusedEV * T; v0 < nvec; v0 += kRem * T)
   {
-    float4 pv = P4[v], yv = Y4[v], rv = R4[v], xv = X4[v], zv;
-    const float4 dv = PRE ? D4[v] : pv;
-    step(pv, yv, rv, xv, dv, zv);
-    X4[v] = xv;
-    R4[v] = rv;
+    float4 pv[kRem], yv[kRem], rv[kRem], xv[kRem], dv[kRem];
+#pragma unroll
+    for (int k = 0; k < kRem; ++k)
+    {
+      const int64_t v = v0 + k * T;
+      if (v < nvec)
+      {
+        pv[k] = P4[v];
+        yv[k] = Y4[v];
+        rv[k] = R4[v];
+        xv[k] = X4[v];
+        dv[k] = PRE ? D4[v] : pv[k];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < kRem; ++k)
+    {
+      const int64_t v = v0 + k * T;
+      if (v < nvec)
+      {
+        float4 z;
+        step(pv[k], yv[k], rv[k], xv[k], dv[k], z);
+        X4[v] = xv[k];
+        R4[v] = rv[k];
+      }
+    }
   }
   if (blockIdx.x == 0)
     for (int64_t i = nvec * 4 + threadIdx.x; i < n; i += kFusedThreads)
@@ -1144,16 +1192,38 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
     const int64_t v = t0 + k * T;
     if (v < nvec)
     {
-      const float4 z = keep_z[k], q = keep_p[k];
+      const float4 r = kr[k], d = kd[k], q = kp[k];
+      const float4 z = PRE ? make_float4(d.x * r.x, d.y * r.y, d.z * r.z, d.w * r.w) : r;
       PW[v] = make_float4(z.x + fb * q.x, z.y + fb * q.y, z.z + fb * q.z, z.w + fb * q.w);
     }
   }
-  for (int64_t v = t0 + kFusedEV * T; v < nvec; v += T)
+  for (int64_t v0 = t0 + kFusedEV * T; v0 < nvec; v0 += kRem * T)
   {
-    const float4 q = P4[v], r = R4[v];
-    const float4 d = PRE ? D4[v] : r;
-    const float4 z = PRE ? make_float4(d.x * r.x, d.y * r.y, d.z * r.z, d.w * r.w) : r;
-    PW[v] = make_float4(z.x + fb * q.x, z.y + fb * q.y, z.z + fb * q.z, z.w + fb * q.w);
+    float4 q[kRem], r[kRem], d[kRem];
+#pragma unroll
+    for (int k = 0; k < kRem; ++k)
+    {
+      const int64_t v = v0 + k * T;
+      if (v < nvec)
+      {
+        q[k] = P4[v];
+        r[k] = R4[v];
+        d[k] = PRE ? D4[v] : r[k];
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < kRem; ++k)
+    {
+      const int64_t v = v0 + k * T;
+      if (v < nvec)
+      {
+        const float4 z = PRE ? make_float4(d[k].x * r[k].x, d[k].y * r[k].y, d[k].z * r[k].z,
+                                           d[k].w * r[k].w)
+                             : r[k];
+        PW[v] = make_float4(z.x + fb * q[k].x, z.y + fb * q[k].y, z.z + fb * q[k].z,
+                            z.w + fb * q[k].w);
+      }
+    }
   }
   if (blockIdx.x == 0)
     for (int64_t i = nvec * 4 + threadIdx.x; i < n; i += kFusedThreads)
