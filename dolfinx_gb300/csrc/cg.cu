@@ -874,8 +874,14 @@ __device__ __forceinline__ bool grid_barrier(CgState* st)
     ok = 1;
     volatile unsigned int* gen = &st->bar_gen;
     const unsigned int g = *gen;
-    __threadfence();
-    if (atomicAdd(&st->bar_count, 1u) == gridDim.x - 1)
+    // Arrival: an acquire-release add publishes this block's partials and,
+    // for the last block, acquires everyone's (release sequence of the count).
+    unsigned int old;
+    asm volatile("atom.add.acq_rel.gpu.u32 %0, [%1], 1;"
+                 : "=r"(old)
+                 : "l"(&st->bar_count)
+                 : "memory");
+    if (old == gridDim.x - 1)
     {
       st->bar_count = 0;
       __threadfence();
@@ -937,6 +943,45 @@ __device__ __forceinline__ double fused_block_sum_f32(float v, double* sh)
   return t;
 }
 
+// Sums of two rows of block partials (gridDim.x values each) in index
+// order, the same in every block; every thread receives both.
+__device__ __forceinline__ void fused_grid_total2(const double* p0, const double* p1,
+                                                  double* sh, double* bc, double& t0,
+                                                  double& t1)
+{
+  double v0 = 0.0, v1 = 0.0;
+  for (unsigned i = threadIdx.x; i < gridDim.x; i += blockDim.x)
+  {
+    v0 += __ldcg(p0 + i);
+    v1 += __ldcg(p1 + i);
+  }
+  v0 = dfx::warp_sum(v0);
+  v1 = dfx::warp_sum(v1);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0)
+  {
+    sh[warp] = v0;
+    sh[16 + warp] = v1;
+  }
+  __syncthreads();
+  if (warp == 0)
+  {
+    const int nw = (int)(blockDim.x >> 5);
+    double a = lane < nw ? sh[lane] : 0.0, b = lane < nw ? sh[16 + lane] : 0.0;
+    a = dfx::warp_sum(a);
+    b = dfx::warp_sum(b);
+    if (lane == 0)
+    {
+      bc[0] = a;
+      bc[1] = b;
+    }
+  }
+  __syncthreads();
+  t0 = bc[0];
+  t1 = bc[1];
+  __syncthreads();
+}
+
 // Sum of row k of the block partials (gridDim.x values) in index order,
 // the same in every block; every thread receives it.
 __device__ __forceinline__ double fused_grid_total(const double* part, double* sh, double* bc)
@@ -960,6 +1005,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
 {
   __shared__ double sh[32];
   __shared__ double bc;
+  __shared__ double bc2[2];
   CgState* st = w.st;
   if (is_done(st))
     return;
@@ -1127,8 +1173,8 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
     }
     return;
   }
-  const double srr = fused_grid_total(w.bpart + G, sh, &bc);
-  const double srz = fused_grid_total(w.bpart + 2 * G, sh, &bc);
+  double srr, srz;
+  fused_grid_total2(w.bpart + G, w.bpart + 2 * G, sh, bc2, srr, srz);
 
   // The decision of update_finish, taken alike in every block.
   bool done = false, pause = false;
