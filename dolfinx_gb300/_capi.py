@@ -224,6 +224,7 @@ _SIGS = {
     "dfx_operator_set_chunk": (C.c_int, [_P, C.c_int32]),
     "dfx_set_cg_fused_update": (C.c_int, [C.c_int32]),
     "dfx_get_cg_fused_update": (C.c_int, [C.POINTER(C.c_int32)]),
+    "dfx_selftest_grid_barrier": (C.c_int, [C.POINTER(C.c_int32)]),
     "dfx_dofmap_device_workspace_bytes": (C.c_size_t, [C.c_int32, C.c_int32, C.c_int32]),
     "dfx_dofmap_create_tet_device": (C.c_int, [C.c_int32, _P, C.c_int32, C.c_int32, _P, _P, _P,
                                                C.c_size_t, _P]),

@@ -865,7 +865,7 @@ constexpr int kBarrierPolls = 1 << 22;    // polls of one barrier wait (x 64 ns 
 
 // Grid-wide barrier; false in every thread of the block when its wait gave
 // up. All threads of every block call it.
-__device__ __forceinline__ bool grid_barrier(CgState* st)
+__device__ __forceinline__ bool grid_barrier(CgState* st, unsigned int arrivals)
 {
   __shared__ int ok;
   __syncthreads();
@@ -881,7 +881,7 @@ __device__ __forceinline__ bool grid_barrier(CgState* st)
                  : "=r"(old)
                  : "l"(&st->bar_count)
                  : "memory");
-    if (old == gridDim.x - 1)
+    if (old == arrivals - 1)
     {
       st->bar_count = 0;
       __threadfence();
@@ -904,6 +904,18 @@ __device__ __forceinline__ bool grid_barrier(CgState* st)
   }
   __syncthreads();
   return ok != 0;
+}
+
+// Self-test of the barrier's bounded wait: the blocks wait for one arrival
+// more than the grid has, so every wait runs out; each block records that
+// it gave up (st->updates counts them) and the status DFX_ERR_TIMEOUT.
+__global__ void k_barrier_selftest(CgState* st)
+{
+  if (!grid_barrier(st, gridDim.x + 1) && threadIdx.x == 0)
+  {
+    atomicAdd(&st->updates, 1);
+    st->status = DFX_ERR_TIMEOUT;
+  }
 }
 
 // Block sum in a fixed order (lane, then warp); thread 0 holds the result.
@@ -1054,7 +1066,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
     if (threadIdx.x == 0)
       w.bpart[blockIdx.x] = a;
   }
-  if (!grid_barrier(st))
+  if (!grid_barrier(st, gridDim.x))
   {
     if (threadIdx.x == 0)
     {
@@ -1164,7 +1176,7 @@ __global__ void __launch_bounds__(kFusedThreads, 1)
       w.bpart[2 * G + blockIdx.x] = brz;
     }
   }
-  if (!grid_barrier(st))
+  if (!grid_barrier(st, gridDim.x))
   {
     if (threadIdx.x == 0)
     {
@@ -2742,5 +2754,40 @@ extern "C" int dfx_get_cg_fused_update(int32_t* on)
 {
   DFX_REQUIRE(on, "on is NULL");
   *on = fused_update_on() ? 1 : 0;
+  return DFX_OK;
+}
+
+// Runs the grid barrier of the fused update with one arrival missing (two
+// cooperative blocks waiting for three), so that its bounded waits run out;
+// *gave_up = the number of blocks that reported the timeout (2 when the
+// wait limit works). The device stays usable. Uses its own small state
+// allocation.
+extern "C" int dfx_selftest_grid_barrier(int32_t* gave_up)
+{
+  DFX_REQUIRE(gave_up, "gave_up is NULL");
+  *gave_up = 0;
+  CgState* st = nullptr;
+  if (cudaMalloc(&st, sizeof(CgState)) != cudaSuccess)
+    return dfx::no_memory("barrier self-test state");
+  cudaError_t e = cudaMemset(st, 0, sizeof(CgState));
+  if (e == cudaSuccess)
+  {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3(2);
+    cfg.blockDim = dim3(64);
+    cfg.stream = 0;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    e = cudaLaunchKernelEx(&cfg, k_barrier_selftest, st);
+  }
+  CgState h{};
+  if (e == cudaSuccess)
+    e = cudaMemcpy(&h, st, sizeof(CgState), cudaMemcpyDeviceToHost);
+  cudaFree(st);
+  DFX_CUDA(e);
+  *gave_up = h.status == DFX_ERR_TIMEOUT ? h.updates : 0;
   return DFX_OK;
 }

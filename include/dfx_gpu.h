@@ -579,6 +579,13 @@ int dfx_operator_set_chunk(dfx_operator op, int32_t chunk);
  * the thread starts after the call. */
 int dfx_set_cg_fused_update(int32_t on);
 int dfx_get_cg_fused_update(int32_t* on);
+/* Self-test of the fused update's grid barrier (no reference counterpart):
+ * two cooperative blocks wait for a third arrival that never comes, so
+ * their bounded waits run out (about a quarter of a second) and each
+ * reports DFX_ERR_TIMEOUT instead of hanging. *gave_up = the number of
+ * blocks that reported it (2 when the limit works). Synchronises the
+ * device. */
+int dfx_selftest_grid_barrier(int32_t* gave_up);
 
 /* dfx_cg_solve on an FP64 operator (same iteration and stopping test). */
 size_t dfx_cg_op_workspace_bytes(int64_t n);

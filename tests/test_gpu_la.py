@@ -372,6 +372,23 @@ def test_fused_update_matches_four_kernel_iteration(cuda, oracle, capi, n):
     _fused_vs_unfused(capi, A, b, residual)
 
 
+def test_grid_barrier_wait_is_bounded(cuda, capi):
+    """The grid barrier of the fused update gives up instead of hanging: with
+    an arrival missing, both blocks of the self-test report DFX_ERR_TIMEOUT
+    within the wait limit, and the context still runs work afterwards."""
+    import time
+
+    from dolfinx_gb300 import la
+
+    gave_up = C.c_int32(-1)
+    t0 = time.perf_counter()
+    capi.check(capi.lib().dfx_selftest_grid_barrier(C.byref(gave_up)))
+    assert gave_up.value == 2
+    assert time.perf_counter() - t0 < 30.0
+    x = torch.arange(1000, dtype=torch.float64, device="cuda")
+    assert abs(la.inner_product(x, x) - float((x * x).sum())) < 1e-6
+
+
 def test_fused_update_large_system(cuda, capi):
     """A P2 system of 1.77M unknowns: more float4 per thread than the fused
     kernel keeps in registers between its phases, so part of p, r and D^-1
