@@ -12,6 +12,13 @@
 // device_vector, an owning container with .data() and .size() as DOLFINx's
 // containers are used; there is no CPU fallback for device work.
 //
+// The classes keep DOLFINx's template shapes: la::MatrixCSR<Scalar,
+// Container, ColContainer, RowPtrContainer>, la::Vector<T, Container>,
+// fem::FunctionSpace<T>, fem::Form<T, U>, fem::DirichletBC<T, U>, with the
+// containers defaulting to device_vector. The device kernels take FP64
+// values and geometry, so each template admits double only (a
+// static_assert says so).
+//
 // Paths cited below are relative to the DOLFINx source tree. C++20.
 #pragma once
 
@@ -32,6 +39,7 @@
 #include <stdexcept>
 #include <string>
 #include <string_view>
+#include <type_traits>
 #include <utility>
 #include <vector>
 
@@ -406,9 +414,13 @@ namespace fem
 /// mesh: the dofmap of fem::create_dofmap (fem/utils.cpp:32-76), numbered
 /// as DOLFINx numbers it on one rank. Device copies of the mesh and dofmap
 /// are made on first use.
+template <typename T = double>
 class FunctionSpace
 {
+  static_assert(std::is_same_v<T, double>, "the device kernels take FP64 geometry");
+
 public:
+  using geometry_type = T;
   FunctionSpace(std::shared_ptr<const mesh::Mesh> m, int degree, int bs = 1)
       : mesh_(std::move(m)), degree_(degree), bs_(bs)
   {
@@ -475,7 +487,8 @@ struct SparsityPattern
 
 /// fem::create_sparsity_pattern + SparsityPattern::finalize
 /// (fem/utils.h:197-314, la/SparsityPattern.cpp:264-491), on the host.
-inline SparsityPattern create_sparsity_pattern(const FunctionSpace& V)
+template <typename U>
+SparsityPattern create_sparsity_pattern(const FunctionSpace<U>& V)
 {
   SparsityPattern sp;
   sp.row_ptr.resize(V.num_nodes() + 1);
@@ -493,11 +506,50 @@ inline SparsityPattern create_sparsity_pattern(const FunctionSpace& V)
 // ------------------------------------------------------------------- la
 namespace la
 {
-/// la::MatrixCSR on the device (la/MatrixCSR.h:67-70): int64 row
-/// pointers, int32 columns, FP64 values of bs x bs row-major blocks.
+/// la::Vector<T, Container> (la/Vector.h:35-120) on the device: the
+/// entries of one rank (no ghosts), in block size bs.
+template <typename T = double, typename Container = device_vector<T>>
+class Vector
+{
+  static_assert(std::is_same_v<T, double>, "the device kernels take FP64 vectors");
+
+public:
+  using value_type = T;
+  using container_type = Container;
+  Vector(std::int64_t n, int bs = 1) : bs_(bs), x_((std::size_t)n * bs) {}
+  int bs() const { return bs_; }
+  std::size_t size() const { return x_.size(); }
+  /// The entries (device memory).
+  std::span<const T> array() const { return {x_.data(), x_.size()}; }
+  std::span<T> mutable_array() { return {x_.data(), x_.size()}; }
+  /// Set every entry to v.
+  void set(T v)
+  {
+    if (v == T(0))
+      x_.zero();
+    else
+      x_.assign(std::vector<T>(x_.size(), v));
+  }
+  Container& device() { return x_; }
+  const Container& device() const { return x_; }
+
+private:
+  int bs_;
+  Container x_;
+};
+
+/// la::MatrixCSR<Scalar, Container, ColContainer, RowPtrContainer>
+/// (la/MatrixCSR.h:67-70) on the device: int64 row pointers, int32
+/// columns, FP64 values of bs x bs row-major blocks.
+template <typename Scalar = double, typename Container = device_vector<Scalar>,
+          typename ColContainer = device_vector<std::int32_t>,
+          typename RowPtrContainer = device_vector<std::int64_t>>
 class MatrixCSR
 {
+  static_assert(std::is_same_v<Scalar, double>, "the device kernels take FP64 values");
+
 public:
+  using value_type = Scalar;
   MatrixCSR(const fem::SparsityPattern& sp, int bs = 1)
       : nrows_((std::int32_t)sp.row_ptr.size() - 1), bs_(bs), row_ptr_(sp.row_ptr),
         cols_(sp.cols), vals_(sp.cols.size() * bs * bs)
@@ -505,10 +557,22 @@ public:
   }
   std::int32_t num_rows() const { return nrows_; }
   int bs() const { return bs_; }
+  /// MatrixCSR::block_size.
+  std::array<int, 2> block_size() const { return {bs_, bs_}; }
   std::int64_t nnz() const { return (std::int64_t)cols_.size(); }
-  device_vector<double>& values() { return vals_; }
-  const device_vector<double>& values() const { return vals_; }
+  Container& values() { return vals_; }
+  const Container& values() const { return vals_; }
+  const RowPtrContainer& row_ptr() const { return row_ptr_; }
+  const ColContainer& cols() const { return cols_; }
   void set_zero() { vals_.zero(); }
+  /// MatrixCSR::set: every stored value to x.
+  void set(Scalar x)
+  {
+    if (x == Scalar(0))
+      vals_.zero();
+    else
+      vals_.assign(std::vector<Scalar>(vals_.size(), x));
+  }
 
   /// The dfx_csr view of this matrix for the C ABI.
   dfx_csr csr() const
@@ -519,7 +583,7 @@ public:
   }
 
   /// MatrixCSR::mult (la/MatrixCSR.h:877-946): y += A x.
-  void mult(const device_vector<double>& x, device_vector<double>& y) const
+  void mult(const device_vector<Scalar>& x, device_vector<Scalar>& y) const
   {
     const std::size_t n = (std::size_t)nrows_ * bs_;
     if (x.size() != n || y.size() != n)
@@ -527,13 +591,14 @@ public:
     const dfx_csr A = csr();
     check(dfx_spmv(&A, x.data(), y.data(), 1.0, nullptr));
   }
+  void mult(const Vector<Scalar>& x, Vector<Scalar>& y) const { mult(x.device(), y.device()); }
 
 private:
   std::int32_t nrows_;
   int bs_;
-  device_vector<std::int64_t> row_ptr_;
-  device_vector<std::int32_t> cols_;
-  device_vector<double> vals_;
+  RowPtrContainer row_ptr_;
+  ColContainer cols_;
+  Container vals_;
 };
 
 /// la::inner_product (la/Vector.h:434-460), a deterministic reduction.
@@ -551,6 +616,25 @@ inline double inner_product(const device_vector<double>& a, const device_vector<
 
 /// la::norm(x, Norm::l2) (la/Vector.h:489-514).
 inline double norm(const device_vector<double>& x) { return std::sqrt(inner_product(x, x)); }
+
+template <typename T>
+T inner_product(const Vector<T>& a, const Vector<T>& b)
+{
+  return inner_product(a.device(), b.device());
+}
+
+/// la::Norm (la/utils.h): only the l2 norm is provided on the device.
+enum class Norm
+{
+  l2
+};
+
+template <typename T>
+T norm(const Vector<T>& x, Norm type = Norm::l2)
+{
+  (void)type;
+  return norm(x.device());
+}
 } // namespace la
 
 // ----------------------------------------------------- fem (device side)
@@ -560,9 +644,16 @@ namespace fem
 /// the element kernel is chosen by the kind, coefficients live on the
 /// device. Per-cell coefficients have one value per cell, P1 sources one
 /// value per geometry node; an empty span selects the constant.
+template <typename T = double, typename U = T>
 class Form
 {
+  static_assert(std::is_same_v<T, double> && std::is_same_v<U, double>,
+                "the device kernels take FP64 values and geometry");
+  using FunctionSpace = fem::FunctionSpace<U>;
+
 public:
+  using scalar_type = T;
+  using geometry_type = U;
   static Form poisson(std::shared_ptr<const FunctionSpace> V, std::span<const double> kappa = {},
                       double kappa_const = 1.0, double k2 = 0.0)
   {
@@ -743,8 +834,13 @@ private:
 
 /// DirichletBC (fem/DirichletBC.h): u = g on the given nodes (all bs
 /// components), g a constant or a full vector of num_dofs values.
+template <typename T = double, typename U = T>
 class DirichletBC
 {
+  static_assert(std::is_same_v<T, double> && std::is_same_v<U, double>,
+                "the device kernels take FP64 values and geometry");
+  using FunctionSpace = fem::FunctionSpace<U>;
+
 public:
   DirichletBC(std::shared_ptr<const FunctionSpace> V, std::span<const std::int32_t> nodes,
               double value)
@@ -776,6 +872,10 @@ public:
                      (std::int32_t)dofs_host_.size(), g_.size() ? g_.data() : nullptr, g_const_,
                      x0 ? x0->data() : nullptr, alpha, nullptr));
   }
+  void set(la::Vector<T>& x, const la::Vector<T>* x0 = nullptr, T alpha = 1.0) const
+  {
+    set(x.device(), x0 ? &x0->device() : nullptr, alpha);
+  }
   const std::int32_t* device_dofs() const { return dofs_.data(); }
 
 private:
@@ -798,7 +898,9 @@ private:
   double g_const_ = 0.0;
 };
 
-using BCs = std::vector<std::shared_ptr<const DirichletBC>>;
+/// The boundary conditions of an assembly call.
+template <typename T = double, typename U = T>
+using BCs = std::vector<std::shared_ptr<const DirichletBC<T, U>>>;
 
 namespace detail
 {
@@ -808,7 +910,8 @@ struct Lifting
   device_vector<std::int8_t> markers;
   device_vector<double> g;
 };
-inline Lifting lifting_data(const FunctionSpace& V, const BCs& bcs)
+template <typename T, typename U>
+Lifting lifting_data(const FunctionSpace<U>& V, const BCs<T, U>& bcs)
 {
   Lifting l;
   std::vector<std::int8_t> mk(V.num_dofs(), 0);
@@ -824,14 +927,16 @@ inline Lifting lifting_data(const FunctionSpace& V, const BCs& bcs)
 } // namespace detail
 
 /// A zeroed matrix with the sparsity pattern of the form's space.
-inline la::MatrixCSR create_matrix(const Form& a)
+template <typename T, typename U>
+la::MatrixCSR<T> create_matrix(const Form<T, U>& a)
 {
   if (!a.interior())
-    return la::MatrixCSR(create_sparsity_pattern(a.function_space()), a.function_space().bs());
+    return la::MatrixCSR<T>(create_sparsity_pattern(a.function_space()),
+                            a.function_space().bs());
   // sparsitybuild::cells + interior_facets: the cells, each listed twice so
   // that every element has 2 nd dofs (repeats are dropped), then every
   // facet's macro element (both cells' dofs).
-  const FunctionSpace& V = a.function_space();
+  const FunctionSpace<U>& V = a.function_space();
   const int nd = V.degree() == 1 ? 4 : 10;
   const std::span<const std::int32_t> dm = V.dofmap();
   const std::vector<std::int32_t>& q = a.host_facets();
@@ -852,17 +957,18 @@ inline la::MatrixCSR create_matrix(const Form& a)
   sp.cols.resize((std::size_t)nnz);
   check(dfx_sparsity_create(V.num_nodes(), (std::int32_t)(nc + nf), 2 * nd, macro.data(),
                             sp.row_ptr.data(), sp.cols.data(), &nnz));
-  return la::MatrixCSR(sp, V.bs());
+  return la::MatrixCSR<T>(sp, V.bs());
 }
 
 /// fem::assemble_matrix (fem/assembler.h:513-602): A += the cell
 /// integrals, rows and columns of constrained dofs left out. A is not
 /// zeroed (the reference's accumulate semantics).
-inline void assemble_matrix(la::MatrixCSR& A, const Form& a, const BCs& bcs = {})
+template <typename T, typename U>
+void assemble_matrix(la::MatrixCSR<T>& A, const Form<T, U>& a, const BCs<T, U>& bcs = {})
 {
   if (!a.bilinear())
     throw Error(DFX_ERR_INVALID, "assemble_matrix needs a bilinear form");
-  const FunctionSpace& V = a.function_space();
+  const FunctionSpace<U>& V = a.function_space();
   if (A.num_rows() != V.num_nodes() || A.bs() != V.bs())
     throw Error(DFX_ERR_INVALID, "A does not match the form's space");
   std::optional<detail::Lifting> l;
@@ -884,7 +990,8 @@ inline void assemble_matrix(la::MatrixCSR& A, const Form& a, const BCs& bcs = {}
 
 /// set_diagonal (fem/assembler.h:644-686): A[d, d] = diagonal on every
 /// constrained dof.
-inline void set_diagonal(la::MatrixCSR& A, const BCs& bcs, double diagonal = 1.0)
+template <typename T, typename U>
+void set_diagonal(la::MatrixCSR<T>& A, const BCs<T, U>& bcs, T diagonal = 1.0)
 {
   const dfx_csr csr = A.csr();
   for (const auto& bc : bcs)
@@ -893,7 +1000,8 @@ inline void set_diagonal(la::MatrixCSR& A, const BCs& bcs, double diagonal = 1.0
 }
 
 /// fem::assemble_vector (fem/assembler.h:229-257): b += the cell integrals.
-inline void assemble_vector(device_vector<double>& b, const Form& L)
+template <typename T, typename U>
+void assemble_vector(device_vector<T>& b, const Form<T, U>& L)
 {
   if (L.bilinear())
     throw Error(DFX_ERR_INVALID, "assemble_vector needs a linear form");
@@ -912,7 +1020,8 @@ inline void assemble_vector(device_vector<double>& b, const Form& L)
 /// fem::assemble_scalar over the cells (fem/assembler.h:173-215): a(u, u)
 /// of a Poisson/Helmholtz form or L(u) of a source form, summed in a fixed
 /// order.
-inline double assemble_scalar(const Form& M, const device_vector<double>& u)
+template <typename T, typename U>
+T assemble_scalar(const Form<T, U>& M, const device_vector<T>& u)
 {
   if (M.on_facets())
     throw Error(DFX_ERR_UNSUPPORTED, "functionals are cell integrals");
@@ -928,12 +1037,13 @@ inline double assemble_scalar(const Form& M, const device_vector<double>& u)
 
 /// fem::apply_lifting for one bilinear form (fem/assembler.h:336-421):
 /// b -= alpha A (g - x0) over the constrained columns.
-inline void apply_lifting(device_vector<double>& b, const Form& a, const BCs& bcs,
-                          const device_vector<double>* x0 = nullptr, double alpha = 1.0)
+template <typename T, typename U>
+void apply_lifting(device_vector<T>& b, const Form<T, U>& a, const BCs<T, U>& bcs,
+                   const device_vector<T>* x0 = nullptr, T alpha = 1.0)
 {
   if (bcs.empty())
     return;
-  const FunctionSpace& V = a.function_space();
+  const FunctionSpace<U>& V = a.function_space();
   if (b.size() != (std::size_t)V.num_dofs() || (x0 && x0->size() != b.size()))
     throw Error(DFX_ERR_INVALID, "b (and x0) must have num_dofs entries");
   const detail::Lifting l = detail::lifting_data(V, bcs);
@@ -951,11 +1061,36 @@ inline void apply_lifting(device_vector<double>& b, const Form& a, const BCs& bc
 }
 
 /// fem::set_bc: DirichletBC::set for each condition.
-inline void set_bc(device_vector<double>& b, const BCs& bcs,
-                   const device_vector<double>* x0 = nullptr, double alpha = 1.0)
+template <typename T, typename U>
+void set_bc(device_vector<T>& b, const BCs<T, U>& bcs, const device_vector<T>* x0 = nullptr,
+            T alpha = 1.0)
 {
   for (const auto& bc : bcs)
     bc->set(b, x0, alpha);
+}
+
+// The same calls on la::Vector.
+template <typename T, typename U>
+void assemble_vector(la::Vector<T>& b, const Form<T, U>& L)
+{
+  assemble_vector(b.device(), L);
+}
+template <typename T, typename U>
+T assemble_scalar(const Form<T, U>& M, const la::Vector<T>& u)
+{
+  return assemble_scalar(M, u.device());
+}
+template <typename T, typename U>
+void apply_lifting(la::Vector<T>& b, const Form<T, U>& a, const BCs<T, U>& bcs,
+                   const la::Vector<T>* x0 = nullptr, T alpha = 1.0)
+{
+  apply_lifting(b.device(), a, bcs, x0 ? &x0->device() : nullptr, alpha);
+}
+template <typename T, typename U>
+void set_bc(la::Vector<T>& b, const BCs<T, U>& bcs, const la::Vector<T>* x0 = nullptr,
+            T alpha = 1.0)
+{
+  set_bc(b.device(), bcs, x0 ? &x0->device() : nullptr, alpha);
 }
 } // namespace fem
 
@@ -971,8 +1106,9 @@ struct CGResult
 /// Jacobi-preconditioned CG (the demo's CG, demo/poisson_matrix_free/
 /// main.cpp:84-132, with z = D^-1 r), FP64, stopping at |r|/|r0| < rtol.
 /// x holds the initial guess. Throws on non-convergence or breakdown.
-inline CGResult cg(const MatrixCSR& A, const device_vector<double>& b, device_vector<double>& x,
-                   double rtol = 1e-10, int max_iters = 100000)
+template <typename T>
+CGResult cg(const MatrixCSR<T>& A, const device_vector<T>& b, device_vector<T>& x,
+            double rtol = 1e-10, int max_iters = 100000)
 {
   const std::size_t n = (std::size_t)A.num_rows() * A.bs();
   if (b.size() != n || x.size() != n)
@@ -988,13 +1124,20 @@ inline CGResult cg(const MatrixCSR& A, const device_vector<double>& b, device_ve
   return {info.iterations, info.status, info.rnorm0_sq, info.rnorm_sq};
 }
 
+template <typename T>
+CGResult cg(const MatrixCSR<T>& A, const Vector<T>& b, Vector<T>& x, double rtol = 1e-10,
+            int max_iters = 100000)
+{
+  return cg(A, b.device(), x.device(), rtol, max_iters);
+}
+
 /// The solvers' sliced-ELL copy of a scalar MatrixCSR (rows sorted by
 /// length in windows of sigma rows, 32-row column-major slices): FP64, or
 /// FP32 with 16-bit column deltas. Owns the library's operator.
 class SellOperator
 {
 public:
-  SellOperator(const MatrixCSR& A, bool fp32, int sigma = 256)
+  SellOperator(const MatrixCSR<double>& A, bool fp32, int sigma = 256)
   {
     if (A.bs() != 1)
       throw Error(DFX_ERR_UNSUPPORTED, "the solver operator takes scalar (bs 1) matrices");
@@ -1013,7 +1156,7 @@ public:
   SellOperator(SellOperator&& o) noexcept : op_(std::exchange(o.op_, nullptr)), n_(o.n_) {}
 
   /// Refill the values from A (after re-assembly).
-  void update_values(const MatrixCSR& A)
+  void update_values(const MatrixCSR<double>& A)
   {
     const dfx_csr csr = A.csr();
     check(dfx_operator_update_values(op_, &csr, nullptr));
@@ -1042,7 +1185,7 @@ struct IRResult
 class IRSolver
 {
 public:
-  explicit IRSolver(const MatrixCSR& A, int sigma = 256, double inner_rtol = 0.03)
+  explicit IRSolver(const MatrixCSR<double>& A, int sigma = 256, double inner_rtol = 0.03)
       : op64_(A, false, sigma), op32_(A, true, sigma), dinv_(A.num_rows()),
         inner_rtol_(inner_rtol)
   {
@@ -1051,7 +1194,7 @@ public:
     jacobi(A);
   }
   /// Re-read the values of A (after re-assembly).
-  void refresh(const MatrixCSR& A)
+  void refresh(const MatrixCSR<double>& A)
   {
     op64_.update_values(A);
     op32_.update_values(A);
@@ -1070,9 +1213,14 @@ public:
     return {info.outer_iterations, info.inner_iterations, info.status, info.rnorm0_sq,
             info.rnorm_sq};
   }
+  IRResult solve(const Vector<double>& b, Vector<double>& x, double rtol = 1e-10,
+                 int max_outer = 200, int max_inner = 100000)
+  {
+    return solve(b.device(), x.device(), rtol, max_outer, max_inner);
+  }
 
 private:
-  void jacobi(const MatrixCSR& A)
+  void jacobi(const MatrixCSR<double>& A)
   {
     const dfx_csr csr = A.csr();
     check(dfx_jacobi_inverse_diagonal(&csr, dinv_.data(), nullptr));

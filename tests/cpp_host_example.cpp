@@ -1,7 +1,10 @@
 // A C++ host of libdfxgpu through include/dolfinx_gb300.hpp, written the
-// way a DOLFINx C++ program is: mesh::create_box, a function space, the
-// sparsity pattern, dof coordinates, exterior facets, common::Timer and
-// list_timings, and an error path that throws the reference's message.
+// way a DOLFINx C++ program is, with its class templates
+// (fem::FunctionSpace<double>, fem::Form<double>, fem::DirichletBC<double>,
+// la::MatrixCSR<double>, la::Vector<double>): mesh::create_box, a function
+// space, the sparsity pattern, dof coordinates, exterior facets,
+// common::Timer and list_timings, and an error path that throws the
+// reference's message.
 // With a GPU it also assembles and solves the Poisson problem of the
 // matrix-free demo on P1 (fem::assemble_matrix, assemble_vector,
 // apply_lifting, set_bc, CG). Without one, device work must fail loudly:
@@ -23,7 +26,7 @@ int main()
   auto m = std::make_shared<dg::mesh::Mesh>(dg::mesh::create_unit_cube(4, 4, 4));
   auto [off, adj] = dg::mesh::dual_graph(*m);
   const std::vector<std::int32_t> perm = dg::graph::reorder_rcm(off, adj);
-  auto V = std::make_shared<const dg::fem::FunctionSpace>(m, 2);
+  auto V = std::make_shared<const dg::fem::FunctionSpace<double>>(m, 2);
   const dg::fem::SparsityPattern sp = dg::fem::create_sparsity_pattern(*V);
   const std::vector<double> X = V->tabulate_dof_coordinates();
   const std::vector<std::int32_t> facets = dg::mesh::exterior_facets(*m);
@@ -71,7 +74,7 @@ int main()
   }
 
   // with a GPU: P1 Poisson, u = 0 on the boundary, f = 1, Jacobi-CG
-  auto V1 = std::make_shared<const dg::fem::FunctionSpace>(m, 1);
+  auto V1 = std::make_shared<const dg::fem::FunctionSpace<double>>(m, 1);
   std::vector<std::int32_t> bnd;
   const std::vector<double> X1 = V1->tabulate_dof_coordinates();
   for (std::int32_t i = 0; i < V1->num_nodes(); ++i)
@@ -81,13 +84,14 @@ int main()
         bnd.push_back(i);
         break;
       }
-  dg::fem::BCs bcs = {std::make_shared<const dg::fem::DirichletBC>(V1, bnd, 0.0)};
-  const dg::fem::Form a = dg::fem::Form::poisson(V1);
-  const dg::fem::Form L = dg::fem::Form::source(V1, {}, 1.0);
-  dg::la::MatrixCSR A = dg::fem::create_matrix(a);
+  dg::fem::BCs<double> bcs = {
+      std::make_shared<const dg::fem::DirichletBC<double>>(V1, bnd, 0.0)};
+  const auto a = dg::fem::Form<double>::poisson(V1);
+  const auto L = dg::fem::Form<double>::source(V1, {}, 1.0);
+  dg::la::MatrixCSR<double> A = dg::fem::create_matrix(a);
   dg::fem::assemble_matrix(A, a, bcs);
   dg::fem::set_diagonal(A, bcs);
-  dg::device_vector<double> b(V1->num_dofs()), x(V1->num_dofs());
+  dg::la::Vector<double> b(V1->num_dofs()), x(V1->num_dofs());
   dg::fem::assemble_vector(b, L);
   dg::fem::apply_lifting(b, a, bcs);
   dg::fem::set_bc(b, bcs);
@@ -95,21 +99,21 @@ int main()
   std::printf("device cg %d %d\n", r.iterations, r.status);
   // the same system by FP32-inner / FP64-outer refinement
   dg::la::IRSolver ir(A);
-  dg::device_vector<double> x2(V1->num_dofs());
+  dg::la::Vector<double> x2(V1->num_dofs());
   const dg::la::IRResult r2 = ir.solve(b, x2, 1e-10);
   std::printf("device ir %d %d %d\n", r2.inner_iterations, r2.outer_iterations, r2.status);
   // the energy a(u, u) of the solution and a Neumann term on the boundary
   std::printf("device energy %.6e\n", dg::fem::assemble_scalar(a, x));
   dg::device_vector<double> bn(V1->num_dofs());
-  dg::fem::assemble_vector(bn, dg::fem::Form::facet_source(V1, {}, 1.0));
+  dg::fem::assemble_vector(bn, dg::fem::Form<double>::facet_source(V1, {}, 1.0));
   double area = 0.0; // sum_i int_F phi_i ds = the boundary's area, 6
   for (double v : bn.to_host())
     area += v;
   std::printf("device boundary_area %.12f\n", area);
   // interior facets: the penalty matrix on its macro-element pattern, and a
   // linear function's gradient does not jump, so A_penalty u = 0 for u = x
-  const dg::fem::Form jp = dg::fem::Form::interior_penalty(V1, {}, 1.0);
-  dg::la::MatrixCSR P = dg::fem::create_matrix(jp);
+  const auto jp = dg::fem::Form<double>::interior_penalty(V1, {}, 1.0);
+  dg::la::MatrixCSR<double> P = dg::fem::create_matrix(jp);
   dg::fem::assemble_matrix(P, jp);
   std::vector<double> ux(V1->num_nodes());
   for (std::int32_t i = 0; i < V1->num_nodes(); ++i)
