@@ -419,14 +419,18 @@ def elasticity_sample(steps=1, warmup=1):
     A = masm.assemble()
     S = A.expand_blocks()
     b = rhs.assemble()
-    fp64 = la.OperatorCGSolver(S)
+    # Both paths use the window sigma the autotuner picks for this matrix.
+    from dolfinx_gb300 import autotune
+
+    sigma = autotune.tune_sigma(S)["sigma"]
+    fp64 = la.OperatorCGSolver(S, sigma=sigma)
     # FP32 arithmetic cannot carry this system: its FP32 PCG loses accuracy at
     # the level of the smallest eigenvalue, and FP32 corrections inside FP64
     # refinement (reliable updates, or flexible CG) stall or need hundreds of
     # thousands of FP32 iterations. The matrix is therefore applied as two
     # FP32 words per value on the FP32 pipe (error-free products): the FP64
     # SpMV of this system is bound by the FP64 pipe, not by HBM.
-    ir = la.OperatorCGSolver(S, split=True)
+    ir = la.OperatorCGSolver(S, split=True, sigma=sigma)
     x = torch.zeros_like(b)
     stream = torch.cuda.current_stream()
 
@@ -439,7 +443,7 @@ def elasticity_sample(steps=1, warmup=1):
         return solver.solve(b, x, rtol=STEP_RTOL, raise_on_fail=False)
 
     out = {"workload": "vector P2 elasticity, box 4x1x1, 96x24x24x6 tets", "cells": m.num_cells,
-           "dofs": V.num_dofs, "blocks": A.nnz, "scalar_nnz": S.nnz}
+           "dofs": V.num_dofs, "blocks": A.nnz, "scalar_nnz": S.nnz, "sigma": sigma}
     for name, solver in (("fp64_plain", fp64), ("mixed", ir)):
         for _ in range(warmup):
             step_raw(solver)

@@ -29,7 +29,7 @@ import torch
 
 from . import _capi, la
 
-SIGMA_CANDIDATES = (64, 256, 1024)
+SIGMA_CANDIDATES = (64, 256, 1024, 2048, 4096)
 CACHE_FORMAT = "dfx-tuning"
 CACHE_VERSION = 1
 
