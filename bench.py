@@ -87,7 +87,11 @@ def parse():
     p.add_argument("--profile-step", action="store_true",
                    help="run one mixed-precision P2 Poisson step only (for an ncu launch list)")
     p.add_argument("--profile", action="store_true",
-                   help="profiling target: a few launches of every hot kernel, no timing")
+                   help="profiling target: a few launches of every hot kernel, no timing "
+                        "and no autotuning")
+    p.add_argument("--profile-sigma", type=int, default=4096,
+                   help="--profile: window sigma of the solver operators (the autotuner's "
+                        "choice at P2 64^3)")
     p.add_argument("--accuracy-trials", type=int, default=0, metavar="N",
                    help="N last-bit perturbations of the P2 Poisson matrix: iterations and "
                         "errors of both paths at several stopping tolerances")
@@ -129,7 +133,7 @@ class Problem:
     mixed-precision path (FP32 inner PCG inside FP64 refinement)."""
 
     def __init__(self, m, kappa, f, mode="atomic", inner_rtol=None, variant="reliable",
-                 tune=True):
+                 tune=True, sigma=256):
         import numpy as np
         import torch
 
@@ -156,7 +160,6 @@ class Problem:
         from dolfinx_gb300 import autotune
 
         self.tuning = {}
-        sigma = 256
         if tune:
             self.tuning["assembly"] = autotune.tune_assembly(self.masm)
             self.tuning["sigma"] = autotune.tune_sigma(self.A)
@@ -1054,14 +1057,16 @@ def run_ours(args):
 
 
 def run_profile(args):
-    """A short run for ncu: one assembly, two launches of each operator's
+    """A short run for ncu: two assemblies, two launches of each operator's
     SpMV, and a mixed-precision solve stopped at rtol 1e-3 (a few dozen
-    iterations of the fused CG kernels)."""
+    iterations of the CG kernels). No autotuning: the launch shapes are the
+    defaults (32 cells per block) and --profile-sigma."""
     import torch
 
     torch.cuda.set_device(0)
     m, kappa, f = make_inputs(args.n, seed=0)
-    P = Problem(m, kappa, f, mode=args.mode, inner_rtol=args.inner_rtol, variant=args.ir_variant)
+    P = Problem(m, kappa, f, mode=args.mode, inner_rtol=args.inner_rtol, variant=args.ir_variant,
+                tune=False, sigma=args.profile_sigma)
     P.assemble()
     P.ir.refresh()
     n = P.A.nrows
