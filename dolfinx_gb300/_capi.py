@@ -206,6 +206,9 @@ _SIGS = {
     "dfx_operator_device_bytes": (C.c_int, [_P, C.POINTER(C.c_size_t)]),
     "dfx_operator_release_values": (C.c_int, [_P]),
     "dfx_operator_share": (C.c_int, [_P, C.POINTER(C.c_void_p)]),
+    "dfx_operator_share_async": (C.c_int, [_P, C.c_void_p, C.POINTER(C.c_void_p)]),
+    "dfx_operator_destroy_async": (C.c_int, [_P, C.c_void_p]),
+    "dfx_operator_pool_trim": (C.c_int, []),
     "dfx_operator_permute": (C.c_int, [_P, _P, _P, C.c_int32, _P]),
     "dfx_batch_workspace_bytes": (C.c_size_t, [C.c_int64, C.c_int32]),
     "dfx_batch_create": (C.c_int, [C.c_int32, C.POINTER(C.c_void_p)]),

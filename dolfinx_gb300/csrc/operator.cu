@@ -6,6 +6,8 @@
 
 #include <algorithm>
 #include <atomic>
+#include <cstdint>
+#include <mutex>
 #include <numeric>
 #include <type_traits>
 #include <thread>
@@ -113,6 +115,35 @@ __global__ void k_permute(const T* __restrict__ in, T* __restrict__ out,
     out[i] = in[idx[i]];
 }
 
+// A stream-ordered memory pool per device for the values of operator
+// shares (one set per request in a server): shares are made and dropped at
+// the request rate, and a cudaFree waits for the whole device. The pool
+// keeps freed memory for reuse (release threshold: no limit) until
+// dfx_operator_pool_trim.
+std::mutex g_pool_mutex;
+cudaMemPool_t g_pools[64] = {};
+
+int share_pool(int dev, cudaMemPool_t* out)
+{
+  DFX_REQUIRE(dev >= 0 && dev < 64, "device index %d out of range", dev);
+  std::lock_guard<std::mutex> lk(g_pool_mutex);
+  if (!g_pools[dev])
+  {
+    cudaMemPoolProps props{};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.handleTypes = cudaMemHandleTypeNone;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = dev;
+    cudaMemPool_t pool = nullptr;
+    DFX_CUDA(cudaMemPoolCreate(&pool, &props));
+    uint64_t keep = UINT64_MAX;
+    DFX_CUDA(cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    g_pools[dev] = pool;
+  }
+  *out = g_pools[dev];
+  return DFX_OK;
+}
+
 void free_op(dfx_operator_s* op)
 {
   if (!op)
@@ -120,6 +151,17 @@ void free_op(dfx_operator_s* op)
   int cur = 0;
   cudaGetDevice(&cur);
   cudaSetDevice(op->device);
+  if (op->pooled)
+  {
+    // No stream is known here: wait for the device, then return the values
+    // to the pool (the synchronous cudaFree semantics).
+    cudaDeviceSynchronize();
+    for (void* p : {op->vals, op->tmp})
+      if (p)
+        cudaFreeAsync(p, 0);
+    cudaStreamSynchronize(0);
+    op->vals = op->tmp = nullptr;
+  }
   if (op->owns_structure)
   {
     for (void* p : {(void*)op->perm, (void*)op->iperm, (void*)op->slice_ptr, (void*)op->cols,
@@ -707,6 +749,82 @@ extern "C" int dfx_operator_share(dfx_operator src, dfx_operator* out)
   }
   src->shares += 1;
   *out = op;
+  return DFX_OK;
+}
+
+extern "C" int dfx_operator_share_async(dfx_operator src, void* stream, dfx_operator* out)
+{
+  DFX_REQUIRE(src && out, "arguments must be non-NULL");
+  DFX_REQUIRE(src->owns_structure, "share the source operator, not a share");
+  *out = nullptr;
+  cudaMemPool_t pool = nullptr;
+  if (int st = share_pool(src->device, &pool))
+    return st;
+  cudaStream_t s = dfx::as_stream(stream);
+  auto* op = new dfx_operator_s(*src);
+  op->serial = dfx::next_operator_serial();
+  op->owns_structure = 0;
+  op->shares = 0;
+  op->source = src;
+  op->pooled = 1;
+  op->vals = nullptr;
+  op->tmp = nullptr;
+  if (cudaMallocFromPoolAsync(&op->vals, dfx::value_bytes(*op), pool, s) != cudaSuccess
+      || cudaMallocFromPoolAsync(&op->tmp, dfx::scratch_bytes(*op), pool, s) != cudaSuccess)
+  {
+    if (op->vals)
+      cudaFreeAsync(op->vals, s);
+    delete op;
+    return dfx::no_memory("operator values");
+  }
+  src->shares += 1;
+  *out = op;
+  return DFX_OK;
+}
+
+extern "C" int dfx_operator_destroy_async(dfx_operator op, void* stream)
+{
+  if (!op)
+    return DFX_OK;
+  if (op->shares > 0)
+    return dfx::fail(DFX_ERR_INVALID, "operator structure is still shared by %d operators",
+                     op->shares);
+  if (!op->pooled)
+  {
+    free_op(op);
+    return DFX_OK;
+  }
+  cudaStream_t s = dfx::as_stream(stream);
+  int cur = 0;
+  cudaGetDevice(&cur);
+  cudaSetDevice(op->device);
+  for (void* p : {op->vals, op->tmp})
+    if (p)
+      cudaFreeAsync(p, s);
+  cudaSetDevice(cur);
+  if (op->source)
+    op->source->shares -= 1;
+  delete op;
+  return DFX_OK;
+}
+
+extern "C" int dfx_operator_pool_trim(void)
+{
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess)
+  {
+    (void)cudaGetLastError();
+    return DFX_OK; // no device: no pool
+  }
+  cudaMemPool_t pool = nullptr;
+  {
+    std::lock_guard<std::mutex> lk(g_pool_mutex);
+    if (dev < 0 || dev >= 64 || !g_pools[dev])
+      return DFX_OK;
+    pool = g_pools[dev];
+  }
+  DFX_CUDA(cudaDeviceSynchronize());
+  DFX_CUDA(cudaMemPoolTrimTo(pool, 0));
   return DFX_OK;
 }
 

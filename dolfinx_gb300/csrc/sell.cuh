@@ -53,6 +53,9 @@ struct dfx_operator_s
   // loads of one chunk are in flight together (autotuned; 4 by default).
   int32_t chunk = 4;
   int32_t owns_structure = 1;
+  // Values and scratch come from the library's stream-ordered pool
+  // (dfx_operator_share_async) and go back to it in stream order.
+  int32_t pooled = 0;
   int32_t shares = 0;
   dfx_operator_s* source = nullptr;
 };

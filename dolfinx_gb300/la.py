@@ -232,9 +232,14 @@ class SellOperator:
 
     def __init__(self, A: MatrixCSR, dtype=torch.float64, sigma: int = 256,
                  compress_cols: bool | None = None, share_of: "SellOperator | None" = None,
-                 build: int = 0, split: bool = False):
+                 build: int = 0, split: bool = False, pool_stream=None):
         """build: where the structure is built (0 device with host fallback,
-        1 device only, 2 host); every place gives the same operator."""
+        1 device only, 2 host); every place gives the same operator.
+        pool_stream (shares only): take the values from the library's
+        stream-ordered pool in the order of this torch stream, and return them
+        there when the share is dropped -- for servers that make and drop a
+        share per request, where cudaMalloc / cudaFree would wait for the
+        whole device. Drop such a share only after its last use."""
         self.A, self.dtype, self.sigma = A, dtype, sigma
         self.csr_nnz = A.nnz if A is not None else share_of.csr_nnz
         self.split = bool(split)
@@ -246,7 +251,12 @@ class SellOperator:
             self.dtype, self.sigma, self.compressed = share_of.dtype, share_of.sigma, share_of.compressed
             self.split = share_of.split
             self.n, self.device = share_of.n, share_of.device
-            _capi.check(_capi.lib().dfx_operator_share(share_of.handle, C.byref(h)))
+            if pool_stream is not None:
+                self._pool_stream = pool_stream
+                _capi.check(_capi.lib().dfx_operator_share_async(
+                    share_of.handle, C.c_void_p(pool_stream.cuda_stream), C.byref(h)))
+            else:
+                _capi.check(_capi.lib().dfx_operator_share(share_of.handle, C.byref(h)))
             self.source = share_of
             self.handle = h
             if A is not None:
@@ -264,9 +274,10 @@ class SellOperator:
         self.handle = h
         self.compressed = bool(compress_cols)
 
-    def share(self, A: MatrixCSR) -> "SellOperator":
-        """An operator with this structure and the values of A."""
-        return SellOperator(A, share_of=self)
+    def share(self, A: MatrixCSR, pool_stream=None) -> "SellOperator":
+        """An operator with this structure and the values of A (pool_stream:
+        see __init__)."""
+        return SellOperator(A, share_of=self, pool_stream=pool_stream)
 
     def to_operator(self, v: torch.Tensor, out: torch.Tensor | None = None) -> torch.Tensor:
         """v in the operator's (renumbered) numbering."""
@@ -339,7 +350,11 @@ class SellOperator:
         h = getattr(self, "handle", None)
         if h is not None and h.value and _capi is not None:
             try:
-                _capi.lib().dfx_operator_destroy(h)
+                ps = getattr(self, "_pool_stream", None)
+                if ps is not None:
+                    _capi.lib().dfx_operator_destroy_async(h, C.c_void_p(ps.cuda_stream))
+                else:
+                    _capi.lib().dfx_operator_destroy(h)
             except Exception:
                 pass
             self.handle = None

@@ -281,8 +281,10 @@ class Job:
                 _stream_ptr(stream)))
             self.b = fem.RhsAssembler(L, a, [st.bc], mode=assembly).assemble()
             self.dinv = self.A.inverse_diagonal()
-            self.op64 = st.op64.share(self.A)
-            self.op32 = st.op32.share(self.A) if mode == "mixed" else None
+            # Shares from the library's stream-ordered pool: dropping one at
+            # the end of the request does not wait for the whole device.
+            self.op64 = st.op64.share(self.A, pool_stream=stream)
+            self.op32 = st.op32.share(self.A, pool_stream=stream) if mode == "mixed" else None
             self.bp = self.op64.to_operator(self.b)
             self.dp = self.op64.to_operator(self.dinv)
             self.xp = torch.zeros_like(self.bp)
@@ -374,6 +376,7 @@ class Server:
                 # the library's own allocations can use them.
                 gc.collect()
                 torch.cuda.empty_cache()
+                _capi.check(_capi.lib().dfx_operator_pool_trim())
                 _log.logger.info("structure n=%s P%s evicted", key[0], key[1])
 
     def prewarm(self, requests):
@@ -595,6 +598,7 @@ class Server:
         self.used = 0
         gc.collect()
         torch.cuda.empty_cache()
+        _capi.check(_capi.lib().dfx_operator_pool_trim())
 
 
 def serve(requests, mode="mixed", max_wall_s: float = 600.0, **kw) -> tuple[dict, list[Job]]:

@@ -642,6 +642,18 @@ int dfx_ir_solve(dfx_operator op64, dfx_operator op32, const double* d_b, double
  * src's and whose values are its own: one structure per mesh, one set of
  * values per request. src must outlive its shares. */
 int dfx_operator_share(dfx_operator src, dfx_operator* out);
+/* dfx_operator_share with the values and scratch taken, in the order of
+ * `stream`, from a stream-ordered pool the library keeps per device (no
+ * reference counterpart). For servers that make and drop a share per
+ * request: cudaMalloc and cudaFree would wait for the whole device each
+ * time. Drop such a share with dfx_operator_destroy_async on a stream
+ * ordered after every use of it (dfx_operator_destroy works too, but waits
+ * for the device). Freed memory stays in the pool for the next shares until
+ * dfx_operator_pool_trim. */
+int dfx_operator_share_async(dfx_operator src, void* stream, dfx_operator* out);
+int dfx_operator_destroy_async(dfx_operator op, void* stream);
+/* Return the pool's unused memory to the device (waits for the device). */
+int dfx_operator_pool_trim(void);
 /* to_operator != 0: out[i] = in[perm[i]] (into the operator's numbering);
  * otherwise out[perm[i]] = in[i] (back to the original numbering). */
 int dfx_operator_permute(dfx_operator op, const double* d_in, double* d_out,

@@ -372,6 +372,29 @@ def test_fused_update_matches_four_kernel_iteration(cuda, oracle, capi, n):
     _fused_vs_unfused(capi, A, b, residual)
 
 
+def test_pooled_operator_shares(cuda, oracle, capi):
+    """Shares whose values come from the library's stream-ordered pool give
+    the same products as plain shares; dropping them (in stream order) and
+    making new ones reuses the pool, and trimming returns its memory."""
+    from dolfinx_gb300 import la
+
+    A, b, rp, cols = _poisson_system(oracle, (6, 5, 4), 2, 41)
+    for dtype in (torch.float64, torch.float32):
+        op = la.SellOperator(A, dtype, 256)
+        x = torch.from_numpy(np.random.default_rng(2).standard_normal(A.nrows)).to(
+            device="cuda", dtype=dtype)
+        ref = op.share(A).apply(x)
+        s = torch.cuda.Stream()
+        for _ in range(3):
+            with torch.cuda.stream(s):
+                sh = op.share(A, pool_stream=s)
+                y = sh.apply(x)
+            s.synchronize()
+            assert torch.equal(y, ref)
+            del sh
+        capi.check(capi.lib().dfx_operator_pool_trim())
+
+
 def test_grid_barrier_wait_is_bounded(cuda, capi):
     """The grid barrier of the fused update gives up instead of hanging: with
     an arrival missing, both blocks of the self-test report DFX_ERR_TIMEOUT
