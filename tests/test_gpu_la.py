@@ -328,7 +328,7 @@ def test_iterative_refinement_reaches_fp64(cuda, oracle, capi, variant, inner_rt
     assert rel < 1e-10, rel
 
 
-def _fused_vs_unfused(capi, A, b, residual):
+def _fused_vs_unfused(capi, A, b, residual, jacobi=True, variant="reliable"):
     """IR solves of A x = b with the fused FP32 update on and off."""
     from dolfinx_gb300 import la
 
@@ -340,7 +340,7 @@ def _fused_vs_unfused(capi, A, b, residual):
             on = C.c_int32(-1)
             capi.check(L.dfx_get_cg_fused_update(C.byref(on)))
             assert on.value == fused
-            ir = la.IRSolver(A, jacobi=True)
+            ir = la.IRSolver(A, jacobi=jacobi, variant=variant)
             x = torch.zeros_like(b)
             r = ir.solve(b, x, rtol=1e-11)
             assert r.status == 0
@@ -355,13 +355,18 @@ def _fused_vs_unfused(capi, A, b, residual):
     assert r1.kernel_launches < r0.kernel_launches
 
 
-@pytest.mark.parametrize("n", [(12, 12, 12), (23, 21, 19)])
-def test_fused_update_matches_four_kernel_iteration(cuda, oracle, capi, n):
+@pytest.mark.parametrize("n,jacobi,variant", [((12, 12, 12), True, "reliable"),
+                                               ((23, 21, 19), True, "reliable"),
+                                               ((12, 12, 12), False, "reliable"),
+                                               ((12, 12, 12), True, "restart")])
+def test_fused_update_matches_four_kernel_iteration(cuda, oracle, capi, n, jacobi, variant):
     """The two-kernel FP32 inner iteration (SpMV + one cooperative kernel
     with grid-wide barriers) and the four-kernel one run the same
     recurrence: both meet the FP64 stopping test in the oracle's SpMV, with
     inner iteration counts within 1 % and solutions within the accuracy the
-    solves carry. (23, 21, 19) P2 has a ragged tail (n % 4 = 3)."""
+    solves carry. (23, 21, 19) P2 has a ragged tail (n % 4 = 3); the cases
+    without Jacobi and with restarted refinement take the kernel's other
+    instantiations."""
     A, b, rp, cols = _poisson_system(oracle, n, 2, 33)
     bh = b.cpu().numpy()
 
@@ -369,7 +374,7 @@ def test_fused_update_matches_four_kernel_iteration(cuda, oracle, capi, n):
         res = bh - oracle.spmv(rp, cols, A.vals.cpu().numpy(), x.cpu().numpy())
         return np.linalg.norm(res) / np.linalg.norm(bh)
 
-    _fused_vs_unfused(capi, A, b, residual)
+    _fused_vs_unfused(capi, A, b, residual, jacobi=jacobi, variant=variant)
 
 
 def test_pooled_operator_shares(cuda, oracle, capi):
