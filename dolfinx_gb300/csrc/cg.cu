@@ -956,7 +956,8 @@ __device__ __forceinline__ double fused_block_sum_f32(float v, double* sh)
 }
 
 // Sums of two rows of block partials (gridDim.x values each) in index
-// order, the same in every block; every thread receives both.
+// order, the same in every block; every thread receives both. Blocks of at
+// most 512 threads (16 warps: sh holds 32 values).
 __device__ __forceinline__ void fused_grid_total2(const double* p0, const double* p1,
                                                   double* sh, double* bc, double& t0,
                                                   double& t1)
