@@ -80,7 +80,7 @@ def test_bench_defaults_and_host_helpers(monkeypatch):
     assert cfg["parallelism"] == "single"
     peak, kind = bench.measured_peaks()
     assert peak > 0 and kind in ("measured", "fallback")
-    assert bench.profile_traffic("sell_f32_p2_64") == 418223104
+    assert bench.profile_traffic("sell_f32_p2_64") == 399360512
     assert bench.profile_traffic("no such kernel") is None
 
 
