@@ -38,11 +38,11 @@ UNIT = "GDoF/s"
 # speed-up is stated at: the mixed solution within 1e-10 (relative) of the
 # plain FP64 solution. Measured over 12 last-bit perturbations of the 64^3
 # matrix (bench.py --accuracy-trials 12): at rtol 2.5e-11 the two solutions
-# differ by 1.05-1.15e-10 (none within the bound; another set of trials had
-# one at 3.1e-10, whose FP32 inner solve stopped ~75 iterations early); at
-# 1e-11 by 3.5-4.3e-11; at 5e-12 by 1.9-2.1e-11, a margin of four against
-# such early stops. Both solutions and their distance are measured every run
-# (and against an FP64 solve to rtol 1e-13) and printed in the config block.
+# differ by 1.01-2.10e-10 (none within the bound; the worst trial's FP32
+# inner solve stopped ~110 iterations early); at 1e-11 by 3.4e-11 - 1.3e-10
+# (one early stop); at 5e-12 by 2.0-2.3e-11, a margin of four. Both
+# solutions and their distance are measured every run (and against an FP64
+# solve to rtol 1e-13) and printed in the config block.
 STEP_RTOL = 5e-12
 # Serving requests (Poisson/Helmholtz, P1/P2, n in [8, 96]) stop at 2e-12:
 # over the 64-request sample at 5e-12 one whole-GPU request (n = 95, P1)
