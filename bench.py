@@ -83,7 +83,10 @@ def parse():
                    help="apply the tensor-core Q4 action only (ncu capture of k_q4_cells_tc)")
     p.add_argument("--profile-split", type=int, default=0, metavar="NY",
                    help="elasticity on a 4NY x NY x NY box: apply the FP64 and the split "
-                        "FP32-word operators twice each (ncu capture of k_sell_spmv_split)")
+                        "3x3-block operators twice each (ncu capture of k_bsell_spmv3)")
+    p.add_argument("--profile-solve", action="store_true",
+                   help="with --profile-split: then solve the clamped system twice by PCG on "
+                        "the split 3x3-block operator (an ncu launch list of its iteration)")
     p.add_argument("--profile-step", action="store_true",
                    help="run one mixed-precision P2 Poisson step only (for an ncu launch list)")
     p.add_argument("--profile", action="store_true",
@@ -401,10 +404,10 @@ def elasticity_sample(steps=1, warmup=1):
     """Linear elasticity, vector P2 on [0,4]x[0,1]^2 split into 96x24x24
     hexahedra x 6 tetrahedra (331,776 cells, 1,390,179 dofs), E lognormal
     (log 1e3, 0.5) per cell, nu = 0.3, body force (0,0,-1), clamped at x = 0.
-    Block (3x3) CSR assembly, expansion to the scalar CSR, then plain FP64
-    Jacobi-PCG and the same PCG on the split operator (two FP32 words per
-    value, FP32-pipe products), both to the step's relative residual
-    evaluated in FP64."""
+    Block (3x3) CSR assembly, then plain FP64 Jacobi-PCG on the FP64 3x3-block
+    operator and the same PCG on the split 3x3-block operator (two FP32
+    words per value, FP32-pipe products), both to the step's relative
+    residual evaluated in FP64."""
     import numpy as np
     import torch
 
@@ -420,33 +423,34 @@ def elasticity_sample(steps=1, warmup=1):
     masm = fem.MatrixAssembler(a, [bc])
     rhs = fem.RhsAssembler(fem.body_force_form(V, (0.0, 0.0, -1.0)), a, [bc])
     A = masm.assemble()
-    S = A.expand_blocks()
     b = rhs.assemble()
     # Both paths use the window sigma the autotuner picks for this matrix.
     from dolfinx_gb300 import autotune
 
-    sigma = autotune.tune_sigma(S)["sigma"]
-    fp64 = la.OperatorCGSolver(S, sigma=sigma)
+    sigma = autotune.tune_sigma(A)["sigma"]
+    # 3x3-block operators (one column index per block) of the block CSR:
+    # no scalar expansion in the step.
+    fp64 = la.OperatorCGSolver(A, sigma=sigma)
     # FP32 arithmetic cannot carry this system: its FP32 PCG loses accuracy at
     # the level of the smallest eigenvalue, and FP32 corrections inside FP64
     # refinement (reliable updates, or flexible CG) stall or need hundreds of
     # thousands of FP32 iterations. The matrix is therefore applied as two
     # FP32 words per value on the FP32 pipe (error-free products): the FP64
     # SpMV of this system is bound by the FP64 pipe, not by HBM.
-    ir = la.OperatorCGSolver(S, split=True, sigma=sigma)
+    ir = la.OperatorCGSolver(A, split=True, sigma=sigma)
     x = torch.zeros_like(b)
     stream = torch.cuda.current_stream()
 
     def step_raw(solver):
         masm.assemble(zero=True)
-        A.expand_blocks(out=S)
         rhs.assemble(b)
         solver.refresh()
         x.zero_()
         return solver.solve(b, x, rtol=STEP_RTOL, raise_on_fail=False)
 
     out = {"workload": "vector P2 elasticity, box 4x1x1, 96x24x24x6 tets", "cells": m.num_cells,
-           "dofs": V.num_dofs, "blocks": A.nnz, "scalar_nnz": S.nnz, "sigma": sigma}
+           "dofs": V.num_dofs, "blocks": A.nnz, "scalar_nnz": 9 * A.nnz, "sigma": sigma,
+           "operator": "3x3-block sliced ELL, sigma in block rows"}
     for name, solver in (("fp64_plain", fp64), ("mixed", ir)):
         for _ in range(warmup):
             step_raw(solver)
@@ -456,8 +460,9 @@ def elasticity_sample(steps=1, warmup=1):
                      "iterations": [q.iterations for q in res], "status": r.status,
                      "final_rel_residual": float(np.sqrt(r.rnorm_sq / r.rnorm0_sq))}
         if name == "mixed":
-            out[name]["variant"] = ("FP64 Jacobi-PCG; matrix as two FP32 words per value, "
-                                    "FP32-pipe products with error-free transformations")
+            out[name]["variant"] = ("FP64 Jacobi-PCG; matrix as two FP32 words per value "
+                                    "(3x3 blocks), FP32-pipe products with error-free "
+                                    "transformations")
         if name == "fp64_plain":
             x64 = x.clone()
     out["rel_err_vs_fp64_solution"] = float((x - x64).norm() / x64.norm())
@@ -476,7 +481,7 @@ def elasticity_sample(steps=1, warmup=1):
                    "useful cost; the mixed path keeps FP64 vectors and forms the products on "
                    "the FP32 pipe from two FP32 words per value")
     # The two SpMVs alone (renumbered vectors), L2 flushed by the 933 MB of values.
-    xr = torch.rand(S.nrows, dtype=torch.float64, device="cuda")
+    xr = torch.rand(fp64.n, dtype=torch.float64, device="cuda")
     yr = torch.empty_like(xr)
     out["spmv_ms"] = {"fp64": _kernel_ms(lambda: fp64.op.apply_renumbered(xr, yr), 10, stream),
                       "split_fp32_words": _kernel_ms(lambda: ir.op.apply_renumbered(xr, yr), 10,
@@ -1153,9 +1158,9 @@ def run_profile_q4_tc(args):
 
 
 def run_profile_split(args):
-    """Vector P2 elasticity on [0,4]x[0,1]^2 with 4NY x NY x NY hexahedra x 6,
-    expanded to the scalar CSR; the FP64 and the split operators applied
-    twice each: the run behind an ncu capture of k_sell_spmv_split."""
+    """Vector P2 elasticity on [0,4]x[0,1]^2 with 4NY x NY x NY hexahedra x 6;
+    the FP64 and the split 3x3-block operators (sigma 4096 block rows)
+    applied twice each: the run behind an ncu capture of k_bsell_spmv3."""
     import numpy as np
     import torch
 
@@ -1166,17 +1171,31 @@ def run_profile_split(args):
     m = mesh.create_box(((0.0, 0.0, 0.0), (4.0, 1.0, 1.0)), (4 * ny, ny, ny))
     V = fem.functionspace(m, ("Lagrange", 2, (3,)))
     E = np.exp(np.random.default_rng(3).normal(np.log(1e3), 0.5, m.num_cells))
-    S = fem.assemble_matrix(fem.elasticity_form(V, torch.from_numpy(E).cuda(), 0.3)).expand_blocks()
-    o64 = la.SellOperator(S, torch.float64, 1024)
-    osp = la.SellOperator(S, torch.float64, 1024, split=True)
-    x = torch.rand(S.nrows, dtype=torch.float64, device="cuda")
+    A = fem.assemble_matrix(fem.elasticity_form(V, torch.from_numpy(E).cuda(), 0.3))
+    o64 = la.SellOperator(A, torch.float64, 4096)
+    osp = la.SellOperator(A, torch.float64, 4096, split=True)
+    x = torch.rand(o64.n, dtype=torch.float64, device="cuda")
     y = torch.empty_like(x)
     for _ in range(2):
         o64.apply_renumbered(x, y)
         osp.apply_renumbered(x, y)
     torch.cuda.synchronize()
-    print(json.dumps({"profile_split": "ok", "rows": S.nrows, "nnz": S.nnz,
-                      "slots": osp.info()["slots"]}))
+    out = {"profile_split": "ok", "rows": o64.n, "blocks": A.nnz, "slots": osp.info()["slots"]}
+    if args.profile_solve:
+        # the c3 system at NY = 24: clamped at x = 0, body force (0, 0, -1)
+        X = V.tabulate_dof_coordinates()
+        bc = fem.dirichletbc(np.zeros(3), np.flatnonzero(np.isclose(X[:, 0], 0.0)).astype(np.int32),
+                             V)
+        a = fem.elasticity_form(V, torch.from_numpy(E).cuda(), 0.3)
+        Ac = fem.MatrixAssembler(a, [bc]).assemble()
+        b = fem.RhsAssembler(fem.body_force_form(V, (0.0, 0.0, -1.0)), a, [bc]).assemble()
+        sol = la.OperatorCGSolver(Ac, split=True, sigma=4096)
+        for _ in range(2):
+            x = torch.zeros_like(b)
+            r = sol.solve(b, x, rtol=STEP_RTOL, raise_on_fail=False)
+        torch.cuda.synchronize()
+        out.update(iterations=r.iterations, status=r.status)
+    print(json.dumps(out))
 
 
 def accuracy_trials(args):

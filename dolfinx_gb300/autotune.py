@@ -141,13 +141,25 @@ def tune_sigma(A: la.MatrixCSR, candidates=SIGMA_CANDIDATES, reps: int = 10,
     the candidate with the least FP32 + FP64 SpMV time. Both operators of a
     mixed-precision solve must share one sigma, so one value is picked. The
     choice is recorded for matrices of A's shape. reuse: when a sigma is
-    already recorded for the shape, return it without timing."""
+    already recorded for the shape, return it without timing. A 3x3-block
+    matrix (bs 3) has no FP32 operator: its split and FP64 block operators
+    are timed instead, sigma counted in block rows."""
     if reuse:
         v = recorded_sigma(A)
         if v is not None:
             return {"sigma": v, "candidates": None, "recorded": True}
-    n = A.nrows
+    n = A.nrows * A.bs
     res = {}
+    if A.bs == 3:
+        for sg in candidates:
+            osp = la.SellOperator(A, torch.float64, sg, split=True)
+            o64 = la.SellOperator(A, torch.float64, sg)
+            res[sg] = {"split_ms": _op_ms(osp, torch.float64, n, reps),
+                       "f64_ms": _op_ms(o64, torch.float64, n, reps)}
+            del osp, o64
+        best = min(res, key=lambda sg: res[sg]["split_ms"] + res[sg]["f64_ms"])
+        _sigma_choices[(_device_index(A.vals), int(A.nrows), int(A.nnz))] = best
+        return {"sigma": best, "candidates": res}
     for sg in candidates:
         o32 = la.SellOperator(A, torch.float32, sg, compress_cols=True)
         o64 = la.SellOperator(A, torch.float64, sg)

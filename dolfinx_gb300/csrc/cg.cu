@@ -616,6 +616,41 @@ __global__ void __launch_bounds__(kSellThreads, 12)
   finish_pap(publish<double>(dot, 0.0, w.red, &w.st->ticket[1], false), w.st);
 }
 
+// y = A p, p.y -- 3x3-block operator (bs 3, lane = block row): FP64
+// values, or split values on the FP32 words of p.
+template <bool SPLIT>
+__global__ void __launch_bounds__(kSellThreads, 8)
+    k_spmv_dot_bsell3(const dfx_operator_s op, Work<double> w)
+{
+  block_reduce_init();
+
+  if (is_done(w.st))
+    return;
+  const int lane = threadIdx.x & 31;
+  const dfx::SliceRange sr = dfx::block_slices(op.nslices);
+  double dot = 0;
+  for (int32_t s = sr.begin; s < sr.end; s += sr.step)
+  {
+    double acc[3];
+    if constexpr (SPLIT)
+      dfx::bsell_row3_split(op, (const float2*)op.vals, reinterpret_cast<const float2*>(w.ph),
+                            s, lane, acc);
+    else
+      dfx::bsell_row3(op, (const double*)op.vals, w.p, s, lane, acc);
+    const int32_t row = 3 * (32 * s + lane);
+    if (row < op.n)
+    {
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+      {
+        w.y[row + r] = acc[r];
+        dot += acc[r] * w.p[row + r];
+      }
+    }
+  }
+  finish_pap(publish<double>(dot, 0.0, w.red, &w.st->ticket[1], false), w.st);
+}
+
 // 16-byte vectors of the elementwise kernels.
 template <typename T>
 struct Vec16;
@@ -1720,7 +1755,15 @@ void enqueue_spmv_dot<double>(const OpRef& o, const Work<double>& w, cudaStream_
   const int blocks = stride_grid();
   if (o.kind == kSell)
   {
-    if (o.op->dtype == DFX_F32X2)
+    if (o.op->bs == 3)
+    {
+      const unsigned g = (unsigned)dfx::sell_grid(o.op->nslices);
+      if (o.op->dtype == DFX_F32X2)
+        k_spmv_dot_bsell3<true><<<g, kSellThreads, 0, s>>>(*o.op, w);
+      else
+        k_spmv_dot_bsell3<false><<<g, kSellThreads, 0, s>>>(*o.op, w);
+    }
+    else if (o.op->dtype == DFX_F32X2)
     {
       if (o.op->compressed)
         k_spmv_dot_sell_split<true><<<sell_blocks(o.op->n), kSellThreads, 0, s>>>(*o.op, w);
@@ -2271,6 +2314,7 @@ extern "C" int dfx_ir_solve(dfx_operator op64, dfx_operator op32, const double* 
                             void* stream)
 {
   DFX_REQUIRE(op64 && op32, "operators must be non-NULL");
+  DFX_REQUIRE(op64->bs == 1 && op32->bs == 1, "refinement takes scalar (bs 1) operators");
   DFX_REQUIRE(op64->dtype == DFX_F64 && op32->dtype == DFX_F32,
               "refinement needs an FP64 outer and an FP32 inner operator");
   DFX_REQUIRE(op64->n == op32->n && op64->sigma == op32->sigma && op64->nslices == op32->nslices

@@ -45,6 +45,57 @@ __global__ void k_fill(const int32_t* __restrict__ map, const double* __restrict
   }
 }
 
+// Values of a 3x3-block operator, one output value o of the 9 nslots per
+// thread: slot row g = o / 288 (32 slots x 9 values), value e = o % 288 / 32
+// of lane o % 32's block, slot 32 g + o % 32. Block CSR values are
+// row-major 3x3 blocks, so e indexes them directly. Split operators store
+// (hi, lo) of each value as one float2.
+template <bool SPLIT>
+__global__ void k_fill_b3(const int32_t* __restrict__ map, const double* __restrict__ csr,
+                          void* __restrict__ out, int64_t nvals)
+{
+  for (int64_t o = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; o < nvals;
+       o += (int64_t)gridDim.x * blockDim.x)
+  {
+    const int64_t g = o / 288;
+    const int q = (int)(o - 288 * g);
+    const int32_t m = __ldg(map + 32 * g + (q & 31));
+    const double v = m >= 0 ? __ldg(csr + 9 * (int64_t)m + (q >> 5)) : 0.0;
+    if constexpr (SPLIT)
+    {
+      float hi, lo;
+      dfx::split_f64(v, hi, lo);
+      __stcs(reinterpret_cast<float2*>(out) + o, make_float2(hi, lo));
+    }
+    else
+      __stcs(reinterpret_cast<double*>(out) + o, v);
+  }
+}
+
+// y = A x, 3x3-block operator (lane = block row), FP64 or split values.
+template <bool SPLIT>
+__global__ void __launch_bounds__(128, 8)
+    k_bsell_spmv3(const dfx_operator_s op, const void* __restrict__ x, double* __restrict__ y)
+{
+  const int lane = threadIdx.x & 31;
+  const dfx::SliceRange sr = dfx::block_slices(op.nslices);
+  for (int32_t s = sr.begin; s < sr.end; s += sr.step)
+  {
+    double acc[3];
+    if constexpr (SPLIT)
+      dfx::bsell_row3_split(op, (const float2*)op.vals, (const float2*)x, s, lane, acc);
+    else
+      dfx::bsell_row3(op, (const double*)op.vals, (const double*)x, s, lane, acc);
+    const int32_t row = 3 * (32 * s + lane);
+    if (row < op.n)
+    {
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+        y[row + r] = acc[r];
+    }
+  }
+}
+
 // Split values (DFX_F32X2): hi = fl32(v) at i, lo = fl32(v - hi) at n + i.
 __global__ void k_fill_split(const int32_t* __restrict__ map, const double* __restrict__ csr,
                              float* __restrict__ out, int64_t n)
@@ -439,6 +490,130 @@ int finish_create(dfx_operator_s* op, const dfx_csr* A, dfx_operator* out, void*
     return dfx_operator_update_values(op, A, stream);
   return DFX_OK;
 }
+
+// The 3x3-block operator of a bs 3 block CSR (host build): block rows sorted
+// by length, stable, within windows of sigma block rows; slices of 32 block
+// rows; one 32-bit column per block. The scalar permutation is the block
+// one expanded (row 3 i + c -> 3 perm[i] + c).
+int create_b3(const dfx_csr* A, int32_t sigma, int32_t dtype, dfx_operator* out, void* stream)
+{
+  cudaStream_t s = dfx::as_stream(stream);
+  const int32_t nb = A->nrows;
+  DFX_REQUIRE((int64_t)3 * nb < INT32_MAX, "matrix too large for a 3x3-block operator");
+  std::vector<int64_t> rp(nb + 1);
+  std::vector<int32_t> cols(A->nnz);
+  DFX_CUDA(cudaMemcpyAsync(rp.data(), A->row_ptr, sizeof(int64_t) * (nb + 1),
+                           cudaMemcpyDeviceToHost, s));
+  if (A->nnz)
+    DFX_CUDA(cudaMemcpyAsync(cols.data(), A->cols, sizeof(int32_t) * A->nnz,
+                             cudaMemcpyDeviceToHost, s));
+  DFX_CUDA(cudaStreamSynchronize(s));
+  std::vector<int32_t> bperm(nb), biperm(nb);
+  std::iota(bperm.begin(), bperm.end(), 0);
+  parallel_for((nb + sigma - 1) / sigma,
+               [&](int64_t w0, int64_t w1)
+               {
+                 for (int64_t w = w0; w < w1; ++w)
+                 {
+                   auto b = bperm.begin() + w * sigma;
+                   auto e = bperm.begin() + std::min<int64_t>((w + 1) * (int64_t)sigma, nb);
+                   std::stable_sort(b, e, [&](int32_t a, int32_t c)
+                                    { return rp[a + 1] - rp[a] > rp[c + 1] - rp[c]; });
+                 }
+               });
+  for (int32_t i = 0; i < nb; ++i)
+    biperm[bperm[i]] = i;
+  const int32_t ns = (nb + 31) / 32;
+  std::vector<int64_t> sp(ns + 1, 0);
+  for (int32_t sl = 0; sl < ns; ++sl)
+  {
+    int64_t len = 0;
+    for (int l = 0; l < 32; ++l)
+    {
+      const int64_t i = 32 * (int64_t)sl + l;
+      if (i < nb)
+        len = std::max(len, rp[bperm[i] + 1] - rp[bperm[i]]);
+    }
+    sp[sl + 1] = sp[sl] + 32 * len;
+  }
+  const int64_t nslots = sp[ns];
+  DFX_REQUIRE(nslots < INT32_MAX, "operator too large");
+  std::vector<int32_t> scols(nslots), smap(nslots);
+  parallel_for(ns,
+               [&](int64_t s0, int64_t s1)
+               {
+                 std::vector<std::pair<int32_t, int32_t>> row;
+                 for (int64_t sl = s0; sl < s1; ++sl)
+                 {
+                   const int64_t len = (sp[sl + 1] - sp[sl]) / 32;
+                   for (int l = 0; l < 32; ++l)
+                   {
+                     const int64_t i = 32 * sl + l;
+                     row.clear();
+                     if (i < nb)
+                     {
+                       const int32_t r = bperm[i];
+                       for (int64_t j = rp[r]; j < rp[r + 1]; ++j)
+                         row.push_back({biperm[cols[j]], (int32_t)j});
+                       std::sort(row.begin(), row.end());
+                     }
+                     int32_t prev =
+                         row.empty() ? (int32_t)std::min<int64_t>(i, nb - 1) : row[0].first;
+                     for (int64_t k = 0; k < len; ++k)
+                     {
+                       const int64_t slot = sp[sl] + 32 * k + l;
+                       const bool real = k < (int64_t)row.size();
+                       const int32_t c = real ? row[k].first : prev;
+                       smap[slot] = real ? row[k].second : -1;
+                       scols[slot] = c;
+                       prev = c;
+                     }
+                   }
+                 }
+               });
+  std::vector<int32_t> perm(3 * (size_t)nb), iperm(3 * (size_t)nb);
+  for (int32_t i = 0; i < nb; ++i)
+    for (int c = 0; c < 3; ++c)
+    {
+      perm[3 * (size_t)i + c] = 3 * bperm[i] + c;
+      iperm[3 * (size_t)i + c] = 3 * biperm[i] + c;
+    }
+
+  auto* op = new dfx_operator_s();
+  op->serial = dfx::next_operator_serial();
+  cudaGetDevice(&op->device);
+  op->n = 3 * nb;
+  op->bs = 3;
+  op->nslices = ns;
+  op->sigma = sigma;
+  op->dtype = dtype;
+  op->compressed = 0;
+  op->nslots = nslots;
+  op->csr_nnz = A->nnz;
+  int st = DFX_OK;
+  if (!st)
+    st = upload(&op->perm, perm, s);
+  if (!st)
+    st = upload(&op->iperm, iperm, s);
+  if (!st)
+    st = upload(&op->slice_ptr, sp, s);
+  if (!st)
+    st = upload(&op->map, smap, s);
+  if (!st)
+    st = upload(&op->cols, scols, s);
+  if (!st)
+  {
+    cudaError_t e = cudaStreamSynchronize(s); // host vectors die at return
+    if (e != cudaSuccess)
+      st = dfx::cuda_fail(e, "upload", __FILE__, __LINE__);
+  }
+  if (st)
+  {
+    free_op(op);
+    return st;
+  }
+  return finish_create(op, A, out, stream);
+}
 } // namespace
 
 namespace dfx
@@ -459,7 +634,7 @@ uint64_t next_operator_serial()
 size_t value_bytes(const dfx_operator_s& op)
 {
   const size_t per = op.dtype == DFX_F32 ? 4 : 8; // F64, or two FP32 words
-  return per * (size_t)std::max<int64_t>(op.nslots, 1);
+  return per * (size_t)op.bs * op.bs * (size_t)std::max<int64_t>(op.nslots, 1);
 }
 
 // dfx_operator_apply's permuted x and y (and, split operators, x's words).
@@ -476,7 +651,14 @@ int sell_spmv(const dfx_operator_s& op, const void* x, void* y, cudaStream_t s)
   const unsigned grid = (unsigned)sell_grid(op.nslices);
   if (op.nslices == 0)
     return DFX_OK;
-  if (op.dtype == DFX_F64)
+  if (op.bs == 3)
+  {
+    if (op.dtype == DFX_F32X2)
+      k_bsell_spmv3<true><<<grid, 128, 0, s>>>(op, x, (double*)y);
+    else
+      k_bsell_spmv3<false><<<grid, 128, 0, s>>>(op, x, (double*)y);
+  }
+  else if (op.dtype == DFX_F64)
     k_sell_spmv<double, double, double, false><<<grid, 128, 0, s>>>(
         op, (const double*)op.vals, (const double*)x, (double*)y);
   else if (op.dtype == DFX_F32X2)
@@ -526,7 +708,8 @@ extern "C" int dfx_operator_create_ex(const dfx_csr* A, int32_t sigma, int32_t d
     return st;
   DFX_REQUIRE(out, "output handle is NULL");
   *out = nullptr;
-  DFX_REQUIRE(A->bs == 1, "the sliced-ELL operator takes scalar (bs 1) matrices");
+  DFX_REQUIRE(A->bs == 1 || A->bs == 3,
+              "the sliced-ELL operator takes scalar (bs 1) or 3x3-block matrices");
   DFX_REQUIRE(A->nrows == A->ncols, "matrix must be square");
   DFX_REQUIRE(dtype == DFX_F64 || dtype == DFX_F32 || dtype == DFX_F32X2,
               "unknown value type %d", dtype);
@@ -536,6 +719,13 @@ extern "C" int dfx_operator_create_ex(const dfx_csr* A, int32_t sigma, int32_t d
   DFX_REQUIRE(A->nnz < INT32_MAX, "matrix too large for the operator slot map");
   DFX_REQUIRE(build == DFX_BUILD_AUTO || build == DFX_BUILD_DEVICE || build == DFX_BUILD_HOST,
               "unknown build place %d", build);
+  if (A->bs == 3)
+  {
+    DFX_REQUIRE(dtype != DFX_F32, "3x3-block operators hold FP64 or split (DFX_F32X2) values");
+    DFX_REQUIRE(!compress_cols, "3x3-block operators keep 32-bit block columns");
+    DFX_REQUIRE(build != DFX_BUILD_DEVICE, "3x3-block operators are built on the host");
+    return create_b3(A, sigma, dtype, out, stream);
+  }
   cudaStream_t s = dfx::as_stream(stream);
   const int32_t n = A->nrows;
   if (build != DFX_BUILD_HOST)
@@ -700,10 +890,22 @@ extern "C" int dfx_operator_update_values(dfx_operator op, const dfx_csr* A, voi
   DFX_REQUIRE(op && A && A->vals, "operator and matrix must be non-NULL");
   DFX_REQUIRE(op->vals, "operator values were released (dfx_operator_release_values): use a share");
   DFX_REQUIRE(A->dtype == DFX_F64, "values are refilled from FP64 CSR values");
-  DFX_REQUIRE(A->nnz == op->csr_nnz && A->nrows == op->n, "matrix does not match the operator");
+  DFX_REQUIRE(A->nnz == op->csr_nnz && A->bs == op->bs && A->nrows * A->bs == op->n,
+              "matrix does not match the operator");
   if (op->nslots == 0)
     return DFX_OK;
   cudaStream_t s = dfx::as_stream(stream);
+  if (op->bs == 3)
+  {
+    const int64_t nv = 9 * op->nslots;
+    const unsigned g3 = (unsigned)std::min<int64_t>((nv + 255) / 256, 16 * dfx::num_sms());
+    if (op->dtype == DFX_F32X2)
+      k_fill_b3<true><<<g3, 256, 0, s>>>(op->map, (const double*)A->vals, op->vals, nv);
+    else
+      k_fill_b3<false><<<g3, 256, 0, s>>>(op->map, (const double*)A->vals, op->vals, nv);
+    DFX_CHECK_LAUNCH();
+    return DFX_OK;
+  }
   const unsigned grid = (unsigned)std::min<int64_t>((op->nslots + 255) / 256, 16 * dfx::num_sms());
   if (op->dtype == DFX_F64)
     k_fill<double><<<grid, 256, 0, s>>>(op->map, (const double*)A->vals, (double*)op->vals,

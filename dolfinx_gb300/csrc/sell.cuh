@@ -25,7 +25,13 @@
 
 struct dfx_operator_s
 {
-  int32_t n = 0;        // rows (scalar rows; block size 1)
+  int32_t n = 0;        // scalar rows
+  // 1, or 3: a 3x3-block operator. Its slices hold 32 block rows (lane =
+  // block row), one column index per block, and the 9 values of slot j at
+  // 9 (j - j % 32) + 32 e + j % 32, e = 3 r + c row-major within the block;
+  // split operators keep (hi, lo) of a value together there as one float2.
+  // perm / iperm are the block permutation expanded to the scalar rows.
+  int32_t bs = 1;
   int32_t nslices = 0;
   int32_t sigma = 0;
   int32_t dtype = DFX_F64;
@@ -286,6 +292,83 @@ __device__ __forceinline__ double sell_row_split(const dfx_operator_s& op,
     }
   }
   return (double)S + (double)L;
+}
+
+// Block row sums of a 3x3-block operator (bs 3): lane's block row
+// 32 s + lane, acc[r] = row 3 (32 s + lane) + r. The entries of a scalar
+// row are added in ascending column order, as in the scalar operator.
+// FP64 values: 76 bytes per block (one column, nine values) against 108
+// for the same nine entries in the scalar layout.
+__device__ __forceinline__ void bsell_row3(const dfx_operator_s& op, const double* __restrict__ vals,
+                                           const double* __restrict__ x, int32_t s, int lane,
+                                           double acc[3])
+{
+  const int64_t b = __ldg(op.slice_ptr + s);
+  const int len = (int)((__ldg(op.slice_ptr + s + 1) - b) >> 5);
+  const double* v = vals + 9 * b + lane;
+  const int32_t* c = op.cols + b + lane;
+  acc[0] = acc[1] = acc[2] = 0.0;
+#pragma unroll 2
+  for (int k = 0; k < len; ++k)
+  {
+    const int32_t cb = __ldcs(c + 32 * k);
+    double a[9];
+#pragma unroll
+    for (int e = 0; e < 9; ++e)
+      a[e] = __ldcs(v + 288 * (int64_t)k + 32 * e);
+    const double* xp = x + 3 * (int64_t)cb;
+    const double x0 = __ldg(xp), x1 = __ldg(xp + 1), x2 = __ldg(xp + 2);
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+      acc[r] = fma(a[3 * r + 2], x2, fma(a[3 * r + 1], x1, fma(a[3 * r], x0, acc[r])));
+  }
+}
+
+// The same for a split 3x3-block operator (DFX_F32X2, bs 3): each value's
+// (hi, lo) words in one float2, x's words (hi, lo) per scalar row, and the
+// error-free FP32 products and sums of sell_row_split per scalar row.
+__device__ __forceinline__ void bsell_row3_split(const dfx_operator_s& op,
+                                                 const float2* __restrict__ vw,
+                                                 const float2* __restrict__ xw, int32_t s,
+                                                 int lane, double out[3])
+{
+  const int64_t b = __ldg(op.slice_ptr + s);
+  const int len = (int)((__ldg(op.slice_ptr + s + 1) - b) >> 5);
+  const float2* v = vw + 9 * b + lane;
+  const int32_t* c = op.cols + b + lane;
+  float S[3] = {0.f, 0.f, 0.f}, L[3] = {0.f, 0.f, 0.f};
+  auto add = [&](int r, float ah, float al, float x0, float x1)
+  {
+    const float p = __fmul_rn(ah, x0);
+    const float e = fmaf(ah, x0, -p);
+    const float t = fmaf(ah, x1, fmaf(al, x0, e));
+    const float u = __fadd_rn(S[r], p);
+    const float bp = __fsub_rn(u, S[r]);
+    const float err = __fadd_rn(__fsub_rn(S[r], __fsub_rn(u, bp)), __fsub_rn(p, bp));
+    S[r] = u;
+    L[r] += err + t;
+  };
+#pragma unroll 2
+  for (int k = 0; k < len; ++k)
+  {
+    const int32_t cb = __ldcs(c + 32 * k);
+    float2 a[9];
+#pragma unroll
+    for (int e = 0; e < 9; ++e)
+      a[e] = __ldcs(v + 288 * (int64_t)k + 32 * e);
+    const float2* xp = xw + 3 * (int64_t)cb;
+    const float2 x0 = __ldg(xp), x1 = __ldg(xp + 1), x2 = __ldg(xp + 2);
+#pragma unroll
+    for (int r = 0; r < 3; ++r)
+    {
+      add(r, a[3 * r].x, a[3 * r].y, x0.x, x0.y);
+      add(r, a[3 * r + 1].x, a[3 * r + 1].y, x1.x, x1.y);
+      add(r, a[3 * r + 2].x, a[3 * r + 2].y, x2.x, x2.y);
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+    out[r] = (double)S[r] + (double)L[r];
 }
 
 // Splits an FP64 vector into the (hi, lo) FP32 words a split operator reads.

@@ -227,8 +227,10 @@ class SellOperator:
     """Sliced-ELL (SELL-32-sigma) solver copy of a scalar MatrixCSR: FP64, or
     FP32 with 16-bit column deltas, or (split=True) each FP64 value as two
     FP32 words multiplied on the FP32 pipe with error-free transformations
-    -- FP64-equivalent products on FP64 vectors. Values are refreshed from
-    the CSR values with update_values() after re-assembly."""
+    -- FP64-equivalent products on FP64 vectors. A 3x3-block MatrixCSR
+    (bs 3) gives a block operator, FP64 or split: one column index per
+    block, slices of 32 block rows, sigma counted in block rows. Values are
+    refreshed from the CSR values with update_values() after re-assembly."""
 
     def __init__(self, A: MatrixCSR, dtype=torch.float64, sigma: int = 256,
                  compress_cols: bool | None = None, share_of: "SellOperator | None" = None,
@@ -262,9 +264,9 @@ class SellOperator:
             if A is not None:
                 self.update_values()
             return
-        self.n, self.device = A.nrows, A.vals.device
+        self.n, self.device = A.nrows * A.bs, A.vals.device
         if compress_cols is None:
-            compress_cols = dtype == torch.float32 or self.split
+            compress_cols = (dtype == torch.float32 or self.split) and A.bs == 1
         dt = _capi.F64 if dtype == torch.float64 else _capi.F32
         if self.split:
             dt = _capi.F32X2
@@ -370,7 +372,7 @@ class OperatorCGSolver:
                  sigma: int = 256, split: bool = False):
         self.A = A
         self.op = SellOperator(A, torch.float64, sigma, split=split)
-        self.n = A.nrows
+        self.n = A.nrows * A.bs
         self.dinv = A.inverse_diagonal() if jacobi else None
         wb = int(_capi.lib().dfx_cg_op_workspace_bytes(self.n))
         self.work = torch.empty(wb, dtype=torch.uint8, device=A.vals.device)

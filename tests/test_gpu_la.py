@@ -251,6 +251,85 @@ def test_split_operator_cg_matches_fp64(cuda, oracle, capi):
         assert (xs - x64).norm().item() / x64.norm().item() < 1e-9
 
 
+@pytest.mark.parametrize("split", [False, True])
+@pytest.mark.parametrize("sigma", [32, 4096])
+def test_block_operator_matches_oracle(cuda, oracle, capi, split, sigma):
+    """The 3x3-block operator of an elasticity matrix (one column per block,
+    FP64 or split values) against the oracle's block SpMV, in both
+    numberings, for block-row counts that are not multiples of 32, after a
+    value refresh and through a share with other values."""
+    from dolfinx_gb300 import fem, la
+
+    for shape in ((5, 3, 4), (6, 4, 3)):
+        m, V, E, f, rp, cols = problem(oracle, shape, 2, bs=3, seed=29)
+        A = fem.assemble_matrix(fem.elasticity_form(V, 1e3 * E, 0.3))
+        op = la.SellOperator(A, torch.float64, sigma, split=split)
+        assert op.n == V.num_dofs and not op.compressed
+        x = np.random.default_rng(5).standard_normal(V.num_dofs)
+        # Row-wise against (|A| |x|)_i: elasticity rows cancel, so a bound
+        # relative to the largest entry of y would not hold. FP64 rows of
+        # ~81 entries are within (81 + 81) u of the oracle's; split rows
+        # round at ~2^-44 of |A| |x|.
+        tol = 2e-13 if split else 2e-14
+
+        def check(y, M):
+            v = M.vals.cpu().numpy()
+            ref = oracle.spmv(rp, cols, v, x, bs=3)
+            mag = oracle.spmv(rp, cols, np.abs(v), np.abs(x), bs=3)
+            err = (np.abs(np.asarray(y) - ref) / np.maximum(mag, 1e-300)).max()
+            assert err <= tol, f"row error {err:.3e} of |A||x| > {tol:.1e}"
+
+        check(op.apply(torch.from_numpy(x).cuda()).cpu().numpy(), A)
+        xp = op.to_operator(torch.from_numpy(x).cuda())
+        yp = op.apply_renumbered(xp, torch.empty_like(xp))
+        check(op.from_operator(yp).cpu().numpy(), A)
+        A2 = fem.assemble_matrix(fem.elasticity_form(V, 2e3 * E, 0.25))
+        sh = op.share(A2)
+        check(sh.apply(torch.from_numpy(x).cuda()).cpu().numpy(), A2)
+        del sh
+        A.vals.mul_(3.0)
+        op.update_values()
+        check(op.apply(torch.from_numpy(x).cuda()).cpu().numpy(), A)
+
+
+def test_block_operator_cg_matches_scalar(cuda, oracle, capi):
+    """Jacobi-PCG on the 3x3-block operators (FP64 and split) of a clamped
+    elasticity system takes the scalar FP64 operator's iteration count
+    (within 1 %), meets the stopping test in the oracle's FP64 SpMV and
+    reaches the same solution."""
+    from dolfinx_gb300 import fem, la
+
+    m, V, E, f, rpe, colse = problem(oracle, (8, 3, 3), 2, bs=3, seed=13)
+    X = V.tabulate_dof_coordinates()
+    clamp = np.flatnonzero(np.isclose(X[:, 0], 0)).astype(np.int32)
+    bc = fem.dirichletbc(np.zeros(3), clamp, V)
+    a = fem.elasticity_form(V, 1e3 * E, 0.3)
+    Ae = fem.assemble_matrix(a, bcs=[bc])
+    be = fem.RhsAssembler(fem.body_force_form(V, (0, 0, -1)), a, [bc]).assemble()
+    S = Ae.expand_blocks()
+    x64 = torch.zeros_like(be)
+    r64 = la.OperatorCGSolver(S).solve(be, x64, rtol=1e-11)
+    bh = be.cpu().numpy()
+    for split in (False, True):
+        solver = la.OperatorCGSolver(Ae, split=split)
+        xb = torch.zeros_like(be)
+        rb = solver.solve(be, xb, rtol=1e-11)
+        tol = max(2, int(0.01 * r64.iterations))
+        assert rb.status == 0 and abs(rb.iterations - r64.iterations) <= tol, (split, rb, r64)
+        res = bh - oracle.spmv(rpe, colse, Ae.vals.cpu().numpy(), xb.cpu().numpy(), bs=3)
+        assert np.linalg.norm(res) / np.linalg.norm(bh) < 1e-11 * 1.25
+        assert (xb - x64).norm().item() / x64.norm().item() < 1e-9
+        # a re-assembly with other coefficients, through refresh()
+        Ae2 = fem.assemble_matrix(fem.elasticity_form(V, 2e3 * E, 0.3), bcs=[bc])
+        Ae.vals.copy_(Ae2.vals)
+        solver.refresh()
+        xr = torch.zeros_like(be)
+        assert solver.solve(be, xr, rtol=1e-11).status == 0
+        res = bh - oracle.spmv(rpe, colse, Ae.vals.cpu().numpy(), xr.cpu().numpy(), bs=3)
+        assert np.linalg.norm(res) / np.linalg.norm(bh) < 1e-11 * 1.25
+        Ae = fem.assemble_matrix(a, bcs=[bc])
+
+
 def _poisson_system(oracle, n, deg, seed):
     from dolfinx_gb300 import fem
 
