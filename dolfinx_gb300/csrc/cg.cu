@@ -617,9 +617,9 @@ __global__ void __launch_bounds__(kSellThreads, 12)
 }
 
 // y = A p, p.y -- 3x3-block operator (bs 3, lane = block row): FP64
-// values, or split values on the FP32 words of p.
-template <bool SPLIT>
-__global__ void __launch_bounds__(kSellThreads, 8)
+// values, or split values on the FP32 words of p; SL block slots per round.
+template <bool SPLIT, int SL>
+__global__ void __launch_bounds__(kSellThreads, dfx::kBsellMinBlocks<SL>)
     k_spmv_dot_bsell3(const dfx_operator_s op, Work<double> w)
 {
   block_reduce_init();
@@ -633,10 +633,10 @@ __global__ void __launch_bounds__(kSellThreads, 8)
   {
     double acc[3];
     if constexpr (SPLIT)
-      dfx::bsell_row3_split(op, (const float2*)op.vals, reinterpret_cast<const float2*>(w.ph),
-                            s, lane, acc);
+      dfx::bsell_row3_split<SL>(op, (const float2*)op.vals,
+                                reinterpret_cast<const float2*>(w.ph), s, lane, acc);
     else
-      dfx::bsell_row3(op, (const double*)op.vals, w.p, s, lane, acc);
+      dfx::bsell_row3<SL>(op, (const double*)op.vals, w.p, s, lane, acc);
     const int32_t row = 3 * (32 * s + lane);
     if (row < op.n)
     {
@@ -1758,10 +1758,24 @@ void enqueue_spmv_dot<double>(const OpRef& o, const Work<double>& w, cudaStream_
     if (o.op->bs == 3)
     {
       const unsigned g = (unsigned)dfx::sell_grid(o.op->nslices);
+      auto launch = [&](auto split, auto sl)
+      {
+        k_spmv_dot_bsell3<decltype(split)::value, decltype(sl)::value>
+            <<<g, kSellThreads, 0, s>>>(*o.op, w);
+      };
+      auto by_chunk = [&](auto split)
+      {
+        if (o.op->chunk == 2)
+          launch(split, std::integral_constant<int, 1>{});
+        else if (o.op->chunk == 8)
+          launch(split, std::integral_constant<int, 4>{});
+        else
+          launch(split, std::integral_constant<int, 2>{});
+      };
       if (o.op->dtype == DFX_F32X2)
-        k_spmv_dot_bsell3<true><<<g, kSellThreads, 0, s>>>(*o.op, w);
+        by_chunk(std::true_type{});
       else
-        k_spmv_dot_bsell3<false><<<g, kSellThreads, 0, s>>>(*o.op, w);
+        by_chunk(std::false_type{});
     }
     else if (o.op->dtype == DFX_F32X2)
     {

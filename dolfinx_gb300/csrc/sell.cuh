@@ -57,6 +57,8 @@ struct dfx_operator_s
   uint64_t serial = 0;
   // FP32 operators: value pairs per load chunk of a lane (2, 4 or 8): the
   // loads of one chunk are in flight together (autotuned; 4 by default).
+  // 3x3-block operators: 2, 4 or 8 for 1, 2 or 4 block slots per round
+  // (8 by default).
   int32_t chunk = 4;
   int32_t owns_structure = 1;
   // Values and scratch come from the library's stream-ordered pool
@@ -298,7 +300,9 @@ __device__ __forceinline__ double sell_row_split(const dfx_operator_s& op,
 // 32 s + lane, acc[r] = row 3 (32 s + lane) + r. The entries of a scalar
 // row are added in ascending column order, as in the scalar operator.
 // FP64 values: 76 bytes per block (one column, nine values) against 108
-// for the same nine entries in the scalar layout.
+// for the same nine entries in the scalar layout. SL block slots are read
+// per round, their loads issued together (the operator's chunk / 2).
+template <int SL>
 __device__ __forceinline__ void bsell_row3(const dfx_operator_s& op, const double* __restrict__ vals,
                                            const double* __restrict__ x, int32_t s, int lane,
                                            double acc[3])
@@ -308,25 +312,44 @@ __device__ __forceinline__ void bsell_row3(const dfx_operator_s& op, const doubl
   const double* v = vals + 9 * b + lane;
   const int32_t* c = op.cols + b + lane;
   acc[0] = acc[1] = acc[2] = 0.0;
-#pragma unroll 2
-  for (int k = 0; k < len; ++k)
+  for (int k0 = 0; k0 < len; k0 += SL)
   {
-    const int32_t cb = __ldcs(c + 32 * k);
-    double a[9];
+    int32_t cb[SL];
+    double a[SL][9];
 #pragma unroll
-    for (int e = 0; e < 9; ++e)
-      a[e] = __ldcs(v + 288 * (int64_t)k + 32 * e);
-    const double* xp = x + 3 * (int64_t)cb;
-    const double x0 = __ldg(xp), x1 = __ldg(xp + 1), x2 = __ldg(xp + 2);
+    for (int u = 0; u < SL; ++u)
+    {
+      const bool ok = SL == 1 || k0 + u < len;
+      cb[u] = ok ? __ldcs(c + 32 * (k0 + u)) : 0;
 #pragma unroll
-    for (int r = 0; r < 3; ++r)
-      acc[r] = fma(a[3 * r + 2], x2, fma(a[3 * r + 1], x1, fma(a[3 * r], x0, acc[r])));
+      for (int e = 0; e < 9; ++e)
+        a[u][e] = ok ? __ldcs(v + 288 * (int64_t)(k0 + u) + 32 * e) : 0.0;
+    }
+    double xv[SL][3];
+#pragma unroll
+    for (int u = 0; u < SL; ++u)
+    {
+      const double* xp = x + 3 * (int64_t)cb[u];
+#pragma unroll
+      for (int q = 0; q < 3; ++q)
+        xv[u][q] = __ldg(xp + q);
+    }
+#pragma unroll
+    for (int u = 0; u < SL; ++u)
+      if (SL == 1 || k0 + u < len)
+      {
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+          acc[r] = fma(a[u][3 * r + 2], xv[u][2],
+                       fma(a[u][3 * r + 1], xv[u][1], fma(a[u][3 * r], xv[u][0], acc[r])));
+      }
   }
 }
 
 // The same for a split 3x3-block operator (DFX_F32X2, bs 3): each value's
 // (hi, lo) words in one float2, x's words (hi, lo) per scalar row, and the
 // error-free FP32 products and sums of sell_row_split per scalar row.
+template <int SL>
 __device__ __forceinline__ void bsell_row3_split(const dfx_operator_s& op,
                                                  const float2* __restrict__ vw,
                                                  const float2* __restrict__ xw, int32_t s,
@@ -348,28 +371,48 @@ __device__ __forceinline__ void bsell_row3_split(const dfx_operator_s& op,
     S[r] = u;
     L[r] += err + t;
   };
-#pragma unroll 2
-  for (int k = 0; k < len; ++k)
+  for (int k0 = 0; k0 < len; k0 += SL)
   {
-    const int32_t cb = __ldcs(c + 32 * k);
-    float2 a[9];
+    int32_t cb[SL];
+    float2 a[SL][9];
 #pragma unroll
-    for (int e = 0; e < 9; ++e)
-      a[e] = __ldcs(v + 288 * (int64_t)k + 32 * e);
-    const float2* xp = xw + 3 * (int64_t)cb;
-    const float2 x0 = __ldg(xp), x1 = __ldg(xp + 1), x2 = __ldg(xp + 2);
-#pragma unroll
-    for (int r = 0; r < 3; ++r)
+    for (int u = 0; u < SL; ++u)
     {
-      add(r, a[3 * r].x, a[3 * r].y, x0.x, x0.y);
-      add(r, a[3 * r + 1].x, a[3 * r + 1].y, x1.x, x1.y);
-      add(r, a[3 * r + 2].x, a[3 * r + 2].y, x2.x, x2.y);
+      const bool ok = SL == 1 || k0 + u < len;
+      cb[u] = ok ? __ldcs(c + 32 * (k0 + u)) : 0;
+#pragma unroll
+      for (int e = 0; e < 9; ++e)
+        a[u][e] = ok ? __ldcs(v + 288 * (int64_t)(k0 + u) + 32 * e) : make_float2(0.f, 0.f);
     }
+    float2 xv[SL][3];
+#pragma unroll
+    for (int u = 0; u < SL; ++u)
+    {
+      const float2* xp = xw + 3 * (int64_t)cb[u];
+#pragma unroll
+      for (int q = 0; q < 3; ++q)
+        xv[u][q] = __ldg(xp + q);
+    }
+#pragma unroll
+    for (int u = 0; u < SL; ++u)
+      if (SL == 1 || k0 + u < len)
+      {
+#pragma unroll
+        for (int r = 0; r < 3; ++r)
+#pragma unroll
+          for (int q = 0; q < 3; ++q)
+            add(r, a[u][3 * r + q].x, a[u][3 * r + q].y, xv[u][q].x, xv[u][q].y);
+      }
   }
 #pragma unroll
   for (int r = 0; r < 3; ++r)
     out[r] = (double)S[r] + (double)L[r];
 }
+
+// Blocks per SM of the 3x3-block SpMV kernels by slots per round: the
+// registers of SL slots of values (64, 80 and 128 registers).
+template <int SL>
+constexpr int kBsellMinBlocks = SL == 1 ? 8 : (SL == 2 ? 6 : 4);
 
 // Splits an FP64 vector into the (hi, lo) FP32 words a split operator reads.
 __device__ __forceinline__ void split_f64(double v, float& hi, float& lo)

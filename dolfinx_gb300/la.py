@@ -320,8 +320,9 @@ class SellOperator:
         return yp
 
     def set_chunk(self, chunk: int) -> None:
-        """Value pairs per load chunk of the FP32 SpMV (2, 4 or 8); the
-        product is bitwise the same for each."""
+        """Value pairs per load chunk of the FP32 SpMV (2, 4 or 8); for a
+        3x3-block operator 2, 4 or 8 stand for 1, 2 or 4 block slots per
+        round. The product is bitwise the same for each."""
         _capi.check(_capi.lib().dfx_operator_set_chunk(self.handle, int(chunk)))
 
     def info(self):

@@ -565,7 +565,9 @@ int dfx_operator_release_values(dfx_operator op);
 int dfx_operator_device_bytes(dfx_operator op, size_t* bytes);
 /* Launch shape of an FP32 operator's SpMV (no reference counterpart; an
  * autotuner knob): value pairs per load chunk of a lane, 2, 4 (default) or
- * 8. Results are bitwise the same for every choice. */
+ * 8. For a 3x3-block operator: 2, 4 or 8 (default) stand for 1, 2 or 4
+ * block slots per round of a lane. Results are bitwise the same for every
+ * choice. */
 int dfx_operator_set_chunk(dfx_operator op, int32_t chunk);
 
 /* Launch setting of the FP32 inner iteration (no reference counterpart),

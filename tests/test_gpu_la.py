@@ -279,7 +279,12 @@ def test_block_operator_matches_oracle(cuda, oracle, capi, split, sigma):
             err = (np.abs(np.asarray(y) - ref) / np.maximum(mag, 1e-300)).max()
             assert err <= tol, f"row error {err:.3e} of |A||x| > {tol:.1e}"
 
-        check(op.apply(torch.from_numpy(x).cuda()).cpu().numpy(), A)
+        y0 = op.apply(torch.from_numpy(x).cuda())
+        check(y0.cpu().numpy(), A)
+        # 1, 2 and 4 block slots per round give the same bits
+        for ch in (2, 4, 8):
+            op.set_chunk(ch)
+            assert torch.equal(op.apply(torch.from_numpy(x).cuda()), y0)
         xp = op.to_operator(torch.from_numpy(x).cuda())
         yp = op.apply_renumbered(xp, torch.empty_like(xp))
         check(op.from_operator(yp).cpu().numpy(), A)
