@@ -524,7 +524,10 @@ int dfx_timing_clear(void);
  * is the GB300 layout behind MatrixCSR::mult inside the solvers
  * (la/MatrixCSR.h:877-946). FP32 operators may store columns as a first
  * column per row plus 16-bit deltas (DFX_ERR_UNSUPPORTED if a row has a
- * gap above 65535). The library owns the operator's device memory. */
+ * gap above 65535). A bs 3 matrix gives a 3x3-block operator (FP64 or
+ * DFX_F32X2 values, 32-bit block columns, host build): slices of 32 block
+ * rows, sigma counted in block rows, vectors of 3 nrows scalar entries.
+ * The library owns the operator's device memory. */
 typedef struct dfx_operator_s* dfx_operator;
 
 int dfx_operator_create(const dfx_csr* A, int32_t sigma, int32_t value_dtype,
