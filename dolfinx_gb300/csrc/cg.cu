@@ -2729,24 +2729,14 @@ constexpr size_t kNoAllocBytes = (size_t)13 << 20;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
 
-std::mutex g_noalloc_mutex;
-void* g_noalloc_ptr[64] = {};
-
-// Device address of the scratch array on the current device (set up once
-// per device, with that device current).
+// Device address of the scratch array in the current context, looked up on
+// every call: it allocates nothing, and a context that was reset and made
+// again (cudaDeviceReset) may place the array elsewhere.
 int noalloc_scratch(void** out)
 {
-  int dev = 0;
-  DFX_CUDA(cudaGetDevice(&dev));
-  DFX_REQUIRE(dev >= 0 && dev < 64, "device index %d out of range", dev);
-  std::lock_guard<std::mutex> lk(g_noalloc_mutex);
-  if (!g_noalloc_ptr[dev])
-  {
-    void* p = nullptr;
-    DFX_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
-    g_noalloc_ptr[dev] = p;
-  }
-  *out = g_noalloc_ptr[dev];
+  void* p = nullptr;
+  DFX_CUDA(cudaGetSymbolAddress(&p, g_noalloc_scratch));
+  *out = p;
   return DFX_OK;
 }
 } // namespace
