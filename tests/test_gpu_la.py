@@ -297,6 +297,69 @@ def test_block_operator_matches_oracle(cuda, oracle, capi, split, sigma):
         check(op.apply(torch.from_numpy(x).cuda()).cpu().numpy(), A)
 
 
+@pytest.mark.parametrize("nb", [1, 31, 32, 33, 97])
+def test_block_operator_edge_sizes(cuda, capi, nb):
+    """3x3-block operators of random block CSR matrices (ragged rows of 1
+    to 9 blocks, block-row counts around the 32-row slice) against a dense
+    product in numpy, FP64 and split, for every slots-per-round choice;
+    an empty bs 3 matrix gives an empty operator."""
+    from dolfinx_gb300 import la
+
+    rng = np.random.default_rng(nb)
+    rows = []
+    for i in range(nb):
+        k = int(rng.integers(1, min(nb, 9) + 1))
+        rows.append(np.unique(np.concatenate([[i], rng.choice(nb, k - 1, replace=True)]))
+                    .astype(np.int64))
+    rp = np.zeros(nb + 1, np.int64)
+    rp[1:] = np.cumsum([r.size for r in rows])
+    cols = np.concatenate(rows).astype(np.int32)
+    vals = rng.standard_normal(9 * cols.size)
+    dense = np.zeros((3 * nb, 3 * nb))
+    for i, r in enumerate(rows):
+        for j, c in enumerate(r):
+            blk = vals[9 * (rp[i] + j): 9 * (rp[i] + j + 1)].reshape(3, 3)
+            dense[3 * i:3 * i + 3, 3 * c:3 * c + 3] = blk
+    A = la.MatrixCSR(torch.from_numpy(rp).cuda(), torch.from_numpy(cols).cuda(),
+                     torch.from_numpy(vals).cuda(), 3)
+    x = rng.standard_normal(3 * nb)
+    ref = dense @ x
+    mag = np.abs(dense) @ np.abs(x)
+    for split in (False, True):
+        op = la.SellOperator(A, torch.float64, 32, split=split)
+        assert op.n == 3 * nb
+        tol = 2e-13 if split else 2e-15 * 27
+        for ch in (2, 4, 8):
+            op.set_chunk(ch)
+            y = op.apply(torch.from_numpy(x).cuda()).cpu().numpy()
+            assert (np.abs(y - ref) / mag).max() <= tol
+
+    E = la.MatrixCSR(torch.zeros(1, dtype=torch.int64, device="cuda"),
+                     torch.zeros(0, dtype=torch.int32, device="cuda"),
+                     torch.zeros(0, dtype=torch.float64, device="cuda"), 3)
+    for split in (False, True):
+        op = la.SellOperator(E, torch.float64, split=split)
+        assert op.info()["slots"] == 0 and op.n == 0
+        assert op.apply(torch.zeros(0, dtype=torch.float64, device="cuda")).numel() == 0
+
+
+def test_block_operator_refuses_what_it_does_not_hold(cuda, capi):
+    """3x3-block operators hold FP64 or split values with 32-bit columns,
+    built on the host; refinement takes scalar operators."""
+    from dolfinx_gb300 import la
+    from dolfinx_gb300._capi import DfxError
+
+    rp = torch.tensor([0, 1], dtype=torch.int64, device="cuda")
+    A = la.MatrixCSR(rp, torch.zeros(1, dtype=torch.int32, device="cuda"),
+                     torch.eye(3, dtype=torch.float64, device="cuda").flatten(), 3)
+    with pytest.raises(DfxError, match="FP64 or split"):
+        la.SellOperator(A, torch.float32)
+    with pytest.raises(DfxError, match="32-bit block columns"):
+        la.SellOperator(A, torch.float64, split=True, compress_cols=True)
+    with pytest.raises(DfxError, match="built on the host"):
+        la.SellOperator(A, torch.float64, build=1)
+
+
 def test_block_operator_cg_matches_scalar(cuda, oracle, capi):
     """Jacobi-PCG on the 3x3-block operators (FP64 and split) of a clamped
     elasticity system takes the scalar FP64 operator's iteration count
