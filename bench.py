@@ -486,6 +486,19 @@ def elasticity_sample(steps=1, warmup=1):
     out["spmv_ms"] = {"fp64": _kernel_ms(lambda: fp64.op.apply_renumbered(xr, yr), 10, stream),
                       "split_fp32_words": _kernel_ms(lambda: ir.op.apply_renumbered(xr, yr), 10,
                                                      stream)}
+    # Algorithmic bytes of one block SpMV: 76 per block (one column, nine
+    # values as FP64 or as two FP32 words) plus x (8 B: FP64, or its two
+    # words) and y (8 B) per row.
+    peak, peak_kind = measured_peaks()
+    alg = 76 * A.nnz + 16 * fp64.n
+    out["roofline_spmv"] = {
+        name: {"bound": bound, "alg_bytes_per_launch": alg, "launch_ms": ms,
+               "achieved": alg / (ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
+               "frac": alg / (ms * 1e-3) / 1e9 / peak, "peak_source": peak_kind}
+        for name, bound, ms in (("split_fp32_words", "hbm", out["spmv_ms"]["split_fp32_words"]),
+                                ("fp64", f"fp64 pipe ({9 * A.nnz / 1e6:.1f}M FMAs at 2 per "
+                                         "clock per SM)",
+                                 out["spmv_ms"]["fp64"]))}
     return out
 
 
