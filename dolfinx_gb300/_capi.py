@@ -123,6 +123,8 @@ class Q4Mesh(C.Structure):
         ("verts", C.c_void_p),
         ("kappa", C.c_double),
         ("edges32", C.c_void_p),
+        ("geom32", C.c_void_p),
+        ("geom64", C.c_void_p),
     ]
 
 
@@ -238,6 +240,7 @@ _SIGS = {
                                            _P, _P, C.c_double, _P]),
     "dfx_q4_tc_check": (C.c_int, [_P]),
     "dfx_q4_edges": (C.c_int, [C.POINTER(Q4Mesh), _P, _P]),
+    "dfx_q4_geometry": (C.c_int, [C.POINTER(Q4Mesh), C.c_int32, _P, _P]),
     "dfx_q4_cg_workspace_bytes": (C.c_size_t, [C.c_int64, C.c_int32]),
     "dfx_q4_cg_solve": (C.c_int, [C.POINTER(Q4Mesh), _P, _P, C.c_double, C.c_int32, C.c_int32,
                                   C.c_double, C.c_int32, _P, C.c_size_t, C.POINTER(CgInfo), _P]),

@@ -341,7 +341,10 @@ struct CellIter
 __device__ __forceinline__ float div_abs(float x, float d) { return __fdividef(x, fabsf(d)); }
 __device__ __forceinline__ double div_abs(double x, double d) { return x / fabs(d); }
 
-template <typename T>
+// GQ: read the cached geometric factors (dfx_q4_geometry) in phase 3 in
+// place of the Jacobian, adjugate and determinant; the edge vectors are
+// then not staged.
+template <typename T, bool GQ>
 __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2)
     k_q4_cells(const dfx_q4_mesh_s m, const T* __restrict__ u, T* __restrict__ y,
                const Colour col, const int32_t* __restrict__ skip)
@@ -411,6 +414,13 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2)
     return __ldg(reinterpret_cast<const float4*>(m.edges32) + 9 * cell + l);
   };
 
+  const T* geo = nullptr;
+  if constexpr (sizeof(T) == 4)
+    geo = m.geom32;
+  else
+    geo = m.geom64;
+  constexpr bool gq = GQ;
+
   // Per-thread quadrature data of the phase-3 line (x = la, y = lb).
   const T X = Tb::G(la), Y = Tb::G(lb);
   const T qwl = Tb::W(la) * Tb::W(lb) * (T)m.kappa;
@@ -426,10 +436,13 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2)
   T un[5];
   double vn = 0.0;
   float4 en = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (pre)
-    en = edges_of(L);
-  else
-    vn = vert_of(L);
+  if constexpr (!GQ)
+  {
+    if (pre)
+      en = edges_of(L);
+    else
+      vn = vert_of(L);
+  }
 #pragma unroll
   for (int a = 0; a < 5; ++a)
     un[a] = L.valid ? u[L.base + a] : T(0);
@@ -447,10 +460,10 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2)
     }
     if constexpr (sizeof(T) == 4)
     {
-      if (pre && act && l < 9)
+      if (!gq && pre && act && l < 9)
         reinterpret_cast<float4*>(&se[c][0][0])[l] = en;
     }
-    if (!pre && act && l < 24)
+    if (!gq && !pre && act && l < 24)
       sv[c][l] = vn;
     // Inputs of the next batch, in flight while this one is processed.
     const Line Lc = L;
@@ -461,14 +474,17 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2)
 #pragma unroll
       for (int a = 0; a < 5; ++a)
         un[a] = L.valid ? u[L.base + a] : T(0);
-      if (pre)
-        en = edges_of(L);
-      else
-        vn = vert_of(L);
+      if constexpr (!GQ)
+      {
+        if (pre)
+          en = edges_of(L);
+        else
+          vn = vert_of(L);
+      }
     }
     __syncthreads();
     // Edge vectors: differences of the FP64 vertices, rounded once to T.
-    for (int e = pre ? kBatch * 36 : t; e < kBatch * 36; e += blockDim.x)
+    for (int e = (pre || gq) ? kBatch * 36 : t; e < kBatch * 36; e += blockDim.x)
     {
       const int cc = e / 36, r = e % 36, comp = r / 12, ed = r % 12;
       const int lo = edge_lo(ed), hi = lo + (1 << (ed >> 2));
@@ -497,6 +513,20 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2)
     }
     __syncthreads();
     const bool cv = Lc.valid;
+    // The cached geometric factors of this thread's phase-3 line (points
+    // la + 5 lb + 25 q of the cell), loaded here so that phase 2 covers
+    // their latency.
+    T gm[GQ ? 6 : 1][5];
+    if constexpr (GQ)
+      if (cv)
+      {
+        const T* gp = geo + 750 * (Lc.i + (int64_t)m.nx * (Lc.j + (int64_t)m.ny * Lc.k)) + l;
+#pragma unroll
+        for (int k = 0; k < 6; ++k)
+#pragma unroll
+          for (int q = 0; q < 5; ++q)
+            gm[k][q] = __ldg(gp + 125 * k + 25 * q);
+      }
     // Phase 2: contract y on the (x, z) = (la, lb) line.
     if (cv)
     {
@@ -536,64 +566,85 @@ __global__ void __launch_bounds__(128, sizeof(T) == 4 ? 4 : 2)
         cy[r] = S3[lay_b<T>(la, lb, r)];
         cx[r] = S4[lay_b<T>(la, lb, r)];
       }
-      // Jacobian columns along the line: d/dX and d/dY are linear in Z,
-      // d/dZ does not depend on Z.
-      T P0[3], dP[3], Q0[3], dQ[3], R[3];
-#pragma unroll
-      for (int comp = 0; comp < 3; ++comp)
-      {
-        T e[12];
-        load_edges(se[c][comp], e);
-        const T p0 = (1 - Y) * e[0] + Y * e[1], p1 = (1 - Y) * e[2] + Y * e[3];
-        const T q0 = (1 - X) * e[4] + X * e[5], q1 = (1 - X) * e[6] + X * e[7];
-        P0[comp] = p0;
-        dP[comp] = p1 - p0;
-        Q0[comp] = q0;
-        dQ[comp] = q1 - q0;
-        R[comp] = (1 - X) * (1 - Y) * e[8] + X * (1 - Y) * e[9] + (1 - X) * Y * e[10]
-                  + X * Y * e[11];
-      }
       T vx[5], vy[5], vz[5];
-#pragma unroll
-      for (int q = 0; q < 5; ++q)
+      if constexpr (GQ)
       {
-        T ux = 0, uy = 0, uz = 0;
 #pragma unroll
-        for (int r = 0; r < 5; ++r)
+        for (int q = 0; q < 5; ++q)
         {
-          ux += Tb::B(q, r) * cx[r];
-          uy += Tb::B(q, r) * cy[r];
-          uz += Tb::D(q, r) * c0[r];
+          T ux = 0, uy = 0, uz = 0;
+#pragma unroll
+          for (int r = 0; r < 5; ++r)
+          {
+            ux += Tb::B(q, r) * cx[r];
+            uy += Tb::B(q, r) * cy[r];
+            uz += Tb::D(q, r) * c0[r];
+          }
+          vx[q] = gm[0][q] * ux + gm[1][q] * uy + gm[2][q] * uz;
+          vy[q] = gm[1][q] * ux + gm[3][q] * uy + gm[4][q] * uz;
+          vz[q] = gm[2][q] * ux + gm[4][q] * uy + gm[5][q] * uz;
         }
-        const T Z = Tb::G(q);
-        T J[3][3];
+      }
+      else
+      {
+        // Jacobian columns along the line: d/dX and d/dY are linear in Z,
+        // d/dZ does not depend on Z.
+        T P0[3], dP[3], Q0[3], dQ[3], R[3];
 #pragma unroll
         for (int comp = 0; comp < 3; ++comp)
         {
-          J[comp][0] = P0[comp] + Z * dP[comp];
-          J[comp][1] = Q0[comp] + Z * dQ[comp];
-          J[comp][2] = R[comp];
+          T e[12];
+          load_edges(se[c][comp], e);
+          const T p0 = (1 - Y) * e[0] + Y * e[1], p1 = (1 - Y) * e[2] + Y * e[3];
+          const T q0 = (1 - X) * e[4] + X * e[5], q1 = (1 - X) * e[6] + X * e[7];
+          P0[comp] = p0;
+          dP[comp] = p1 - p0;
+          Q0[comp] = q0;
+          dQ[comp] = q1 - q0;
+          R[comp] = (1 - X) * (1 - Y) * e[8] + X * (1 - Y) * e[9] + (1 - X) * Y * e[10]
+                    + X * Y * e[11];
         }
-        T adj[3][3];
-        adj[0][0] = J[1][1] * J[2][2] - J[1][2] * J[2][1];
-        adj[0][1] = J[0][2] * J[2][1] - J[0][1] * J[2][2];
-        adj[0][2] = J[0][1] * J[1][2] - J[0][2] * J[1][1];
-        adj[1][0] = J[1][2] * J[2][0] - J[1][0] * J[2][2];
-        adj[1][1] = J[0][0] * J[2][2] - J[0][2] * J[2][0];
-        adj[1][2] = J[0][2] * J[1][0] - J[0][0] * J[1][2];
-        adj[2][0] = J[1][0] * J[2][1] - J[1][1] * J[2][0];
-        adj[2][1] = J[0][1] * J[2][0] - J[0][0] * J[2][1];
-        adj[2][2] = J[0][0] * J[1][1] - J[0][1] * J[1][0];
-        const T det = J[0][0] * adj[0][0] + J[0][1] * adj[1][0] + J[0][2] * adj[2][0];
-        // G grad = w kappa |det| K K^T grad = sc adj (adj^T grad), K = J^{-1} =
-        // adj / det, sc = w kappa / |det|.
-        const T sc = div_abs(qwl * Tb::W(q), det);
-        const T w0 = sc * (adj[0][0] * ux + adj[1][0] * uy + adj[2][0] * uz);
-        const T w1 = sc * (adj[0][1] * ux + adj[1][1] * uy + adj[2][1] * uz);
-        const T w2 = sc * (adj[0][2] * ux + adj[1][2] * uy + adj[2][2] * uz);
-        vx[q] = adj[0][0] * w0 + adj[0][1] * w1 + adj[0][2] * w2;
-        vy[q] = adj[1][0] * w0 + adj[1][1] * w1 + adj[1][2] * w2;
-        vz[q] = adj[2][0] * w0 + adj[2][1] * w1 + adj[2][2] * w2;
+#pragma unroll
+        for (int q = 0; q < 5; ++q)
+        {
+          T ux = 0, uy = 0, uz = 0;
+#pragma unroll
+          for (int r = 0; r < 5; ++r)
+          {
+            ux += Tb::B(q, r) * cx[r];
+            uy += Tb::B(q, r) * cy[r];
+            uz += Tb::D(q, r) * c0[r];
+          }
+          const T Z = Tb::G(q);
+          T J[3][3];
+#pragma unroll
+          for (int comp = 0; comp < 3; ++comp)
+          {
+            J[comp][0] = P0[comp] + Z * dP[comp];
+            J[comp][1] = Q0[comp] + Z * dQ[comp];
+            J[comp][2] = R[comp];
+          }
+          T adj[3][3];
+          adj[0][0] = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+          adj[0][1] = J[0][2] * J[2][1] - J[0][1] * J[2][2];
+          adj[0][2] = J[0][1] * J[1][2] - J[0][2] * J[1][1];
+          adj[1][0] = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+          adj[1][1] = J[0][0] * J[2][2] - J[0][2] * J[2][0];
+          adj[1][2] = J[0][2] * J[1][0] - J[0][0] * J[1][2];
+          adj[2][0] = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+          adj[2][1] = J[0][1] * J[2][0] - J[0][0] * J[2][1];
+          adj[2][2] = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+          const T det = J[0][0] * adj[0][0] + J[0][1] * adj[1][0] + J[0][2] * adj[2][0];
+          // G grad = w kappa |det| K K^T grad = sc adj (adj^T grad), K = J^{-1} =
+          // adj / det, sc = w kappa / |det|.
+          const T sc = div_abs(qwl * Tb::W(q), det);
+          const T w0 = sc * (adj[0][0] * ux + adj[1][0] * uy + adj[2][0] * uz);
+          const T w1 = sc * (adj[0][1] * ux + adj[1][1] * uy + adj[2][1] * uz);
+          const T w2 = sc * (adj[0][2] * ux + adj[1][2] * uy + adj[2][2] * uz);
+          vx[q] = adj[0][0] * w0 + adj[0][1] * w1 + adj[0][2] * w2;
+          vy[q] = adj[1][0] * w0 + adj[1][1] * w1 + adj[1][2] * w2;
+          vz[q] = adj[2][0] * w0 + adj[2][1] * w1 + adj[2][2] * w2;
+        }
       }
 #pragma unroll
       for (int a = 0; a < 5; ++a)
@@ -1114,6 +1165,69 @@ __global__ void k_q4_edges(const dfx_q4_mesh_s m, float* __restrict__ edges, int
   edges[g] = (float)(coord(hi) - coord(lo));
 }
 
+// Geometric factors of every quadrature point, [cell][6][125]: the
+// Jacobian at the point from the cell's edge vectors (rounded once to T
+// from the FP64 vertices), G = w kappa adj adj^T / |det| in T, stored as
+// 00, 01, 02, 11, 12, 22. One thread per (cell, point); the formulas are
+// those of the colour kernel's phase 3.
+template <typename T>
+__global__ void k_q4_geom(const dfx_q4_mesh_s m, T* __restrict__ geom, int64_t cells)
+{
+  using Tb = Tab<T>;
+  const int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (g >= cells * 125)
+    return;
+  const int64_t cell = g / 125;
+  const int p = (int)(g % 125), la = p % 5, lb = (p / 5) % 5, q = p / 25;
+  const int64_t i = cell % m.nx, j = (cell / m.nx) % m.ny, k = cell / ((int64_t)m.nx * m.ny);
+  auto coord = [&](int v, int comp)
+  {
+    const int64_t vi = i + (v & 1), vj = j + ((v >> 1) & 1), vk = k + ((v >> 2) & 1);
+    return m.verts[3 * ((vk * (m.ny + 1) + vj) * (m.nx + 1) + vi) + comp];
+  };
+  const T X = Tb::G(la), Y = Tb::G(lb), Z = Tb::G(q);
+  T J[3][3];
+#pragma unroll
+  for (int comp = 0; comp < 3; ++comp)
+  {
+    T e[12];
+#pragma unroll
+    for (int ed = 0; ed < 12; ++ed)
+    {
+      const int lo = edge_lo(ed), hi = lo + (1 << (ed >> 2));
+      e[ed] = (T)(coord(hi, comp) - coord(lo, comp));
+    }
+    const T p0 = (1 - Y) * e[0] + Y * e[1], p1 = (1 - Y) * e[2] + Y * e[3];
+    const T q0 = (1 - X) * e[4] + X * e[5], q1 = (1 - X) * e[6] + X * e[7];
+    J[comp][0] = p0 + Z * (p1 - p0);
+    J[comp][1] = q0 + Z * (q1 - q0);
+    J[comp][2] = (1 - X) * (1 - Y) * e[8] + X * (1 - Y) * e[9] + (1 - X) * Y * e[10]
+                 + X * Y * e[11];
+  }
+  T adj[3][3];
+  adj[0][0] = J[1][1] * J[2][2] - J[1][2] * J[2][1];
+  adj[0][1] = J[0][2] * J[2][1] - J[0][1] * J[2][2];
+  adj[0][2] = J[0][1] * J[1][2] - J[0][2] * J[1][1];
+  adj[1][0] = J[1][2] * J[2][0] - J[1][0] * J[2][2];
+  adj[1][1] = J[0][0] * J[2][2] - J[0][2] * J[2][0];
+  adj[1][2] = J[0][2] * J[1][0] - J[0][0] * J[1][2];
+  adj[2][0] = J[1][0] * J[2][1] - J[1][1] * J[2][0];
+  adj[2][1] = J[0][1] * J[2][0] - J[0][0] * J[2][1];
+  adj[2][2] = J[0][0] * J[1][1] - J[0][1] * J[1][0];
+  const T det = J[0][0] * adj[0][0] + J[0][1] * adj[1][0] + J[0][2] * adj[2][0];
+  const T qwl = Tb::W(la) * Tb::W(lb) * (T)m.kappa;
+  const T sc = div_abs(qwl * Tb::W(q), det);
+  auto dot3 = [&](int a, int b)
+  { return sc * (adj[a][0] * adj[b][0] + adj[a][1] * adj[b][1] + adj[a][2] * adj[b][2]); };
+  T* o = geom + 750 * cell + p;
+  o[0] = dot3(0, 0);
+  o[125] = dot3(0, 1);
+  o[250] = dot3(0, 2);
+  o[375] = dot3(1, 1);
+  o[500] = dot3(1, 2);
+  o[625] = dot3(2, 2);
+}
+
 // Grid of the tensor-core colour kernel: 4 resident CTAs per SM, the
 // register bound of its launch bounds; 4 x (52 KB dynamic + 2 KB static +
 // 1 KB reserved) shared memory fits the SM's 228 KB. (The occupancy query
@@ -1131,14 +1245,15 @@ int q4_tc_grid_limit()
   return (ok ? 4 : 1) * dfx::num_sms();
 }
 
-// Resident CTAs per SM of the colour kernel (queried once per type).
-template <typename T>
+// Resident CTAs per SM of the colour kernel (queried once per type and
+// geometry source).
+template <typename T, bool GQ>
 int q4_grid_limit()
 {
   static int per_sm = 0;
   static std::once_flag once;
   std::call_once(once, [] {
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_q4_cells<T>, 128, 0)
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_q4_cells<T, GQ>, 128, 0)
         != cudaSuccess)
       per_sm = 1;
   });
@@ -1152,8 +1267,10 @@ int q4_prepare()
 {
   // Also settles the grid sizes, so that nothing below queries the device
   // during a stream capture.
-  q4_grid_limit<float>();
-  q4_grid_limit<double>();
+  q4_grid_limit<float, false>();
+  q4_grid_limit<double, false>();
+  q4_grid_limit<float, true>();
+  q4_grid_limit<double, true>();
   q4_tc_grid_limit();
   return upload_tables();
 }
@@ -1233,12 +1350,18 @@ int q4_apply(const dfx_q4_mesh_s& m, const T* u, T* y, cudaStream_t s, const int
     const int64_t cells = (int64_t)col.hx * col.hy * col.hz;
     if (cells == 0)
       continue;
-    const int64_t grid = std::min<int64_t>((cells + kBatch - 1) / kBatch, q4_grid_limit<T>());
+    const bool gq = sizeof(T) == 4 ? m.geom32 != nullptr : m.geom64 != nullptr;
+    const int64_t grid = std::min<int64_t>((cells + kBatch - 1) / kBatch,
+                                           gq ? q4_grid_limit<T, true>()
+                                              : q4_grid_limit<T, false>());
     const int64_t step = kBatch * grid;
     col.dx = (int)(step % col.hx);
     col.dy = (int)((step / col.hx) % col.hy);
     col.dz = (int)(step / ((int64_t)col.hx * col.hy));
-    k_q4_cells<T><<<(unsigned)grid, 128, 0, s>>>(m, u, y, col, skip);
+    if (gq)
+      k_q4_cells<T, true><<<(unsigned)grid, 128, 0, s>>>(m, u, y, col, skip);
+    else
+      k_q4_cells<T, false><<<(unsigned)grid, 128, 0, s>>>(m, u, y, col, skip);
   }
   DFX_CHECK_LAUNCH();
   return DFX_OK;
@@ -1261,6 +1384,28 @@ extern "C" int dfx_q4_edges(const dfx_q4_mesh* mesh, float* d_edges, void* strea
   const int64_t total = 36 * cells;
   k_q4_edges<<<(unsigned)((total + 255) / 256), 256, 0, dfx::as_stream(stream)>>>(*mesh, d_edges,
                                                                                    cells);
+  DFX_CHECK_LAUNCH();
+  return DFX_OK;
+}
+
+extern "C" int dfx_q4_geometry(const dfx_q4_mesh* mesh, int32_t dtype, void* d_geom,
+                               void* stream)
+{
+  DFX_REQUIRE(mesh && d_geom, "arguments must be non-NULL");
+  DFX_REQUIRE(mesh->nx > 0 && mesh->ny > 0 && mesh->nz > 0 && mesh->verts, "invalid Q4 mesh");
+  const int64_t cells = (int64_t)mesh->nx * mesh->ny * mesh->nz;
+  DFX_REQUIRE(cells < ((int64_t)1 << 31), "Q4 mesh too large (%lld cells)", (long long)cells);
+  // The quadrature tables live in constant memory, uploaded on first use.
+  if (int st = dfx::q4_prepare())
+    return st;
+  const unsigned grid = (unsigned)((125 * cells + 255) / 256);
+  cudaStream_t s = dfx::as_stream(stream);
+  if (dtype == DFX_F64)
+    k_q4_geom<double><<<grid, 256, 0, s>>>(*mesh, (double*)d_geom, cells);
+  else if (dtype == DFX_F32)
+    k_q4_geom<float><<<grid, 256, 0, s>>>(*mesh, (float*)d_geom, cells);
+  else
+    return dfx::fail(DFX_ERR_INVALID, "unknown dtype %d", dtype);
   DFX_CHECK_LAUNCH();
   return DFX_OK;
 }

@@ -90,10 +90,19 @@ class Q4Laplacian:
     identity rows on the boundary. Vertex coordinates stay resident in HBM."""
 
     def __init__(self, verts, nx: int, ny: int | None = None, nz: int | None = None,
-                 kappa: float = 1.0, device="cuda", cache_edges: bool = True):
+                 kappa: float = 1.0, device="cuda", cache_edges: bool = True,
+                 cache_geometry=(torch.float64,)):
         """cache_edges: keep the cells' FP32 edge vectors in HBM (36 floats
         per cell) for the FP32 action instead of forming them from the FP64
-        vertices in every application (same results, bitwise)."""
+        vertices in every application (same results, bitwise).
+        cache_geometry: the precisions (torch.float64, torch.float32) whose
+        action reads the geometric factor of every quadrature point from HBM
+        (750 values per cell: 6 KB in FP64, 3 KB in FP32) instead of forming
+        the Jacobian, its adjugate and determinant at each point; results
+        agree to rounding. FP64 only by default: at 64^3 cells the FP64
+        action took 6.56 ms against 10.07 ms (FP64-pipe bound), while the
+        FP32 action took 0.411 ms with the cache against 0.394 ms without
+        (its extra 786 MB cost more than the instructions it saves)."""
         ny = nx if ny is None else ny
         nz = nx if nz is None else nz
         v = torch.as_tensor(np.ascontiguousarray(verts, np.float64))
@@ -103,7 +112,8 @@ class Q4Laplacian:
         self.verts = v.to(device)
         self.dims = (nx, ny, nz)
         self.kappa = float(kappa)
-        self._mesh = _capi.Q4Mesh(nx, ny, nz, self.verts.data_ptr(), self.kappa, None)
+        self._mesh = _capi.Q4Mesh(nx, ny, nz, self.verts.data_ptr(), self.kappa, None, None,
+                                  None)
         self.n = int(_capi.lib().dfx_q4_num_dofs(C.byref(self._mesh)))
         self.edges = None
         if cache_edges:
@@ -111,6 +121,17 @@ class Q4Laplacian:
             _capi.check(_capi.lib().dfx_q4_edges(C.byref(self._mesh), _ptr(self.edges),
                                                  _stream()))
             self._mesh.edges32 = self.edges.data_ptr()
+        self.geom = {}
+        if cache_geometry is True:
+            cache_geometry = (torch.float64, torch.float32)
+        for dt, cdt, field in ((torch.float32, _capi.F32, "geom32"),
+                               (torch.float64, _capi.F64, "geom64")):
+            if cache_geometry and dt in tuple(cache_geometry):
+                g = torch.empty(750 * nx * ny * nz, dtype=dt, device=device)
+                _capi.check(_capi.lib().dfx_q4_geometry(C.byref(self._mesh), cdt, _ptr(g),
+                                                        _stream()))
+                self.geom[dt] = g
+                setattr(self._mesh, field, g.data_ptr())
 
     def mesh(self):
         return self._mesh

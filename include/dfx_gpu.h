@@ -720,12 +720,26 @@ typedef struct dfx_q4_mesh
    * 36 floats per cell, 16-byte aligned, written by dfx_q4_edges. Used by
    * the FP32 action only; results are bitwise the same either way. */
   const float* edges32;
+  /* Optional (NULL: formed on the fly): the geometric factor of every
+   * quadrature point, G = w kappa adj(J) adj(J)^T / |det J| (symmetric, 6
+   * values: 00, 01, 02, 11, 12, 22), written by dfx_q4_geometry. 750
+   * values per cell, [cell][6][125], point x + 5 y + 25 z, cells
+   * lexicographic. geom32 serves the FP32 action, geom64 the FP64 one; they
+   * agree with the on-the-fly path to the precision's rounding. No
+   * counterpart in the reference, which forms the geometry in every cell
+   * kernel call: a cache of 3 KB (FP32) or 6 KB (FP64) per cell. */
+  const float* geom32;
+  const double* geom64;
 } dfx_q4_mesh;
 
 int64_t dfx_q4_num_dofs(const dfx_q4_mesh* mesh);
 /* Writes the 36 * nx * ny * nz FP32 edge components of dfx_q4_mesh.edges32
  * (no counterpart in the reference: a cache of per-cell geometry). */
 int dfx_q4_edges(const dfx_q4_mesh* mesh, float* d_edges, void* stream);
+/* Writes the 750 * nx * ny * nz geometric factors of dfx_q4_mesh.geom32
+ * (dtype DFX_F32) or .geom64 (DFX_F64), computed in that precision from the
+ * edge vectors rounded once from the FP64 vertices. */
+int dfx_q4_geometry(const dfx_q4_mesh* mesh, int32_t dtype, void* d_geom, void* stream);
 /* y = A u; u, y of `dtype` (DFX_F64 or DFX_F32; FP32 forms the geometry
  * and contractions in FP32 from FP64 vertex differences). */
 int dfx_q4_action(const dfx_q4_mesh* mesh, int32_t dtype, const void* d_u, void* d_y,

@@ -81,6 +81,42 @@ def test_q4_tensor_core_cg(cuda):
         assert ((xs[mode] - xs["fp64"]).norm() / xs["fp64"].norm()).item() < 1e-8
 
 
+@pytest.mark.parametrize("dims", [(3, 3, 3), (1, 1, 1), (2, 3, 4), (5, 4, 3)])
+def test_q4_geometry_cache_matches_oracle(cuda, oracle, dims):
+    """Actions on the cached geometric factors (dfx_q4_geometry) against the
+    oracle's full-quadrature element loop (FP64 to 1e-12, FP32 to 2e-5) and
+    against the actions that form the geometry on the fly; the mixed CG on
+    them meets the FP64 stopping test."""
+    from dolfinx_gb300 import matrix_free as mf
+
+    v = mf.hex_box_vertices(*dims, perturb=0.05, seed=21)
+    op = mf.Q4Laplacian(v, *dims, kappa=1.7, cache_geometry=True)
+    plain = mf.Q4Laplacian(v, *dims, kappa=1.7, cache_geometry=False)
+    assert set(op.geom) == {torch.float32, torch.float64}
+    assert op.geom[torch.float32].numel() == 750 * int(np.prod(dims))
+    # G = w kappa adj adj^T / |det J| is positive definite: its diagonal
+    # (entries 00, 11, 22 of each point) is positive everywhere.
+    for g in op.geom.values():
+        diag = g.view(-1, 6, 125)[:, [0, 3, 5], :]
+        assert bool((diag > 0).all())
+    u = np.random.default_rng(22).standard_normal(op.n)
+    ref = oracle.q4_action(dims, v, u, kappa=1.7)
+    u64 = torch.from_numpy(u).cuda()
+    y64 = op(u64)
+    assert_close(y64.cpu().numpy(), ref, rtol=1e-12)
+    assert_close(y64.cpu().numpy(), plain(u64).cpu().numpy(), rtol=1e-13)
+    y32 = op(u64.float()).double().cpu().numpy()
+    assert_close(y32, ref, rtol=2e-5)
+    assert_close(y32, plain(u64.float()).double().cpu().numpy(), rtol=5e-6)
+    if min(dims) >= 3:
+        bnd = torch.from_numpy(mf.boundary_mask(*dims)).cuda()
+        b = u64.masked_fill(bnd, 0)
+        x = torch.zeros_like(b)
+        r = mf.MatrixFreeCG(op, mode="mixed").solve(b, x, rtol=1e-10)
+        assert r.status == 0
+        assert ((b - plain(x)).norm() / b.norm()).item() < 1e-10 * 1.001
+
+
 def test_q4_edge_cache_is_bitwise_neutral(cuda):
     from dolfinx_gb300 import matrix_free as mf
 

@@ -560,7 +560,8 @@ _STRUCTS = {
                                "rnorm0_sq", "rnorm_sq", "kernel_launches"]),
     "BatchSystem": ("dfx_batch_system", ["op32", "op64", "b", "x", "dinv", "work", "rtol",
                                          "delta", "max_iters", "mode"]),
-    "Q4Mesh": ("dfx_q4_mesh", ["nx", "ny", "nz", "verts", "kappa", "edges32"]),
+    "Q4Mesh": ("dfx_q4_mesh", ["nx", "ny", "nz", "verts", "kappa", "edges32", "geom32",
+                               "geom64"]),
 }
 
 
