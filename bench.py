@@ -494,11 +494,14 @@ def elasticity_sample(steps=1, warmup=1):
     out["roofline_spmv"] = {
         name: {"bound": bound, "alg_bytes_per_launch": alg, "launch_ms": ms,
                "achieved": alg / (ms * 1e-3) / 1e9, "peak": peak, "unit": "GB/s",
-               "frac": alg / (ms * 1e-3) / 1e9 / peak, "peak_source": peak_kind}
-        for name, bound, ms in (("split_fp32_words", "hbm", out["spmv_ms"]["split_fp32_words"]),
-                                ("fp64", f"fp64 pipe ({9 * A.nnz / 1e6:.1f}M FMAs at 2 per "
-                                         "clock per SM)",
-                                 out["spmv_ms"]["fp64"]))}
+               "frac": alg / (ms * 1e-3) / 1e9 / peak, "peak_source": peak_kind,
+               "traffic": profile_traffic(key)}
+        for name, key, bound, ms in (("split_fp32_words", "bsell_split_elasticity_96x24x24",
+                                      "hbm", out["spmv_ms"]["split_fp32_words"]),
+                                     ("fp64", "bsell_f64_elasticity_96x24x24",
+                                      f"fp64 pipe ({9 * A.nnz / 1e6:.1f}M FMAs at 2 per "
+                                      "clock per SM)",
+                                      out["spmv_ms"]["fp64"]))}
     return out
 
 
